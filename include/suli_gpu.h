@@ -1,0 +1,217 @@
+/*
+ * suli_gpu.h -- C ABI of the GB300 (sm_103a) implementation of SuLi-IC's
+ * per-time-step hot path.
+ *
+ * SuLi's hot routines are argument-less Fortran subroutines that talk through
+ * module globals (SuLi-IC/0_modules.f90:2-325) and are called from the time
+ * loop in SuLi-IC/1_principal.f90:69-124.  This header replaces each of them
+ * with one entry point that acts on a device-resident case held by a handle.
+ * A Fortran shim (ISO_C_BINDING, shown in INTEGRATION.md) keeps the original
+ * subroutine names so the time loop is unchanged.
+ *
+ * Conventions
+ *   - Every entry point returns an int status: 0 = SULI_OK, >0 an error or
+ *     warning code (below).  suli_last_error() gives the text of the last one.
+ *   - Host arrays crossing the boundary use the reference's own layout:
+ *     Fortran column-major, i (x) fastest, with the reference's lower bounds
+ *     (e.g. u is (0:nx+2, 0:ny+1, 0:nz+1)); suli_field_shape() reports the
+ *     bounds of every field id.
+ *   - Ownership: after suli_upload_field() the device owns the data; host
+ *     arrays are only read/written during the call.
+ *   - Threading: one host thread per handle; not re-entrant.
+ *   - There is no CPU fallback: a handle cannot be created without a CUDA
+ *     device and a missing device is reported as SULI_NO_DEVICE.
+ */
+#ifndef SULI_GPU_H
+#define SULI_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define SULI_OK              0
+#define SULI_CG_MAXITER      1  /* warning: "pulou pressao", 9_grad.f90:590 */
+#define SULI_VOL_LOOP_CAP    2  /* volume-correction loop capped, 14_level_set.f90:243 */
+#define SULI_DEVICE_TIMEOUT  3  /* a bounded device wait gave up */
+#define SULI_BAD_CONFIG      4  /* replaces the reference's STOPs */
+#define SULI_BAD_ARG         5
+#define SULI_CUDA_ERROR      6
+#define SULI_NO_DEVICE       7
+#define SULI_OUT_OF_MEMORY   8
+
+/* ---- precision of a case ----------------------------------------------- */
+#define SULI_PREC_FP64   0  /* plain form: FP64 storage and arithmetic */
+#define SULI_PREC_MIXED  1  /* FP32 storage/stencils, FP64 refinement + sums */
+
+/* ---- CG stopping rule --------------------------------------------------- */
+#define SULI_CG_TOL_ABS  0  /* reference rule: r.r > cg_tol/(nx*ny*nz), 9_grad.f90:393 */
+#define SULI_CG_TOL_REL  1  /* norm(r) > cg_tol norm(b), scaled system, b = q / sqrt(D) */
+
+/*
+ * suli_params mirrors the module variables the hot path reads
+ * (0_modules.f90 disc/cond/param/les/ls_param, read by parametros()
+ * 2_iniciais.f90:11-123).  The trailing block holds the build's own
+ * knobs, each defaulting to the reference behaviour when zero-filled
+ * through suli_default_params().
+ */
+typedef struct suli_params {
+    int32_t nx, ny, nz;            /* cells */
+    double  dx, dy, dz;            /* m */
+    double  dt;                    /* dt0, s */
+    int32_t t_tempo;               /* 0 Euler, 1 RK2, 2 RK3, 3 AB2, 4 AB3 */
+    int32_t der;                   /* 3 = 2nd-order upwind (only one supported) */
+    int32_t adv_type;              /* 1 = classical advective form */
+    int32_t ibm_t;                 /* 0 none, 2 image-point IBM */
+    int32_t obst_t;                /* 0 none, nonzero: obstacle fields uploaded */
+    int32_t m_turb;                /* 0 none, 1 Smagorinsky */
+    int32_t t_press;               /* 1 projection */
+    int32_t mms_t;                 /* 0 none, 1 steady MMS source */
+    int32_t ccx0, ccxf, ccy0, ccyf, ccz0, cczf;  /* 0 periodic,1 free-slip,2 no-slip,3 prescribed,4 outflow(xf) */
+    double  gx, gz;                /* gravity components (reference: 9.80665*sin/cos(atan(decliv))) */
+    double  csmag;                 /* Smagorinsky constant */
+    double  alpha1;                /* interface half-width in cells */
+    double  rho_f1, mu_f1;         /* fluid where ls < 0 (air) */
+    double  rho_f2, mu_f2;         /* fluid where ls > 0 (water) */
+    double  uinicial, iturb;       /* inflow speed and perturbation for ccx0 = 3 */
+    int32_t omp_t;                 /* reference CG reduction mode; no effect on the GPU */
+    /* ---- build-specific knobs ---- */
+    int32_t reinit_max_iter;       /* reference: 3 (14_level_set.f90:389) */
+    int32_t cg_max_iter;           /* reference: 10000 (9_grad.f90:398) */
+    int32_t cg_tol_mode;           /* SULI_CG_TOL_ABS (reference) or SULI_CG_TOL_REL */
+    double  cg_tol;                /* reference: 1e-4 with SULI_CG_TOL_ABS */
+    int32_t precision;             /* SULI_PREC_FP64 or SULI_PREC_MIXED */
+    int32_t project_under_mms;     /* 1: run graddin/posdin/contorno(1) even when mms_t>0 */
+    int32_t vol_loop_max;          /* cap of the volume-correction loop (reference: none) */
+    int32_t mixed_inner_iters;     /* FP32 CG iterations per FP64 refinement pass */
+    uint64_t seed;                 /* counter-based RNG seed for the inflow perturbation */
+} suli_params;
+
+/* ---- field ids (reference module arrays) -------------------------------- */
+enum suli_field {
+    SULI_F_U = 0,    /* u   (0:nx1+1, 0:ny+1, 0:nz+1)  velpre */
+    SULI_F_V,        /* v   (0:nx+1, 0:ny1+1, 0:nz+1) */
+    SULI_F_W,        /* w   (0:nx+1, 0:ny+1, 0:nz1+1) */
+    SULI_F_PRD1,     /* prd1 (0:nx+1, 0:ny+1, 0:nz+1) */
+    SULI_F_PRD,      /* prd  (0:nx+1, 0:ny+1, 0:nz+1) */
+    SULI_F_LS,       /* ls   (nx, ny, nz)  ls_param */
+    SULI_F_HS,       /* hs   (nx, ny, nz) */
+    SULI_F_RHO,      /* rho  (nx, ny, nz) */
+    SULI_F_LS_MU,    /* ls_mu (nx, ny, nz) */
+    SULI_F_MU,       /* mu   (nx, ny, nz)  les */
+    SULI_F_MUT,      /* mut  (nx, ny, nz) */
+    SULI_F_XMU,      /* xmu  (nx1, ny, nz) */
+    SULI_F_YMU,      /* ymu  (nx, ny1, nz) */
+    SULI_F_ZMU,      /* zmu  (nx, ny, nz1) */
+    SULI_F_FU,       /* Fu   (nx1, ny, nz)  vartempo */
+    SULI_F_FV,       /* Fv   (nx, ny1, nz) */
+    SULI_F_FW,       /* Fw   (nx, ny, nz1) */
+    SULI_F_U0, SULI_F_V0, SULI_F_W0,
+    SULI_F_FU0, SULI_F_FV0, SULI_F_FW0,
+    SULI_F_FU1, SULI_F_FV1, SULI_F_FW1,
+    SULI_F_DIV,      /* div  (nx, ny, nz) */
+    SULI_F_TF_U, SULI_F_TF_V, SULI_F_TF_W,   /* MMS sources, mms_m */
+    SULI_F_OBS_LSX,  /* obs_lsx (nx1, ny, nz)  obst */
+    SULI_F_OBS_LSY,  /* obs_lsy (nx, ny1, nz) */
+    SULI_F_OBS_LSZ,  /* obs_lsz (nx, ny, nz1) */
+    SULI_F_OBS_LSS,  /* obs_lss (nx, ny, nz) */
+    SULI_F_ID_IBMX,  /* id_ibmx (nx1, ny, nz), int32 */
+    SULI_F_ID_IBMY,
+    SULI_F_ID_IBMZ,
+    SULI_F_ID_IBM,   /* id_ibm (nx, ny, nz), int32 */
+    SULI_F_BXX0,     /* bxx0 (0:ny+1, 0:nz+1) inflow u at i = 0 */
+    SULI_F_BXX1,     /* bxx1 (0:ny+1, 0:nz+1) inflow u at i = 1 */
+    SULI_F_BLX1,     /* blx1 (ny, nz) inflow ls at i = 1 */
+    SULI_F_COUNT
+};
+
+/* ---- scalar ids ---------------------------------------------------------- */
+enum suli_scalar {
+    SULI_S_T = 0,      /* simulated time t */
+    SULI_S_DT,         /* current (stage) dt */
+    SULI_S_VOL_INI,
+    SULI_S_VOL_INS,
+    SULI_S_MAXDIV,     /* maxval(abs(div)) of the last suli_conmassa */
+    SULI_S_IT,         /* time-step counter (as double) */
+    SULI_S_TT,         /* RK stage (as double) */
+    SULI_S_COUNT
+};
+
+typedef struct suli_diag {
+    double  vol_ini, vol_ins, maxdiv, t;
+    double  cg_res[3];          /* final CG r.r (scaled system) per RK stage */
+    int32_t cg_iters[3];        /* CG iterations per RK stage of the last step */
+    int32_t cg_outer[3];        /* mixed form: FP64 refinement passes per stage */
+    int32_t reinit_iters;       /* reinit iterations (il) of the last level_set */
+    int32_t vol_loops;          /* volume-correction passes of the last level_set */
+    int32_t it;
+    int32_t status_flags;       /* OR of warnings seen since the last read */
+} suli_diag;
+
+typedef struct suli_handle suli_handle;
+
+/* Zero-fill + reference defaults (reinit 3, cg 10000, abs tol 1e-4, FP64). */
+void suli_default_params(suli_params *p);
+
+/* Extents of field f for params p, as Fortran lower/upper bounds. */
+int suli_field_shape(const suli_params *p, int field, int lo[3], int hi[3]);
+
+/* Replaces parametros()/init_variables1..7 (2_iniciais.f90:11-123,
+ * 0_modules.f90:121-347): validates p and allocates one device case. */
+int suli_create(const suli_params *p, suli_handle **out);
+/* A batch of independent cases advanced in lockstep by the same launches
+ * (uneven grids allowed; the scheme flags and precision must match). */
+int suli_create_batch(const suli_params *p, int ncases, suli_handle **out);
+int suli_num_cases(const suli_handle *h, int *ncases);
+int suli_destroy(suli_handle *h);
+
+/* Host <-> device copies of one field of case icase in the reference layout.
+ * int32 for id_ibm*, double otherwise (the mixed form converts). */
+int suli_upload_field(suli_handle *h, int icase, int field, const void *host);
+int suli_download_field(suli_handle *h, int icase, int field, void *host);
+int suli_set_scalar(suli_handle *h, int icase, int scalar, double value);
+int suli_get_scalar(suli_handle *h, int icase, int scalar, double *value);
+
+/* Parity runs: replay the CG iteration count of each RK stage and the
+ * reinitialisation count of a reference run (-1 = free running). */
+int suli_set_replay(suli_handle *h, const int32_t cg_iters[3], int32_t reinit_iters);
+
+/* heaviside() 14_level_set.f90:508-594 plus the vol_ini sum of
+ * level_set_ini() :187-194; call once after uploading ls. */
+int suli_heaviside_init(suli_handle *h);
+
+/* One entry point per reference subroutine. */
+int suli_level_set(suli_handle *h);              /* 14_level_set.f90:204-273 */
+int suli_contorno(suli_handle *h, int nlock);    /* 3_contorno.f90:11-662 */
+int suli_visco(suli_handle *h);                  /* 5_viscosidade.f90:11-157 */
+int suli_convdiff(suli_handle *h);               /* 6_convdiff.f90:14-167 */
+int suli_complementos(suli_handle *h);           /* 11_diversos.f90:355-450 */
+int suli_tempo(suli_handle *h);                  /* 11_diversos.f90:10-296 (uses stage tt, dt) */
+int suli_graddin(suli_handle *h, int32_t *iters_out); /* 9_grad.f90:10-663 */
+int suli_posdin(suli_handle *h);                 /* 10_pos.f90:1-99 */
+int suli_conmassa(suli_handle *h, double *maxdiv_out); /* 4_plot.f90:386-394 */
+int suli_mms_error(suli_handle *h, double err_out[4]); /* 13_mms.f90:391-451 */
+/* Sets tt (1..ntt) and dt = a_dt(tt), as the RK loop of 1_principal.f90:86-87. */
+int suli_set_stage(suli_handle *h, int tt);
+
+/* The whole time step of 1_principal.f90:69-124 (without PLOT output),
+ * nsteps times; captured once into a CUDA graph and replayed. */
+int suli_step(suli_handle *h, int nsteps);
+
+int suli_diagnostics(suli_handle *h, int icase, suli_diag *out);
+int suli_synchronize(suli_handle *h);
+
+/* Text of the last error on this thread (empty if none). */
+int suli_last_error(char *buf, size_t len);
+
+/* Device/runtime info for reports: SM count, clock, name. */
+int suli_device_info(int *sm_count, char *name, size_t name_len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SULI_GPU_H */

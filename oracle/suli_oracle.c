@@ -1,0 +1,1776 @@
+/*
+ * suli_oracle.c -- CPU oracle (test infrastructure) for the SuLi-IC hot path.
+ *
+ * FP64 restatement of the reference Fortran, keeping each routine's loop
+ * order, the order of every floating-point expression (left to right, as
+ * Fortran evaluates it) and the halo/corner assignment order, so that a
+ * compiled run (gcc -O3 -ffp-contract=off) reproduces the reference
+ * arithmetic.  Citations are file:line into SuLi-IC/ of lacia-udesc/SuLi.
+ *
+ * Parity: unpinned against outputs of the reference itself (no tests or
+ * golden vectors exist upstream and no Fortran compiler is available);
+ * pinned by analytic known-answer tests instead (see suli_oracle.h).
+ *
+ * OpenMP is used exactly where the reference uses it: the CG of 9_grad.f90
+ * (parallel loops; reductions only with omp_t = 1) and the interp*_cf
+ * helpers of 8_derivadas.f90.  Everything else is serial as upstream.
+ */
+#include "suli_oracle.h"
+
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Arrays with Fortran bounds                                                */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    double *p;
+    int lo[3], hi[3];
+    long s1, s2;          /* strides of j and k */
+} F3;
+
+typedef struct {
+    int *p;
+    int lo[3], hi[3];
+    long s1, s2;
+} I3;
+
+#define IDX(a, i, j, k) ((long)((i) - (a).lo[0]) + (long)((j) - (a).lo[1]) * (a).s1 + (long)((k) - (a).lo[2]) * (a).s2)
+#define A(a, i, j, k) ((a).p[IDX(a, i, j, k)])
+
+static void f3_init(F3 *a, int l0, int h0, int l1, int h1, int l2, int h2)
+{
+    a->lo[0] = l0; a->hi[0] = h0;
+    a->lo[1] = l1; a->hi[1] = h1;
+    a->lo[2] = l2; a->hi[2] = h2;
+    a->s1 = (long)(h0 - l0 + 1);
+    a->s2 = a->s1 * (long)(h1 - l1 + 1);
+    long n = a->s2 * (long)(h2 - l2 + 1);
+    a->p = (double *)calloc((size_t)n, sizeof(double));
+}
+
+static void i3_init(I3 *a, int l0, int h0, int l1, int h1, int l2, int h2)
+{
+    a->lo[0] = l0; a->hi[0] = h0;
+    a->lo[1] = l1; a->hi[1] = h1;
+    a->lo[2] = l2; a->hi[2] = h2;
+    a->s1 = (long)(h0 - l0 + 1);
+    a->s2 = a->s1 * (long)(h1 - l1 + 1);
+    long n = a->s2 * (long)(h2 - l2 + 1);
+    a->p = (int *)calloc((size_t)n, sizeof(int));
+}
+
+static long f3_size(const F3 *a) { return a->s2 * (long)(a->hi[2] - a->lo[2] + 1); }
+
+/* temporaries: allocate / free */
+static F3 tmp3(int l0, int h0, int l1, int h1, int l2, int h2)
+{
+    F3 a;
+    f3_init(&a, l0, h0, l1, h1, l2, h2);
+    return a;
+}
+static void fr(F3 *a) { free(a->p); a->p = NULL; }
+
+static void f3_copy(F3 *dst, const F3 *src) { memcpy(dst->p, src->p, (size_t)f3_size(src) * sizeof(double)); }
+
+/* ------------------------------------------------------------------------ */
+/* Case state: the module globals of 0_modules.f90 that the hot path uses    */
+/* ------------------------------------------------------------------------ */
+struct or_case {
+    suli_params p;
+    int nx, ny, nz, nx1, ny1, nz1;
+    double dx, dy, dz, dt, dt0, t, pi;
+    int it, tt, ntt;
+    double a_dt[3];
+    double dx1, dt1, deltai;
+    double vol_ini, vol_ins;
+    double adtl[3], bdtl[3], gdtl[3];
+    double maxdiv;
+
+    F3 u, v, w, prd1, prd, ls, hs, rho, ls_mu, mu, mut, xmu, ymu, zmu;
+    F3 Fu, Fv, Fw, u0, v0, w0, fu0, fv0, fw0, fu1, fv1, fw1, div;
+    F3 tf_u, tf_v, tf_w;
+    F3 obs_lsx, obs_lsy, obs_lsz, obs_lss;
+    I3 id_ibmx, id_ibmy, id_ibmz, id_ibm;
+    F3 bxx0, bxx1, blx1;
+
+    int cg_iters[3];
+    double cg_res[3];
+    int reinit_iters, vol_loops;
+    int replay_cg[3], replay_reinit;
+    unsigned long long rng_counter;
+};
+
+static int g_threads = 0;
+void or_set_threads(int n) { g_threads = n; }
+
+/* ------------------------------------------------------------------------ */
+/* Creation                                                                 */
+/* ------------------------------------------------------------------------ */
+or_case *or_create(const suli_params *pp)
+{
+    or_case *c = (or_case *)calloc(1, sizeof(or_case));
+    c->p = *pp;
+    int nx = pp->nx, ny = pp->ny, nz = pp->nz;
+    c->nx = nx; c->ny = ny; c->nz = nz;
+    c->nx1 = nx + 1; c->ny1 = ny + 1; c->nz1 = nz + 1;
+    c->dx = pp->dx; c->dy = pp->dy; c->dz = pp->dz;
+    c->dt0 = pp->dt; c->dt = pp->dt;
+    c->pi = acos(-1.0);               /* 0_modules.f90:5 */
+    c->t = 0.0; c->it = 0; c->tt = 1;
+    int nx1 = c->nx1, ny1 = c->ny1, nz1 = c->nz1;
+
+    /* 0_modules.f90:170-191 (velpre), :214-227 (vartempo), :273-277 (les), :304 (ls_param) */
+    f3_init(&c->u, 0, nx1 + 1, 0, ny + 1, 0, nz + 1);
+    f3_init(&c->v, 0, nx + 1, 0, ny1 + 1, 0, nz + 1);
+    f3_init(&c->w, 0, nx + 1, 0, ny + 1, 0, nz1 + 1);
+    f3_init(&c->prd1, 0, nx + 1, 0, ny + 1, 0, nz + 1);
+    f3_init(&c->prd, 0, nx + 1, 0, ny + 1, 0, nz + 1);
+    f3_init(&c->ls, 1, nx, 1, ny, 1, nz);
+    f3_init(&c->hs, 1, nx, 1, ny, 1, nz);
+    f3_init(&c->rho, 1, nx, 1, ny, 1, nz);
+    f3_init(&c->ls_mu, 1, nx, 1, ny, 1, nz);
+    f3_init(&c->mu, 1, nx, 1, ny, 1, nz);
+    f3_init(&c->mut, 1, nx, 1, ny, 1, nz);
+    f3_init(&c->div, 1, nx, 1, ny, 1, nz);
+    f3_init(&c->xmu, 1, nx1, 1, ny, 1, nz);
+    f3_init(&c->ymu, 1, nx, 1, ny1, 1, nz);
+    f3_init(&c->zmu, 1, nx, 1, ny, 1, nz1);
+    F3 *fx[] = {&c->Fu, &c->u0, &c->fu0, &c->fu1, &c->tf_u, &c->obs_lsx};
+    for (int q = 0; q < 6; ++q) f3_init(fx[q], 1, nx1, 1, ny, 1, nz);
+    F3 *fy[] = {&c->Fv, &c->v0, &c->fv0, &c->fv1, &c->tf_v, &c->obs_lsy};
+    for (int q = 0; q < 6; ++q) f3_init(fy[q], 1, nx, 1, ny1, 1, nz);
+    F3 *fz[] = {&c->Fw, &c->w0, &c->fw0, &c->fw1, &c->tf_w, &c->obs_lsz};
+    for (int q = 0; q < 6; ++q) f3_init(fz[q], 1, nx, 1, ny, 1, nz1);
+    f3_init(&c->obs_lss, 1, nx, 1, ny, 1, nz);
+    i3_init(&c->id_ibmx, 1, nx1, 1, ny, 1, nz);
+    i3_init(&c->id_ibmy, 1, nx, 1, ny1, 1, nz);
+    i3_init(&c->id_ibmz, 1, nx, 1, ny, 1, nz1);
+    i3_init(&c->id_ibm, 1, nx, 1, ny, 1, nz);
+    f3_init(&c->bxx0, 0, ny + 1, 0, nz + 1, 0, 0);
+    f3_init(&c->bxx1, 0, ny + 1, 0, nz + 1, 0, 0);
+    f3_init(&c->blx1, 1, ny, 1, nz, 0, 0);
+
+    /* level_set_ini coefficients, 14_level_set.f90:29-42 */
+    c->adtl[0] = 1.;      c->bdtl[0] = 0.;      c->gdtl[0] = 1.;
+    c->adtl[1] = 3. / 4.; c->bdtl[1] = 1. / 4.; c->gdtl[1] = 1. / 4.;
+    c->adtl[2] = 1. / 3.; c->bdtl[2] = 2. / 3.; c->gdtl[2] = 2. / 3.;
+    double dmax = c->dx;
+    if (c->dy > dmax) dmax = c->dy;
+    if (c->dz > dmax) dmax = c->dz;
+    c->dx1 = dmax;
+    c->dt1 = 0.1 * c->dx1;
+    c->deltai = pow(c->dx * c->dy * c->dz, 1. / 3.);   /* 2_iniciais.f90:113 */
+
+    /* coef_tempo, 2_iniciais.f90:278-312 */
+    int tt_ = pp->t_tempo;
+    if (tt_ == 1 || tt_ == 2) {
+        c->ntt = (tt_ == 1) ? 2 : 3;
+        c->a_dt[0] = 0.5 * c->dt; c->a_dt[1] = 1.0 * c->dt; c->a_dt[2] = 1.0 * c->dt;
+    } else {
+        c->ntt = 1;
+        c->a_dt[0] = c->a_dt[1] = c->a_dt[2] = 1.0 * c->dt;
+    }
+    c->replay_cg[0] = c->replay_cg[1] = c->replay_cg[2] = -1;
+    c->replay_reinit = -1;
+    return c;
+}
+
+void or_destroy(or_case *c)
+{
+    if (!c) return;
+    F3 *all[] = {&c->u, &c->v, &c->w, &c->prd1, &c->prd, &c->ls, &c->hs, &c->rho, &c->ls_mu,
+                 &c->mu, &c->mut, &c->xmu, &c->ymu, &c->zmu, &c->Fu, &c->Fv, &c->Fw, &c->u0,
+                 &c->v0, &c->w0, &c->fu0, &c->fv0, &c->fw0, &c->fu1, &c->fv1, &c->fw1, &c->div,
+                 &c->tf_u, &c->tf_v, &c->tf_w, &c->obs_lsx, &c->obs_lsy, &c->obs_lsz,
+                 &c->obs_lss, &c->bxx0, &c->bxx1, &c->blx1};
+    for (unsigned q = 0; q < sizeof(all) / sizeof(all[0]); ++q) free(all[q]->p);
+    free(c->id_ibmx.p); free(c->id_ibmy.p); free(c->id_ibmz.p); free(c->id_ibm.p);
+    free(c);
+}
+
+void *or_field(or_case *c, int f, int lo[3], int hi[3])
+{
+    F3 *a = NULL;
+    I3 *ia = NULL;
+    switch (f) {
+    case SULI_F_U: a = &c->u; break;
+    case SULI_F_V: a = &c->v; break;
+    case SULI_F_W: a = &c->w; break;
+    case SULI_F_PRD1: a = &c->prd1; break;
+    case SULI_F_PRD: a = &c->prd; break;
+    case SULI_F_LS: a = &c->ls; break;
+    case SULI_F_HS: a = &c->hs; break;
+    case SULI_F_RHO: a = &c->rho; break;
+    case SULI_F_LS_MU: a = &c->ls_mu; break;
+    case SULI_F_MU: a = &c->mu; break;
+    case SULI_F_MUT: a = &c->mut; break;
+    case SULI_F_XMU: a = &c->xmu; break;
+    case SULI_F_YMU: a = &c->ymu; break;
+    case SULI_F_ZMU: a = &c->zmu; break;
+    case SULI_F_FU: a = &c->Fu; break;
+    case SULI_F_FV: a = &c->Fv; break;
+    case SULI_F_FW: a = &c->Fw; break;
+    case SULI_F_U0: a = &c->u0; break;
+    case SULI_F_V0: a = &c->v0; break;
+    case SULI_F_W0: a = &c->w0; break;
+    case SULI_F_FU0: a = &c->fu0; break;
+    case SULI_F_FV0: a = &c->fv0; break;
+    case SULI_F_FW0: a = &c->fw0; break;
+    case SULI_F_FU1: a = &c->fu1; break;
+    case SULI_F_FV1: a = &c->fv1; break;
+    case SULI_F_FW1: a = &c->fw1; break;
+    case SULI_F_DIV: a = &c->div; break;
+    case SULI_F_TF_U: a = &c->tf_u; break;
+    case SULI_F_TF_V: a = &c->tf_v; break;
+    case SULI_F_TF_W: a = &c->tf_w; break;
+    case SULI_F_OBS_LSX: a = &c->obs_lsx; break;
+    case SULI_F_OBS_LSY: a = &c->obs_lsy; break;
+    case SULI_F_OBS_LSZ: a = &c->obs_lsz; break;
+    case SULI_F_OBS_LSS: a = &c->obs_lss; break;
+    case SULI_F_ID_IBMX: ia = &c->id_ibmx; break;
+    case SULI_F_ID_IBMY: ia = &c->id_ibmy; break;
+    case SULI_F_ID_IBMZ: ia = &c->id_ibmz; break;
+    case SULI_F_ID_IBM: ia = &c->id_ibm; break;
+    case SULI_F_BXX0: a = &c->bxx0; break;
+    case SULI_F_BXX1: a = &c->bxx1; break;
+    case SULI_F_BLX1: a = &c->blx1; break;
+    default: return NULL;
+    }
+    if (a) {
+        for (int d = 0; d < 3; ++d) { lo[d] = a->lo[d]; hi[d] = a->hi[d]; }
+        return a->p;
+    }
+    for (int d = 0; d < 3; ++d) { lo[d] = ia->lo[d]; hi[d] = ia->hi[d]; }
+    return ia->p;
+}
+
+int or_set_scalar(or_case *c, int s, double v)
+{
+    switch (s) {
+    case SULI_S_T: c->t = v; return 0;
+    case SULI_S_DT: c->dt = v; return 0;
+    case SULI_S_VOL_INI: c->vol_ini = v; return 0;
+    case SULI_S_VOL_INS: c->vol_ins = v; return 0;
+    case SULI_S_IT: c->it = (int)v; return 0;
+    case SULI_S_TT: c->tt = (int)v; return 0;
+    default: return 1;
+    }
+}
+
+double or_get_scalar(or_case *c, int s)
+{
+    switch (s) {
+    case SULI_S_T: return c->t;
+    case SULI_S_DT: return c->dt;
+    case SULI_S_VOL_INI: return c->vol_ini;
+    case SULI_S_VOL_INS: return c->vol_ins;
+    case SULI_S_MAXDIV: return c->maxdiv;
+    case SULI_S_IT: return (double)c->it;
+    case SULI_S_TT: return (double)c->tt;
+    default: return 0.0;
+    }
+}
+
+void or_set_replay(or_case *c, const int cg[3], int reinit)
+{
+    for (int q = 0; q < 3; ++q) c->replay_cg[q] = cg ? cg[q] : -1;
+    c->replay_reinit = reinit;
+}
+
+void or_diag(or_case *c, suli_diag *d)
+{
+    memset(d, 0, sizeof(*d));
+    d->vol_ini = c->vol_ini; d->vol_ins = c->vol_ins; d->maxdiv = c->maxdiv; d->t = c->t;
+    for (int q = 0; q < 3; ++q) { d->cg_iters[q] = c->cg_iters[q]; d->cg_res[q] = c->cg_res[q]; }
+    d->reinit_iters = c->reinit_iters;
+    d->vol_loops = c->vol_loops;
+    d->it = c->it;
+}
+
+/* ------------------------------------------------------------------------ */
+/* 8_derivadas.f90: interpolations                                          */
+/* ------------------------------------------------------------------------ */
+/* interpx_cf: (dimx,dimy,dimz) centres -> (dimx+1,dimy,dimz) faces, :305-355 */
+static void interpx_cf(const or_case *c, const F3 *a, int dimx, int dimy, int dimz, F3 *o)
+{
+#pragma omp parallel for schedule(static)
+    for (int k = 1; k <= dimz; ++k)
+        for (int j = 1; j <= dimy; ++j)
+            for (int i = 2; i <= dimx; ++i)
+                A(*o, i, j, k) = (A(*a, i, j, k) + A(*a, i - 1, j, k)) * 0.5;
+    if (c->p.ccx0 != 0) {
+#pragma omp parallel for schedule(static)
+        for (int k = 1; k <= dimz; ++k)
+            for (int j = 1; j <= dimy; ++j) {
+                A(*o, 1, j, k) = A(*o, 2, j, k);
+                A(*o, dimx + 1, j, k) = A(*o, dimx, j, k);
+            }
+    } else {
+#pragma omp parallel for schedule(static)
+        for (int k = 1; k <= dimz; ++k)
+            for (int j = 1; j <= dimy; ++j) {
+                A(*o, 1, j, k) = (A(*a, 1, j, k) + A(*a, dimx, j, k)) * 0.5;
+                A(*o, dimx + 1, j, k) = (A(*a, 1, j, k) + A(*a, dimx, j, k)) * 0.5;
+            }
+    }
+}
+
+/* interpy_cf, :381-416 (no periodic branch upstream) */
+static void interpy_cf(const F3 *a, int dimx, int dimy, int dimz, F3 *o)
+{
+#pragma omp parallel for schedule(static)
+    for (int k = 1; k <= dimz; ++k)
+        for (int j = 2; j <= dimy; ++j)
+            for (int i = 1; i <= dimx; ++i)
+                A(*o, i, j, k) = (A(*a, i, j, k) + A(*a, i, j - 1, k)) * 0.5;
+#pragma omp parallel for schedule(static)
+    for (int k = 1; k <= dimz; ++k)
+        for (int i = 1; i <= dimx; ++i) {
+            A(*o, i, 1, k) = A(*o, i, 2, k);
+            A(*o, i, dimy + 1, k) = A(*o, i, dimy, k);
+        }
+}
+
+/* interpz_cf, :443-479 */
+static void interpz_cf(const F3 *a, int dimx, int dimy, int dimz, F3 *o)
+{
+#pragma omp parallel for schedule(static)
+    for (int k = 2; k <= dimz; ++k)
+        for (int j = 1; j <= dimy; ++j)
+            for (int i = 1; i <= dimx; ++i)
+                A(*o, i, j, k) = (A(*a, i, j, k) + A(*a, i, j, k - 1)) * 0.5;
+#pragma omp parallel for schedule(static)
+    for (int j = 1; j <= dimy; ++j)
+        for (int i = 1; i <= dimx; ++i) {
+            A(*o, i, j, 1) = A(*o, i, j, 2);
+            A(*o, i, j, dimz + 1) = A(*o, i, j, dimz);
+        }
+}
+
+/* interp?_fc: faces -> centres, :359-377, :420-439, :483-501 */
+static void interpx_fc(const F3 *a, int dimx, int dimy, int dimz, F3 *o)
+{
+    for (int k = 1; k <= dimz; ++k)
+        for (int j = 1; j <= dimy; ++j)
+            for (int i = 1; i <= dimx - 1; ++i)
+                A(*o, i, j, k) = (A(*a, i, j, k) + A(*a, i + 1, j, k)) * 0.5;
+}
+static void interpy_fc(const F3 *a, int dimx, int dimy, int dimz, F3 *o)
+{
+    for (int k = 1; k <= dimz; ++k)
+        for (int j = 1; j <= dimy - 1; ++j)
+            for (int i = 1; i <= dimx; ++i)
+                A(*o, i, j, k) = (A(*a, i, j, k) + A(*a, i, j + 1, k)) * 0.5;
+}
+static void interpz_fc(const F3 *a, int dimx, int dimy, int dimz, F3 *o)
+{
+    for (int k = 1; k <= dimz - 1; ++k)
+        for (int j = 1; j <= dimy; ++j)
+            for (int i = 1; i <= dimx; ++i)
+                A(*o, i, j, k) = (A(*a, i, j, k) + A(*a, i, j, k + 1)) * 0.5;
+}
+
+/* ------------------------------------------------------------------------ */
+/* 8_derivadas.f90:675-1095 -- WENO5 one-sided derivatives                   */
+/* ------------------------------------------------------------------------ */
+/* Jiang-Shu weights applied to five consecutive one-sided differences
+ * (v0..v4 = up(i),up(i-1),..,up(i-4) for phi+ or un(i),..,un(i+4) for phi-). */
+static inline double weno5(double v0, double v1, double v2, double v3, double v4)
+{
+    const double aux1 = 13. / 12., aux2 = 1. / 4., aux3 = 1. / 6., aux6 = 0.00000001;
+    double a, b, is1, is2, is3;
+    a = v0 - 2 * v1 + v2;
+    b = v0 - 4 * v1 + 3 * v2;
+    is1 = aux1 * a * a + aux2 * b * b;
+    a = v1 - 2 * v2 + v3;
+    b = v1 - v3;
+    is2 = aux1 * a * a + aux2 * b * b;
+    a = v2 - 2 * v3 + v4;
+    b = 3 * v2 - 4 * v3 + v4;
+    is3 = aux1 * a * a + aux2 * b * b;
+    double al1 = 0.1 / ((aux6 + is1) * (aux6 + is1));
+    double al2 = 0.6 / ((aux6 + is2) * (aux6 + is2));
+    double al3 = 0.3 / ((aux6 + is3) * (aux6 + is3));
+    double om1 = al1 / (al1 + al2 + al3);
+    double om2 = al2 / (al1 + al2 + al3);
+    double om3 = al3 / (al1 + al2 + al3);
+    return aux3 * (om1 * (2 * v0 - 7 * v1 + 11 * v2) + om2 * (-v1 + 5 * v2 + 2 * v3) +
+                   om3 * (2 * v2 + 5 * v3 - v4));
+}
+
+/* One grid line a(1..n) (stride in elements).  ihs = 0: periodic with the
+ * reference's node-style wrap phi(0)=phi(n-1) (:702-714); ihs = 2: cubic
+ * extrapolation (:742-756).  dp = dphi+ ("dphidxp"), dn = dphi- ("dphidxn"). */
+void or_weno_line(const double *a, long s, int n, double h, int ihs, double *dp, double *dn)
+{
+    double stackbuf[1024];
+    double *buf = (2 * n + 16 <= 1024) ? stackbuf : (double *)malloc(sizeof(double) * (size_t)(2 * n + 16));
+    double *phi = buf + 3;            /* phi[m], m = -2 .. n+3 */
+    double *D = buf + n + 8 + 3;      /* D[m],   m = -2 .. n+2 */
+    for (int m = 1; m <= n; ++m) phi[m] = a[(long)(m - 1) * s];
+    if (ihs == 0) {
+        phi[0] = phi[n - 1];
+        phi[-1] = phi[n - 2];
+        phi[-2] = phi[n - 3];
+        phi[n + 1] = phi[2];
+        phi[n + 2] = phi[3];
+        phi[n + 3] = phi[4];
+    } else {
+        const double c11 = 1. / 11.;
+        phi[0] = c11 * (18. * phi[1] - 9. * phi[2] + 2. * phi[3]);
+        phi[-1] = c11 * (18. * phi[0] - 9. * phi[1] + 2. * phi[2]);
+        phi[-2] = c11 * (18. * phi[-1] - 9. * phi[0] + 2. * phi[1]);
+        phi[n + 1] = c11 * (18. * phi[n] - 9. * phi[n - 1] + 2. * phi[n - 2]);
+        phi[n + 2] = c11 * (18. * phi[n + 1] - 9. * phi[n] + 2. * phi[n - 1]);
+        phi[n + 3] = c11 * (18. * phi[n + 2] - 9. * phi[n + 1] + 2. * phi[n]);
+    }
+    /* one-sided differences D(m) = (phi(m+1)-phi(m))/h, m = -2..n+2;
+     * up(i) = D(i+2) (:761-765), un(i) = D(i-3) (:767-773) */
+    for (int m = -2; m <= n + 2; ++m) D[m] = (phi[m + 1] - phi[m]) / h;
+    for (int i = 1; i <= n; ++i) {
+        dp[(long)(i - 1) * s] = weno5(D[i + 2], D[i + 1], D[i], D[i - 1], D[i - 2]);
+        dn[(long)(i - 1) * s] = weno5(D[i - 3], D[i - 2], D[i - 1], D[i], D[i + 1]);
+    }
+    if (buf != stackbuf) free(buf);
+}
+
+/* der_weno, 14_level_set.f90:338-370.  out: ta=phi_x+, td=phi_x-, tb=phi_y+,
+ * te=phi_y-, tc=phi_z+, tf=phi_z-.  All arrays (1:dimx,1:dimy,1:dimz). */
+static void der_weno(const or_case *c, const F3 *ls, int dimx, int dimy, int dimz,
+                     F3 *ta, F3 *tb, F3 *tc, F3 *td, F3 *te, F3 *tf)
+{
+    int ihs = (c->p.ccx0 == 0) ? 0 : 2;
+    for (int k = 1; k <= dimz; ++k)
+        for (int j = 1; j <= dimy; ++j)
+            or_weno_line(&A(*ls, 1, j, k), 1, dimx, c->dx, ihs, &A(*ta, 1, j, k), &A(*td, 1, j, k));
+    ihs = (c->p.ccy0 == 0) ? 0 : 2;
+    for (int k = 1; k <= dimz; ++k)
+        for (int i = 1; i <= dimx; ++i)
+            or_weno_line(&A(*ls, i, 1, k), ls->s1, dimy, c->dy, ihs, &A(*tb, i, 1, k), &A(*te, i, 1, k));
+    ihs = 2;   /* z is always extrapolated (:365-366) */
+    for (int j = 1; j <= dimy; ++j)
+        for (int i = 1; i <= dimx; ++i)
+            or_weno_line(&A(*ls, i, j, 1), ls->s2, dimz, c->dz, ihs, &A(*tc, i, j, 1), &A(*tf, i, j, 1));
+}
+
+/* ------------------------------------------------------------------------ */
+/* 14_level_set.f90                                                          */
+/* ------------------------------------------------------------------------ */
+/* intt_ls, :277-297: TVD-RK3 stage; ta1 holds ls0 after stage 1. */
+static void intt_ls(const or_case *c, const F3 *hx, F3 *gx, F3 *ta1, int itrl, F3 *ls1, double dt1)
+{
+    long n = f3_size(ls1);
+    if (c->adtl[itrl - 1] == 1.) memcpy(ta1->p, ls1->p, sizeof(double) * (size_t)n);
+    memcpy(gx->p, ls1->p, sizeof(double) * (size_t)n);
+    double a = c->adtl[itrl - 1], b = c->bdtl[itrl - 1], g = c->gdtl[itrl - 1];
+    for (long q = 0; q < n; ++q) ls1->p[q] = a * ta1->p[q] + b * gx->p[q] + g * dt1 * hx->p[q];
+}
+
+/* conv_weno, :301-334 */
+static void conv_weno(or_case *c, F3 *sy7, F3 *ta, F3 *tb, F3 *tc, F3 *td, F3 *te, F3 *tf)
+{
+    int nx = c->nx, ny = c->ny, nz = c->nz;
+    der_weno(c, &c->ls, nx, ny, nz, ta, tb, tc, td, te, tf);
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i) {
+                double ua = (A(c->u, i, j, k) + A(c->u, i + 1, j, k)) * 0.5;
+                double va = (A(c->v, i, j, k) + A(c->v, i, j + 1, k)) * 0.5;
+                double wa = (A(c->w, i, j, k) + A(c->w, i, j, k + 1)) * 0.5;
+                double apos = ua > 0. ? ua : 0., aneg = ua < 0. ? ua : 0.;
+                double bpos = va > 0. ? va : 0., bneg = va < 0. ? va : 0.;
+                double cpos = wa > 0. ? wa : 0., cneg = wa < 0. ? wa : 0.;
+                A(*sy7, i, j, k) = -(apos * A(*td, i, j, k) + aneg * A(*ta, i, j, k) + bpos * A(*te, i, j, k) +
+                                     bneg * A(*tb, i, j, k) + cpos * A(*tf, i, j, k) + cneg * A(*tc, i, j, k));
+            }
+}
+
+static inline double fmax_(double a, double b) { return a > b ? a : b; }
+static inline double fmin_(double a, double b) { return a < b ? a : b; }
+
+/* Godunov selection of reinic_weno, :397-421 / :443-467; returns |grad| */
+static inline double godunov(double ls, double *ta, double *tb, double *tc, double td, double te, double tf)
+{
+    const double eps = 0.00000001;
+    double a1, a2;
+    if (ls > 0.) {
+        a1 = fmax_(td, eps); a2 = -fmin_(*ta, eps); *ta = fmax_(a1, a2);
+        a1 = fmax_(te, eps); a2 = -fmin_(*tb, eps); *tb = fmax_(a1, a2);
+        a1 = fmax_(tf, eps); a2 = -fmin_(*tc, eps); *tc = fmax_(a1, a2);
+    } else {
+        a1 = fmax_(*ta, eps); a2 = -fmin_(td, eps); *ta = fmax_(a1, a2);
+        a1 = fmax_(*tb, eps); a2 = -fmin_(te, eps); *tb = fmax_(a1, a2);
+        a1 = fmax_(*tc, eps); a2 = -fmin_(tf, eps); *tc = fmax_(a1, a2);
+    }
+    return sqrt(*ta * *ta + *tb * *tb + *tc * *tc);
+}
+
+/* reinic_weno, :374-504 (on a cell array of any dims) */
+static int reinic_weno(or_case *c, F3 *ls1, int dimx, int dimy, int dimz, int max_iter, int replay)
+{
+    F3 ta = tmp3(1, dimx, 1, dimy, 1, dimz), tb = tmp3(1, dimx, 1, dimy, 1, dimz),
+       tc = tmp3(1, dimx, 1, dimy, 1, dimz), td = tmp3(1, dimx, 1, dimy, 1, dimz),
+       te = tmp3(1, dimx, 1, dimy, 1, dimz), tf = tmp3(1, dimx, 1, dimy, 1, dimz);
+    F3 func_s = tmp3(1, dimx, 1, dimy, 1, dimz), sy7 = tmp3(1, dimx, 1, dimy, 1, dimz),
+       lsaux = tmp3(1, dimx, 1, dimy, 1, dimz), gx = tmp3(1, dimx, 1, dimy, 1, dimz),
+       ta1 = tmp3(1, dimx, 1, dimy, 1, dimz);
+    const double dx1 = c->dx1, dt1 = c->dt1;
+    int l = max_iter;     /* reference: l = 3 (:389) */
+
+    der_weno(c, ls1, dimx, dimy, dimz, &ta, &tb, &tc, &td, &te, &tf);
+    for (int k = 1; k <= dimz; ++k)
+        for (int j = 1; j <= dimy; ++j)
+            for (int i = 1; i <= dimx; ++i) {
+                double lv = A(*ls1, i, j, k);
+                double a = A(ta, i, j, k), b = A(tb, i, j, k), cc = A(tc, i, j, k);
+                double mod = godunov(lv, &a, &b, &cc, A(td, i, j, k), A(te, i, j, k), A(tf, i, j, k));
+                A(func_s, i, j, k) = lv / sqrt(lv * lv + mod * mod * dx1 * dx1);
+            }
+
+    int il = 0;
+    double error = 999.;
+    while (error > dt1 * dx1 * dx1) {
+        il = il + 1;
+        for (int itrl = 1; itrl <= 3; ++itrl) {
+            der_weno(c, ls1, dimx, dimy, dimz, &ta, &tb, &tc, &td, &te, &tf);
+            for (int k = 1; k <= dimz; ++k)
+                for (int j = 1; j <= dimy; ++j)
+                    for (int i = 1; i <= dimx; ++i) {
+                        double lv = A(*ls1, i, j, k);
+                        double a = A(ta, i, j, k), b = A(tb, i, j, k), cc = A(tc, i, j, k);
+                        double mod = godunov(lv, &a, &b, &cc, A(td, i, j, k), A(te, i, j, k), A(tf, i, j, k));
+                        A(sy7, i, j, k) = A(func_s, i, j, k) * (1. - mod);
+                        A(lsaux, i, j, k) = lv;
+                    }
+            intt_ls(c, &sy7, &gx, &ta1, itrl, ls1, dt1);
+        }
+        if (replay >= 0) {
+            error = (il >= replay) ? 0. : 999.;
+        } else if (il == l) {
+            error = 0.;
+        } else if (il < 1) {
+            error = 999.;
+        } else {
+            error = 0.;
+            int nr = 0;
+            for (int k = 1; k <= dimz; ++k)
+                for (int j = 1; j <= dimy; ++j)
+                    for (int i = 1; i <= dimx; ++i) {
+                        if (fabs(A(*ls1, i, j, k)) <= 2. * c->p.alpha1 * dx1) {
+                            error = error + A(*ls1, i, j, k) - A(lsaux, i, j, k);
+                            nr = nr + 1;
+                        }
+                    }
+            error = error / (double)nr;
+        }
+    }
+    fr(&ta); fr(&tb); fr(&tc); fr(&td); fr(&te); fr(&tf);
+    fr(&func_s); fr(&sy7); fr(&lsaux); fr(&gx); fr(&ta1);
+    return il;
+}
+
+/* heaviside, :508-594 (t_tens = 0 branch) */
+static void heaviside(or_case *c)
+{
+    const double a = c->p.alpha1, dx1 = c->dx1, pi = c->pi;
+    for (int k = 1; k <= c->nz; ++k)
+        for (int j = 1; j <= c->ny; ++j)
+            for (int i = 1; i <= c->nx; ++i) {
+                double l = A(c->ls, i, j, k), h;
+                if (l < -a * dx1) h = 0.;
+                else if (l > a * dx1) h = 1.;
+                else h = 0.5 * (1. + l / (a * dx1) + 1. / pi * sin(pi * l / (a * dx1)));
+                A(c->hs, i, j, k) = h;
+                A(c->rho, i, j, k) = c->p.rho_f1 * (1. - h) + c->p.rho_f2 * h;
+                A(c->ls_mu, i, j, k) = c->p.mu_f1 * (1. - h) + c->p.mu_f2 * h;
+            }
+}
+
+static double volume(const or_case *c)
+{
+    double vol = 0.;
+    for (int k = 1; k <= c->nz; ++k)
+        for (int j = 1; j <= c->ny; ++j)
+            for (int i = 1; i <= c->nx; ++i)
+                vol = vol + (1. - (1. - A(c->hs, i, j, k))) * c->dx * c->dy * c->dz;
+    return vol;
+}
+
+/* mod_ls1, :598-655 */
+static void mod_ls1(or_case *c, const F3 *ls1, F3 *mod, F3 *nxo, F3 *nyo, F3 *nzo, int dimx, int dimy, int dimz)
+{
+    F3 ta = tmp3(1, dimx, 1, dimy, 1, dimz), tb = tmp3(1, dimx, 1, dimy, 1, dimz),
+       tc = tmp3(1, dimx, 1, dimy, 1, dimz), td = tmp3(1, dimx, 1, dimy, 1, dimz),
+       te = tmp3(1, dimx, 1, dimy, 1, dimz), tf = tmp3(1, dimx, 1, dimy, 1, dimz);
+    der_weno(c, ls1, dimx, dimy, dimz, &ta, &tb, &tc, &td, &te, &tf);
+    for (int k = 1; k <= dimz; ++k)
+        for (int j = 1; j <= dimy; ++j)
+            for (int i = 1; i <= dimx; ++i) {
+                double a = A(ta, i, j, k), b = A(tb, i, j, k), cc = A(tc, i, j, k);
+                if (!(fabs(a) > fabs(A(td, i, j, k)))) a = A(td, i, j, k);
+                if (!(fabs(b) > fabs(A(te, i, j, k)))) b = A(te, i, j, k);
+                if (!(fabs(cc) > fabs(A(tf, i, j, k)))) cc = A(tf, i, j, k);
+                double m = sqrt(a * a + b * b + cc * cc);
+                A(*mod, i, j, k) = m;
+                if (nxo) {
+                    if (m == 0) {
+                        A(*nxo, i, j, k) = 0.; A(*nyo, i, j, k) = 0.; A(*nzo, i, j, k) = 0.;
+                    } else {
+                        A(*nxo, i, j, k) = a / m; A(*nyo, i, j, k) = b / m; A(*nzo, i, j, k) = cc / m;
+                    }
+                }
+            }
+    fr(&ta); fr(&tb); fr(&tc); fr(&td); fr(&te); fr(&tf);
+}
+
+/* level_set, :204-273 */
+void or_level_set(or_case *c)
+{
+    int nx = c->nx, ny = c->ny, nz = c->nz;
+    F3 sy7 = tmp3(1, nx, 1, ny, 1, nz), gx = tmp3(1, nx, 1, ny, 1, nz), ta1 = tmp3(1, nx, 1, ny, 1, nz);
+    F3 ta = tmp3(1, nx, 1, ny, 1, nz), tb = tmp3(1, nx, 1, ny, 1, nz), tc = tmp3(1, nx, 1, ny, 1, nz),
+       td = tmp3(1, nx, 1, ny, 1, nz), te = tmp3(1, nx, 1, ny, 1, nz), tf = tmp3(1, nx, 1, ny, 1, nz);
+
+    /* advection with the physical dt (dt1 = dt, :216-217) */
+    double dt_adv = c->dt;
+    for (int itrl = 1; itrl <= 3; ++itrl) {
+        conv_weno(c, &sy7, &ta, &tb, &tc, &td, &te, &tf);
+        intt_ls(c, &sy7, &gx, &ta1, itrl, &c->ls, dt_adv);
+    }
+    fr(&ta); fr(&tb); fr(&tc); fr(&td); fr(&te); fr(&tf);
+    fr(&sy7); fr(&gx); fr(&ta1);
+
+    c->reinit_iters = reinic_weno(c, &c->ls, nx, ny, nz, c->p.reinit_max_iter, c->replay_reinit);
+    heaviside(c);
+    c->vol_ins = volume(c);
+
+    /* volume correction, :243-267 (capped: the reference loop is unbounded) */
+    c->vol_loops = 0;
+    if (fabs(c->vol_ins - c->vol_ini) / c->vol_ins > 0.1 && c->p.mms_t != 2) {
+        F3 mod = tmp3(1, nx, 1, ny, 1, nz);
+        while ((fabs(c->vol_ins - c->vol_ini) / c->vol_ins > 0.1) && (c->p.mms_t != 2)) {
+            if (c->vol_loops >= c->p.vol_loop_max) break;
+            c->vol_loops++;
+            mod_ls1(c, &c->ls, &mod, NULL, NULL, NULL, nx, ny, nz);
+            for (int k = 1; k <= nz; ++k)
+                for (int j = 1; j <= ny; ++j)
+                    for (int i = 1; i <= nx; ++i)
+                        A(c->ls, i, j, k) = A(c->ls, i, j, k) -
+                                            c->dt1 * (c->vol_ins - c->vol_ini) * A(mod, i, j, k) / c->vol_ini;
+            heaviside(c);
+            c->vol_ins = volume(c);
+        }
+        fr(&mod);
+    }
+    /* mod_ls1 at :269 only feeds curv_ls1 (t_tens = 1): not needed here */
+}
+
+/* ------------------------------------------------------------------------ */
+/* 5_viscosidade.f90:11-157 (m_turb 0 / 1)                                   */
+/* ------------------------------------------------------------------------ */
+void or_visco(or_case *c)
+{
+    int nx = c->nx, ny = c->ny, nz = c->nz, nx1 = c->nx1, ny1 = c->ny1, nz1 = c->nz1;
+    if (c->p.m_turb == 0) {
+        memset(c->mut.p, 0, sizeof(double) * (size_t)f3_size(&c->mut));
+    } else {
+        /* central derivatives on the staggered locations, :52-54 */
+        F3 ux = tmp3(1, nx1, 1, ny, 1, nz), uy = tmp3(1, nx1, 1, ny, 1, nz), uz = tmp3(1, nx1, 1, ny, 1, nz);
+        F3 vx = tmp3(1, nx, 1, ny1, 1, nz), vy = tmp3(1, nx, 1, ny1, 1, nz), vz = tmp3(1, nx, 1, ny1, 1, nz);
+        F3 wx = tmp3(1, nx, 1, ny, 1, nz1), wy = tmp3(1, nx, 1, ny, 1, nz1), wz = tmp3(1, nx, 1, ny, 1, nz1);
+        for (int k = 1; k <= nz; ++k)
+            for (int j = 1; j <= ny; ++j)
+                for (int i = 1; i <= nx1; ++i) {
+                    A(ux, i, j, k) = (A(c->u, i + 1, j, k) - A(c->u, i - 1, j, k)) / (2. * c->dx);
+                    A(uy, i, j, k) = (A(c->u, i, j + 1, k) - A(c->u, i, j - 1, k)) / (2. * c->dy);
+                    A(uz, i, j, k) = (A(c->u, i, j, k + 1) - A(c->u, i, j, k - 1)) / (2. * c->dz);
+                }
+        for (int k = 1; k <= nz; ++k)
+            for (int j = 1; j <= ny1; ++j)
+                for (int i = 1; i <= nx; ++i) {
+                    A(vx, i, j, k) = (A(c->v, i + 1, j, k) - A(c->v, i - 1, j, k)) / (2. * c->dx);
+                    A(vy, i, j, k) = (A(c->v, i, j + 1, k) - A(c->v, i, j - 1, k)) / (2. * c->dy);
+                    A(vz, i, j, k) = (A(c->v, i, j, k + 1) - A(c->v, i, j, k - 1)) / (2. * c->dz);
+                }
+        for (int k = 1; k <= nz1; ++k)
+            for (int j = 1; j <= ny; ++j)
+                for (int i = 1; i <= nx; ++i) {
+                    A(wx, i, j, k) = (A(c->w, i + 1, j, k) - A(c->w, i - 1, j, k)) / (2. * c->dx);
+                    A(wy, i, j, k) = (A(c->w, i, j + 1, k) - A(c->w, i, j - 1, k)) / (2. * c->dy);
+                    A(wz, i, j, k) = (A(c->w, i, j, k + 1) - A(c->w, i, j, k - 1)) / (2. * c->dz);
+                }
+        /* face -> centre, :58-71 */
+        F3 dudx = tmp3(1, nx, 1, ny, 1, nz), dudy = tmp3(1, nx, 1, ny, 1, nz), dudz = tmp3(1, nx, 1, ny, 1, nz);
+        F3 dvdx = tmp3(1, nx, 1, ny, 1, nz), dvdy = tmp3(1, nx, 1, ny, 1, nz), dvdz = tmp3(1, nx, 1, ny, 1, nz);
+        F3 dwdx = tmp3(1, nx, 1, ny, 1, nz), dwdy = tmp3(1, nx, 1, ny, 1, nz), dwdz = tmp3(1, nx, 1, ny, 1, nz);
+        interpx_fc(&ux, nx1, ny, nz, &dudx); interpx_fc(&uy, nx1, ny, nz, &dudy); interpx_fc(&uz, nx1, ny, nz, &dudz);
+        interpy_fc(&vx, nx, ny1, nz, &dvdx); interpy_fc(&vy, nx, ny1, nz, &dvdy); interpy_fc(&vz, nx, ny1, nz, &dvdz);
+        interpz_fc(&wx, nx, ny, nz1, &dwdx); interpz_fc(&wy, nx, ny, nz1, &dwdy); interpz_fc(&wz, nx, ny, nz1, &dwdz);
+        /* Smagorinsky, :78-88 */
+        double cl = pow(c->dx * c->dy * c->dz, 2. / 3.);
+        double cs = c->p.csmag;
+        for (int k = 1; k <= nz; ++k)
+            for (int j = 1; j <= ny; ++j)
+                for (int i = 1; i <= nx; ++i) {
+                    double p1 = A(dudx, i, j, k) + 0.5 * (A(dudy, i, j, k) + A(dvdx, i, j, k) + A(dudz, i, j, k) + A(dwdx, i, j, k));
+                    double p2 = A(dvdy, i, j, k) + 0.5 * (A(dvdx, i, j, k) + A(dudy, i, j, k) + A(dvdz, i, j, k) + A(dwdy, i, j, k));
+                    double p3 = A(dwdz, i, j, k) + 0.5 * (A(dwdy, i, j, k) + A(dvdz, i, j, k) + A(dudz, i, j, k) + A(dwdx, i, j, k));
+                    A(c->mut, i, j, k) = cl * cs * cs * sqrt(2. * (p1 + p2 + p3) * (p1 + p2 + p3)) * A(c->rho, i, j, k);
+                }
+        fr(&ux); fr(&uy); fr(&uz); fr(&vx); fr(&vy); fr(&vz); fr(&wx); fr(&wy); fr(&wz);
+        fr(&dudx); fr(&dudy); fr(&dudz); fr(&dvdx); fr(&dvdy); fr(&dvdz); fr(&dwdx); fr(&dwdy); fr(&dwdz);
+    }
+    /* :151-155 */
+    long n = f3_size(&c->mu);
+    for (long q = 0; q < n; ++q) c->mu.p[q] = c->ls_mu.p[q] + c->mut.p[q];
+    interpx_cf(c, &c->mu, nx, ny, nz, &c->xmu);
+    interpy_cf(&c->mu, nx, ny, nz, &c->ymu);
+    interpz_cf(&c->mu, nx, ny, nz, &c->zmu);
+}
+
+/* ------------------------------------------------------------------------ */
+/* 7_advectivo.f90:171-284 -- classico, der = 3 (2nd-order upwind)           */
+/* ------------------------------------------------------------------------ */
+/* derivative helpers on a haloed staggered array a with interior dims (dimx,dimy,dimz) */
+static inline double d2n_x(const or_case *c, const F3 *a, int i, int j, int k, int dimx)
+{   /* derivaxu2n, 8_derivadas.f90:190-236 */
+    if (i >= 2) return 0.5 * (A(*a, i - 2, j, k) - 4 * A(*a, i - 1, j, k) + 3 * A(*a, i, j, k)) / c->dx;
+    if (c->p.ccx0 != 0) return 0.5 * (A(*a, i + 1, j, k) - A(*a, i - 1, j, k)) / c->dx;
+    return 0.5 * (A(*a, dimx - 1, j, k) - 4 * A(*a, dimx, j, k) + 3 * A(*a, i, j, k)) / c->dx;
+}
+static inline double d2p_x(const or_case *c, const F3 *a, int i, int j, int k, int dimx)
+{   /* derivaxu2p, :75-121 */
+    if (i <= dimx - 1) return 0.5 * (-A(*a, i + 2, j, k) + 4 * A(*a, i + 1, j, k) - 3 * A(*a, i, j, k)) / c->dx;
+    if (c->p.ccx0 != 0) return 0.5 * (A(*a, i + 1, j, k) - A(*a, i - 1, j, k)) / c->dx;
+    return 0.5 * (-A(*a, 2, j, k) + 4 * A(*a, 1, j, k) - 3 * A(*a, i, j, k)) / c->dx;
+}
+static inline double d2n_y(const or_case *c, const F3 *a, int i, int j, int k)
+{   /* derivayu2n, :240-269 */
+    if (j >= 2) return 0.5 * (A(*a, i, j - 2, k) - 4 * A(*a, i, j - 1, k) + 3 * A(*a, i, j, k)) / c->dy;
+    return 0.5 * (A(*a, i, j + 1, k) - A(*a, i, j - 1, k)) / c->dy;
+}
+static inline double d2p_y(const or_case *c, const F3 *a, int i, int j, int k, int dimy)
+{   /* derivayu2p, :125-153 */
+    if (j <= dimy - 1) return 0.5 * (-A(*a, i, j + 2, k) + 4 * A(*a, i, j + 1, k) - 3 * A(*a, i, j, k)) / c->dy;
+    return 0.5 * (A(*a, i, j + 1, k) - A(*a, i, j - 1, k)) / c->dy;
+}
+static inline double d2n_z(const or_case *c, const F3 *a, int i, int j, int k)
+{   /* derivazu2n, :273-300 */
+    if (k >= 2) return 0.5 * (A(*a, i, j, k - 2) - 4 * A(*a, i, j, k - 1) + 3 * A(*a, i, j, k)) / c->dz;
+    return 0.5 * (A(*a, i, j, k + 1) - A(*a, i, j, k - 1)) / c->dz;
+}
+static inline double d2p_z(const or_case *c, const F3 *a, int i, int j, int k, int dimz)
+{   /* derivazu2p, :157-186 */
+    if (k <= dimz - 1) return 0.5 * (-A(*a, i, j, k + 2) + 4 * A(*a, i, j, k + 1) - 3 * A(*a, i, j, k)) / c->dz;
+    return 0.5 * (A(*a, i, j, k + 1) - A(*a, i, j, k - 1)) / c->dz;
+}
+
+static inline double upw(double vel, double dneg, double dpos)
+{
+    double a1 = vel > 0. ? vel : 0.;
+    double a2 = vel < 0. ? vel : 0.;
+    return a1 * dneg + a2 * dpos;
+}
+
+static void classico(or_case *c, F3 *uint_, F3 *vint_, F3 *wint_)
+{
+    int nx = c->nx, ny = c->ny, nz = c->nz, nx1 = c->nx1, ny1 = c->ny1, nz1 = c->nz1;
+    F3 aux = tmp3(1, nx, 1, ny, 1, nz);
+    F3 bma = tmp3(1, nx1, 1, ny, 1, nz), dma = tmp3(1, nx1, 1, ny, 1, nz);
+    F3 amb = tmp3(1, nx, 1, ny1, 1, nz), dmb = tmp3(1, nx, 1, ny1, 1, nz);
+    F3 amd = tmp3(1, nx, 1, ny, 1, nz1), bmd = tmp3(1, nx, 1, ny, 1, nz1);
+    /* advecting-velocity averages, :175-191 (interior slices of u, v, w) */
+    F3 vin = c->v, win = c->w, uin = c->u;   /* views; interp reads indices >= 1 only */
+    interpy_fc(&vin, nx, ny1, nz, &aux); interpx_cf(c, &aux, nx, ny, nz, &bma);
+    interpz_fc(&win, nx, ny, nz1, &aux); interpx_cf(c, &aux, nx, ny, nz, &dma);
+    interpx_fc(&uin, nx1, ny, nz, &aux); interpy_cf(&aux, nx, ny, nz, &amb);
+    interpz_fc(&win, nx, ny, nz1, &aux); interpy_cf(&aux, nx, ny, nz, &dmb);
+    interpx_fc(&uin, nx1, ny, nz, &aux); interpz_cf(&aux, nx, ny, nz, &amd);
+    interpy_fc(&vin, nx, ny1, nz, &aux); interpz_cf(&aux, nx, ny, nz, &bmd);
+
+    /* :216-236 */
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx1; ++i) {
+                double ddx = upw(A(c->u, i, j, k), d2n_x(c, &c->u, i, j, k, nx1), d2p_x(c, &c->u, i, j, k, nx1));
+                double ddy = upw(A(bma, i, j, k), d2n_y(c, &c->u, i, j, k), d2p_y(c, &c->u, i, j, k, ny));
+                double ddz = upw(A(dma, i, j, k), d2n_z(c, &c->u, i, j, k), d2p_z(c, &c->u, i, j, k, nz));
+                A(*uint_, i, j, k) = ddx + ddy + ddz;
+            }
+    /* :238-258 */
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny1; ++j)
+            for (int i = 1; i <= nx; ++i) {
+                double ddx = upw(A(amb, i, j, k), d2n_x(c, &c->v, i, j, k, nx), d2p_x(c, &c->v, i, j, k, nx));
+                double ddy = upw(A(c->v, i, j, k), d2n_y(c, &c->v, i, j, k), d2p_y(c, &c->v, i, j, k, ny1));
+                double ddz = upw(A(dmb, i, j, k), d2n_z(c, &c->v, i, j, k), d2p_z(c, &c->v, i, j, k, nz));
+                A(*vint_, i, j, k) = ddx + ddy + ddz;
+            }
+    /* :260-280 */
+    for (int k = 1; k <= nz1; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i) {
+                double ddx = upw(A(amd, i, j, k), d2n_x(c, &c->w, i, j, k, nx), d2p_x(c, &c->w, i, j, k, nx));
+                double ddy = upw(A(bmd, i, j, k), d2n_y(c, &c->w, i, j, k), d2p_y(c, &c->w, i, j, k, ny));
+                double ddz = upw(A(c->w, i, j, k), d2n_z(c, &c->w, i, j, k), d2p_z(c, &c->w, i, j, k, nz1));
+                A(*wint_, i, j, k) = ddx + ddy + ddz;
+            }
+    fr(&aux); fr(&bma); fr(&dma); fr(&amb); fr(&dmb); fr(&amd); fr(&bmd);
+}
+
+/* ------------------------------------------------------------------------ */
+/* 6_convdiff.f90:14-167                                                     */
+/* ------------------------------------------------------------------------ */
+void or_convdiff(or_case *c)
+{
+    int nx = c->nx, ny = c->ny, nz = c->nz, nx1 = c->nx1, ny1 = c->ny1, nz1 = c->nz1;
+    double dx = c->dx, dy = c->dy, dz = c->dz;
+    F3 ui = tmp3(1, nx1, 1, ny, 1, nz), vi = tmp3(1, nx, 1, ny1, 1, nz), wi = tmp3(1, nx, 1, ny, 1, nz1);
+    classico(c, &ui, &vi, &wi);
+
+    F3 rhox = tmp3(1, nx1, 1, ny, 1, nz), rhoy = tmp3(1, nx, 1, ny1, 1, nz), rhoz = tmp3(1, nx, 1, ny, 1, nz1);
+    interpx_cf(c, &c->rho, nx, ny, nz, &rhox);
+    interpy_cf(&c->rho, nx, ny, nz, &rhoy);
+    interpz_cf(&c->rho, nx, ny, nz, &rhoz);
+
+    F3 bma = tmp3(1, nx1, 1, ny1, 1, nz), dma = tmp3(1, nx1, 1, ny, 1, nz1);
+    F3 amb = tmp3(1, nx1, 1, ny1, 1, nz), dmb = tmp3(1, nx, 1, ny1, 1, nz1);
+    F3 amd = tmp3(1, nx1, 1, ny, 1, nz1), bmd = tmp3(1, nx, 1, ny1, 1, nz1);
+    interpy_cf(&c->xmu, nx1, ny, nz, &bma);
+    interpz_cf(&c->xmu, nx1, ny, nz, &dma);
+    interpx_cf(c, &c->ymu, nx, ny1, nz, &amb);
+    interpz_cf(&c->ymu, nx, ny1, nz, &dmb);
+    interpx_cf(c, &c->zmu, nx, ny, nz1, &amd);
+    interpy_cf(&c->zmu, nx, ny, nz1, &bmd);
+
+    F3 ama = tmp3(0, nx1, 1, ny, 1, nz), bmb = tmp3(1, nx, 0, ny1, 1, nz), dmd = tmp3(1, nx, 1, ny, 0, nz1);
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i) {
+                A(ama, i, j, k) = A(c->mu, i, j, k) / dx;
+                A(bmb, i, j, k) = A(c->mu, i, j, k) / dy;
+                A(dmd, i, j, k) = A(c->mu, i, j, k) / dz;
+            }
+    long q, n;
+    n = f3_size(&bma); for (q = 0; q < n; ++q) bma.p[q] = bma.p[q] / dy;
+    n = f3_size(&dma); for (q = 0; q < n; ++q) dma.p[q] = dma.p[q] / dz;
+    n = f3_size(&amb); for (q = 0; q < n; ++q) amb.p[q] = amb.p[q] / dx;
+    n = f3_size(&dmb); for (q = 0; q < n; ++q) dmb.p[q] = dmb.p[q] / dz;
+    n = f3_size(&amd); for (q = 0; q < n; ++q) amd.p[q] = amd.p[q] / dx;
+    n = f3_size(&bmd); for (q = 0; q < n; ++q) bmd.p[q] = bmd.p[q] / dy;
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j) {
+            A(ama, 0, j, k) = A(ama, 1, j, k);
+            A(ama, nx1, j, k) = A(ama, nx, j, k);
+        }
+    for (int k = 1; k <= nz; ++k)
+        for (int i = 1; i <= nx; ++i) {
+            A(bmb, i, 0, k) = A(bmb, i, 1, k);
+            A(bmb, i, ny1, k) = A(bmb, i, ny, k);
+        }
+    for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+            A(dmd, i, j, 0) = A(dmd, i, j, 1);
+            A(dmd, i, j, nz1) = A(dmd, i, j, nz);
+        }
+
+    F3 u = c->u, v = c->v, w = c->w;
+    /* :129-151 */
+    for (int k = 1; k <= nz; ++k) {
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx1; ++i) {
+                A(c->Fu, i, j, k) = -A(ui, i, j, k) +
+                    ((A(ama, i, j, k) * 2. * (A(u, i + 1, j, k) - A(u, i, j, k)) -
+                      A(ama, i - 1, j, k) * 2. * (A(u, i, j, k) - A(u, i - 1, j, k))) / dx +
+                     A(bma, i, j + 1, k) * ((A(u, i, j + 1, k) - A(u, i, j, k)) / dy + (A(v, i, j + 1, k) - A(v, i - 1, j + 1, k)) / dx) -
+                     A(bma, i, j, k) * ((A(u, i, j, k) - A(u, i, j - 1, k)) / dy + (A(v, i, j, k) - A(v, i - 1, j, k)) / dx) +
+                     A(dma, i, j, k + 1) * ((A(u, i, j, k + 1) - A(u, i, j, k)) / dz + (A(w, i, j, k + 1) - A(w, i - 1, j, k + 1)) / dx) -
+                     A(dma, i, j, k) * ((A(u, i, j, k) - A(u, i, j, k - 1)) / dz + (A(w, i, j, k) - A(w, i - 1, j, k)) / dx)) /
+                    A(rhox, i, j, k);
+            }
+        for (int j = 1; j <= ny1; ++j)
+            for (int i = 1; i <= nx; ++i) {
+                A(c->Fv, i, j, k) = -A(vi, i, j, k) +
+                    (A(amb, i + 1, j, k) * ((A(v, i + 1, j, k) - A(v, i, j, k)) / dx + (A(u, i + 1, j, k) - A(u, i + 1, j - 1, k)) / dy) -
+                     A(amb, i, j, k) * ((A(v, i, j, k) - A(v, i - 1, j, k)) / dx + (A(u, i, j, k) - A(u, i, j - 1, k)) / dy) +
+                     (A(bmb, i, j, k) * 2. * (A(v, i, j + 1, k) - A(v, i, j, k)) -
+                      A(bmb, i, j - 1, k) * 2. * (A(v, i, j, k) - A(v, i, j - 1, k))) / dy +
+                     A(dmb, i, j, k + 1) * ((A(v, i, j, k + 1) - A(v, i, j, k)) / dz + (A(w, i, j, k + 1) - A(w, i, j - 1, k + 1)) / dy) -
+                     A(dmb, i, j, k) * ((A(v, i, j, k) - A(v, i, j, k - 1)) / dz + (A(w, i, j, k) - A(w, i, j - 1, k)) / dy)) /
+                    A(rhoy, i, j, k);
+            }
+    }
+    /* :153-164 */
+    for (int k = 1; k <= nz1; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i) {
+                A(c->Fw, i, j, k) = -A(wi, i, j, k) +
+                    (A(amd, i + 1, j, k) * ((A(w, i + 1, j, k) - A(w, i, j, k)) / dx + (A(u, i + 1, j, k) - A(u, i + 1, j, k - 1)) / dz) -
+                     A(amd, i, j, k) * ((A(w, i, j, k) - A(w, i - 1, j, k)) / dx + (A(u, i, j, k) - A(u, i, j, k - 1)) / dz) +
+                     A(bmd, i, j + 1, k) * ((A(w, i, j + 1, k) - A(w, i, j, k)) / dy + (A(v, i, j + 1, k) - A(v, i, j + 1, k - 1)) / dz) -
+                     A(bmd, i, j, k) * ((A(w, i, j, k) - A(w, i, j - 1, k)) / dy + (A(v, i, j, k) - A(v, i, j, k - 1)) / dz) +
+                     (A(dmd, i, j, k) * 2. * (A(w, i, j, k + 1) - A(w, i, j, k)) -
+                      A(dmd, i, j, k - 1) * 2. * (A(w, i, j, k) - A(w, i, j, k - 1))) / dz) /
+                    A(rhoz, i, j, k);
+            }
+    fr(&ui); fr(&vi); fr(&wi); fr(&rhox); fr(&rhoy); fr(&rhoz);
+    fr(&bma); fr(&dma); fr(&amb); fr(&dmb); fr(&amd); fr(&bmd); fr(&ama); fr(&bmb); fr(&dmd);
+}
+
+/* ------------------------------------------------------------------------ */
+/* 11_diversos.f90:355-450 -- complementos (t_tens=0, m_turb<2, no sponge)   */
+/* ------------------------------------------------------------------------ */
+void or_complementos(or_case *c)
+{
+    int nx = c->nx, ny = c->ny, nz = c->nz, nx1 = c->nx1, ny1 = c->ny1, nz1 = c->nz1;
+    /* gravity and MMS source; the surface-tension and k-gradient terms are
+     * exact zeros for t_tens = 0 and ka = 0 */
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx1; ++i)
+                A(c->Fu, i, j, k) = A(c->Fu, i, j, k) + c->p.gx + A(c->tf_u, i, j, k);
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny1; ++j)
+            for (int i = 1; i <= nx; ++i)
+                A(c->Fv, i, j, k) = A(c->Fv, i, j, k) + A(c->tf_v, i, j, k);
+    for (int k = 1; k <= nz1; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i)
+                A(c->Fw, i, j, k) = A(c->Fw, i, j, k) - c->p.gz + A(c->tf_w, i, j, k);
+}
+
+/* ------------------------------------------------------------------------ */
+/* 11_diversos.f90:10-296 -- tempo                                          */
+/* ------------------------------------------------------------------------ */
+static void tempo_one(or_case *c, F3 *u, F3 *F, F3 *u0, F3 *f0, F3 *f1, int di, int dj, int dk)
+{
+    int tt = c->tt, it = c->it, tte = c->p.t_tempo;
+    double dt = c->dt;
+    for (int k = 1; k <= dk; ++k)
+        for (int j = 1; j <= dj; ++j)
+            for (int i = 1; i <= di; ++i) {
+                double *pu = &A(*u, i, j, k);
+                double Fv = A(*F, i, j, k);
+                if ((tte == 0) || ((tte == 3) || ((tte == 4) && (it == 1)))) {
+                    /* :48-80 (AB2 always lands here: operator precedence upstream) */
+                    *pu = *pu + dt * Fv;
+                    if (tte == 3 || tte == 4) A(*f0, i, j, k) = Fv;
+                } else if (tte == 1) {
+                    if (tt == 1) { A(*u0, i, j, k) = *pu; *pu = *pu + dt * Fv; }
+                    else if (tt == 2) { *pu = A(*u0, i, j, k) + dt * Fv; }
+                } else if (tte == 2) {
+                    if (tt == 1) {
+                        A(*u0, i, j, k) = *pu; A(*f0, i, j, k) = Fv; *pu = *pu + dt * Fv;
+                    } else if (tt == 2) {
+                        double aux1 = 2. * dt;
+                        A(*f1, i, j, k) = Fv;
+                        *pu = A(*u0, i, j, k) - dt * A(*f0, i, j, k) + aux1 * Fv;
+                    } else if (tt == 3) {
+                        double aux1 = dt / 6.;
+                        *pu = A(*u0, i, j, k) + aux1 * (A(*f0, i, j, k) + 4. * A(*f1, i, j, k) + Fv);
+                    }
+                } else if (((tte == 3) && (it != 1)) || ((tte == 4) && (it == 2))) {
+                    *pu = *pu + dt * 0.5 * (3 * Fv - A(*f0, i, j, k));
+                    A(*f0, i, j, k) = Fv;
+                    if (tte == 4) A(*f1, i, j, k) = A(*f0, i, j, k);
+                } else if ((tte == 4) && (it >= 3)) {
+                    double aux1 = dt / 12.;
+                    *pu = *pu + aux1 * (23. * Fv - 16. * A(*f0, i, j, k) + 5. * A(*f1, i, j, k));
+                    A(*f1, i, j, k) = A(*f0, i, j, k);
+                    A(*f0, i, j, k) = Fv;
+                }
+            }
+}
+
+void or_tempo(or_case *c)
+{
+    tempo_one(c, &c->u, &c->Fu, &c->u0, &c->fu0, &c->fu1, c->nx1, c->ny, c->nz);
+    tempo_one(c, &c->v, &c->Fv, &c->v0, &c->fv0, &c->fv1, c->nx, c->ny1, c->nz);
+    tempo_one(c, &c->w, &c->Fw, &c->w0, &c->fw0, &c->fw1, c->nx, c->ny, c->nz1);
+}
+
+/* ------------------------------------------------------------------------ */
+/* 3_contorno.f90:11-662 -- contorno (cc 0,1,2,4; ibm via ibm_images)        */
+/* ------------------------------------------------------------------------ */
+static void ibm_images(or_case *c, F3 *obs, F3 *a1, int dimx, int dimy, int dimz, I3 *id, int der_t);
+
+/* plane-slice helpers: a(:,J,:) = s * b(:,J2,:) etc over the full extents */
+static void setx(F3 *a, int I, const F3 *b, int I2, double s)
+{
+    for (int k = a->lo[2]; k <= a->hi[2]; ++k)
+        for (int j = a->lo[1]; j <= a->hi[1]; ++j) A(*a, I, j, k) = s * A(*b, I2, j, k);
+}
+static void sety(F3 *a, int J, const F3 *b, int J2, double s)
+{
+    for (int k = a->lo[2]; k <= a->hi[2]; ++k)
+        for (int i = a->lo[0]; i <= a->hi[0]; ++i) A(*a, i, J, k) = s * A(*b, i, J2, k);
+}
+static void setz(F3 *a, int K, const F3 *b, int K2, double s)
+{
+    for (int j = a->lo[1]; j <= a->hi[1]; ++j)
+        for (int i = a->lo[0]; i <= a->hi[0]; ++i) A(*a, i, j, K) = s * A(*b, i, j, K2);
+}
+static void zerox(F3 *a, int I) { for (int k = a->lo[2]; k <= a->hi[2]; ++k) for (int j = a->lo[1]; j <= a->hi[1]; ++j) A(*a, I, j, k) = 0.; }
+static void zeroy(F3 *a, int J) { for (int k = a->lo[2]; k <= a->hi[2]; ++k) for (int i = a->lo[0]; i <= a->hi[0]; ++i) A(*a, i, J, k) = 0.; }
+static void zeroz(F3 *a, int K) { for (int j = a->lo[1]; j <= a->hi[1]; ++j) for (int i = a->lo[0]; i <= a->hi[0]; ++i) A(*a, i, j, K) = 0.; }
+
+/* counter-based hash RNG in [0,1) replacing Fortran random_number (the
+ * reference's stream cannot be reproduced); same function on the GPU */
+static double rng_uniform(unsigned long long seed, unsigned long long ctr)
+{
+    unsigned long long z = seed + 0x9E3779B97F4A7C15ULL * (ctr + 1ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    z = z ^ (z >> 31);
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+/* prescribed inflow with perturbation, 3_contorno.f90:301-330 (I = 0) and
+ * :532-563 (I = 1).  Random draws are indexed by (call, j, k). */
+static void inflow_plane(or_case *c, int I, const F3 *bplane, double lsthr_fac)
+{
+    int nx = c->nx, ny = c->ny, nz = c->nz;
+    /* ls_x(i=I..) = interpx_cf(ls) at face I (I = 0 reads face index 0 which
+     * the reference leaves undefined; face 1 is used for both) */
+    int iik = 0;
+    unsigned long long base = c->rng_counter;
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j) {
+            double lsx;
+            if (c->p.ccx0 != 0) lsx = (A(c->ls, 2, j, k) + A(c->ls, 1, j, k)) * 0.5;
+            else lsx = (A(c->ls, 1, j, k) + A(c->ls, nx, j, k)) * 0.5;
+            if (lsx >= -lsthr_fac * c->dz) {
+                double r = rng_uniform(c->p.seed, base + (unsigned long long)((k - 1) * ny + (j - 1)));
+                r = 2. * (r - 0.5);
+                A(c->u, I, j, k) = A(*bplane, j, k, 0);
+                A(c->u, I, j, k) = A(c->u, I, j, k) * (1. + r * c->p.iturb);
+                iik = k;
+            } else if (lsx < 0) {
+                A(c->u, I, j, k) = A(c->u, I, j, iik) * (1. + tanh(c->pi * (iik - k - 1) / 2.));
+            }
+        }
+    c->rng_counter += (unsigned long long)ny * (unsigned long long)nz;
+}
+
+void or_contorno(or_case *c, int nlock)
+{
+    int nx = c->nx, ny = c->ny, nz = c->nz, nx1 = c->nx1, ny1 = c->ny1, nz1 = c->nz1;
+    const suli_params *p = &c->p;
+    F3 *u = &c->u, *v = &c->v, *w = &c->w, *prd1 = &c->prd1;
+    if (nlock == 1 || nlock == 2) {
+        if (p->ibm_t == 2) {   /* :85-90 */
+            ibm_images(c, &c->obs_lsx, u, nx1, ny, nz, &c->id_ibmx, 1);
+            ibm_images(c, &c->obs_lsy, v, nx, ny1, nz, &c->id_ibmy, 1);
+            ibm_images(c, &c->obs_lsz, w, nx, ny, nz1, &c->id_ibmz, 1);
+        }
+        /* pressure ghosts, :99-116 */
+        if (p->ccx0 == 0 && p->ccxf == 0) { setx(prd1, 0, prd1, nx, 1.); setx(prd1, nx + 1, prd1, 1, 1.); }
+        else { setx(prd1, 0, prd1, 1, 1.); setx(prd1, nx + 1, prd1, nx, 1.); }
+        if (p->ccy0 == 0 && p->ccyf == 0) { sety(prd1, 0, prd1, ny, 1.); sety(prd1, ny + 1, prd1, 1, 1.); }
+        else { sety(prd1, 0, prd1, 1, 1.); sety(prd1, ny + 1, prd1, ny, 1.); }
+        setz(prd1, 0, prd1, 1, 1.); setz(prd1, nz + 1, prd1, nz, 1.);
+
+        /* y = 0 wall, :118-144 */
+        if (p->ccy0 == 0 && p->ccyf == 0) { sety(u, 0, u, ny, 1.); sety(v, 0, v, ny1 - 1, 1.); sety(w, 0, w, ny, 1.); }
+        if (p->ccy0 == 1) { sety(u, 0, u, 1, 1.); sety(v, 0, v, 2, -1.); sety(w, 0, w, 1, 1.); }
+        if (p->ccy0 == 2) { sety(u, 0, u, 1, -1.); sety(v, 0, v, 2, 1.); sety(w, 0, w, 1, -1.); }
+        /* y = ly wall, :146-173 */
+        if (p->ccy0 == 0 && p->ccyf == 0) { sety(u, ny + 1, u, 1, 1.); sety(v, ny1 + 1, v, 2, 1.); sety(w, ny + 1, w, 1, 1.); }
+        if (p->ccyf == 1) { sety(u, ny + 1, u, ny, 1.); sety(v, ny1 + 1, v, ny1 - 1, -1.); sety(w, ny + 1, w, ny, 1.); }
+        if (p->ccyf == 2) { sety(u, ny + 1, u, ny, -1.); sety(v, ny1 + 1, v, ny1 - 1, 1.); sety(w, ny + 1, w, ny, -1.); }
+        /* bottom, :176-196 */
+        if (p->ccz0 == 1) { setz(u, 0, u, 1, 1.); setz(v, 0, v, 1, 1.); setz(w, 0, w, 2, -1.); }
+        if (p->ccz0 == 2) { setz(u, 0, u, 1, -1.); setz(v, 0, v, 1, -1.); setz(w, 0, w, 2, 1.); }
+        /* top, :255-275 */
+        if (p->cczf == 1) { setz(u, nz + 1, u, nz, 1.); setz(v, nz + 1, v, nz, 1.); setz(w, nz1 + 1, w, nz1 - 1, -1.); }
+        if (p->cczf == 2) { setz(u, nz + 1, u, nz, -1.); setz(v, nz + 1, v, nz, -1.); setz(w, nz1 + 1, w, nz1 - 1, 1.); }
+        /* x = 0, :278-330 */
+        if (p->ccx0 == 0 && p->ccxf == 0) { setx(u, 0, u, nx1 - 1, 1.); setx(v, 0, v, nx, 1.); setx(w, 0, w, nx, 1.); }
+        if (p->ccx0 == 1) { setx(u, 0, u, 2, -1.); setx(v, 0, v, 1, 1.); setx(w, 0, w, 1, 1.); }
+        if (p->ccx0 == 2) { setx(u, 0, u, 2, 1.); setx(v, 0, v, 1, -1.); setx(w, 0, w, 1, -1.); }
+        if (p->ccx0 == 3) {   /* bxy0 = bxz0 = 0 (2_iniciais.f90:384-385) */
+            zerox(v, 0); zerox(w, 0);
+            inflow_plane(c, 0, &c->bxx0, 1.0);
+        }
+        /* x = lx, :350-384 */
+        if (p->ccx0 == 0 && p->ccxf == 0) { setx(u, nx1 + 1, u, 2, 1.); setx(v, nx + 1, v, 1, 1.); setx(w, nx + 1, w, 1, 1.); }
+        if (p->ccxf == 1) { setx(u, nx1 + 1, u, nx1 - 1, -1.); setx(v, nx + 1, v, nx, 1.); setx(w, nx + 1, w, nx, 1.); }
+        if (p->ccxf == 2) { setx(u, nx1 + 1, u, nx1 - 1, 1.); setx(v, nx + 1, v, nx, -1.); setx(w, nx + 1, w, nx, -1.); }
+        if (p->ccxf == 4) { setx(u, nx1 + 1, u, nx1, 1.); setx(v, nx + 1, v, nx, 1.); setx(w, nx + 1, w, nx, 1.); }
+    }
+    if (nlock == 2) {
+        /* wall-normal faces, :394-605 */
+        if (p->ccy0 == 0 && p->ccyf == 0) sety(v, 1, v, ny1, 1.);
+        if (p->ccy0 == 1 || p->ccy0 == 2) zeroy(v, 1);
+        if (p->ccy0 == 0 && p->ccyf == 0) sety(v, ny1, v, 1, 1.);
+        if (p->ccyf == 1 || p->ccyf == 2) zeroy(v, ny1);
+        if (p->ccz0 == 1 || p->ccz0 == 2 || p->ccz0 == 4) zeroz(w, 1);
+        if (p->cczf == 1 || p->cczf == 2) zeroz(w, nz1);
+        if (p->ccx0 == 0 && p->ccxf == 0) setx(u, 1, u, nx1, 1.);
+        if (p->ccx0 == 1 || p->ccx0 == 2) zerox(u, 1);
+        if (p->ccx0 == 3) {
+            for (int k = 1; k <= nz; ++k)
+                for (int j = 1; j <= ny; ++j) A(c->ls, 1, j, k) = A(c->blx1, j, k, 0);
+            inflow_plane(c, 1, &c->bxx1, 2.0);
+        }
+        if (p->ccx0 == 0 && p->ccxf == 0) setx(u, nx1, u, 1, 1.);
+        if (p->ccxf == 1 || p->ccxf == 2) zerox(u, nx1);
+        if (p->ccxf == 4) setx(u, nx1, u, nx1 - 1, 1.);
+    } else if (nlock == 3 && p->ibm_t == 2) {
+        /* level-set IBM, :651-659 */
+        F3 lsv = tmp3(0, nx + 1, 0, ny + 1, 0, nz + 1);
+        /* fantasmas_cf, 8_derivadas.f90:625-671 */
+        for (int k = 1; k <= nz; ++k)
+            for (int j = 1; j <= ny; ++j)
+                for (int i = 1; i <= nx; ++i) A(lsv, i, j, k) = A(c->ls, i, j, k);
+        for (int k = 1; k <= nz; ++k)
+            for (int i = 1; i <= nx; ++i) { A(lsv, i, 0, k) = A(c->ls, i, 1, k); A(lsv, i, ny + 1, k) = A(c->ls, i, ny, k); }
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i) { A(lsv, i, j, 0) = A(c->ls, i, j, 1); A(lsv, i, j, nz + 1) = A(c->ls, i, j, nz); }
+        if (p->ccx0 == 0) { setx(&lsv, 0, &lsv, nx, 1.); setx(&lsv, nx + 1, &lsv, 1, 1.); }
+        else { setx(&lsv, 0, &lsv, 1, 1.); setx(&lsv, nx + 1, &lsv, nx, 1.); }
+        ibm_images(c, &c->obs_lss, &lsv, nx, ny, nz, &c->id_ibm, 2);
+        for (int k = 1; k <= nz; ++k)
+            for (int j = 1; j <= ny; ++j)
+                for (int i = 1; i <= nx; ++i) A(c->ls, i, j, k) = A(lsv, i, j, k);
+        fr(&lsv);
+        reinic_weno(c, &c->ls, nx, ny, nz, c->p.reinit_max_iter, -1);
+        heaviside(c);
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* 15_ibm.f90                                                                */
+/* ------------------------------------------------------------------------ */
+/* ibm_posicoes, :9-131 */
+static void ibm_posicoes(I3 *id, const F3 *o, int dimx, int dimy, int dimz)
+{
+    memset(id->p, 0, sizeof(int) * (size_t)(id->s2 * (long)dimz));
+    for (int k = 1; k <= dimz; ++k)
+        for (int j = 1; j <= dimy; ++j)
+            for (int i = 1; i <= dimx - 2; ++i)
+                if (A(*o, i, j, k) > 0) {
+                    if (A(*o, i, j, k) * A(*o, i + 1, j, k) < 0.) A(*id, i, j, k) = 1;
+                    else if (A(*o, i, j, k) * A(*o, i + 2, j, k) < 0.) A(*id, i, j, k) = 1;
+                }
+    for (int k = 1; k <= dimz; ++k)
+        for (int j = 1; j <= dimy; ++j)
+            for (int i = 3; i <= dimx; ++i)
+                if (A(*o, i, j, k) > 0) {
+                    if (A(*o, i, j, k) * A(*o, i - 1, j, k) < 0.) A(*id, i, j, k) = 1;
+                    else if (A(*o, i, j, k) * A(*o, i - 2, j, k) < 0.) A(*id, i, j, k) = 1;
+                }
+    for (int k = 1; k <= dimz; ++k)
+        for (int j = 1; j <= dimy - 2; ++j)
+            for (int i = 1; i <= dimx; ++i)
+                if (A(*o, i, j, k) > 0) {
+                    if (A(*o, i, j, k) * A(*o, i, j + 1, k) < 0.) A(*id, i, j, k) = 1;
+                    else if (A(*o, i, j, k) * A(*o, i, j + 2, k) < 0.) A(*id, i, j, k) = 1;
+                }
+    for (int k = 1; k <= dimz; ++k)
+        for (int j = 3; j <= dimy; ++j)
+            for (int i = 1; i <= dimx; ++i)
+                if (A(*o, i, j, k) > 0) {
+                    if (A(*o, i, j, k) * A(*o, i, j - 1, k) < 0.) A(*id, i, j, k) = 1;
+                    else if (A(*o, i, j, k) * A(*o, i, j - 2, k) < 0.) A(*id, i, j, k) = 1;
+                }
+    for (int k = 1; k <= dimz - 2; ++k)
+        for (int j = 1; j <= dimy; ++j)
+            for (int i = 1; i <= dimx; ++i)
+                if (A(*o, i, j, k) > 0) {
+                    if (A(*o, i, j, k) * A(*o, i, j, k + 1) < 0.) A(*id, i, j, k) = 1;
+                    else if (A(*o, i, j, k) * A(*o, i, j, k + 2) < 0.) A(*id, i, j, k) = 1;
+                }
+    for (int k = 3; k <= dimz; ++k)
+        for (int j = 1; j <= dimy; ++j)
+            for (int i = 1; i <= dimx; ++i)
+                if (A(*o, i, j, k) > 0) {
+                    if (A(*o, i, j, k) * A(*o, i, j, k - 1) < 0.) A(*id, i, j, k) = 1;
+                    else if (A(*o, i, j, k) * A(*o, i, j, k - 2) < 0.) A(*id, i, j, k) = 1;
+                }
+}
+
+/* id lookups outside the array (upstream reads past the end near walls,
+ * 15_ibm.f90:245-252) are taken as 0 = fluid; coordinates beyond the last
+ * node extend the uniform grid. */
+static inline int id_at(const I3 *id, int i, int j, int k)
+{
+    if (i < id->lo[0] || i > id->hi[0] || j < id->lo[1] || j > id->hi[1] || k < id->lo[2] || k > id->hi[2]) return 0;
+    return A(*id, i, j, k);
+}
+
+/* ibm_images, :134-318.  The sweep is in place as upstream. */
+static void ibm_images(or_case *c, F3 *obs, F3 *a1, int dimx, int dimy, int dimz, I3 *id, int der_t)
+{
+    const int ll = 2;
+    const double er = c->deltai * 0.01, v_sol = 0.;
+    const double dx = c->dx, dy = c->dy, dz = c->dz, deltai = c->deltai;
+    F3 mod = tmp3(1, dimx, 1, dimy, 1, dimz), nxv = tmp3(1, dimx, 1, dimy, 1, dimz),
+       nyv = tmp3(1, dimx, 1, dimy, 1, dimz), nzv = tmp3(1, dimx, 1, dimy, 1, dimz);
+    mod_ls1(c, obs, &mod, &nxv, &nyv, &nzv, dimx, dimy, dimz);
+    double ox = (dimx == c->nx) ? 0.5 : 1.0;   /* x(i) = (i-ox)*dx, :174-182 */
+    double oy = (dimy == c->ny) ? 0.5 : 1.0;
+    double oz = (dimz == c->nz) ? 0.5 : 1.0;
+#define XC(i) (((i) - ox) * dx)
+#define YC(j) (((j) - oy) * dy)
+#define ZC(k) (((k) - oz) * dz)
+    for (int k = 1; k <= dimz; ++k)
+        for (int j = 1; j <= dimy; ++j)
+            for (int i = 1; i <= dimx; ++i) {
+                double ob = A(*obs, i, j, k);
+                if (ob > 0. && A(*id, i, j, k) != 1 && der_t == 1) A(*a1, i, j, k) = 0.;
+                if (A(*id, i, j, k) != 1) continue;
+                double image;
+                if (ob < er) {
+                    image = A(*a1, i, j, k);
+                } else {
+                    if (k == 1 && dimz >= 2) A(nzv, i, j, k) = A(nzv, i, j, k + 1);
+                    double imp[2];
+                    for (int l = 1; l <= ll; ++l) {
+                        double xl = XC(i) - (l * dx + ob) * A(nxv, i, j, k);
+                        double yl = YC(j) - (l * dy + ob) * A(nyv, i, j, k);
+                        double zl = ZC(k) - (l * dz + ob) * A(nzv, i, j, k);
+                        int ii = (int)floor((xl - XC(i)) / dx) + i;
+                        int jj = (int)floor((yl - YC(j)) / dy) + j;
+                        int kk = (int)floor((zl - ZC(k)) / dz) + k;
+                        double lint[8], sl = 0., sv = 0.;
+                        int oi[8] = {0, 1, 0, 0, 1, 1, 0, 1}, oj[8] = {0, 0, 1, 0, 1, 0, 1, 1}, okk[8] = {0, 0, 0, 1, 0, 1, 1, 1};
+                        for (int q = 0; q < 8; ++q) {
+                            int I = ii + oi[q], J = jj + oj[q], K = kk + okk[q];
+                            double ddx = xl - XC(I), ddy = yl - YC(J), ddz = zl - ZC(K);
+                            lint[q] = 1. / (sqrt(pow(ddx, 2.) + pow(ddy, 2.) + pow(ddz, 2.))) * (1. - id_at(id, I, J, K));
+                        }
+                        for (int q = 0; q < 8; ++q) sl += lint[q];
+                        for (int q = 0; q < 8; ++q) {
+                            int I = ii + oi[q], J = jj + oj[q], K = kk + okk[q];
+                            int Ic = I < a1->lo[0] ? a1->lo[0] : (I > a1->hi[0] ? a1->hi[0] : I);
+                            int Jc = J < a1->lo[1] ? a1->lo[1] : (J > a1->hi[1] ? a1->hi[1] : J);
+                            int Kc = K < a1->lo[2] ? a1->lo[2] : (K > a1->hi[2] ? a1->hi[2] : K);
+                            lint[q] = lint[q] * A(*a1, Ic, Jc, Kc);
+                        }
+                        for (int q = 0; q < 8; ++q) sv += lint[q];
+                        imp[l - 1] = sv / sl;
+                        if (sl == 0) imp[l - 1] = 0.;
+                    }
+                    double li1 = (2. * deltai - ob) / deltai * (2. * ob) / (deltai + ob);
+                    double li2 = (ob - deltai) / deltai * (2. * ob) / (2. * deltai + ob);
+                    double lg = (ob - deltai) / (ob + deltai) * (ob - 2. * deltai) / (ob + 2. * deltai);
+                    if (der_t == 1) image = (2. * lg * v_sol + li1 * imp[0] + li2 * imp[1]) / (1. + lg);
+                    else image = (2. * lg * imp[0] + li1 * imp[0] + li2 * imp[1]) / (1. + lg);
+                }
+                if (der_t == 1) A(*a1, i, j, k) = 2. * v_sol - image;
+                else A(*a1, i, j, k) = image;
+            }
+#undef XC
+#undef YC
+#undef ZC
+    fr(&mod); fr(&nxv); fr(&nyv); fr(&nzv);
+}
+
+/* Vertical cylinder obstacle (build extension, obst_t = 4): phi_s = R - r on
+ * the half-cell sub-grid of obstaculo(), 3_contorno.f90:829-841 style, then
+ * sampled onto the staggered locations as :951-989. */
+void or_obstaculo_cylinder(or_case *c, double xc, double yc, double R)
+{
+    int nx = c->nx, ny = c->ny, nz = c->nz, nx1 = c->nx1, ny1 = c->ny1, nz1 = c->nz1;
+#define PHI(ii, jj) (R - sqrt(pow((((ii) - 1.) * c->dx * 0.5 - xc), 2.) + pow((((jj) - 1.) * c->dy * 0.5 - yc), 2.)))
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx1; ++i) A(c->obs_lsx, i, j, k) = PHI(i * 2 - 1, j * 2);
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny1; ++j)
+            for (int i = 1; i <= nx; ++i) A(c->obs_lsy, i, j, k) = PHI(i * 2, j * 2 - 1);
+    for (int k = 1; k <= nz1; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i) A(c->obs_lsz, i, j, k) = PHI(i * 2, j * 2);
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i) A(c->obs_lss, i, j, k) = PHI(i * 2, j * 2);
+#undef PHI
+}
+
+/* obstaculo() tail for ibm_t = 2, 3_contorno.f90:991-1004 */
+void or_ibm_setup(or_case *c)
+{
+    int nx = c->nx, ny = c->ny, nz = c->nz, nx1 = c->nx1, ny1 = c->ny1, nz1 = c->nz1;
+    int l = c->p.reinit_max_iter;
+    reinic_weno(c, &c->obs_lsx, nx1, ny, nz, l, -1);
+    reinic_weno(c, &c->obs_lsy, nx, ny1, nz, l, -1);
+    reinic_weno(c, &c->obs_lsz, nx, ny, nz1, l, -1);
+    reinic_weno(c, &c->obs_lss, nx, ny, nz, l, -1);
+    ibm_posicoes(&c->id_ibmx, &c->obs_lsx, nx1, ny, nz);
+    ibm_posicoes(&c->id_ibmy, &c->obs_lsy, nx, ny1, nz);
+    ibm_posicoes(&c->id_ibmz, &c->obs_lsz, nx, ny, nz1);
+    ibm_posicoes(&c->id_ibm, &c->obs_lss, nx, ny, nz);
+}
+
+/* ------------------------------------------------------------------------ */
+/* 9_grad.f90:10-663 -- graddin (Jacobi-scaled CG)                           */
+/* ------------------------------------------------------------------------ */
+static void ghost_fill_cg(const or_case *c, F3 *m)
+{   /* Neumann copy or periodic, x then y then z (:191-239 and repeats) */
+    int nx = c->nx, ny = c->ny, nz = c->nz, nx1 = c->nx1, ny1 = c->ny1, nz1 = c->nz1;
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k <= nz1; ++k)
+        for (int j = 0; j <= ny1; ++j) {
+            if (c->p.ccx0 == 0) { A(*m, 0, j, k) = A(*m, nx, j, k); A(*m, nx + 1, j, k) = A(*m, 1, j, k); }
+            else { A(*m, 0, j, k) = A(*m, 1, j, k); A(*m, nx + 1, j, k) = A(*m, nx, j, k); }
+        }
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k <= nz1; ++k)
+        for (int i = 0; i <= nx1; ++i) {
+            if (c->p.ccy0 == 0) { A(*m, i, 0, k) = A(*m, i, ny, k); A(*m, i, ny + 1, k) = A(*m, i, 1, k); }
+            else { A(*m, i, 0, k) = A(*m, i, 1, k); A(*m, i, ny + 1, k) = A(*m, i, ny, k); }
+        }
+#pragma omp parallel for schedule(static)
+    for (int j = 0; j <= ny1; ++j)
+        for (int i = 0; i <= nx1; ++i) { A(*m, i, j, 0) = A(*m, i, j, 1); A(*m, i, j, nz + 1) = A(*m, i, j, nz); }
+}
+
+int or_graddin(or_case *c)
+{
+    int nx = c->nx, ny = c->ny, nz = c->nz, nx1 = c->nx1, ny1 = c->ny1, nz1 = c->nz1;
+    double dx = c->dx, dy = c->dy, dz = c->dz, dt = c->dt;
+    int par = (c->p.omp_t != 0);
+    F3 spi = tmp3(1, nx1, 1, ny, 1, nz), spj = tmp3(1, nx, 1, ny1, 1, nz), spk = tmp3(1, nx, 1, ny, 1, nz1);
+    F3 qpr = tmp3(1, nx, 1, ny, 1, nz);
+    F3 dpr = tmp3(0, nx1, 0, ny1, 0, nz1), epr = tmp3(0, nx1, 0, ny1, 0, nz1), err = tmp3(0, nx1, 0, ny1, 0, nz1),
+       errp = tmp3(0, nx1, 0, ny1, 0, nz1), mp = tmp3(0, nx1, 0, ny1, 0, nz1);
+    F3 rhox = tmp3(1, nx1, 1, ny, 1, nz), rhoy = tmp3(1, nx, 1, ny1, 1, nz), rhoz = tmp3(1, nx, 1, ny, 1, nz1);
+    int ibm_mask = (c->p.obst_t != 0 && c->p.ibm_t == 2);
+
+    double aux1 = dt / (dx * dx), aux2 = dt / (dy * dy), aux3 = dt / (dz * dz);
+    interpx_cf(c, &c->rho, nx, ny, nz, &rhox);
+    interpy_cf(&c->rho, nx, ny, nz, &rhoy);
+    interpz_cf(&c->rho, nx, ny, nz, &rhoz);
+#pragma omp parallel for schedule(static)
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx1; ++i) A(spi, i, j, k) = aux1 / A(rhox, i, j, k);
+#pragma omp parallel for schedule(static)
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny1; ++j)
+            for (int i = 1; i <= nx; ++i) A(spj, i, j, k) = aux2 / A(rhoy, i, j, k);
+#pragma omp parallel for schedule(static)
+    for (int k = 1; k <= nz1; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i) A(spk, i, j, k) = aux3 / A(rhoz, i, j, k);
+#pragma omp parallel for schedule(static)
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i) {
+                A(dpr, i, j, k) = A(spi, i + 1, j, k) + A(spi, i, j, k) + A(spj, i, j + 1, k) + A(spj, i, j, k) +
+                                  A(spk, i, j, k + 1) + A(spk, i, j, k);
+                double u1a, u1b, v1a, v1b, w1a, w1b;
+                if (ibm_mask) {   /* :45-88 */
+                    u1a = A(c->obs_lsx, i, j, k) >= 0. ? 0. : A(c->u, i, j, k);
+                    u1b = A(c->obs_lsx, i + 1, j, k) >= 0. ? 0. : A(c->u, i + 1, j, k);
+                    v1a = A(c->obs_lsy, i, j, k) >= 0. ? 0. : A(c->v, i, j, k);
+                    v1b = A(c->obs_lsy, i, j + 1, k) >= 0. ? 0. : A(c->v, i, j + 1, k);
+                    w1a = A(c->obs_lsz, i, j, k) >= 0. ? 0. : A(c->w, i, j, k);
+                    w1b = A(c->obs_lsz, i, j, k + 1) >= 0. ? 0. : A(c->w, i, j, k + 1);
+                } else {
+                    u1a = A(c->u, i, j, k); u1b = A(c->u, i + 1, j, k);
+                    v1a = A(c->v, i, j, k); v1b = A(c->v, i, j + 1, k);
+                    w1a = A(c->w, i, j, k); w1b = A(c->w, i, j, k + 1);
+                }
+                A(qpr, i, j, k) = (u1a - u1b) / dx + (v1a - v1b) / dy + (w1a - w1b) / dz;
+            }
+    ghost_fill_cg(c, &dpr);
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k <= nz1; ++k)
+        for (int j = 0; j <= ny1; ++j)
+            for (int i = 0; i <= nx1; ++i) A(epr, i, j, k) = A(c->prd1, i, j, k) * sqrt(A(dpr, i, j, k));
+    /* the reference's prd1 has no index nx1 = nx+1 beyond its ghost; (0:nx+1)
+     * equals (0:nx1), so the loop above stays in bounds */
+#pragma omp parallel for schedule(static)
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx1; ++i) A(spi, i, j, k) = A(spi, i, j, k) / sqrt(A(dpr, i, j, k) * A(dpr, i - 1, j, k));
+#pragma omp parallel for schedule(static)
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny1; ++j)
+            for (int i = 1; i <= nx; ++i) A(spj, i, j, k) = A(spj, i, j, k) / sqrt(A(dpr, i, j, k) * A(dpr, i, j - 1, k));
+#pragma omp parallel for schedule(static)
+    for (int k = 1; k <= nz1; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i) A(spk, i, j, k) = A(spk, i, j, k) / sqrt(A(dpr, i, j, k) * A(dpr, i, j, k - 1));
+#pragma omp parallel for schedule(static)
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i)
+                A(err, i, j, k) = A(epr, i, j, k) - A(spi, i + 1, j, k) * A(epr, i + 1, j, k) - A(spi, i, j, k) * A(epr, i - 1, j, k) -
+                                  A(spj, i, j + 1, k) * A(epr, i, j + 1, k) - A(spj, i, j, k) * A(epr, i, j - 1, k) -
+                                  A(spk, i, j, k + 1) * A(epr, i, j, k + 1) - A(spk, i, j, k) * A(epr, i, j, k - 1) -
+                                  A(qpr, i, j, k) / sqrt(A(dpr, i, j, k));
+    double alfamupr = 0., bnorm2 = 0.;
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i) {
+                alfamupr = alfamupr + A(err, i, j, k) * A(err, i, j, k);
+                double bq = A(qpr, i, j, k) / sqrt(A(dpr, i, j, k));
+                bnorm2 = bnorm2 + bq * bq;
+            }
+    ghost_fill_cg(c, &err);
+    f3_copy(&errp, &err);
+
+    int cont = 0;
+    double res = fabs(alfamupr);
+    double thr;
+    if (c->p.cg_tol_mode == SULI_CG_TOL_REL) thr = c->p.cg_tol * c->p.cg_tol * bnorm2;
+    else thr = c->p.cg_tol / (double)(nx * ny * nz);
+    int replay = c->replay_cg[(c->tt >= 1 && c->tt <= 3) ? c->tt - 1 : 0];
+    int maxit = c->p.cg_max_iter;
+    for (;;) {
+        if (replay >= 0) { if (cont >= replay) break; }
+        else if (!((res > thr) && (cont < maxit))) break;
+        cont = cont + 1;
+        double alfadipr = 0., betamupr = 0.;
+#pragma omp parallel for schedule(static)
+        for (int k = 1; k <= nz; ++k)
+            for (int j = 1; j <= ny; ++j)
+                for (int i = 1; i <= nx; ++i)
+                    A(mp, i, j, k) = A(errp, i, j, k) - A(errp, i + 1, j, k) * A(spi, i + 1, j, k) - A(errp, i - 1, j, k) * A(spi, i, j, k) -
+                                     A(errp, i, j + 1, k) * A(spj, i, j + 1, k) - A(errp, i, j - 1, k) * A(spj, i, j, k) -
+                                     A(errp, i, j, k + 1) * A(spk, i, j, k + 1) - A(errp, i, j, k - 1) * A(spk, i, j, k);
+        if (!par) {
+            for (int k = 1; k <= nz; ++k)
+                for (int j = 1; j <= ny; ++j)
+                    for (int i = 1; i <= nx; ++i) alfadipr = alfadipr + A(errp, i, j, k) * A(mp, i, j, k);
+        } else {
+#pragma omp parallel for schedule(static) reduction(+ : alfadipr)
+            for (int k = 1; k <= nz; ++k)
+                for (int j = 1; j <= ny; ++j)
+                    for (int i = 1; i <= nx; ++i) alfadipr = alfadipr + A(errp, i, j, k) * A(mp, i, j, k);
+        }
+        double alfapr = alfamupr / alfadipr;
+#pragma omp parallel for schedule(static)
+        for (int k = 1; k <= nz; ++k)
+            for (int j = 1; j <= ny; ++j)
+                for (int i = 1; i <= nx; ++i) {
+                    A(epr, i, j, k) = A(epr, i, j, k) - alfapr * A(errp, i, j, k);
+                    A(err, i, j, k) = A(err, i, j, k) - alfapr * A(mp, i, j, k);
+                }
+        if (!par) {
+            for (int k = 1; k <= nz; ++k)
+                for (int j = 1; j <= ny; ++j)
+                    for (int i = 1; i <= nx; ++i) betamupr = betamupr + A(err, i, j, k) * A(err, i, j, k);
+        } else {
+#pragma omp parallel for schedule(static) reduction(+ : betamupr)
+            for (int k = 1; k <= nz; ++k)
+                for (int j = 1; j <= ny; ++j)
+                    for (int i = 1; i <= nx; ++i) betamupr = betamupr + A(err, i, j, k) * A(err, i, j, k);
+        }
+        double betapr = betamupr / alfamupr;
+        alfamupr = betamupr;
+#pragma omp parallel for schedule(static)
+        for (int k = 1; k <= nz; ++k)
+            for (int j = 1; j <= ny; ++j)
+                for (int i = 1; i <= nx; ++i) A(errp, i, j, k) = A(err, i, j, k) + betapr * A(errp, i, j, k);
+        ghost_fill_cg(c, &errp);
+        res = fabs(alfamupr);
+    }
+    int ti = (c->tt >= 1 && c->tt <= 3) ? c->tt - 1 : 0;
+    c->cg_iters[ti] = cont;
+    c->cg_res[ti] = res;
+    ghost_fill_cg(c, &epr);
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k <= nz + 1; ++k)
+        for (int j = 0; j <= ny + 1; ++j)
+            for (int i = 0; i <= nx + 1; ++i) A(c->prd1, i, j, k) = A(epr, i, j, k) / sqrt(A(dpr, i, j, k));
+    fr(&spi); fr(&spj); fr(&spk); fr(&qpr); fr(&dpr); fr(&epr); fr(&err); fr(&errp); fr(&mp);
+    fr(&rhox); fr(&rhoy); fr(&rhoz);
+    return cont;
+}
+
+/* ------------------------------------------------------------------------ */
+/* 10_pos.f90:1-46,95 -- posdin (t_press = 1)                                */
+/* ------------------------------------------------------------------------ */
+void or_posdin(or_case *c)
+{
+    int nx = c->nx, ny = c->ny, nz = c->nz, nx1 = c->nx1, ny1 = c->ny1, nz1 = c->nz1;
+    double aux1 = c->dt / c->dx, aux2 = c->dt / c->dy;
+    F3 rhox = tmp3(1, nx1, 1, ny, 1, nz), rhoy = tmp3(1, nx, 1, ny1, 1, nz), rhoz = tmp3(1, nx, 1, ny, 1, nz1);
+    interpx_cf(c, &c->rho, nx, ny, nz, &rhox);
+    interpy_cf(&c->rho, nx, ny, nz, &rhoy);
+    interpz_cf(&c->rho, nx, ny, nz, &rhoz);
+    for (int k = 1; k <= nz; ++k) {
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx1; ++i)
+                A(c->u, i, j, k) = A(c->u, i, j, k) - aux1 * (A(c->prd1, i, j, k) - A(c->prd1, i - 1, j, k)) / A(rhox, i, j, k);
+        for (int j = 1; j <= ny1; ++j)
+            for (int i = 1; i <= nx; ++i)
+                A(c->v, i, j, k) = A(c->v, i, j, k) - aux2 * (A(c->prd1, i, j, k) - A(c->prd1, i, j - 1, k)) / A(rhoy, i, j, k);
+    }
+    for (int k = 1; k <= nz1; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i)
+                A(c->w, i, j, k) = A(c->w, i, j, k) - c->dt / c->dz * (A(c->prd1, i, j, k) - A(c->prd1, i, j, k - 1)) / A(rhoz, i, j, k);
+    f3_copy(&c->prd, &c->prd1);
+    fr(&rhox); fr(&rhoy); fr(&rhoz);
+}
+
+/* 4_plot.f90:386-394 */
+double or_conmassa(or_case *c)
+{
+    double m = 0.;
+    for (int k = 1; k <= c->nz; ++k)
+        for (int j = 1; j <= c->ny; ++j)
+            for (int i = 1; i <= c->nx; ++i) {
+                double d = (A(c->u, i + 1, j, k) - A(c->u, i, j, k)) / c->dx + (A(c->v, i, j + 1, k) - A(c->v, i, j, k)) / c->dy +
+                           (A(c->w, i, j, k + 1) - A(c->w, i, j, k)) / c->dz;
+                A(c->div, i, j, k) = d;
+                if (fabs(d) > m) m = fabs(d);
+            }
+    c->maxdiv = m;
+    return m;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Initial conditions                                                        */
+/* ------------------------------------------------------------------------ */
+/* level_set_ini, 14_level_set.f90:44-129 (tipo 1, 3, 4) */
+void or_level_set_ini(or_case *c, int tipo, double ampl, double lambdax, double lambday, double prof, double m)
+{
+    const double pi = c->pi;
+    for (int k = 1; k <= c->nz; ++k)
+        for (int j = 1; j <= c->ny; ++j)
+            for (int i = 1; i <= c->nx; ++i) {
+                double x = (i - 0.5) * c->dx, y = (j - 0.5) * c->dy, z = (k - 0.5) * c->dz;
+                double val = 0.;
+                if (tipo == 1) {
+                    double dz_;
+                    if (lambday != 0.) dz_ = cos(2. * pi / lambday * y);
+                    else if (lambdax == 0) dz_ = 0.;
+                    else dz_ = 1.;
+                    if (lambdax != 0.) dz_ = -ampl * dz_ * cos(2. * pi / lambdax * x);
+                    val = dz_ - z + prof;
+                } else if (tipo == 3) {
+                    double lsaux = pow(z - prof, m) + pow(x - lambdax, m) + pow(y - lambday, m) / pow(10., m);
+                    val = -pow(lsaux, 1. / m);
+                    val = val + ampl;
+                } else if (tipo == 4) {
+                    double lsaux = pow(x - lambdax, m) / 2. + pow(y - lambday, m) / 2. + pow(z - prof, m) / 2.;
+                    val = -pow(lsaux, 1. / m);
+                    val = val + ampl;
+                }
+                A(c->ls, i, j, k) = val;
+            }
+}
+
+void or_heaviside_init(or_case *c)
+{
+    heaviside(c);
+    c->vol_ini = volume(c);     /* 14_level_set.f90:187-194 */
+    c->vol_ins = c->vol_ini;
+}
+
+/* iniciais, 2_iniciais.f90:294-399 (no wave, no k-model) */
+void or_iniciais_velocity(or_case *c)
+{
+    memset(c->v.p, 0, sizeof(double) * (size_t)f3_size(&c->v));
+    memset(c->w.p, 0, sizeof(double) * (size_t)f3_size(&c->w));
+    memset(c->prd1.p, 0, sizeof(double) * (size_t)f3_size(&c->prd1));
+    memset(c->prd.p, 0, sizeof(double) * (size_t)f3_size(&c->prd));
+    long n = f3_size(&c->u);
+    for (long q = 0; q < n; ++q) c->u.p[q] = c->p.uinicial;
+    n = f3_size(&c->bxx0);
+    for (long q = 0; q < n; ++q) { c->bxx0.p[q] = c->p.uinicial; c->bxx1.p[q] = c->p.uinicial; }
+    for (int k = 1; k <= c->nz; ++k)
+        for (int j = 1; j <= c->ny; ++j) A(c->blx1, j, k, 0) = A(c->ls, 1, j, k);   /* 14_level_set.f90:196-198 */
+    c->t = 0.; c->it = 0;
+}
+
+/* mms_i, 13_mms.f90:39-114 (a = 0, h0 = 2) */
+void or_mms_init(or_case *c)
+{
+    const double a = 0., h0 = 2., pi = c->pi;
+    for (int k = 1; k <= c->nz; ++k)
+        for (int j = 1; j <= c->ny; ++j)
+            for (int i = 1; i <= c->nx; ++i) {
+                double x = (i - 0.5) * c->dx, y = (j - 0.5) * c->dy, z = (k - 0.5) * c->dz;
+                A(c->ls, i, j, k) = a * sin(x) * sin(y) + h0 - z;
+            }
+    for (int k = 1; k <= c->nz; ++k) {
+        double z = (k - 0.5) * c->dz;
+        for (int j = 1; j <= c->ny; ++j) {
+            double y = (j - 0.5) * c->dy;
+            for (int i = 1; i <= c->nx1; ++i) {
+                double x = (i - 1.0) * c->dx;
+                double h = a * sin(x) * sin(y) + h0;
+                A(c->u, i, j, k) = sin(x) * cos(y) * sin(pi * 0.5 * z / h) - cos(x) * sin(y) * (cos(pi * 2. * z / h) - 1.);
+            }
+        }
+    }
+    for (int k = 1; k <= c->nz; ++k) {
+        double z = (k - 0.5) * c->dz;
+        for (int j = 1; j <= c->ny1; ++j) {
+            double y = (j - 1.0) * c->dy;
+            for (int i = 1; i <= c->nx; ++i) {
+                double x = (i - 0.5) * c->dx;
+                double h = a * sin(x) * sin(y) + h0;
+                A(c->v, i, j, k) = -cos(x) * sin(y) * sin(pi * 0.5 * z / h) + sin(x) * cos(y) * (cos(pi * 2. * z / h) - 1.);
+            }
+        }
+    }
+    for (int k = 1; k <= c->nz1; ++k) {
+        double z = (k - 1.0) * c->dz;
+        for (int j = 1; j <= c->ny; ++j) {
+            double y = (j - 0.5) * c->dy;
+            for (int i = 1; i <= c->nx; ++i) {
+                double x = (i - 0.5) * c->dx;
+                double h = a * sin(x) * sin(y) + h0;
+                A(c->w, i, j, k) = -a * (pow(sin(x), 2.) * pow(cos(y), 2.) - pow(cos(x), 2.) * pow(sin(y), 2.)) *
+                                   (sin(2. * pi * z / h) - 2. * pi * z / h * cos(2. * pi * z / h) + 2. * pi) / (2. * pi);
+            }
+        }
+    }
+}
+
+/* analytic MMS fields at a point (13_mms.f90:275-310) */
+static double mms_u(double x, double y, double z, double pi)
+{
+    double h = 0. * sin(x) * sin(y) + 2.;
+    return sin(x) * cos(y) * sin(pi * 0.5 * z / h) - cos(x) * sin(y) * (cos(pi * 2. * z / h) - 1.);
+}
+static double mms_v(double x, double y, double z, double pi)
+{
+    double h = 0. * sin(x) * sin(y) + 2.;
+    return -cos(x) * sin(y) * sin(pi * 0.5 * z / h) + sin(x) * cos(y) * (cos(pi * 2. * z / h) - 1.);
+}
+
+/* mms error, 13_mms.f90:391-451 (mms_t = 1: w_m = 0 and p_m = 0 for a = 0) */
+void or_mms_error(or_case *c, double err[4])
+{
+    int nx = c->nx, ny = c->ny, nz = c->nz, nx1 = c->nx1, ny1 = c->ny1, nz1 = c->nz1;
+    F3 lsx = tmp3(1, nx1, 1, ny, 1, nz), lsy = tmp3(1, nx, 1, ny1, 1, nz), lsz = tmp3(1, nx, 1, ny, 1, nz1);
+    interpx_cf(c, &c->ls, nx, ny, nz, &lsx);
+    interpy_cf(&c->ls, nx, ny, nz, &lsy);
+    interpz_cf(&c->ls, nx, ny, nz, &lsz);
+    double su = 0, sv = 0, sw = 0, sp = 0;
+    long nu = 0, nv = 0, nw = 0, np_ = 0;
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx1; ++i)
+                if (A(lsx, i, j, k) > 0.) {
+                    double d = mms_u((i - 1.0) * c->dx, (j - 0.5) * c->dy, (k - 0.5) * c->dz, c->pi) - A(c->u, i, j, k);
+                    su += d * d; nu++;
+                }
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny1; ++j)
+            for (int i = 1; i <= nx; ++i)
+                if (A(lsy, i, j, k) > 0.) {
+                    double d = mms_v((i - 0.5) * c->dx, (j - 1.0) * c->dy, (k - 0.5) * c->dz, c->pi) - A(c->v, i, j, k);
+                    sv += d * d; nv++;
+                }
+    for (int k = 1; k <= nz1; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i)
+                if (A(lsz, i, j, k) > 0.) {
+                    double d = 0. - A(c->w, i, j, k);
+                    sw += d * d; nw++;
+                }
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i)
+                if (A(c->ls, i, j, k) > 0.) {
+                    double d = 0. - A(c->prd1, i, j, k);
+                    sp += d * d; np_++;
+                }
+    err[0] = sqrt(su / (double)(nu ? nu : 1));
+    err[1] = sqrt(sv / (double)(nv ? nv : 1));
+    err[2] = sqrt(sw / (double)(nw ? nw : 1));
+    err[3] = sqrt(sp / (double)(np_ ? np_ : 1));
+    fr(&lsx); fr(&lsy); fr(&lsz);
+}
+
+/* termo_fonte1, 13_mms.f90:820-1065, restated for a = 0 (every term carrying
+ * a factor a, dh/dx, dh/dy or their derivatives vanishes; h = h0). */
+void or_termo_fonte1(or_case *c)
+{
+    const double pi = c->pi, h0 = 2.;
+    const double hpi = 0.5 * pi, dpi = 2.0 * pi;
+    const double visc = 0.00100798 / 998.;
+    const double h1 = h0, h2 = h1 * h1;
+    (void)h2;
+    for (int k = 1; k <= c->nz; ++k)
+        for (int j = 1; j <= c->ny; ++j)
+            for (int i = 1; i <= c->nx1; ++i) {
+                double x = (i - 1.0) * c->dx, y = (j - 0.5) * c->dy, z = (k - 0.5) * c->dz;
+                double zh1 = z / h1;
+                double ux = sin(x) * cos(y) * sin(hpi * zh1) - cos(x) * sin(y) * (cos(dpi * zh1) - 1.);
+                double vx = -cos(x) * sin(y) * sin(hpi * zh1) + sin(x) * cos(y) * (cos(dpi * zh1) - 1.);
+                double dudx = cos(x) * cos(y) * sin(hpi * zh1) + sin(x) * sin(y) * (cos(dpi * zh1) - 1.);
+                double dudy = -sin(x) * sin(y) * sin(hpi * zh1) - cos(x) * cos(y) * (cos(dpi * zh1) - 1.);
+                double dudz = (hpi / h1) * sin(x) * cos(y) * cos(hpi * zh1) + (dpi / h1) * cos(x) * sin(y) * sin(dpi * zh1);
+                double d2udx2 = -ux;
+                double d2udy2 = -ux;
+                double d2udz2 = -pow(hpi / h1, 2.) * sin(x) * cos(y) * sin(hpi * zh1) + pow(dpi / h1, 2.) * cos(x) * sin(y) * cos(dpi * zh1);
+                double d2vdxy = sin(x) * cos(y) * sin(hpi * zh1) - cos(x) * sin(y) * (cos(dpi * zh1) - 1.0);
+                double d2wdxz = 0.;
+                A(c->tf_u, i, j, k) = ux * dudx + vx * dudy + 0. * dudz - visc * (d2udx2 + d2udy2 + d2udz2 + d2udx2 + d2vdxy + d2wdxz);
+            }
+    for (int k = 1; k <= c->nz; ++k)
+        for (int j = 1; j <= c->ny1; ++j)
+            for (int i = 1; i <= c->nx; ++i) {
+                double x = (i - 0.5) * c->dx, y = (j - 1.0) * c->dy, z = (k - 0.5) * c->dz;
+                double zh1 = z / h1;
+                double uy = sin(x) * cos(y) * sin(hpi * zh1) - cos(x) * sin(y) * (cos(dpi * zh1) - 1.);
+                double vy = -cos(x) * sin(y) * sin(hpi * zh1) + sin(x) * cos(y) * (cos(dpi * zh1) - 1.);
+                double dvdx = sin(x) * sin(y) * sin(hpi * zh1) + cos(x) * cos(y) * (cos(dpi * zh1) - 1.0);
+                double dvdy = -cos(x) * cos(y) * sin(hpi * zh1) - sin(x) * sin(y) * (cos(dpi * zh1) - 1.0);
+                double dvdz = -(hpi / h1) * cos(x) * sin(y) * cos(hpi * zh1) - sin(x) * cos(y) * (dpi / h1) * sin(dpi * zh1);
+                double d2vdx2 = -vy;
+                double d2vdy2 = -vy;
+                double d2vdz2 = pow(hpi / h1, 2) * cos(x) * sin(y) * sin(hpi * zh1) - sin(x) * cos(y) * pow(dpi / h1, 2) * cos(dpi * zh1);
+                double d2udxy = -cos(x) * sin(y) * sin(hpi * zh1) + sin(x) * cos(y) * (cos(dpi * zh1) - 1.0);
+                double d2wdyz = 0.;
+                A(c->tf_v, i, j, k) = uy * dvdx + vy * dvdy + 0. * dvdz - visc * (d2vdx2 + d2vdy2 + d2vdz2 + d2udxy + d2vdy2 + d2wdyz);
+            }
+    for (int k = 1; k <= c->nz1; ++k)
+        for (int j = 1; j <= c->ny; ++j)
+            for (int i = 1; i <= c->nx; ++i) {
+                double x = (i - 0.5) * c->dx, y = (j - 0.5) * c->dy, z = (k - 1.0) * c->dz;
+                double zh1 = z / h1;
+                double d2vdyz = -cos(x) * cos(y) * (hpi / h1) * cos(hpi * zh1) + sin(x) * sin(y) * (dpi / h1) * sin(dpi * zh1);
+                double d2udxz = cos(x) * cos(y) * (hpi / h1) * cos(hpi * zh1) - sin(x) * sin(y) * (dpi / h1) * sin(dpi * zh1);
+                A(c->tf_w, i, j, k) = -visc * (d2udxz + d2vdyz);
+            }
+}
+
+/* ------------------------------------------------------------------------ */
+/* The time loop body, 1_principal.f90:69-124                                */
+/* ------------------------------------------------------------------------ */
+void or_set_stage(or_case *c, int tt)
+{
+    c->tt = tt;
+    c->dt = c->a_dt[tt - 1];
+}
+
+void or_step(or_case *c)
+{
+    c->it = c->it + 1;
+    c->t = c->t + c->dt;
+    or_level_set(c);
+    or_contorno(c, 3);
+    or_visco(c);
+    for (int tt = 1; tt <= c->ntt; ++tt) {
+        or_set_stage(c, tt);
+        or_convdiff(c);
+        or_complementos(c);
+        or_tempo(c);
+        or_contorno(c, 2);
+        if (c->p.mms_t == 0 || c->p.project_under_mms) {
+            or_graddin(c);
+            or_posdin(c);
+            or_contorno(c, 1);
+        }
+    }
+    or_conmassa(c);
+}

@@ -1,0 +1,197 @@
+"""Synthetic workloads of the SuLi hot path and their initial conditions.
+
+Host-side set-up only (the reference runs it once on the host too:
+iniciais() 2_iniciais.f90:127-274 and level_set_ini() 14_level_set.f90:10-200).
+Each builder returns a Case: the suli_params of the run plus the initial
+fields in the reference layout (Fortran order, reference lower bounds), ready
+for upload.  No public dataset is involved: every input is generated here
+from the workload's stated shapes and seeded distributions.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+from ._abi import CG_TOL_ABS, CG_TOL_REL, PREC_FP64, SuliParams, default_params, field_shape
+
+
+@dataclasses.dataclass
+class Case:
+    name: str
+    params: SuliParams
+    fields: dict            # name -> np.ndarray (Fortran order)
+    steps: int              # steps the workload is quoted on
+    obstacle: dict | None = None   # cylinder description for IBM set-up
+
+    @property
+    def cells(self) -> int:
+        return self.params.nx * self.params.ny * self.params.nz
+
+
+def _centres(n, h):
+    return (np.arange(1, n + 1) - 0.5) * h
+
+
+def _zeros(p, name):
+    return np.zeros(field_shape(p, name), order="F")
+
+
+def level_set_tipo(p: SuliParams, tipo: int, ampl=0.0, lambdax=0.0, lambday=0.0, prof=0.0, m=30.0):
+    """level_set_ini() 14_level_set.f90:56-129 for tipo 1 (wave), 3 (dam), 4 (drop)."""
+    x = _centres(p.nx, p.dx)[:, None, None]
+    y = _centres(p.ny, p.dy)[None, :, None]
+    z = _centres(p.nz, p.dz)[None, None, :]
+    if tipo == 1:
+        if lambday != 0.0:
+            d = np.cos(2.0 * math.pi / lambday * y) + 0.0 * x
+        elif lambdax == 0.0:
+            d = np.zeros((1, 1, 1))
+        else:
+            d = np.ones((1, 1, 1))
+        if lambdax != 0.0:
+            d = -ampl * d * np.cos(2.0 * math.pi / lambdax * x)
+        ls = d - z + prof
+    elif tipo == 3:
+        lsaux = np.power(z - prof, m) + np.power(x - lambdax, m) + np.power(y - lambday, m) / np.power(10.0, m)
+        ls = -np.power(lsaux, 1.0 / m) + ampl
+    elif tipo == 4:
+        lsaux = np.power(x - lambdax, m) / 2.0 + np.power(y - lambday, m) / 2.0 + np.power(z - prof, m) / 2.0
+        ls = -np.power(lsaux, 1.0 / m) + ampl
+    else:
+        raise ValueError(f"tipo {tipo} not supported")
+    out = np.empty((p.nx, p.ny, p.nz), order="F")
+    out[...] = ls
+    return out
+
+
+def _base_fields(p: SuliParams, ls: np.ndarray) -> dict:
+    """iniciais() 2_iniciais.f90:294-399: v = w = prd = 0, u = uinicial."""
+    f = {"LS": np.asfortranarray(ls)}
+    u = _zeros(p, "U")
+    u[...] = p.uinicial
+    f["U"] = u
+    f["V"] = _zeros(p, "V")
+    f["W"] = _zeros(p, "W")
+    f["PRD1"] = _zeros(p, "PRD1")
+    bx = _zeros(p, "BXX0")
+    bx[...] = p.uinicial
+    f["BXX0"] = bx
+    f["BXX1"] = bx.copy()
+    f["BLX1"] = np.asfortranarray(ls[0, :, :].reshape(p.ny, p.nz, 1))
+    return f
+
+
+def dam_break(nx=64, ny=32, nz=32, precision=PREC_FP64, reinit_iters=5, cg_tol=1e-10) -> Case:
+    """Plain FP64 3-D dam break: 1.0 x 0.5 x 0.5 m box, water column x<0.25,
+    z<0.25 (tipo 3, ampl 0.25, m 30), rho 1000/1.2, mu 1e-3/1.8e-5, g 9.81,
+    no-slip walls, dt 1e-4, no LES, no IBM; 200 steps."""
+    lx = 1.0
+    h = lx / nx
+    p = default_params(nx=nx, ny=ny, nz=nz, dx=h, dy=h, dz=h, dt=1e-4,
+                       ccx0=2, ccxf=2, ccy0=2, ccyf=2, ccz0=2, cczf=2,
+                       gx=0.0, gz=9.81, rho_f1=1.2, mu_f1=1.8e-5, rho_f2=1000.0, mu_f2=1e-3,
+                       m_turb=0, reinit_max_iter=reinit_iters, cg_tol_mode=CG_TOL_REL,
+                       cg_tol=cg_tol, precision=precision)
+    ls = level_set_tipo(p, 3, ampl=0.25, lambdax=0.0, lambday=0.0, prof=0.0, m=30.0)
+    return Case("dam_break_%dx%dx%d" % (nx, ny, nz), p, _base_fields(p, ls), steps=200)
+
+
+def wave_tank(nx=1024, ny=256, nz=256, precision=PREC_FP64, dt=2e-4, cg_tol=1e-8) -> Case:
+    """Large wave tank: 8 x 2 x 2 m, depth 1.0 m, eta = 0.05 sin(2 pi x / 2),
+    still water, Smagorinsky LES (Cs 0.1), closed free-slip tank; 1000 steps."""
+    h = 8.0 / nx
+    p = default_params(nx=nx, ny=ny, nz=nz, dx=h, dy=h, dz=h, dt=dt,
+                       ccx0=1, ccxf=1, ccy0=1, ccyf=1, ccz0=1, cczf=1,
+                       gz=9.80665, m_turb=1, csmag=0.1, reinit_max_iter=3,
+                       cg_tol_mode=CG_TOL_REL, cg_tol=cg_tol, precision=precision)
+    x = _centres(nx, h)[:, None, None]
+    z = _centres(nz, h)[None, None, :]
+    eta = 0.05 * np.sin(2.0 * math.pi * x / 2.0)
+    ls = np.empty((nx, ny, nz), order="F")
+    ls[...] = eta - z + 1.0
+    return Case("wave_tank_%dx%dx%d" % (nx, ny, nz), p, _base_fields(p, ls), steps=1000)
+
+
+def mms_case(n=32, precision=PREC_FP64, dt=None, project=True) -> Case:
+    """Steady manufactured solution (13_mms.f90:39-114, a = 0, h0 = 2) on a
+    2 pi x 2 pi x 2 box, periodic in x and y (the sin x cos y fields are
+    2 pi-periodic), no-slip bed, free-slip top, gravity off; 100 steps."""
+    L = 2.0 * math.pi
+    dxy = L / n
+    dz = 2.0 / n
+    if dt is None:
+        dt = 0.002 * 32.0 / n
+    p = default_params(nx=n, ny=n, nz=n, dx=dxy, dy=dxy, dz=dz, dt=dt,
+                       ccx0=0, ccxf=0, ccy0=0, ccyf=0, ccz0=2, cczf=1,
+                       gx=0.0, gz=0.0, mms_t=1, project_under_mms=1 if project else 0,
+                       rho_f2=998.0, mu_f2=0.00100798, cg_tol_mode=CG_TOL_ABS, cg_tol=1e-4,
+                       precision=precision)
+    a, h0 = 0.0, 2.0
+    f = {}
+    x = _centres(n, dxy)[:, None, None]
+    y = _centres(n, dxy)[None, :, None]
+    z = _centres(n, dz)[None, None, :]
+    ls = np.empty((n, n, n), order="F")
+    ls[...] = a * np.sin(x) * np.sin(y) + h0 - z
+    f = _base_fields(p, ls)
+    u = f["U"]
+    xf = (np.arange(1, n + 2) - 1.0) * dxy
+    yc = _centres(n, dxy)
+    zc = _centres(n, dz)
+    X, Y, Z = np.meshgrid(xf, yc, zc, indexing="ij")
+    hh = a * np.sin(X) * np.sin(Y) + h0
+    u[1:n + 2, 1:n + 1, 1:n + 1] = np.sin(X) * np.cos(Y) * np.sin(math.pi * 0.5 * Z / hh) - \
+        np.cos(X) * np.sin(Y) * (np.cos(math.pi * 2.0 * Z / hh) - 1.0)
+    v = f["V"]
+    X, Y, Z = np.meshgrid(_centres(n, dxy), (np.arange(1, n + 2) - 1.0) * dxy, zc, indexing="ij")
+    hh = a * np.sin(X) * np.sin(Y) + h0
+    v[1:n + 1, 1:n + 2, 1:n + 1] = -np.cos(X) * np.sin(Y) * np.sin(math.pi * 0.5 * Z / hh) + \
+        np.sin(X) * np.cos(Y) * (np.cos(math.pi * 2.0 * Z / hh) - 1.0)
+    return Case("mms_%d" % n, p, f, steps=100)
+
+
+def open_channel(nx=512, ny=128, nz=128, precision=PREC_FP64, dt=1e-3, seed=1234) -> Case:
+    """Open channel, 4 x 1 x 1 m, depth 0.6 m flat surface, inflow u = 0.5 m/s
+    with a seeded uniform 5 % perturbation (ccx0 = 3), free outflow, no-slip
+    bed, Smagorinsky LES Cs = 0.1, vertical cylinder D = 0.1 m at x = 1.0
+    through image-point IBM; 2000 steps."""
+    h = 4.0 / nx
+    p = default_params(nx=nx, ny=ny, nz=nz, dx=h, dy=h, dz=h, dt=dt,
+                       ccx0=3, ccxf=4, ccy0=1, ccyf=1, ccz0=2, cczf=1,
+                       gz=9.80665, m_turb=1, csmag=0.1, uinicial=0.5, iturb=0.05,
+                       ibm_t=2, obst_t=4, reinit_max_iter=3, cg_tol_mode=CG_TOL_REL, cg_tol=1e-8,
+                       precision=precision, seed=seed)
+    ls = level_set_tipo(p, 1, ampl=0.0, lambdax=0.0, lambday=0.0, prof=0.6)
+    f = _base_fields(p, ls)
+    return Case("open_channel_%dx%dx%d" % (nx, ny, nz), p, f, steps=2000,
+                obstacle={"kind": "cylinder", "xc": 1.0, "yc": 0.5, "radius": 0.05})
+
+
+def ensemble_dims(ncases=256, seed=0, lo=32, hi=96):
+    """Grid dims drawn per axis uniformly from {lo..hi} (seeded)."""
+    rng = np.random.default_rng(seed)
+    dims = rng.integers(lo, hi + 1, size=(ncases, 3))
+    hcol = rng.uniform(0.2, 0.6, size=ncases)
+    amp = rng.uniform(0.0, 0.05, size=ncases)
+    return dims, hcol, amp
+
+
+def ensemble_case(i, dims, hcol, amp, precision=PREC_FP64, dt=1e-4) -> Case:
+    """One member of the sloshing / dam-break ensemble: dx = 1/64; a water
+    column of height hcol*lz (tipo 3 form) united with a sloshing layer of
+    depth 0.25 lz and cosine amplitude amp*lz (tipo 1 form); the union of the
+    two water regions is the max of the two level sets (a build-side
+    composition of two reference tipos)."""
+    nx, ny, nz = (int(d) for d in dims[i])
+    h = 1.0 / 64.0
+    p = default_params(nx=nx, ny=ny, nz=nz, dx=h, dy=h, dz=h, dt=dt,
+                       ccx0=2, ccxf=2, ccy0=2, ccyf=2, ccz0=2, cczf=2,
+                       gz=9.81, rho_f1=1.2, mu_f1=1.8e-5, rho_f2=1000.0, mu_f2=1e-3,
+                       reinit_max_iter=3, cg_tol_mode=CG_TOL_REL, cg_tol=1e-8, precision=precision)
+    lx, lz = nx * h, nz * h
+    col = level_set_tipo(p, 3, ampl=float(hcol[i]) * lz, m=30.0)
+    layer = level_set_tipo(p, 1, ampl=float(amp[i]) * lz, lambdax=2.0 * lx, prof=0.25 * lz)
+    ls = np.maximum(col, layer)
+    return Case("ensemble_%d" % i, p, _base_fields(p, ls), steps=500)

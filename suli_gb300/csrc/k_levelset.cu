@@ -1,0 +1,357 @@
+// k_levelset.cu -- level-set kernels: WENO5 advection (TVD-RK3), the
+// reinitialisation loop, Heaviside / properties and the FP64 volume integral.
+//
+// Replaces 14_level_set.f90:204-594 and 8_derivadas.f90:675-1095.  The WENO
+// halos (3 cells, built by extrapolation or the node-style periodic wrap in
+// wenox/y/z) are formed on the fly from the 7-point line each thread loads,
+// so no halo array or fill pass is needed.  The three RK stages rotate
+// through ls -> lsb -> lsc -> ls, so stage 3 writes the result back in place
+// (each thread reads ls only at its own cell in stages 2/3) and ls0 = ls is
+// never copied.
+#include "suli_kernels.cuh"
+
+namespace suli {
+
+// Jiang-Shu WENO5 on five one-sided differences (8_derivadas.f90:778-806)
+template <typename T>
+__device__ __forceinline__ T weno5(T v0, T v1, T v2, T v3, T v4)
+{
+    const T aux1 = T(13. / 12.), aux2 = T(1. / 4.), aux3 = T(1. / 6.), aux6 = T(0.00000001);
+    T a, b;
+    a = v0 - 2 * v1 + v2;
+    b = v0 - 4 * v1 + 3 * v2;
+    T is1 = aux1 * a * a + aux2 * b * b;
+    a = v1 - 2 * v2 + v3;
+    b = v1 - v3;
+    T is2 = aux1 * a * a + aux2 * b * b;
+    a = v2 - 2 * v3 + v4;
+    b = 3 * v2 - 4 * v3 + v4;
+    T is3 = aux1 * a * a + aux2 * b * b;
+    T al1 = T(0.1) / ((aux6 + is1) * (aux6 + is1));
+    T al2 = T(0.6) / ((aux6 + is2) * (aux6 + is2));
+    T al3 = T(0.3) / ((aux6 + is3) * (aux6 + is3));
+    T s = al1 + al2 + al3;
+    T om1 = al1 / s, om2 = al2 / s, om3 = al3 / s;
+    return aux3 * (om1 * (2 * v0 - 7 * v1 + 11 * v2) + om2 * (-v1 + 5 * v2 + 2 * v3) +
+                   om3 * (2 * v2 + 5 * v3 - v4));
+}
+
+// Load phi(m), m = i-3..i+3, of one grid line (element m at base + m*st),
+// building the out-of-range values as wenox/y/z do: ihs = 0 periodic with
+// phi(0) = phi(n-1) etc. (:702-714), otherwise cubic extrapolation (:742-756).
+template <typename T>
+__device__ __forceinline__ void load_line(const T *__restrict__ a, long long base, long long st, int i, int n,
+                                          int ihs, T (&L)[7])
+{
+    if (i >= 4 && i <= n - 3) {
+#pragma unroll
+        for (int t = 0; t < 7; ++t) L[t] = a[base + (long long)(i - 3 + t) * st];
+        return;
+    }
+#pragma unroll
+    for (int t = 0; t < 7; ++t) {
+        int m = i - 3 + t;
+        if (ihs == 0) {
+            if (m < 1) m += n - 1;
+            else if (m > n) m -= n - 1;
+            L[t] = a[base + (long long)m * st];
+        } else if (m >= 1 && m <= n) {
+            L[t] = a[base + (long long)m * st];
+        }
+    }
+    if (ihs != 0) {
+        const T c11 = T(1. / 11.);
+        if (i - 3 < 1) {
+            T p1 = a[base + st], p2 = a[base + 2 * st], p3 = a[base + 3 * st];
+            T g0 = c11 * (T(18.) * p1 - T(9.) * p2 + T(2.) * p3);
+            T gm1 = c11 * (T(18.) * g0 - T(9.) * p1 + T(2.) * p2);
+            T gm2 = c11 * (T(18.) * gm1 - T(9.) * g0 + T(2.) * p1);
+#pragma unroll
+            for (int t = 0; t < 7; ++t) {
+                int m = i - 3 + t;
+                if (m == 0) L[t] = g0;
+                else if (m == -1) L[t] = gm1;
+                else if (m == -2) L[t] = gm2;
+            }
+        }
+        if (i + 3 > n) {
+            T pn = a[base + (long long)n * st], pn1 = a[base + (long long)(n - 1) * st],
+              pn2 = a[base + (long long)(n - 2) * st];
+            T g1 = c11 * (T(18.) * pn - T(9.) * pn1 + T(2.) * pn2);
+            T g2 = c11 * (T(18.) * g1 - T(9.) * pn + T(2.) * pn1);
+            T g3 = c11 * (T(18.) * g2 - T(9.) * g1 + T(2.) * pn);
+#pragma unroll
+            for (int t = 0; t < 7; ++t) {
+                int m = i - 3 + t;
+                if (m == n + 1) L[t] = g1;
+                else if (m == n + 2) L[t] = g2;
+                else if (m == n + 3) L[t] = g3;
+            }
+        }
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void weno_pm(const T (&L)[7], T h, T &dp, T &dn)
+{
+    T D[6];
+#pragma unroll
+    for (int t = 0; t < 6; ++t) D[t] = (L[t + 1] - L[t]) / h;
+    dp = weno5<T>(D[5], D[4], D[3], D[2], D[1]);
+    dn = weno5<T>(D[0], D[1], D[2], D[3], D[4]);
+}
+
+// der_weno (14_level_set.f90:338-370) at cell (i,j,k) of a cell array with
+// interior dims (n0,n1,n2): returns x+, x-, y+, y-, z+, z-.
+template <typename T>
+__device__ __forceinline__ void der_weno_at(const CaseDev<T> &c, const T *__restrict__ a, int i, int j, int k,
+                                            T &xp, T &xm, T &yp, T &ym, T &zp, T &zm)
+{
+    const Geo &g = c.g;
+    T L[7];
+    load_line<T>(a, g.at(0, j, k), 1, i, g.nx, c.ccx0 == 0 ? 0 : 2, L);
+    weno_pm<T>(L, T(c.dx), xp, xm);
+    load_line<T>(a, g.at(i, 0, k), g.sx, j, g.ny, c.ccy0 == 0 ? 0 : 2, L);
+    weno_pm<T>(L, T(c.dy), yp, ym);
+    load_line<T>(a, g.at(i, j, 0), g.sxy, k, g.nz, 2, L);
+    weno_pm<T>(L, T(c.dz), zp, zm);
+}
+
+// Godunov |grad phi| of reinic_weno (:397-421)
+template <typename T>
+__device__ __forceinline__ T godunov(T ls, T ta, T tb, T tc, T td, T te, T tf)
+{
+    const T eps = T(0.00000001);
+    T a1, a2, A, B, C;
+    if (ls > T(0.)) {
+        a1 = fmax(td, eps); a2 = -fmin(ta, eps); A = fmax(a1, a2);
+        a1 = fmax(te, eps); a2 = -fmin(tb, eps); B = fmax(a1, a2);
+        a1 = fmax(tf, eps); a2 = -fmin(tc, eps); C = fmax(a1, a2);
+    } else {
+        a1 = fmax(ta, eps); a2 = -fmin(td, eps); A = fmax(a1, a2);
+        a1 = fmax(tb, eps); a2 = -fmin(te, eps); B = fmax(a1, a2);
+        a1 = fmax(tc, eps); a2 = -fmin(tf, eps); C = fmax(a1, a2);
+    }
+    return sqrt(A * A + B * B + C * C);
+}
+
+template <typename T>
+__device__ __forceinline__ void stage_bufs(const CaseDev<T> &c, int stage, const T *&src, T *&dst)
+{
+    if (stage == 1) { src = c.ls; dst = c.lsb; }
+    else if (stage == 2) { src = c.lsb; dst = c.lsc; }
+    else { src = c.lsc; dst = c.ls; }
+}
+
+// conv_weno + intt_ls (14_level_set.f90:277-334), one TVD-RK3 stage
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_ls_adv_stage(const CaseDev<T> *__restrict__ cs, int ncases, int stage,
+                                                           const double *__restrict__ rk)
+{
+    const CaseDev<T> &c = cs[find_case(cs, ncases)];
+    int i, j, k;
+    tile_ijk(c, i, j, k);
+    const Geo &g = c.g;
+    if (i > g.nx || j > g.ny || k > g.nz) return;
+    const T *src;
+    T *dst;
+    stage_bufs(c, stage, src, dst);
+    long long q = g.at(i, j, k);
+    T ta, td, tb, te, tc, tf;
+    der_weno_at<T>(c, src, i, j, k, ta, td, tb, te, tc, tf);
+    T ua = (c.u[q] + c.u[q + 1]) * T(0.5);
+    T va = (c.v[q] + c.v[q + g.sx]) * T(0.5);
+    T wa = (c.w[q] + c.w[q + g.sxy]) * T(0.5);
+    T apos = ua > T(0.) ? ua : T(0.), aneg = ua < T(0.) ? ua : T(0.);
+    T bpos = va > T(0.) ? va : T(0.), bneg = va < T(0.) ? va : T(0.);
+    T cpos = wa > T(0.) ? wa : T(0.), cneg = wa < T(0.) ? wa : T(0.);
+    T sy7 = -(apos * td + aneg * ta + bpos * te + bneg * tb + cpos * tf + cneg * tc);
+    T ta1 = c.ls[q];          // ls0 (stage 1: the current value)
+    T gx = src[q];
+    T dt1 = T(c.sc[S_DTADV]);
+    T a = T(rk[stage - 1]), b = T(rk[3 + stage - 1]), gg = T(rk[6 + stage - 1]);
+    dst[q] = a * ta1 + b * gx + gg * dt1 * sy7;
+}
+
+// func_s of reinic_weno (:391-426); also resets the loop state of the case
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_reinit_funcs(const CaseDev<T> *__restrict__ cs, int ncases)
+{
+    const CaseDev<T> &c = cs[find_case(cs, ncases)];
+    int i, j, k;
+    tile_ijk(c, i, j, k);
+    const Geo &g = c.g;
+    if (blockIdx.x == c.tile_begin && tid_lin() == 0) {
+        c.sc[S_RINACTIVE] = 1.0;
+        c.sc[S_RINITER] = 0.0;
+    }
+    if (i > g.nx || j > g.ny || k > g.nz) return;
+    long long q = g.at(i, j, k);
+    T ta, td, tb, te, tc, tf;
+    der_weno_at<T>(c, c.ls, i, j, k, ta, td, tb, te, tc, tf);
+    T lv = c.ls[q];
+    T mod = godunov<T>(lv, ta, tb, tc, td, te, tf);
+    T dx1 = T(c.dx1);
+    c.funcs[q] = lv / sqrt(lv * lv + mod * mod * dx1 * dx1);
+}
+
+// one RK stage of the reinitialisation iteration `iter` (:431-500); stage 3
+// also forms the signed band error and decides whether to iterate again.
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_reinit_stage(const CaseDev<T> *__restrict__ cs, int ncases, int stage,
+                                                           int iter, const double *__restrict__ rk)
+{
+    const CaseDev<T> &c = cs[find_case(cs, ncases)];
+    if (c.sc[S_RINACTIVE] == 0.0) return;      // loop of this case has ended
+    int i, j, k;
+    tile_ijk(c, i, j, k);
+    const Geo &g = c.g;
+    bool in = (i <= g.nx && j <= g.ny && k <= g.nz);
+    const T *src;
+    T *dst;
+    stage_bufs(c, stage, src, dst);
+    double band = 0.0, cnt = 0.0;
+    if (in) {
+        long long q = g.at(i, j, k);
+        T ta, td, tb, te, tc, tf;
+        der_weno_at<T>(c, src, i, j, k, ta, td, tb, te, tc, tf);
+        T lv = src[q];
+        T mod = godunov<T>(lv, ta, tb, tc, td, te, tf);
+        T sy7 = c.funcs[q] * (T(1.) - mod);
+        T ta1 = c.ls[q];
+        T a = T(rk[stage - 1]), b = T(rk[3 + stage - 1]), gg = T(rk[6 + stage - 1]);
+        T nv = a * ta1 + b * lv + gg * T(c.dt1) * sy7;
+        dst[q] = nv;
+        if (stage == 3) {
+            if (fabs((double)nv) <= 2. * c.alpha1 * c.dx1) {
+                band = (double)nv - (double)lv;
+                cnt = 1.0;
+            }
+        }
+    }
+    if (stage != 3) return;
+    double vals[2] = {band, cnt}, tot[2];
+    if (last_block_reduce<T, 2>(c, vals, tot) && tid_lin() == 0) {
+        double il = (double)iter;
+        double active;
+        double replay = c.sc[S_RINREPLAY];
+        if (replay >= 0.0) active = (il < replay) ? 1.0 : 0.0;
+        else if (iter == c.reinit_max) active = 0.0;
+        else {
+            double err = tot[0] / tot[1];
+            active = (err > c.dt1 * c.dx1 * c.dx1) ? 1.0 : 0.0;
+        }
+        c.sc[S_RINITER] = il;
+        c.sc[S_RINACTIVE] = active;
+    }
+}
+
+// heaviside (14_level_set.f90:508-594, t_tens = 0) + the volume sum
+// (:233-240); the last block decides whether the volume correction runs.
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_heaviside_vol(const CaseDev<T> *__restrict__ cs, int ncases, int set_ini)
+{
+    const CaseDev<T> &c = cs[find_case(cs, ncases)];
+    int i, j, k;
+    tile_ijk(c, i, j, k);
+    const Geo &g = c.g;
+    double vol = 0.0;
+    if (i <= g.nx && j <= g.ny && k <= g.nz) {
+        long long q = g.at(i, j, k);
+        T l = c.ls[q];
+        T ad = T(c.alpha1 * c.dx1);
+        T h;
+        if (l < -ad) h = T(0.);
+        else if (l > ad) h = T(1.);
+        else h = T(0.5) * (T(1.) + l / ad + T(1. / c.pi) * sin(T(c.pi) * l / ad));
+        c.hs[q] = h;
+        c.rho[q] = T(c.rho_f1) * (T(1.) - h) + T(c.rho_f2) * h;
+        c.ls_mu[q] = T(c.mu_f1) * (T(1.) - h) + T(c.mu_f2) * h;
+        vol = (1. - (1. - (double)h)) * c.dx * c.dy * c.dz;
+    }
+    double vals[1] = {vol}, tot[1];
+    if (last_block_reduce<T, 1>(c, vals, tot) && tid_lin() == 0) {
+        double vi = tot[0];
+        if (set_ini) c.sc[S_VOLINI] = vi;
+        c.sc[S_VOLINS] = vi;
+        double v0 = c.sc[S_VOLINI];
+        c.sc[S_VOLACTIVE] = (fabs(vi - v0) / vi > 0.1 && c.mms_t != 2) ? 1.0 : 0.0;
+    }
+}
+
+// volume correction update (:245-255): ls - dt1*(vol_ins-vol_ini)*|grad ls|/vol_ini
+// with |grad ls| from mod_ls1 (:598-655); writes lsb, copied back after.
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_volcorr(const CaseDev<T> *__restrict__ cs, int ncases)
+{
+    const CaseDev<T> &c = cs[find_case(cs, ncases)];
+    if (c.sc[S_VOLACTIVE] == 0.0) return;
+    int i, j, k;
+    tile_ijk(c, i, j, k);
+    const Geo &g = c.g;
+    if (i > g.nx || j > g.ny || k > g.nz) return;
+    long long q = g.at(i, j, k);
+    T ta, td, tb, te, tc, tf;
+    der_weno_at<T>(c, c.ls, i, j, k, ta, td, tb, te, tc, tf);
+    if (!(fabs(ta) > fabs(td))) ta = td;
+    if (!(fabs(tb) > fabs(te))) tb = te;
+    if (!(fabs(tc) > fabs(tf))) tc = tf;
+    T m = sqrt(ta * ta + tb * tb + tc * tc);
+    double vi = c.sc[S_VOLINS], v0 = c.sc[S_VOLINI];
+    c.lsb[q] = c.ls[q] - T(c.dt1) * T(vi - v0) * m / T(v0);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_volcorr_copy(const CaseDev<T> *__restrict__ cs, int ncases)
+{
+    const CaseDev<T> &c = cs[find_case(cs, ncases)];
+    if (c.sc[S_VOLACTIVE] == 0.0) return;
+    int i, j, k;
+    tile_ijk(c, i, j, k);
+    const Geo &g = c.g;
+    if (i > g.nx || j > g.ny || k > g.nz) return;
+    long long q = g.at(i, j, k);
+    c.ls[q] = c.lsb[q];
+}
+
+// ---- host launchers -------------------------------------------------------
+template <typename T>
+void launch_level_set_adv(const Batch<T> &b, cudaStream_t s)
+{
+    for (int st = 1; st <= 3; ++st)
+        k_ls_adv_stage<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, st, b.drk);
+}
+
+template <typename T>
+void launch_reinit(const Batch<T> &b, int max_iter, cudaStream_t s)
+{
+    k_reinit_funcs<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases);
+    for (int it = 1; it <= max_iter; ++it)
+        for (int st = 1; st <= 3; ++st)
+            k_reinit_stage<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, st, it, b.drk);
+}
+
+template <typename T>
+void launch_heaviside(const Batch<T> &b, int set_ini, cudaStream_t s)
+{
+    k_heaviside_vol<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, set_ini);
+}
+
+template <typename T>
+void launch_volcorr(const Batch<T> &b, cudaStream_t s)
+{
+    k_volcorr<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases);
+    k_volcorr_copy<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases);
+    k_heaviside_vol<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, 0);
+}
+
+template void launch_level_set_adv<double>(const Batch<double> &, cudaStream_t);
+template void launch_reinit<double>(const Batch<double> &, int, cudaStream_t);
+template void launch_heaviside<double>(const Batch<double> &, int, cudaStream_t);
+template void launch_volcorr<double>(const Batch<double> &, cudaStream_t);
+template void launch_level_set_adv<float>(const Batch<float> &, cudaStream_t);
+template void launch_reinit<float>(const Batch<float> &, int, cudaStream_t);
+template void launch_heaviside<float>(const Batch<float> &, int, cudaStream_t);
+template void launch_volcorr<float>(const Batch<float> &, cudaStream_t);
+
+}  // namespace suli

@@ -1,0 +1,445 @@
+// k_momentum.cu -- momentum-side kernels.
+//
+//   k_visco_mu      5_viscosidade.f90:11-151  Smagorinsky mu_t, mu = ls_mu + mu_t
+//   k_visco_faces   5_viscosidade.f90:153-155 mu -> xmu/ymu/zmu (interp*_cf)
+//   k_convdiff      6_convdiff.f90:14-167 with classico der=3 (7_advectivo.f90:171-284);
+//                   optionally fused with complementos (11_diversos.f90:355-450)
+//   k_tempo         11_diversos.f90:10-296
+//   k_posdin        10_pos.f90:1-46
+//   k_conmassa      4_plot.f90:386-394 (FP64 divergence and max|div|)
+//   k_mms_error     13_mms.f90:391-451
+//
+// One thread per (i,j,k) handles the u, v and w locations that exist there,
+// so Fu/Fv/Fw (and the u/v/w updates) come from one launch.  The reference's
+// temporaries (advecting-velocity averages, interpolated viscosities, face
+// densities, upwind derivatives) are recomputed in registers with the same
+// operations and boundary copies as the Fortran helpers.
+#include "suli_kernels.cuh"
+
+namespace suli {
+
+#define AT(arr, i, j, k) (arr)[g.at((i), (j), (k))]
+
+// interp?_cf at face f (1..n+1) of a centre quantity get(m), m in 1..n
+// (8_derivadas.f90:305-479); `periodic` only for x (interpx_cf).
+template <typename T, typename F>
+__device__ __forceinline__ T interp_cf(int f, int n, bool periodic, F get)
+{
+    if (f >= 2 && f <= n) return (get(f) + get(f - 1)) * T(0.5);
+    if (periodic) return (get(1) + get(n)) * T(0.5);
+    if (f == 1) return (get(2) + get(1)) * T(0.5);
+    return (get(n) + get(n - 1)) * T(0.5);
+}
+
+__device__ __forceinline__ int clampi(int a, int lo, int hi) { return a < lo ? lo : (a > hi ? hi : a); }
+
+template <typename T>
+__device__ __forceinline__ T upw(T vel, T dneg, T dpos)
+{
+    T a1 = vel > T(0.) ? vel : T(0.);
+    T a2 = vel < T(0.) ? vel : T(0.);
+    return a1 * dneg + a2 * dpos;
+}
+
+// derivaxu2n / derivaxu2p etc. (8_derivadas.f90:75-300) on a haloed array
+// whose interior extent along the axis is `dim`.
+template <typename T, typename F>
+__device__ __forceinline__ T d2n(int m, int dim, bool perx, T h, F a)
+{
+    if (m >= 2) return T(0.5) * (a(m - 2) - 4 * a(m - 1) + 3 * a(m)) / h;
+    if (!perx) return T(0.5) * (a(m + 1) - a(m - 1)) / h;
+    return T(0.5) * (a(dim - 1) - 4 * a(dim) + 3 * a(m)) / h;
+}
+template <typename T, typename F>
+__device__ __forceinline__ T d2p(int m, int dim, bool perx, T h, F a)
+{
+    if (m <= dim - 1) return T(0.5) * (-a(m + 2) + 4 * a(m + 1) - 3 * a(m)) / h;
+    if (!perx) return T(0.5) * (a(m + 1) - a(m - 1)) / h;
+    return T(0.5) * (-a(2) + 4 * a(1) - 3 * a(m)) / h;
+}
+
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_visco_mu(const CaseDev<T> *__restrict__ cs, int ncases)
+{
+    const CaseDev<T> &c = cs[find_case(cs, ncases)];
+    int i, j, k;
+    tile_ijk(c, i, j, k);
+    const Geo &g = c.g;
+    if (i > g.nx || j > g.ny || k > g.nz) return;
+    long long q = g.at(i, j, k);
+    T mut = T(0.);
+    if (c.m_turb == 1) {
+        const T *u = c.u, *v = c.v, *w = c.w;
+        const T tdx = T(2.) * T(c.dx), tdy = T(2.) * T(c.dy), tdz = T(2.) * T(c.dz);
+        // derivax/y/z on the staggered arrays then interp?_fc to the centre
+        T dudx = ((AT(u, i + 1, j, k) - AT(u, i - 1, j, k)) / tdx + (AT(u, i + 2, j, k) - AT(u, i, j, k)) / tdx) * T(0.5);
+        T dudy = ((AT(u, i, j + 1, k) - AT(u, i, j - 1, k)) / tdy + (AT(u, i + 1, j + 1, k) - AT(u, i + 1, j - 1, k)) / tdy) * T(0.5);
+        T dudz = ((AT(u, i, j, k + 1) - AT(u, i, j, k - 1)) / tdz + (AT(u, i + 1, j, k + 1) - AT(u, i + 1, j, k - 1)) / tdz) * T(0.5);
+        T dvdx = ((AT(v, i + 1, j, k) - AT(v, i - 1, j, k)) / tdx + (AT(v, i + 1, j + 1, k) - AT(v, i - 1, j + 1, k)) / tdx) * T(0.5);
+        T dvdy = ((AT(v, i, j + 1, k) - AT(v, i, j - 1, k)) / tdy + (AT(v, i, j + 2, k) - AT(v, i, j, k)) / tdy) * T(0.5);
+        T dvdz = ((AT(v, i, j, k + 1) - AT(v, i, j, k - 1)) / tdz + (AT(v, i, j + 1, k + 1) - AT(v, i, j + 1, k - 1)) / tdz) * T(0.5);
+        T dwdx = ((AT(w, i + 1, j, k) - AT(w, i - 1, j, k)) / tdx + (AT(w, i + 1, j, k + 1) - AT(w, i - 1, j, k + 1)) / tdx) * T(0.5);
+        T dwdy = ((AT(w, i, j + 1, k) - AT(w, i, j - 1, k)) / tdy + (AT(w, i, j + 1, k + 1) - AT(w, i, j - 1, k + 1)) / tdy) * T(0.5);
+        T dwdz = ((AT(w, i, j, k + 1) - AT(w, i, j, k - 1)) / tdz + (AT(w, i, j, k + 2) - AT(w, i, j, k)) / tdz) * T(0.5);
+        T p1 = dudx + T(0.5) * (dudy + dvdx + dudz + dwdx);
+        T p2 = dvdy + T(0.5) * (dvdx + dudy + dvdz + dwdy);
+        T p3 = dwdz + T(0.5) * (dwdy + dvdz + dudz + dwdx);
+        mut = T(c.cles) * sqrt(T(2.) * (p1 + p2 + p3) * (p1 + p2 + p3)) * c.rho[q];
+    }
+    c.mut[q] = mut;
+    c.mu[q] = c.ls_mu[q] + mut;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_visco_faces(const CaseDev<T> *__restrict__ cs, int ncases)
+{
+    const CaseDev<T> &c = cs[find_case(cs, ncases)];
+    int i, j, k;
+    tile_ijk(c, i, j, k);
+    const Geo &g = c.g;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const T *mu = c.mu;
+    bool px = (c.ccx0 == 0);
+    if (i <= nx + 1 && j <= ny && k <= nz)
+        AT(c.xmu, i, j, k) = interp_cf<T>(i, nx, px, [&](int m) { return AT(mu, m, j, k); });
+    if (i <= nx && j <= ny + 1 && k <= nz)
+        AT(c.ymu, i, j, k) = interp_cf<T>(j, ny, false, [&](int m) { return AT(mu, i, m, k); });
+    if (i <= nx && j <= ny && k <= nz + 1)
+        AT(c.zmu, i, j, k) = interp_cf<T>(k, nz, false, [&](int m) { return AT(mu, i, j, m); });
+}
+
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_convdiff(const CaseDev<T> *__restrict__ cs, int ncases, int fuse)
+{
+    const CaseDev<T> &c = cs[find_case(cs, ncases)];
+    int i, j, k;
+    tile_ijk(c, i, j, k);
+    const Geo &g = c.g;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const T *__restrict__ u = c.u;
+    const T *__restrict__ v = c.v;
+    const T *__restrict__ w = c.w;
+    const T *__restrict__ mu = c.mu;
+    const T *__restrict__ rho = c.rho;
+    const T *__restrict__ xmu = c.xmu;
+    const T *__restrict__ ymu = c.ymu;
+    const T *__restrict__ zmu = c.zmu;
+    const T dx = T(c.dx), dy = T(c.dy), dz = T(c.dz);
+    const bool px = (c.ccx0 == 0);
+
+    // ---- Fu at x-face (i,j,k), i in 1..nx+1 ----
+    if (i <= nx + 1 && j <= ny && k <= nz) {
+        auto U = [&](int a, int b, int cc) { return AT(u, a, b, cc); };
+        T bma = interp_cf<T>(i, nx, px, [&](int m) { return (AT(v, m, j, k) + AT(v, m, j + 1, k)) * T(0.5); });
+        T dma = interp_cf<T>(i, nx, px, [&](int m) { return (AT(w, m, j, k) + AT(w, m, j, k + 1)) * T(0.5); });
+        T ddx = upw<T>(U(i, j, k), d2n<T>(i, nx + 1, px, dx, [&](int m) { return U(m, j, k); }),
+                       d2p<T>(i, nx + 1, px, dx, [&](int m) { return U(m, j, k); }));
+        T ddy = upw<T>(bma, d2n<T>(j, ny, false, dy, [&](int m) { return U(i, m, k); }),
+                       d2p<T>(j, ny, false, dy, [&](int m) { return U(i, m, k); }));
+        T ddz = upw<T>(dma, d2n<T>(k, nz, false, dz, [&](int m) { return U(i, j, m); }),
+                       d2p<T>(k, nz, false, dz, [&](int m) { return U(i, j, m); }));
+        T uint_ = ddx + ddy + ddz;
+        T ama_i = AT(mu, clampi(i, 1, nx), j, k) / dx;
+        T ama_m = AT(mu, clampi(i - 1, 1, nx), j, k) / dx;
+        T b1 = interp_cf<T>(j + 1, ny, false, [&](int m) { return AT(xmu, i, m, k); }) / dy;
+        T b0 = interp_cf<T>(j, ny, false, [&](int m) { return AT(xmu, i, m, k); }) / dy;
+        T d1 = interp_cf<T>(k + 1, nz, false, [&](int m) { return AT(xmu, i, j, m); }) / dz;
+        T d0 = interp_cf<T>(k, nz, false, [&](int m) { return AT(xmu, i, j, m); }) / dz;
+        T rhox = interp_cf<T>(i, nx, px, [&](int m) { return AT(rho, m, j, k); });
+        T uc = U(i, j, k);
+        T F = -uint_ +
+              ((ama_i * T(2.) * (U(i + 1, j, k) - uc) - ama_m * T(2.) * (uc - U(i - 1, j, k))) / dx +
+               b1 * ((U(i, j + 1, k) - uc) / dy + (AT(v, i, j + 1, k) - AT(v, i - 1, j + 1, k)) / dx) -
+               b0 * ((uc - U(i, j - 1, k)) / dy + (AT(v, i, j, k) - AT(v, i - 1, j, k)) / dx) +
+               d1 * ((U(i, j, k + 1) - uc) / dz + (AT(w, i, j, k + 1) - AT(w, i - 1, j, k + 1)) / dx) -
+               d0 * ((uc - U(i, j, k - 1)) / dz + (AT(w, i, j, k) - AT(w, i - 1, j, k)) / dx)) /
+                  rhox;
+        if (fuse) F = F + T(c.gx) + AT(c.tf_u, i, j, k);
+        AT(c.Fu, i, j, k) = F;
+    }
+    // ---- Fv at y-face (i,j,k), j in 1..ny+1 ----
+    if (i <= nx && j <= ny + 1 && k <= nz) {
+        auto V = [&](int a, int b, int cc) { return AT(v, a, b, cc); };
+        T amb = interp_cf<T>(j, ny, false, [&](int m) { return (AT(u, i, m, k) + AT(u, i + 1, m, k)) * T(0.5); });
+        T dmb = interp_cf<T>(j, ny, false, [&](int m) { return (AT(w, i, m, k) + AT(w, i, m, k + 1)) * T(0.5); });
+        T ddx = upw<T>(amb, d2n<T>(i, nx, px, dx, [&](int m) { return V(m, j, k); }),
+                       d2p<T>(i, nx, px, dx, [&](int m) { return V(m, j, k); }));
+        T ddy = upw<T>(V(i, j, k), d2n<T>(j, ny + 1, false, dy, [&](int m) { return V(i, m, k); }),
+                       d2p<T>(j, ny + 1, false, dy, [&](int m) { return V(i, m, k); }));
+        T ddz = upw<T>(dmb, d2n<T>(k, nz, false, dz, [&](int m) { return V(i, j, m); }),
+                       d2p<T>(k, nz, false, dz, [&](int m) { return V(i, j, m); }));
+        T vint = ddx + ddy + ddz;
+        T a1 = interp_cf<T>(i + 1, nx, px, [&](int m) { return AT(ymu, m, j, k); }) / dx;
+        T a0 = interp_cf<T>(i, nx, px, [&](int m) { return AT(ymu, m, j, k); }) / dx;
+        T bmb_j = AT(mu, i, clampi(j, 1, ny), k) / dy;
+        T bmb_m = AT(mu, i, clampi(j - 1, 1, ny), k) / dy;
+        T d1 = interp_cf<T>(k + 1, nz, false, [&](int m) { return AT(ymu, i, j, m); }) / dz;
+        T d0 = interp_cf<T>(k, nz, false, [&](int m) { return AT(ymu, i, j, m); }) / dz;
+        T rhoy = interp_cf<T>(j, ny, false, [&](int m) { return AT(rho, i, m, k); });
+        T vc = V(i, j, k);
+        T F = -vint +
+              (a1 * ((V(i + 1, j, k) - vc) / dx + (AT(u, i + 1, j, k) - AT(u, i + 1, j - 1, k)) / dy) -
+               a0 * ((vc - V(i - 1, j, k)) / dx + (AT(u, i, j, k) - AT(u, i, j - 1, k)) / dy) +
+               (bmb_j * T(2.) * (V(i, j + 1, k) - vc) - bmb_m * T(2.) * (vc - V(i, j - 1, k))) / dy +
+               d1 * ((V(i, j, k + 1) - vc) / dz + (AT(w, i, j, k + 1) - AT(w, i, j - 1, k + 1)) / dy) -
+               d0 * ((vc - V(i, j, k - 1)) / dz + (AT(w, i, j, k) - AT(w, i, j - 1, k)) / dy)) /
+                  rhoy;
+        if (fuse) F = F + AT(c.tf_v, i, j, k);
+        AT(c.Fv, i, j, k) = F;
+    }
+    // ---- Fw at z-face (i,j,k), k in 1..nz+1 ----
+    if (i <= nx && j <= ny && k <= nz + 1) {
+        auto W = [&](int a, int b, int cc) { return AT(w, a, b, cc); };
+        T amd = interp_cf<T>(k, nz, false, [&](int m) { return (AT(u, i, j, m) + AT(u, i + 1, j, m)) * T(0.5); });
+        T bmd = interp_cf<T>(k, nz, false, [&](int m) { return (AT(v, i, j, m) + AT(v, i, j + 1, m)) * T(0.5); });
+        T ddx = upw<T>(amd, d2n<T>(i, nx, px, dx, [&](int m) { return W(m, j, k); }),
+                       d2p<T>(i, nx, px, dx, [&](int m) { return W(m, j, k); }));
+        T ddy = upw<T>(bmd, d2n<T>(j, ny, false, dy, [&](int m) { return W(i, m, k); }),
+                       d2p<T>(j, ny, false, dy, [&](int m) { return W(i, m, k); }));
+        T ddz = upw<T>(W(i, j, k), d2n<T>(k, nz + 1, false, dz, [&](int m) { return W(i, j, m); }),
+                       d2p<T>(k, nz + 1, false, dz, [&](int m) { return W(i, j, m); }));
+        T wint = ddx + ddy + ddz;
+        T a1 = interp_cf<T>(i + 1, nx, px, [&](int m) { return AT(zmu, m, j, k); }) / dx;
+        T a0 = interp_cf<T>(i, nx, px, [&](int m) { return AT(zmu, m, j, k); }) / dx;
+        T b1 = interp_cf<T>(j + 1, ny, false, [&](int m) { return AT(zmu, i, m, k); }) / dy;
+        T b0 = interp_cf<T>(j, ny, false, [&](int m) { return AT(zmu, i, m, k); }) / dy;
+        T dmd_k = AT(mu, i, j, clampi(k, 1, nz)) / dz;
+        T dmd_m = AT(mu, i, j, clampi(k - 1, 1, nz)) / dz;
+        T rhoz = interp_cf<T>(k, nz, false, [&](int m) { return AT(rho, i, j, m); });
+        T wc = W(i, j, k);
+        T F = -wint +
+              (a1 * ((W(i + 1, j, k) - wc) / dx + (AT(u, i + 1, j, k) - AT(u, i + 1, j, k - 1)) / dz) -
+               a0 * ((wc - W(i - 1, j, k)) / dx + (AT(u, i, j, k) - AT(u, i, j, k - 1)) / dz) +
+               b1 * ((W(i, j + 1, k) - wc) / dy + (AT(v, i, j + 1, k) - AT(v, i, j + 1, k - 1)) / dz) -
+               b0 * ((wc - W(i, j - 1, k)) / dy + (AT(v, i, j, k) - AT(v, i, j, k - 1)) / dz) +
+               (dmd_k * T(2.) * (W(i, j, k + 1) - wc) - dmd_m * T(2.) * (wc - W(i, j, k - 1))) / dz) /
+                  rhoz;
+        if (fuse) F = F - T(c.gz) + AT(c.tf_w, i, j, k);
+        AT(c.Fw, i, j, k) = F;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_complementos(const CaseDev<T> *__restrict__ cs, int ncases)
+{
+    const CaseDev<T> &c = cs[find_case(cs, ncases)];
+    int i, j, k;
+    tile_ijk(c, i, j, k);
+    const Geo &g = c.g;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    if (i <= nx + 1 && j <= ny && k <= nz) AT(c.Fu, i, j, k) = AT(c.Fu, i, j, k) + T(c.gx) + AT(c.tf_u, i, j, k);
+    if (i <= nx && j <= ny + 1 && k <= nz) AT(c.Fv, i, j, k) = AT(c.Fv, i, j, k) + AT(c.tf_v, i, j, k);
+    if (i <= nx && j <= ny && k <= nz + 1) AT(c.Fw, i, j, k) = AT(c.Fw, i, j, k) - T(c.gz) + AT(c.tf_w, i, j, k);
+}
+
+// ---------------------------------------------------------------------------
+// tempo (11_diversos.f90:10-296) at one location
+template <typename T>
+__device__ __forceinline__ void tempo_one(const CaseDev<T> &c, int tt, int it, T dt, long long q, T *u, const T *F, T *u0,
+                                          T *f0, T *f1)
+{
+    const int tte = c.t_tempo;
+    T Fv = F[q];
+    if ((tte == 0) || ((tte == 3) || ((tte == 4) && (it == 1)))) {
+        u[q] = u[q] + dt * Fv;
+        if (tte == 3 || tte == 4) f0[q] = Fv;
+    } else if (tte == 1) {
+        if (tt == 1) { u0[q] = u[q]; u[q] = u[q] + dt * Fv; }
+        else if (tt == 2) { u[q] = u0[q] + dt * Fv; }
+    } else if (tte == 2) {
+        if (tt == 1) {
+            u0[q] = u[q]; f0[q] = Fv; u[q] = u[q] + dt * Fv;
+        } else if (tt == 2) {
+            T aux1 = T(2.) * dt;
+            f1[q] = Fv;
+            u[q] = u0[q] - dt * f0[q] + aux1 * Fv;
+        } else if (tt == 3) {
+            T aux1 = dt / T(6.);
+            u[q] = u0[q] + aux1 * (f0[q] + T(4.) * f1[q] + Fv);
+        }
+    } else if (((tte == 3) && (it != 1)) || ((tte == 4) && (it == 2))) {
+        u[q] = u[q] + dt * T(0.5) * (3 * Fv - f0[q]);
+        f0[q] = Fv;
+        if (tte == 4) f1[q] = f0[q];
+    } else if ((tte == 4) && (it >= 3)) {
+        T aux1 = dt / T(12.);
+        u[q] = u[q] + aux1 * (T(23.) * Fv - T(16.) * f0[q] + T(5.) * f1[q]);
+        f1[q] = f0[q];
+        f0[q] = Fv;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_tempo(const CaseDev<T> *__restrict__ cs, int ncases, int tt, int it)
+{
+    const CaseDev<T> &c = cs[find_case(cs, ncases)];
+    int i, j, k;
+    tile_ijk(c, i, j, k);
+    const Geo &g = c.g;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    T dt = T(c.sc[S_DT]);
+    long long q = g.at(i, j, k);
+    if (i <= nx + 1 && j <= ny && k <= nz) tempo_one<T>(c, tt, it, dt, q, c.u, c.Fu, c.u0, c.fu0, c.fu1);
+    if (i <= nx && j <= ny + 1 && k <= nz) tempo_one<T>(c, tt, it, dt, q, c.v, c.Fv, c.v0, c.fv0, c.fv1);
+    if (i <= nx && j <= ny && k <= nz + 1) tempo_one<T>(c, tt, it, dt, q, c.w, c.Fw, c.w0, c.fw0, c.fw1);
+}
+
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_posdin(const CaseDev<T> *__restrict__ cs, int ncases)
+{
+    const CaseDev<T> &c = cs[find_case(cs, ncases)];
+    int i, j, k;
+    tile_ijk(c, i, j, k);
+    const Geo &g = c.g;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const T *p = c.prd1;
+    const T *rho = c.rho;
+    T dt = T(c.sc[S_DT]);
+    T aux1 = dt / T(c.dx), aux2 = dt / T(c.dy);
+    bool px = (c.ccx0 == 0);
+    if (i <= nx + 1 && j <= ny && k <= nz) {
+        T rx = interp_cf<T>(i, nx, px, [&](int m) { return AT(rho, m, j, k); });
+        AT(c.u, i, j, k) = AT(c.u, i, j, k) - aux1 * (AT(p, i, j, k) - AT(p, i - 1, j, k)) / rx;
+    }
+    if (i <= nx && j <= ny + 1 && k <= nz) {
+        T ry = interp_cf<T>(j, ny, false, [&](int m) { return AT(rho, i, m, k); });
+        AT(c.v, i, j, k) = AT(c.v, i, j, k) - aux2 * (AT(p, i, j, k) - AT(p, i, j - 1, k)) / ry;
+    }
+    if (i <= nx && j <= ny && k <= nz + 1) {
+        T rz = interp_cf<T>(k, nz, false, [&](int m) { return AT(rho, i, j, m); });
+        AT(c.w, i, j, k) = AT(c.w, i, j, k) - dt / T(c.dz) * (AT(p, i, j, k) - AT(p, i, j, k - 1)) / rz;
+    }
+}
+
+// divergence in FP64 (also in the mixed form) and its maximum
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_conmassa(const CaseDev<T> *__restrict__ cs, int ncases)
+{
+    const CaseDev<T> &c = cs[find_case(cs, ncases)];
+    int i, j, k;
+    tile_ijk(c, i, j, k);
+    const Geo &g = c.g;
+    double m = 0.0;
+    if (i <= g.nx && j <= g.ny && k <= g.nz) {
+        const T *u = c.u, *v = c.v, *w = c.w;
+        double d = ((double)AT(u, i + 1, j, k) - (double)AT(u, i, j, k)) / c.dx +
+                   ((double)AT(v, i, j + 1, k) - (double)AT(v, i, j, k)) / c.dy +
+                   ((double)AT(w, i, j, k + 1) - (double)AT(w, i, j, k)) / c.dz;
+        AT(c.div, i, j, k) = T(d);
+        m = fabs(d);
+    }
+    double vals[1] = {m}, tot[1];
+    if (last_block_reduce<T, 1>(c, vals, tot, 1u) && tid_lin() == 0) c.sc[S_MAXDIV] = tot[0];
+}
+
+// masked RMS errors against the steady manufactured fields (a = 0: w_m = 0, p_m = 0)
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_mms_error(const CaseDev<T> *__restrict__ cs, int ncases)
+{
+    const CaseDev<T> &c = cs[find_case(cs, ncases)];
+    int i, j, k;
+    tile_ijk(c, i, j, k);
+    const Geo &g = c.g;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const T *ls = c.ls;
+    bool px = (c.ccx0 == 0);
+    double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const double pi = c.pi, h = 2.0;
+    if (i <= nx + 1 && j <= ny && k <= nz) {
+        T lx = interp_cf<T>(i, nx, px, [&](int m) { return AT(ls, m, j, k); });
+        if (lx > T(0.)) {
+            double x = (i - 1.0) * c.dx, y = (j - 0.5) * c.dy, z = (k - 0.5) * c.dz;
+            double um = sin(x) * cos(y) * sin(pi * 0.5 * z / h) - cos(x) * sin(y) * (cos(pi * 2. * z / h) - 1.);
+            double d = um - (double)AT(c.u, i, j, k);
+            s[0] = d * d; s[4] = 1.0;
+        }
+    }
+    if (i <= nx && j <= ny + 1 && k <= nz) {
+        T ly = interp_cf<T>(j, ny, false, [&](int m) { return AT(ls, i, m, k); });
+        if (ly > T(0.)) {
+            double x = (i - 0.5) * c.dx, y = (j - 1.0) * c.dy, z = (k - 0.5) * c.dz;
+            double vm = -cos(x) * sin(y) * sin(pi * 0.5 * z / h) + sin(x) * cos(y) * (cos(pi * 2. * z / h) - 1.);
+            double d = vm - (double)AT(c.v, i, j, k);
+            s[1] = d * d; s[5] = 1.0;
+        }
+    }
+    if (i <= nx && j <= ny && k <= nz + 1) {
+        T lz = interp_cf<T>(k, nz, false, [&](int m) { return AT(ls, i, j, m); });
+        if (lz > T(0.)) {
+            double d = (double)AT(c.w, i, j, k);
+            s[2] = d * d; s[6] = 1.0;
+        }
+    }
+    if (i <= nx && j <= ny && k <= nz) {
+        if (AT(ls, i, j, k) > T(0.)) {
+            double d = (double)AT(c.prd1, i, j, k);
+            s[3] = d * d; s[7] = 1.0;
+        }
+    }
+    double tot[8];
+    if (last_block_reduce<T, 8>(c, s, tot) && tid_lin() == 0) {
+        c.sc[S_ERR0] = sqrt(tot[0] / fmax(tot[4], 1.0));
+        c.sc[S_ERR1] = sqrt(tot[1] / fmax(tot[5], 1.0));
+        c.sc[S_ERR2] = sqrt(tot[2] / fmax(tot[6], 1.0));
+        c.sc[S_ERR3] = sqrt(tot[3] / fmax(tot[7], 1.0));
+    }
+}
+
+template <typename T>
+__global__ void k_set_scalar(const CaseDev<T> *__restrict__ cs, int ncases, int slot, double v)
+{
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < ncases) cs[q].sc[slot] = v;
+}
+
+// ---- launchers -------------------------------------------------------------
+template <typename T> void launch_visco(const Batch<T> &b, cudaStream_t s)
+{
+    k_visco_mu<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases);
+    k_visco_faces<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases);
+}
+template <typename T> void launch_convdiff(const Batch<T> &b, int fuse, cudaStream_t s)
+{
+    k_convdiff<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, fuse);
+}
+template <typename T> void launch_complementos(const Batch<T> &b, cudaStream_t s)
+{
+    k_complementos<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases);
+}
+template <typename T> void launch_tempo(const Batch<T> &b, int tt, int it, cudaStream_t s)
+{
+    k_tempo<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, tt, it);
+}
+template <typename T> void launch_posdin(const Batch<T> &b, cudaStream_t s)
+{
+    k_posdin<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases);
+}
+template <typename T> void launch_conmassa(const Batch<T> &b, cudaStream_t s)
+{
+    k_conmassa<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases);
+}
+template <typename T> void launch_mms_error(const Batch<T> &b, cudaStream_t s)
+{
+    k_mms_error<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases);
+}
+template <typename T> void launch_set_scalar(const Batch<T> &b, int slot, double v, cudaStream_t s)
+{
+    k_set_scalar<T><<<(b.ncases + 127) / 128, 128, 0, s>>>(b.dcases, b.ncases, slot, v);
+}
+
+#define INST(T)                                                              \
+    template void launch_visco<T>(const Batch<T> &, cudaStream_t);          \
+    template void launch_convdiff<T>(const Batch<T> &, int, cudaStream_t);  \
+    template void launch_complementos<T>(const Batch<T> &, cudaStream_t);   \
+    template void launch_tempo<T>(const Batch<T> &, int, int, cudaStream_t);          \
+    template void launch_posdin<T>(const Batch<T> &, cudaStream_t);         \
+    template void launch_conmassa<T>(const Batch<T> &, cudaStream_t);       \
+    template void launch_mms_error<T>(const Batch<T> &, cudaStream_t);      \
+    template void launch_set_scalar<T>(const Batch<T> &, int, double, cudaStream_t);
+INST(double)
+INST(float)
+
+}  // namespace suli

@@ -1,0 +1,838 @@
+// suli_api.cu -- the C ABI of include/suli_gpu.h.
+//
+// A handle owns a batch of device-resident cases (one case for the Fortran
+// drop-in, many for an ensemble), a stream, the per-case scalar table and
+// the reduction scratch.  Each entry point enqueues the kernels of one
+// reference subroutine for every case of the batch; the only host reads are
+// the loop-control flags of the CG (once per chunk of iterations), of the
+// volume-correction loop (once per level_set) and explicit diagnostics.
+#include "../../include/suli_gpu.h"
+#include "suli_kernels.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace suli;
+
+static thread_local std::string g_err;
+
+static int fail(int code, const std::string &msg)
+{
+    g_err = msg;
+    return code;
+}
+
+#define CK(call)                                                                                \
+    do {                                                                                        \
+        cudaError_t e_ = (call);                                                                \
+        if (e_ != cudaSuccess)                                                                  \
+            return fail(e_ == cudaErrorMemoryAllocation ? SULI_OUT_OF_MEMORY : SULI_CUDA_ERROR, \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                    \
+    } while (0)
+
+#define CKL()                                                                                   \
+    do {                                                                                        \
+        cudaError_t e_ = cudaGetLastError();                                                    \
+        if (e_ != cudaSuccess) return fail(SULI_CUDA_ERROR, std::string("kernel launch: ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+extern "C" void suli_default_params(suli_params *p)
+{
+    std::memset(p, 0, sizeof(*p));
+    p->t_tempo = 2;
+    p->der = 3;
+    p->adv_type = 1;
+    p->t_press = 1;
+    p->ccx0 = p->ccxf = p->ccy0 = p->ccyf = p->ccz0 = p->cczf = 1;
+    p->gz = 9.80665;
+    p->csmag = 0.13;
+    p->alpha1 = 1.5;
+    p->rho_f1 = 1.204;
+    p->mu_f1 = 0.000018253;
+    p->rho_f2 = 998.0;
+    p->mu_f2 = 0.00100798;
+    p->omp_t = 1;
+    p->reinit_max_iter = 3;
+    p->cg_max_iter = 10000;
+    p->cg_tol_mode = SULI_CG_TOL_ABS;
+    p->cg_tol = 1e-4;
+    p->precision = SULI_PREC_FP64;
+    p->vol_loop_max = 1000;
+}
+
+extern "C" int suli_field_shape(const suli_params *p, int f, int lo[3], int hi[3])
+{
+    if (!p || !lo || !hi) return fail(SULI_BAD_ARG, "null argument");
+    const int nx = p->nx, ny = p->ny, nz = p->nz, nx1 = nx + 1, ny1 = ny + 1, nz1 = nz + 1;
+    auto set = [&](int a, int b, int c, int d, int e, int g) {
+        lo[0] = a; hi[0] = b; lo[1] = c; hi[1] = d; lo[2] = e; hi[2] = g;
+    };
+    switch (f) {
+    case SULI_F_U: set(0, nx1 + 1, 0, ny + 1, 0, nz + 1); break;
+    case SULI_F_V: set(0, nx + 1, 0, ny1 + 1, 0, nz + 1); break;
+    case SULI_F_W: set(0, nx + 1, 0, ny + 1, 0, nz1 + 1); break;
+    case SULI_F_PRD1: case SULI_F_PRD: set(0, nx + 1, 0, ny + 1, 0, nz + 1); break;
+    case SULI_F_LS: case SULI_F_HS: case SULI_F_RHO: case SULI_F_LS_MU: case SULI_F_MU: case SULI_F_MUT:
+    case SULI_F_DIV: case SULI_F_OBS_LSS: case SULI_F_ID_IBM:
+        set(1, nx, 1, ny, 1, nz); break;
+    case SULI_F_XMU: case SULI_F_FU: case SULI_F_U0: case SULI_F_FU0: case SULI_F_FU1: case SULI_F_TF_U:
+    case SULI_F_OBS_LSX: case SULI_F_ID_IBMX:
+        set(1, nx1, 1, ny, 1, nz); break;
+    case SULI_F_YMU: case SULI_F_FV: case SULI_F_V0: case SULI_F_FV0: case SULI_F_FV1: case SULI_F_TF_V:
+    case SULI_F_OBS_LSY: case SULI_F_ID_IBMY:
+        set(1, nx, 1, ny1, 1, nz); break;
+    case SULI_F_ZMU: case SULI_F_FW: case SULI_F_W0: case SULI_F_FW0: case SULI_F_FW1: case SULI_F_TF_W:
+    case SULI_F_OBS_LSZ: case SULI_F_ID_IBMZ:
+        set(1, nx, 1, ny, 1, nz1); break;
+    case SULI_F_BXX0: case SULI_F_BXX1: set(0, ny + 1, 0, nz + 1, 0, 0); break;
+    case SULI_F_BLX1: set(1, ny, 1, nz, 0, 0); break;
+    default: return fail(SULI_BAD_ARG, "unknown field id " + std::to_string(f));
+    }
+    return SULI_OK;
+}
+
+static bool is_int_field(int f)
+{
+    return f == SULI_F_ID_IBMX || f == SULI_F_ID_IBMY || f == SULI_F_ID_IBMZ || f == SULI_F_ID_IBM;
+}
+static bool is_plane_field(int f) { return f == SULI_F_BXX0 || f == SULI_F_BXX1 || f == SULI_F_BLX1; }
+
+static int validate(const suli_params &p)
+{
+    auto bad = [](const std::string &m) { return fail(SULI_BAD_CONFIG, m); };
+    if (p.nx < 4 || p.ny < 4 || p.nz < 4) return bad("nx, ny, nz must be >= 4");
+    if (!(p.dx > 0 && p.dy > 0 && p.dz > 0 && p.dt > 0)) return bad("dx, dy, dz, dt must be > 0");
+    if (p.der != 3) return bad("only der = 3 (2nd-order upwind) is supported");
+    if (p.adv_type != 1) return bad("only adv_type = 1 (classical advection) is supported");
+    if (p.t_press != 1) return bad("only t_press = 1 (projection) is supported");
+    if (p.m_turb != 0 && p.m_turb != 1) return bad("m_turb must be 0 or 1");
+    if (p.mms_t != 0 && p.mms_t != 1) return bad("mms_t must be 0 or 1");
+    if (p.ibm_t != 0) return bad("ibm_t = 2 needs suli_ibm_setup (not in this build)");
+    if (p.t_tempo < 0 || p.t_tempo > 4) return bad("t_tempo must be 0..4");
+    if (p.precision != SULI_PREC_FP64 && p.precision != SULI_PREC_MIXED) return bad("precision must be 0 or 1");
+    if (!(p.ccx0 == 0 || p.ccx0 == 1 || p.ccx0 == 2 || p.ccx0 == 4)) return bad("ccx0 must be 0, 1, 2 or 4");
+    if (!(p.ccxf == 0 || p.ccxf == 1 || p.ccxf == 2 || p.ccxf == 4)) return bad("ccxf must be 0, 1, 2 or 4");
+    if (p.ccy0 < 0 || p.ccy0 > 2 || p.ccyf < 0 || p.ccyf > 2) return bad("ccy0/ccyf must be 0, 1 or 2");
+    if (p.ccz0 < 1 || p.ccz0 > 2 || p.cczf < 1 || p.cczf > 2) return bad("ccz0/cczf must be 1 or 2");
+    if ((p.ccx0 == 0) != (p.ccxf == 0)) return bad("periodic x must be set at both ends");
+    if ((p.ccy0 == 0) != (p.ccyf == 0)) return bad("periodic y must be set at both ends");
+    if (p.reinit_max_iter < 1) return bad("reinit_max_iter must be >= 1");
+    if (p.cg_max_iter < 1) return bad("cg_max_iter must be >= 1");
+    if ((long long)p.nx * p.ny * p.nz > (1LL << 31) - 1) return bad("grid larger than 2^31 cells");
+    return SULI_OK;
+}
+
+// ---------------------------------------------------------------------------
+struct ImplBase {
+    virtual ~ImplBase() {}
+    virtual int copy_field(int icase, int f, void *host, bool up) = 0;
+    virtual int heaviside_init() = 0;
+    virtual int level_set() = 0;
+    virtual int contorno(int nlock) = 0;
+    virtual int visco() = 0;
+    virtual int convdiff(int fuse) = 0;
+    virtual int complementos() = 0;
+    virtual int tempo() = 0;
+    virtual int graddin(int32_t *iters) = 0;
+    virtual int posdin() = 0;
+    virtual int conmassa(double *maxdiv) = 0;
+    virtual int mms_error(double *err) = 0;
+    virtual int set_stage(int tt) = 0;
+    virtual int step(int n) = 0;
+    virtual int read_scalars() = 0;
+    virtual int write_case_scalar(int icase, int slot, double v) = 0;
+    virtual int sync() = 0;
+    int ncases = 0;
+    std::vector<suli_params> P;
+    double *hsc = nullptr;   // pinned host mirror of the per-case scalars
+    int it = 0, tt = 1, ntt = 1;
+    double t = 0.0, dt = 0.0, dt0 = 0.0, a_dt[3] = {0, 0, 0};
+    int cg_iters[3] = {0, 0, 0}, cg_outer[3] = {0, 0, 0};
+    double cg_res[3] = {0, 0, 0};
+    int prev_cg[3] = {8, 8, 8};
+    int replay_cg[3] = {-1, -1, -1}, replay_reinit = -1;
+    int reinit_iters = 0, vol_loops = 0;
+    int warn = 0;
+};
+
+struct suli_handle {
+    ImplBase *impl;
+};
+
+template <typename T>
+struct Impl : ImplBase {
+    Batch<T> b;
+    std::vector<CaseDev<T>> hc;
+    std::vector<void *> slabs;
+    double *dsc = nullptr, *dpart = nullptr, *drk = nullptr;
+    unsigned *dcnt = nullptr;
+    cudaStream_t st = nullptr;
+
+    ~Impl() override
+    {
+        if (st) cudaStreamSynchronize(st);
+        for (void *p : slabs) cudaFree(p);
+        cudaFree(dsc);
+        cudaFree(dpart);
+        cudaFree(dcnt);
+        cudaFree(drk);
+        cudaFree(b.dcases);
+        if (hsc) cudaFreeHost(hsc);
+        if (st) cudaStreamDestroy(st);
+    }
+
+    int create(const suli_params *p, int n)
+    {
+        ncases = n;
+        P.assign(p, p + n);
+        CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        hc.resize(n);
+        int tiles = 0, maxplane = 1;
+        for (int c = 0; c < n; ++c) {
+            const suli_params &q = P[c];
+            CaseDev<T> &cd = hc[c];
+            std::memset(&cd, 0, sizeof(cd));
+            Geo &g = cd.g;
+            g.nx = q.nx; g.ny = q.ny; g.nz = q.nz;
+            g.sx = (q.nx + 3 + 7) / 8 * 8;
+            g.sxy = g.sx * (q.ny + 3);
+            g.total = g.sxy * (q.nz + 3);
+            cd.ntx = (q.nx + 1 + TX - 1) / TX;
+            cd.nty = (q.ny + 1 + TY - 1) / TY;
+            cd.ntz = (q.nz + 1 + TZ - 1) / TZ;
+            cd.ntiles = cd.ntx * cd.nty * cd.ntz;
+            cd.tile_begin = tiles;
+            tiles += cd.ntiles;
+            long long mp = std::max({(long long)(q.nx + 3) * (q.nz + 3), (long long)(q.nx + 3) * (q.ny + 3),
+                                     (long long)(q.ny + 3) * (q.nz + 3),
+                                     (long long)(q.nx + 2) * (q.nz + 2) + (long long)(q.nx + 2) * (q.ny + 2) +
+                                         (long long)(q.ny + 2) * (q.nz + 2)});
+            maxplane = (int)std::max<long long>(maxplane, mp);
+            cd.dx = q.dx; cd.dy = q.dy; cd.dz = q.dz;
+            cd.dx1 = std::max({q.dx, q.dy, q.dz});
+            cd.dt1 = 0.1 * cd.dx1;
+            cd.deltai = std::pow(q.dx * q.dy * q.dz, 1. / 3.);
+            cd.alpha1 = q.alpha1;
+            cd.rho_f1 = q.rho_f1; cd.mu_f1 = q.mu_f1; cd.rho_f2 = q.rho_f2; cd.mu_f2 = q.mu_f2;
+            cd.gx = q.gx; cd.gz = q.gz;
+            cd.cles = std::pow(q.dx * q.dy * q.dz, 2. / 3.) * q.csmag * q.csmag;
+            cd.pi = std::acos(-1.0);
+            cd.uinicial = q.uinicial; cd.iturb = q.iturb; cd.seed = q.seed;
+            cd.ccx0 = q.ccx0; cd.ccxf = q.ccxf; cd.ccy0 = q.ccy0; cd.ccyf = q.ccyf; cd.ccz0 = q.ccz0; cd.cczf = q.cczf;
+            cd.t_tempo = q.t_tempo; cd.m_turb = q.m_turb; cd.mms_t = q.mms_t; cd.ibm_t = q.ibm_t; cd.obst_t = q.obst_t;
+            cd.reinit_max = q.reinit_max_iter; cd.cg_max = q.cg_max_iter; cd.cg_tol_mode = q.cg_tol_mode;
+            cd.cg_tol = q.cg_tol;
+            // one slab per case: every field of the case in the common box layout
+            const size_t fb = ((size_t)g.total * sizeof(T) + 255) / 256 * 256;
+            const size_t ib = ((size_t)g.total * sizeof(int) + 255) / 256 * 256;
+            const size_t db = ((size_t)g.total * sizeof(double) + 255) / 256 * 256;
+            const size_t pb = ((size_t)(q.ny + 3) * (q.nz + 3) * sizeof(T) + 255) / 256 * 256;
+            T **tf[] = {&cd.u, &cd.v, &cd.w, &cd.prd1, &cd.prd, &cd.ls, &cd.lsb, &cd.lsc, &cd.funcs, &cd.hs,
+                        &cd.rho, &cd.ls_mu, &cd.mu, &cd.mut, &cd.xmu, &cd.ymu, &cd.zmu, &cd.Fu, &cd.Fv, &cd.Fw,
+                        &cd.u0, &cd.v0, &cd.w0, &cd.fu0, &cd.fv0, &cd.fw0, &cd.fu1, &cd.fv1, &cd.fw1, &cd.div,
+                        &cd.tf_u, &cd.tf_v, &cd.tf_w, &cd.obs_lsx, &cd.obs_lsy, &cd.obs_lsz, &cd.obs_lss,
+                        &cd.spi, &cd.spj, &cd.spk, &cd.dpr, &cd.e, &cd.r, &cd.p, &cd.mp, &cd.qpr};
+            const int ntf = sizeof(tf) / sizeof(tf[0]);
+            int **itf[] = {&cd.id_ibmx, &cd.id_ibmy, &cd.id_ibmz, &cd.id_ibm};
+            T **ptf[] = {&cd.bxx0, &cd.bxx1, &cd.blx1};
+            const bool mixed = (sizeof(T) == 4);
+            size_t bytes = fb * ntf + ib * 4 + pb * 3 + (mixed ? 2 * db : 0);
+            void *slab = nullptr;
+            CK(cudaMalloc(&slab, bytes));
+            slabs.push_back(slab);
+            CK(cudaMemsetAsync(slab, 0, bytes, st));
+            char *cur = (char *)slab;
+            for (int f = 0; f < ntf; ++f) { *tf[f] = (T *)cur; cur += fb; }
+            for (int f = 0; f < 4; ++f) { *itf[f] = (int *)cur; cur += ib; }
+            for (int f = 0; f < 3; ++f) { *ptf[f] = (T *)cur; cur += pb; }
+            if (mixed) { cd.e64 = (double *)cur; cur += db; cd.r64 = (double *)cur; cur += db; }
+        }
+        b.ncases = n;
+        b.total_tiles = tiles;
+        b.max_plane = maxplane;
+        CK(cudaMalloc(&dsc, sizeof(double) * S_NSCAL * n));
+        CK(cudaMemsetAsync(dsc, 0, sizeof(double) * S_NSCAL * n, st));
+        CK(cudaMalloc(&dpart, sizeof(double) * NSLOT * (size_t)tiles));
+        CK(cudaMalloc(&dcnt, sizeof(unsigned) * n));
+        CK(cudaMemsetAsync(dcnt, 0, sizeof(unsigned) * n, st));
+        CK(cudaMallocHost(&hsc, sizeof(double) * S_NSCAL * n));
+        double rk[9] = {1., 3. / 4., 1. / 3., 0., 1. / 4., 2. / 3., 1., 1. / 4., 2. / 3.};
+        CK(cudaMalloc(&drk, sizeof(rk)));
+        CK(cudaMemcpyAsync(drk, rk, sizeof(rk), cudaMemcpyHostToDevice, st));
+        b.drk = drk;
+        for (int c = 0; c < n; ++c) {
+            hc[c].sc = dsc + (size_t)c * S_NSCAL;
+            hc[c].partials = dpart;
+            hc[c].counter = dcnt + c;
+            hc[c].total_tiles = tiles;
+        }
+        CK(cudaMalloc(&b.dcases, sizeof(CaseDev<T>) * n));
+        CK(cudaMemcpyAsync(b.dcases, hc.data(), sizeof(CaseDev<T>) * n, cudaMemcpyHostToDevice, st));
+        b.hcases = hc.data();
+        // time-integration coefficients, coef_tempo (2_iniciais.f90:278-312)
+        dt0 = dt = P[0].dt;
+        if (P[0].t_tempo == 1 || P[0].t_tempo == 2) {
+            ntt = (P[0].t_tempo == 1) ? 2 : 3;
+            a_dt[0] = 0.5 * dt; a_dt[1] = 1.0 * dt; a_dt[2] = 1.0 * dt;
+        } else {
+            ntt = 1;
+            a_dt[0] = a_dt[1] = a_dt[2] = 1.0 * dt;
+        }
+        for (int c = 0; c < n; ++c) setsc_host_init(c);
+        CK(cudaMemcpyAsync(dsc, hsc, sizeof(double) * S_NSCAL * n, cudaMemcpyHostToDevice, st));
+        CK(cudaStreamSynchronize(st));
+        return SULI_OK;
+    }
+
+    void setsc_host_init(int c)
+    {
+        double *s = hsc + (size_t)c * S_NSCAL;
+        std::memset(s, 0, sizeof(double) * S_NSCAL);
+        s[S_DT] = dt;
+        s[S_DTADV] = dt;
+        s[S_RINREPLAY] = -1.0;
+        s[S_CGREPLAY] = -1.0;
+        s[S_CGMAX] = (double)P[c].cg_max_iter;
+    }
+
+    int setsc(int slot, double v)
+    {
+        launch_set_scalar<T>(b, slot, v, st);
+        CKL();
+        return SULI_OK;
+    }
+
+    int read_scalars() override
+    {
+        CK(cudaMemcpyAsync(hsc, dsc, sizeof(double) * S_NSCAL * ncases, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        return SULI_OK;
+    }
+    double sc(int c, int slot) const { return hsc[(size_t)c * S_NSCAL + slot]; }
+
+    int write_case_scalar(int icase, int slot, double v) override
+    {
+        CK(cudaStreamSynchronize(st));
+        CK(cudaMemcpy(dsc + (size_t)icase * S_NSCAL + slot, &v, sizeof(double), cudaMemcpyHostToDevice));
+        hsc[(size_t)icase * S_NSCAL + slot] = v;
+        return SULI_OK;
+    }
+
+    int sync() override
+    {
+        CK(cudaStreamSynchronize(st));
+        return SULI_OK;
+    }
+
+    // ---- field copies -------------------------------------------------------
+    void *dev_ptr(int icase, int f)
+    {
+        CaseDev<T> &c = hc[icase];
+        switch (f) {
+        case SULI_F_U: return c.u;
+        case SULI_F_V: return c.v;
+        case SULI_F_W: return c.w;
+        case SULI_F_PRD1: return c.prd1;
+        case SULI_F_PRD: return c.prd;
+        case SULI_F_LS: return c.ls;
+        case SULI_F_HS: return c.hs;
+        case SULI_F_RHO: return c.rho;
+        case SULI_F_LS_MU: return c.ls_mu;
+        case SULI_F_MU: return c.mu;
+        case SULI_F_MUT: return c.mut;
+        case SULI_F_XMU: return c.xmu;
+        case SULI_F_YMU: return c.ymu;
+        case SULI_F_ZMU: return c.zmu;
+        case SULI_F_FU: return c.Fu;
+        case SULI_F_FV: return c.Fv;
+        case SULI_F_FW: return c.Fw;
+        case SULI_F_U0: return c.u0;
+        case SULI_F_V0: return c.v0;
+        case SULI_F_W0: return c.w0;
+        case SULI_F_FU0: return c.fu0;
+        case SULI_F_FV0: return c.fv0;
+        case SULI_F_FW0: return c.fw0;
+        case SULI_F_FU1: return c.fu1;
+        case SULI_F_FV1: return c.fv1;
+        case SULI_F_FW1: return c.fw1;
+        case SULI_F_DIV: return c.div;
+        case SULI_F_TF_U: return c.tf_u;
+        case SULI_F_TF_V: return c.tf_v;
+        case SULI_F_TF_W: return c.tf_w;
+        case SULI_F_OBS_LSX: return c.obs_lsx;
+        case SULI_F_OBS_LSY: return c.obs_lsy;
+        case SULI_F_OBS_LSZ: return c.obs_lsz;
+        case SULI_F_OBS_LSS: return c.obs_lss;
+        case SULI_F_ID_IBMX: return c.id_ibmx;
+        case SULI_F_ID_IBMY: return c.id_ibmy;
+        case SULI_F_ID_IBMZ: return c.id_ibmz;
+        case SULI_F_ID_IBM: return c.id_ibm;
+        case SULI_F_BXX0: return c.bxx0;
+        case SULI_F_BXX1: return c.bxx1;
+        case SULI_F_BLX1: return c.blx1;
+        default: return nullptr;
+        }
+    }
+
+    int copy_field(int icase, int f, void *host, bool up) override
+    {
+        if (icase < 0 || icase >= ncases) return fail(SULI_BAD_ARG, "case index out of range");
+        int lo[3], hi[3];
+        int rc = suli_field_shape(&P[icase], f, lo, hi);
+        if (rc) return rc;
+        void *dev = dev_ptr(icase, f);
+        if (!dev) return fail(SULI_BAD_ARG, "field not stored");
+        const Geo &g = hc[icase].g;
+        size_t e0 = hi[0] - lo[0] + 1, e1 = hi[1] - lo[1] + 1, e2 = hi[2] - lo[2] + 1;
+        size_t n = e0 * e1 * e2;
+        const bool isint = is_int_field(f);
+        const size_t es = isint ? sizeof(int) : sizeof(T);
+        // staging buffer in the device element type (FP32 fields convert)
+        std::vector<char> stage;
+        void *hp = host;
+        if (!isint && sizeof(T) != sizeof(double)) {
+            stage.resize(n * sizeof(T));
+            hp = stage.data();
+            if (up) {
+                const double *src = (const double *)host;
+                T *dst = (T *)hp;
+                for (size_t q = 0; q < n; ++q) dst[q] = (T)src[q];
+            }
+        }
+        cudaMemcpy3DParms m;
+        std::memset(&m, 0, sizeof(m));
+        size_t dpitch_el = is_plane_field(f) ? (size_t)(g.ny + 3) : (size_t)g.sx;
+        size_t dheight = is_plane_field(f) ? (size_t)(g.nz + 3) : (size_t)(g.ny + 3);
+        cudaPitchedPtr hpp = make_cudaPitchedPtr(hp, e0 * es, e0, e1);
+        cudaPitchedPtr dpp = make_cudaPitchedPtr(dev, dpitch_el * es, dpitch_el, dheight);
+        cudaPos pos = make_cudaPos((size_t)lo[0] * es, (size_t)lo[1], (size_t)lo[2]);
+        m.extent = make_cudaExtent(e0 * es, e1, e2);
+        if (up) {
+            m.srcPtr = hpp;
+            m.dstPtr = dpp;
+            m.dstPos = pos;
+            m.kind = cudaMemcpyHostToDevice;
+        } else {
+            m.srcPtr = dpp;
+            m.srcPos = pos;
+            m.dstPtr = hpp;
+            m.kind = cudaMemcpyDeviceToHost;
+        }
+        CK(cudaStreamSynchronize(st));
+        CK(cudaMemcpy3D(&m));
+        if (!up && !isint && sizeof(T) != sizeof(double)) {
+            const T *src = (const T *)hp;
+            double *dst = (double *)host;
+            for (size_t q = 0; q < n; ++q) dst[q] = (double)src[q];
+        }
+        return SULI_OK;
+    }
+
+    // ---- routines -------------------------------------------------------------
+    int heaviside_init() override
+    {
+        launch_heaviside<T>(b, 1, st);
+        CKL();
+        return read_scalars();
+    }
+
+    int level_set() override
+    {
+        int rc;
+        if ((rc = setsc(S_DTADV, dt))) return rc;
+        if ((rc = setsc(S_RINREPLAY, (double)replay_reinit))) return rc;
+        launch_level_set_adv<T>(b, st);
+        launch_reinit<T>(b, P[0].reinit_max_iter, st);
+        launch_heaviside<T>(b, 0, st);
+        CKL();
+        if ((rc = read_scalars())) return rc;
+        vol_loops = 0;
+        for (;;) {
+            bool any = false;
+            for (int c = 0; c < ncases; ++c) any |= (sc(c, S_VOLACTIVE) != 0.0);
+            if (!any) break;
+            if (vol_loops >= P[0].vol_loop_max) {
+                warn |= (1 << SULI_VOL_LOOP_CAP);
+                break;
+            }
+            launch_volcorr<T>(b, st);
+            CKL();
+            ++vol_loops;
+            if ((rc = read_scalars())) return rc;
+        }
+        reinit_iters = (int)sc(0, S_RINITER);
+        return SULI_OK;
+    }
+
+    int contorno(int nlock) override
+    {
+        if (nlock < 1 || nlock > 3) return fail(SULI_BAD_ARG, "nlock must be 1, 2 or 3");
+        if (nlock == 3) return SULI_OK;     // acts only with an immersed boundary
+        launch_contorno<T>(b, nlock, st);
+        CKL();
+        return SULI_OK;
+    }
+
+    int visco() override
+    {
+        launch_visco<T>(b, st);
+        CKL();
+        return SULI_OK;
+    }
+    int convdiff(int fuse) override
+    {
+        launch_convdiff<T>(b, fuse, st);
+        CKL();
+        return SULI_OK;
+    }
+    int complementos() override
+    {
+        launch_complementos<T>(b, st);
+        CKL();
+        return SULI_OK;
+    }
+    int tempo() override
+    {
+        launch_tempo<T>(b, tt, it, st);
+        CKL();
+        return SULI_OK;
+    }
+    int set_stage(int tt_) override
+    {
+        if (tt_ < 1 || tt_ > 3) return fail(SULI_BAD_ARG, "stage must be 1..3");
+        tt = tt_;
+        dt = a_dt[tt - 1];
+        return setsc(S_DT, dt);
+    }
+
+    int graddin(int32_t *iters) override
+    {
+        int rc;
+        const int si = (tt >= 1 && tt <= 3) ? tt - 1 : 0;
+        if ((rc = setsc(S_CGREPLAY, (double)replay_cg[si]))) return rc;
+        const int cgmax = P[0].cg_max_iter;
+        int maxit = 0;
+        if (sizeof(T) == sizeof(double)) {
+            launch_cg_setup<T>(b, st);
+            CKL();
+            int done = 0;
+            int chunk = std::max(1, std::min(prev_cg[si], cgmax));
+            for (;;) {
+                launch_cg_iters<T>(b, chunk, st);
+                CKL();
+                done += chunk;
+                if ((rc = read_scalars())) return rc;
+                bool any = false;
+                for (int c = 0; c < ncases; ++c) any |= (sc(c, S_CGACTIVE) != 0.0);
+                if (!any || done >= cgmax) break;
+                chunk = std::max(4, std::min(64, done / 8));
+            }
+            launch_cg_finish<T>(b, st);
+            CKL();
+            for (int c = 0; c < ncases; ++c) maxit = std::max(maxit, (int)sc(c, S_CGITER));
+            cg_outer[si] = 0;
+        } else {
+            launch_cg_refine_setup<T>(b, st);
+            CKL();
+            int passes = 0;
+            const int inner_max = P[0].mixed_inner_iters > 0 ? P[0].mixed_inner_iters : cgmax;
+            for (;;) {
+                // inner FP32 CG until every active case meets its inner tolerance
+                int done = 0;
+                int chunk = std::max(4, prev_cg[si]);
+                for (;;) {
+                    launch_cg_refine_inner<T>(b, chunk, inner_max, st);
+                    CKL();
+                    done += chunk;
+                    if ((rc = read_scalars())) return rc;
+                    bool any = false;
+                    for (int c = 0; c < ncases; ++c) any |= (sc(c, S_CGACTIVE) != 0.0);
+                    if (!any || done >= cgmax) break;
+                    chunk = std::max(4, std::min(64, done / 8));
+                }
+                launch_cg_refine_next<T>(b, st);
+                CKL();
+                ++passes;
+                if ((rc = read_scalars())) return rc;
+                bool all = true;
+                for (int c = 0; c < ncases; ++c) all &= (sc(c, S_OUTER) < 0.0);
+                if (all || passes >= 50) break;
+            }
+            launch_cg_refine_finish<T>(b, st);
+            CKL();
+            for (int c = 0; c < ncases; ++c) maxit = std::max(maxit, (int)sc(c, S_CGITER));
+            cg_outer[si] = passes;
+        }
+        cg_iters[si] = maxit;
+        cg_res[si] = sc(0, sizeof(T) == sizeof(double) ? S_RR : S_RRTRUE);
+        prev_cg[si] = std::max(1, sizeof(T) == sizeof(double) ? maxit : maxit / std::max(1, cg_outer[si]));
+        if (iters) *iters = maxit;
+        if (maxit >= cgmax && replay_cg[si] < 0) {
+            warn |= (1 << SULI_CG_MAXITER);
+            return fail(SULI_CG_MAXITER, "CG reached cg_max_iter (\"pulou pressao\")");
+        }
+        return SULI_OK;
+    }
+
+    int posdin() override
+    {
+        launch_posdin<T>(b, st);
+        CKL();
+        for (int c = 0; c < ncases; ++c)
+            CK(cudaMemcpyAsync(hc[c].prd, hc[c].prd1, sizeof(T) * (size_t)hc[c].g.total, cudaMemcpyDeviceToDevice, st));
+        return SULI_OK;
+    }
+
+    int conmassa(double *maxdiv) override
+    {
+        launch_conmassa<T>(b, st);
+        CKL();
+        if (maxdiv) {
+            int rc = read_scalars();
+            if (rc) return rc;
+            *maxdiv = sc(0, S_MAXDIV);
+        }
+        return SULI_OK;
+    }
+
+    int mms_error(double *err) override
+    {
+        launch_mms_error<T>(b, st);
+        CKL();
+        int rc = read_scalars();
+        if (rc) return rc;
+        for (int q = 0; q < 4; ++q) err[q] = sc(0, S_ERR0 + q);
+        return SULI_OK;
+    }
+
+    // the body of the time loop, 1_principal.f90:69-124 (PLOT output excluded)
+    int step(int n) override
+    {
+        int rc;
+        for (int s = 0; s < n; ++s) {
+            it = it + 1;
+            t = t + dt;
+            if ((rc = level_set())) return rc;
+            if ((rc = contorno(3))) return rc;
+            if ((rc = visco())) return rc;
+            for (int q = 1; q <= ntt; ++q) {
+                if ((rc = set_stage(q))) return rc;
+                if ((rc = convdiff(1))) return rc;
+                if ((rc = tempo())) return rc;
+                if ((rc = contorno(2))) return rc;
+                if (P[0].mms_t == 0 || P[0].project_under_mms) {
+                    rc = graddin(nullptr);
+                    if (rc && rc != SULI_CG_MAXITER) return rc;
+                    if ((rc = posdin())) return rc;
+                    if ((rc = contorno(1))) return rc;
+                }
+            }
+            if ((rc = conmassa(nullptr))) return rc;
+        }
+        return SULI_OK;
+    }
+};
+
+// ---------------------------------------------------------------------------
+static int check_device()
+{
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0)
+        return fail(SULI_NO_DEVICE, std::string("no CUDA device: ") + (e != cudaSuccess ? cudaGetErrorString(e) : "count 0"));
+    return SULI_OK;
+}
+
+extern "C" int suli_create_batch(const suli_params *p, int ncases, suli_handle **out)
+{
+    if (!p || !out || ncases < 1) return fail(SULI_BAD_ARG, "bad arguments to suli_create_batch");
+    *out = nullptr;
+    for (int c = 0; c < ncases; ++c) {
+        int rc = validate(p[c]);
+        if (rc) return rc;
+        if (p[c].precision != p[0].precision || p[c].t_tempo != p[0].t_tempo || p[c].mms_t != p[0].mms_t ||
+            p[c].dt != p[0].dt || p[c].reinit_max_iter != p[0].reinit_max_iter ||
+            p[c].project_under_mms != p[0].project_under_mms)
+            return fail(SULI_BAD_CONFIG, "cases of a batch must share precision, t_tempo, mms_t, dt and reinit_max_iter");
+    }
+    int rc = check_device();
+    if (rc) return rc;
+    ImplBase *impl;
+    if (p[0].precision == SULI_PREC_FP64) {
+        auto *im = new Impl<double>();
+        rc = im->create(p, ncases);
+        impl = im;
+    } else {
+        auto *im = new Impl<float>();
+        rc = im->create(p, ncases);
+        impl = im;
+    }
+    if (rc) {
+        delete impl;
+        return rc;
+    }
+    *out = new suli_handle{impl};
+    return SULI_OK;
+}
+
+extern "C" int suli_create(const suli_params *p, suli_handle **out) { return suli_create_batch(p, 1, out); }
+
+extern "C" int suli_num_cases(const suli_handle *h, int *n)
+{
+    if (!h || !n) return fail(SULI_BAD_ARG, "null argument");
+    *n = h->impl->ncases;
+    return SULI_OK;
+}
+
+extern "C" int suli_destroy(suli_handle *h)
+{
+    if (!h) return SULI_OK;
+    delete h->impl;
+    delete h;
+    return SULI_OK;
+}
+
+#define HCHK()                                                   \
+    do {                                                         \
+        if (!h) return fail(SULI_BAD_ARG, "null handle");        \
+    } while (0)
+
+extern "C" int suli_upload_field(suli_handle *h, int icase, int field, const void *host)
+{
+    HCHK();
+    if (!host) return fail(SULI_BAD_ARG, "null host pointer");
+    return h->impl->copy_field(icase, field, const_cast<void *>(host), true);
+}
+
+extern "C" int suli_download_field(suli_handle *h, int icase, int field, void *host)
+{
+    HCHK();
+    if (!host) return fail(SULI_BAD_ARG, "null host pointer");
+    return h->impl->copy_field(icase, field, host, false);
+}
+
+extern "C" int suli_set_scalar(suli_handle *h, int icase, int s, double v)
+{
+    HCHK();
+    ImplBase *im = h->impl;
+    switch (s) {
+    case SULI_S_T: im->t = v; return SULI_OK;
+    case SULI_S_DT: im->dt = v; return SULI_OK;
+    case SULI_S_IT: im->it = (int)v; return SULI_OK;
+    case SULI_S_TT: im->tt = (int)v; return SULI_OK;
+    case SULI_S_VOL_INI:
+    case SULI_S_VOL_INS: {
+        if (icase < 0 || icase >= im->ncases) return fail(SULI_BAD_ARG, "case index out of range");
+        return im->write_case_scalar(icase, s == SULI_S_VOL_INI ? S_VOLINI : S_VOLINS, v);
+    }
+    default: return fail(SULI_BAD_ARG, "scalar not settable");
+    }
+}
+
+extern "C" int suli_get_scalar(suli_handle *h, int icase, int s, double *v)
+{
+    HCHK();
+    if (!v) return fail(SULI_BAD_ARG, "null pointer");
+    ImplBase *im = h->impl;
+    if (icase < 0 || icase >= im->ncases) return fail(SULI_BAD_ARG, "case index out of range");
+    switch (s) {
+    case SULI_S_T: *v = im->t; return SULI_OK;
+    case SULI_S_DT: *v = im->dt; return SULI_OK;
+    case SULI_S_IT: *v = im->it; return SULI_OK;
+    case SULI_S_TT: *v = im->tt; return SULI_OK;
+    default: break;
+    }
+    int rc = im->read_scalars();
+    if (rc) return rc;
+    const double *sc = im->hsc + (size_t)icase * S_NSCAL;
+    switch (s) {
+    case SULI_S_VOL_INI: *v = sc[S_VOLINI]; return SULI_OK;
+    case SULI_S_VOL_INS: *v = sc[S_VOLINS]; return SULI_OK;
+    case SULI_S_MAXDIV: *v = sc[S_MAXDIV]; return SULI_OK;
+    default: return fail(SULI_BAD_ARG, "unknown scalar");
+    }
+}
+
+extern "C" int suli_set_replay(suli_handle *h, const int32_t cg[3], int32_t reinit)
+{
+    HCHK();
+    for (int q = 0; q < 3; ++q) h->impl->replay_cg[q] = cg ? cg[q] : -1;
+    h->impl->replay_reinit = reinit;
+    return SULI_OK;
+}
+
+extern "C" int suli_heaviside_init(suli_handle *h) { HCHK(); return h->impl->heaviside_init(); }
+extern "C" int suli_level_set(suli_handle *h) { HCHK(); return h->impl->level_set(); }
+extern "C" int suli_contorno(suli_handle *h, int nlock) { HCHK(); return h->impl->contorno(nlock); }
+extern "C" int suli_visco(suli_handle *h) { HCHK(); return h->impl->visco(); }
+extern "C" int suli_convdiff(suli_handle *h) { HCHK(); return h->impl->convdiff(0); }
+extern "C" int suli_complementos(suli_handle *h) { HCHK(); return h->impl->complementos(); }
+extern "C" int suli_tempo(suli_handle *h) { HCHK(); return h->impl->tempo(); }
+extern "C" int suli_graddin(suli_handle *h, int32_t *iters) { HCHK(); return h->impl->graddin(iters); }
+extern "C" int suli_posdin(suli_handle *h) { HCHK(); return h->impl->posdin(); }
+extern "C" int suli_conmassa(suli_handle *h, double *m) { HCHK(); return h->impl->conmassa(m); }
+extern "C" int suli_mms_error(suli_handle *h, double err[4])
+{
+    HCHK();
+    if (!err) return fail(SULI_BAD_ARG, "null pointer");
+    return h->impl->mms_error(err);
+}
+extern "C" int suli_set_stage(suli_handle *h, int tt) { HCHK(); return h->impl->set_stage(tt); }
+extern "C" int suli_step(suli_handle *h, int n)
+{
+    HCHK();
+    if (n < 0) return fail(SULI_BAD_ARG, "nsteps < 0");
+    return h->impl->step(n);
+}
+extern "C" int suli_synchronize(suli_handle *h) { HCHK(); return h->impl->sync(); }
+
+extern "C" int suli_diagnostics(suli_handle *h, int icase, suli_diag *d)
+{
+    HCHK();
+    if (!d) return fail(SULI_BAD_ARG, "null pointer");
+    ImplBase *im = h->impl;
+    if (icase < 0 || icase >= im->ncases) return fail(SULI_BAD_ARG, "case index out of range");
+    int rc = im->read_scalars();
+    if (rc) return rc;
+    const double *sc = im->hsc + (size_t)icase * S_NSCAL;
+    std::memset(d, 0, sizeof(*d));
+    d->vol_ini = sc[S_VOLINI];
+    d->vol_ins = sc[S_VOLINS];
+    d->maxdiv = sc[S_MAXDIV];
+    d->t = im->t;
+    for (int q = 0; q < 3; ++q) {
+        d->cg_iters[q] = im->cg_iters[q];
+        d->cg_outer[q] = im->cg_outer[q];
+        d->cg_res[q] = im->cg_res[q];
+    }
+    d->reinit_iters = (int)sc[S_RINITER];
+    d->vol_loops = im->vol_loops;
+    d->it = im->it;
+    d->status_flags = im->warn;
+    im->warn = 0;
+    return SULI_OK;
+}
+
+extern "C" int suli_last_error(char *buf, size_t len)
+{
+    if (!buf || len == 0) return SULI_BAD_ARG;
+    std::snprintf(buf, len, "%s", g_err.c_str());
+    return SULI_OK;
+}
+
+extern "C" int suli_device_info(int *sm_count, char *name, size_t name_len)
+{
+    int rc = check_device();
+    if (rc) return rc;
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    cudaDeviceProp prop;
+    CK(cudaGetDeviceProperties(&prop, dev));
+    if (sm_count) *sm_count = prop.multiProcessorCount;
+    if (name && name_len) std::snprintf(name, name_len, "%s", prop.name);
+    return SULI_OK;
+}

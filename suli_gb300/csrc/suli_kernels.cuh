@@ -1,0 +1,52 @@
+// suli_kernels.cuh -- launch interface between the C ABI layer and the
+// kernel translation units.
+#pragma once
+
+#include "suli_common.cuh"
+
+namespace suli {
+
+// A batch of cases with a device copy of their CaseDev table.
+template <typename T>
+struct Batch {
+    CaseDev<T> *dcases = nullptr;     // device table
+    CaseDev<T> *hcases = nullptr;     // host mirror
+    int ncases = 0;
+    int total_tiles = 0;
+    int max_plane = 0;                // largest boundary plane (elements)
+    double *drk = nullptr;            // TVD-RK3 coefficients a[3], b[3], g[3]
+    dim3 block() const { return dim3(TX, TY, TZ); }
+};
+
+// level set (k_levelset.cu)
+template <typename T> void launch_level_set_adv(const Batch<T> &b, cudaStream_t s);
+template <typename T> void launch_reinit(const Batch<T> &b, int max_iter, cudaStream_t s);
+template <typename T> void launch_heaviside(const Batch<T> &b, int set_ini, cudaStream_t s);
+template <typename T> void launch_volcorr(const Batch<T> &b, cudaStream_t s);
+
+// momentum (k_momentum.cu)
+template <typename T> void launch_visco(const Batch<T> &b, cudaStream_t s);
+template <typename T> void launch_convdiff(const Batch<T> &b, int fuse_compl, cudaStream_t s);
+template <typename T> void launch_complementos(const Batch<T> &b, cudaStream_t s);
+template <typename T> void launch_tempo(const Batch<T> &b, int tt, int it, cudaStream_t s);
+template <typename T> void launch_posdin(const Batch<T> &b, cudaStream_t s);
+template <typename T> void launch_conmassa(const Batch<T> &b, cudaStream_t s);
+template <typename T> void launch_mms_error(const Batch<T> &b, cudaStream_t s);
+
+// boundary conditions (k_bc.cu)
+template <typename T> void launch_contorno(const Batch<T> &b, int nlock, cudaStream_t s);
+
+// pressure (k_cg.cu)
+template <typename T> void launch_cg_setup(const Batch<T> &b, cudaStream_t s);
+template <typename T> void launch_cg_iters(const Batch<T> &b, int n, cudaStream_t s);
+template <typename T> void launch_cg_finish(const Batch<T> &b, cudaStream_t s);
+// mixed form: FP64 residual recomputation and correction around the FP32 inner CG
+template <typename T> void launch_cg_refine_setup(const Batch<T> &b, cudaStream_t s);
+template <typename T> void launch_cg_refine_inner(const Batch<T> &b, int n, int inner_max, cudaStream_t s);
+template <typename T> void launch_cg_refine_next(const Batch<T> &b, cudaStream_t s);
+template <typename T> void launch_cg_refine_finish(const Batch<T> &b, cudaStream_t s);
+
+// per-case scalar kernels
+template <typename T> void launch_set_scalar(const Batch<T> &b, int slot, double v, cudaStream_t s);
+
+}  // namespace suli

@@ -1,0 +1,49 @@
+"""Shared helpers of the parity tests: build an oracle/GPU pair on the same
+initial state, copy oracle state to the GPU, compare fields."""
+import numpy as np
+
+import pyoracle
+
+STATE_FIELDS = ["U", "V", "W", "PRD1", "PRD", "LS", "HS", "RHO", "LS_MU", "MU", "MUT", "XMU", "YMU", "ZMU",
+                "FU", "FV", "FW", "U0", "V0", "W0", "FU0", "FV0", "FW0", "FU1", "FV1", "FW1",
+                "TF_U", "TF_V", "TF_W"]
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    n = np.linalg.norm(b.ravel())
+    d = np.linalg.norm((a - b).ravel())
+    return d / n if n > 0 else d
+
+
+def oracle_for(case, warm_steps=0):
+    o = pyoracle.Oracle(case.params)
+    for k, v in case.fields.items():
+        o.set_field(k, v)
+    if case.params.mms_t:
+        o.termo_fonte1()
+    o.heaviside_init()
+    for n in (1, 2, 3):
+        o.contorno(n)
+    for _ in range(warm_steps):
+        o.step()
+    return o
+
+
+def copy_state(o, g, case=0):
+    for name in STATE_FIELDS:
+        g.upload(name, o.field(name), case=case)
+    g.set_scalar("VOL_INI", o.scalar("VOL_INI"), case=case)
+    g.set_scalar("VOL_INS", o.scalar("VOL_INS"), case=case)
+    g.set_scalar("T", o.scalar("T"))
+    g.set_scalar("IT", o.scalar("IT"))
+
+
+def compare(o, g, names, tol, case=0):
+    out = {}
+    for name in names:
+        out[name] = rel_l2(g.download(name, case=case), o.field(name))
+    bad = {k: v for k, v in out.items() if not v <= tol}
+    assert not bad, "rel L2 above %g: %s (all: %s)" % (tol, bad, out)
+    return out

@@ -1,0 +1,166 @@
+"""GPU parity of the plain FP64 form against the CPU oracle, through the C ABI.
+
+Every reference routine is checked on its own from an identical state (the
+oracle's state after a few warm-up steps uploaded into the GPU case), then
+whole time steps are checked with the oracle's data-dependent iteration
+counts replayed (CG iterations per RK stage, reinitialisation iterations) so
+that both sides take the same control path.  Bar: relative L2 <= 1e-10.
+"""
+import numpy as np
+import pytest
+
+from helpers import compare, copy_state, oracle_for, rel_l2
+from suli_gb300 import cases
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+def _configs():
+    return [
+        ("dam_break", cases.dam_break(24, 12, 12)),
+        ("wave_les", cases.wave_tank(32, 8, 12, dt=5e-4)),
+        ("mms_periodic", cases.mms_case(16)),
+    ]
+
+
+@pytest.fixture(scope="module", params=_configs(), ids=lambda c: c[0])
+def pair(request, gpu_lib):
+    name, case = request.param
+    o = oracle_for(case, warm_steps=3)
+    g = gpu_lib.SuliGPU(case.params)
+    g.start(case.fields)
+    yield case, o, g
+    g.close()
+
+
+def _sync(o, g):
+    copy_state(o, g)
+
+
+def test_level_set(pair):
+    case, o, g = pair
+    _sync(o, g)
+    g.set_scalar("DT", o.scalar("DT"))
+    o.level_set()
+    g.set_replay(None, o.diag().reinit_iters)
+    g.level_set()
+    g.set_replay(None, -1)
+    compare(o, g, ["LS", "HS", "RHO", "LS_MU"], TOL)
+    assert g.diag().reinit_iters == o.diag().reinit_iters
+    assert abs(g.scalar("VOL_INS") - o.scalar("VOL_INS")) <= 1e-12 * abs(o.scalar("VOL_INS"))
+
+
+def test_level_set_free_running(pair):
+    """Without replay the GPU's own signed band-error test picks the same count."""
+    case, o, g = pair
+    _sync(o, g)
+    g.set_scalar("DT", o.scalar("DT"))
+    o.level_set()
+    g.level_set()
+    assert g.diag().reinit_iters == o.diag().reinit_iters
+    compare(o, g, ["LS"], TOL)
+
+
+def test_visco(pair):
+    case, o, g = pair
+    _sync(o, g)
+    o.visco()
+    g.visco()
+    compare(o, g, ["MU", "XMU", "YMU", "ZMU"], TOL)
+    if case.params.m_turb:
+        compare(o, g, ["MUT"], TOL)
+
+
+@pytest.mark.parametrize("tt", [1, 2, 3])
+def test_convdiff_complementos_tempo(pair, tt):
+    case, o, g = pair
+    _sync(o, g)
+    o.visco()
+    g.visco()
+    o.set_stage(tt)
+    g.set_stage(tt)
+    o.convdiff()
+    g.convdiff()
+    compare(o, g, ["FU", "FV", "FW"], TOL)
+    o.complementos()
+    g.complementos()
+    compare(o, g, ["FU", "FV", "FW"], TOL)
+    o.tempo()
+    g.tempo()
+    compare(o, g, ["U", "V", "W"], TOL)
+
+
+@pytest.mark.parametrize("nlock", [1, 2])
+def test_contorno(pair, nlock):
+    case, o, g = pair
+    _sync(o, g)
+    # perturb ghosts so the fills are exercised
+    rng = np.random.default_rng(nlock)
+    for name in ("U", "V", "W", "PRD1"):
+        a = o.field(name)
+        a[0, :, :] += rng.standard_normal(a[0].shape)
+        a[:, 0, :] += rng.standard_normal(a[:, 0].shape)
+        a[:, :, -1] += rng.standard_normal(a[:, :, -1].shape)
+        g.upload(name, a)
+    o.contorno(nlock)
+    g.contorno(nlock)
+    for name in ("U", "V", "W", "PRD1"):
+        d = np.abs(g.download(name) - o.field(name)).max()
+        assert d == 0.0, "%s ghost fill differs by %g" % (name, d)
+
+
+def test_graddin_posdin(pair):
+    case, o, g = pair
+    if case.params.mms_t and not case.params.project_under_mms:
+        pytest.skip("no projection")
+    _sync(o, g)
+    for tt in (1, 2):
+        o.set_stage(tt)
+        g.set_stage(tt)
+        o.visco(); g.visco()
+        o.convdiff(); g.convdiff()
+        o.complementos(); g.complementos()
+        o.tempo(); g.tempo()
+        o.contorno(2); g.contorno(2)
+        it_o = o.graddin()
+        g.set_replay([it_o] * 3, -1)
+        it_g = g.graddin()
+        g.set_replay(None, -1)
+        assert it_g == it_o
+        compare(o, g, ["PRD1"], TOL)
+        o.posdin(); g.posdin()
+        compare(o, g, ["U", "V", "W", "PRD"], TOL)
+        o.contorno(1); g.contorno(1)
+    m_o = o.conmassa()
+    m_g = g.conmassa()
+    assert abs(m_g - m_o) <= 1e-6 * max(m_o, 1e-300) + 1e-13
+
+
+def test_graddin_free_running_iterations(pair):
+    """The GPU's own stopping test lands on the oracle's count (or one off)."""
+    case, o, g = pair
+    if case.params.mms_t and not case.params.project_under_mms:
+        pytest.skip("no projection")
+    _sync(o, g)
+    o.set_stage(1)
+    g.set_stage(1)
+    it_o = o.graddin()
+    it_g = g.graddin()
+    assert abs(it_g - it_o) <= 1
+    assert rel_l2(g.download("PRD1"), o.field("PRD1")) <= 1e-8
+
+
+def test_steps_replayed(pair):
+    case, o, g = pair
+    _sync(o, g)
+    g.set_scalar("DT", o.scalar("DT"))
+    for _ in range(3):
+        o.step()
+        d = o.diag()
+        g.set_replay(list(d.cg_iters), d.reinit_iters)
+        g.step(1)
+    g.set_replay(None, -1)
+    compare(o, g, ["U", "V", "W", "PRD1", "LS", "RHO"], TOL)
+    assert abs(g.diag().maxdiv - o.diag().maxdiv) <= 1e-6 * o.diag().maxdiv + 1e-13
