@@ -1,0 +1,367 @@
+#!/usr/bin/env python
+"""Benchmark of the SuLi per-time-step hot path on GB300.
+
+Workload (default): the batched ensemble -- 256 independent sloshing /
+dam-break cases, grid dims drawn per axis from U{32..96} (seed 0), advanced
+in lockstep by the same launches, mixed precision (FP32 storage and
+stencils, FP32 inner CG inside FP64 iterative refinement, FP64 sums).  A
+"step" is one full time step of every case (1_principal.f90:69-124).
+
+Printed JSON line (rank 0): value = cell-steps/s of the mixed form with all
+fields resident in HBM; the plain FP64 form of the same workload is timed
+beside it ("fp64"), the e2e figure goes through the C ABI with host
+buffers (state uploaded from pinned host memory and read back every step),
+the roofline entry is the CG iteration loop (event-timed inside the
+library's stream) and cpu_baseline is the oracle (a port of the reference,
+OpenMP where the reference has it) on a bounded sample.
+
+--impl reference times the reference's CPU implementation (the oracle port:
+no Fortran compiler exists on either machine) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="ensemble", choices=["ensemble", "wave_tank", "dam_break"])
+    ap.add_argument("--ncases", type=int, default=256)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+def make_cases(args, precision, rank=0):
+    from suli_gb300 import cases
+    if args.workload == "ensemble":
+        dims, hcol, amp = cases.ensemble_dims(args.ncases, seed=rank)
+        cs = [cases.ensemble_case(i, dims, hcol, amp, precision=precision) for i in range(args.ncases)]
+        name = "ensemble_%d_U32-96_seed%d" % (args.ncases, rank)
+    elif args.workload == "wave_tank":
+        cs = [cases.wave_tank(precision=precision)]
+        name = "wave_tank_1024x256x256"
+    else:
+        cs = [cases.dam_break(precision=precision)]
+        name = "dam_break_64x32x32"
+    return name, cs
+
+
+class ClockSampler:
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        cmd = ["nvidia-smi", "-i", str(self.index),
+               "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+               "--format=csv,noheader,nounits", "-lms", "200"]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thr = threading.Thread(target=self._read, daemon=True)
+            self.thr.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        for k in ("hbm_gbs", "hbm_GBs", "hbm"):
+            if k in d:
+                v = d[k]
+                if isinstance(v, dict):
+                    v = v.get("burst", v.get("value"))
+                return float(v), "measured"
+    except Exception:
+        pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def start_gpu(cs):
+    from suli_gb300.solver import SuliGPU
+    g = SuliGPU([c.params for c in cs])
+    g.start([c.fields for c in cs])
+    return g
+
+
+def timed_steps(g, k, torch):
+    """Time k steps with CUDA events on the library's stream (synchronized on both sides)."""
+    s = torch.cuda.ExternalStream(g.stream_handle())
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    g.synchronize()
+    e0.record(s)
+    g.step(k)
+    e1.record(s)
+    g.synchronize()
+    e1.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def run_form(args, cs, torch, sampler=None, dist=None):
+    g = start_gpu(cs)
+    g.step(args.warmup)
+    g.synchronize()
+    if dist is not None:
+        dist.barrier()
+    g.profile(True)
+    if sampler:
+        sampler.start()
+    ms = timed_steps(g, args.steps, torch)
+    clocks = sampler.stop() if sampler else None
+    prof = g.profile_read()
+    if dist is not None:
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return g, ms, prof, clocks
+
+
+def rel_l2(a, b):
+    n = np.linalg.norm(b.ravel())
+    return float(np.linalg.norm((a - b).ravel()) / n) if n > 0 else float(np.linalg.norm(a.ravel()))
+
+
+def compare_forms(gm, g64, ncheck):
+    errs = {"velocity": 0.0, "PRD1": 0.0, "LS": 0.0}
+    for c in range(ncheck):
+        vm = np.concatenate([gm.download(n, c).ravel() for n in ("U", "V", "W")])
+        v6 = np.concatenate([g64.download(n, c).ravel() for n in ("U", "V", "W")])
+        errs["velocity"] = max(errs["velocity"], rel_l2(vm, v6))
+        for n in ("PRD1", "LS"):
+            a = gm.download(n, c)[1:-1, 1:-1, 1:-1] if n == "PRD1" else gm.download(n, c)
+            b = g64.download(n, c)[1:-1, 1:-1, 1:-1] if n == "PRD1" else g64.download(n, c)
+            if n == "PRD1":
+                a = a - a.mean()
+                b = b - b.mean()
+            errs[n] = max(errs[n], rel_l2(a, b))
+    return errs
+
+
+def e2e_run(args, cs, torch):
+    """Per step: pinned host state -> device, one step, device -> host."""
+    g = start_gpu(cs)
+    g.step(1)
+    names = ("U", "V", "W", "LS", "PRD1")
+    host = []
+    h2d = 0
+    for c in range(len(cs)):
+        d = {}
+        for n in names:
+            a = g.download(n, c)
+            pinned = torch.empty(a.shape[::-1], dtype=torch.float64).pin_memory().numpy().T
+            pinned[...] = a
+            d[n] = pinned
+            h2d += a.nbytes
+        host.append(d)
+    g.synchronize()
+    ksteps = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for _ in range(ksteps):
+        for c, d in enumerate(host):
+            for n, a in d.items():
+                g.upload(n, a, c)
+        g.step(1)
+        for c, d in enumerate(host):
+            for n in d:
+                d[n][...] = g.download(n, c)
+    g.synchronize()
+    dt = time.perf_counter() - t0
+    cells = sum(c.cells for c in cs)
+    g.close()
+    return {"value": cells * ksteps / dt, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": h2d, "steps": ksteps,
+            "path": "suli_upload_field/suli_step/suli_download_field, pinned host buffers"}
+
+
+def cpu_baseline(args, cs):
+    """The oracle (port of the reference) on a bounded sample: the first case
+    of the workload, stepped until ~cpu_seconds of work have been done."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    pyoracle.Oracle.set_threads(cores)
+    c = cs[0]
+    p = c.params.copy()
+    p.precision = 0
+    o = pyoracle.Oracle(p)
+    for k, v in c.fields.items():
+        o.set_field(k, v)
+    o.heaviside_init()
+    for n in (1, 2, 3):
+        o.contorno(n)
+    o.step(1)
+    steps = 0
+    t0 = time.perf_counter()
+    while True:
+        o.step(1)
+        steps += 1
+        if time.perf_counter() - t0 > args.cpu_seconds or steps >= 50:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": c.cells * steps / dt, "unit": "cell-steps/s", "cores": cores, "kind": "port",
+            "sample": "%s: %d steps of one %dx%dx%d case, FP64 oracle, OpenMP in CG/interp as upstream"
+                      % (c.name, steps, p.nx, p.ny, p.nz)}
+
+
+# ---------------------------------------------------------------------------
+def main():
+    args = parse()
+    assert args.warmup >= 3 or args.impl == "reference", "at least 3 warm-up steps"
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+    from suli_gb300._abi import PREC_FP64, PREC_MIXED
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        name, cs = make_cases(args, PREC_FP64)
+        res = cpu_baseline(args, cs) if True else None
+        line = {"metric": "cell-steps/s", "value": res["value"], "unit": "cell-steps/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "impl": "reference",
+                "config": {"workload": name, "sample": res["sample"]},
+                "cpu_baseline": res,
+                "e2e": {"value": res["value"], "unit": "cell-steps/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    from suli_gb300 import build
+    build.build()
+    from suli_gb300 import solver
+    sms, devname = solver.device_info()
+
+    name, cs_m = make_cases(args, PREC_MIXED, rank)
+    cells = sum(c.cells for c in cs_m)
+    sampler = ClockSampler(local) if rank == 0 else None
+    gm, ms_m, prof_m, clocks = run_form(args, cs_m, torch, sampler, dist)
+    value = world * cells * args.steps / (ms_m / 1e3)
+    peak, peak_src = measured_peak_hbm()
+    s_bytes = 4.0
+    cg_ach = None
+    if prof_m.cg_ms > 0:
+        cg_ach = 7.0 * s_bytes * prof_m.cg_cell_iters / (prof_m.cg_ms / 1e3) / 1e9
+    line = {
+        "metric": "cell-steps/s (mixed-precision batched SuLi steps)",
+        "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_m / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": name, "cases": len(cs_m), "cells_per_gpu": cells, "precision": "mixed",
+                   "l2": "inputs larger than L2 (working set %.1f GB)" % (cells * 4 * 46 / 1e9),
+                   "device": devname, "sms": sms},
+        "gpu_launches": int(prof_m.launches),
+        "clocks": clocks,
+        "roofline": {"bound": "hbm", "kernel": "CG iteration (k_cg_A + k_cg_B_inner + k_cg_C)",
+                     "achieved": cg_ach, "peak": peak, "unit": "GB/s",
+                     "frac": (cg_ach / peak) if cg_ach else None, "traffic": None,
+                     "peak_source": peak_src,
+                     "algorithmic_bytes_per_cell_iter": 7 * s_bytes,
+                     "kernel_bytes_per_cell_iter": prof_m.cg_bytes_per_cell_iter,
+                     "cg_cell_iters": prof_m.cg_cell_iters, "cg_ms": prof_m.cg_ms},
+    }
+    diag = gm.diag(0)
+    line["cg_iters_case0"] = list(diag.cg_iters)
+    line["cg_outer_case0"] = list(diag.cg_outer)
+    if not args.no_fp64:
+        try:
+            name64, cs_64 = make_cases(args, PREC_FP64, rank)
+            g64, ms_64, prof_64, _ = run_form(args, cs_64, torch, None, dist)
+            v64 = world * cells * args.steps / (ms_64 / 1e3)
+            line["fp64"] = {"value": v64, "ms_per_step": ms_64 / args.steps,
+                            "cg_GBs_algorithmic": (7 * 8.0 * prof_64.cg_cell_iters / (prof_64.cg_ms / 1e3) / 1e9)
+                            if prof_64.cg_ms > 0 else None,
+                            "gpu_launches": int(prof_64.launches)}
+            line["mixed_over_fp64"] = value / v64
+            line["mixed_vs_fp64_rel_l2"] = compare_forms(gm, g64, min(4, len(cs_m)))
+            g64.close()
+        except Exception as e:  # reported, not hidden
+            line["fp64"] = {"error": repr(e)}
+    gm.close()
+    if not args.no_e2e:
+        try:
+            line["e2e"] = e2e_run(args, cs_m, torch)
+        except Exception as e:
+            line["e2e"] = {"error": repr(e)}
+    if rank == 0 and not args.no_cpu:
+        try:
+            line["cpu_baseline"] = cpu_baseline(args, cs_m)
+        except Exception as e:
+            line["cpu_baseline"] = {"error": repr(e)}
+    if rank == 0:
+        print(json.dumps(line))
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

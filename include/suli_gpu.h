@@ -137,6 +137,7 @@ enum suli_scalar {
     SULI_S_MAXDIV,     /* maxval(abs(div)) of the last suli_conmassa */
     SULI_S_IT,         /* time-step counter (as double) */
     SULI_S_TT,         /* RK stage (as double) */
+    SULI_S_RNG,        /* inflow perturbation draws so far (calls of the ccx0 = 3 fill) */
     SULI_S_COUNT
 };
 
@@ -183,6 +184,11 @@ int suli_set_replay(suli_handle *h, const int32_t cg_iters[3], int32_t reinit_it
  * level_set_ini() :187-194; call once after uploading ls. */
 int suli_heaviside_init(suli_handle *h);
 
+/* obstaculo() tail for ibm_t = 2 (3_contorno.f90:991-1002): after the
+ * obstacle level sets obs_lsx/y/z/s are uploaded, reinitialise them and
+ * build the integer image-point masks id_ibm* (ibm_posicoes, 15_ibm.f90:9-131). */
+int suli_ibm_setup(suli_handle *h);
+
 /* One entry point per reference subroutine. */
 int suli_level_set(suli_handle *h);              /* 14_level_set.f90:204-273 */
 int suli_contorno(suli_handle *h, int nlock);    /* 3_contorno.f90:11-662 */
@@ -203,6 +209,21 @@ int suli_step(suli_handle *h, int nsteps);
 
 int suli_diagnostics(suli_handle *h, int icase, suli_diag *out);
 int suli_synchronize(suli_handle *h);
+
+/* Measurement support.  suli_get_stream: the CUDA stream (cudaStream_t)
+ * every kernel of the handle is launched on, for events recorded by the
+ * caller.  suli_profile(h, 1) starts counting kernel launches and timing the
+ * CG iteration loop with CUDA events on that stream; suli_profile_read
+ * returns the totals since then. */
+typedef struct suli_profile_t {
+    uint64_t launches;          /* kernels launched by the handle */
+    double   cg_ms;             /* event time spent in CG iteration chunks */
+    double   cg_cell_iters;     /* sum over cases of cells x CG iterations */
+    double   cg_bytes_per_cell_iter; /* bytes the iteration kernels move per cell */
+} suli_profile_t;
+int suli_get_stream(suli_handle *h, void **stream);
+int suli_profile(suli_handle *h, int enable);
+int suli_profile_read(suli_handle *h, suli_profile_t *out);
 
 /* Text of the last error on this thread (empty if none). */
 int suli_last_error(char *buf, size_t len);

@@ -259,6 +259,7 @@ int or_set_scalar(or_case *c, int s, double v)
     case SULI_S_VOL_INS: c->vol_ins = v; return 0;
     case SULI_S_IT: c->it = (int)v; return 0;
     case SULI_S_TT: c->tt = (int)v; return 0;
+    case SULI_S_RNG: c->rng_counter = (unsigned long long)v * (unsigned long long)c->ny * (unsigned long long)c->nz; return 0;
     default: return 1;
     }
 }
@@ -273,6 +274,7 @@ double or_get_scalar(or_case *c, int s)
     case SULI_S_MAXDIV: return c->maxdiv;
     case SULI_S_IT: return (double)c->it;
     case SULI_S_TT: return (double)c->tt;
+    case SULI_S_RNG: return (double)(c->rng_counter / ((unsigned long long)c->ny * (unsigned long long)c->nz));
     default: return 0.0;
     }
 }

@@ -115,7 +115,7 @@ FIELDS = [
 FIELD_ID = {name: i for i, name in enumerate(FIELDS)}
 INT_FIELDS = {"ID_IBMX", "ID_IBMY", "ID_IBMZ", "ID_IBM"}
 
-SCALARS = ["T", "DT", "VOL_INI", "VOL_INS", "MAXDIV", "IT", "TT"]
+SCALARS = ["T", "DT", "VOL_INI", "VOL_INS", "MAXDIV", "IT", "TT", "RNG"]
 SCALAR_ID = {name: i for i, name in enumerate(SCALARS)}
 
 

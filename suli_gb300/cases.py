@@ -152,7 +152,35 @@ def mms_case(n=32, precision=PREC_FP64, dt=None, project=True) -> Case:
     return Case("mms_%d" % n, p, f, steps=100)
 
 
-def open_channel(nx=512, ny=128, nz=128, precision=PREC_FP64, dt=1e-3, seed=1234) -> Case:
+def cylinder_obstacle(p: SuliParams, xc: float, yc: float, radius: float) -> dict:
+    """Vertical cylinder as an obstacle level set (positive inside):
+    phi_s = R - sqrt((x-xc)^2 + (y-yc)^2) on the half-cell sub-grid of
+    obstaculo() (x = (i-1) dx/2, 3_contorno.f90:829-841) sampled at the
+    staggered locations as 3_contorno.f90:951-989 does."""
+    nx, ny, nz = p.nx, p.ny, p.nz
+
+    def phi(ii, jj):
+        x = (ii - 1.0) * p.dx * 0.5
+        y = (jj - 1.0) * p.dy * 0.5
+        return radius - np.sqrt(np.power(x - xc, 2.0) + np.power(y - yc, 2.0))
+
+    def field(ni, nj, nk, fi, fj):
+        i = np.arange(1, ni + 1)[:, None, None]
+        j = np.arange(1, nj + 1)[None, :, None]
+        out = np.empty((ni, nj, nk), order="F")
+        out[...] = phi(fi(i), fj(j))
+        return out
+
+    return {
+        "OBS_LSX": field(nx + 1, ny, nz, lambda i: 2 * i - 1, lambda j: 2 * j),
+        "OBS_LSY": field(nx, ny + 1, nz, lambda i: 2 * i, lambda j: 2 * j - 1),
+        "OBS_LSZ": field(nx, ny, nz + 1, lambda i: 2 * i, lambda j: 2 * j),
+        "OBS_LSS": field(nx, ny, nz, lambda i: 2 * i, lambda j: 2 * j),
+    }
+
+
+def open_channel(nx=512, ny=128, nz=128, precision=PREC_FP64, dt=1e-3, seed=1234, radius=0.05,
+                 cg_tol=1e-8) -> Case:
     """Open channel, 4 x 1 x 1 m, depth 0.6 m flat surface, inflow u = 0.5 m/s
     with a seeded uniform 5 % perturbation (ccx0 = 3), free outflow, no-slip
     bed, Smagorinsky LES Cs = 0.1, vertical cylinder D = 0.1 m at x = 1.0
@@ -161,12 +189,15 @@ def open_channel(nx=512, ny=128, nz=128, precision=PREC_FP64, dt=1e-3, seed=1234
     p = default_params(nx=nx, ny=ny, nz=nz, dx=h, dy=h, dz=h, dt=dt,
                        ccx0=3, ccxf=4, ccy0=1, ccyf=1, ccz0=2, cczf=1,
                        gz=9.80665, m_turb=1, csmag=0.1, uinicial=0.5, iturb=0.05,
-                       ibm_t=2, obst_t=4, reinit_max_iter=3, cg_tol_mode=CG_TOL_REL, cg_tol=1e-8,
+                       ibm_t=2, obst_t=4, reinit_max_iter=3, cg_tol_mode=CG_TOL_REL, cg_tol=cg_tol,
                        precision=precision, seed=seed)
     ls = level_set_tipo(p, 1, ampl=0.0, lambdax=0.0, lambday=0.0, prof=0.6)
     f = _base_fields(p, ls)
+    # inflow profile of iniciais() (2_iniciais.f90:316-336) is replaced by the
+    # uniform u = uinicial start; the boundary perturbation enters through contorno
+    f.update(cylinder_obstacle(p, 1.0, 0.5, radius))
     return Case("open_channel_%dx%dx%d" % (nx, ny, nz), p, f, steps=2000,
-                obstacle={"kind": "cylinder", "xc": 1.0, "yc": 0.5, "radius": 0.05})
+                obstacle={"kind": "cylinder", "xc": 1.0, "yc": 0.5, "radius": radius})
 
 
 def ensemble_dims(ncases=256, seed=0, lo=32, hi=96):
@@ -178,7 +209,7 @@ def ensemble_dims(ncases=256, seed=0, lo=32, hi=96):
     return dims, hcol, amp
 
 
-def ensemble_case(i, dims, hcol, amp, precision=PREC_FP64, dt=1e-4) -> Case:
+def ensemble_case(i, dims, hcol, amp, precision=PREC_FP64, dt=1e-4, cg_tol=1e-10) -> Case:
     """One member of the sloshing / dam-break ensemble: dx = 1/64; a water
     column of height hcol*lz (tipo 3 form) united with a sloshing layer of
     depth 0.25 lz and cosine amplitude amp*lz (tipo 1 form); the union of the
@@ -189,7 +220,7 @@ def ensemble_case(i, dims, hcol, amp, precision=PREC_FP64, dt=1e-4) -> Case:
     p = default_params(nx=nx, ny=ny, nz=nz, dx=h, dy=h, dz=h, dt=dt,
                        ccx0=2, ccxf=2, ccy0=2, ccyf=2, ccz0=2, cczf=2,
                        gz=9.81, rho_f1=1.2, mu_f1=1.8e-5, rho_f2=1000.0, mu_f2=1e-3,
-                       reinit_max_iter=3, cg_tol_mode=CG_TOL_REL, cg_tol=1e-8, precision=precision)
+                       reinit_max_iter=3, cg_tol_mode=CG_TOL_REL, cg_tol=cg_tol, precision=precision)
     lx, lz = nx * h, nz * h
     col = level_set_tipo(p, 3, ampl=float(hcol[i]) * lz, m=30.0)
     layer = level_set_tipo(p, 1, ampl=float(amp[i]) * lz, lambdax=2.0 * lx, prof=0.25 * lz)

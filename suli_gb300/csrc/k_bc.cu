@@ -188,19 +188,86 @@ __global__ void k_bc_phase(const CaseDev<T> *__restrict__ cs, int ncases, int ph
     }
 }
 
+// Prescribed inflow with perturbation (3_contorno.f90:301-330 for I = 0 and
+// :532-563 for I = 1).  The reference sweeps k outer, j inner, carrying the
+// last water level `iik` across the sweep; one block per case walks the
+// levels in that order.  For I = 1 the inflow level set blx1 is imposed on
+// ls(1,:,:) first.  Uniform draws come from the counter-based generator
+// indexed by (call, j, k), as in the oracle.
 template <typename T>
-void launch_contorno(const Batch<T> &b, int nlock, cudaStream_t s)
+__global__ void k_inflow(const CaseDev<T> *__restrict__ cs, int ncases, int I, double thr_dz,
+                         unsigned long long call)
+{
+    const CaseDev<T> &c = cs[blockIdx.x];
+    if (c.ccx0 != 3) return;
+    const Geo &g = c.g;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const unsigned long long base = call * (unsigned long long)ny * (unsigned long long)nz;
+    const long long pl = ny + 3;
+    T *u = c.u;
+    const T *bx = (I == 0) ? c.bxx0 : c.bxx1;
+    if (I == 1) {
+        for (int t = threadIdx.x; t < ny * nz; t += blockDim.x) {
+            int j = 1 + t % ny, k = 1 + t / ny;
+            AT(c.ls, 1, j, k) = c.blx1[j + pl * k];
+        }
+        __syncthreads();
+    }
+    __shared__ int firstw, lastw;
+    if (threadIdx.x == 0) lastw = 0;
+    __syncthreads();
+    (void)nx;
+    for (int k = 1; k <= nz; ++k) {
+        if (threadIdx.x == 0) firstw = ny + 1;
+        __syncthreads();
+        for (int j = 1 + threadIdx.x; j <= ny; j += blockDim.x) {
+            T lsx = (AT(c.ls, 2, j, k) + AT(c.ls, 1, j, k)) * T(0.5);
+            if ((double)lsx >= -thr_dz * c.dz) atomicMin(&firstw, j);
+        }
+        __syncthreads();
+        for (int j = 1 + threadIdx.x; j <= ny; j += blockDim.x) {
+            T lsx = (AT(c.ls, 2, j, k) + AT(c.ls, 1, j, k)) * T(0.5);
+            if ((double)lsx >= -thr_dz * c.dz) {
+                double r = rng_uniform(c.seed, base + (unsigned long long)((k - 1) * ny + (j - 1)));
+                r = 2. * (r - 0.5);
+                T v = bx[j + pl * k];
+                AT(u, I, j, k) = v * (T(1.) + T(r) * T(c.iturb));
+            } else if (lsx < T(0)) {
+                int iik = (firstw < j) ? k : lastw;
+                AT(u, I, j, k) = AT(u, I, j, iik) * (T(1.) + T(tanh(c.pi * (double)(iik - k - 1) / 2.)));
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0 && firstw <= ny) lastw = k;
+        __syncthreads();
+    }
+}
+
+template <typename T>
+void launch_contorno(const Batch<T> &b, int nlock, cudaStream_t s, unsigned long long rng_call)
 {
     if (nlock != 1 && nlock != 2) return;   // nlock = 3 acts only with an IBM (handled by the caller)
     int nb = (b.max_plane + 255) / 256;
     if (nb < 1) nb = 1;
     if (nb > 1024) nb = 1024;
     dim3 grid(nb, b.ncases);
-    for (int ph = 0; ph < 3; ++ph) k_bc_phase<T><<<grid, 256, 0, s>>>(b.dcases, b.ncases, ph);
-    if (nlock == 2) k_bc_phase<T><<<grid, 256, 0, s>>>(b.dcases, b.ncases, 3);
+    bool inflow = false;
+    for (int c = 0; c < b.ncases; ++c) inflow |= (b.hcases[c].ccx0 == 3);
+    for (int ph = 0; ph < 3; ++ph) {
+        k_bc_phase<T><<<grid, 256, 0, s>>>(b.dcases, b.ncases, ph); count_launch();
+    }
+    if (inflow) {
+        k_inflow<T><<<b.ncases, 256, 0, s>>>(b.dcases, b.ncases, 0, 1.0, rng_call); count_launch();
+    }
+    if (nlock == 2) {
+        k_bc_phase<T><<<grid, 256, 0, s>>>(b.dcases, b.ncases, 3); count_launch();
+        if (inflow) {
+            k_inflow<T><<<b.ncases, 256, 0, s>>>(b.dcases, b.ncases, 1, 2.0, rng_call + 1); count_launch();
+        }
+    }
 }
 
-template void launch_contorno<double>(const Batch<double> &, int, cudaStream_t);
-template void launch_contorno<float>(const Batch<float> &, int, cudaStream_t);
+template void launch_contorno<double>(const Batch<double> &, int, cudaStream_t, unsigned long long);
+template void launch_contorno<float>(const Batch<float> &, int, cudaStream_t, unsigned long long);
 
 }  // namespace suli

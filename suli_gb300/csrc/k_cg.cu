@@ -271,14 +271,19 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_finish(const CaseDev<T> *__rest
     }
 }
 
-// ---- mixed form: FP64 iterative refinement around the FP32 inner CG --------
-// r64 = A e64 - b in FP64 (A's scaled coefficients are the FP32 values,
-// promoted), the FP32 inner system starts from x = 0 with r = (float) r64.
+// ---- mixed form: FP32 CG passes inside FP64 iterative refinement -------------
+// Each pass: the FP64 residual r64 = A e64 - b (k_cg_true_residual, which also
+// tests convergence on its FP64 norm), then an FP32 CG started from x = 0 on
+// A x = r (k_cg_A, k_cg_B_pass, k_cg_C) until its residual has dropped by
+// 1e3 (or reaches the outer target), then e64 -= x (k_cg_fold).  FP32 CG
+// follows FP64 CG iteration for iteration down to ~1e-5 relative residual and
+// stalls below, so each pass asks for 1e-3; the FP64 residual of the next
+// pass removes the FP32 drift.
 template <typename T>
-__global__ void __launch_bounds__(NTHREADS) k_cg_refine_begin(const CaseDev<T> *__restrict__ cs, int ncases, int first)
+__global__ void __launch_bounds__(NTHREADS) k_cg_true_residual(const CaseDev<T> *__restrict__ cs, int ncases, int first)
 {
     const CaseDev<T> &c = cs[find_case(cs, ncases)];
-    if (!first && c.sc[S_OUTER] < 0.0) return;     // this case has converged
+    if (!first && c.sc[S_OUTER] < 0.0) return;     // converged earlier
     int i, j, k;
     tile_ijk(c, i, j, k);
     const Geo &g = c.g;
@@ -288,20 +293,15 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_refine_begin(const CaseDev<T> *
     if (i <= nx && j <= ny && k <= nz) {
         long long q = g.at(i, j, k);
         const double *e = c.e64;
-        if (first) {
-            // e64 = prd1 sqrt(D) with the ghost rule of e_nb
-            // (computed on the fly below; store the interior value here)
-        }
-        auto E = [&](int a, int b, int d) -> double {
-            int ma = bmap(a, nx, px), mb = bmap(b, ny, py), md = bmap(d, nz, false);
-            if (first) return (double)AT(c.prd1, a, b, d) * sqrt((double)AT(c.dpr, ma, mb, md));
+        auto E = [&](int a, int b2, int d) -> double {
+            int ma = bmap(a, nx, px), mb = bmap(b2, ny, py), md = bmap(d, nz, false);
+            if (first && !(ma == a && mb == b2 && md == d))
+                return (double)AT(c.prd1, a, b2, d) * sqrt((double)AT(c.dpr, ma, mb, md));
             return AT(e, ma, mb, md);
         };
-        double ec = E(i, j, k);
-        double r = ec - (double)c.spi[q + 1] * E(i + 1, j, k) - (double)c.spi[q] * E(i - 1, j, k) -
+        double r = E(i, j, k) - (double)c.spi[q + 1] * E(i + 1, j, k) - (double)c.spi[q] * E(i - 1, j, k) -
                    (double)c.spj[q + g.sx] * E(i, j + 1, k) - (double)c.spj[q] * E(i, j - 1, k) -
                    (double)c.spk[q + g.sxy] * E(i, j, k + 1) - (double)c.spk[q] * E(i, j, k - 1) - (double)c.qpr[q];
-        c.r64[q] = r;
         T r32 = T(r);
         c.r[q] = r32;
         c.p[q] = r32;
@@ -323,25 +323,23 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_refine_begin(const CaseDev<T> *
             c.sc[S_OUTER] = 0.0;
             c.sc[S_CGITER] = 0.0;
         }
+        double passes = c.sc[S_OUTER] + 1.0;
         bool conv = !(rrt > c.sc[S_THR]) || c.sc[S_CGITER] >= c.sc[S_CGMAX];
+        c.sc[S_RR] = tot[1];
+        // inner target: 1e3 reduction, but no further than half the outer target
+        c.sc[S_RRREF] = fmax(1e-6 * tot[1], 0.25 * c.sc[S_THR]);
         if (conv) {
-            c.sc[S_OUTER] = -1.0 - c.sc[S_OUTER];   // negative marks done; -1-n encodes n passes
+            c.sc[S_OUTER] = -passes;           // negative: done after `passes` FP64 residuals
             c.sc[S_CGACTIVE] = 0.0;
         } else {
-            c.sc[S_RR] = tot[1];
-            // inner FP32 stop: reduce r.r by 1e-8 (residual norm by 1e-4), not below the outer target
-            double ithr = tot[1] * 1e-8;
-            c.sc[S_ALPHA] = 0.0;
-            c.sc[S_BETA] = 0.0;
-            c.sc[S_BANDSUM] = ithr;     // inner threshold slot
+            c.sc[S_OUTER] = passes;
             c.sc[S_CGACTIVE] = 1.0;
         }
     }
 }
 
-// inner FP32 iteration convergence uses S_BANDSUM as its threshold
 template <typename T>
-__global__ void __launch_bounds__(NTHREADS) k_cg_B_inner(const CaseDev<T> *__restrict__ cs, int ncases, int inner_max)
+__global__ void __launch_bounds__(NTHREADS) k_cg_B_rel(const CaseDev<T> *__restrict__ cs, int ncases)
 {
     const CaseDev<T> &c = cs[find_case(cs, ncases)];
     if (c.sc[S_CGACTIVE] == 0.0) return;
@@ -360,33 +358,29 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_B_inner(const CaseDev<T> *__res
     double vals[1] = {rr}, tot[1];
     if (last_block_reduce<T, 1>(c, vals, tot) && tid_lin() == 0) {
         double rrn = tot[0];
-        c.sc[S_BETA] = rrn / c.sc[S_RR];
-        c.sc[S_RR] = rrn;
         double it = c.sc[S_CGITER] + 1.0;
         c.sc[S_CGITER] = it;
-        double inner = c.sc[S_RRTRUE];   // unused here
-        (void)inner;
-        c.sc[S_CGACTIVE] = (rrn > c.sc[S_BANDSUM] && it < c.sc[S_CGMAX]) ? 1.0 : 0.0;
+        c.sc[S_BETA] = rrn / c.sc[S_RR];
+        c.sc[S_RR] = rrn;
+        c.sc[S_CGACTIVE] = (rrn > c.sc[S_RRREF] && it < c.sc[S_CGMAX]) ? 1.0 : 0.0;
     }
 }
 
-// e64 += x (the inner correction), counts the refinement pass
+// e64 += x (the pass's correction) for cases still refining
 template <typename T>
-__global__ void __launch_bounds__(NTHREADS) k_cg_refine_update(const CaseDev<T> *__restrict__ cs, int ncases)
+__global__ void __launch_bounds__(NTHREADS) k_cg_fold(const CaseDev<T> *__restrict__ cs, int ncases)
 {
     const CaseDev<T> &c = cs[find_case(cs, ncases)];
     if (c.sc[S_OUTER] < 0.0) return;
     int i, j, k;
     tile_ijk(c, i, j, k);
     const Geo &g = c.g;
-    const int nx = g.nx, ny = g.ny, nz = g.nz;
-    if (blockIdx.x == c.tile_begin && tid_lin() == 0) c.sc[S_OUTER] = c.sc[S_OUTER] + 1.0;
-    if (i > nx || j > ny || k > nz) return;
+    if (i > g.nx || j > g.ny || k > g.nz) return;
     long long q = g.at(i, j, k);
     c.e64[q] = c.e64[q] + (double)c.e[q];
 }
 
-// e64 = prd1 sqrt(D) on the interior (first refinement pass)
+// e64 = prd1 sqrt(D) on the interior (start of the solve)
 template <typename T>
 __global__ void __launch_bounds__(NTHREADS) k_cg_e64_init(const CaseDev<T> *__restrict__ cs, int ncases)
 {
@@ -402,47 +396,48 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_e64_init(const CaseDev<T> *__re
 // ---- launchers ----------------------------------------------------------------
 template <typename T> void launch_cg_setup(const Batch<T> &b, cudaStream_t s)
 {
-    k_cg_setup1<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases);
-    k_cg_setup2<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, 1);
-    k_cg_setup3<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases);
+    k_cg_setup1<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
+    k_cg_setup2<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, 1); count_launch();
+    k_cg_setup3<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
 }
 template <typename T> void launch_cg_iters(const Batch<T> &b, int n, cudaStream_t s)
 {
     for (int q = 0; q < n; ++q) {
-        k_cg_A<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases);
-        k_cg_B<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases);
-        k_cg_C<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases);
+        k_cg_A<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
+        k_cg_B<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
+        k_cg_C<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
     }
 }
 template <typename T> void launch_cg_finish(const Batch<T> &b, cudaStream_t s)
 {
-    k_cg_finish<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, 0);
+    k_cg_finish<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, 0); count_launch();
 }
 
 // mixed-form pieces
 template <typename T> void launch_cg_refine_setup(const Batch<T> &b, cudaStream_t s)
 {
-    k_cg_setup1<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases);
-    k_cg_setup2<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, 0);
-    k_cg_e64_init<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases);
-    k_cg_refine_begin<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, 1);
+    k_cg_setup1<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
+    k_cg_setup2<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, 0); count_launch();
+    k_cg_e64_init<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
+    k_cg_true_residual<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, 1); count_launch();
 }
 template <typename T> void launch_cg_refine_inner(const Batch<T> &b, int n, int inner_max, cudaStream_t s)
 {
+    (void)inner_max;
     for (int q = 0; q < n; ++q) {
-        k_cg_A<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases);
-        k_cg_B_inner<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, inner_max);
-        k_cg_C<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases);
+        k_cg_A<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
+        k_cg_B_rel<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
+        k_cg_C<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
     }
 }
 template <typename T> void launch_cg_refine_next(const Batch<T> &b, cudaStream_t s)
 {
-    k_cg_refine_update<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases);
-    k_cg_refine_begin<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, 0);
+    k_cg_fold<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
+    k_cg_true_residual<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, 0); count_launch();
 }
 template <typename T> void launch_cg_refine_finish(const Batch<T> &b, cudaStream_t s)
 {
-    k_cg_finish<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, 1);
+    k_cg_finish<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, 1); count_launch();
 }
 
 template void launch_cg_setup<double>(const Batch<double> &, cudaStream_t);

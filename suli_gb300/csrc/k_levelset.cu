@@ -105,16 +105,37 @@ __device__ __forceinline__ void weno_pm(const T (&L)[7], T h, T &dp, T &dn)
 // interior dims (n0,n1,n2): returns x+, x-, y+, y-, z+, z-.
 template <typename T>
 __device__ __forceinline__ void der_weno_at(const CaseDev<T> &c, const T *__restrict__ a, int i, int j, int k,
-                                            T &xp, T &xm, T &yp, T &ym, T &zp, T &zm)
+                                            int n0, int n1, int n2, T &xp, T &xm, T &yp, T &ym, T &zp, T &zm)
 {
     const Geo &g = c.g;
     T L[7];
-    load_line<T>(a, g.at(0, j, k), 1, i, g.nx, c.ccx0 == 0 ? 0 : 2, L);
+    load_line<T>(a, g.at(0, j, k), 1, i, n0, c.ccx0 == 0 ? 0 : 2, L);
     weno_pm<T>(L, T(c.dx), xp, xm);
-    load_line<T>(a, g.at(i, 0, k), g.sx, j, g.ny, c.ccy0 == 0 ? 0 : 2, L);
+    load_line<T>(a, g.at(i, 0, k), g.sx, j, n1, c.ccy0 == 0 ? 0 : 2, L);
     weno_pm<T>(L, T(c.dy), yp, ym);
-    load_line<T>(a, g.at(i, j, 0), g.sxy, k, g.nz, 2, L);
+    load_line<T>(a, g.at(i, j, 0), g.sxy, k, n2, 2, L);
     weno_pm<T>(L, T(c.dz), zp, zm);
+}
+template <typename T>
+__device__ __forceinline__ void der_weno_at(const CaseDev<T> &c, const T *__restrict__ a, int i, int j, int k,
+                                            T &xp, T &xm, T &yp, T &ym, T &zp, T &zm)
+{
+    der_weno_at<T>(c, a, i, j, k, c.g.nx, c.g.ny, c.g.nz, xp, xm, yp, ym, zp, zm);
+}
+
+// level-set array the reinitialisation acts on: 0 = ls, 1..4 = the obstacle
+// level sets obs_lsx/obs_lsy/obs_lsz/obs_lss (obstaculo(), 3_contorno.f90:991-996)
+template <typename T>
+__device__ __forceinline__ T *reinit_target(const CaseDev<T> &c, int target, int &n0, int &n1, int &n2)
+{
+    n0 = c.g.nx; n1 = c.g.ny; n2 = c.g.nz;
+    switch (target) {
+    case 1: n0 += 1; return c.obs_lsx;
+    case 2: n1 += 1; return c.obs_lsy;
+    case 3: n2 += 1; return c.obs_lsz;
+    case 4: return c.obs_lss;
+    default: return c.ls;
+    }
 }
 
 // Godunov |grad phi| of reinic_weno (:397-421)
@@ -136,11 +157,11 @@ __device__ __forceinline__ T godunov(T ls, T ta, T tb, T tc, T td, T te, T tf)
 }
 
 template <typename T>
-__device__ __forceinline__ void stage_bufs(const CaseDev<T> &c, int stage, const T *&src, T *&dst)
+__device__ __forceinline__ void stage_bufs(const CaseDev<T> &c, T *base, int stage, const T *&src, T *&dst)
 {
-    if (stage == 1) { src = c.ls; dst = c.lsb; }
+    if (stage == 1) { src = base; dst = c.lsb; }
     else if (stage == 2) { src = c.lsb; dst = c.lsc; }
-    else { src = c.lsc; dst = c.ls; }
+    else { src = c.lsc; dst = base; }
 }
 
 // conv_weno + intt_ls (14_level_set.f90:277-334), one TVD-RK3 stage
@@ -155,7 +176,7 @@ __global__ void __launch_bounds__(NTHREADS) k_ls_adv_stage(const CaseDev<T> *__r
     if (i > g.nx || j > g.ny || k > g.nz) return;
     const T *src;
     T *dst;
-    stage_bufs(c, stage, src, dst);
+    stage_bufs(c, c.ls, stage, src, dst);
     long long q = g.at(i, j, k);
     T ta, td, tb, te, tc, tf;
     der_weno_at<T>(c, src, i, j, k, ta, td, tb, te, tc, tf);
@@ -175,21 +196,24 @@ __global__ void __launch_bounds__(NTHREADS) k_ls_adv_stage(const CaseDev<T> *__r
 
 // func_s of reinic_weno (:391-426); also resets the loop state of the case
 template <typename T>
-__global__ void __launch_bounds__(NTHREADS) k_reinit_funcs(const CaseDev<T> *__restrict__ cs, int ncases)
+__global__ void __launch_bounds__(NTHREADS) k_reinit_funcs(const CaseDev<T> *__restrict__ cs, int ncases, int target)
 {
     const CaseDev<T> &c = cs[find_case(cs, ncases)];
     int i, j, k;
     tile_ijk(c, i, j, k);
     const Geo &g = c.g;
     if (blockIdx.x == c.tile_begin && tid_lin() == 0) {
-        c.sc[S_RINACTIVE] = 1.0;
+        c.sc[S_RINACTIVE] = (target == 0 || c.ibm_t == 2) ? 1.0 : 0.0;
         c.sc[S_RINITER] = 0.0;
     }
-    if (i > g.nx || j > g.ny || k > g.nz) return;
+    int n0, n1, n2;
+    const T *a = reinit_target(c, target, n0, n1, n2);
+    if (i > n0 || j > n1 || k > n2) return;
+    if (target != 0 && c.ibm_t != 2) return;
     long long q = g.at(i, j, k);
     T ta, td, tb, te, tc, tf;
-    der_weno_at<T>(c, c.ls, i, j, k, ta, td, tb, te, tc, tf);
-    T lv = c.ls[q];
+    der_weno_at<T>(c, a, i, j, k, n0, n1, n2, ta, td, tb, te, tc, tf);
+    T lv = a[q];
     T mod = godunov<T>(lv, ta, tb, tc, td, te, tf);
     T dx1 = T(c.dx1);
     c.funcs[q] = lv / sqrt(lv * lv + mod * mod * dx1 * dx1);
@@ -199,26 +223,28 @@ __global__ void __launch_bounds__(NTHREADS) k_reinit_funcs(const CaseDev<T> *__r
 // also forms the signed band error and decides whether to iterate again.
 template <typename T>
 __global__ void __launch_bounds__(NTHREADS) k_reinit_stage(const CaseDev<T> *__restrict__ cs, int ncases, int stage,
-                                                           int iter, const double *__restrict__ rk)
+                                                           int iter, const double *__restrict__ rk, int target)
 {
     const CaseDev<T> &c = cs[find_case(cs, ncases)];
     if (c.sc[S_RINACTIVE] == 0.0) return;      // loop of this case has ended
     int i, j, k;
     tile_ijk(c, i, j, k);
     const Geo &g = c.g;
-    bool in = (i <= g.nx && j <= g.ny && k <= g.nz);
+    int n0, n1, n2;
+    T *base = reinit_target(c, target, n0, n1, n2);
+    bool in = (i <= n0 && j <= n1 && k <= n2);
     const T *src;
     T *dst;
-    stage_bufs(c, stage, src, dst);
+    stage_bufs(c, base, stage, src, dst);
     double band = 0.0, cnt = 0.0;
     if (in) {
         long long q = g.at(i, j, k);
         T ta, td, tb, te, tc, tf;
-        der_weno_at<T>(c, src, i, j, k, ta, td, tb, te, tc, tf);
+        der_weno_at<T>(c, src, i, j, k, n0, n1, n2, ta, td, tb, te, tc, tf);
         T lv = src[q];
         T mod = godunov<T>(lv, ta, tb, tc, td, te, tf);
         T sy7 = c.funcs[q] * (T(1.) - mod);
-        T ta1 = c.ls[q];
+        T ta1 = base[q];
         T a = T(rk[stage - 1]), b = T(rk[3 + stage - 1]), gg = T(rk[6 + stage - 1]);
         T nv = a * ta1 + b * lv + gg * T(c.dt1) * sy7;
         dst[q] = nv;
@@ -269,6 +295,7 @@ __global__ void __launch_bounds__(NTHREADS) k_heaviside_vol(const CaseDev<T> *__
         c.ls_mu[q] = T(c.mu_f1) * (T(1.) - h) + T(c.mu_f2) * h;
         vol = (1. - (1. - (double)h)) * c.dx * c.dy * c.dz;
     }
+    if (set_ini < 0) return;     // properties only (heaviside after the level-set IBM)
     double vals[1] = {vol}, tot[1];
     if (last_block_reduce<T, 1>(c, vals, tot) && tid_lin() == 0) {
         double vi = tot[0];
@@ -319,38 +346,40 @@ template <typename T>
 void launch_level_set_adv(const Batch<T> &b, cudaStream_t s)
 {
     for (int st = 1; st <= 3; ++st)
-        k_ls_adv_stage<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, st, b.drk);
+        k_ls_adv_stage<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, st, b.drk); count_launch();
 }
 
 template <typename T>
-void launch_reinit(const Batch<T> &b, int max_iter, cudaStream_t s)
+void launch_reinit(const Batch<T> &b, int max_iter, cudaStream_t s, int target)
 {
-    k_reinit_funcs<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases);
+    k_reinit_funcs<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, target); count_launch();
     for (int it = 1; it <= max_iter; ++it)
-        for (int st = 1; st <= 3; ++st)
-            k_reinit_stage<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, st, it, b.drk);
+        for (int st = 1; st <= 3; ++st) {
+            k_reinit_stage<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, st, it, b.drk, target);
+            count_launch();
+        }
 }
 
 template <typename T>
 void launch_heaviside(const Batch<T> &b, int set_ini, cudaStream_t s)
 {
-    k_heaviside_vol<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, set_ini);
+    k_heaviside_vol<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, set_ini); count_launch();
 }
 
 template <typename T>
 void launch_volcorr(const Batch<T> &b, cudaStream_t s)
 {
-    k_volcorr<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases);
-    k_volcorr_copy<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases);
-    k_heaviside_vol<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, 0);
+    k_volcorr<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
+    k_volcorr_copy<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
+    k_heaviside_vol<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, 0); count_launch();
 }
 
 template void launch_level_set_adv<double>(const Batch<double> &, cudaStream_t);
-template void launch_reinit<double>(const Batch<double> &, int, cudaStream_t);
+template void launch_reinit<double>(const Batch<double> &, int, cudaStream_t, int);
 template void launch_heaviside<double>(const Batch<double> &, int, cudaStream_t);
 template void launch_volcorr<double>(const Batch<double> &, cudaStream_t);
 template void launch_level_set_adv<float>(const Batch<float> &, cudaStream_t);
-template void launch_reinit<float>(const Batch<float> &, int, cudaStream_t);
+template void launch_reinit<float>(const Batch<float> &, int, cudaStream_t, int);
 template void launch_heaviside<float>(const Batch<float> &, int, cudaStream_t);
 template void launch_volcorr<float>(const Batch<float> &, cudaStream_t);
 

@@ -398,36 +398,36 @@ __global__ void k_set_scalar(const CaseDev<T> *__restrict__ cs, int ncases, int 
 // ---- launchers -------------------------------------------------------------
 template <typename T> void launch_visco(const Batch<T> &b, cudaStream_t s)
 {
-    k_visco_mu<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases);
-    k_visco_faces<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases);
+    k_visco_mu<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
+    k_visco_faces<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
 }
 template <typename T> void launch_convdiff(const Batch<T> &b, int fuse, cudaStream_t s)
 {
-    k_convdiff<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, fuse);
+    k_convdiff<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, fuse); count_launch();
 }
 template <typename T> void launch_complementos(const Batch<T> &b, cudaStream_t s)
 {
-    k_complementos<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases);
+    k_complementos<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
 }
 template <typename T> void launch_tempo(const Batch<T> &b, int tt, int it, cudaStream_t s)
 {
-    k_tempo<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, tt, it);
+    k_tempo<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, tt, it); count_launch();
 }
 template <typename T> void launch_posdin(const Batch<T> &b, cudaStream_t s)
 {
-    k_posdin<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases);
+    k_posdin<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
 }
 template <typename T> void launch_conmassa(const Batch<T> &b, cudaStream_t s)
 {
-    k_conmassa<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases);
+    k_conmassa<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
 }
 template <typename T> void launch_mms_error(const Batch<T> &b, cudaStream_t s)
 {
-    k_mms_error<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases);
+    k_mms_error<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
 }
 template <typename T> void launch_set_scalar(const Batch<T> &b, int slot, double v, cudaStream_t s)
 {
-    k_set_scalar<T><<<(b.ncases + 127) / 128, 128, 0, s>>>(b.dcases, b.ncases, slot, v);
+    k_set_scalar<T><<<(b.ncases + 127) / 128, 128, 0, s>>>(b.dcases, b.ncases, slot, v); count_launch();
 }
 
 #define INST(T)                                                              \

@@ -18,6 +18,10 @@
 
 using namespace suli;
 
+namespace suli {
+std::atomic<unsigned long long> g_launches{0};
+}
+
 static thread_local std::string g_err;
 
 static int fail(int code, const std::string &msg)
@@ -111,10 +115,11 @@ static int validate(const suli_params &p)
     if (p.t_press != 1) return bad("only t_press = 1 (projection) is supported");
     if (p.m_turb != 0 && p.m_turb != 1) return bad("m_turb must be 0 or 1");
     if (p.mms_t != 0 && p.mms_t != 1) return bad("mms_t must be 0 or 1");
-    if (p.ibm_t != 0) return bad("ibm_t = 2 needs suli_ibm_setup (not in this build)");
+    if (p.ibm_t != 0 && p.ibm_t != 2) return bad("ibm_t must be 0 or 2 (image-point IBM)");
+    if (p.ibm_t == 2 && p.obst_t == 0) return bad("ibm_t = 2 needs an obstacle (obst_t != 0, obstacle fields uploaded)");
     if (p.t_tempo < 0 || p.t_tempo > 4) return bad("t_tempo must be 0..4");
     if (p.precision != SULI_PREC_FP64 && p.precision != SULI_PREC_MIXED) return bad("precision must be 0 or 1");
-    if (!(p.ccx0 == 0 || p.ccx0 == 1 || p.ccx0 == 2 || p.ccx0 == 4)) return bad("ccx0 must be 0, 1, 2 or 4");
+    if (!(p.ccx0 >= 0 && p.ccx0 <= 4)) return bad("ccx0 must be 0..4");
     if (!(p.ccxf == 0 || p.ccxf == 1 || p.ccxf == 2 || p.ccxf == 4)) return bad("ccxf must be 0, 1, 2 or 4");
     if (p.ccy0 < 0 || p.ccy0 > 2 || p.ccyf < 0 || p.ccyf > 2) return bad("ccy0/ccyf must be 0, 1 or 2");
     if (p.ccz0 < 1 || p.ccz0 > 2 || p.cczf < 1 || p.cczf > 2) return bad("ccz0/cczf must be 1 or 2");
@@ -146,6 +151,8 @@ struct ImplBase {
     virtual int read_scalars() = 0;
     virtual int write_case_scalar(int icase, int slot, double v) = 0;
     virtual int sync() = 0;
+    virtual int ibm_setup() = 0;
+    unsigned long long inflow_calls = 0;
     int ncases = 0;
     std::vector<suli_params> P;
     double *hsc = nullptr;   // pinned host mirror of the per-case scalars
@@ -157,6 +164,11 @@ struct ImplBase {
     int replay_cg[3] = {-1, -1, -1}, replay_reinit = -1;
     int reinit_iters = 0, vol_loops = 0;
     int warn = 0;
+    // measurement
+    bool prof = false;
+    unsigned long long launch0 = 0;
+    double cg_ms = 0.0, cg_cell_iters = 0.0;
+    virtual void *stream() = 0;
 };
 
 struct suli_handle {
@@ -327,6 +339,29 @@ struct Impl : ImplBase {
         CK(cudaStreamSynchronize(st));
         return SULI_OK;
     }
+    void *stream() override { return (void *)st; }
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int ev_begin()
+    {
+        if (!prof) return SULI_OK;
+        if (!ev0) {
+            CK(cudaEventCreate(&ev0));
+            CK(cudaEventCreate(&ev1));
+        }
+        CK(cudaEventRecord(ev0, st));
+        return SULI_OK;
+    }
+    int ev_end()
+    {
+        if (!prof) return SULI_OK;
+        CK(cudaEventRecord(ev1, st));
+        CK(cudaEventSynchronize(ev1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, ev0, ev1));
+        cg_ms += ms;
+        return SULI_OK;
+    }
+    double cells(int c) const { return (double)P[c].nx * P[c].ny * P[c].nz; }
 
     // ---- field copies -------------------------------------------------------
     void *dev_ptr(int icase, int f)
@@ -468,13 +503,46 @@ struct Impl : ImplBase {
         return SULI_OK;
     }
 
+    bool any_ibm() const
+    {
+        for (const auto &q : P) if (q.ibm_t == 2) return true;
+        return false;
+    }
+    bool any_inflow() const
+    {
+        for (const auto &q : P) if (q.ccx0 == 3) return true;
+        return false;
+    }
+
     int contorno(int nlock) override
     {
         if (nlock < 1 || nlock > 3) return fail(SULI_BAD_ARG, "nlock must be 1, 2 or 3");
-        if (nlock == 3) return SULI_OK;     // acts only with an immersed boundary
-        launch_contorno<T>(b, nlock, st);
+        if (nlock == 3) {
+            // level-set IBM (3_contorno.f90:651-659); nothing without an obstacle
+            if (!any_ibm()) return SULI_OK;
+            int rc = setsc(S_RINREPLAY, -1.0);
+            if (rc) return rc;
+            launch_ibm_levelset<T>(b, st);
+            launch_reinit<T>(b, P[0].reinit_max_iter, st, 0);
+            launch_heaviside<T>(b, -1, st);
+            CKL();
+            return SULI_OK;
+        }
+        if (any_ibm()) launch_ibm_velocity<T>(b, st);     // 3_contorno.f90:85-90
+        launch_contorno<T>(b, nlock, st, inflow_calls);
+        if (any_inflow()) inflow_calls += (nlock == 2) ? 2 : 1;
         CKL();
         return SULI_OK;
+    }
+
+    int ibm_setup() override
+    {
+        // obstaculo() for ibm_t = 2 (3_contorno.f90:991-1002): reinitialise the
+        // four obstacle level sets, then mark the image points
+        for (int t = 1; t <= 4; ++t) launch_reinit<T>(b, P[0].reinit_max_iter, st, t);
+        launch_ibm_posicoes<T>(b, st);
+        CKL();
+        return sync();
     }
 
     int visco() override
@@ -522,8 +590,10 @@ struct Impl : ImplBase {
             int done = 0;
             int chunk = std::max(1, std::min(prev_cg[si], cgmax));
             for (;;) {
+                if ((rc = ev_begin())) return rc;
                 launch_cg_iters<T>(b, chunk, st);
                 CKL();
+                if ((rc = ev_end())) return rc;
                 done += chunk;
                 if ((rc = read_scalars())) return rc;
                 bool any = false;
@@ -538,35 +608,43 @@ struct Impl : ImplBase {
         } else {
             launch_cg_refine_setup<T>(b, st);
             CKL();
+            int done = 0;
             int passes = 0;
-            const int inner_max = P[0].mixed_inner_iters > 0 ? P[0].mixed_inner_iters : cgmax;
             for (;;) {
-                // inner FP32 CG until every active case meets its inner tolerance
-                int done = 0;
-                int chunk = std::max(4, prev_cg[si]);
+                // FP32 pass until every refining case meets its inner target
+                int chunk = std::max(4, std::min(prev_cg[si], 256));
+                int pass_done = 0;
                 for (;;) {
-                    launch_cg_refine_inner<T>(b, chunk, inner_max, st);
+                    if ((rc = ev_begin())) return rc;
+                    launch_cg_refine_inner<T>(b, chunk, 0, st);
                     CKL();
+                    if ((rc = ev_end())) return rc;
                     done += chunk;
+                    pass_done += chunk;
                     if ((rc = read_scalars())) return rc;
                     bool any = false;
                     for (int c = 0; c < ncases; ++c) any |= (sc(c, S_CGACTIVE) != 0.0);
-                    if (!any || done >= cgmax) break;
-                    chunk = std::max(4, std::min(64, done / 8));
+                    if (!any || done >= cgmax + 256) break;
+                    chunk = std::max(4, std::min(64, pass_done / 4));
                 }
                 launch_cg_refine_next<T>(b, st);
                 CKL();
-                ++passes;
                 if ((rc = read_scalars())) return rc;
                 bool all = true;
-                for (int c = 0; c < ncases; ++c) all &= (sc(c, S_OUTER) < 0.0);
-                if (all || passes >= 50) break;
+                passes = 0;
+                for (int c = 0; c < ncases; ++c) {
+                    all &= (sc(c, S_OUTER) < 0.0);
+                    passes = std::max(passes, (int)std::fabs(sc(c, S_OUTER)));
+                }
+                if (all || done >= cgmax + 256) break;
             }
             launch_cg_refine_finish<T>(b, st);
             CKL();
             for (int c = 0; c < ncases; ++c) maxit = std::max(maxit, (int)sc(c, S_CGITER));
             cg_outer[si] = passes;
         }
+        if (prof)
+            for (int c = 0; c < ncases; ++c) cg_cell_iters += cells(c) * sc(c, S_CGITER);
         cg_iters[si] = maxit;
         cg_res[si] = sc(0, sizeof(T) == sizeof(double) ? S_RR : S_RRTRUE);
         prev_cg[si] = std::max(1, sizeof(T) == sizeof(double) ? maxit : maxit / std::max(1, cg_outer[si]));
@@ -724,6 +802,7 @@ extern "C" int suli_set_scalar(suli_handle *h, int icase, int s, double v)
     case SULI_S_DT: im->dt = v; return SULI_OK;
     case SULI_S_IT: im->it = (int)v; return SULI_OK;
     case SULI_S_TT: im->tt = (int)v; return SULI_OK;
+    case SULI_S_RNG: im->inflow_calls = (unsigned long long)v; return SULI_OK;
     case SULI_S_VOL_INI:
     case SULI_S_VOL_INS: {
         if (icase < 0 || icase >= im->ncases) return fail(SULI_BAD_ARG, "case index out of range");
@@ -744,6 +823,7 @@ extern "C" int suli_get_scalar(suli_handle *h, int icase, int s, double *v)
     case SULI_S_DT: *v = im->dt; return SULI_OK;
     case SULI_S_IT: *v = im->it; return SULI_OK;
     case SULI_S_TT: *v = im->tt; return SULI_OK;
+    case SULI_S_RNG: *v = (double)im->inflow_calls; return SULI_OK;
     default: break;
     }
     int rc = im->read_scalars();
@@ -766,6 +846,7 @@ extern "C" int suli_set_replay(suli_handle *h, const int32_t cg[3], int32_t rein
 }
 
 extern "C" int suli_heaviside_init(suli_handle *h) { HCHK(); return h->impl->heaviside_init(); }
+extern "C" int suli_ibm_setup(suli_handle *h) { HCHK(); return h->impl->ibm_setup(); }
 extern "C" int suli_level_set(suli_handle *h) { HCHK(); return h->impl->level_set(); }
 extern "C" int suli_contorno(suli_handle *h, int nlock) { HCHK(); return h->impl->contorno(nlock); }
 extern "C" int suli_visco(suli_handle *h) { HCHK(); return h->impl->visco(); }
@@ -814,6 +895,40 @@ extern "C" int suli_diagnostics(suli_handle *h, int icase, suli_diag *d)
     d->it = im->it;
     d->status_flags = im->warn;
     im->warn = 0;
+    return SULI_OK;
+}
+
+extern "C" int suli_get_stream(suli_handle *h, void **stream)
+{
+    HCHK();
+    if (!stream) return fail(SULI_BAD_ARG, "null pointer");
+    *stream = h->impl->stream();
+    return SULI_OK;
+}
+
+extern "C" int suli_profile(suli_handle *h, int enable)
+{
+    HCHK();
+    ImplBase *im = h->impl;
+    im->prof = (enable != 0);
+    im->launch0 = g_launches.load();
+    im->cg_ms = 0.0;
+    im->cg_cell_iters = 0.0;
+    return SULI_OK;
+}
+
+extern "C" int suli_profile_read(suli_handle *h, suli_profile_t *out)
+{
+    HCHK();
+    if (!out) return fail(SULI_BAD_ARG, "null pointer");
+    ImplBase *im = h->impl;
+    out->launches = g_launches.load() - im->launch0;
+    out->cg_ms = im->cg_ms;
+    out->cg_cell_iters = im->cg_cell_iters;
+    // bytes the three iteration kernels move per cell: A reads p and the three
+    // scaled coefficients and writes mp; B reads e, p, r, mp and writes e, r;
+    // C reads r, p and writes p -- 14 arrays of the storage type
+    out->cg_bytes_per_cell_iter = 14.0 * (im->P[0].precision == SULI_PREC_FP64 ? 8.0 : 4.0);
     return SULI_OK;
 }
 

@@ -47,7 +47,10 @@ enum Scal {
     S_CGMAX,
     S_ERR0, S_ERR1, S_ERR2, S_ERR3,     // MMS errors
     S_RRTRUE,      // mixed form: FP64 true residual r.r
-    S_OUTER,       // mixed form: refinement passes
+    S_OUTER,       // mixed form: FP64 residual passes (negative once converged)
+    S_UPDATE,      // mixed form: 1 while a reliable update is pending
+    S_RRREF,       // mixed form: FP32 r.r at the last update
+    S_RRPREV,      // mixed form: r.r before the pending update
     S_NSCAL
 };
 

@@ -4,7 +4,13 @@
 
 #include "suli_common.cuh"
 
+#include <atomic>
+
 namespace suli {
+
+// kernels launched by this library (all handles); read by suli_profile_read
+extern std::atomic<unsigned long long> g_launches;
+inline void count_launch(unsigned long long n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 // A batch of cases with a device copy of their CaseDev table.
 template <typename T>
@@ -20,7 +26,7 @@ struct Batch {
 
 // level set (k_levelset.cu)
 template <typename T> void launch_level_set_adv(const Batch<T> &b, cudaStream_t s);
-template <typename T> void launch_reinit(const Batch<T> &b, int max_iter, cudaStream_t s);
+template <typename T> void launch_reinit(const Batch<T> &b, int max_iter, cudaStream_t s, int target = 0);
 template <typename T> void launch_heaviside(const Batch<T> &b, int set_ini, cudaStream_t s);
 template <typename T> void launch_volcorr(const Batch<T> &b, cudaStream_t s);
 
@@ -34,7 +40,12 @@ template <typename T> void launch_conmassa(const Batch<T> &b, cudaStream_t s);
 template <typename T> void launch_mms_error(const Batch<T> &b, cudaStream_t s);
 
 // boundary conditions (k_bc.cu)
-template <typename T> void launch_contorno(const Batch<T> &b, int nlock, cudaStream_t s);
+template <typename T> void launch_contorno(const Batch<T> &b, int nlock, cudaStream_t s, unsigned long long rng_call = 0);
+
+// immersed boundary (k_ibm.cu)
+template <typename T> void launch_ibm_posicoes(const Batch<T> &b, cudaStream_t s);
+template <typename T> void launch_ibm_velocity(const Batch<T> &b, cudaStream_t s);
+template <typename T> void launch_ibm_levelset(const Batch<T> &b, cudaStream_t s);
 
 // pressure (k_cg.cu)
 template <typename T> void launch_cg_setup(const Batch<T> &b, cudaStream_t s);

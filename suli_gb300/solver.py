@@ -27,8 +27,14 @@ EXPORTS = [
     "suli_set_replay", "suli_heaviside_init", "suli_level_set", "suli_contorno", "suli_visco",
     "suli_convdiff", "suli_complementos", "suli_tempo", "suli_graddin", "suli_posdin", "suli_conmassa",
     "suli_mms_error", "suli_set_stage", "suli_step", "suli_diagnostics", "suli_synchronize",
-    "suli_last_error", "suli_device_info",
+    "suli_last_error", "suli_device_info", "suli_get_stream", "suli_profile", "suli_profile_read",
+    "suli_ibm_setup",
 ]
+
+
+class SuliProfile(C.Structure):
+    _fields_ = [("launches", C.c_uint64), ("cg_ms", C.c_double), ("cg_cell_iters", C.c_double),
+                ("cg_bytes_per_cell_iter", C.c_double)]
 
 _lib = None
 
@@ -61,7 +67,7 @@ def load_library(path: str = LIB_PATH):
     L.suli_set_scalar.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double]
     L.suli_get_scalar.argtypes = [C.c_void_p, C.c_int, C.c_int, P(C.c_double)]
     L.suli_set_replay.argtypes = [C.c_void_p, P(i32), i32]
-    for name in ("suli_heaviside_init", "suli_level_set", "suli_visco", "suli_convdiff",
+    for name in ("suli_heaviside_init", "suli_ibm_setup", "suli_level_set", "suli_visco", "suli_convdiff",
                  "suli_complementos", "suli_tempo", "suli_posdin", "suli_synchronize"):
         getattr(L, name).argtypes = [C.c_void_p]
     L.suli_contorno.argtypes = [C.c_void_p, C.c_int]
@@ -73,6 +79,9 @@ def load_library(path: str = LIB_PATH):
     L.suli_diagnostics.argtypes = [C.c_void_p, C.c_int, P(SuliDiag)]
     L.suli_last_error.argtypes = [C.c_char_p, C.c_size_t]
     L.suli_device_info.argtypes = [P(C.c_int), C.c_char_p, C.c_size_t]
+    L.suli_get_stream.argtypes = [C.c_void_p, P(C.c_void_p)]
+    L.suli_profile.argtypes = [C.c_void_p, C.c_int]
+    L.suli_profile_read.argtypes = [C.c_void_p, P(SuliProfile)]
     _lib = L
     return L
 
@@ -161,6 +170,9 @@ class SuliGPU:
     def heaviside_init(self):
         _check(load_library().suli_heaviside_init(self._h))
 
+    def ibm_setup(self):
+        _check(load_library().suli_ibm_setup(self._h))
+
     def level_set(self):
         _check(load_library().suli_level_set(self._h))
 
@@ -208,6 +220,20 @@ class SuliGPU:
     def synchronize(self):
         _check(load_library().suli_synchronize(self._h))
 
+    def stream_handle(self) -> int:
+        """The cudaStream_t all of this handle's kernels run on."""
+        p = C.c_void_p()
+        _check(load_library().suli_get_stream(self._h, C.byref(p)))
+        return p.value or 0
+
+    def profile(self, enable: bool = True):
+        _check(load_library().suli_profile(self._h, 1 if enable else 0))
+
+    def profile_read(self) -> SuliProfile:
+        out = SuliProfile()
+        _check(load_library().suli_profile_read(self._h, C.byref(out)))
+        return out
+
     def diag(self, case: int = 0) -> SuliDiag:
         d = SuliDiag()
         _check(load_library().suli_diagnostics(self._h, case, C.byref(d)))
@@ -223,5 +249,7 @@ class SuliGPU:
             for name, arr in fields.items():
                 self.upload(name, arr, case=c)
         self.heaviside_init()
+        if any(p.ibm_t == 2 for p in self.params):
+            self.ibm_setup()          # obstaculo(): reinit obstacle level sets, image masks
         for n in (1, 2, 3):
             self.contorno(n)
