@@ -86,7 +86,8 @@ typedef struct suli_params {
     int32_t precision;             /* SULI_PREC_FP64 or SULI_PREC_MIXED */
     int32_t project_under_mms;     /* 1: run graddin/posdin/contorno(1) even when mms_t>0 */
     int32_t vol_loop_max;          /* cap of the volume-correction loop (reference: none) */
-    int32_t mixed_inner_iters;     /* FP32 CG iterations per FP64 refinement pass */
+    int32_t mixed_precond;         /* mixed form: FP32 passes as 0 Jacobi-scaled CG (graddin's own
+                                      iteration), 1 CG preconditioned by a multigrid V-cycle */
     uint64_t seed;                 /* counter-based RNG seed for the inflow perturbation */
 } suli_params;
 

@@ -1207,6 +1207,15 @@ static inline int id_at(const I3 *id, int i, int j, int k)
     return A(*id, i, j, k);
 }
 
+/* A unit-normal component below 1e-9 is roundoff of a component that is zero
+ * in exact arithmetic (z for an obstacle extruded along z, whose z-derivative
+ * comes from equal values and extrapolated ghosts).  Upstream the sign of that
+ * roundoff decides, through floor() at :214-216, whether the image stencil
+ * takes the cell below or above, so its value depends on the compiler's
+ * rounding; it is taken as 0 here so the image cell is the one exact
+ * arithmetic gives. */
+static inline double snap_normal(double n) { return fabs(n) < 1e-9 ? 0. : n; }
+
 /* ibm_images, :134-318.  The sweep is in place as upstream. */
 static void ibm_images(or_case *c, F3 *obs, F3 *a1, int dimx, int dimy, int dimz, I3 *id, int der_t)
 {
@@ -1233,11 +1242,13 @@ static void ibm_images(or_case *c, F3 *obs, F3 *a1, int dimx, int dimy, int dimz
                     image = A(*a1, i, j, k);
                 } else {
                     if (k == 1 && dimz >= 2) A(nzv, i, j, k) = A(nzv, i, j, k + 1);
+                    const double nxq = snap_normal(A(nxv, i, j, k)), nyq = snap_normal(A(nyv, i, j, k)),
+                                 nzq = snap_normal(A(nzv, i, j, k));
                     double imp[2];
                     for (int l = 1; l <= ll; ++l) {
-                        double xl = XC(i) - (l * dx + ob) * A(nxv, i, j, k);
-                        double yl = YC(j) - (l * dy + ob) * A(nyv, i, j, k);
-                        double zl = ZC(k) - (l * dz + ob) * A(nzv, i, j, k);
+                        double xl = XC(i) - (l * dx + ob) * nxq;
+                        double yl = YC(j) - (l * dy + ob) * nyq;
+                        double zl = ZC(k) - (l * dz + ob) * nzq;
                         int ii = (int)floor((xl - XC(i)) / dx) + i;
                         int jj = (int)floor((yl - YC(j)) / dy) + j;
                         int kk = (int)floor((zl - ZC(k)) / dz) + k;

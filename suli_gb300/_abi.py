@@ -47,7 +47,7 @@ class SuliParams(C.Structure):
         ("precision", C.c_int32),
         ("project_under_mms", C.c_int32),
         ("vol_loop_max", C.c_int32),
-        ("mixed_inner_iters", C.c_int32),
+        ("mixed_precond", C.c_int32),
         ("seed", C.c_uint64),
     ]
 
@@ -95,7 +95,7 @@ def default_params(**kw) -> SuliParams:
     p.cg_tol = 1e-4
     p.precision = PREC_FP64
     p.vol_loop_max = 1000
-    p.mixed_inner_iters = 0
+    p.mixed_precond = 1
     for k, v in kw.items():
         if not hasattr(p, k):
             raise AttributeError(f"suli_params has no field {k!r}")

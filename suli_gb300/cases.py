@@ -179,24 +179,65 @@ def cylinder_obstacle(p: SuliParams, xc: float, yc: float, radius: float) -> dic
     }
 
 
+def inflow_profile(p: SuliParams, ls: np.ndarray, seed: int) -> np.ndarray:
+    """Initial u of iniciais() for ccx0 = 0 or 3 (2_iniciais.f90:189-210):
+    u = uinicial (1 + r iturb), r uniform in [-1, 1), on x faces where the
+    face level set is >= -2 dz, and above that the tanh decay
+    u(i,j,iik) (1 + tanh(pi (iik - k - 1) / 2)) from the last such level iik
+    (loop order k, j, i as upstream).  random_number is replaced by a seeded
+    numpy generator."""
+    nx, ny, nz = p.nx, p.ny, p.nz
+    # interpx_cf: face average, end faces from the two nearest cells (periodic: wrap)
+    lsx = np.empty((nx + 1, ny, nz))
+    lsx[1:nx] = 0.5 * (ls[1:] + ls[:-1])
+    if p.ccx0 == 0:
+        lsx[0] = lsx[nx] = 0.5 * (ls[0] + ls[nx - 1])
+    else:
+        lsx[0] = 0.5 * (ls[1] + ls[0])
+        lsx[nx] = 0.5 * (ls[nx - 1] + ls[nx - 2])
+    rng = np.random.default_rng(seed)
+    u = _zeros(p, "U")
+    iik = 0
+    for k in range(1, nz + 1):
+        r = 2.0 * (rng.random((nx + 1, ny)) - 0.5)
+        for j in range(1, ny + 1):
+            water = lsx[:, j - 1, k - 1] >= -2 * p.dz
+            # air faces before the row's first water face still see the old
+            # iik; from it on iik = k and u(i,j,k) itself (still 0) is scaled
+            seen = np.cumsum(water) > 0
+            air_old = u[1:nx + 2, j, iik] * (1.0 + math.tanh(math.pi * (iik - k - 1) / 2.0))
+            col = np.where(water, p.uinicial * (1.0 + r[:, j - 1] * p.iturb), np.where(seen, 0.0, air_old))
+            if water.any():
+                iik = k
+            u[1:nx + 2, j, k] = col
+    return u
+
+
 def open_channel(nx=512, ny=128, nz=128, precision=PREC_FP64, dt=1e-3, seed=1234, radius=0.05,
-                 cg_tol=1e-8) -> Case:
+                 cg_tol=1e-8, periodic=False) -> Case:
     """Open channel, 4 x 1 x 1 m, depth 0.6 m flat surface, inflow u = 0.5 m/s
     with a seeded uniform 5 % perturbation (ccx0 = 3), free outflow, no-slip
     bed, Smagorinsky LES Cs = 0.1, vertical cylinder D = 0.1 m at x = 1.0
-    through image-point IBM; 2000 steps."""
+    through image-point IBM; 2000 steps.  The start is the reference's
+    inflow profile (water at uinicial, air decaying to rest).
+
+    periodic=True closes the channel in x (ccx0 = ccxf = 0): the pressure
+    equation then has a solution (zero net boundary flux), where prescribed
+    inflow with free outflow leaves the all-Neumann system of graddin with
+    a net flux that its CG cannot remove."""
     h = 4.0 / nx
+    cx = (0, 0) if periodic else (3, 4)
     p = default_params(nx=nx, ny=ny, nz=nz, dx=h, dy=h, dz=h, dt=dt,
-                       ccx0=3, ccxf=4, ccy0=1, ccyf=1, ccz0=2, cczf=1,
+                       ccx0=cx[0], ccxf=cx[1], ccy0=1, ccyf=1, ccz0=2, cczf=1,
                        gz=9.80665, m_turb=1, csmag=0.1, uinicial=0.5, iturb=0.05,
                        ibm_t=2, obst_t=4, reinit_max_iter=3, cg_tol_mode=CG_TOL_REL, cg_tol=cg_tol,
                        precision=precision, seed=seed)
     ls = level_set_tipo(p, 1, ampl=0.0, lambdax=0.0, lambday=0.0, prof=0.6)
     f = _base_fields(p, ls)
-    # inflow profile of iniciais() (2_iniciais.f90:316-336) is replaced by the
-    # uniform u = uinicial start; the boundary perturbation enters through contorno
+    f["U"] = inflow_profile(p, ls, seed)
     f.update(cylinder_obstacle(p, 1.0, 0.5, radius))
-    return Case("open_channel_%dx%dx%d" % (nx, ny, nz), p, f, steps=2000,
+    name = "periodic_channel" if periodic else "open_channel"
+    return Case("%s_%dx%dx%d" % (name, nx, ny, nz), p, f, steps=2000,
                 obstacle={"kind": "cylinder", "xc": 1.0, "yc": 0.5, "radius": radius})
 
 

@@ -8,12 +8,13 @@
 //   k_cg_setup2  symmetric scaling s/sqrt(D_i D_j) (:256-287), e = prd1 sqrt(D)
 //                (:245-251), b = q/sqrt(D)
 //   k_cg_setup3  r0 = A e - b (:292-300), p = r0, r0.r0 and the stop threshold
-// Iteration (the loop of :398-587):
-//   k_cg_A       mp = A p and p.mp; the case's last block forms alpha
-//   k_cg_B       e -= alpha p, r -= alpha mp and r.r; last block forms beta,
-//                counts the iteration and clears the case's active flag on
-//                convergence (so finished cases drop out of later launches)
-//   k_cg_C       p = r + beta p
+// Iteration (the loop of :398-587), over the tiles of the cases still
+// iterating only:
+//   k_cgi_A      mp = A p and p.mp; the case's last tile forms alpha
+//   k_cgi_B      e -= alpha p, r -= alpha mp and r.r; the last tile forms beta,
+//                counts the iteration and applies the stop rule; the last
+//                case to finish lists the cases still iterating
+//   k_cgi_C      p = r + beta p
 // Finish: prd1 = e / sqrt(D) (:650-659) on the interior and on every ghost,
 // each ghost taking the value of the interior cell its Neumann copy or
 // periodic wrap points at (what the reference's ghost fills of matepr and
@@ -23,6 +24,8 @@
 // out-of-range neighbour to the interior cell the reference's ghost copy
 // would hold (Neumann: itself; periodic in x/y: the opposite end).
 #include "suli_kernels.cuh"
+
+#include <algorithm>
 
 namespace suli {
 
@@ -108,6 +111,102 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_setup2(const CaseDev<T> *__rest
     c.qpr[q] = c.qpr[q] / sD;
 }
 
+// Mixed form: the operator in FP64 from rho64 (setup1m), then its scaling
+// (setup2m) in FP64; the FP32 iteration uses the rounded scaled coefficients.
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_cg_setup1m(const CaseDev<T> *__restrict__ cs, int ncases)
+{
+    const CaseDev<T> &c = cs[find_case(cs, ncases)];
+    int i, j, k;
+    tile_ijk(c, i, j, k);
+    const Geo &g = c.g;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    if (i > nx || j > ny || k > nz) return;
+    const bool px = (c.ccx0 == 0);
+    const double dt = c.sc[S_DT];
+    const double aux1 = dt / (c.dx * c.dx), aux2 = dt / (c.dy * c.dy), aux3 = dt / (c.dz * c.dz);
+    const double *rho = c.rho64;
+    double si0 = aux1 / icf<double>(i, nx, px, [&](int m) { return AT(rho, m, j, k); });
+    double si1 = aux1 / icf<double>(i + 1, nx, px, [&](int m) { return AT(rho, m, j, k); });
+    double sj0 = aux2 / icf<double>(j, ny, false, [&](int m) { return AT(rho, i, m, k); });
+    double sj1 = aux2 / icf<double>(j + 1, ny, false, [&](int m) { return AT(rho, i, m, k); });
+    double sk0 = aux3 / icf<double>(k, nz, false, [&](int m) { return AT(rho, i, j, m); });
+    double sk1 = aux3 / icf<double>(k + 1, nz, false, [&](int m) { return AT(rho, i, j, m); });
+    long long q = g.at(i, j, k);
+    c.spi64[q] = si0;
+    c.spj64[q] = sj0;
+    c.spk64[q] = sk0;
+    if (i == nx) c.spi64[q + 1] = si1;
+    if (j == ny) c.spj64[q + g.sx] = sj1;
+    if (k == nz) c.spk64[q + g.sxy] = sk1;
+    c.dpr64[q] = si1 + si0 + sj1 + sj0 + sk1 + sk0;
+    if (c.nlev > 0) {
+        // level 0 of the multigrid preconditioner: the unscaled face
+        // conductances, zero on Neumann walls (the wall's ghost copy cancels
+        // the face), the wrap face kept on periodic x/y
+        const bool py = (c.ccy0 == 0);
+        const MgLev<T> &L = c.mg[0];
+        const T x0 = (i == 1 && !px) ? T(0) : T(si0), x1 = (i == nx && !px) ? T(0) : T(si1);
+        const T y0 = (j == 1 && !py) ? T(0) : T(sj0), y1 = (j == ny && !py) ? T(0) : T(sj1);
+        const T z0 = (k == 1) ? T(0) : T(sk0), z1 = (k == nz) ? T(0) : T(sk1);
+        L.cx[q] = x0;
+        L.cy[q] = y0;
+        L.cz[q] = z0;
+        if (i == nx) L.cx[q + 1] = x1;
+        if (j == ny) L.cy[q + g.sx] = y1;
+        if (k == nz) L.cz[q + g.sxy] = z1;
+        L.dg[q] = x0 + x1 + y0 + y1 + z0 + z1;
+    }
+    double ua = c.u[q], ub = c.u[q + 1], va = c.v[q], vb = c.v[q + g.sx], wa = c.w[q], wb = c.w[q + g.sxy];
+    if (c.obst_t != 0 && c.ibm_t == 2) {
+        if (c.obs_lsx[q] >= T(0.)) ua = 0.;
+        if (c.obs_lsx[q + 1] >= T(0.)) ub = 0.;
+        if (c.obs_lsy[q] >= T(0.)) va = 0.;
+        if (c.obs_lsy[q + g.sx] >= T(0.)) vb = 0.;
+        if (c.obs_lsz[q] >= T(0.)) wa = 0.;
+        if (c.obs_lsz[q + g.sxy] >= T(0.)) wb = 0.;
+    }
+    c.qpr64[q] = (ua - ub) / c.dx + (va - vb) / c.dy + (wa - wb) / c.dz;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_cg_setup2m(const CaseDev<T> *__restrict__ cs, int ncases)
+{
+    const CaseDev<T> &c = cs[find_case(cs, ncases)];
+    int i, j, k;
+    tile_ijk(c, i, j, k);
+    const Geo &g = c.g;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    if (i > nx || j > ny || k > nz) return;
+    const bool px = (c.ccx0 == 0), py = (c.ccy0 == 0);
+    const double *D = c.dpr64;
+    long long q = g.at(i, j, k);
+    double Dc = D[q];
+    double a = c.spi64[q] / sqrt(Dc * AT(D, bmap(i - 1, nx, px), j, k));
+    double b = c.spj64[q] / sqrt(Dc * AT(D, i, bmap(j - 1, ny, py), k));
+    double d = c.spk64[q] / sqrt(Dc * AT(D, i, j, bmap(k - 1, nz, false)));
+    c.spi64[q] = a; c.spi[q] = T(a);
+    c.spj64[q] = b; c.spj[q] = T(b);
+    c.spk64[q] = d; c.spk[q] = T(d);
+    if (i == nx) {
+        double x = c.spi64[q + 1] / sqrt(AT(D, bmap(nx + 1, nx, px), j, k) * Dc);
+        c.spi64[q + 1] = x; c.spi[q + 1] = T(x);
+    }
+    if (j == ny) {
+        double x = c.spj64[q + g.sx] / sqrt(AT(D, i, bmap(ny + 1, ny, py), k) * Dc);
+        c.spj64[q + g.sx] = x; c.spj[q + g.sx] = T(x);
+    }
+    if (k == nz) {
+        double x = c.spk64[q + g.sxy] / sqrt(AT(D, i, j, bmap(nz + 1, nz, false)) * Dc);
+        c.spk64[q + g.sxy] = x; c.spk[q + g.sxy] = T(x);
+    }
+    double sD = sqrt(Dc);
+    c.dpr[q] = T(Dc);
+    c.qpr64[q] = c.qpr64[q] / sD;
+    c.qpr[q] = T(c.qpr64[q]);
+    c.e64[q] = (double)c.prd1[q] * sD;
+}
+
 // e at a possibly-ghost neighbour: matepr(ghost) = prd1(ghost) * sqrt(matdpr(mapped))
 template <typename T>
 __device__ __forceinline__ T e_nb(const CaseDev<T> &c, int a, int b, int d, bool px, bool py)
@@ -159,82 +258,199 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_setup3(const CaseDev<T> *__rest
     if (last_block_reduce<T, 2>(c, vals, tot) && tid_lin() == 0) cg_start_final(c, tot[0], tot[1]);
 }
 
-// mp = A p, partial p.mp  (9_grad.f90:411-452)
+// ---- the iteration (the loop of 9_grad.f90:398-587) ----------------------------
+// A fixed grid (SMs x resident blocks) walks the chunks (CG_CHUNK tiles) of the
+// cases listed in an active-case table (for_active_units); cases that have
+// converged are not in the table and cost nothing.  Each thread accumulates
+// its cells of a chunk in tile order and the chunk publishes one partial, so
+// the reduction order depends on the case alone.  Tables are double-buffered:
+// k_cgi_B reads table `in` and, once every listed case has finished its
+// reduction, the block that finished last writes the cases still iterating
+// to table `out`, which the rest of the iteration and the next k_cgi_A read.
+
+// mp = A p, partial p.mp (:411-452); the case's last chunk forms
+// alpha = sc[num] / p.mp (num = S_RR for CG, S_RZ for preconditioned CG)
 template <typename T>
-__global__ void __launch_bounds__(NTHREADS) k_cg_A(const CaseDev<T> *__restrict__ cs, int ncases)
+__global__ void __launch_bounds__(NTHREADS) k_cgi_A(const CaseDev<T> *__restrict__ cs, const int *__restrict__ tab,
+                                                    int N, int num)
 {
-    const CaseDev<T> &c = cs[find_case(cs, ncases)];
-    if (c.sc[S_CGACTIVE] == 0.0) return;
-    int i, j, k;
-    tile_ijk(c, i, j, k);
-    const Geo &g = c.g;
-    const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const bool px = (c.ccx0 == 0), py = (c.ccy0 == 0);
-    double pm = 0.0;
-    if (i <= nx && j <= ny && k <= nz) {
+    for_active_units(tab, N, 0, [&](int id, int u) {
+        const CaseDev<T> &c = cs[id];
+        const Geo &g = c.g;
+        const int nx = g.nx, ny = g.ny, nz = g.nz;
+        const bool px = (c.ccx0 == 0), py = (c.ccy0 == 0);
         const T *__restrict__ p = c.p;
-        long long q = g.at(i, j, k);
-        T pc = p[q];
-        T pxp = (i < nx) ? p[q + 1] : AT(p, bmap(nx + 1, nx, px), j, k);
-        T pxm = (i > 1) ? p[q - 1] : AT(p, bmap(0, nx, px), j, k);
-        T pyp = (j < ny) ? p[q + g.sx] : AT(p, i, bmap(ny + 1, ny, py), k);
-        T pym = (j > 1) ? p[q - g.sx] : AT(p, i, bmap(0, ny, py), k);
-        T pzp = (k < nz) ? p[q + g.sxy] : pc;
-        T pzm = (k > 1) ? p[q - g.sxy] : pc;
-        T m = pc - pxp * c.spi[q + 1] - pxm * c.spi[q] - pyp * c.spj[q + g.sx] - pym * c.spj[q] -
-              pzp * c.spk[q + g.sxy] - pzm * c.spk[q];
-        c.mp[q] = m;
-        pm = (double)pc * (double)m;
-    }
-    double vals[1] = {pm}, tot[1];
-    if (last_block_reduce<T, 1>(c, vals, tot) && tid_lin() == 0) c.sc[S_ALPHA] = c.sc[S_RR] / tot[0];
+        int t0, t1;
+        unit_tiles(c, 0, u, t0, t1);
+        double pm = 0.0;
+        for (int lt = t0; lt < t1; ++lt) {
+            int i, j, k;
+            tile_ijk_of(c, lt, i, j, k);
+            if (i > nx || j > ny || k > nz) continue;
+            const long long q = g.at(i, j, k);
+            T pc = p[q];
+            T pxp = (i < nx) ? p[q + 1] : AT(p, bmap(nx + 1, nx, px), j, k);
+            T pxm = (i > 1) ? p[q - 1] : AT(p, bmap(0, nx, px), j, k);
+            T pyp = (j < ny) ? p[q + g.sx] : AT(p, i, bmap(ny + 1, ny, py), k);
+            T pym = (j > 1) ? p[q - g.sx] : AT(p, i, bmap(0, ny, py), k);
+            T pzp = (k < nz) ? p[q + g.sxy] : pc;
+            T pzm = (k > 1) ? p[q - g.sxy] : pc;
+            T m = pc - pxp * c.spi[q + 1] - pxm * c.spi[q] - pyp * c.spj[q + g.sx] - pym * c.spj[q] -
+                  pzp * c.spk[q + g.sxy] - pzm * c.spk[q];
+            c.mp[q] = m;
+            pm += (double)pc * (double)m;
+        }
+        double vals[1] = {pm}, tot[1];
+        if (chunk_reduce<T, 1>(c, u, vals, tot) && tid_lin() == 0) c.sc[S_ALPHA] = c.sc[num] / tot[0];
+    });
 }
 
-// e -= alpha p, r -= alpha mp, partial r.r  (:458-508)
-template <typename T>
-__global__ void __launch_bounds__(NTHREADS) k_cg_B(const CaseDev<T> *__restrict__ cs, int ncases)
+// e -= alpha p, r -= alpha mp, partial r.r (:458-508); the case's last chunk
+// counts the iteration and applies the stop rule:
+//   MODE 0  the case's rule (r.r > threshold, iteration cap) or a replayed
+//           count; beta = r.r / r.r_old
+//   MODE 1  one FP32 pass of the mixed form: r.r above the pass target S_RRREF
+//   MODE 2  as 1, preconditioned: also writes the V-cycle's right-hand side
+//           D^1/2 r (beta comes from r.z, k_pcg_dot)
+template <typename T, int MODE>
+__global__ void __launch_bounds__(NTHREADS) k_cgi_B(const CaseDev<T> *__restrict__ cs, const int *__restrict__ tab,
+                                                    int *__restrict__ out, unsigned *__restrict__ done, int N, int NL)
 {
-    const CaseDev<T> &c = cs[find_case(cs, ncases)];
-    if (c.sc[S_CGACTIVE] == 0.0) return;
-    int i, j, k;
-    tile_ijk(c, i, j, k);
-    const Geo &g = c.g;
-    double rr = 0.0;
-    if (i <= g.nx && j <= g.ny && k <= g.nz) {
-        long long q = g.at(i, j, k);
-        T alpha = T(c.sc[S_ALPHA]);
-        c.e[q] = c.e[q] - alpha * c.p[q];
-        T r = c.r[q] - alpha * c.mp[q];
-        c.r[q] = r;
-        rr = (double)r * (double)r;
+    __shared__ bool compact;
+    const int nin = tab[0];
+    if (nin == 0) {     // nothing iterates: the next table is empty too
+        if (blockIdx.x == 0 && tid_lin() == 0) {
+            out[0] = 0;
+            for (int s = 0; s < NL; ++s) { out[act_level(N, s)] = 0; out[act_level(N, s) + 1] = 0; }
+        }
+        return;
     }
-    double vals[1] = {rr}, tot[1];
-    if (last_block_reduce<T, 1>(c, vals, tot) && tid_lin() == 0) {
-        double rrn = tot[0];
-        c.sc[S_BETA] = rrn / c.sc[S_RR];
-        c.sc[S_RR] = rrn;
-        double it = c.sc[S_CGITER] + 1.0;
-        c.sc[S_CGITER] = it;
-        double replay = c.sc[S_CGREPLAY];
-        double active;
-        if (replay >= 0.0) active = (it < replay) ? 1.0 : 0.0;
-        else active = (fabs(rrn) > c.sc[S_THR] && it < c.sc[S_CGMAX]) ? 1.0 : 0.0;
-        c.sc[S_CGACTIVE] = active;
-    }
+    for_active_units(tab, N, 0, [&](int id, int u) {
+        const CaseDev<T> &c = cs[id];
+        const Geo &g = c.g;
+        const T alpha = T(c.sc[S_ALPHA]);
+        int t0, t1;
+        unit_tiles(c, 0, u, t0, t1);
+        double rr = 0.0;
+        for (int lt = t0; lt < t1; ++lt) {
+            int i, j, k;
+            tile_ijk_of(c, lt, i, j, k);
+            if (i > g.nx || j > g.ny || k > g.nz) continue;
+            const long long q = g.at(i, j, k);
+            c.e[q] = c.e[q] - alpha * c.p[q];
+            T r = c.r[q] - alpha * c.mp[q];
+            c.r[q] = r;
+            if (MODE == 2) c.mg[0].f[q] = sqrt(c.dpr[q]) * r;
+            rr += (double)r * (double)r;
+        }
+        double vals[1] = {rr}, tot[1];
+        if (chunk_reduce<T, 1>(c, u, vals, tot)) {
+            if (tid_lin() == 0) {
+                double rrn = tot[0];
+                double it = c.sc[S_CGITER] + 1.0;
+                c.sc[S_CGITER] = it;
+                if (MODE != 2) c.sc[S_BETA] = rrn / c.sc[S_RR];
+                c.sc[S_RR] = rrn;
+                double active;
+                if (MODE >= 1) {
+                    active = (rrn > c.sc[S_RRREF] && it < c.sc[S_CGMAX]) ? 1.0 : 0.0;
+                } else {
+                    double replay = c.sc[S_CGREPLAY];
+                    if (replay >= 0.0) active = (it < replay) ? 1.0 : 0.0;
+                    else active = (fabs(rrn) > c.sc[S_THR] && it < c.sc[S_CGMAX]) ? 1.0 : 0.0;
+                }
+                c.sc[S_CGACTIVE] = active;
+                __threadfence();
+                compact = (atomicAdd(done, 1u) == (unsigned)(nin - 1));
+            }
+            __syncthreads();
+            if (compact) {
+                __threadfence();
+                build_active_table(cs, N, NL, tab, out);
+                if (tid_lin() == 0) *done = 0u;
+            }
+        }
+    });
 }
 
-// p = r + beta p  (:520-526)
+// p = r + beta p (:520-526) over the cases still iterating
 template <typename T>
-__global__ void __launch_bounds__(NTHREADS) k_cg_C(const CaseDev<T> *__restrict__ cs, int ncases)
+__global__ void __launch_bounds__(NTHREADS) k_cgi_C(const CaseDev<T> *__restrict__ cs, const int *__restrict__ tab,
+                                                    int N)
 {
-    const CaseDev<T> &c = cs[find_case(cs, ncases)];
-    if (c.sc[S_CGACTIVE] == 0.0) return;
-    int i, j, k;
-    tile_ijk(c, i, j, k);
-    const Geo &g = c.g;
-    if (i > g.nx || j > g.ny || k > g.nz) return;
-    long long q = g.at(i, j, k);
-    c.p[q] = c.r[q] + T(c.sc[S_BETA]) * c.p[q];
+    for_active_units(tab, N, 0, [&](int id, int u) {
+        const CaseDev<T> &c = cs[id];
+        const Geo &g = c.g;
+        const T beta = T(c.sc[S_BETA]);
+        int t0, t1;
+        unit_tiles(c, 0, u, t0, t1);
+        for (int lt = t0; lt < t1; ++lt) {
+            int i, j, k;
+            tile_ijk_of(c, lt, i, j, k);
+            if (i > g.nx || j > g.ny || k > g.nz) continue;
+            const long long q = g.at(i, j, k);
+            c.p[q] = c.r[q] + beta * c.p[q];
+        }
+    });
+}
+
+// preconditioned CG: r.z with z = D^1/2 z0 (z0 = the V-cycle's result);
+// first: start of a pass (beta = 0), else beta = r.z / r.z_old
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_pcg_dot(const CaseDev<T> *__restrict__ cs, const int *__restrict__ tab,
+                                                      int N, int first)
+{
+    for_active_units(tab, N, 0, [&](int id, int u) {
+        const CaseDev<T> &c = cs[id];
+        const Geo &g = c.g;
+        int t0, t1;
+        unit_tiles(c, 0, u, t0, t1);
+        double rz = 0.0;
+        for (int lt = t0; lt < t1; ++lt) {
+            int i, j, k;
+            tile_ijk_of(c, lt, i, j, k);
+            if (i > g.nx || j > g.ny || k > g.nz) continue;
+            const long long q = g.at(i, j, k);
+            T z = sqrt(c.dpr[q]) * c.mg[0].z[q];
+            rz += (double)z * (double)c.r[q];
+        }
+        double vals[1] = {rz}, tot[1];
+        if (chunk_reduce<T, 1>(c, u, vals, tot) && tid_lin() == 0) {
+            c.sc[S_BETA] = first ? 0.0 : tot[0] / c.sc[S_RZ];
+            c.sc[S_RZ] = tot[0];
+        }
+    });
+}
+
+// preconditioned CG: p = D^1/2 z0 + beta p
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_pcg_C(const CaseDev<T> *__restrict__ cs, const int *__restrict__ tab,
+                                                    int N)
+{
+    for_active_units(tab, N, 0, [&](int id, int u) {
+        const CaseDev<T> &c = cs[id];
+        const Geo &g = c.g;
+        const T beta = T(c.sc[S_BETA]);
+        int t0, t1;
+        unit_tiles(c, 0, u, t0, t1);
+        for (int lt = t0; lt < t1; ++lt) {
+            int i, j, k;
+            tile_ijk_of(c, lt, i, j, k);
+            if (i > g.nx || j > g.ny || k > g.nz) continue;
+            const long long q = g.at(i, j, k);
+            c.p[q] = sqrt(c.dpr[q]) * c.mg[0].z[q] + beta * c.p[q];
+        }
+    });
+}
+
+// table `out` := every case of the batch whose S_CGACTIVE is set; clears the
+// completion counter (one block)
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_cgi_table(const CaseDev<T> *__restrict__ cs, int *__restrict__ out,
+                                                        unsigned *__restrict__ done, int N, int NL)
+{
+    build_active_table<T>(cs, N, NL, nullptr, out);
+    if (tid_lin() == 0) *done = 0u;
 }
 
 // prd1 = e / sqrt(D) on the interior and every ghost mapped to it
@@ -250,8 +466,16 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_finish(const CaseDev<T> *__rest
     const bool px = (c.ccx0 == 0), py = (c.ccy0 == 0);
     long long q = g.at(i, j, k);
     T val;
-    if (from64) val = T(c.e64[q] / sqrt((double)c.dpr[q]));
-    else val = c.e[q] / sqrt(c.dpr[q]);
+    if (from64) {
+        // keep the FP64 pressure too (in r64, free after the solve): posdin
+        // forms its pressure differences from it
+        const double p64 = c.e64[q] / sqrt(c.dpr64[q]);
+        c.r64[q] = p64;
+        val = T(p64);
+        if (i == 1 && j == 1 && k == 1) c.sc[S_P64OK] = 1.0;
+    } else {
+        val = c.e[q] / sqrt(c.dpr[q]);
+    }
     int xs[3] = {i, -1, -1}, ys[3] = {j, -1, -1}, zs[3] = {k, -1, -1};
     if (bmap(0, nx, px) == i) xs[1] = 0;
     if (bmap(nx + 1, nx, px) == i) xs[2] = nx + 1;
@@ -272,9 +496,9 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_finish(const CaseDev<T> *__rest
 }
 
 // ---- mixed form: FP32 CG passes inside FP64 iterative refinement -------------
-// Each pass: the FP64 residual r64 = A e64 - b (k_cg_true_residual, which also
+// Each pass: the FP64 residual A e64 - b (k_cg_true_residual, which also
 // tests convergence on its FP64 norm), then an FP32 CG started from x = 0 on
-// A x = r (k_cg_A, k_cg_B_pass, k_cg_C) until its residual has dropped by
+// A x = r (k_cgi_A, k_cgi_B<1>, k_cgi_C) until its residual has dropped by
 // 1e3 (or reaches the outer target), then e64 -= x (k_cg_fold).  FP32 CG
 // follows FP64 CG iteration for iteration down to ~1e-5 relative residual and
 // stalls below, so each pass asks for 1e-3; the FP64 residual of the next
@@ -296,19 +520,20 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_true_residual(const CaseDev<T> 
         auto E = [&](int a, int b2, int d) -> double {
             int ma = bmap(a, nx, px), mb = bmap(b2, ny, py), md = bmap(d, nz, false);
             if (first && !(ma == a && mb == b2 && md == d))
-                return (double)AT(c.prd1, a, b2, d) * sqrt((double)AT(c.dpr, ma, mb, md));
+                return (double)AT(c.prd1, a, b2, d) * sqrt(AT(c.dpr64, ma, mb, md));
             return AT(e, ma, mb, md);
         };
-        double r = E(i, j, k) - (double)c.spi[q + 1] * E(i + 1, j, k) - (double)c.spi[q] * E(i - 1, j, k) -
-                   (double)c.spj[q + g.sx] * E(i, j + 1, k) - (double)c.spj[q] * E(i, j - 1, k) -
-                   (double)c.spk[q + g.sxy] * E(i, j, k + 1) - (double)c.spk[q] * E(i, j, k - 1) - (double)c.qpr[q];
+        double r = E(i, j, k) - c.spi64[q + 1] * E(i + 1, j, k) - c.spi64[q] * E(i - 1, j, k) -
+                   c.spj64[q + g.sx] * E(i, j + 1, k) - c.spj64[q] * E(i, j - 1, k) -
+                   c.spk64[q + g.sxy] * E(i, j, k + 1) - c.spk64[q] * E(i, j, k - 1) - c.qpr64[q];
         T r32 = T(r);
         c.r[q] = r32;
         c.p[q] = r32;
         c.e[q] = T(0.);
+        if (c.nlev > 0) c.mg[0].f[q] = sqrt(c.dpr[q]) * r32;   // V-cycle right-hand side D^1/2 r
         rr = r * r;
         rr32 = (double)r32 * (double)r32;
-        bb = (double)c.qpr[q] * (double)c.qpr[q];
+        bb = c.qpr64[q] * c.qpr64[q];
     }
     double vals[3] = {rr, rr32, bb}, tot[3];
     if (last_block_reduce<T, 3>(c, vals, tot) && tid_lin() == 0) {
@@ -335,34 +560,6 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_true_residual(const CaseDev<T> 
             c.sc[S_OUTER] = passes;
             c.sc[S_CGACTIVE] = 1.0;
         }
-    }
-}
-
-template <typename T>
-__global__ void __launch_bounds__(NTHREADS) k_cg_B_rel(const CaseDev<T> *__restrict__ cs, int ncases)
-{
-    const CaseDev<T> &c = cs[find_case(cs, ncases)];
-    if (c.sc[S_CGACTIVE] == 0.0) return;
-    int i, j, k;
-    tile_ijk(c, i, j, k);
-    const Geo &g = c.g;
-    double rr = 0.0;
-    if (i <= g.nx && j <= g.ny && k <= g.nz) {
-        long long q = g.at(i, j, k);
-        T alpha = T(c.sc[S_ALPHA]);
-        c.e[q] = c.e[q] - alpha * c.p[q];
-        T r = c.r[q] - alpha * c.mp[q];
-        c.r[q] = r;
-        rr = (double)r * (double)r;
-    }
-    double vals[1] = {rr}, tot[1];
-    if (last_block_reduce<T, 1>(c, vals, tot) && tid_lin() == 0) {
-        double rrn = tot[0];
-        double it = c.sc[S_CGITER] + 1.0;
-        c.sc[S_CGITER] = it;
-        c.sc[S_BETA] = rrn / c.sc[S_RR];
-        c.sc[S_RR] = rrn;
-        c.sc[S_CGACTIVE] = (rrn > c.sc[S_RRREF] && it < c.sc[S_CGMAX]) ? 1.0 : 0.0;
     }
 }
 
@@ -400,14 +597,83 @@ template <typename T> void launch_cg_setup(const Batch<T> &b, cudaStream_t s)
     k_cg_setup2<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, 1); count_launch();
     k_cg_setup3<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
 }
-template <typename T> void launch_cg_iters(const Batch<T> &b, int n, cudaStream_t s)
+// grid of the iteration kernels: every SM full
+template <typename T> int cg_iter_grid()
 {
-    for (int q = 0; q < n; ++q) {
-        k_cg_A<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
-        k_cg_B<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
-        k_cg_C<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
+    static int grid = 0;
+    if (grid == 0) {
+        int dev = 0, sms = 0, a = 0, bb = 0, cc = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_cgi_A<T>, NTHREADS, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bb, k_cgi_B<T, 0>, NTHREADS, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cc, k_cgi_C<T>, NTHREADS, 0);
+        int per = std::max(1, std::min(a, std::min(bb, cc)));
+        grid = std::max(1, sms) * per;
     }
+    return grid;
 }
+
+template <typename T> const int *cg_table(const Batch<T> &b, int slot)
+{
+    return b.act + slot * act_stride(b.ncases, b.nlev);
+}
+
+template <typename T> void launch_cg_table(const Batch<T> &b, int slot, cudaStream_t s)
+{
+    k_cgi_table<T><<<1, b.block(), 0, s>>>(b.dcases, b.act + slot * act_stride(b.ncases, b.nlev), b.act_done,
+                                           b.ncases, b.nlev);
+    count_launch();
+}
+
+// n iterations starting from table `slot`; returns the slot of the last table
+template <typename T> int launch_cg_iters(const Batch<T> &b, int n, int slot, int mode, cudaStream_t s)
+{
+    const int G = cg_iter_grid<T>();
+    const int st = act_stride(b.ncases, b.nlev);
+    for (int q = 0; q < n; ++q) {
+        int *tin = b.act + slot * st, *tout = b.act + (1 - slot) * st;
+        k_cgi_A<T><<<G, b.block(), 0, s>>>(b.dcases, tin, b.ncases, S_RR);
+        if (mode == 1) k_cgi_B<T, 1><<<G, b.block(), 0, s>>>(b.dcases, tin, tout, b.act_done, b.ncases, b.nlev);
+        else k_cgi_B<T, 0><<<G, b.block(), 0, s>>>(b.dcases, tin, tout, b.act_done, b.ncases, b.nlev);
+        k_cgi_C<T><<<G, b.block(), 0, s>>>(b.dcases, tout, b.ncases);
+        count_launch(3);
+        slot = 1 - slot;
+    }
+    return slot;
+}
+
+// start of a preconditioned pass on table `slot` (r and the V-cycle's
+// right-hand side written by k_cg_true_residual): z = M r, r.z, p = z
+template <typename T> void launch_pcg_start(const Batch<T> &b, int slot, cudaStream_t s)
+{
+    const int G = cg_iter_grid<T>();
+    const int *tab = cg_table(b, slot);
+    launch_mg_vcycle<T>(b, tab, G, s);
+    k_pcg_dot<T><<<G, b.block(), 0, s>>>(b.dcases, tab, b.ncases, 1);
+    k_pcg_C<T><<<G, b.block(), 0, s>>>(b.dcases, tab, b.ncases);
+    count_launch(2);
+}
+
+// n preconditioned iterations from table `slot`; returns the current slot
+template <typename T> int launch_pcg_iters(const Batch<T> &b, int n, int slot, cudaStream_t s)
+{
+    const int G = cg_iter_grid<T>();
+    const int st = act_stride(b.ncases, b.nlev);
+    for (int q = 0; q < n; ++q) {
+        int *tin = b.act + slot * st, *tout = b.act + (1 - slot) * st;
+        k_cgi_A<T><<<G, b.block(), 0, s>>>(b.dcases, tin, b.ncases, S_RZ);
+        k_cgi_B<T, 2><<<G, b.block(), 0, s>>>(b.dcases, tin, tout, b.act_done, b.ncases, b.nlev);
+        count_launch(2);
+        launch_mg_vcycle<T>(b, tout, G, s);
+        k_pcg_dot<T><<<G, b.block(), 0, s>>>(b.dcases, tout, b.ncases, 0);
+        k_pcg_C<T><<<G, b.block(), 0, s>>>(b.dcases, tout, b.ncases);
+        count_launch(2);
+        slot = 1 - slot;
+    }
+    return slot;
+}
+
 template <typename T> void launch_cg_finish(const Batch<T> &b, cudaStream_t s)
 {
     k_cg_finish<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, 0); count_launch();
@@ -416,19 +682,9 @@ template <typename T> void launch_cg_finish(const Batch<T> &b, cudaStream_t s)
 // mixed-form pieces
 template <typename T> void launch_cg_refine_setup(const Batch<T> &b, cudaStream_t s)
 {
-    k_cg_setup1<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
-    k_cg_setup2<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, 0); count_launch();
-    k_cg_e64_init<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
+    k_cg_setup1m<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
+    k_cg_setup2m<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
     k_cg_true_residual<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, 1); count_launch();
-}
-template <typename T> void launch_cg_refine_inner(const Batch<T> &b, int n, int inner_max, cudaStream_t s)
-{
-    (void)inner_max;
-    for (int q = 0; q < n; ++q) {
-        k_cg_A<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
-        k_cg_B_rel<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
-        k_cg_C<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
-    }
 }
 template <typename T> void launch_cg_refine_next(const Batch<T> &b, cudaStream_t s)
 {
@@ -441,13 +697,16 @@ template <typename T> void launch_cg_refine_finish(const Batch<T> &b, cudaStream
 }
 
 template void launch_cg_setup<double>(const Batch<double> &, cudaStream_t);
-template void launch_cg_iters<double>(const Batch<double> &, int, cudaStream_t);
+template void launch_cg_table<double>(const Batch<double> &, int, cudaStream_t);
+template int launch_cg_iters<double>(const Batch<double> &, int, int, int, cudaStream_t);
 template void launch_cg_finish<double>(const Batch<double> &, cudaStream_t);
 template void launch_cg_setup<float>(const Batch<float> &, cudaStream_t);
-template void launch_cg_iters<float>(const Batch<float> &, int, cudaStream_t);
+template void launch_cg_table<float>(const Batch<float> &, int, cudaStream_t);
+template int launch_cg_iters<float>(const Batch<float> &, int, int, int, cudaStream_t);
+template void launch_pcg_start<float>(const Batch<float> &, int, cudaStream_t);
+template int launch_pcg_iters<float>(const Batch<float> &, int, int, cudaStream_t);
 template void launch_cg_finish<float>(const Batch<float> &, cudaStream_t);
 template void launch_cg_refine_setup<float>(const Batch<float> &, cudaStream_t);
-template void launch_cg_refine_inner<float>(const Batch<float> &, int, int, cudaStream_t);
 template void launch_cg_refine_next<float>(const Batch<float> &, cudaStream_t);
 template void launch_cg_refine_finish<float>(const Batch<float> &, cudaStream_t);
 

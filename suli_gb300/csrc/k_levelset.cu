@@ -16,6 +16,10 @@ namespace suli {
 template <typename T>
 __device__ __forceinline__ T weno5(T v0, T v1, T v2, T v3, T v4)
 {
+    // Jiang-Shu WENO5 (8_derivadas.f90:778-806).  The nonlinear weights
+    // om_k = (c_k/q_k) / sum_j (c_j/q_j), q_k = (eps + IS_k)^2, are formed as
+    // c_k P_k / sum_j c_j P_j with P_k the product of the other two q's:
+    // algebraically the reference's weights, one division instead of six.
     const T aux1 = T(13. / 12.), aux2 = T(1. / 4.), aux3 = T(1. / 6.), aux6 = T(0.00000001);
     T a, b;
     a = v0 - 2 * v1 + v2;
@@ -27,13 +31,13 @@ __device__ __forceinline__ T weno5(T v0, T v1, T v2, T v3, T v4)
     a = v2 - 2 * v3 + v4;
     b = 3 * v2 - 4 * v3 + v4;
     T is3 = aux1 * a * a + aux2 * b * b;
-    T al1 = T(0.1) / ((aux6 + is1) * (aux6 + is1));
-    T al2 = T(0.6) / ((aux6 + is2) * (aux6 + is2));
-    T al3 = T(0.3) / ((aux6 + is3) * (aux6 + is3));
-    T s = al1 + al2 + al3;
-    T om1 = al1 / s, om2 = al2 / s, om3 = al3 / s;
-    return aux3 * (om1 * (2 * v0 - 7 * v1 + 11 * v2) + om2 * (-v1 + 5 * v2 + 2 * v3) +
-                   om3 * (2 * v2 + 5 * v3 - v4));
+    T q1 = (aux6 + is1) * (aux6 + is1);
+    T q2 = (aux6 + is2) * (aux6 + is2);
+    T q3 = (aux6 + is3) * (aux6 + is3);
+    T w1 = T(0.1) * (q2 * q3), w2 = T(0.6) * (q1 * q3), w3 = T(0.3) * (q1 * q2);
+    T inv = T(1.) / (w1 + w2 + w3);
+    return aux3 * inv * (w1 * (2 * v0 - 7 * v1 + 11 * v2) + w2 * (-v1 + 5 * v2 + 2 * v3) +
+                         w3 * (2 * v2 + 5 * v3 - v4));
 }
 
 // Load phi(m), m = i-3..i+3, of one grid line (element m at base + m*st),
@@ -96,7 +100,8 @@ __device__ __forceinline__ void weno_pm(const T (&L)[7], T h, T &dp, T &dn)
 {
     T D[6];
 #pragma unroll
-    for (int t = 0; t < 6; ++t) D[t] = (L[t + 1] - L[t]) / h;
+    const T rh = T(1.) / h;
+    for (int t = 0; t < 6; ++t) D[t] = (L[t + 1] - L[t]) * rh;
     dp = weno5<T>(D[5], D[4], D[3], D[2], D[1]);
     dn = weno5<T>(D[0], D[1], D[2], D[3], D[4]);
 }
@@ -292,6 +297,14 @@ __global__ void __launch_bounds__(NTHREADS) k_heaviside_vol(const CaseDev<T> *__
         else h = T(0.5) * (T(1.) + l / ad + T(1. / c.pi) * sin(T(c.pi) * l / ad));
         c.hs[q] = h;
         c.rho[q] = T(c.rho_f1) * (T(1.) - h) + T(c.rho_f2) * h;
+        if (c.rho64) {
+            // FP64 density for the refinement operator of the mixed form
+            double l64 = (double)l, ad64 = c.alpha1 * c.dx1, h64;
+            if (l64 < -ad64) h64 = 0.;
+            else if (l64 > ad64) h64 = 1.;
+            else h64 = 0.5 * (1. + l64 / ad64 + 1. / c.pi * sin(c.pi * l64 / ad64));
+            c.rho64[q] = c.rho_f1 * (1. - h64) + c.rho_f2 * h64;
+        }
         c.ls_mu[q] = T(c.mu_f1) * (T(1.) - h) + T(c.mu_f2) * h;
         vol = (1. - (1. - (double)h)) * c.dx * c.dy * c.dz;
     }

@@ -1,0 +1,253 @@
+// k_mg.cu -- geometric multigrid V-cycle that preconditions the FP32 CG
+// passes of the mixed form (no counterpart in the reference, whose graddin
+// is Jacobi-scaled CG, 9_grad.f90:398-587).
+//
+// The pressure operator of graddin in unscaled form is
+//   (L p)_i = sum over the six faces f of cell i of  c_f (p_i - p_nb(f))
+// with c_f = dt / (h^2 rho_f) (9_grad.f90:95-148); Neumann walls have c = 0,
+// periodic x/y wrap.  The CG iterates on the Jacobi-scaled A = D^-1/2 L D^-1/2,
+// so the preconditioner applied to a scaled residual r is
+//   z = D^1/2 V(D^1/2 r),   V ~ L^-1 one V-cycle.
+//
+// Hierarchy: level 0 is the case grid; level l+1 halves every dimension
+// (n -> (n+1)/2), coarse cell I owning fine cells 2I-1, 2I.  The coarse
+// operator is half the Galerkin product of piecewise-constant aggregation,
+// A_c = 1/2 P^T A P: a coarse face conductance is half the sum of the (up to
+// four) fine face conductances it covers.  Restriction is P^T (sum of the
+// children's residuals), prolongation P (a child takes its parent's value).
+// Smoother: red-black Gauss-Seidel, red then black before the coarse
+// correction and black then red after it, so the V-cycle is symmetric and
+// the preconditioned CG stays a CG.  On a periodic dimension of odd length no
+// red-black colouring exists (the wrap neighbours share a colour); there the
+// smoother reads the wrap neighbour as zero (keeping the full diagonal) so no
+// two cells of one colour couple; residuals and restriction use the full
+// operator.
+//
+// Every kernel runs on a fixed grid over the work units of level l (chunks of
+// tiles on level 0, tiles above) of the cases in an active-case table, so
+// cases that have converged cost nothing.
+#include "suli_kernels.cuh"
+
+namespace suli {
+
+#define LAT(arr, i, j, k) (arr)[g.at((i), (j), (k))]
+
+// sum of c_f z_nb over the faces of cell (i,j,k); `smooth` drops the wrap
+// couplings of odd periodic dimensions (see above)
+template <typename T>
+__device__ __forceinline__ T mg_nbsum(const MgLev<T> &L, int i, int j, int k, long long q, bool px, bool py,
+                                      bool smooth)
+{
+    const Geo &g = L.g;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const T *z = L.z;
+    const bool wx = px && !(smooth && (nx & 1)) && nx > 1;
+    const bool wy = py && !(smooth && (ny & 1)) && ny > 1;
+    T s = T(0);
+    // x faces: face i (to i-1) and face i+1 (to i+1)
+    if (i > 1) s += L.cx[q] * z[q - 1];
+    else if (wx) s += L.cx[q] * LAT(z, nx, j, k);
+    if (i < nx) s += L.cx[q + 1] * z[q + 1];
+    else if (wx) s += L.cx[q + 1] * LAT(z, 1, j, k);
+    if (j > 1) s += L.cy[q] * z[q - g.sx];
+    else if (wy) s += L.cy[q] * LAT(z, i, ny, k);
+    if (j < ny) s += L.cy[q + g.sx] * z[q + g.sx];
+    else if (wy) s += L.cy[q + g.sx] * LAT(z, i, 1, k);
+    if (k > 1) s += L.cz[q] * z[q - g.sxy];
+    if (k < nz) s += L.cz[q + g.sxy] * z[q + g.sxy];
+    return s;
+}
+
+// one colour of red-black Gauss-Seidel on L z = f; zero != 0: the sweep
+// starts from z = 0 (this colour gets f / dg, the other colour 0)
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_mg_smooth(const CaseDev<T> *__restrict__ cs, const int *__restrict__ tab,
+                                                        int N, int l, int color, int zero)
+{
+    for_active_units(tab, N, l, [&](int id, int u) {
+        const CaseDev<T> &c = cs[id];
+        const MgLev<T> &L = c.mg[l];
+        const Geo &g = L.g;
+        int t0, t1;
+        unit_tiles(c, l, u, t0, t1);
+        for (int lt = t0; lt < t1; ++lt) {
+            int i, j, k;
+            tile_cell(L.ntx, L.nty, lt, i, j, k);
+            if (i > g.nx || j > g.ny || k > g.nz) continue;
+            const long long q = g.at(i, j, k);
+            const bool mine = ((i + j + k) & 1) == color;
+            const T d = L.dg[q];
+            if (zero) {
+                L.z[q] = (mine && d > T(0)) ? L.f[q] / d : T(0);
+                continue;
+            }
+            if (!mine) continue;
+            if (!(d > T(0))) { L.z[q] = T(0); continue; }
+            L.z[q] = (L.f[q] + mg_nbsum(L, i, j, k, q, c.ccx0 == 0, c.ccy0 == 0, true)) / d;
+        }
+    });
+}
+
+// f(l) = P^T (f - L z)(l-1): the coarse right-hand side, each coarse cell
+// summing the residuals of its children
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_mg_restrict(const CaseDev<T> *__restrict__ cs,
+                                                          const int *__restrict__ tab, int N, int l)
+{
+    for_active_units(tab, N, l, [&](int id, int lt) {     // l >= 1: one unit = one tile
+        const CaseDev<T> &c = cs[id];
+        const MgLev<T> &C = c.mg[l];
+        const MgLev<T> &F = c.mg[l - 1];
+        int I, J, K;
+        tile_cell(C.ntx, C.nty, lt, I, J, K);
+        if (I > C.g.nx || J > C.g.ny || K > C.g.nz) return;
+        const bool px = c.ccx0 == 0, py = c.ccy0 == 0;
+        T acc = T(0);
+        for (int dk = 0; dk < 2; ++dk) {
+            const int k = 2 * K - 1 + dk;
+            if (k > F.g.nz) continue;
+            for (int dj = 0; dj < 2; ++dj) {
+                const int j = 2 * J - 1 + dj;
+                if (j > F.g.ny) continue;
+                for (int di = 0; di < 2; ++di) {
+                    const int i = 2 * I - 1 + di;
+                    if (i > F.g.nx) continue;
+                    const long long q = F.g.at(i, j, k);
+                    acc += F.f[q] - F.dg[q] * F.z[q] + mg_nbsum(F, i, j, k, q, px, py, false);
+                }
+            }
+        }
+        C.f[C.g.at(I, J, K)] = acc;
+    });
+}
+
+// z(l) += P z(l+1)
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_mg_prolong(const CaseDev<T> *__restrict__ cs,
+                                                         const int *__restrict__ tab, int N, int l)
+{
+    for_active_units(tab, N, l, [&](int id, int u) {
+        const CaseDev<T> &c = cs[id];
+        const MgLev<T> &F = c.mg[l];
+        const MgLev<T> &C = c.mg[l + 1];
+        int t0, t1;
+        unit_tiles(c, l, u, t0, t1);
+        for (int lt = t0; lt < t1; ++lt) {
+            int i, j, k;
+            tile_cell(F.ntx, F.nty, lt, i, j, k);
+            if (i > F.g.nx || j > F.g.ny || k > F.g.nz) continue;
+            F.z[F.g.at(i, j, k)] += C.z[C.g.at((i + 1) >> 1, (j + 1) >> 1, (k + 1) >> 1)];
+        }
+    });
+}
+
+// coarse conductances of level l from level l-1 (all cases of the batch;
+// once per pressure solve, after the case grid's level 0 is written)
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_mg_coarsen(const CaseDev<T> *__restrict__ cs, int N, int l)
+{
+    // grid: one block per (case, tile of level l), cases laid out by mg tile
+    // offsets computed on the fly (all cases: the launch grid is the sum)
+    int b = blockIdx.x, id = 0;
+    while (id < N && b >= cs[id].mg[l].ntiles) { b -= cs[id].mg[l].ntiles; ++id; }
+    if (id >= N || cs[id].nlev <= l) return;
+    const CaseDev<T> &c = cs[id];
+    const MgLev<T> &C = c.mg[l];
+    const MgLev<T> &F = c.mg[l - 1];
+    int I, J, K;
+    tile_cell(C.ntx, C.nty, b, I, J, K);
+    const int mx = C.g.nx, my = C.g.ny, mz = C.g.nz;
+    if (I > mx || J > my || K > mz) return;
+    const int fx = F.g.nx, fy = F.g.ny, fz = F.g.nz;
+    // fine face index covered by coarse face A (A = 1 .. m+1)
+    auto ff = [](int A, int m, int fn) { return (A == m + 1) ? fn + 1 : 2 * A - 1; };
+    auto xface = [&](int A) {
+        const int fi = ff(A, mx, fx);
+        T s = T(0);
+        for (int dk = 0; dk < 2; ++dk)
+            for (int dj = 0; dj < 2; ++dj) {
+                const int j = 2 * J - 1 + dj, k = 2 * K - 1 + dk;
+                if (j <= fy && k <= fz) s += F.cx[F.g.at(fi, j, k)];
+            }
+        return T(0.5) * s;
+    };
+    auto yface = [&](int A) {
+        const int fj = ff(A, my, fy);
+        T s = T(0);
+        for (int dk = 0; dk < 2; ++dk)
+            for (int di = 0; di < 2; ++di) {
+                const int i = 2 * I - 1 + di, k = 2 * K - 1 + dk;
+                if (i <= fx && k <= fz) s += F.cy[F.g.at(i, fj, k)];
+            }
+        return T(0.5) * s;
+    };
+    auto zface = [&](int A) {
+        const int fk = ff(A, mz, fz);
+        T s = T(0);
+        for (int dj = 0; dj < 2; ++dj)
+            for (int di = 0; di < 2; ++di) {
+                const int i = 2 * I - 1 + di, j = 2 * J - 1 + dj;
+                if (i <= fx && j <= fy) s += F.cz[F.g.at(i, j, fk)];
+            }
+        return T(0.5) * s;
+    };
+    const Geo &g = C.g;
+    const long long q = g.at(I, J, K);
+    T x0 = xface(I), x1 = xface(I + 1), y0 = yface(J), y1 = yface(J + 1);
+    const T z0 = zface(K), z1 = zface(K + 1);
+    // a periodic dimension of one cell: the wrap face joins the cell to itself
+    if (c.ccx0 == 0 && mx == 1) x0 = x1 = T(0);
+    if (c.ccy0 == 0 && my == 1) y0 = y1 = T(0);
+    C.cx[q] = x0;
+    C.cy[q] = y0;
+    C.cz[q] = z0;
+    if (I == mx) C.cx[q + 1] = x1;
+    if (J == my) C.cy[q + g.sx] = y1;
+    if (K == mz) C.cz[q + g.sxy] = z1;
+    // a wrap face joins cells 1 and m: it enters both diagonals; a Neumann
+    // wall face is zero already
+    C.dg[q] = x0 + x1 + y0 + y1 + z0 + z1;
+}
+
+// ---- launchers ---------------------------------------------------------------
+template <typename T> void launch_mg_coarsen(const Batch<T> &b, cudaStream_t s)
+{
+    for (int l = 1; l < b.nlev; ++l) {
+        k_mg_coarsen<T><<<b.mg_tiles[l], b.block(), 0, s>>>(b.dcases, b.ncases, l);
+        count_launch();
+    }
+}
+
+// one V-cycle on the cases of table `tab`: level-0 rhs in mg[0].f, result in
+// mg[0].z
+template <typename T> void launch_mg_vcycle(const Batch<T> &b, const int *tab, int grid, cudaStream_t s)
+{
+    const int N = b.ncases, NL = b.nlev;
+    const int nu = 2, ncoarse = 6;
+    for (int l = 0; l + 1 < NL; ++l) {
+        for (int it = 0; it < nu; ++it) {
+            k_mg_smooth<T><<<grid, b.block(), 0, s>>>(b.dcases, tab, N, l, 0, it == 0);
+            k_mg_smooth<T><<<grid, b.block(), 0, s>>>(b.dcases, tab, N, l, 1, 0);
+        }
+        k_mg_restrict<T><<<grid, b.block(), 0, s>>>(b.dcases, tab, N, l + 1);
+        count_launch(2 * nu + 1);
+    }
+    for (int it = 0; it < ncoarse; ++it) {
+        k_mg_smooth<T><<<grid, b.block(), 0, s>>>(b.dcases, tab, N, NL - 1, 0, it == 0);
+        k_mg_smooth<T><<<grid, b.block(), 0, s>>>(b.dcases, tab, N, NL - 1, 1, 0);
+    }
+    count_launch(2 * ncoarse);
+    for (int l = NL - 2; l >= 0; --l) {
+        k_mg_prolong<T><<<grid, b.block(), 0, s>>>(b.dcases, tab, N, l);
+        for (int it = 0; it < nu; ++it) {
+            k_mg_smooth<T><<<grid, b.block(), 0, s>>>(b.dcases, tab, N, l, 1, 0);
+            k_mg_smooth<T><<<grid, b.block(), 0, s>>>(b.dcases, tab, N, l, 0, 0);
+        }
+        count_launch(2 * nu + 1);
+    }
+}
+
+template void launch_mg_coarsen<float>(const Batch<float> &, cudaStream_t);
+template void launch_mg_vcycle<float>(const Batch<float> &, const int *, int, cudaStream_t);
+
+}  // namespace suli

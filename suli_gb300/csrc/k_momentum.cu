@@ -43,19 +43,21 @@ __device__ __forceinline__ T upw(T vel, T dneg, T dpos)
 
 // derivaxu2n / derivaxu2p etc. (8_derivadas.f90:75-300) on a haloed array
 // whose interior extent along the axis is `dim`.
+// (divisions by the fixed spacing are multiplications by its reciprocal rh;
+// GB300's FP64 divide is a long instruction sequence)
 template <typename T, typename F>
-__device__ __forceinline__ T d2n(int m, int dim, bool perx, T h, F a)
+__device__ __forceinline__ T d2n(int m, int dim, bool perx, T rh, F a)
 {
-    if (m >= 2) return T(0.5) * (a(m - 2) - 4 * a(m - 1) + 3 * a(m)) / h;
-    if (!perx) return T(0.5) * (a(m + 1) - a(m - 1)) / h;
-    return T(0.5) * (a(dim - 1) - 4 * a(dim) + 3 * a(m)) / h;
+    if (m >= 2) return T(0.5) * (a(m - 2) - 4 * a(m - 1) + 3 * a(m)) * rh;
+    if (!perx) return T(0.5) * (a(m + 1) - a(m - 1)) * rh;
+    return T(0.5) * (a(dim - 1) - 4 * a(dim) + 3 * a(m)) * rh;
 }
 template <typename T, typename F>
-__device__ __forceinline__ T d2p(int m, int dim, bool perx, T h, F a)
+__device__ __forceinline__ T d2p(int m, int dim, bool perx, T rh, F a)
 {
-    if (m <= dim - 1) return T(0.5) * (-a(m + 2) + 4 * a(m + 1) - 3 * a(m)) / h;
-    if (!perx) return T(0.5) * (a(m + 1) - a(m - 1)) / h;
-    return T(0.5) * (-a(2) + 4 * a(1) - 3 * a(m)) / h;
+    if (m <= dim - 1) return T(0.5) * (-a(m + 2) + 4 * a(m + 1) - 3 * a(m)) * rh;
+    if (!perx) return T(0.5) * (a(m + 1) - a(m - 1)) * rh;
+    return T(0.5) * (-a(2) + 4 * a(1) - 3 * a(m)) * rh;
 }
 
 // ---------------------------------------------------------------------------
@@ -71,17 +73,17 @@ __global__ void __launch_bounds__(NTHREADS) k_visco_mu(const CaseDev<T> *__restr
     T mut = T(0.);
     if (c.m_turb == 1) {
         const T *u = c.u, *v = c.v, *w = c.w;
-        const T tdx = T(2.) * T(c.dx), tdy = T(2.) * T(c.dy), tdz = T(2.) * T(c.dz);
+        const T tdx = T(1.0 / (2. * c.dx)), tdy = T(1.0 / (2. * c.dy)), tdz = T(1.0 / (2. * c.dz));
         // derivax/y/z on the staggered arrays then interp?_fc to the centre
-        T dudx = ((AT(u, i + 1, j, k) - AT(u, i - 1, j, k)) / tdx + (AT(u, i + 2, j, k) - AT(u, i, j, k)) / tdx) * T(0.5);
-        T dudy = ((AT(u, i, j + 1, k) - AT(u, i, j - 1, k)) / tdy + (AT(u, i + 1, j + 1, k) - AT(u, i + 1, j - 1, k)) / tdy) * T(0.5);
-        T dudz = ((AT(u, i, j, k + 1) - AT(u, i, j, k - 1)) / tdz + (AT(u, i + 1, j, k + 1) - AT(u, i + 1, j, k - 1)) / tdz) * T(0.5);
-        T dvdx = ((AT(v, i + 1, j, k) - AT(v, i - 1, j, k)) / tdx + (AT(v, i + 1, j + 1, k) - AT(v, i - 1, j + 1, k)) / tdx) * T(0.5);
-        T dvdy = ((AT(v, i, j + 1, k) - AT(v, i, j - 1, k)) / tdy + (AT(v, i, j + 2, k) - AT(v, i, j, k)) / tdy) * T(0.5);
-        T dvdz = ((AT(v, i, j, k + 1) - AT(v, i, j, k - 1)) / tdz + (AT(v, i, j + 1, k + 1) - AT(v, i, j + 1, k - 1)) / tdz) * T(0.5);
-        T dwdx = ((AT(w, i + 1, j, k) - AT(w, i - 1, j, k)) / tdx + (AT(w, i + 1, j, k + 1) - AT(w, i - 1, j, k + 1)) / tdx) * T(0.5);
-        T dwdy = ((AT(w, i, j + 1, k) - AT(w, i, j - 1, k)) / tdy + (AT(w, i, j + 1, k + 1) - AT(w, i, j - 1, k + 1)) / tdy) * T(0.5);
-        T dwdz = ((AT(w, i, j, k + 1) - AT(w, i, j, k - 1)) / tdz + (AT(w, i, j, k + 2) - AT(w, i, j, k)) / tdz) * T(0.5);
+        T dudx = ((AT(u, i + 1, j, k) - AT(u, i - 1, j, k)) * tdx + (AT(u, i + 2, j, k) - AT(u, i, j, k)) * tdx) * T(0.5);
+        T dudy = ((AT(u, i, j + 1, k) - AT(u, i, j - 1, k)) * tdy + (AT(u, i + 1, j + 1, k) - AT(u, i + 1, j - 1, k)) * tdy) * T(0.5);
+        T dudz = ((AT(u, i, j, k + 1) - AT(u, i, j, k - 1)) * tdz + (AT(u, i + 1, j, k + 1) - AT(u, i + 1, j, k - 1)) * tdz) * T(0.5);
+        T dvdx = ((AT(v, i + 1, j, k) - AT(v, i - 1, j, k)) * tdx + (AT(v, i + 1, j + 1, k) - AT(v, i - 1, j + 1, k)) * tdx) * T(0.5);
+        T dvdy = ((AT(v, i, j + 1, k) - AT(v, i, j - 1, k)) * tdy + (AT(v, i, j + 2, k) - AT(v, i, j, k)) * tdy) * T(0.5);
+        T dvdz = ((AT(v, i, j, k + 1) - AT(v, i, j, k - 1)) * tdz + (AT(v, i, j + 1, k + 1) - AT(v, i, j + 1, k - 1)) * tdz) * T(0.5);
+        T dwdx = ((AT(w, i + 1, j, k) - AT(w, i - 1, j, k)) * tdx + (AT(w, i + 1, j, k + 1) - AT(w, i - 1, j, k + 1)) * tdx) * T(0.5);
+        T dwdy = ((AT(w, i, j + 1, k) - AT(w, i, j - 1, k)) * tdy + (AT(w, i, j + 1, k + 1) - AT(w, i, j - 1, k + 1)) * tdy) * T(0.5);
+        T dwdz = ((AT(w, i, j, k + 1) - AT(w, i, j, k - 1)) * tdz + (AT(w, i, j, k + 2) - AT(w, i, j, k)) * tdz) * T(0.5);
         T p1 = dudx + T(0.5) * (dudy + dvdx + dudz + dwdx);
         T p2 = dvdy + T(0.5) * (dvdx + dudy + dvdz + dwdy);
         T p3 = dwdz + T(0.5) * (dwdy + dvdz + dudz + dwdx);
@@ -126,7 +128,7 @@ __global__ void __launch_bounds__(NTHREADS) k_convdiff(const CaseDev<T> *__restr
     const T *__restrict__ xmu = c.xmu;
     const T *__restrict__ ymu = c.ymu;
     const T *__restrict__ zmu = c.zmu;
-    const T dx = T(c.dx), dy = T(c.dy), dz = T(c.dz);
+    const T dx = T(1.0 / c.dx), dy = T(1.0 / c.dy), dz = T(1.0 / c.dz);   // reciprocal spacings
     const bool px = (c.ccx0 == 0);
 
     // ---- Fu at x-face (i,j,k), i in 1..nx+1 ----
@@ -141,21 +143,22 @@ __global__ void __launch_bounds__(NTHREADS) k_convdiff(const CaseDev<T> *__restr
         T ddz = upw<T>(dma, d2n<T>(k, nz, false, dz, [&](int m) { return U(i, j, m); }),
                        d2p<T>(k, nz, false, dz, [&](int m) { return U(i, j, m); }));
         T uint_ = ddx + ddy + ddz;
-        T ama_i = AT(mu, clampi(i, 1, nx), j, k) / dx;
-        T ama_m = AT(mu, clampi(i - 1, 1, nx), j, k) / dx;
-        T b1 = interp_cf<T>(j + 1, ny, false, [&](int m) { return AT(xmu, i, m, k); }) / dy;
-        T b0 = interp_cf<T>(j, ny, false, [&](int m) { return AT(xmu, i, m, k); }) / dy;
-        T d1 = interp_cf<T>(k + 1, nz, false, [&](int m) { return AT(xmu, i, j, m); }) / dz;
-        T d0 = interp_cf<T>(k, nz, false, [&](int m) { return AT(xmu, i, j, m); }) / dz;
+        T ama_i = AT(mu, clampi(i, 1, nx), j, k) * dx;
+        T ama_m = AT(mu, clampi(i - 1, 1, nx), j, k) * dx;
+        T b1 = interp_cf<T>(j + 1, ny, false, [&](int m) { return AT(xmu, i, m, k); }) * dy;
+        T b0 = interp_cf<T>(j, ny, false, [&](int m) { return AT(xmu, i, m, k); }) * dy;
+        T d1 = interp_cf<T>(k + 1, nz, false, [&](int m) { return AT(xmu, i, j, m); }) * dz;
+        T d0 = interp_cf<T>(k, nz, false, [&](int m) { return AT(xmu, i, j, m); }) * dz;
         T rhox = interp_cf<T>(i, nx, px, [&](int m) { return AT(rho, m, j, k); });
         T uc = U(i, j, k);
+        const T rrho = T(1.) / rhox;
         T F = -uint_ +
-              ((ama_i * T(2.) * (U(i + 1, j, k) - uc) - ama_m * T(2.) * (uc - U(i - 1, j, k))) / dx +
-               b1 * ((U(i, j + 1, k) - uc) / dy + (AT(v, i, j + 1, k) - AT(v, i - 1, j + 1, k)) / dx) -
-               b0 * ((uc - U(i, j - 1, k)) / dy + (AT(v, i, j, k) - AT(v, i - 1, j, k)) / dx) +
-               d1 * ((U(i, j, k + 1) - uc) / dz + (AT(w, i, j, k + 1) - AT(w, i - 1, j, k + 1)) / dx) -
-               d0 * ((uc - U(i, j, k - 1)) / dz + (AT(w, i, j, k) - AT(w, i - 1, j, k)) / dx)) /
-                  rhox;
+              ((ama_i * T(2.) * (U(i + 1, j, k) - uc) - ama_m * T(2.) * (uc - U(i - 1, j, k))) * dx +
+               b1 * ((U(i, j + 1, k) - uc) * dy + (AT(v, i, j + 1, k) - AT(v, i - 1, j + 1, k)) * dx) -
+               b0 * ((uc - U(i, j - 1, k)) * dy + (AT(v, i, j, k) - AT(v, i - 1, j, k)) * dx) +
+               d1 * ((U(i, j, k + 1) - uc) * dz + (AT(w, i, j, k + 1) - AT(w, i - 1, j, k + 1)) * dx) -
+               d0 * ((uc - U(i, j, k - 1)) * dz + (AT(w, i, j, k) - AT(w, i - 1, j, k)) * dx)) *
+                  rrho;
         if (fuse) F = F + T(c.gx) + AT(c.tf_u, i, j, k);
         AT(c.Fu, i, j, k) = F;
     }
@@ -171,20 +174,20 @@ __global__ void __launch_bounds__(NTHREADS) k_convdiff(const CaseDev<T> *__restr
         T ddz = upw<T>(dmb, d2n<T>(k, nz, false, dz, [&](int m) { return V(i, j, m); }),
                        d2p<T>(k, nz, false, dz, [&](int m) { return V(i, j, m); }));
         T vint = ddx + ddy + ddz;
-        T a1 = interp_cf<T>(i + 1, nx, px, [&](int m) { return AT(ymu, m, j, k); }) / dx;
-        T a0 = interp_cf<T>(i, nx, px, [&](int m) { return AT(ymu, m, j, k); }) / dx;
-        T bmb_j = AT(mu, i, clampi(j, 1, ny), k) / dy;
-        T bmb_m = AT(mu, i, clampi(j - 1, 1, ny), k) / dy;
-        T d1 = interp_cf<T>(k + 1, nz, false, [&](int m) { return AT(ymu, i, j, m); }) / dz;
-        T d0 = interp_cf<T>(k, nz, false, [&](int m) { return AT(ymu, i, j, m); }) / dz;
+        T a1 = interp_cf<T>(i + 1, nx, px, [&](int m) { return AT(ymu, m, j, k); }) * dx;
+        T a0 = interp_cf<T>(i, nx, px, [&](int m) { return AT(ymu, m, j, k); }) * dx;
+        T bmb_j = AT(mu, i, clampi(j, 1, ny), k) * dy;
+        T bmb_m = AT(mu, i, clampi(j - 1, 1, ny), k) * dy;
+        T d1 = interp_cf<T>(k + 1, nz, false, [&](int m) { return AT(ymu, i, j, m); }) * dz;
+        T d0 = interp_cf<T>(k, nz, false, [&](int m) { return AT(ymu, i, j, m); }) * dz;
         T rhoy = interp_cf<T>(j, ny, false, [&](int m) { return AT(rho, i, m, k); });
         T vc = V(i, j, k);
         T F = -vint +
-              (a1 * ((V(i + 1, j, k) - vc) / dx + (AT(u, i + 1, j, k) - AT(u, i + 1, j - 1, k)) / dy) -
-               a0 * ((vc - V(i - 1, j, k)) / dx + (AT(u, i, j, k) - AT(u, i, j - 1, k)) / dy) +
-               (bmb_j * T(2.) * (V(i, j + 1, k) - vc) - bmb_m * T(2.) * (vc - V(i, j - 1, k))) / dy +
-               d1 * ((V(i, j, k + 1) - vc) / dz + (AT(w, i, j, k + 1) - AT(w, i, j - 1, k + 1)) / dy) -
-               d0 * ((vc - V(i, j, k - 1)) / dz + (AT(w, i, j, k) - AT(w, i, j - 1, k)) / dy)) /
+              (a1 * ((V(i + 1, j, k) - vc) * dx + (AT(u, i + 1, j, k) - AT(u, i + 1, j - 1, k)) * dy) -
+               a0 * ((vc - V(i - 1, j, k)) * dx + (AT(u, i, j, k) - AT(u, i, j - 1, k)) * dy) +
+               (bmb_j * T(2.) * (V(i, j + 1, k) - vc) - bmb_m * T(2.) * (vc - V(i, j - 1, k))) * dy +
+               d1 * ((V(i, j, k + 1) - vc) * dz + (AT(w, i, j, k + 1) - AT(w, i, j - 1, k + 1)) * dy) -
+               d0 * ((vc - V(i, j, k - 1)) * dz + (AT(w, i, j, k) - AT(w, i, j - 1, k)) * dy)) /
                   rhoy;
         if (fuse) F = F + AT(c.tf_v, i, j, k);
         AT(c.Fv, i, j, k) = F;
@@ -201,20 +204,20 @@ __global__ void __launch_bounds__(NTHREADS) k_convdiff(const CaseDev<T> *__restr
         T ddz = upw<T>(W(i, j, k), d2n<T>(k, nz + 1, false, dz, [&](int m) { return W(i, j, m); }),
                        d2p<T>(k, nz + 1, false, dz, [&](int m) { return W(i, j, m); }));
         T wint = ddx + ddy + ddz;
-        T a1 = interp_cf<T>(i + 1, nx, px, [&](int m) { return AT(zmu, m, j, k); }) / dx;
-        T a0 = interp_cf<T>(i, nx, px, [&](int m) { return AT(zmu, m, j, k); }) / dx;
-        T b1 = interp_cf<T>(j + 1, ny, false, [&](int m) { return AT(zmu, i, m, k); }) / dy;
-        T b0 = interp_cf<T>(j, ny, false, [&](int m) { return AT(zmu, i, m, k); }) / dy;
-        T dmd_k = AT(mu, i, j, clampi(k, 1, nz)) / dz;
-        T dmd_m = AT(mu, i, j, clampi(k - 1, 1, nz)) / dz;
+        T a1 = interp_cf<T>(i + 1, nx, px, [&](int m) { return AT(zmu, m, j, k); }) * dx;
+        T a0 = interp_cf<T>(i, nx, px, [&](int m) { return AT(zmu, m, j, k); }) * dx;
+        T b1 = interp_cf<T>(j + 1, ny, false, [&](int m) { return AT(zmu, i, m, k); }) * dy;
+        T b0 = interp_cf<T>(j, ny, false, [&](int m) { return AT(zmu, i, m, k); }) * dy;
+        T dmd_k = AT(mu, i, j, clampi(k, 1, nz)) * dz;
+        T dmd_m = AT(mu, i, j, clampi(k - 1, 1, nz)) * dz;
         T rhoz = interp_cf<T>(k, nz, false, [&](int m) { return AT(rho, i, j, m); });
         T wc = W(i, j, k);
         T F = -wint +
-              (a1 * ((W(i + 1, j, k) - wc) / dx + (AT(u, i + 1, j, k) - AT(u, i + 1, j, k - 1)) / dz) -
-               a0 * ((wc - W(i - 1, j, k)) / dx + (AT(u, i, j, k) - AT(u, i, j, k - 1)) / dz) +
-               b1 * ((W(i, j + 1, k) - wc) / dy + (AT(v, i, j + 1, k) - AT(v, i, j + 1, k - 1)) / dz) -
-               b0 * ((wc - W(i, j - 1, k)) / dy + (AT(v, i, j, k) - AT(v, i, j, k - 1)) / dz) +
-               (dmd_k * T(2.) * (W(i, j, k + 1) - wc) - dmd_m * T(2.) * (wc - W(i, j, k - 1))) / dz) /
+              (a1 * ((W(i + 1, j, k) - wc) * dx + (AT(u, i + 1, j, k) - AT(u, i + 1, j, k - 1)) * dz) -
+               a0 * ((wc - W(i - 1, j, k)) * dx + (AT(u, i, j, k) - AT(u, i, j, k - 1)) * dz) +
+               b1 * ((W(i, j + 1, k) - wc) * dy + (AT(v, i, j + 1, k) - AT(v, i, j + 1, k - 1)) * dz) -
+               b0 * ((wc - W(i, j - 1, k)) * dy + (AT(v, i, j, k) - AT(v, i, j, k - 1)) * dz) +
+               (dmd_k * T(2.) * (W(i, j, k + 1) - wc) - dmd_m * T(2.) * (wc - W(i, j, k - 1))) * dz) /
                   rhoz;
         if (fuse) F = F - T(c.gz) + AT(c.tf_w, i, j, k);
         AT(c.Fw, i, j, k) = F;
@@ -300,17 +303,30 @@ __global__ void __launch_bounds__(NTHREADS) k_posdin(const CaseDev<T> *__restric
     T dt = T(c.sc[S_DT]);
     T aux1 = dt / T(c.dx), aux2 = dt / T(c.dy);
     bool px = (c.ccx0 == 0);
+    const bool py = (c.ccy0 == 0);
+    // pressure difference across a face: in the mixed form from the FP64
+    // pressure of the last solve when it is current (the FP32 pressure loses
+    // a digit to cancellation where the hydrostatic part dominates); ghost
+    // indices map to the interior cell their Neumann copy / periodic wrap holds
+    const bool p64 = (sizeof(T) == 4) && c.r64 != nullptr && c.sc[S_P64OK] != 0.0;
+    auto dp = [&](int i1, int j1, int k1, int i0, int j0, int k0) -> T {
+        if (!p64) return AT(p, i1, j1, k1) - AT(p, i0, j0, k0);
+        auto mi = [&](int a) { return a < 1 ? (px ? nx : 1) : (a > nx ? (px ? 1 : nx) : a); };
+        auto mj = [&](int a) { return a < 1 ? (py ? ny : 1) : (a > ny ? (py ? 1 : ny) : a); };
+        auto mk = [&](int a) { return a < 1 ? 1 : (a > nz ? nz : a); };
+        return T(c.r64[g.at(mi(i1), mj(j1), mk(k1))] - c.r64[g.at(mi(i0), mj(j0), mk(k0))]);
+    };
     if (i <= nx + 1 && j <= ny && k <= nz) {
         T rx = interp_cf<T>(i, nx, px, [&](int m) { return AT(rho, m, j, k); });
-        AT(c.u, i, j, k) = AT(c.u, i, j, k) - aux1 * (AT(p, i, j, k) - AT(p, i - 1, j, k)) / rx;
+        AT(c.u, i, j, k) = AT(c.u, i, j, k) - aux1 * dp(i, j, k, i - 1, j, k) / rx;
     }
     if (i <= nx && j <= ny + 1 && k <= nz) {
         T ry = interp_cf<T>(j, ny, false, [&](int m) { return AT(rho, i, m, k); });
-        AT(c.v, i, j, k) = AT(c.v, i, j, k) - aux2 * (AT(p, i, j, k) - AT(p, i, j - 1, k)) / ry;
+        AT(c.v, i, j, k) = AT(c.v, i, j, k) - aux2 * dp(i, j, k, i, j - 1, k) / ry;
     }
     if (i <= nx && j <= ny && k <= nz + 1) {
         T rz = interp_cf<T>(k, nz, false, [&](int m) { return AT(rho, i, j, m); });
-        AT(c.w, i, j, k) = AT(c.w, i, j, k) - dt / T(c.dz) * (AT(p, i, j, k) - AT(p, i, j, k - 1)) / rz;
+        AT(c.w, i, j, k) = AT(c.w, i, j, k) - dt / T(c.dz) * dp(i, j, k, i, j, k - 1) / rz;
     }
 }
 

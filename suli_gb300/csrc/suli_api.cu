@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -181,7 +182,8 @@ struct Impl : ImplBase {
     std::vector<CaseDev<T>> hc;
     std::vector<void *> slabs;
     double *dsc = nullptr, *dpart = nullptr, *drk = nullptr;
-    unsigned *dcnt = nullptr;
+    unsigned *dcnt = nullptr, *dactdone = nullptr;
+    int *dact = nullptr;
     cudaStream_t st = nullptr;
 
     ~Impl() override
@@ -191,6 +193,8 @@ struct Impl : ImplBase {
         cudaFree(dsc);
         cudaFree(dpart);
         cudaFree(dcnt);
+        cudaFree(dact);
+        cudaFree(dactdone);
         cudaFree(drk);
         cudaFree(b.dcases);
         if (hsc) cudaFreeHost(hsc);
@@ -203,7 +207,7 @@ struct Impl : ImplBase {
         P.assign(p, p + n);
         CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
         hc.resize(n);
-        int tiles = 0, maxplane = 1;
+        int tiles = 0, chunks = 0, maxplane = 1;
         for (int c = 0; c < n; ++c) {
             const suli_params &q = P[c];
             CaseDev<T> &cd = hc[c];
@@ -219,6 +223,9 @@ struct Impl : ImplBase {
             cd.ntiles = cd.ntx * cd.nty * cd.ntz;
             cd.tile_begin = tiles;
             tiles += cd.ntiles;
+            cd.nchunks = (cd.ntiles + CG_CHUNK - 1) / CG_CHUNK;
+            cd.chunk_begin = chunks;
+            chunks += cd.nchunks;
             long long mp = std::max({(long long)(q.nx + 3) * (q.nz + 3), (long long)(q.nx + 3) * (q.ny + 3),
                                      (long long)(q.ny + 3) * (q.nz + 3),
                                      (long long)(q.nx + 2) * (q.nz + 2) + (long long)(q.nx + 2) * (q.ny + 2) +
@@ -252,7 +259,8 @@ struct Impl : ImplBase {
             int **itf[] = {&cd.id_ibmx, &cd.id_ibmy, &cd.id_ibmz, &cd.id_ibm};
             T **ptf[] = {&cd.bxx0, &cd.bxx1, &cd.blx1};
             const bool mixed = (sizeof(T) == 4);
-            size_t bytes = fb * ntf + ib * 4 + pb * 3 + (mixed ? 2 * db : 0);
+            const bool mg = mixed && q.mixed_precond == 1;
+            size_t bytes = fb * ntf + ib * 4 + pb * 3 + (mixed ? 8 * db : 0) + (mg ? 6 * fb : 0);
             void *slab = nullptr;
             CK(cudaMalloc(&slab, bytes));
             slabs.push_back(slab);
@@ -261,8 +269,60 @@ struct Impl : ImplBase {
             for (int f = 0; f < ntf; ++f) { *tf[f] = (T *)cur; cur += fb; }
             for (int f = 0; f < 4; ++f) { *itf[f] = (int *)cur; cur += ib; }
             for (int f = 0; f < 3; ++f) { *ptf[f] = (T *)cur; cur += pb; }
-            if (mixed) { cd.e64 = (double *)cur; cur += db; cd.r64 = (double *)cur; cur += db; }
+            if (mixed) {
+                double **d64[] = {&cd.e64, &cd.r64, &cd.rho64, &cd.spi64, &cd.spj64, &cd.spk64, &cd.dpr64, &cd.qpr64};
+                for (int f = 0; f < 8; ++f) { *d64[f] = (double *)cur; cur += db; }
+            }
+            if (mg) {
+                // multigrid level 0: the case grid, its box and its tiles
+                MgLev<T> &L = cd.mg[0];
+                L.g = g;
+                L.ntx = cd.ntx; L.nty = cd.nty; L.ntz = cd.ntz; L.ntiles = cd.ntiles;
+                T **lf[] = {&L.cx, &L.cy, &L.cz, &L.dg, &L.z, &L.f};
+                for (int f = 0; f < 6; ++f) { *lf[f] = (T *)cur; cur += fb; }
+            }
         }
+        // multigrid levels: halve every dimension until the largest is at most
+        // 4 in every case; all cases get the batch's level count
+        int nlev = 1;
+        if (sizeof(T) == 4 && P[0].mixed_precond == 1) {
+            for (int c = 0; c < n; ++c) {
+                int m = std::max({P[c].nx, P[c].ny, P[c].nz}), l = 1;
+                while (m > 4 && l < MG_MAXL) { m = (m + 1) / 2; ++l; }
+                nlev = std::max(nlev, l);
+            }
+            nlev = std::max(nlev, 2);
+            for (int c = 0; c < n; ++c) {
+                CaseDev<T> &cd = hc[c];
+                cd.nlev = nlev;
+                size_t bytes = 0;
+                int dx = cd.g.nx, dy = cd.g.ny, dz = cd.g.nz;
+                for (int l = 1; l < nlev; ++l) {
+                    dx = (dx + 1) / 2; dy = (dy + 1) / 2; dz = (dz + 1) / 2;
+                    MgLev<T> &L = cd.mg[l];
+                    L.g.nx = dx; L.g.ny = dy; L.g.nz = dz;
+                    L.g.sx = dx + 2;
+                    L.g.sxy = L.g.sx * (dy + 2);
+                    L.g.total = L.g.sxy * (dz + 2);
+                    L.ntx = (dx + TX - 1) / TX; L.nty = (dy + TY - 1) / TY; L.ntz = (dz + TZ - 1) / TZ;
+                    L.ntiles = L.ntx * L.nty * L.ntz;
+                    bytes += 6 * (((size_t)L.g.total * sizeof(T) + 255) / 256 * 256);
+                    b.mg_tiles[l] += L.ntiles;
+                }
+                void *slab = nullptr;
+                CK(cudaMalloc(&slab, bytes));
+                slabs.push_back(slab);
+                CK(cudaMemsetAsync(slab, 0, bytes, st));
+                char *cur = (char *)slab;
+                for (int l = 1; l < nlev; ++l) {
+                    MgLev<T> &L = cd.mg[l];
+                    const size_t lb = ((size_t)L.g.total * sizeof(T) + 255) / 256 * 256;
+                    T **lf[] = {&L.cx, &L.cy, &L.cz, &L.dg, &L.z, &L.f};
+                    for (int f = 0; f < 6; ++f) { *lf[f] = (T *)cur; cur += lb; }
+                }
+            }
+        }
+        b.nlev = nlev;
         b.ncases = n;
         b.total_tiles = tiles;
         b.max_plane = maxplane;
@@ -271,6 +331,12 @@ struct Impl : ImplBase {
         CK(cudaMalloc(&dpart, sizeof(double) * NSLOT * (size_t)tiles));
         CK(cudaMalloc(&dcnt, sizeof(unsigned) * n));
         CK(cudaMemsetAsync(dcnt, 0, sizeof(unsigned) * n, st));
+        CK(cudaMalloc(&dact, sizeof(int) * 2 * act_stride(n, nlev)));
+        CK(cudaMemsetAsync(dact, 0, sizeof(int) * 2 * act_stride(n, nlev), st));
+        CK(cudaMalloc(&dactdone, sizeof(unsigned)));
+        CK(cudaMemsetAsync(dactdone, 0, sizeof(unsigned), st));
+        b.act = dact;
+        b.act_done = dactdone;
         CK(cudaMallocHost(&hsc, sizeof(double) * S_NSCAL * n));
         double rk[9] = {1., 3. / 4., 1. / 3., 0., 1. / 4., 2. / 3., 1., 1. / 4., 2. / 3.};
         CK(cudaMalloc(&drk, sizeof(rk)));
@@ -459,6 +525,11 @@ struct Impl : ImplBase {
         }
         CK(cudaStreamSynchronize(st));
         CK(cudaMemcpy3D(&m));
+        if (up && f == SULI_F_PRD1 && sizeof(T) == 4) {
+            // a pressure from the host replaces the FP64 pressure of the last solve
+            int rc2 = write_case_scalar(icase, S_P64OK, 0.0);
+            if (rc2) return rc2;
+        }
         if (!up && !isint && sizeof(T) != sizeof(double)) {
             const T *src = (const T *)hp;
             double *dst = (double *)host;
@@ -577,6 +648,18 @@ struct Impl : ImplBase {
         return setsc(S_DT, dt);
     }
 
+    // CG loop: the persistent tile kernels over the active cases (default), or
+    // one thread-block cluster per case for the whole loop (SULI_CG_PATH=clusters)
+    int cg_path = -1;   // -1 undecided, 0 tiles, 1 clusters
+    bool use_cluster()
+    {
+        if (cg_path < 0) {
+            const char *env = std::getenv("SULI_CG_PATH");
+            cg_path = (env && std::string(env) == "clusters" && cluster_cg_size<T>() > 0) ? 1 : 0;
+        }
+        return cg_path == 1;
+    }
+
     int graddin(int32_t *iters) override
     {
         int rc;
@@ -589,9 +672,18 @@ struct Impl : ImplBase {
             CKL();
             int done = 0;
             int chunk = std::max(1, std::min(prev_cg[si], cgmax));
-            for (;;) {
+            if (use_cluster()) {
                 if ((rc = ev_begin())) return rc;
-                launch_cg_iters<T>(b, chunk, st);
+                CK(launch_cg_cluster<T>(b, 0, st));
+                if ((rc = ev_end())) return rc;
+                if ((rc = read_scalars())) return rc;
+                chunk = 0;
+            }
+            int slot = 0;
+            if (chunk > 0) launch_cg_table<T>(b, slot, st);
+            for (; chunk > 0;) {
+                if ((rc = ev_begin())) return rc;
+                slot = launch_cg_iters<T>(b, chunk, slot, 0, st);
                 CKL();
                 if ((rc = ev_end())) return rc;
                 done += chunk;
@@ -606,17 +698,30 @@ struct Impl : ImplBase {
             for (int c = 0; c < ncases; ++c) maxit = std::max(maxit, (int)sc(c, S_CGITER));
             cg_outer[si] = 0;
         } else {
+            const bool mg = b.nlev > 1;
             launch_cg_refine_setup<T>(b, st);
+            if (mg) launch_mg_coarsen<T>(b, st);
             CKL();
             int done = 0;
             int passes = 0;
             for (;;) {
                 // FP32 pass until every refining case meets its inner target
-                int chunk = std::max(4, std::min(prev_cg[si], 256));
+                int chunk = mg ? std::max(2, std::min(prev_cg[si], 16)) : std::max(4, std::min(prev_cg[si], 256));
                 int pass_done = 0;
-                for (;;) {
+                if (!mg && use_cluster()) {
                     if ((rc = ev_begin())) return rc;
-                    launch_cg_refine_inner<T>(b, chunk, 0, st);
+                    CK(launch_cg_cluster<T>(b, 1, st));
+                    if ((rc = ev_end())) return rc;
+                    chunk = 0;
+                }
+                int slot = 0;
+                if (chunk > 0) {
+                    launch_cg_table<T>(b, slot, st);
+                    if (mg) launch_pcg_start<T>(b, slot, st);
+                }
+                for (; chunk > 0;) {
+                    if ((rc = ev_begin())) return rc;
+                    slot = mg ? launch_pcg_iters<T>(b, chunk, slot, st) : launch_cg_iters<T>(b, chunk, slot, 1, st);
                     CKL();
                     if ((rc = ev_end())) return rc;
                     done += chunk;
@@ -625,7 +730,7 @@ struct Impl : ImplBase {
                     bool any = false;
                     for (int c = 0; c < ncases; ++c) any |= (sc(c, S_CGACTIVE) != 0.0);
                     if (!any || done >= cgmax + 256) break;
-                    chunk = std::max(4, std::min(64, pass_done / 4));
+                    chunk = mg ? std::max(2, std::min(8, pass_done / 2)) : std::max(4, std::min(64, pass_done / 4));
                 }
                 launch_cg_refine_next<T>(b, st);
                 CKL();

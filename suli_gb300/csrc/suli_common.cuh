@@ -22,6 +22,7 @@ constexpr int TY = 4;
 constexpr int TZ = 2;
 constexpr int NTHREADS = TX * TY * TZ;
 constexpr int NSLOT = 8; // reduction slots per block
+constexpr int CG_CHUNK = 16;  // tiles per work unit of the persistent CG kernels
 
 // per-case device scalars (double), indices into CaseDev::sc
 enum Scal {
@@ -51,6 +52,8 @@ enum Scal {
     S_UPDATE,      // mixed form: 1 while a reliable update is pending
     S_RRREF,       // mixed form: FP32 r.r at the last update
     S_RRPREV,      // mixed form: r.r before the pending update
+    S_RZ,          // mixed form, multigrid-preconditioned passes: r.z
+    S_P64OK,       // mixed form: r64 holds the FP64 pressure of the last solve
     S_NSCAL
 };
 
@@ -64,11 +67,27 @@ struct Geo {
     }
 };
 
+// One multigrid level of a case (mixed form).  Level 0 is the case's own grid
+// and box; coarser levels halve each dimension (n -> (n+1)/2, cell I owning
+// fine cells 2I-1 and 2I) in a compact box of sx = nx+2, sxy = sx (ny+2).
+// cx(i,j,k) is the conductance of the face between cells i-1 and i (zero on
+// a Neumann wall), dg the sum of a cell's six face conductances.
+constexpr int MG_MAXL = 12;
+template <typename T>
+struct MgLev {
+    Geo g;
+    int ntx, nty, ntz, ntiles;
+    T *cx, *cy, *cz, *dg, *z, *f;
+};
+
 template <typename T>
 struct CaseDev {
     Geo g;
     // tiles of this case in the launch grid
     int tile_begin, ntiles, ntx, nty, ntz;
+    // chunks of CG_CHUNK consecutive tiles (the unit of the persistent CG
+    // kernels and of their reductions)
+    int chunk_begin, nchunks;
     // discretisation / physics (double in both forms)
     double dx, dy, dz, dx1, dt1, deltai;
     double alpha1, rho_f1, mu_f1, rho_f2, mu_f2, gx, gz;
@@ -90,7 +109,13 @@ struct CaseDev {
     T *bxx0, *bxx1, *blx1;      // inflow planes, indexed at(0, j, k)
     // CG work arrays
     T *spi, *spj, *spk, *dpr, *e, *r, *p, *mp, *qpr;
-    double *e64, *r64;          // mixed form: FP64 refinement vectors
+    double *e64, *r64;          // mixed form: FP64 refined solution; FP64 pressure of the last solve
+    // mixed form: FP64 pressure operator for the refinement residual (density
+    // from the FP32 level set in FP64, scaled face coefficients, diagonal, rhs)
+    double *rho64, *spi64, *spj64, *spk64, *dpr64, *qpr64;
+    // multigrid hierarchy of the mixed form's preconditioner (nlev = 0: none)
+    int nlev;
+    MgLev<T> mg[MG_MAXL];
     // reductions
     double *sc;                 // S_NSCAL scalars of this case
     double *partials;           // NSLOT * total_tiles (global base, slot-major)
@@ -168,13 +193,14 @@ __device__ __forceinline__ double block_max(double v, double *sh)
     return v;
 }
 
-// Publish NS per-block partial values; returns true in every thread of the
-// last block of the case to arrive, after which `tot` holds the case totals
-// (sums for slots with maxmask bit clear, maxima otherwise), reduced in a
-// fixed order so results do not depend on block scheduling.
+// Publish NS per-tile partial values of tile `gtile` (global tile id);
+// returns true in every thread of the block that completes the case's last
+// tile, after which `tot` holds the case totals (sums for slots with maxmask
+// bit clear, maxima otherwise), reduced in tile order so results do not
+// depend on block scheduling.
 template <typename T, int NS>
-__device__ bool last_block_reduce(const CaseDev<T> &c, const double (&vals)[NS], double (&tot)[NS],
-                                  unsigned maxmask = 0u)
+__device__ bool unit_reduce(const CaseDev<T> &c, int gunit, int ubegin, int nunits, const double (&vals)[NS],
+                            double (&tot)[NS], unsigned maxmask = 0u)
 {
     __shared__ double sh[32];
     __shared__ bool amlast;
@@ -185,10 +211,10 @@ __device__ bool last_block_reduce(const CaseDev<T> &c, const double (&vals)[NS],
     int t = tid_lin();
     if (t == 0) {
 #pragma unroll
-        for (int s = 0; s < NS; ++s) c.partials[(long long)s * c.total_tiles + blockIdx.x] = bv[s];
+        for (int s = 0; s < NS; ++s) c.partials[(long long)s * c.total_tiles + gunit] = bv[s];
         __threadfence();
         unsigned prev = atomicAdd(c.counter, 1u);
-        amlast = (prev == (unsigned)(c.ntiles - 1));
+        amlast = (prev == (unsigned)(nunits - 1));
     }
     __syncthreads();
     if (!amlast) return false;
@@ -197,8 +223,8 @@ __device__ bool last_block_reduce(const CaseDev<T> &c, const double (&vals)[NS],
     for (int s = 0; s < NS; ++s) {
         bool ismax = (maxmask >> s) & 1u;
         double a = ismax ? 0.0 : 0.0;
-        const double *src = c.partials + (long long)s * c.total_tiles + c.tile_begin;
-        for (int q = t; q < c.ntiles; q += NTHREADS) {
+        const double *src = c.partials + (long long)s * c.total_tiles + ubegin;
+        for (int q = t; q < nunits; q += NTHREADS) {
             double x = __ldcg(src + q);
             a = ismax ? fmax(a, x) : a + x;
         }
@@ -206,6 +232,164 @@ __device__ bool last_block_reduce(const CaseDev<T> &c, const double (&vals)[NS],
     }
     if (t == 0) *c.counter = 0u;
     return true;
+}
+
+// one tile per block (the launch grid is the tile grid)
+template <typename T, int NS>
+__device__ __forceinline__ bool last_block_reduce(const CaseDev<T> &c, const double (&vals)[NS], double (&tot)[NS],
+                                                  unsigned maxmask = 0u)
+{
+    return unit_reduce<T, NS>(c, (int)blockIdx.x, c.tile_begin, c.ntiles, vals, tot, maxmask);
+}
+
+// one chunk of the persistent CG kernels (u = the case's chunk index)
+template <typename T, int NS>
+__device__ __forceinline__ bool chunk_reduce(const CaseDev<T> &c, int u, const double (&vals)[NS], double (&tot)[NS])
+{
+    return unit_reduce<T, NS>(c, c.chunk_begin + u, c.chunk_begin, c.nchunks, vals, tot, 0u);
+}
+
+// ---- active-case tables (persistent CG iteration) ---------------------------
+// A table lists the cases whose CG still iterates and, per grid level s, the
+// prefix of their work-unit counts, so a fixed grid can walk exactly the
+// active units of a level.  Level 0 is the case grid and its unit is a chunk
+// of CG_CHUNK tiles; level s > 0 is multigrid level s and its unit a tile:
+//   tab[0] = n, tab[1 .. 1+n) = case ids,
+//   level s at B = 1 + N + s (N + 2): tab[B] = tiles, tab[B+1 .. B+1+n] = prefix
+// (N = cases in the batch, NL = levels in the table).
+__host__ __device__ __forceinline__ int act_stride(int ncases, int nl) { return 1 + ncases + nl * (ncases + 2); }
+__host__ __device__ __forceinline__ int act_level(int ncases, int s) { return 1 + ncases + s * (ncases + 2); }
+
+// tile `lt` of a grid with ntx x nty tiles -> the cell of this thread
+__device__ __forceinline__ void tile_cell(int ntx, int nty, int lt, int &i, int &j, int &k)
+{
+    int ti = lt % ntx;
+    int r = lt / ntx;
+    int tj = r % nty;
+    int tk = r / nty;
+    i = 1 + ti * TX + (int)threadIdx.x;
+    j = 1 + tj * TY + (int)threadIdx.y;
+    k = 1 + tk * TZ + (int)threadIdx.z;
+}
+
+template <typename T>
+__device__ __forceinline__ void tile_ijk_of(const CaseDev<T> &c, int lt, int &i, int &j, int &k)
+{
+    tile_cell(c.ntx, c.nty, lt, i, j, k);
+}
+
+// tiles [t0, t1) of unit u of a case at table level s
+template <typename T>
+__device__ __forceinline__ void unit_tiles(const CaseDev<T> &c, int s, int u, int &t0, int &t1)
+{
+    if (s == 0) {
+        t0 = u * CG_CHUNK;
+        t1 = min(c.ntiles, t0 + CG_CHUNK);
+    } else {
+        t0 = u;
+        t1 = u + 1;
+    }
+}
+
+// Block b of the grid takes the contiguous range of active units of level s,
+// [U b / G, U (b+1) / G), and calls f(case id, local unit) for each, in
+// order.  Every thread of the block makes the same calls.
+template <typename F>
+__device__ __forceinline__ void for_active_units(const int *__restrict__ tab, int N, int s, F f)
+{
+    const int n = tab[0];
+    const int *ids = tab + 1;
+    const int *lv = tab + act_level(N, s);
+    const int tiles = lv[0];
+    const int *off = lv + 1;
+    const int lo = (int)((long long)tiles * blockIdx.x / gridDim.x);
+    const int hi = (int)((long long)tiles * (blockIdx.x + 1) / gridDim.x);
+    if (lo >= hi) return;
+    int a0 = 0, a1 = n - 1;        // last slot with off <= lo
+    while (a0 < a1) {
+        int mid = (a0 + a1 + 1) >> 1;
+        if (off[mid] <= lo) a0 = mid; else a1 = mid - 1;
+    }
+    int a = a0;
+    int end = off[a + 1];
+    for (int t = lo; t < hi; ++t) {
+        while (t >= end) { ++a; end = off[a + 1]; }
+        f(ids[a], t - off[a]);
+    }
+}
+
+// exclusive prefix sum over the block (NTHREADS threads, linear id order);
+// *total gets the sum.  Contains __syncthreads: call from every thread.
+__device__ __forceinline__ int block_exscan(int v, int *total)
+{
+    __shared__ int wsum[NTHREADS / 32];
+    const int t = tid_lin(), lane = t & 31, w = t >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        int s = (lane < NTHREADS / 32) ? wsum[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        if (lane < NTHREADS / 32) wsum[lane] = s;   // inclusive warp prefix
+    }
+    __syncthreads();
+    const int before = (w > 0) ? wsum[w - 1] : 0;
+    *total = wsum[NTHREADS / 32 - 1];
+    __syncthreads();
+    return before + x - v;
+}
+
+// Build table `out` (NL levels) from the cases listed in `in` (or all N
+// cases when in is null) whose S_CGACTIVE flag is set, keeping their order.
+// One block; every thread calls it.
+template <typename T>
+__device__ void build_active_table(const CaseDev<T> *__restrict__ cs, int N, int NL, const int *in, int *out)
+{
+    const int nin = in ? in[0] : N;
+    const int t = tid_lin();
+    const int per = (nin + NTHREADS - 1) / NTHREADS;
+    const int a0 = min(nin, t * per), a1 = min(nin, a0 + per);
+    int cnt = 0;
+    for (int a = a0; a < a1; ++a) {
+        const int id = in ? in[1 + a] : a;
+        if (__ldcg(&cs[id].sc[S_CGACTIVE]) != 0.0) ++cnt;
+    }
+    int ncnt;
+    const int pos0 = block_exscan(cnt, &ncnt);
+    for (int s = 0; s < NL; ++s) {
+        int til = 0;
+        for (int a = a0; a < a1; ++a) {
+            const int id = in ? in[1 + a] : a;
+            if (__ldcg(&cs[id].sc[S_CGACTIVE]) != 0.0) til += (s == 0) ? cs[id].nchunks : cs[id].mg[s].ntiles;
+        }
+        int ntil;
+        int tpos = block_exscan(til, &ntil);
+        int *lv = out + act_level(N, s);
+        int pos = pos0;
+        for (int a = a0; a < a1; ++a) {
+            const int id = in ? in[1 + a] : a;
+            if (__ldcg(&cs[id].sc[S_CGACTIVE]) != 0.0) {
+                if (s == 0) out[1 + pos] = id;
+                lv[1 + pos] = tpos;
+                ++pos;
+                tpos += (s == 0) ? cs[id].nchunks : cs[id].mg[s].ntiles;
+            }
+        }
+        if (t == 0) {
+            lv[0] = ntil;
+            lv[1 + ncnt] = ntil;
+        }
+    }
+    if (t == 0) out[0] = ncnt;
 }
 
 // counter-based hash RNG in [0,1): the same function runs in the oracle

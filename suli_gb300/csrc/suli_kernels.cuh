@@ -21,6 +21,10 @@ struct Batch {
     int total_tiles = 0;
     int max_plane = 0;                // largest boundary plane (elements)
     double *drk = nullptr;            // TVD-RK3 coefficients a[3], b[3], g[3]
+    int *act = nullptr;               // two active-case tables of the CG iteration
+    unsigned *act_done = nullptr;     // cases done with the current B phase
+    int nlev = 1;                     // grid levels in the tables (multigrid levels, or 1)
+    int mg_tiles[MG_MAXL] = {0};      // tiles of multigrid level l over all cases
     dim3 block() const { return dim3(TX, TY, TZ); }
 };
 
@@ -49,13 +53,28 @@ template <typename T> void launch_ibm_levelset(const Batch<T> &b, cudaStream_t s
 
 // pressure (k_cg.cu)
 template <typename T> void launch_cg_setup(const Batch<T> &b, cudaStream_t s);
-template <typename T> void launch_cg_iters(const Batch<T> &b, int n, cudaStream_t s);
+// active-case table `slot` := cases with S_CGACTIVE set
+template <typename T> void launch_cg_table(const Batch<T> &b, int slot, cudaStream_t s);
+// n iterations from table `slot` (mode 0: the case's stop rule, 1: one FP32
+// pass of the mixed form); returns the slot of the table now current
+template <typename T> int launch_cg_iters(const Batch<T> &b, int n, int slot, int mode, cudaStream_t s);
+// mixed form, multigrid-preconditioned passes: start (z = M r, p = z) and n
+// iterations from table `slot` (returns the current slot)
+template <typename T> void launch_pcg_start(const Batch<T> &b, int slot, cudaStream_t s);
+template <typename T> int launch_pcg_iters(const Batch<T> &b, int n, int slot, cudaStream_t s);
+
+// multigrid (k_mg.cu): coarse operators from level 0, one V-cycle over a table
+template <typename T> void launch_mg_coarsen(const Batch<T> &b, cudaStream_t s);
+template <typename T> void launch_mg_vcycle(const Batch<T> &b, const int *tab, int grid, cudaStream_t s);
 template <typename T> void launch_cg_finish(const Batch<T> &b, cudaStream_t s);
 // mixed form: FP64 residual recomputation and correction around the FP32 inner CG
 template <typename T> void launch_cg_refine_setup(const Batch<T> &b, cudaStream_t s);
-template <typename T> void launch_cg_refine_inner(const Batch<T> &b, int n, int inner_max, cudaStream_t s);
 template <typename T> void launch_cg_refine_next(const Batch<T> &b, cudaStream_t s);
 template <typename T> void launch_cg_refine_finish(const Batch<T> &b, cudaStream_t s);
+
+// CG loop of batched small cases, one thread-block cluster per case (k_cg_cluster.cu)
+template <typename T> cudaError_t launch_cg_cluster(const Batch<T> &b, int mode, cudaStream_t s);
+template <typename T> int cluster_cg_size();
 
 // per-case scalar kernels
 template <typename T> void launch_set_scalar(const Batch<T> &b, int slot, double v, cudaStream_t s);

@@ -22,8 +22,19 @@ def _configs():
         ("dam_break", cases.dam_break(24, 12, 12)),
         ("wave_les", cases.wave_tank(32, 8, 12, dt=5e-4, cg_tol=1e-10)),
         ("mms_periodic", cases.mms_case(16)),
-        ("channel_ibm", cases.open_channel(48, 16, 16, dt=2e-3, radius=0.25, cg_tol=1e-10)),
+        ("channel_ibm", cases.open_channel(48, 16, 16, dt=2e-3, radius=0.25, cg_tol=1e-10, periodic=True)),
+        ("inflow_ibm", cases.open_channel(48, 16, 16, dt=2e-3, radius=0.25, cg_tol=1e-10)),
     ]
+
+
+def _needs_solvable_pressure(case):
+    """Prescribed inflow with free outflow (ccx0 = 3, ccxf = 4) leaves a net
+    boundary flux in the all-Neumann pressure equation of graddin: the system
+    has no solution, the CG drifts the constant mode of p without bound and
+    both sides end in round-off of a huge constant.  Routines downstream of
+    the pressure solve are compared on the closed (periodic) channel."""
+    if case.params.ccx0 == 3 and case.params.ccxf == 4:
+        pytest.skip("pressure equation without a solution (net inflow through an all-Neumann boundary)")
 
 
 @pytest.fixture(scope="module", params=_configs(), ids=lambda c: c[0])
@@ -108,12 +119,18 @@ def test_contorno(pair, nlock):
     o.contorno(nlock)
     g.contorno(nlock)
     for name in ("U", "V", "W", "PRD1"):
-        d = np.abs(g.download(name) - o.field(name)).max()
-        assert d == 0.0, "%s ghost fill differs by %g" % (name, d)
+        if case.params.ibm_t == 2 and name != "PRD1":
+            # image-point values are arithmetic (distance weights), not
+            # copies: they agree to round-off, and so do ghosts copied from them
+            assert rel_l2(g.download(name), o.field(name)) <= TOL, name
+        else:
+            d = np.abs(g.download(name) - o.field(name)).max()
+            assert d == 0.0, "%s ghost fill differs by %g" % (name, d)
 
 
 def test_graddin_posdin(pair):
     case, o, g = pair
+    _needs_solvable_pressure(case)
     if case.params.mms_t and not case.params.project_under_mms:
         pytest.skip("no projection")
     _sync(o, g)
@@ -143,6 +160,7 @@ def test_graddin_posdin(pair):
 def test_graddin_free_running_iterations(pair):
     """The GPU's own stopping test lands on the oracle's count (or one off)."""
     case, o, g = pair
+    _needs_solvable_pressure(case)
     if case.params.mms_t and not case.params.project_under_mms:
         pytest.skip("no projection")
     _sync(o, g)
@@ -162,6 +180,7 @@ def test_graddin_free_running_iterations(pair):
 
 def test_steps_replayed(pair):
     case, o, g = pair
+    _needs_solvable_pressure(case)
     _sync(o, g)
     g.set_scalar("DT", o.scalar("DT"))
     for _ in range(3):
