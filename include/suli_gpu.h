@@ -226,6 +226,23 @@ int suli_get_stream(suli_handle *h, void **stream);
 int suli_profile(suli_handle *h, int enable);
 int suli_profile_read(suli_handle *h, suli_profile_t *out);
 
+/* Divergence and max|div| of a velocity field held in caller-owned device
+ * memory, computing exactly what suli_conmassa computes, but allocating no
+ * device memory (no counterpart in the reference: it exists for callers that
+ * own every device buffer through their own allocator or memory budget, e.g.
+ * a Fortran host whose arrays live in CUDA Fortran / OpenACC data regions).
+ * u, v, w, div are device arrays in the reference layout: u(0:nx+2,0:ny+1,
+ * 0:nz+1), v(0:nx+1,0:ny+2,0:nz+1), w(0:nx+1,0:ny+1,0:nz+2), div(1:nx,1:ny,
+ * 1:nz), column-major; maxdiv is one device double.  Limit: nz <= 4096 (the
+ * z-planes its built-in 32 KiB scratch holds); larger nz returns
+ * SULI_BAD_ARG.  The scratch is one static device array shared by every
+ * call: calls that overlap on the GPU race and must be serialised.  The first
+ * call on each device looks up the scratch address; make it before any
+ * stream capture.  Enqueued on `stream` (a cudaStream_t; NULL = default). */
+int suli_conmassa_noalloc(const double *u, const double *v, const double *w, int32_t nx, int32_t ny,
+                          int32_t nz, double dx, double dy, double dz, double *div, double *maxdiv,
+                          void *stream);
+
 /* Text of the last error on this thread (empty if none). */
 int suli_last_error(char *buf, size_t len);
 

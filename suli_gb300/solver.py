@@ -28,7 +28,7 @@ EXPORTS = [
     "suli_convdiff", "suli_complementos", "suli_tempo", "suli_graddin", "suli_posdin", "suli_conmassa",
     "suli_mms_error", "suli_set_stage", "suli_step", "suli_diagnostics", "suli_synchronize",
     "suli_last_error", "suli_device_info", "suli_get_stream", "suli_profile", "suli_profile_read",
-    "suli_ibm_setup",
+    "suli_ibm_setup", "suli_conmassa_noalloc",
 ]
 
 
@@ -82,6 +82,8 @@ def load_library(path: str = LIB_PATH):
     L.suli_get_stream.argtypes = [C.c_void_p, P(C.c_void_p)]
     L.suli_profile.argtypes = [C.c_void_p, C.c_int]
     L.suli_profile_read.argtypes = [C.c_void_p, P(SuliProfile)]
+    L.suli_conmassa_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, i32, i32, i32, C.c_double,
+                                        C.c_double, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]
     _lib = L
     return L
 
