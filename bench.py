@@ -4,16 +4,20 @@
 Workload (default): the batched ensemble -- 256 independent sloshing /
 dam-break cases, grid dims drawn per axis from U{32..96} (seed 0), advanced
 in lockstep by the same launches, mixed precision (FP32 storage and
-stencils, FP32 inner CG inside FP64 iterative refinement, FP64 sums).  A
-"step" is one full time step of every case (1_principal.f90:69-124).
+stencils, FP32 inner passes -- CG preconditioned by a multigrid V-cycle by
+default, --precond jacobi for the reference's Jacobi-scaled CG -- inside
+FP64 iterative refinement, FP64 sums).  A "step" is one full time step of
+every case (1_principal.f90:69-124).
 
 Printed JSON line (rank 0): value = cell-steps/s of the mixed form with all
 fields resident in HBM; the plain FP64 form of the same workload is timed
 beside it ("fp64"), the e2e figure goes through the C ABI with host
 buffers (state uploaded from pinned host memory and read back every step),
-the roofline entry is the CG iteration loop (event-timed inside the
-library's stream) and cpu_baseline is the oracle (a port of the reference,
-OpenMP where the reference has it) on a bounded sample.
+the roofline entry is the dominant kernel timed alone over every case
+(CUDA events on the library's stream), "accuracy" is the mixed form against
+the FP64 form on the 64x32x32 dam break after 200 steps, and cpu_baseline
+is the oracle (a port of the reference, OpenMP where the reference has it)
+on a bounded sample.
 
 --impl reference times the reference's CPU implementation (the oracle port:
 no Fortran compiler exists on either machine) on the same workload.
@@ -51,6 +55,12 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--profile-kernel", type=int, default=-1,
+                    help="profiling mode: after the warm-up steps of the mixed form, one launch of kernel K "
+                         "(0 CG matrix-vector, 1 smoother half-sweep, 2 CG update) between "
+                         "cudaProfilerStart/Stop, for ncu --profile-from-start off; prints its time")
+    ap.add_argument("--accuracy-steps", type=int, default=200,
+                    help="steps of the dam-break mixed-vs-FP64 accuracy run (0: skip)")
     return ap.parse_args()
 
 
@@ -200,6 +210,28 @@ def compare_forms(gm, g64, ncheck):
     return errs
 
 
+def accuracy_run(args):
+    """The mixed form against the plain FP64 form (which matches the oracle
+    to 1e-10) on the dam-break configuration: 64x32x32, 200 steps, outside
+    any timed region.  Relative L2 after the last step."""
+    from suli_gb300 import cases
+    from suli_gb300._abi import PREC_FP64, PREC_MIXED
+    out = {"workload": "dam_break_64x32x32", "steps": args.accuracy_steps}
+    gs = {}
+    for name, prec in (("fp64", PREC_FP64), ("mixed", PREC_MIXED)):
+        c = cases.dam_break(64, 32, 32, precision=prec)
+        c.params.mixed_precond = 1 if args.precond == "multigrid" else 0
+        g = start_gpu([c])
+        g.step(args.accuracy_steps)
+        g.synchronize()
+        gs[name] = g
+    errs = compare_forms(gs["mixed"], gs["fp64"], 1)
+    for g in gs.values():
+        g.close()
+    out.update({"rel_l2_" + k: v for k, v in errs.items()})
+    return out
+
+
 def e2e_run(args, cs, torch):
     """Per step: pinned host state -> device, one step, device -> host."""
     g = start_gpu(cs)
@@ -306,14 +338,22 @@ def main():
 
     name, cs_m = make_cases(args, PREC_MIXED, rank)
     cells = sum(c.cells for c in cs_m)
+    if args.profile_kernel >= 0:
+        g = start_gpu(cs_m)
+        g.step(args.warmup)
+        g.time_kernel(args.profile_kernel, 2)      # untimed: tables and caches warm
+        g.synchronize()
+        torch.cuda.cudart().cudaProfilerStart()
+        ms, by = g.time_kernel(args.profile_kernel, 1)
+        torch.cuda.cudart().cudaProfilerStop()
+        g.close()
+        print(json.dumps({"profile_kernel": args.profile_kernel, "workload": name, "cells": cells,
+                          "ms_per_launch": ms, "algorithmic_bytes_per_launch": by}))
+        return
     sampler = ClockSampler(local) if rank == 0 else None
     gm, ms_m, prof_m, clocks = run_form(args, cs_m, torch, sampler, dist)
     value = world * cells * args.steps / (ms_m / 1e3)
     peak, peak_src = measured_peak_hbm()
-    s_bytes = 4.0
-    cg_ach = None
-    if prof_m.cg_ms > 0:
-        cg_ach = 7.0 * s_bytes * prof_m.cg_cell_iters / (prof_m.cg_ms / 1e3) / 1e9
     line = {
         "metric": "cell-steps/s (mixed-precision batched SuLi steps)",
         "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -326,14 +366,22 @@ def main():
                    "device": devname, "sms": sms},
         "gpu_launches": int(prof_m.launches),
         "clocks": clocks,
-        "roofline": {"bound": "hbm", "kernel": "CG iteration (k_cgi_A + k_cgi_B + k_cgi_C)",
-                     "achieved": cg_ach, "peak": peak, "unit": "GB/s",
-                     "frac": (cg_ach / peak) if cg_ach else None, "traffic": None,
-                     "peak_source": peak_src,
-                     "algorithmic_bytes_per_cell_iter": 7 * s_bytes,
-                     "kernel_bytes_per_cell_iter": prof_m.cg_bytes_per_cell_iter,
-                     "cg_cell_iters": prof_m.cg_cell_iters, "cg_ms": prof_m.cg_ms},
     }
+    # roofline of the dominant kernel, timed alone over every case of the
+    # workload with CUDA events on the library's stream (burst peak)
+    kern = 1 if args.precond == "multigrid" else 0
+    kname = {0: "k_cgi_A (CG matrix-vector product + p.Ap)",
+             1: "k_mg_smooth on the case grid (one red-black half-sweep)"}[kern]
+    ms_k, bytes_k = gm.time_kernel(kern, 20)
+    ach = bytes_k / (ms_k / 1e3) / 1e9
+    line["roofline"] = {"bound": "hbm", "kernel": kname, "achieved": ach, "peak": peak, "unit": "GB/s",
+                        "frac": ach / peak, "traffic": None, "peak_source": peak_src,
+                        "algorithmic_bytes_per_launch": bytes_k, "ms_per_launch": ms_k,
+                        "timing": "kernel alone, 20 launches between CUDA events, all cases of the workload"}
+    ms_a, bytes_a = gm.time_kernel(0, 20)
+    line["roofline_cg_matvec"] = {"kernel": "k_cgi_A", "achieved": bytes_a / (ms_a / 1e3) / 1e9,
+                                  "ms_per_launch": ms_a, "algorithmic_bytes_per_launch": bytes_a}
+    line["cg_loop"] = {"cell_iters": prof_m.cg_cell_iters, "ms": prof_m.cg_ms}
     diag = gm.diag(0)
     line["cg_iters_case0"] = list(diag.cg_iters)
     line["cg_outer_case0"] = list(diag.cg_outer)
@@ -353,6 +401,11 @@ def main():
         except Exception as e:  # reported, not hidden
             line["fp64"] = {"error": repr(e)}
     gm.close()
+    if args.accuracy_steps > 0 and rank == 0:
+        try:
+            line["accuracy"] = accuracy_run(args)
+        except Exception as e:
+            line["accuracy"] = {"error": repr(e)}
     if not args.no_e2e:
         try:
             line["e2e"] = e2e_run(args, cs_m, torch)

@@ -225,6 +225,15 @@ typedef struct suli_profile_t {
 int suli_get_stream(suli_handle *h, void **stream);
 int suli_profile(suli_handle *h, int enable);
 int suli_profile_read(suli_handle *h, suli_profile_t *out);
+/* Measurement only (no counterpart in the reference): time one kernel alone
+ * over every case of the handle, `reps` launches between CUDA events on the
+ * handle's stream.  kernel 0: the CG matrix-vector product (k_cgi_A),
+ * 1: one red half-sweep of the multigrid smoother on the case grid (mixed form
+ * with mixed_precond = 1 only), 2: the CG direction update (k_cgi_C).
+ * Returns the mean time per launch and the algorithmic bytes one launch
+ * moves.  The solver work arrays it touches are rebuilt by the next
+ * suli_graddin. */
+int suli_time_kernel(suli_handle *h, int kernel, int reps, double *ms_per_launch, double *bytes_per_launch);
 
 /* Divergence and max|div| of a velocity field held in caller-owned device
  * memory, computing exactly what suli_conmassa computes, but allocating no

@@ -31,6 +31,10 @@ namespace suli {
 
 #define AT(arr, i, j, k) (arr)[g.at((i), (j), (k))]
 
+// iterations of one multigrid-preconditioned FP32 pass at most (a pass that
+// stagnates in FP32 hands over to the next FP64 residual)
+constexpr int MG_PASS_MAX = 40;
+
 __device__ __forceinline__ int bmap(int i, int n, bool per)
 {
     if (i < 1) return per ? n : 1;
@@ -269,7 +273,9 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_setup3(const CaseDev<T> *__rest
 // to table `out`, which the rest of the iteration and the next k_cgi_A read.
 
 // mp = A p, partial p.mp (:411-452); the case's last chunk forms
-// alpha = sc[num] / p.mp (num = S_RR for CG, S_RZ for preconditioned CG)
+// alpha = sc[num] / p.mp (num = S_RR for CG, S_RZ for preconditioned CG).
+// Every kernel below walks its unit UW tiles at a time, issuing the loads of
+// UW cells before the stores.
 template <typename T>
 __global__ void __launch_bounds__(NTHREADS) k_cgi_A(const CaseDev<T> *__restrict__ cs, const int *__restrict__ tab,
                                                     int N, int num)
@@ -279,26 +285,41 @@ __global__ void __launch_bounds__(NTHREADS) k_cgi_A(const CaseDev<T> *__restrict
         const Geo &g = c.g;
         const int nx = g.nx, ny = g.ny, nz = g.nz;
         const bool px = (c.ccx0 == 0), py = (c.ccy0 == 0);
-        const T *__restrict__ p = c.p;
+        const T *p = c.p;
         int t0, t1;
         unit_tiles(c, 0, u, t0, t1);
+        TileWalk w(t0, c.ntx, c.nty);
         double pm = 0.0;
-        for (int lt = t0; lt < t1; ++lt) {
-            int i, j, k;
-            tile_ijk_of(c, lt, i, j, k);
-            if (i > nx || j > ny || k > nz) continue;
-            const long long q = g.at(i, j, k);
-            T pc = p[q];
-            T pxp = (i < nx) ? p[q + 1] : AT(p, bmap(nx + 1, nx, px), j, k);
-            T pxm = (i > 1) ? p[q - 1] : AT(p, bmap(0, nx, px), j, k);
-            T pyp = (j < ny) ? p[q + g.sx] : AT(p, i, bmap(ny + 1, ny, py), k);
-            T pym = (j > 1) ? p[q - g.sx] : AT(p, i, bmap(0, ny, py), k);
-            T pzp = (k < nz) ? p[q + g.sxy] : pc;
-            T pzm = (k > 1) ? p[q - g.sxy] : pc;
-            T m = pc - pxp * c.spi[q + 1] - pxm * c.spi[q] - pyp * c.spj[q + g.sx] - pym * c.spj[q] -
-                  pzp * c.spk[q + g.sxy] - pzm * c.spk[q];
-            c.mp[q] = m;
-            pm += (double)pc * (double)m;
+        for (int lt = t0; lt < t1; lt += UW) {
+            long long q[UW];
+            int ci[UW], cj[UW], ck[UW];
+            bool v[UW];
+            w.next<UW>(lt, t1, g, q, ci, cj, ck, v);
+            T m[UW], pcs[UW];
+#pragma unroll
+            for (int a = 0; a < UW; ++a) {
+                // neighbour indices: Neumann maps a wall neighbour to the cell
+                // itself, periodic x/y to the opposite end (no branch: every
+                // load is issued, at a clamped cell for padding lanes)
+                const int i = ci[a], j = cj[a], k = ck[a];
+                const long long qq = q[a];
+                const long long qxp = (i < nx) ? qq + 1 : (px ? qq - (nx - 1) : qq);
+                const long long qxm = (i > 1) ? qq - 1 : (px ? qq + (nx - 1) : qq);
+                const long long qyp = (j < ny) ? qq + g.sx : (py ? qq - (long long)(ny - 1) * g.sx : qq);
+                const long long qym = (j > 1) ? qq - g.sx : (py ? qq + (long long)(ny - 1) * g.sx : qq);
+                const long long qzp = (k < nz) ? qq + g.sxy : qq;
+                const long long qzm = (k > 1) ? qq - g.sxy : qq;
+                const T pc = p[qq];
+                m[a] = pc - p[qxp] * c.spi[qq + 1] - p[qxm] * c.spi[qq] - p[qyp] * c.spj[qq + g.sx] -
+                       p[qym] * c.spj[qq] - p[qzp] * c.spk[qq + g.sxy] - p[qzm] * c.spk[qq];
+                pcs[a] = pc;
+            }
+#pragma unroll
+            for (int a = 0; a < UW; ++a)
+                if (v[a]) {
+                    c.mp[q[a]] = m[a];
+                    pm += (double)pcs[a] * (double)m[a];
+                }
         }
         double vals[1] = {pm}, tot[1];
         if (chunk_reduce<T, 1>(c, u, vals, tot) && tid_lin() == 0) c.sc[S_ALPHA] = c.sc[num] / tot[0];
@@ -331,17 +352,29 @@ __global__ void __launch_bounds__(NTHREADS) k_cgi_B(const CaseDev<T> *__restrict
         const T alpha = T(c.sc[S_ALPHA]);
         int t0, t1;
         unit_tiles(c, 0, u, t0, t1);
+        TileWalk w(t0, c.ntx, c.nty);
         double rr = 0.0;
-        for (int lt = t0; lt < t1; ++lt) {
-            int i, j, k;
-            tile_ijk_of(c, lt, i, j, k);
-            if (i > g.nx || j > g.ny || k > g.nz) continue;
-            const long long q = g.at(i, j, k);
-            c.e[q] = c.e[q] - alpha * c.p[q];
-            T r = c.r[q] - alpha * c.mp[q];
-            c.r[q] = r;
-            if (MODE == 2) c.mg[0].f[q] = sqrt(c.dpr[q]) * r;
-            rr += (double)r * (double)r;
+        for (int lt = t0; lt < t1; lt += UW) {
+            long long q[UW];
+            int ci[UW], cj[UW], ck[UW];
+            bool v[UW];
+            w.next<UW>(lt, t1, g, q, ci, cj, ck, v);
+            T en[UW], rn[UW], fn[UW];
+#pragma unroll
+            for (int a = 0; a < UW; ++a) {
+                const long long qq = q[a];
+                en[a] = c.e[qq] - alpha * c.p[qq];
+                rn[a] = c.r[qq] - alpha * c.mp[qq];
+                fn[a] = (MODE == 2) ? sqrt(c.dpr[qq]) * rn[a] : T(0);
+            }
+#pragma unroll
+            for (int a = 0; a < UW; ++a)
+                if (v[a]) {
+                    c.e[q[a]] = en[a];
+                    c.r[q[a]] = rn[a];
+                    if (MODE == 2) c.mg[0].f[q[a]] = fn[a];
+                    rr += (double)rn[a] * (double)rn[a];
+                }
         }
         double vals[1] = {rr}, tot[1];
         if (chunk_reduce<T, 1>(c, u, vals, tot)) {
@@ -353,7 +386,8 @@ __global__ void __launch_bounds__(NTHREADS) k_cgi_B(const CaseDev<T> *__restrict
                 c.sc[S_RR] = rrn;
                 double active;
                 if (MODE >= 1) {
-                    active = (rrn > c.sc[S_RRREF] && it < c.sc[S_CGMAX]) ? 1.0 : 0.0;
+                    active = (rrn > c.sc[S_RRREF] && it < c.sc[S_CGMAX] &&
+                              (MODE == 1 || it - c.sc[S_PASS0] < (double)MG_PASS_MAX)) ? 1.0 : 0.0;
                 } else {
                     double replay = c.sc[S_CGREPLAY];
                     if (replay >= 0.0) active = (it < replay) ? 1.0 : 0.0;
@@ -384,12 +418,18 @@ __global__ void __launch_bounds__(NTHREADS) k_cgi_C(const CaseDev<T> *__restrict
         const T beta = T(c.sc[S_BETA]);
         int t0, t1;
         unit_tiles(c, 0, u, t0, t1);
-        for (int lt = t0; lt < t1; ++lt) {
-            int i, j, k;
-            tile_ijk_of(c, lt, i, j, k);
-            if (i > g.nx || j > g.ny || k > g.nz) continue;
-            const long long q = g.at(i, j, k);
-            c.p[q] = c.r[q] + beta * c.p[q];
+        TileWalk w(t0, c.ntx, c.nty);
+        for (int lt = t0; lt < t1; lt += UW) {
+            long long q[UW];
+            int ci[UW], cj[UW], ck[UW];
+            bool v[UW];
+            w.next<UW>(lt, t1, g, q, ci, cj, ck, v);
+            T pn[UW];
+#pragma unroll
+            for (int a = 0; a < UW; ++a) pn[a] = c.r[q[a]] + beta * c.p[q[a]];
+#pragma unroll
+            for (int a = 0; a < UW; ++a)
+                if (v[a]) c.p[q[a]] = pn[a];
         }
     });
 }
@@ -405,14 +445,22 @@ __global__ void __launch_bounds__(NTHREADS) k_pcg_dot(const CaseDev<T> *__restri
         const Geo &g = c.g;
         int t0, t1;
         unit_tiles(c, 0, u, t0, t1);
+        TileWalk w(t0, c.ntx, c.nty);
         double rz = 0.0;
-        for (int lt = t0; lt < t1; ++lt) {
-            int i, j, k;
-            tile_ijk_of(c, lt, i, j, k);
-            if (i > g.nx || j > g.ny || k > g.nz) continue;
-            const long long q = g.at(i, j, k);
-            T z = sqrt(c.dpr[q]) * c.mg[0].z[q];
-            rz += (double)z * (double)c.r[q];
+        for (int lt = t0; lt < t1; lt += UW) {
+            long long q[UW];
+            int ci[UW], cj[UW], ck[UW];
+            bool v[UW];
+            w.next<UW>(lt, t1, g, q, ci, cj, ck, v);
+            T zz[UW], rv[UW];
+#pragma unroll
+            for (int a = 0; a < UW; ++a) {
+                zz[a] = sqrt(c.dpr[q[a]]) * c.mg[0].z[q[a]];
+                rv[a] = c.r[q[a]];
+            }
+#pragma unroll
+            for (int a = 0; a < UW; ++a)
+                if (v[a]) rz += (double)zz[a] * (double)rv[a];
         }
         double vals[1] = {rz}, tot[1];
         if (chunk_reduce<T, 1>(c, u, vals, tot) && tid_lin() == 0) {
@@ -433,12 +481,18 @@ __global__ void __launch_bounds__(NTHREADS) k_pcg_C(const CaseDev<T> *__restrict
         const T beta = T(c.sc[S_BETA]);
         int t0, t1;
         unit_tiles(c, 0, u, t0, t1);
-        for (int lt = t0; lt < t1; ++lt) {
-            int i, j, k;
-            tile_ijk_of(c, lt, i, j, k);
-            if (i > g.nx || j > g.ny || k > g.nz) continue;
-            const long long q = g.at(i, j, k);
-            c.p[q] = sqrt(c.dpr[q]) * c.mg[0].z[q] + beta * c.p[q];
+        TileWalk w(t0, c.ntx, c.nty);
+        for (int lt = t0; lt < t1; lt += UW) {
+            long long q[UW];
+            int ci[UW], cj[UW], ck[UW];
+            bool v[UW];
+            w.next<UW>(lt, t1, g, q, ci, cj, ck, v);
+            T pn[UW];
+#pragma unroll
+            for (int a = 0; a < UW; ++a) pn[a] = sqrt(c.dpr[q[a]]) * c.mg[0].z[q[a]] + beta * c.p[q[a]];
+#pragma unroll
+            for (int a = 0; a < UW; ++a)
+                if (v[a]) c.p[q[a]] = pn[a];
         }
     });
 }
@@ -447,9 +501,9 @@ __global__ void __launch_bounds__(NTHREADS) k_pcg_C(const CaseDev<T> *__restrict
 // completion counter (one block)
 template <typename T>
 __global__ void __launch_bounds__(NTHREADS) k_cgi_table(const CaseDev<T> *__restrict__ cs, int *__restrict__ out,
-                                                        unsigned *__restrict__ done, int N, int NL)
+                                                        unsigned *__restrict__ done, int N, int NL, int all)
 {
-    build_active_table<T>(cs, N, NL, nullptr, out);
+    build_active_table<T>(cs, N, NL, nullptr, out, all != 0);
     if (tid_lin() == 0) *done = 0u;
 }
 
@@ -551,8 +605,11 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_true_residual(const CaseDev<T> 
         double passes = c.sc[S_OUTER] + 1.0;
         bool conv = !(rrt > c.sc[S_THR]) || c.sc[S_CGITER] >= c.sc[S_CGMAX];
         c.sc[S_RR] = tot[1];
-        // inner target: 1e3 reduction, but no further than half the outer target
-        c.sc[S_RRREF] = fmax(1e-6 * tot[1], 0.25 * c.sc[S_THR]);
+        // inner target: a residual reduction of 1e3 (Jacobi-scaled passes) or
+        // 1e4 (multigrid-preconditioned passes), but no further than half the
+        // outer target; a pass also ends after MG_PASS_MAX iterations
+        c.sc[S_RRREF] = fmax((c.nlev > 0 ? 1e-8 : 1e-6) * tot[1], 0.25 * c.sc[S_THR]);
+        c.sc[S_PASS0] = c.sc[S_CGITER];
         if (conv) {
             c.sc[S_OUTER] = -passes;           // negative: done after `passes` FP64 residuals
             c.sc[S_CGACTIVE] = 0.0;
@@ -622,8 +679,29 @@ template <typename T> const int *cg_table(const Batch<T> &b, int slot)
 template <typename T> void launch_cg_table(const Batch<T> &b, int slot, cudaStream_t s)
 {
     k_cgi_table<T><<<1, b.block(), 0, s>>>(b.dcases, b.act + slot * act_stride(b.ncases, b.nlev), b.act_done,
-                                           b.ncases, b.nlev);
+                                           b.ncases, b.nlev, 0);
     count_launch();
+}
+
+// Profiling: one launch of a single kernel over every case of the batch,
+// on table slot 2 (which the solver never uses).  kernel 0: k_cgi_A (the
+// CG matrix-vector product and p.Ap), 1: k_mg_smooth on level 0 (one red
+// half-sweep), 2: k_cgi_C (p = r + beta p).  The solver state these touch
+// (mp, the level-0 correction, p) is rebuilt by the next pressure solve.
+template <typename T> int launch_profile_kernel(const Batch<T> &b, int kernel, int prepare, cudaStream_t s)
+{
+    int *tab = b.act + 2 * act_stride(b.ncases, b.nlev);
+    if (prepare) {
+        k_cgi_table<T><<<1, b.block(), 0, s>>>(b.dcases, tab, b.act_done, b.ncases, b.nlev, 1);
+        count_launch();
+    }
+    const int G = cg_iter_grid<T>();
+    if (kernel == 0) k_cgi_A<T><<<G, b.block(), 0, s>>>(b.dcases, tab, b.ncases, S_RR);
+    else if (kernel == 1) return launch_mg_smooth0<T>(b, tab, G, s);
+    else if (kernel == 2) k_cgi_C<T><<<G, b.block(), 0, s>>>(b.dcases, tab, b.ncases);
+    else return -1;
+    count_launch();
+    return 0;
 }
 
 // n iterations starting from table `slot`; returns the slot of the last table
@@ -698,10 +776,12 @@ template <typename T> void launch_cg_refine_finish(const Batch<T> &b, cudaStream
 
 template void launch_cg_setup<double>(const Batch<double> &, cudaStream_t);
 template void launch_cg_table<double>(const Batch<double> &, int, cudaStream_t);
+template int launch_profile_kernel<double>(const Batch<double> &, int, int, cudaStream_t);
 template int launch_cg_iters<double>(const Batch<double> &, int, int, int, cudaStream_t);
 template void launch_cg_finish<double>(const Batch<double> &, cudaStream_t);
 template void launch_cg_setup<float>(const Batch<float> &, cudaStream_t);
 template void launch_cg_table<float>(const Batch<float> &, int, cudaStream_t);
+template int launch_profile_kernel<float>(const Batch<float> &, int, int, cudaStream_t);
 template int launch_cg_iters<float>(const Batch<float> &, int, int, int, cudaStream_t);
 template void launch_pcg_start<float>(const Batch<float> &, int, cudaStream_t);
 template int launch_pcg_iters<float>(const Batch<float> &, int, int, cudaStream_t);

@@ -59,7 +59,8 @@ __device__ __forceinline__ T mg_nbsum(const MgLev<T> &L, int i, int j, int k, lo
 }
 
 // one colour of red-black Gauss-Seidel on L z = f; zero != 0: the sweep
-// starts from z = 0 (this colour gets f / dg, the other colour 0)
+// starts from z = 0 (this colour gets f / dg, the other colour 0).  The cells
+// of UW tiles are loaded before any is written.
 template <typename T>
 __global__ void __launch_bounds__(NTHREADS) k_mg_smooth(const CaseDev<T> *__restrict__ cs, const int *__restrict__ tab,
                                                         int N, int l, int color, int zero)
@@ -68,22 +69,51 @@ __global__ void __launch_bounds__(NTHREADS) k_mg_smooth(const CaseDev<T> *__rest
         const CaseDev<T> &c = cs[id];
         const MgLev<T> &L = c.mg[l];
         const Geo &g = L.g;
+        const int nx = g.nx, ny = g.ny;
+        const long long sx = g.sx, sxy = g.sxy;
+        // wrap couplings the smoother keeps (even periodic length, see above);
+        // elsewhere a wall neighbour is a ghost of z (never written: zero) and
+        // the wall conductance is zero, so the stencil needs no branch
+        const bool wx = c.ccx0 == 0 && !(nx & 1) && nx > 1;
+        const bool wy = c.ccy0 == 0 && !(ny & 1) && ny > 1;
+        const T *z = L.z;
         int t0, t1;
         unit_tiles(c, l, u, t0, t1);
-        for (int lt = t0; lt < t1; ++lt) {
-            int i, j, k;
-            tile_cell(L.ntx, L.nty, lt, i, j, k);
-            if (i > g.nx || j > g.ny || k > g.nz) continue;
-            const long long q = g.at(i, j, k);
-            const bool mine = ((i + j + k) & 1) == color;
-            const T d = L.dg[q];
+        TileWalk w(t0, L.ntx, L.nty);
+        for (int lt = t0; lt < t1; lt += UW) {
+            long long q[UW];
+            int ci[UW], cj[UW], ck[UW];
+            bool v[UW];
+            w.next<UW>(lt, t1, g, q, ci, cj, ck, v);
+            T zn[UW];
+            bool wr[UW];
             if (zero) {
-                L.z[q] = (mine && d > T(0)) ? L.f[q] / d : T(0);
-                continue;
+#pragma unroll
+                for (int a = 0; a < UW; ++a) {
+                    const bool mine = ((ci[a] + cj[a] + ck[a]) & 1) == color;
+                    const T d = L.dg[q[a]], fv = L.f[q[a]];
+                    zn[a] = (mine && d > T(0)) ? fv / d : T(0);
+                    wr[a] = v[a];
+                }
+            } else {
+#pragma unroll
+                for (int a = 0; a < UW; ++a) {
+                    const int i = ci[a], j = cj[a];
+                    const long long qq = q[a];
+                    const long long qxm = (wx && i == 1) ? qq + (nx - 1) : qq - 1;
+                    const long long qxp = (wx && i == nx) ? qq - (nx - 1) : qq + 1;
+                    const long long qym = (wy && j == 1) ? qq + (long long)(ny - 1) * sx : qq - sx;
+                    const long long qyp = (wy && j == ny) ? qq - (long long)(ny - 1) * sx : qq + sx;
+                    const T d = L.dg[qq];
+                    const T s = L.f[qq] + L.cx[qq] * z[qxm] + L.cx[qq + 1] * z[qxp] + L.cy[qq] * z[qym] +
+                                L.cy[qq + sx] * z[qyp] + L.cz[qq] * z[qq - sxy] + L.cz[qq + sxy] * z[qq + sxy];
+                    zn[a] = (d > T(0)) ? s / d : T(0);
+                    wr[a] = v[a] && (((i + j + ck[a]) & 1) == color);
+                }
             }
-            if (!mine) continue;
-            if (!(d > T(0))) { L.z[q] = T(0); continue; }
-            L.z[q] = (L.f[q] + mg_nbsum(L, i, j, k, q, c.ccx0 == 0, c.ccy0 == 0, true)) / d;
+#pragma unroll
+            for (int a = 0; a < UW; ++a)
+                if (wr[a]) L.z[q[a]] = zn[a];
         }
     });
 }
@@ -132,11 +162,19 @@ __global__ void __launch_bounds__(NTHREADS) k_mg_prolong(const CaseDev<T> *__res
         const MgLev<T> &C = c.mg[l + 1];
         int t0, t1;
         unit_tiles(c, l, u, t0, t1);
-        for (int lt = t0; lt < t1; ++lt) {
-            int i, j, k;
-            tile_cell(F.ntx, F.nty, lt, i, j, k);
-            if (i > F.g.nx || j > F.g.ny || k > F.g.nz) continue;
-            F.z[F.g.at(i, j, k)] += C.z[C.g.at((i + 1) >> 1, (j + 1) >> 1, (k + 1) >> 1)];
+        TileWalk w(t0, F.ntx, F.nty);
+        for (int lt = t0; lt < t1; lt += UW) {
+            long long q[UW];
+            int ci[UW], cj[UW], ck[UW];
+            bool v[UW];
+            w.next<UW>(lt, t1, F.g, q, ci, cj, ck, v);
+            T zn[UW];
+#pragma unroll
+            for (int a = 0; a < UW; ++a)
+                zn[a] = F.z[q[a]] + C.z[C.g.at((ci[a] + 1) >> 1, (cj[a] + 1) >> 1, (ck[a] + 1) >> 1)];
+#pragma unroll
+            for (int a = 0; a < UW; ++a)
+                if (v[a]) F.z[q[a]] = zn[a];
         }
     });
 }
@@ -247,7 +285,18 @@ template <typename T> void launch_mg_vcycle(const Batch<T> &b, const int *tab, i
     }
 }
 
+// profiling: one red half-sweep on level 0 over table `tab`
+template <typename T> int launch_mg_smooth0(const Batch<T> &b, const int *tab, int grid, cudaStream_t s)
+{
+    if (b.nlev < 2) return -1;
+    k_mg_smooth<T><<<grid, b.block(), 0, s>>>(b.dcases, tab, b.ncases, 0, 0, 0);
+    count_launch();
+    return 0;
+}
+template <> int launch_mg_smooth0<double>(const Batch<double> &, const int *, int, cudaStream_t) { return -1; }
+
 template void launch_mg_coarsen<float>(const Batch<float> &, cudaStream_t);
+template int launch_mg_smooth0<float>(const Batch<float> &, const int *, int, cudaStream_t);
 template void launch_mg_vcycle<float>(const Batch<float> &, const int *, int, cudaStream_t);
 
 }  // namespace suli

@@ -67,6 +67,7 @@ extern "C" void suli_default_params(suli_params *p)
     p->cg_tol = 1e-4;
     p->precision = SULI_PREC_FP64;
     p->vol_loop_max = 1000;
+    p->mixed_precond = 1;
 }
 
 extern "C" int suli_field_shape(const suli_params *p, int f, int lo[3], int hi[3])
@@ -152,6 +153,7 @@ struct ImplBase {
     virtual int read_scalars() = 0;
     virtual int write_case_scalar(int icase, int slot, double v) = 0;
     virtual int sync() = 0;
+    virtual int time_kernel(int kernel, int reps, double *ms, double *bytes) = 0;
     virtual int ibm_setup() = 0;
     unsigned long long inflow_calls = 0;
     int ncases = 0;
@@ -176,6 +178,38 @@ struct suli_handle {
     ImplBase *impl;
 };
 
+// Field transfer of the mixed form: the caller's FP64 block (reference
+// layout, dense, e0 x e1 x e2 column-major) <-> the padded FP32 device box
+// (row pitch `pitch`, `height` rows per plane, block origin lo0/lo1/lo2),
+// converted on the GPU through an FP64 device staging buffer.
+template <typename T>
+__global__ void k_unpack_field(const double *__restrict__ src, T *__restrict__ box, long long n, int e0, int e1,
+                               int lo0, int lo1, int lo2, long long pitch, long long height)
+{
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % e0);
+        const long long r = t / e0;
+        const int j = (int)(r % e1);
+        const int k = (int)(r / e1);
+        box[(lo0 + i) + pitch * ((lo1 + j) + height * (long long)(lo2 + k))] = T(src[t]);
+    }
+}
+
+template <typename T>
+__global__ void k_pack_field(const T *__restrict__ box, double *__restrict__ dst, long long n, int e0, int e1,
+                             int lo0, int lo1, int lo2, long long pitch, long long height)
+{
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % e0);
+        const long long r = t / e0;
+        const int j = (int)(r % e1);
+        const int k = (int)(r / e1);
+        dst[t] = (double)box[(lo0 + i) + pitch * ((lo1 + j) + height * (long long)(lo2 + k))];
+    }
+}
+
 template <typename T>
 struct Impl : ImplBase {
     Batch<T> b;
@@ -184,6 +218,8 @@ struct Impl : ImplBase {
     double *dsc = nullptr, *dpart = nullptr, *drk = nullptr;
     unsigned *dcnt = nullptr, *dactdone = nullptr;
     int *dact = nullptr;
+    double *dstage = nullptr;      // mixed form: FP64 staging of field transfers
+    size_t stage_elems = 0;
     cudaStream_t st = nullptr;
 
     ~Impl() override
@@ -195,6 +231,7 @@ struct Impl : ImplBase {
         cudaFree(dcnt);
         cudaFree(dact);
         cudaFree(dactdone);
+        cudaFree(dstage);
         cudaFree(drk);
         cudaFree(b.dcases);
         if (hsc) cudaFreeHost(hsc);
@@ -331,12 +368,18 @@ struct Impl : ImplBase {
         CK(cudaMalloc(&dpart, sizeof(double) * NSLOT * (size_t)tiles));
         CK(cudaMalloc(&dcnt, sizeof(unsigned) * n));
         CK(cudaMemsetAsync(dcnt, 0, sizeof(unsigned) * n, st));
-        CK(cudaMalloc(&dact, sizeof(int) * 2 * act_stride(n, nlev)));
-        CK(cudaMemsetAsync(dact, 0, sizeof(int) * 2 * act_stride(n, nlev), st));
+        // tables 0 and 1: the CG iteration; table 2: single-kernel profiling
+        CK(cudaMalloc(&dact, sizeof(int) * 3 * act_stride(n, nlev)));
+        CK(cudaMemsetAsync(dact, 0, sizeof(int) * 3 * act_stride(n, nlev), st));
         CK(cudaMalloc(&dactdone, sizeof(unsigned)));
         CK(cudaMemsetAsync(dactdone, 0, sizeof(unsigned), st));
         b.act = dact;
         b.act_done = dactdone;
+        if (sizeof(T) != sizeof(double)) {
+            for (int c = 0; c < n; ++c)
+                stage_elems = std::max(stage_elems, (size_t)(P[c].nx + 3) * (P[c].ny + 3) * (P[c].nz + 3));
+            CK(cudaMalloc(&dstage, stage_elems * sizeof(double)));
+        }
         CK(cudaMallocHost(&hsc, sizeof(double) * S_NSCAL * n));
         double rk[9] = {1., 3. / 4., 1. / 3., 0., 1. / 4., 2. / 3., 1., 1. / 4., 2. / 3.};
         CK(cudaMalloc(&drk, sizeof(rk)));
@@ -403,6 +446,38 @@ struct Impl : ImplBase {
     int sync() override
     {
         CK(cudaStreamSynchronize(st));
+        return SULI_OK;
+    }
+
+    // one kernel alone over every case, `reps` launches between two events on
+    // the library's stream (after two untimed launches)
+    int time_kernel(int kernel, int reps, double *ms, double *bytes) override
+    {
+        if (reps < 1) return fail(SULI_BAD_ARG, "reps must be >= 1");
+        if (kernel == 1 && b.nlev < 2) return fail(SULI_BAD_ARG, "kernel 1 needs the multigrid mixed form");
+        if (launch_profile_kernel<T>(b, kernel, 1, st) != 0) return fail(SULI_BAD_ARG, "unknown kernel id");
+        launch_profile_kernel<T>(b, kernel, 0, st);
+        cudaEvent_t e0, e1;
+        CK(cudaEventCreate(&e0));
+        CK(cudaEventCreate(&e1));
+        CK(cudaEventRecord(e0, st));
+        for (int r = 0; r < reps; ++r) launch_profile_kernel<T>(b, kernel, 0, st);
+        CK(cudaEventRecord(e1, st));
+        CK(cudaEventSynchronize(e1));
+        float t = 0.f;
+        CK(cudaEventElapsedTime(&t, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        CKL();
+        double cells = 0.0;
+        for (int c = 0; c < ncases; ++c) cells += (double)P[c].nx * P[c].ny * P[c].nz;
+        // algorithmic bytes per cell: A reads p and the three scaled
+        // coefficients and writes mp (5 arrays); a red half-sweep streams z, f,
+        // dg and the three conductances (shared cache lines: both colours) and
+        // writes half of z (6.5); C reads r and p and writes p (3)
+        const double per[3] = {5.0, 6.5, 3.0};
+        *ms = (double)t / reps;
+        *bytes = cells * per[kernel] * (double)sizeof(T);
         return SULI_OK;
     }
     void *stream() override { return (void *)st; }
@@ -492,22 +567,36 @@ struct Impl : ImplBase {
         size_t n = e0 * e1 * e2;
         const bool isint = is_int_field(f);
         const size_t es = isint ? sizeof(int) : sizeof(T);
-        // staging buffer in the device element type (FP32 fields convert)
-        std::vector<char> stage;
-        void *hp = host;
-        if (!isint && sizeof(T) != sizeof(double)) {
-            stage.resize(n * sizeof(T));
-            hp = stage.data();
-            if (up) {
-                const double *src = (const double *)host;
-                T *dst = (T *)hp;
-                for (size_t q = 0; q < n; ++q) dst[q] = (T)src[q];
-            }
-        }
-        cudaMemcpy3DParms m;
-        std::memset(&m, 0, sizeof(m));
         size_t dpitch_el = is_plane_field(f) ? (size_t)(g.ny + 3) : (size_t)g.sx;
         size_t dheight = is_plane_field(f) ? (size_t)(g.nz + 3) : (size_t)(g.ny + 3);
+        if (!isint && sizeof(T) != sizeof(double)) {
+            // FP64 host block <-> FP32 box, converted on the GPU
+            if (n > stage_elems) return fail(SULI_BAD_ARG, "field larger than the transfer staging buffer");
+            const int nb = (int)std::min<size_t>((n + 255) / 256, 4096);
+            if (up) {
+                CK(cudaMemcpyAsync(dstage, host, n * sizeof(double), cudaMemcpyHostToDevice, st));
+                k_unpack_field<T><<<nb, 256, 0, st>>>(dstage, (T *)dev, (long long)n, (int)e0, (int)e1, lo[0], lo[1],
+                                                      lo[2], (long long)dpitch_el, (long long)dheight);
+                CKL();
+                // the caller may reuse its buffer once the call returns
+                CK(cudaStreamSynchronize(st));
+                if (f == SULI_F_PRD1) {
+                    // a pressure from the host replaces the FP64 pressure of the last solve
+                    int rc2 = write_case_scalar(icase, S_P64OK, 0.0);
+                    if (rc2) return rc2;
+                }
+            } else {
+                k_pack_field<T><<<nb, 256, 0, st>>>((const T *)dev, dstage, (long long)n, (int)e0, (int)e1, lo[0],
+                                                    lo[1], lo[2], (long long)dpitch_el, (long long)dheight);
+                CKL();
+                CK(cudaMemcpyAsync(host, dstage, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+                CK(cudaStreamSynchronize(st));
+            }
+            return SULI_OK;
+        }
+        void *hp = host;
+        cudaMemcpy3DParms m;
+        std::memset(&m, 0, sizeof(m));
         cudaPitchedPtr hpp = make_cudaPitchedPtr(hp, e0 * es, e0, e1);
         cudaPitchedPtr dpp = make_cudaPitchedPtr(dev, dpitch_el * es, dpitch_el, dheight);
         cudaPos pos = make_cudaPos((size_t)lo[0] * es, (size_t)lo[1], (size_t)lo[2]);
@@ -523,18 +612,8 @@ struct Impl : ImplBase {
             m.dstPtr = hpp;
             m.kind = cudaMemcpyDeviceToHost;
         }
+        CK(cudaMemcpy3DAsync(&m, st));
         CK(cudaStreamSynchronize(st));
-        CK(cudaMemcpy3D(&m));
-        if (up && f == SULI_F_PRD1 && sizeof(T) == 4) {
-            // a pressure from the host replaces the FP64 pressure of the last solve
-            int rc2 = write_case_scalar(icase, S_P64OK, 0.0);
-            if (rc2) return rc2;
-        }
-        if (!up && !isint && sizeof(T) != sizeof(double)) {
-            const T *src = (const T *)hp;
-            double *dst = (double *)host;
-            for (size_t q = 0; q < n; ++q) dst[q] = (double)src[q];
-        }
         return SULI_OK;
     }
 
@@ -1035,6 +1114,14 @@ extern "C" int suli_profile_read(suli_handle *h, suli_profile_t *out)
     // C reads r, p and writes p -- 14 arrays of the storage type
     out->cg_bytes_per_cell_iter = 14.0 * (im->P[0].precision == SULI_PREC_FP64 ? 8.0 : 4.0);
     return SULI_OK;
+}
+
+extern "C" int suli_time_kernel(suli_handle *h, int kernel, int reps, double *ms_per_launch,
+                                double *bytes_per_launch)
+{
+    HCHK();
+    if (!ms_per_launch || !bytes_per_launch) return fail(SULI_BAD_ARG, "null pointer");
+    return h->impl->time_kernel(kernel, reps, ms_per_launch, bytes_per_launch);
 }
 
 extern "C" int suli_last_error(char *buf, size_t len)

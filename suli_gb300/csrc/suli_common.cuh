@@ -54,6 +54,7 @@ enum Scal {
     S_RRPREV,      // mixed form: r.r before the pending update
     S_RZ,          // mixed form, multigrid-preconditioned passes: r.z
     S_P64OK,       // mixed form: r64 holds the FP64 pressure of the last solve
+    S_PASS0,       // mixed form: CG iteration count at the start of the pass
     S_NSCAL
 };
 
@@ -278,6 +279,44 @@ __device__ __forceinline__ void tile_ijk_of(const CaseDev<T> &c, int lt, int &i,
     tile_cell(c.ntx, c.nty, lt, i, j, k);
 }
 
+// The cells of this thread in U consecutive tiles of a unit, so a kernel can
+// issue the loads of several cells before it uses any (memory parallelism):
+// the walk decodes the unit's first tile once and then steps x-tile, y-tile,
+// z-tile without divisions.  Cells outside the grid (tile padding, tiles past
+// the unit) come back clamped to the nearest interior cell with v = false, so
+// loads at them stay in bounds and can be issued without a branch.
+struct TileWalk {
+    int ti, tj, tk, ntx, nty;
+    __device__ __forceinline__ TileWalk(int t0, int ntx_, int nty_) : ntx(ntx_), nty(nty_)
+    {
+        ti = t0 % ntx;
+        int r = t0 / ntx;
+        tj = r % nty;
+        tk = r / nty;
+    }
+    template <int U>
+    __device__ __forceinline__ void next(int lt, int t1, const Geo &g, long long (&q)[U], int (&ci)[U],
+                                         int (&cj)[U], int (&ck)[U], bool (&v)[U])
+    {
+#pragma unroll
+        for (int a = 0; a < U; ++a) {
+            const int i = 1 + ti * TX + (int)threadIdx.x;
+            const int j = 1 + tj * TY + (int)threadIdx.y;
+            const int k = 1 + tk * TZ + (int)threadIdx.z;
+            v[a] = (lt + a < t1) && i <= g.nx && j <= g.ny && k <= g.nz;
+            ci[a] = min(i, g.nx);
+            cj[a] = min(j, g.ny);
+            ck[a] = min(k, g.nz);
+            q[a] = g.at(ci[a], cj[a], ck[a]);
+            if (++ti == ntx) {
+                ti = 0;
+                if (++tj == nty) { tj = 0; ++tk; }
+            }
+        }
+    }
+};
+constexpr int UW = 2;   // cells per thread per step of the walk
+
 // tiles [t0, t1) of unit u of a case at table level s
 template <typename T>
 __device__ __forceinline__ void unit_tiles(const CaseDev<T> &c, int s, int u, int &t0, int &t1)
@@ -349,10 +388,11 @@ __device__ __forceinline__ int block_exscan(int v, int *total)
 }
 
 // Build table `out` (NL levels) from the cases listed in `in` (or all N
-// cases when in is null) whose S_CGACTIVE flag is set, keeping their order.
-// One block; every thread calls it.
+// cases when in is null) whose S_CGACTIVE flag is set (every case when
+// `all`), keeping their order.  One block; every thread calls it.
 template <typename T>
-__device__ void build_active_table(const CaseDev<T> *__restrict__ cs, int N, int NL, const int *in, int *out)
+__device__ void build_active_table(const CaseDev<T> *__restrict__ cs, int N, int NL, const int *in, int *out,
+                                   bool all = false)
 {
     const int nin = in ? in[0] : N;
     const int t = tid_lin();
@@ -361,7 +401,7 @@ __device__ void build_active_table(const CaseDev<T> *__restrict__ cs, int N, int
     int cnt = 0;
     for (int a = a0; a < a1; ++a) {
         const int id = in ? in[1 + a] : a;
-        if (__ldcg(&cs[id].sc[S_CGACTIVE]) != 0.0) ++cnt;
+        if (all || __ldcg(&cs[id].sc[S_CGACTIVE]) != 0.0) ++cnt;
     }
     int ncnt;
     const int pos0 = block_exscan(cnt, &ncnt);
@@ -369,7 +409,7 @@ __device__ void build_active_table(const CaseDev<T> *__restrict__ cs, int N, int
         int til = 0;
         for (int a = a0; a < a1; ++a) {
             const int id = in ? in[1 + a] : a;
-            if (__ldcg(&cs[id].sc[S_CGACTIVE]) != 0.0) til += (s == 0) ? cs[id].nchunks : cs[id].mg[s].ntiles;
+            if (all || __ldcg(&cs[id].sc[S_CGACTIVE]) != 0.0) til += (s == 0) ? cs[id].nchunks : cs[id].mg[s].ntiles;
         }
         int ntil;
         int tpos = block_exscan(til, &ntil);
@@ -377,7 +417,7 @@ __device__ void build_active_table(const CaseDev<T> *__restrict__ cs, int N, int
         int pos = pos0;
         for (int a = a0; a < a1; ++a) {
             const int id = in ? in[1 + a] : a;
-            if (__ldcg(&cs[id].sc[S_CGACTIVE]) != 0.0) {
+            if (all || __ldcg(&cs[id].sc[S_CGACTIVE]) != 0.0) {
                 if (s == 0) out[1 + pos] = id;
                 lv[1 + pos] = tpos;
                 ++pos;

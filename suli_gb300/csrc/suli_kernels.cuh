@@ -63,6 +63,11 @@ template <typename T> int launch_cg_iters(const Batch<T> &b, int n, int slot, in
 template <typename T> void launch_pcg_start(const Batch<T> &b, int slot, cudaStream_t s);
 template <typename T> int launch_pcg_iters(const Batch<T> &b, int n, int slot, cudaStream_t s);
 
+// profiling: one launch of kernel `kernel` over every case (table slot 2;
+// prepare != 0 builds that table first); returns -1 for an unknown kernel
+template <typename T> int launch_profile_kernel(const Batch<T> &b, int kernel, int prepare, cudaStream_t s);
+template <typename T> int launch_mg_smooth0(const Batch<T> &b, const int *tab, int grid, cudaStream_t s);
+
 // multigrid (k_mg.cu): coarse operators from level 0, one V-cycle over a table
 template <typename T> void launch_mg_coarsen(const Batch<T> &b, cudaStream_t s);
 template <typename T> void launch_mg_vcycle(const Batch<T> &b, const int *tab, int grid, cudaStream_t s);

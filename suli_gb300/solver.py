@@ -28,7 +28,7 @@ EXPORTS = [
     "suli_convdiff", "suli_complementos", "suli_tempo", "suli_graddin", "suli_posdin", "suli_conmassa",
     "suli_mms_error", "suli_set_stage", "suli_step", "suli_diagnostics", "suli_synchronize",
     "suli_last_error", "suli_device_info", "suli_get_stream", "suli_profile", "suli_profile_read",
-    "suli_ibm_setup", "suli_conmassa_noalloc",
+    "suli_ibm_setup", "suli_conmassa_noalloc", "suli_time_kernel",
 ]
 
 
@@ -82,6 +82,7 @@ def load_library(path: str = LIB_PATH):
     L.suli_get_stream.argtypes = [C.c_void_p, P(C.c_void_p)]
     L.suli_profile.argtypes = [C.c_void_p, C.c_int]
     L.suli_profile_read.argtypes = [C.c_void_p, P(SuliProfile)]
+    L.suli_time_kernel.argtypes = [C.c_void_p, C.c_int, C.c_int, P(C.c_double), P(C.c_double)]
     L.suli_conmassa_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, i32, i32, i32, C.c_double,
                                         C.c_double, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]
     _lib = L
@@ -235,6 +236,14 @@ class SuliGPU:
         out = SuliProfile()
         _check(load_library().suli_profile_read(self._h, C.byref(out)))
         return out
+
+    def time_kernel(self, kernel: int, reps: int = 20):
+        """(ms per launch, algorithmic bytes per launch) of one kernel timed
+        alone over every case: 0 CG matrix-vector product, 1 multigrid
+        smoother half-sweep on the case grid, 2 CG direction update."""
+        ms, by = C.c_double(), C.c_double()
+        _check(load_library().suli_time_kernel(self._h, kernel, reps, C.byref(ms), C.byref(by)))
+        return ms.value, by.value
 
     def diag(self, case: int = 0) -> SuliDiag:
         d = SuliDiag()

@@ -20,7 +20,10 @@ TOL = 1e-10
 def _configs():
     return [
         ("dam_break", cases.dam_break(24, 12, 12)),
-        ("wave_les", cases.wave_tank(32, 8, 12, dt=5e-4, cg_tol=1e-10)),
+        # the velocity of a tank near rest is the small difference between the
+        # gravity increment and the hydrostatic gradient, which amplifies the
+        # CG's stopping error: solve to 1e-12 so it stays below the 1e-10 bar
+        ("wave_les", cases.wave_tank(32, 8, 12, dt=5e-4, cg_tol=1e-12)),
         ("mms_periodic", cases.mms_case(16)),
         ("channel_ibm", cases.open_channel(48, 16, 16, dt=2e-3, radius=0.25, cg_tol=1e-10, periodic=True)),
         ("inflow_ibm", cases.open_channel(48, 16, 16, dt=2e-3, radius=0.25, cg_tol=1e-10)),
