@@ -115,8 +115,12 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_setup2(const CaseDev<T> *__rest
     c.qpr[q] = c.qpr[q] / sD;
 }
 
-// Mixed form: the operator in FP64 from rho64 (setup1m), then its scaling
-// (setup2m) in FP64; the FP32 iteration uses the rounded scaled coefficients.
+// Mixed form: the operator in FP64 from rho64.  setup1m forms each face
+// conductance once (the cell's low faces, and the high faces on the last
+// cell of a line) and the right-hand side; setup1mb sums the diagonal, keeps
+// 1/sqrt(D) in r64 (free until the solve's end) and writes the multigrid's
+// level 0; setup2m scales by products of 1/sqrt(D).  The FP32 iteration uses
+// the rounded scaled coefficients.
 template <typename T>
 __global__ void __launch_bounds__(NTHREADS) k_cg_setup1m(const CaseDev<T> *__restrict__ cs, int ncases)
 {
@@ -126,41 +130,18 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_setup1m(const CaseDev<T> *__res
     const Geo &g = c.g;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     if (i > nx || j > ny || k > nz) return;
+    if (i == 1 && j == 1 && k == 1) c.sc[S_P64OK] = 0.0;   // r64 is reused below
     const bool px = (c.ccx0 == 0);
     const double dt = c.sc[S_DT];
     const double aux1 = dt / (c.dx * c.dx), aux2 = dt / (c.dy * c.dy), aux3 = dt / (c.dz * c.dz);
     const double *rho = c.rho64;
-    double si0 = aux1 / icf<double>(i, nx, px, [&](int m) { return AT(rho, m, j, k); });
-    double si1 = aux1 / icf<double>(i + 1, nx, px, [&](int m) { return AT(rho, m, j, k); });
-    double sj0 = aux2 / icf<double>(j, ny, false, [&](int m) { return AT(rho, i, m, k); });
-    double sj1 = aux2 / icf<double>(j + 1, ny, false, [&](int m) { return AT(rho, i, m, k); });
-    double sk0 = aux3 / icf<double>(k, nz, false, [&](int m) { return AT(rho, i, j, m); });
-    double sk1 = aux3 / icf<double>(k + 1, nz, false, [&](int m) { return AT(rho, i, j, m); });
-    long long q = g.at(i, j, k);
-    c.spi64[q] = si0;
-    c.spj64[q] = sj0;
-    c.spk64[q] = sk0;
-    if (i == nx) c.spi64[q + 1] = si1;
-    if (j == ny) c.spj64[q + g.sx] = sj1;
-    if (k == nz) c.spk64[q + g.sxy] = sk1;
-    c.dpr64[q] = si1 + si0 + sj1 + sj0 + sk1 + sk0;
-    if (c.nlev > 0) {
-        // level 0 of the multigrid preconditioner: the unscaled face
-        // conductances, zero on Neumann walls (the wall's ghost copy cancels
-        // the face), the wrap face kept on periodic x/y
-        const bool py = (c.ccy0 == 0);
-        const MgLev<T> &L = c.mg[0];
-        const T x0 = (i == 1 && !px) ? T(0) : T(si0), x1 = (i == nx && !px) ? T(0) : T(si1);
-        const T y0 = (j == 1 && !py) ? T(0) : T(sj0), y1 = (j == ny && !py) ? T(0) : T(sj1);
-        const T z0 = (k == 1) ? T(0) : T(sk0), z1 = (k == nz) ? T(0) : T(sk1);
-        L.cx[q] = x0;
-        L.cy[q] = y0;
-        L.cz[q] = z0;
-        if (i == nx) L.cx[q + 1] = x1;
-        if (j == ny) L.cy[q + g.sx] = y1;
-        if (k == nz) L.cz[q + g.sxy] = z1;
-        L.dg[q] = x0 + x1 + y0 + y1 + z0 + z1;
-    }
+    const long long q = g.at(i, j, k);
+    c.spi64[q] = aux1 / icf<double>(i, nx, px, [&](int m) { return AT(rho, m, j, k); });
+    c.spj64[q] = aux2 / icf<double>(j, ny, false, [&](int m) { return AT(rho, i, m, k); });
+    c.spk64[q] = aux3 / icf<double>(k, nz, false, [&](int m) { return AT(rho, i, j, m); });
+    if (i == nx) c.spi64[q + 1] = aux1 / icf<double>(nx + 1, nx, px, [&](int m) { return AT(rho, m, j, k); });
+    if (j == ny) c.spj64[q + g.sx] = aux2 / icf<double>(ny + 1, ny, false, [&](int m) { return AT(rho, i, m, k); });
+    if (k == nz) c.spk64[q + g.sxy] = aux3 / icf<double>(nz + 1, nz, false, [&](int m) { return AT(rho, i, j, m); });
     double ua = c.u[q], ub = c.u[q + 1], va = c.v[q], vb = c.v[q + g.sx], wa = c.w[q], wb = c.w[q + g.sxy];
     if (c.obst_t != 0 && c.ibm_t == 2) {
         if (c.obs_lsx[q] >= T(0.)) ua = 0.;
@@ -174,6 +155,41 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_setup1m(const CaseDev<T> *__res
 }
 
 template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_cg_setup1mb(const CaseDev<T> *__restrict__ cs, int ncases)
+{
+    const CaseDev<T> &c = cs[find_case(cs, ncases)];
+    int i, j, k;
+    tile_ijk(c, i, j, k);
+    const Geo &g = c.g;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    if (i > nx || j > ny || k > nz) return;
+    const long long q = g.at(i, j, k);
+    const double si0 = c.spi64[q], si1 = c.spi64[q + 1], sj0 = c.spj64[q], sj1 = c.spj64[q + g.sx];
+    const double sk0 = c.spk64[q], sk1 = c.spk64[q + g.sxy];
+    const double D = si1 + si0 + sj1 + sj0 + sk1 + sk0;
+    c.dpr64[q] = D;
+    c.dpr[q] = T(D);
+    c.r64[q] = 1.0 / sqrt(D);
+    if (c.nlev > 0) {
+        // level 0 of the multigrid preconditioner: the unscaled face
+        // conductances, zero on Neumann walls (the wall's ghost copy cancels
+        // the face), the wrap face kept on periodic x/y
+        const bool px = (c.ccx0 == 0), py = (c.ccy0 == 0);
+        const MgLev<T> &L = c.mg[0];
+        const T x0 = (i == 1 && !px) ? T(0) : T(si0), x1 = (i == nx && !px) ? T(0) : T(si1);
+        const T y0 = (j == 1 && !py) ? T(0) : T(sj0), y1 = (j == ny && !py) ? T(0) : T(sj1);
+        const T z0 = (k == 1) ? T(0) : T(sk0), z1 = (k == nz) ? T(0) : T(sk1);
+        L.cx[q] = x0;
+        L.cy[q] = y0;
+        L.cz[q] = z0;
+        if (i == nx) L.cx[q + 1] = x1;
+        if (j == ny) L.cy[q + g.sx] = y1;
+        if (k == nz) L.cz[q + g.sxy] = z1;
+        L.dg[q] = x0 + x1 + y0 + y1 + z0 + z1;
+    }
+}
+
+template <typename T>
 __global__ void __launch_bounds__(NTHREADS) k_cg_setup2m(const CaseDev<T> *__restrict__ cs, int ncases)
 {
     const CaseDev<T> &c = cs[find_case(cs, ncases)];
@@ -183,32 +199,30 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_setup2m(const CaseDev<T> *__res
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     if (i > nx || j > ny || k > nz) return;
     const bool px = (c.ccx0 == 0), py = (c.ccy0 == 0);
-    const double *D = c.dpr64;
-    long long q = g.at(i, j, k);
-    double Dc = D[q];
-    double a = c.spi64[q] / sqrt(Dc * AT(D, bmap(i - 1, nx, px), j, k));
-    double b = c.spj64[q] / sqrt(Dc * AT(D, i, bmap(j - 1, ny, py), k));
-    double d = c.spk64[q] / sqrt(Dc * AT(D, i, j, bmap(k - 1, nz, false)));
+    const double *R = c.r64;      // 1/sqrt(D)
+    const long long q = g.at(i, j, k);
+    const double rc = R[q];
+    const double a = c.spi64[q] * (rc * AT(R, bmap(i - 1, nx, px), j, k));
+    const double b = c.spj64[q] * (rc * AT(R, i, bmap(j - 1, ny, py), k));
+    const double d = c.spk64[q] * (rc * AT(R, i, j, bmap(k - 1, nz, false)));
     c.spi64[q] = a; c.spi[q] = T(a);
     c.spj64[q] = b; c.spj[q] = T(b);
     c.spk64[q] = d; c.spk[q] = T(d);
     if (i == nx) {
-        double x = c.spi64[q + 1] / sqrt(AT(D, bmap(nx + 1, nx, px), j, k) * Dc);
+        double x = c.spi64[q + 1] * (AT(R, bmap(nx + 1, nx, px), j, k) * rc);
         c.spi64[q + 1] = x; c.spi[q + 1] = T(x);
     }
     if (j == ny) {
-        double x = c.spj64[q + g.sx] / sqrt(AT(D, i, bmap(ny + 1, ny, py), k) * Dc);
+        double x = c.spj64[q + g.sx] * (AT(R, i, bmap(ny + 1, ny, py), k) * rc);
         c.spj64[q + g.sx] = x; c.spj[q + g.sx] = T(x);
     }
     if (k == nz) {
-        double x = c.spk64[q + g.sxy] / sqrt(AT(D, i, j, bmap(nz + 1, nz, false)) * Dc);
+        double x = c.spk64[q + g.sxy] * (AT(R, i, j, bmap(nz + 1, nz, false)) * rc);
         c.spk64[q + g.sxy] = x; c.spk[q + g.sxy] = T(x);
     }
-    double sD = sqrt(Dc);
-    c.dpr[q] = T(Dc);
-    c.qpr64[q] = c.qpr64[q] / sD;
+    c.qpr64[q] = c.qpr64[q] * rc;
     c.qpr[q] = T(c.qpr64[q]);
-    c.e64[q] = (double)c.prd1[q] * sD;
+    c.e64[q] = (double)c.prd1[q] * (c.dpr64[q] * rc);   // prd1 sqrt(D)
 }
 
 // e at a possibly-ghost neighbour: matepr(ghost) = prd1(ghost) * sqrt(matdpr(mapped))
@@ -761,6 +775,7 @@ template <typename T> void launch_cg_finish(const Batch<T> &b, cudaStream_t s)
 template <typename T> void launch_cg_refine_setup(const Batch<T> &b, cudaStream_t s)
 {
     k_cg_setup1m<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
+    k_cg_setup1mb<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
     k_cg_setup2m<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
     k_cg_true_residual<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, 1); count_launch();
 }
