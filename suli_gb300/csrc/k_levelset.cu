@@ -169,6 +169,15 @@ __device__ __forceinline__ void stage_bufs(const CaseDev<T> &c, T *base, int sta
     else { src = c.lsc; dst = base; }
 }
 
+// the FP64 masters of the same rotation (mixed form, target 0)
+template <typename T>
+__device__ __forceinline__ void stage_bufs64(const CaseDev<T> &c, int stage, const double *&src, double *&dst)
+{
+    if (stage == 1) { src = c.ls64; dst = c.lsb64; }
+    else if (stage == 2) { src = c.lsb64; dst = c.lsc64; }
+    else { src = c.lsc64; dst = c.ls64; }
+}
+
 // conv_weno + intt_ls (14_level_set.f90:277-334), one TVD-RK3 stage
 template <typename T>
 __global__ void __launch_bounds__(NTHREADS) k_ls_adv_stage(const CaseDev<T> *__restrict__ cs, int ncases, int stage,
@@ -192,6 +201,16 @@ __global__ void __launch_bounds__(NTHREADS) k_ls_adv_stage(const CaseDev<T> *__r
     T bpos = va > T(0.) ? va : T(0.), bneg = va < T(0.) ? va : T(0.);
     T cpos = wa > T(0.) ? wa : T(0.), cneg = wa < T(0.) ? wa : T(0.);
     T sy7 = -(apos * td + aneg * ta + bpos * te + bneg * tb + cpos * tf + cneg * tc);
+    if (c.ls64 != nullptr) {   // mixed form: the stage combination on the FP64 masters
+        const double *s64;
+        double *d64;
+        stage_bufs64(c, stage, s64, d64);
+        const double nv = rk[stage - 1] * c.ls64[q] + rk[3 + stage - 1] * s64[q] +
+                          rk[6 + stage - 1] * c.sc[S_DTADV] * (double)sy7;
+        d64[q] = nv;
+        dst[q] = T(nv);
+        return;
+    }
     T ta1 = c.ls[q];          // ls0 (stage 1: the current value)
     T gx = src[q];
     T dt1 = T(c.sc[S_DTADV]);
@@ -249,13 +268,27 @@ __global__ void __launch_bounds__(NTHREADS) k_reinit_stage(const CaseDev<T> *__r
         T lv = src[q];
         T mod = godunov<T>(lv, ta, tb, tc, td, te, tf);
         T sy7 = c.funcs[q] * (T(1.) - mod);
-        T ta1 = base[q];
-        T a = T(rk[stage - 1]), b = T(rk[3 + stage - 1]), gg = T(rk[6 + stage - 1]);
-        T nv = a * ta1 + b * lv + gg * T(c.dt1) * sy7;
-        dst[q] = nv;
+        double nv64, lv64;
+        if (target == 0 && c.ls64 != nullptr) {
+            // mixed form: the stage combination on the FP64 masters
+            const double *s64;
+            double *d64;
+            stage_bufs64(c, stage, s64, d64);
+            lv64 = s64[q];
+            nv64 = rk[stage - 1] * c.ls64[q] + rk[3 + stage - 1] * lv64 + rk[6 + stage - 1] * c.dt1 * (double)sy7;
+            d64[q] = nv64;
+            dst[q] = T(nv64);
+        } else {
+            T ta1 = base[q];
+            T a = T(rk[stage - 1]), b = T(rk[3 + stage - 1]), gg = T(rk[6 + stage - 1]);
+            T nv = a * ta1 + b * lv + gg * T(c.dt1) * sy7;
+            dst[q] = nv;
+            nv64 = (double)nv;
+            lv64 = (double)lv;
+        }
         if (stage == 3) {
-            if (fabs((double)nv) <= 2. * c.alpha1 * c.dx1) {
-                band = (double)nv - (double)lv;
+            if (fabs(nv64) <= 2. * c.alpha1 * c.dx1) {
+                band = nv64 - lv64;
                 cnt = 1.0;
             }
         }
@@ -290,6 +323,7 @@ __global__ void __launch_bounds__(NTHREADS) k_heaviside_vol(const CaseDev<T> *__
     if (i <= g.nx && j <= g.ny && k <= g.nz) {
         long long q = g.at(i, j, k);
         T l = c.ls[q];
+        const double lm = c.ls64 ? c.ls64[q] : (double)l;   // FP64 master in the mixed form
         T ad = T(c.alpha1 * c.dx1);
         T h;
         if (l < -ad) h = T(0.);
@@ -297,16 +331,19 @@ __global__ void __launch_bounds__(NTHREADS) k_heaviside_vol(const CaseDev<T> *__
         else h = T(0.5) * (T(1.) + l / ad + T(1. / c.pi) * sin(T(c.pi) * l / ad));
         c.hs[q] = h;
         c.rho[q] = T(c.rho_f1) * (T(1.) - h) + T(c.rho_f2) * h;
+        double hv = (double)h;
         if (c.rho64) {
-            // FP64 density for the refinement operator of the mixed form
-            double l64 = (double)l, ad64 = c.alpha1 * c.dx1, h64;
+            // mixed form: Heaviside of the FP64 level-set master in FP64, for
+            // the density of the FP64 pressure operator and the volume integral
+            double l64 = lm, ad64 = c.alpha1 * c.dx1, h64;
             if (l64 < -ad64) h64 = 0.;
             else if (l64 > ad64) h64 = 1.;
             else h64 = 0.5 * (1. + l64 / ad64 + 1. / c.pi * sin(c.pi * l64 / ad64));
             c.rho64[q] = c.rho_f1 * (1. - h64) + c.rho_f2 * h64;
+            hv = h64;
         }
         c.ls_mu[q] = T(c.mu_f1) * (T(1.) - h) + T(c.mu_f2) * h;
-        vol = (1. - (1. - (double)h)) * c.dx * c.dy * c.dz;
+        vol = (1. - (1. - hv)) * c.dx * c.dy * c.dz;
     }
     if (set_ini < 0) return;     // properties only (heaviside after the level-set IBM)
     double vals[1] = {vol}, tot[1];
@@ -338,6 +375,12 @@ __global__ void __launch_bounds__(NTHREADS) k_volcorr(const CaseDev<T> *__restri
     if (!(fabs(tc) > fabs(tf))) tc = tf;
     T m = sqrt(ta * ta + tb * tb + tc * tc);
     double vi = c.sc[S_VOLINS], v0 = c.sc[S_VOLINI];
+    if (c.ls64 != nullptr) {
+        const double x = c.ls64[q] - c.dt1 * (vi - v0) * (double)m / v0;
+        c.lsb64[q] = x;
+        c.lsb[q] = T(x);
+        return;
+    }
     c.lsb[q] = c.ls[q] - T(c.dt1) * T(vi - v0) * m / T(v0);
 }
 
@@ -352,6 +395,7 @@ __global__ void __launch_bounds__(NTHREADS) k_volcorr_copy(const CaseDev<T> *__r
     if (i > g.nx || j > g.ny || k > g.nz) return;
     long long q = g.at(i, j, k);
     c.ls[q] = c.lsb[q];
+    if (c.ls64 != nullptr) c.ls64[q] = c.lsb64[q];
 }
 
 // ---- host launchers -------------------------------------------------------

@@ -274,6 +274,43 @@ __device__ __forceinline__ void tempo_one(const CaseDev<T> &c, int tt, int it, T
     }
 }
 
+// the same update on the FP64 masters of the mixed form (u = master, u0 =
+// its stage copy; F, f0, f1 stay FP32); the FP32 copies follow the masters
+template <typename T>
+__device__ __forceinline__ void tempo_one_m(const CaseDev<T> &c, int tt, int it, double dt, long long q, T *u,
+                                            double *um, const T *F, T *u0, double *u0m, T *f0, T *f1)
+{
+    const int tte = c.t_tempo;
+    const double Fv = (double)F[q];
+    double x = um[q];
+    if ((tte == 0) || ((tte == 3) || ((tte == 4) && (it == 1)))) {
+        x = x + dt * Fv;
+        if (tte == 3 || tte == 4) f0[q] = F[q];
+    } else if (tte == 1) {
+        if (tt == 1) { u0m[q] = x; u0[q] = T(x); x = x + dt * Fv; }
+        else if (tt == 2) { x = u0m[q] + dt * Fv; }
+    } else if (tte == 2) {
+        if (tt == 1) {
+            u0m[q] = x; u0[q] = T(x); f0[q] = F[q]; x = x + dt * Fv;
+        } else if (tt == 2) {
+            f1[q] = F[q];
+            x = u0m[q] - dt * (double)f0[q] + (2. * dt) * Fv;
+        } else if (tt == 3) {
+            x = u0m[q] + (dt / 6.) * ((double)f0[q] + 4. * (double)f1[q] + Fv);
+        }
+    } else if (((tte == 3) && (it != 1)) || ((tte == 4) && (it == 2))) {
+        x = x + dt * 0.5 * (3. * Fv - (double)f0[q]);
+        f0[q] = F[q];
+        if (tte == 4) f1[q] = f0[q];
+    } else if ((tte == 4) && (it >= 3)) {
+        x = x + (dt / 12.) * (23. * Fv - 16. * (double)f0[q] + 5. * (double)f1[q]);
+        f1[q] = f0[q];
+        f0[q] = F[q];
+    }
+    um[q] = x;
+    u[q] = T(x);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(NTHREADS) k_tempo(const CaseDev<T> *__restrict__ cs, int ncases, int tt, int it)
 {
@@ -282,11 +319,37 @@ __global__ void __launch_bounds__(NTHREADS) k_tempo(const CaseDev<T> *__restrict
     tile_ijk(c, i, j, k);
     const Geo &g = c.g;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
-    T dt = T(c.sc[S_DT]);
     long long q = g.at(i, j, k);
+    if (c.u64 != nullptr) {
+        const double dt = c.sc[S_DT];
+        if (i <= nx + 1 && j <= ny && k <= nz) tempo_one_m<T>(c, tt, it, dt, q, c.u, c.u64, c.Fu, c.u0, c.u064, c.fu0, c.fu1);
+        if (i <= nx && j <= ny + 1 && k <= nz) tempo_one_m<T>(c, tt, it, dt, q, c.v, c.v64, c.Fv, c.v0, c.v064, c.fv0, c.fv1);
+        if (i <= nx && j <= ny && k <= nz + 1) tempo_one_m<T>(c, tt, it, dt, q, c.w, c.w64, c.Fw, c.w0, c.w064, c.fw0, c.fw1);
+        return;
+    }
+    T dt = T(c.sc[S_DT]);
     if (i <= nx + 1 && j <= ny && k <= nz) tempo_one<T>(c, tt, it, dt, q, c.u, c.Fu, c.u0, c.fu0, c.fu1);
     if (i <= nx && j <= ny + 1 && k <= nz) tempo_one<T>(c, tt, it, dt, q, c.v, c.Fv, c.v0, c.fv0, c.fv1);
     if (i <= nx && j <= ny && k <= nz + 1) tempo_one<T>(c, tt, it, dt, q, c.w, c.Fw, c.w0, c.fw0, c.fw1);
+}
+
+// FP32 velocity and level-set values written outside the FP64 updates
+// (boundary fills, inflow, IBM images) -> FP64 masters: an element whose FP32
+// copy no longer equals its rounded master takes the FP32 value.  Grid: x
+// strides the case's box, y = case.
+template <typename T>
+__global__ void k_sync_masters(const CaseDev<T> *__restrict__ cs, int ncases)
+{
+    const CaseDev<T> &c = cs[blockIdx.y];
+    if (c.u64 == nullptr) return;
+    const long long n = c.g.total;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const T u = c.u[q], v = c.v[q], w = c.w[q], l = c.ls[q];
+        if (T(c.u64[q]) != u) c.u64[q] = (double)u;
+        if (T(c.v64[q]) != v) c.v64[q] = (double)v;
+        if (T(c.w64[q]) != w) c.w64[q] = (double)w;
+        if (T(c.ls64[q]) != l) c.ls64[q] = (double)l;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -316,6 +379,42 @@ __global__ void __launch_bounds__(NTHREADS) k_posdin(const CaseDev<T> *__restric
         auto mk = [&](int a) { return a < 1 ? 1 : (a > nz ? nz : a); };
         return T(c.r64[g.at(mi(i1), mj(j1), mk(k1))] - c.r64[g.at(mi(i0), mj(j0), mk(k0))]);
     };
+    if (c.u64 != nullptr) {
+        // mixed form: the whole correction in FP64 on the masters, with the
+        // density the FP64 pressure operator was built from (rho64), so the
+        // projection stays consistent with the solve
+        const double ddt = c.sc[S_DT];
+        const double *r64 = c.rho64;
+        auto dp64 = [&](int i1, int j1, int k1, int i0, int j0, int k0) -> double {
+            auto mi = [&](int a) { return a < 1 ? (px ? nx : 1) : (a > nx ? (px ? 1 : nx) : a); };
+            auto mj = [&](int a) { return a < 1 ? (py ? ny : 1) : (a > ny ? (py ? 1 : ny) : a); };
+            auto mk = [&](int a) { return a < 1 ? 1 : (a > nz ? nz : a); };
+            if (p64) return c.r64[g.at(mi(i1), mj(j1), mk(k1))] - c.r64[g.at(mi(i0), mj(j0), mk(k0))];
+            return (double)AT(p, i1, j1, k1) - (double)AT(p, i0, j0, k0);
+        };
+        if (i <= nx + 1 && j <= ny && k <= nz) {
+            const double rx = interp_cf<double>(i, nx, px, [&](int m) { return AT(r64, m, j, k); });
+            const long long q = g.at(i, j, k);
+            const double x = c.u64[q] - ddt / c.dx * dp64(i, j, k, i - 1, j, k) / rx;
+            c.u64[q] = x;
+            c.u[q] = T(x);
+        }
+        if (i <= nx && j <= ny + 1 && k <= nz) {
+            const double ry = interp_cf<double>(j, ny, false, [&](int m) { return AT(r64, i, m, k); });
+            const long long q = g.at(i, j, k);
+            const double x = c.v64[q] - ddt / c.dy * dp64(i, j, k, i, j - 1, k) / ry;
+            c.v64[q] = x;
+            c.v[q] = T(x);
+        }
+        if (i <= nx && j <= ny && k <= nz + 1) {
+            const double rz = interp_cf<double>(k, nz, false, [&](int m) { return AT(r64, i, j, m); });
+            const long long q = g.at(i, j, k);
+            const double x = c.w64[q] - ddt / c.dz * dp64(i, j, k, i, j, k - 1) / rz;
+            c.w64[q] = x;
+            c.w[q] = T(x);
+        }
+        return;
+    }
     if (i <= nx + 1 && j <= ny && k <= nz) {
         T rx = interp_cf<T>(i, nx, px, [&](int m) { return AT(rho, m, j, k); });
         AT(c.u, i, j, k) = AT(c.u, i, j, k) - aux1 * dp(i, j, k, i - 1, j, k) / rx;
@@ -340,10 +439,17 @@ __global__ void __launch_bounds__(NTHREADS) k_conmassa(const CaseDev<T> *__restr
     const Geo &g = c.g;
     double m = 0.0;
     if (i <= g.nx && j <= g.ny && k <= g.nz) {
-        const T *u = c.u, *v = c.v, *w = c.w;
-        double d = ((double)AT(u, i + 1, j, k) - (double)AT(u, i, j, k)) / c.dx +
-                   ((double)AT(v, i, j + 1, k) - (double)AT(v, i, j, k)) / c.dy +
-                   ((double)AT(w, i, j, k + 1) - (double)AT(w, i, j, k)) / c.dz;
+        double d;
+        if (c.u64 != nullptr) {   // mixed form: the FP64 masters
+            const double *u = c.u64, *v = c.v64, *w = c.w64;
+            d = (AT(u, i + 1, j, k) - AT(u, i, j, k)) / c.dx + (AT(v, i, j + 1, k) - AT(v, i, j, k)) / c.dy +
+                (AT(w, i, j, k + 1) - AT(w, i, j, k)) / c.dz;
+        } else {
+            const T *u = c.u, *v = c.v, *w = c.w;
+            d = ((double)AT(u, i + 1, j, k) - (double)AT(u, i, j, k)) / c.dx +
+                ((double)AT(v, i, j + 1, k) - (double)AT(v, i, j, k)) / c.dy +
+                ((double)AT(w, i, j, k + 1) - (double)AT(w, i, j, k)) / c.dz;
+        }
         AT(c.div, i, j, k) = T(d);
         m = fabs(d);
     }
@@ -429,6 +535,12 @@ template <typename T> void launch_tempo(const Batch<T> &b, int tt, int it, cudaS
 {
     k_tempo<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, tt, it); count_launch();
 }
+template <typename T> void launch_sync_masters(const Batch<T> &b, cudaStream_t s)
+{
+    k_sync_masters<T><<<dim3(64, b.ncases), 256, 0, s>>>(b.dcases, b.ncases);
+    count_launch();
+}
+
 template <typename T> void launch_posdin(const Batch<T> &b, cudaStream_t s)
 {
     k_posdin<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
@@ -452,6 +564,7 @@ template <typename T> void launch_set_scalar(const Batch<T> &b, int slot, double
     template void launch_complementos<T>(const Batch<T> &, cudaStream_t);   \
     template void launch_tempo<T>(const Batch<T> &, int, int, cudaStream_t);          \
     template void launch_posdin<T>(const Batch<T> &, cudaStream_t);         \
+    template void launch_sync_masters<T>(const Batch<T> &, cudaStream_t);   \
     template void launch_conmassa<T>(const Batch<T> &, cudaStream_t);       \
     template void launch_mms_error<T>(const Batch<T> &, cudaStream_t);      \
     template void launch_set_scalar<T>(const Batch<T> &, int, double, cudaStream_t);

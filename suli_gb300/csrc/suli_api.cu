@@ -297,7 +297,7 @@ struct Impl : ImplBase {
             T **ptf[] = {&cd.bxx0, &cd.bxx1, &cd.blx1};
             const bool mixed = (sizeof(T) == 4);
             const bool mg = mixed && q.mixed_precond == 1;
-            size_t bytes = fb * ntf + ib * 4 + pb * 3 + (mixed ? 8 * db : 0) + (mg ? 6 * fb : 0);
+            size_t bytes = fb * ntf + ib * 4 + pb * 3 + (mixed ? 17 * db : 0) + (mg ? 6 * fb : 0);
             void *slab = nullptr;
             CK(cudaMalloc(&slab, bytes));
             slabs.push_back(slab);
@@ -307,8 +307,10 @@ struct Impl : ImplBase {
             for (int f = 0; f < 4; ++f) { *itf[f] = (int *)cur; cur += ib; }
             for (int f = 0; f < 3; ++f) { *ptf[f] = (T *)cur; cur += pb; }
             if (mixed) {
-                double **d64[] = {&cd.e64, &cd.r64, &cd.rho64, &cd.spi64, &cd.spj64, &cd.spk64, &cd.dpr64, &cd.qpr64};
-                for (int f = 0; f < 8; ++f) { *d64[f] = (double *)cur; cur += db; }
+                double **d64[] = {&cd.e64, &cd.r64, &cd.rho64, &cd.spi64, &cd.spj64, &cd.spk64, &cd.dpr64, &cd.qpr64,
+                                  &cd.u64, &cd.v64, &cd.w64, &cd.u064, &cd.v064, &cd.w064,
+                                  &cd.ls64, &cd.lsb64, &cd.lsc64};
+                for (int f = 0; f < 17; ++f) { *d64[f] = (double *)cur; cur += db; }
             }
             if (mg) {
                 // multigrid level 0: the case grid, its box and its tiles
@@ -505,6 +507,22 @@ struct Impl : ImplBase {
     double cells(int c) const { return (double)P[c].nx * P[c].ny * P[c].nz; }
 
     // ---- field copies -------------------------------------------------------
+    // FP64 master of a field (mixed form velocities), else null
+    double *master_ptr(int icase, int f)
+    {
+        CaseDev<T> &c = hc[icase];
+        switch (f) {
+        case SULI_F_U: return c.u64;
+        case SULI_F_V: return c.v64;
+        case SULI_F_W: return c.w64;
+        case SULI_F_U0: return c.u064;
+        case SULI_F_V0: return c.v064;
+        case SULI_F_W0: return c.w064;
+        case SULI_F_LS: return c.ls64;
+        default: return nullptr;
+        }
+    }
+
     void *dev_ptr(int icase, int f)
     {
         CaseDev<T> &c = hc[icase];
@@ -570,13 +588,18 @@ struct Impl : ImplBase {
         size_t dpitch_el = is_plane_field(f) ? (size_t)(g.ny + 3) : (size_t)g.sx;
         size_t dheight = is_plane_field(f) ? (size_t)(g.nz + 3) : (size_t)(g.ny + 3);
         if (!isint && sizeof(T) != sizeof(double)) {
-            // FP64 host block <-> FP32 box, converted on the GPU
+            // FP64 host block <-> FP32 box, converted on the GPU; velocities
+            // also go to / come from their FP64 masters
             if (n > stage_elems) return fail(SULI_BAD_ARG, "field larger than the transfer staging buffer");
             const int nb = (int)std::min<size_t>((n + 255) / 256, 4096);
+            double *master = master_ptr(icase, f);
             if (up) {
                 CK(cudaMemcpyAsync(dstage, host, n * sizeof(double), cudaMemcpyHostToDevice, st));
                 k_unpack_field<T><<<nb, 256, 0, st>>>(dstage, (T *)dev, (long long)n, (int)e0, (int)e1, lo[0], lo[1],
                                                       lo[2], (long long)dpitch_el, (long long)dheight);
+                if (master)
+                    k_unpack_field<double><<<nb, 256, 0, st>>>(dstage, master, (long long)n, (int)e0, (int)e1, lo[0],
+                                                               lo[1], lo[2], (long long)dpitch_el, (long long)dheight);
                 CKL();
                 // the caller may reuse its buffer once the call returns
                 CK(cudaStreamSynchronize(st));
@@ -586,8 +609,12 @@ struct Impl : ImplBase {
                     if (rc2) return rc2;
                 }
             } else {
-                k_pack_field<T><<<nb, 256, 0, st>>>((const T *)dev, dstage, (long long)n, (int)e0, (int)e1, lo[0],
-                                                    lo[1], lo[2], (long long)dpitch_el, (long long)dheight);
+                if (master)
+                    k_pack_field<double><<<nb, 256, 0, st>>>(master, dstage, (long long)n, (int)e0, (int)e1, lo[0],
+                                                             lo[1], lo[2], (long long)dpitch_el, (long long)dheight);
+                else
+                    k_pack_field<T><<<nb, 256, 0, st>>>((const T *)dev, dstage, (long long)n, (int)e0, (int)e1, lo[0],
+                                                        lo[1], lo[2], (long long)dpitch_el, (long long)dheight);
                 CKL();
                 CK(cudaMemcpyAsync(host, dstage, n * sizeof(double), cudaMemcpyDeviceToHost, st));
                 CK(cudaStreamSynchronize(st));
@@ -673,6 +700,7 @@ struct Impl : ImplBase {
             int rc = setsc(S_RINREPLAY, -1.0);
             if (rc) return rc;
             launch_ibm_levelset<T>(b, st);
+            if (sizeof(T) == 4) launch_sync_masters<T>(b, st);   // image values -> FP64 level-set master
             launch_reinit<T>(b, P[0].reinit_max_iter, st, 0);
             launch_heaviside<T>(b, -1, st);
             CKL();
@@ -681,6 +709,9 @@ struct Impl : ImplBase {
         if (any_ibm()) launch_ibm_velocity<T>(b, st);     // 3_contorno.f90:85-90
         launch_contorno<T>(b, nlock, st, inflow_calls);
         if (any_inflow()) inflow_calls += (nlock == 2) ? 2 : 1;
+        // values the boundary conditions wrote (ghosts, walls, inflow, IBM
+        // images) into the FP64 masters of the mixed form
+        if (sizeof(T) == 4) launch_sync_masters<T>(b, st);
         CKL();
         return SULI_OK;
     }

@@ -114,6 +114,16 @@ struct CaseDev {
     // mixed form: FP64 pressure operator for the refinement residual (density
     // from the FP32 level set in FP64, scaled face coefficients, diagonal, rhs)
     double *rho64, *spi64, *spj64, *spk64, *dpr64, *qpr64;
+    // mixed form: FP64 masters of the velocity and of its RK stage copy.  The
+    // FP32 u, v, w (and u0 ...) are what every stencil reads; the masters are
+    // what tempo and posdin accumulate into (an FP32 predictor carries the
+    // gravity increment, and rounding it leaves noise that the variable-
+    // density projection moves into the light phase)
+    double *u64, *v64, *w64, *u064, *v064, *w064;
+    // mixed form: FP64 masters of the level set and its two RK stage buffers
+    // (WENO reads the FP32 copies; the stage combinations of advection,
+    // reinitialisation and the volume correction accumulate in FP64)
+    double *ls64, *lsb64, *lsc64;
     // multigrid hierarchy of the mixed form's preconditioner (nlev = 0: none)
     int nlev;
     MgLev<T> mg[MG_MAXL];

@@ -45,6 +45,8 @@ template <typename T> void launch_mms_error(const Batch<T> &b, cudaStream_t s);
 
 // boundary conditions (k_bc.cu)
 template <typename T> void launch_contorno(const Batch<T> &b, int nlock, cudaStream_t s, unsigned long long rng_call = 0);
+// mixed form: FP32 velocity values changed outside tempo/posdin -> FP64 masters
+template <typename T> void launch_sync_masters(const Batch<T> &b, cudaStream_t s);
 
 // immersed boundary (k_ibm.cu)
 template <typename T> void launch_ibm_posicoes(const Batch<T> &b, cudaStream_t s);

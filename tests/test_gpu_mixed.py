@@ -17,7 +17,9 @@ def _vel(get):
 
 @pytest.mark.parametrize("precond", [0, 1], ids=["jacobi", "multigrid"])
 def test_mixed_dam_break_against_oracle(gpu_lib, precond):
-    nsteps = 5
+    """The mixed form's target: within 1e-6 (relative L2) of the FP64 oracle
+    in velocity, pressure and level set."""
+    nsteps = 20
     case = cases.dam_break(32, 16, 16, cg_tol=1e-12)
     o = oracle_for(case)
     o.step(nsteps)
@@ -33,7 +35,7 @@ def test_mixed_dam_break_against_oracle(gpu_lib, precond):
     ep = rel_l2(pg - pg.mean(), po - po.mean())
     g.close()
     print("mixed (precond %d) vs oracle after %d steps: velocity %.2e ls %.2e p %.2e" % (precond, nsteps, ev, els, ep))
-    assert ev <= 1e-5 and els <= 1e-6 and ep <= 1e-5
+    assert ev <= 1e-6 and els <= 1e-6 and ep <= 1e-6
 
 
 @pytest.mark.parametrize("precond", [0, 1], ids=["jacobi", "multigrid"])
