@@ -170,6 +170,20 @@ def timed_steps(g, k, torch):
     return e0.elapsed_time(e1)
 
 
+def job_totals(cells, ms, dist=None, torch=None):
+    """Whole-job totals of a weak-scaling run: each rank advanced its own
+    ensemble (seed = rank) with no data-path collective, so the job's work is
+    the sum of the ranks' cells and its time the slowest rank's."""
+    if dist is None:
+        return float(cells), float(ms)
+    t = torch.tensor([float(cells), float(ms)], dtype=torch.float64)
+    c = t[0:1].clone()
+    m = t[1:2].clone()
+    dist.all_reduce(c, op=dist.ReduceOp.SUM)
+    dist.all_reduce(m, op=dist.ReduceOp.MAX)
+    return float(c.item()), float(m.item())
+
+
 def run_form(args, cs, torch, sampler=None, dist=None):
     g = start_gpu(cs)
     g.step(args.warmup)
@@ -182,10 +196,9 @@ def run_form(args, cs, torch, sampler=None, dist=None):
     ms = timed_steps(g, args.steps, torch)
     clocks = sampler.stop() if sampler else None
     prof = g.profile_read()
-    if dist is not None:
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    cells = sum(c.cells for c in cs)
+    job_cells, ms = job_totals(cells, ms, dist, torch)
+    g.job_cells = job_cells
     return g, ms, prof, clocks
 
 
@@ -344,15 +357,17 @@ def main():
         g.time_kernel(args.profile_kernel, 2)      # untimed: tables and caches warm
         g.synchronize()
         torch.cuda.cudart().cudaProfilerStart()
-        ms, by = g.time_kernel(args.profile_kernel, 1)
+        g.time_kernel(args.profile_kernel, 1)
         torch.cuda.cudart().cudaProfilerStop()
+        ms, by = g.time_kernel(args.profile_kernel, 20)
         g.close()
         print(json.dumps({"profile_kernel": args.profile_kernel, "workload": name, "cells": cells,
-                          "ms_per_launch": ms, "algorithmic_bytes_per_launch": by}))
+                          "ms_per_launch": ms, "algorithmic_bytes_per_launch": by,
+                          "GBs": by / (ms / 1e3) / 1e9, "timing": "20 launches between CUDA events"}))
         return
     sampler = ClockSampler(local) if rank == 0 else None
     gm, ms_m, prof_m, clocks = run_form(args, cs_m, torch, sampler, dist)
-    value = world * cells * args.steps / (ms_m / 1e3)
+    value = gm.job_cells * args.steps / (ms_m / 1e3)
     peak, peak_src = measured_peak_hbm()
     line = {
         "metric": "cell-steps/s (mixed-precision batched SuLi steps)",
@@ -389,7 +404,7 @@ def main():
         try:
             name64, cs_64 = make_cases(args, PREC_FP64, rank)
             g64, ms_64, prof_64, _ = run_form(args, cs_64, torch, None, dist)
-            v64 = world * cells * args.steps / (ms_64 / 1e3)
+            v64 = g64.job_cells * args.steps / (ms_64 / 1e3)
             line["fp64"] = {"value": v64, "ms_per_step": ms_64 / args.steps,
                             "cg_GBs_algorithmic": (7 * 8.0 * prof_64.cg_cell_iters / (prof_64.cg_ms / 1e3) / 1e9)
                             if prof_64.cg_ms > 0 else None,

@@ -286,65 +286,83 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_setup3(const CaseDev<T> *__rest
 // reduction, the block that finished last writes the cases still iterating
 // to table `out`, which the rest of the iteration and the next k_cgi_A read.
 
-// mp = A p, partial p.mp (:411-452); the case's last chunk forms
+// mp = A p, partial p.mp (:411-452); the case's last unit forms
 // alpha = sc[num] / p.mp (num = S_RR for CG, S_RZ for preconditioned CG).
-// Every kernel below walks its unit UW tiles at a time, issuing the loads of
-// UW cells before the stores.
+// Each thread owns a column of COL_Z planes, taken COL_G planes at a time: it
+// issues every load of a group (the COL_G + 2 planes of p, the COL_G + 1
+// z-face coefficients and the x/y neighbours and coefficients of each plane)
+// before any arithmetic, then forms the products; wall and periodic
+// neighbours are fixed index offsets and planes past the top are predicated
+// off, so nothing branches.
 template <typename T>
-__global__ void __launch_bounds__(NTHREADS) k_cgi_A(const CaseDev<T> *__restrict__ cs, const int *__restrict__ tab,
-                                                    int N, int num)
+__global__ void __launch_bounds__(NTHREADS, 4) k_cgi_A(const CaseDev<T> *__restrict__ cs, const int *__restrict__ tab,
+                                                       int N, int num)
 {
-    for_active_units(tab, N, 0, [&](int id, int u) {
+    for_active_units_seg(tab, N, 0, [&](int id, int u) {
         const CaseDev<T> &c = cs[id];
         const Geo &g = c.g;
         const int nx = g.nx, ny = g.ny, nz = g.nz;
         const bool px = (c.ccx0 == 0), py = (c.ccy0 == 0);
-        const T *p = c.p;
-        int t0, t1;
-        unit_tiles(c, 0, u, t0, t1);
-        TileWalk w(t0, c.ntx, c.nty);
+        const T *__restrict__ p = c.p;
+        const T *__restrict__ spi = c.spi;
+        const T *__restrict__ spj = c.spj;
+        const T *__restrict__ spk = c.spk;
+        T *__restrict__ mp = c.mp;
+        const Column cl = column_of(g, u);
+        // 32-bit offsets: a case's box holds fewer than 2^31 elements
+        const int sx = (int)g.sx, sxy = (int)g.sxy;
+        const int dxp = (cl.i < nx) ? 1 : (px ? -(nx - 1) : 0);
+        const int dxm = (cl.i > 1) ? -1 : (px ? (nx - 1) : 0);
+        const int dyp = (cl.j < ny) ? sx : (py ? -(ny - 1) * sx : 0);
+        const int dym = (cl.j > 1) ? -sx : (py ? (ny - 1) * sx : 0);
         double pm = 0.0;
-        for (int lt = t0; lt < t1; lt += UW) {
-            long long q[UW];
-            int ci[UW], cj[UW], ck[UW];
-            bool v[UW];
-            w.next<UW>(lt, t1, g, q, ci, cj, ck, v);
-            T m[UW], pcs[UW];
+        for (int kb = cl.k0; kb <= cl.k1; kb += COL_G) {
+            const int q0 = (int)g.at(cl.i, cl.j, kb);
+            const int np = min(COL_G, cl.k1 - kb + 1);
+            T pz[COL_G + 2], sk[COL_G + 1];
+            T vxp[COL_G], cxp[COL_G], vxm[COL_G], cxm[COL_G], vyp[COL_G], cyp[COL_G], vym[COL_G], cym[COL_G];
 #pragma unroll
-            for (int a = 0; a < UW; ++a) {
-                // neighbour indices: Neumann maps a wall neighbour to the cell
-                // itself, periodic x/y to the opposite end (no branch: every
-                // load is issued, at a clamped cell for padding lanes)
-                const int i = ci[a], j = cj[a], k = ck[a];
-                const long long qq = q[a];
-                const long long qxp = (i < nx) ? qq + 1 : (px ? qq - (nx - 1) : qq);
-                const long long qxm = (i > 1) ? qq - 1 : (px ? qq + (nx - 1) : qq);
-                const long long qyp = (j < ny) ? qq + g.sx : (py ? qq - (long long)(ny - 1) * g.sx : qq);
-                const long long qym = (j > 1) ? qq - g.sx : (py ? qq + (long long)(ny - 1) * g.sx : qq);
-                const long long qzp = (k < nz) ? qq + g.sxy : qq;
-                const long long qzm = (k > 1) ? qq - g.sxy : qq;
-                const T pc = p[qq];
-                m[a] = pc - p[qxp] * c.spi[qq + 1] - p[qxm] * c.spi[qq] - p[qyp] * c.spj[qq + g.sx] -
-                       p[qym] * c.spj[qq] - p[qzp] * c.spk[qq + g.sxy] - p[qzm] * c.spk[qq];
-                pcs[a] = pc;
+            for (int t = 0; t < COL_G + 2; ++t) {
+                // plane kb-1+t, the Neumann copy at the bottom and top walls
+                const int k = min(max(kb - 1 + t, 1), nz);
+                pz[t] = p[q0 + (k - kb) * sxy];
             }
 #pragma unroll
-            for (int a = 0; a < UW; ++a)
-                if (v[a]) {
-                    c.mp[q[a]] = m[a];
-                    pm += (double)pcs[a] * (double)m[a];
-                }
+            for (int t = 0; t < COL_G + 1; ++t) sk[t] = spk[q0 + min(t, np) * sxy];
+#pragma unroll
+            for (int t = 0; t < COL_G; ++t) {
+                const int q = q0 + min(t, np - 1) * sxy;
+                vxp[t] = p[q + dxp]; cxp[t] = spi[q + 1];
+                vxm[t] = p[q + dxm]; cxm[t] = spi[q];
+                vyp[t] = p[q + dyp]; cyp[t] = spj[q + sx];
+                vym[t] = p[q + dym]; cym[t] = spj[q];
+            }
+#pragma unroll
+            for (int t = 0; t < COL_G; ++t) {
+                if (t >= np || !cl.v) continue;
+                const T pc = pz[t + 1];
+                // the reference's order of operations (9_grad.f90:411-452)
+                const T m = pc - vxp[t] * cxp[t] - vxm[t] * cxm[t] - vyp[t] * cyp[t] - vym[t] * cym[t] -
+                            pz[t + 2] * sk[t + 1] - pz[t] * sk[t];
+                mp[q0 + t * sxy] = m;
+                pm += (double)pc * (double)m;
+            }
         }
-        double vals[1] = {pm}, tot[1];
-        if (chunk_reduce<T, 1>(c, u, vals, tot) && tid_lin() == 0) c.sc[S_ALPHA] = c.sc[num] / tot[0];
+        double vals[1] = {pm};
+        unit_partial<T, 1>(c, u, vals);
+    }, [&](int id, int cnt) {
+        const CaseDev<T> &c = cs[id];
+        double tot[1];
+        if (seg_reduce<T, 1>(c, cnt, tot) && tid_lin() == 0) c.sc[S_ALPHA] = c.sc[num] / tot[0];
     });
 }
 
-// e -= alpha p, r -= alpha mp, partial r.r (:458-508); the case's last chunk
+// e -= alpha p, r -= alpha mp, partial r.r (:458-508); the case's last unit
 // counts the iteration and applies the stop rule:
 //   MODE 0  the case's rule (r.r > threshold, iteration cap) or a replayed
 //           count; beta = r.r / r.r_old
 //   MODE 1  one FP32 pass of the mixed form: r.r above the pass target S_RRREF
+//           (at most MG_PASS_MAX iterations when preconditioned, MODE 2)
 //   MODE 2  as 1, preconditioned: also writes the V-cycle's right-hand side
 //           D^1/2 r (beta comes from r.z, k_pcg_dot)
 template <typename T, int MODE>
@@ -360,38 +378,37 @@ __global__ void __launch_bounds__(NTHREADS) k_cgi_B(const CaseDev<T> *__restrict
         }
         return;
     }
-    for_active_units(tab, N, 0, [&](int id, int u) {
+    for_active_units_seg(tab, N, 0, [&](int id, int u) {
         const CaseDev<T> &c = cs[id];
         const Geo &g = c.g;
         const T alpha = T(c.sc[S_ALPHA]);
-        int t0, t1;
-        unit_tiles(c, 0, u, t0, t1);
-        TileWalk w(t0, c.ntx, c.nty);
+        T *__restrict__ e = c.e;
+        T *__restrict__ r = c.r;
+        const T *__restrict__ p = c.p;
+        const T *__restrict__ mp = c.mp;
+        const T *__restrict__ dpr = c.dpr;
+        T *__restrict__ f0 = (MODE == 2) ? c.mg[0].f : nullptr;
+        const Column cl = column_of(g, u);
+        long long q = g.at(cl.i, cl.j, cl.k0);
         double rr = 0.0;
-        for (int lt = t0; lt < t1; lt += UW) {
-            long long q[UW];
-            int ci[UW], cj[UW], ck[UW];
-            bool v[UW];
-            w.next<UW>(lt, t1, g, q, ci, cj, ck, v);
-            T en[UW], rn[UW], fn[UW];
-#pragma unroll
-            for (int a = 0; a < UW; ++a) {
-                const long long qq = q[a];
-                en[a] = c.e[qq] - alpha * c.p[qq];
-                rn[a] = c.r[qq] - alpha * c.mp[qq];
-                fn[a] = (MODE == 2) ? sqrt(c.dpr[qq]) * rn[a] : T(0);
+#pragma unroll 2
+        for (int k = cl.k0; k <= cl.k1; ++k, q += g.sxy) {
+            const T en = e[q] - alpha * p[q];
+            const T rn = r[q] - alpha * mp[q];
+            const T fn = (MODE == 2) ? sqrt(dpr[q]) * rn : T(0);
+            if (cl.v) {
+                e[q] = en;
+                r[q] = rn;
+                if (MODE == 2) f0[q] = fn;
+                rr += (double)rn * (double)rn;
             }
-#pragma unroll
-            for (int a = 0; a < UW; ++a)
-                if (v[a]) {
-                    c.e[q[a]] = en[a];
-                    c.r[q[a]] = rn[a];
-                    if (MODE == 2) c.mg[0].f[q[a]] = fn[a];
-                    rr += (double)rn[a] * (double)rn[a];
-                }
         }
-        double vals[1] = {rr}, tot[1];
-        if (chunk_reduce<T, 1>(c, u, vals, tot)) {
+        double vals[1] = {rr};
+        unit_partial<T, 1>(c, u, vals);
+    }, [&](int id, int cnt) {
+        const CaseDev<T> &c = cs[id];
+        double tot[1];
+        if (seg_reduce<T, 1>(c, cnt, tot)) {
             if (tid_lin() == 0) {
                 double rrn = tot[0];
                 double it = c.sc[S_CGITER] + 1.0;
@@ -430,21 +447,13 @@ __global__ void __launch_bounds__(NTHREADS) k_cgi_C(const CaseDev<T> *__restrict
         const CaseDev<T> &c = cs[id];
         const Geo &g = c.g;
         const T beta = T(c.sc[S_BETA]);
-        int t0, t1;
-        unit_tiles(c, 0, u, t0, t1);
-        TileWalk w(t0, c.ntx, c.nty);
-        for (int lt = t0; lt < t1; lt += UW) {
-            long long q[UW];
-            int ci[UW], cj[UW], ck[UW];
-            bool v[UW];
-            w.next<UW>(lt, t1, g, q, ci, cj, ck, v);
-            T pn[UW];
-#pragma unroll
-            for (int a = 0; a < UW; ++a) pn[a] = c.r[q[a]] + beta * c.p[q[a]];
-#pragma unroll
-            for (int a = 0; a < UW; ++a)
-                if (v[a]) c.p[q[a]] = pn[a];
-        }
+        const T *__restrict__ r = c.r;
+        T *__restrict__ p = c.p;
+        const Column cl = column_of(g, u);
+        if (!cl.v) return;
+        long long q = g.at(cl.i, cl.j, cl.k0);
+#pragma unroll 4
+        for (int k = cl.k0; k <= cl.k1; ++k, q += g.sxy) p[q] = r[q] + beta * p[q];
     });
 }
 
@@ -454,30 +463,26 @@ template <typename T>
 __global__ void __launch_bounds__(NTHREADS) k_pcg_dot(const CaseDev<T> *__restrict__ cs, const int *__restrict__ tab,
                                                       int N, int first)
 {
-    for_active_units(tab, N, 0, [&](int id, int u) {
+    for_active_units_seg(tab, N, 0, [&](int id, int u) {
         const CaseDev<T> &c = cs[id];
         const Geo &g = c.g;
-        int t0, t1;
-        unit_tiles(c, 0, u, t0, t1);
-        TileWalk w(t0, c.ntx, c.nty);
+        const T *__restrict__ dpr = c.dpr;
+        const T *__restrict__ z0 = c.mg[0].z;
+        const T *__restrict__ r = c.r;
+        const Column cl = column_of(g, u);
+        long long q = g.at(cl.i, cl.j, cl.k0);
         double rz = 0.0;
-        for (int lt = t0; lt < t1; lt += UW) {
-            long long q[UW];
-            int ci[UW], cj[UW], ck[UW];
-            bool v[UW];
-            w.next<UW>(lt, t1, g, q, ci, cj, ck, v);
-            T zz[UW], rv[UW];
-#pragma unroll
-            for (int a = 0; a < UW; ++a) {
-                zz[a] = sqrt(c.dpr[q[a]]) * c.mg[0].z[q[a]];
-                rv[a] = c.r[q[a]];
-            }
-#pragma unroll
-            for (int a = 0; a < UW; ++a)
-                if (v[a]) rz += (double)zz[a] * (double)rv[a];
+#pragma unroll 4
+        for (int k = cl.k0; k <= cl.k1; ++k, q += g.sxy) {
+            const T z = sqrt(dpr[q]) * z0[q];
+            if (cl.v) rz += (double)z * (double)r[q];
         }
-        double vals[1] = {rz}, tot[1];
-        if (chunk_reduce<T, 1>(c, u, vals, tot) && tid_lin() == 0) {
+        double vals[1] = {rz};
+        unit_partial<T, 1>(c, u, vals);
+    }, [&](int id, int cnt) {
+        const CaseDev<T> &c = cs[id];
+        double tot[1];
+        if (seg_reduce<T, 1>(c, cnt, tot) && tid_lin() == 0) {
             c.sc[S_BETA] = first ? 0.0 : tot[0] / c.sc[S_RZ];
             c.sc[S_RZ] = tot[0];
         }
@@ -493,21 +498,14 @@ __global__ void __launch_bounds__(NTHREADS) k_pcg_C(const CaseDev<T> *__restrict
         const CaseDev<T> &c = cs[id];
         const Geo &g = c.g;
         const T beta = T(c.sc[S_BETA]);
-        int t0, t1;
-        unit_tiles(c, 0, u, t0, t1);
-        TileWalk w(t0, c.ntx, c.nty);
-        for (int lt = t0; lt < t1; lt += UW) {
-            long long q[UW];
-            int ci[UW], cj[UW], ck[UW];
-            bool v[UW];
-            w.next<UW>(lt, t1, g, q, ci, cj, ck, v);
-            T pn[UW];
-#pragma unroll
-            for (int a = 0; a < UW; ++a) pn[a] = sqrt(c.dpr[q[a]]) * c.mg[0].z[q[a]] + beta * c.p[q[a]];
-#pragma unroll
-            for (int a = 0; a < UW; ++a)
-                if (v[a]) c.p[q[a]] = pn[a];
-        }
+        const T *__restrict__ dpr = c.dpr;
+        const T *__restrict__ z0 = c.mg[0].z;
+        T *__restrict__ p = c.p;
+        const Column cl = column_of(g, u);
+        if (!cl.v) return;
+        long long q = g.at(cl.i, cl.j, cl.k0);
+#pragma unroll 4
+        for (int k = cl.k0; k <= cl.k1; ++k, q += g.sxy) p[q] = sqrt(dpr[q]) * z0[q] + beta * p[q];
     });
 }
 
@@ -668,21 +666,24 @@ template <typename T> void launch_cg_setup(const Batch<T> &b, cudaStream_t s)
     k_cg_setup2<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, 1); count_launch();
     k_cg_setup3<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
 }
-// grid of the iteration kernels: every SM full
-template <typename T> int cg_iter_grid()
-{
-    static int grid = 0;
-    if (grid == 0) {
-        int dev = 0, sms = 0, a = 0, bb = 0, cc = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_cgi_A<T>, NTHREADS, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bb, k_cgi_B<T, 0>, NTHREADS, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cc, k_cgi_C<T>, NTHREADS, 0);
-        int per = std::max(1, std::min(a, std::min(bb, cc)));
-        grid = std::max(1, sms) * per;
+// grids of the persistent kernels (each filled to its own occupancy)
+template <typename T> struct CgGrids {
+    int A, B0, B1, B2, C, dot, pC;
+    CgGrids()
+    {
+        A = occupancy_grid((const void *)k_cgi_A<T>);
+        B0 = occupancy_grid((const void *)k_cgi_B<T, 0>);
+        B1 = occupancy_grid((const void *)k_cgi_B<T, 1>);
+        B2 = occupancy_grid((const void *)k_cgi_B<T, 2>);
+        C = occupancy_grid((const void *)k_cgi_C<T>);
+        dot = occupancy_grid((const void *)k_pcg_dot<T>);
+        pC = occupancy_grid((const void *)k_pcg_C<T>);
     }
-    return grid;
+};
+template <typename T> const CgGrids<T> &cg_grids()
+{
+    static const CgGrids<T> g;
+    return g;
 }
 
 template <typename T> const int *cg_table(const Batch<T> &b, int slot)
@@ -709,10 +710,10 @@ template <typename T> int launch_profile_kernel(const Batch<T> &b, int kernel, i
         k_cgi_table<T><<<1, b.block(), 0, s>>>(b.dcases, tab, b.act_done, b.ncases, b.nlev, 1);
         count_launch();
     }
-    const int G = cg_iter_grid<T>();
-    if (kernel == 0) k_cgi_A<T><<<G, b.block(), 0, s>>>(b.dcases, tab, b.ncases, S_RR);
-    else if (kernel == 1) return launch_mg_smooth0<T>(b, tab, G, s);
-    else if (kernel == 2) k_cgi_C<T><<<G, b.block(), 0, s>>>(b.dcases, tab, b.ncases);
+    const CgGrids<T> &G = cg_grids<T>();
+    if (kernel == 0) k_cgi_A<T><<<G.A, b.cblock(), 0, s>>>(b.dcases, tab, b.ncases, S_RR);
+    else if (kernel == 1) return launch_mg_smooth0<T>(b, tab, 0, s);
+    else if (kernel == 2) k_cgi_C<T><<<G.C, b.cblock(), 0, s>>>(b.dcases, tab, b.ncases);
     else return -1;
     count_launch();
     return 0;
@@ -721,14 +722,14 @@ template <typename T> int launch_profile_kernel(const Batch<T> &b, int kernel, i
 // n iterations starting from table `slot`; returns the slot of the last table
 template <typename T> int launch_cg_iters(const Batch<T> &b, int n, int slot, int mode, cudaStream_t s)
 {
-    const int G = cg_iter_grid<T>();
+    const CgGrids<T> &G = cg_grids<T>();
     const int st = act_stride(b.ncases, b.nlev);
     for (int q = 0; q < n; ++q) {
         int *tin = b.act + slot * st, *tout = b.act + (1 - slot) * st;
-        k_cgi_A<T><<<G, b.block(), 0, s>>>(b.dcases, tin, b.ncases, S_RR);
-        if (mode == 1) k_cgi_B<T, 1><<<G, b.block(), 0, s>>>(b.dcases, tin, tout, b.act_done, b.ncases, b.nlev);
-        else k_cgi_B<T, 0><<<G, b.block(), 0, s>>>(b.dcases, tin, tout, b.act_done, b.ncases, b.nlev);
-        k_cgi_C<T><<<G, b.block(), 0, s>>>(b.dcases, tout, b.ncases);
+        k_cgi_A<T><<<G.A, b.cblock(), 0, s>>>(b.dcases, tin, b.ncases, S_RR);
+        if (mode == 1) k_cgi_B<T, 1><<<G.B1, b.cblock(), 0, s>>>(b.dcases, tin, tout, b.act_done, b.ncases, b.nlev);
+        else k_cgi_B<T, 0><<<G.B0, b.cblock(), 0, s>>>(b.dcases, tin, tout, b.act_done, b.ncases, b.nlev);
+        k_cgi_C<T><<<G.C, b.cblock(), 0, s>>>(b.dcases, tout, b.ncases);
         count_launch(3);
         slot = 1 - slot;
     }
@@ -739,27 +740,27 @@ template <typename T> int launch_cg_iters(const Batch<T> &b, int n, int slot, in
 // right-hand side written by k_cg_true_residual): z = M r, r.z, p = z
 template <typename T> void launch_pcg_start(const Batch<T> &b, int slot, cudaStream_t s)
 {
-    const int G = cg_iter_grid<T>();
+    const CgGrids<T> &G = cg_grids<T>();
     const int *tab = cg_table(b, slot);
-    launch_mg_vcycle<T>(b, tab, G, s);
-    k_pcg_dot<T><<<G, b.block(), 0, s>>>(b.dcases, tab, b.ncases, 1);
-    k_pcg_C<T><<<G, b.block(), 0, s>>>(b.dcases, tab, b.ncases);
+    launch_mg_vcycle<T>(b, tab, 0, s);
+    k_pcg_dot<T><<<G.dot, b.cblock(), 0, s>>>(b.dcases, tab, b.ncases, 1);
+    k_pcg_C<T><<<G.pC, b.cblock(), 0, s>>>(b.dcases, tab, b.ncases);
     count_launch(2);
 }
 
 // n preconditioned iterations from table `slot`; returns the current slot
 template <typename T> int launch_pcg_iters(const Batch<T> &b, int n, int slot, cudaStream_t s)
 {
-    const int G = cg_iter_grid<T>();
+    const CgGrids<T> &G = cg_grids<T>();
     const int st = act_stride(b.ncases, b.nlev);
     for (int q = 0; q < n; ++q) {
         int *tin = b.act + slot * st, *tout = b.act + (1 - slot) * st;
-        k_cgi_A<T><<<G, b.block(), 0, s>>>(b.dcases, tin, b.ncases, S_RZ);
-        k_cgi_B<T, 2><<<G, b.block(), 0, s>>>(b.dcases, tin, tout, b.act_done, b.ncases, b.nlev);
+        k_cgi_A<T><<<G.A, b.cblock(), 0, s>>>(b.dcases, tin, b.ncases, S_RZ);
+        k_cgi_B<T, 2><<<G.B2, b.cblock(), 0, s>>>(b.dcases, tin, tout, b.act_done, b.ncases, b.nlev);
         count_launch(2);
-        launch_mg_vcycle<T>(b, tout, G, s);
-        k_pcg_dot<T><<<G, b.block(), 0, s>>>(b.dcases, tout, b.ncases, 0);
-        k_pcg_C<T><<<G, b.block(), 0, s>>>(b.dcases, tout, b.ncases);
+        launch_mg_vcycle<T>(b, tout, 0, s);
+        k_pcg_dot<T><<<G.dot, b.cblock(), 0, s>>>(b.dcases, tout, b.ncases, 0);
+        k_pcg_C<T><<<G.pC, b.cblock(), 0, s>>>(b.dcases, tout, b.ncases);
         count_launch(2);
         slot = 1 - slot;
     }

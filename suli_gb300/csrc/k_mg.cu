@@ -62,8 +62,8 @@ __device__ __forceinline__ T mg_nbsum(const MgLev<T> &L, int i, int j, int k, lo
 // starts from z = 0 (this colour gets f / dg, the other colour 0).  The cells
 // of UW tiles are loaded before any is written.
 template <typename T>
-__global__ void __launch_bounds__(NTHREADS) k_mg_smooth(const CaseDev<T> *__restrict__ cs, const int *__restrict__ tab,
-                                                        int N, int l, int color, int zero)
+__global__ void __launch_bounds__(NTHREADS, 4) k_mg_smooth(const CaseDev<T> *__restrict__ cs, const int *__restrict__ tab,
+                                                           int N, int l, int color, int zero)
 {
     for_active_units(tab, N, l, [&](int id, int u) {
         const CaseDev<T> &c = cs[id];
@@ -77,8 +77,62 @@ __global__ void __launch_bounds__(NTHREADS) k_mg_smooth(const CaseDev<T> *__rest
         const bool wx = c.ccx0 == 0 && !(nx & 1) && nx > 1;
         const bool wy = c.ccy0 == 0 && !(ny & 1) && ny > 1;
         const T *z = L.z;
-        int t0, t1;
-        unit_tiles(c, l, u, t0, t1);
+        if (l == 0) {
+            // case grid: one column of COL_Z planes per thread, COL_G planes
+            // at a time with every load of a group issued before any
+            // arithmetic (the z-neighbours of a cell of this colour have the
+            // other colour, unchanged by this sweep)
+            const Column cl = column_of(g, u);
+            const int i = cl.i, j = cl.j;
+            // 32-bit offsets: a case's box holds fewer than 2^31 elements
+            const int isx = (int)sx, isxy = (int)sxy;
+            const int dxm = (wx && i == 1) ? (nx - 1) : -1;
+            const int dxp = (wx && i == nx) ? -(nx - 1) : 1;
+            const int dym = (wy && j == 1) ? (ny - 1) * isx : -isx;
+            const int dyp = (wy && j == ny) ? -(ny - 1) * isx : isx;
+            const T *__restrict__ f = L.f;
+            const T *__restrict__ dg = L.dg;
+            const T *__restrict__ cxa = L.cx;
+            const T *__restrict__ cya = L.cy;
+            const T *__restrict__ cza = L.cz;
+            T *zw = L.z;
+            for (int kb = cl.k0; kb <= cl.k1; kb += COL_G) {
+                const int q0 = (int)g.at(i, j, kb);
+                const int np = min(COL_G, cl.k1 - kb + 1);
+                T zz[COL_G + 2], czz[COL_G + 1], fv[COL_G], dv[COL_G];
+                T a0[COL_G], a1[COL_G], b0[COL_G], b1[COL_G], za0[COL_G], za1[COL_G], zb0[COL_G], zb1[COL_G];
+#pragma unroll
+                for (int t = 0; t < COL_G + 2; ++t) zz[t] = z[q0 + (min(t, np + 1) - 1) * isxy];
+#pragma unroll
+                for (int t = 0; t < COL_G + 1; ++t) czz[t] = cza[q0 + min(t, np) * isxy];
+#pragma unroll
+                for (int t = 0; t < COL_G; ++t) {
+                    const int q = q0 + min(t, np - 1) * isxy;
+                    fv[t] = f[q];
+                    dv[t] = dg[q];
+                    a0[t] = cxa[q]; a1[t] = cxa[q + 1]; b0[t] = cya[q]; b1[t] = cya[q + isx];
+                    za0[t] = z[q + dxm]; za1[t] = z[q + dxp]; zb0[t] = z[q + dym]; zb1[t] = z[q + dyp];
+                }
+#pragma unroll
+                for (int t = 0; t < COL_G; ++t) {
+                    if (t >= np || !cl.v) continue;
+                    const bool mine = ((i + j + kb + t) & 1) == color;
+                    const T d = dv[t];
+                    T zn;
+                    if (zero) {
+                        zn = (mine && d > T(0)) ? fv[t] / d : T(0);
+                    } else {
+                        if (!mine) continue;
+                        const T sm = fv[t] + a0[t] * za0[t] + a1[t] * za1[t] + b0[t] * zb0[t] + b1[t] * zb1[t] +
+                                     czz[t] * zz[t] + czz[t + 1] * zz[t + 2];
+                        zn = (d > T(0)) ? sm / d : T(0);
+                    }
+                    zw[q0 + t * isxy] = zn;
+                }
+            }
+            return;
+        }
+        const int t0 = u, t1 = u + 1;
         TileWalk w(t0, L.ntx, L.nty);
         for (int lt = t0; lt < t1; lt += UW) {
             long long q[UW];
@@ -160,8 +214,15 @@ __global__ void __launch_bounds__(NTHREADS) k_mg_prolong(const CaseDev<T> *__res
         const CaseDev<T> &c = cs[id];
         const MgLev<T> &F = c.mg[l];
         const MgLev<T> &C = c.mg[l + 1];
-        int t0, t1;
-        unit_tiles(c, l, u, t0, t1);
+        if (l == 0) {
+            const Column cl = column_of(F.g, u);
+            if (!cl.v) return;
+            long long q = F.g.at(cl.i, cl.j, cl.k0);
+            for (int k = cl.k0; k <= cl.k1; ++k, q += F.g.sxy)
+                F.z[q] += C.z[C.g.at((cl.i + 1) >> 1, (cl.j + 1) >> 1, (k + 1) >> 1)];
+            return;
+        }
+        const int t0 = u, t1 = u + 1;
         TileWalk w(t0, F.ntx, F.nty);
         for (int lt = t0; lt < t1; lt += UW) {
             long long q[UW];
@@ -260,26 +321,30 @@ template <typename T> void launch_mg_coarsen(const Batch<T> &b, cudaStream_t s)
 // mg[0].z
 template <typename T> void launch_mg_vcycle(const Batch<T> &b, const int *tab, int grid, cudaStream_t s)
 {
+    (void)grid;
+    static const int gS = occupancy_grid((const void *)k_mg_smooth<T>);
+    static const int gR = occupancy_grid((const void *)k_mg_restrict<T>);
+    static const int gP = occupancy_grid((const void *)k_mg_prolong<T>);
     const int N = b.ncases, NL = b.nlev;
     const int nu = 2, ncoarse = 6;
     for (int l = 0; l + 1 < NL; ++l) {
         for (int it = 0; it < nu; ++it) {
-            k_mg_smooth<T><<<grid, b.block(), 0, s>>>(b.dcases, tab, N, l, 0, it == 0);
-            k_mg_smooth<T><<<grid, b.block(), 0, s>>>(b.dcases, tab, N, l, 1, 0);
+            k_mg_smooth<T><<<gS, b.cblock(), 0, s>>>(b.dcases, tab, N, l, 0, it == 0);
+            k_mg_smooth<T><<<gS, b.cblock(), 0, s>>>(b.dcases, tab, N, l, 1, 0);
         }
-        k_mg_restrict<T><<<grid, b.block(), 0, s>>>(b.dcases, tab, N, l + 1);
+        k_mg_restrict<T><<<gR, b.cblock(), 0, s>>>(b.dcases, tab, N, l + 1);
         count_launch(2 * nu + 1);
     }
     for (int it = 0; it < ncoarse; ++it) {
-        k_mg_smooth<T><<<grid, b.block(), 0, s>>>(b.dcases, tab, N, NL - 1, 0, it == 0);
-        k_mg_smooth<T><<<grid, b.block(), 0, s>>>(b.dcases, tab, N, NL - 1, 1, 0);
+        k_mg_smooth<T><<<gS, b.cblock(), 0, s>>>(b.dcases, tab, N, NL - 1, 0, it == 0);
+        k_mg_smooth<T><<<gS, b.cblock(), 0, s>>>(b.dcases, tab, N, NL - 1, 1, 0);
     }
     count_launch(2 * ncoarse);
     for (int l = NL - 2; l >= 0; --l) {
-        k_mg_prolong<T><<<grid, b.block(), 0, s>>>(b.dcases, tab, N, l);
+        k_mg_prolong<T><<<gP, b.cblock(), 0, s>>>(b.dcases, tab, N, l);
         for (int it = 0; it < nu; ++it) {
-            k_mg_smooth<T><<<grid, b.block(), 0, s>>>(b.dcases, tab, N, l, 1, 0);
-            k_mg_smooth<T><<<grid, b.block(), 0, s>>>(b.dcases, tab, N, l, 0, 0);
+            k_mg_smooth<T><<<gS, b.cblock(), 0, s>>>(b.dcases, tab, N, l, 1, 0);
+            k_mg_smooth<T><<<gS, b.cblock(), 0, s>>>(b.dcases, tab, N, l, 0, 0);
         }
         count_launch(2 * nu + 1);
     }
@@ -288,8 +353,10 @@ template <typename T> void launch_mg_vcycle(const Batch<T> &b, const int *tab, i
 // profiling: one red half-sweep on level 0 over table `tab`
 template <typename T> int launch_mg_smooth0(const Batch<T> &b, const int *tab, int grid, cudaStream_t s)
 {
+    (void)grid;
     if (b.nlev < 2) return -1;
-    k_mg_smooth<T><<<grid, b.block(), 0, s>>>(b.dcases, tab, b.ncases, 0, 0, 0);
+    static const int gS = occupancy_grid((const void *)k_mg_smooth<T>);
+    k_mg_smooth<T><<<gS, b.cblock(), 0, s>>>(b.dcases, tab, b.ncases, 0, 0, 0);
     count_launch();
     return 0;
 }

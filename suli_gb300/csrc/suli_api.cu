@@ -254,13 +254,14 @@ struct Impl : ImplBase {
             g.sx = (q.nx + 3 + 7) / 8 * 8;
             g.sxy = g.sx * (q.ny + 3);
             g.total = g.sxy * (q.nz + 3);
+            if (g.total >= (1LL << 31)) return fail(SULI_BAD_CONFIG, "a case's grid exceeds 2^31 padded cells");
             cd.ntx = (q.nx + 1 + TX - 1) / TX;
             cd.nty = (q.ny + 1 + TY - 1) / TY;
             cd.ntz = (q.nz + 1 + TZ - 1) / TZ;
             cd.ntiles = cd.ntx * cd.nty * cd.ntz;
             cd.tile_begin = tiles;
             tiles += cd.ntiles;
-            cd.nchunks = (cd.ntiles + CG_CHUNK - 1) / CG_CHUNK;
+            cd.nchunks = col_units(q.nx, q.ny, q.nz);
             cd.chunk_begin = chunks;
             chunks += cd.nchunks;
             long long mp = std::max({(long long)(q.nx + 3) * (q.nz + 3), (long long)(q.nx + 3) * (q.ny + 3),

@@ -22,7 +22,15 @@ constexpr int TY = 4;
 constexpr int TZ = 2;
 constexpr int NTHREADS = TX * TY * TZ;
 constexpr int NSLOT = 8; // reduction slots per block
-constexpr int CG_CHUNK = 16;  // tiles per work unit of the persistent CG kernels
+// work unit of the persistent kernels on the case grid: a column of
+// COL_X x COL_Y cells in x, y (one per thread of a 32 x 8 block) and COL_Z
+// planes, which each thread walks in groups of COL_G planes
+constexpr int COL_X = 32, COL_Y = 8, COL_Z = 8;
+constexpr int COL_G = 4;   // planes a thread loads before it computes (one group)
+__host__ __device__ __forceinline__ int col_units(int nx, int ny, int nz)
+{
+    return ((nx + COL_X - 1) / COL_X) * ((ny + COL_Y - 1) / COL_Y) * ((nz + COL_Z - 1) / COL_Z);
+}
 
 // per-case device scalars (double), indices into CaseDev::sc
 enum Scal {
@@ -86,8 +94,8 @@ struct CaseDev {
     Geo g;
     // tiles of this case in the launch grid
     int tile_begin, ntiles, ntx, nty, ntz;
-    // chunks of CG_CHUNK consecutive tiles (the unit of the persistent CG
-    // kernels and of their reductions)
+    // column units of the case grid (the unit of the persistent CG kernels
+    // and of their reductions), see col_units
     int chunk_begin, nchunks;
     // discretisation / physics (double in both forms)
     double dx, dy, dz, dx1, dt1, deltai;
@@ -253,23 +261,23 @@ __device__ __forceinline__ bool last_block_reduce(const CaseDev<T> &c, const dou
     return unit_reduce<T, NS>(c, (int)blockIdx.x, c.tile_begin, c.ntiles, vals, tot, maxmask);
 }
 
-// one chunk of the persistent CG kernels (u = the case's chunk index)
-template <typename T, int NS>
-__device__ __forceinline__ bool chunk_reduce(const CaseDev<T> &c, int u, const double (&vals)[NS], double (&tot)[NS])
-{
-    return unit_reduce<T, NS>(c, c.chunk_begin + u, c.chunk_begin, c.nchunks, vals, tot, 0u);
-}
 
 // ---- active-case tables (persistent CG iteration) ---------------------------
 // A table lists the cases whose CG still iterates and, per grid level s, the
 // prefix of their work-unit counts, so a fixed grid can walk exactly the
-// active units of a level.  Level 0 is the case grid and its unit is a chunk
-// of CG_CHUNK tiles; level s > 0 is multigrid level s and its unit a tile:
+// active units of a level.  Level 0 is the case grid and its unit a column
+// (column_of); level s > 0 is multigrid level s and its unit a tile:
 //   tab[0] = n, tab[1 .. 1+n) = case ids,
 //   level s at B = 1 + N + s (N + 2): tab[B] = tiles, tab[B+1 .. B+1+n] = prefix
 // (N = cases in the batch, NL = levels in the table).
 __host__ __device__ __forceinline__ int act_stride(int ncases, int nl) { return 1 + ncases + nl * (ncases + 2); }
 __host__ __device__ __forceinline__ int act_level(int ncases, int s) { return 1 + ncases + s * (ncases + 2); }
+
+// this thread's offset inside a TX x TY x TZ tile, from its linear id (so a
+// kernel may run with 32 x 4 x 2 or 32 x 8 x 1 blocks)
+__device__ __forceinline__ int tile_ox() { return tid_lin() & (TX - 1); }
+__device__ __forceinline__ int tile_oy() { return (tid_lin() / TX) % TY; }
+__device__ __forceinline__ int tile_oz() { return tid_lin() / (TX * TY); }
 
 // tile `lt` of a grid with ntx x nty tiles -> the cell of this thread
 __device__ __forceinline__ void tile_cell(int ntx, int nty, int lt, int &i, int &j, int &k)
@@ -278,9 +286,31 @@ __device__ __forceinline__ void tile_cell(int ntx, int nty, int lt, int &i, int 
     int r = lt / ntx;
     int tj = r % nty;
     int tk = r / nty;
-    i = 1 + ti * TX + (int)threadIdx.x;
-    j = 1 + tj * TY + (int)threadIdx.y;
-    k = 1 + tk * TZ + (int)threadIdx.z;
+    i = 1 + ti * TX + tile_ox();
+    j = 1 + tj * TY + tile_oy();
+    k = 1 + tk * TZ + tile_oz();
+}
+
+// column unit u of a grid (see COL_X): this thread's (i, j), clamped into the
+// grid (v = false outside it), and the planes k0..k1 the column covers.
+// Needs 256 threads per block.
+struct Column {
+    int i, j, k0, k1;
+    bool v;
+};
+__device__ __forceinline__ Column column_of(const Geo &g, int u)
+{
+    const int ux = (g.nx + COL_X - 1) / COL_X, uy = (g.ny + COL_Y - 1) / COL_Y;
+    const int a = u % ux, r = u / ux, b = r % uy, cz = r / uy;
+    const int t = tid_lin();
+    const int i = 1 + a * COL_X + (t & (COL_X - 1)), j = 1 + b * COL_Y + t / COL_X;
+    Column c;
+    c.v = i <= g.nx && j <= g.ny;
+    c.i = min(i, g.nx);
+    c.j = min(j, g.ny);
+    c.k0 = 1 + cz * COL_Z;
+    c.k1 = min(g.nz, c.k0 + COL_Z - 1);
+    return c;
 }
 
 template <typename T>
@@ -310,9 +340,9 @@ struct TileWalk {
     {
 #pragma unroll
         for (int a = 0; a < U; ++a) {
-            const int i = 1 + ti * TX + (int)threadIdx.x;
-            const int j = 1 + tj * TY + (int)threadIdx.y;
-            const int k = 1 + tk * TZ + (int)threadIdx.z;
+            const int i = 1 + ti * TX + tile_ox();
+            const int j = 1 + tj * TY + tile_oy();
+            const int k = 1 + tk * TZ + tile_oz();
             v[a] = (lt + a < t1) && i <= g.nx && j <= g.ny && k <= g.nz;
             ci[a] = min(i, g.nx);
             cj[a] = min(j, g.ny);
@@ -327,18 +357,7 @@ struct TileWalk {
 };
 constexpr int UW = 2;   // cells per thread per step of the walk
 
-// tiles [t0, t1) of unit u of a case at table level s
-template <typename T>
-__device__ __forceinline__ void unit_tiles(const CaseDev<T> &c, int s, int u, int &t0, int &t1)
-{
-    if (s == 0) {
-        t0 = u * CG_CHUNK;
-        t1 = min(c.ntiles, t0 + CG_CHUNK);
-    } else {
-        t0 = u;
-        t1 = u + 1;
-    }
-}
+
 
 // Block b of the grid takes the contiguous range of active units of level s,
 // [U b / G, U (b+1) / G), and calls f(case id, local unit) for each, in
@@ -365,6 +384,85 @@ __device__ __forceinline__ void for_active_units(const int *__restrict__ tab, in
         while (t >= end) { ++a; end = off[a + 1]; }
         f(ids[a], t - off[a]);
     }
+}
+
+// As for_active_units, for kernels that reduce per unit: unit(id, u) runs
+// for each unit; seg(id, n) runs once after the block's last unit of a case
+// in its range (n = units it did for that case), so the completion fence
+// and atomic of a reduction are paid per segment, not per unit.
+template <typename F, typename G>
+__device__ __forceinline__ void for_active_units_seg(const int *__restrict__ tab, int N, int s, F unit, G seg)
+{
+    const int n = tab[0];
+    const int *ids = tab + 1;
+    const int *lv = tab + act_level(N, s);
+    const int tiles = lv[0];
+    const int *off = lv + 1;
+    const int lo = (int)((long long)tiles * blockIdx.x / gridDim.x);
+    const int hi = (int)((long long)tiles * (blockIdx.x + 1) / gridDim.x);
+    if (lo >= hi) return;
+    int a0 = 0, a1 = n - 1;
+    while (a0 < a1) {
+        int mid = (a0 + a1 + 1) >> 1;
+        if (off[mid] <= lo) a0 = mid; else a1 = mid - 1;
+    }
+    int a = a0;
+    int end = off[a + 1];
+    int cnt = 0;
+    for (int t = lo; t < hi; ++t) {
+        while (t >= end) {
+            if (cnt > 0) seg(ids[a], cnt);
+            cnt = 0;
+            ++a;
+            end = off[a + 1];
+        }
+        unit(ids[a], t - off[a]);
+        ++cnt;
+    }
+    if (cnt > 0) seg(ids[a], cnt);
+}
+
+// the partials of one column unit (no fence, no counter: see seg_reduce)
+template <typename T, int NS>
+__device__ __forceinline__ void unit_partial(const CaseDev<T> &c, int u, const double (&vals)[NS])
+{
+    __shared__ double sh[32];
+    double bv[NS];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) bv[s] = block_sum(vals[s], sh);
+    if (tid_lin() == 0) {
+#pragma unroll
+        for (int s = 0; s < NS; ++s) c.partials[(long long)s * c.total_tiles + c.chunk_begin + u] = bv[s];
+    }
+}
+
+// end of a segment of `cnt` units of case c: returns true in every thread of
+// the block that completes the case's last unit, with the totals over the
+// case's unit partials (summed in unit order) in tot
+template <typename T, int NS>
+__device__ bool seg_reduce(const CaseDev<T> &c, int cnt, double (&tot)[NS])
+{
+    __shared__ double sh[32];
+    __shared__ bool amlast;
+    const int t = tid_lin();
+    __syncthreads();
+    if (t == 0) {
+        __threadfence();
+        const unsigned prev = atomicAdd(c.counter, (unsigned)cnt);
+        amlast = (prev + (unsigned)cnt == (unsigned)c.nchunks);
+    }
+    __syncthreads();
+    if (!amlast) return false;
+    __threadfence();
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+        double a = 0.0;
+        const double *src = c.partials + (long long)s * c.total_tiles + c.chunk_begin;
+        for (int q = t; q < c.nchunks; q += NTHREADS) a += __ldcg(src + q);
+        tot[s] = block_sum(a, sh);
+    }
+    if (t == 0) *c.counter = 0u;
+    return true;
 }
 
 // exclusive prefix sum over the block (NTHREADS threads, linear id order);

@@ -8,6 +8,17 @@
 
 namespace suli {
 
+// grid of a persistent kernel: every SM filled to the kernel's own occupancy
+// (256 threads per block)
+inline int occupancy_grid(const void *fn)
+{
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, 0);
+    return (sms > 0 ? sms : 1) * (per > 0 ? per : 1);
+}
+
 // kernels launched by this library (all handles); read by suli_profile_read
 extern std::atomic<unsigned long long> g_launches;
 inline void count_launch(unsigned long long n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
@@ -26,6 +37,7 @@ struct Batch {
     int nlev = 1;                     // grid levels in the tables (multigrid levels, or 1)
     int mg_tiles[MG_MAXL] = {0};      // tiles of multigrid level l over all cases
     dim3 block() const { return dim3(TX, TY, TZ); }
+    dim3 cblock() const { return dim3(COL_X, COL_Y, 1); }   // persistent (column) kernels
 };
 
 // level set (k_levelset.cu)
