@@ -315,7 +315,10 @@ __global__ void __launch_bounds__(NTHREADS, 4) k_cgi_A(const CaseDev<T> *__restr
         const int dxm = (cl.i > 1) ? -1 : (px ? (nx - 1) : 0);
         const int dyp = (cl.j < ny) ? sx : (py ? -(ny - 1) * sx : 0);
         const int dym = (cl.j > 1) ? -sx : (py ? (ny - 1) * sx : 0);
-        double pm = 0.0;
+        // a thread's products of one unit summed in the storage type (FP32 in
+        // the mixed form: the FP64 units of GB300 are a small fraction of its
+        // FP32 rate), the block tree and the case total in FP64
+        T pm = T(0);
         for (int kb = cl.k0; kb <= cl.k1; kb += COL_G) {
             const int q0 = (int)g.at(cl.i, cl.j, kb);
             const int np = min(COL_G, cl.k1 - kb + 1);
@@ -345,10 +348,10 @@ __global__ void __launch_bounds__(NTHREADS, 4) k_cgi_A(const CaseDev<T> *__restr
                 const T m = pc - vxp[t] * cxp[t] - vxm[t] * cxm[t] - vyp[t] * cyp[t] - vym[t] * cym[t] -
                             pz[t + 2] * sk[t + 1] - pz[t] * sk[t];
                 mp[q0 + t * sxy] = m;
-                pm += (double)pc * (double)m;
+                pm += pc * m;
             }
         }
-        double vals[1] = {pm};
+        double vals[1] = {(double)pm};
         unit_partial<T, 1>(c, u, vals);
     }, [&](int id, int cnt) {
         const CaseDev<T> &c = cs[id];
@@ -390,7 +393,7 @@ __global__ void __launch_bounds__(NTHREADS) k_cgi_B(const CaseDev<T> *__restrict
         T *__restrict__ f0 = (MODE == 2) ? c.mg[0].f : nullptr;
         const Column cl = column_of(g, u);
         long long q = g.at(cl.i, cl.j, cl.k0);
-        double rr = 0.0;
+        T rr = T(0);
 #pragma unroll 2
         for (int k = cl.k0; k <= cl.k1; ++k, q += g.sxy) {
             const T en = e[q] - alpha * p[q];
@@ -400,10 +403,10 @@ __global__ void __launch_bounds__(NTHREADS) k_cgi_B(const CaseDev<T> *__restrict
                 e[q] = en;
                 r[q] = rn;
                 if (MODE == 2) f0[q] = fn;
-                rr += (double)rn * (double)rn;
+                rr += rn * rn;
             }
         }
-        double vals[1] = {rr};
+        double vals[1] = {(double)rr};
         unit_partial<T, 1>(c, u, vals);
     }, [&](int id, int cnt) {
         const CaseDev<T> &c = cs[id];
@@ -471,13 +474,13 @@ __global__ void __launch_bounds__(NTHREADS) k_pcg_dot(const CaseDev<T> *__restri
         const T *__restrict__ r = c.r;
         const Column cl = column_of(g, u);
         long long q = g.at(cl.i, cl.j, cl.k0);
-        double rz = 0.0;
+        T rz = T(0);
 #pragma unroll 4
         for (int k = cl.k0; k <= cl.k1; ++k, q += g.sxy) {
             const T z = sqrt(dpr[q]) * z0[q];
-            if (cl.v) rz += (double)z * (double)r[q];
+            if (cl.v) rz += z * r[q];
         }
-        double vals[1] = {rz};
+        double vals[1] = {(double)rz};
         unit_partial<T, 1>(c, u, vals);
     }, [&](int id, int cnt) {
         const CaseDev<T> &c = cs[id];
