@@ -59,6 +59,8 @@ def parse():
                     help="profiling mode: after the warm-up steps of the mixed form, one launch of kernel K "
                          "(0 CG matrix-vector, 1 smoother half-sweep, 2 CG update) between "
                          "cudaProfilerStart/Stop, for ncu --profile-from-start off; prints its time")
+    ap.add_argument("--mms-steps", type=int, default=100,
+                    help="steps of the manufactured-solution runs at 32^3, 64^3, 128^3 (0: skip)")
     ap.add_argument("--accuracy-steps", type=int, default=200,
                     help="steps of the dam-break mixed-vs-FP64 accuracy run (0: skip)")
     return ap.parse_args()
@@ -245,6 +247,29 @@ def accuracy_run(args):
     return out
 
 
+def mms_run(args):
+    """The manufactured solution (13_mms.f90, steady) at 32^3, 64^3, 128^3 in
+    both forms, args.mms_steps steps each, outside any timed region: RMS
+    error of u, v, w against the analytic fields and the observed order."""
+    from suli_gb300 import cases
+    from suli_gb300._abi import PREC_FP64, PREC_MIXED
+    out = {"steps": args.mms_steps, "errors_uvw": {}}
+    for n in (32, 64, 128):
+        row = {}
+        for name, prec in (("fp64", PREC_FP64), ("mixed", PREC_MIXED)):
+            c = cases.mms_case(n, precision=prec)
+            c.params.mixed_precond = 1 if args.precond == "multigrid" else 0
+            g = start_gpu([c])
+            g.step(args.mms_steps)
+            row[name] = g.mms_error()[:3]
+            g.close()
+        out["errors_uvw"][str(n)] = row
+    e = out["errors_uvw"]
+    out["observed_order_u"] = {form: [math.log(e[a][form][0] / e[b][form][0], 2) for a, b in (("32", "64"), ("64", "128"))]
+                               for form in ("fp64", "mixed")}
+    return out
+
+
 def e2e_run(args, cs, torch):
     """Per step: pinned host state -> device, one step, device -> host."""
     g = start_gpu(cs)
@@ -421,6 +446,11 @@ def main():
             line["accuracy"] = accuracy_run(args)
         except Exception as e:
             line["accuracy"] = {"error": repr(e)}
+    if args.mms_steps > 0 and rank == 0:
+        try:
+            line["mms"] = mms_run(args)
+        except Exception as e:
+            line["mms"] = {"error": repr(e)}
     if not args.no_e2e:
         try:
             line["e2e"] = e2e_run(args, cs_m, torch)

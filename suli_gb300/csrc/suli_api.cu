@@ -220,6 +220,57 @@ struct Impl : ImplBase {
     int *dact = nullptr;
     double *dstage = nullptr;      // mixed form: FP64 staging of field transfers
     size_t stage_elems = 0;
+    // One preconditioned CG iteration (about 75 kernels: product, update,
+    // V-cycle, r.z, direction) captured per active-table slot and replayed:
+    // the launches are the same every iteration (fixed device pointers and
+    // grids), only the data they find differs.  Captured after an iteration
+    // has run uncaptured (the one-time grid queries are done by then).
+    cudaGraphExec_t pcg_graph[2] = {nullptr, nullptr};
+    unsigned long long pcg_graph_kernels = 0;
+    bool pcg_plain_done = false;
+    int use_graphs = -1;
+
+    // n preconditioned iterations from table `slot`; returns the current slot
+    int pcg_iters(int n, int slot)
+    {
+        if (use_graphs < 0) {
+            const char *env = std::getenv("SULI_GRAPHS");
+            use_graphs = (env && std::string(env) == "0") ? 0 : 1;
+        }
+        if (!use_graphs || !pcg_plain_done) {
+            slot = launch_pcg_iters<T>(b, n, slot, st);
+            pcg_plain_done = true;
+            return slot;
+        }
+        for (int q = 0; q < n; ++q) {
+            if (!pcg_graph[slot]) {
+                const unsigned long long before = g_launches.load();
+                cudaGraph_t graph = nullptr;
+                if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+                    cudaGetLastError();
+                    use_graphs = 0;
+                    return launch_pcg_iters<T>(b, n - q, slot, st);
+                }
+                launch_pcg_iters<T>(b, 1, slot, st);
+                cudaError_t e = cudaStreamEndCapture(st, &graph);
+                const unsigned long long captured = g_launches.load() - before;
+                g_launches.fetch_sub(captured);   // captured launches have not run
+                if (e != cudaSuccess || cudaGraphInstantiate(&pcg_graph[slot], graph, 0) != cudaSuccess) {
+                    cudaGetLastError();
+                    if (graph) cudaGraphDestroy(graph);
+                    pcg_graph[slot] = nullptr;
+                    use_graphs = 0;
+                    return launch_pcg_iters<T>(b, n - q, slot, st);
+                }
+                cudaGraphDestroy(graph);
+                pcg_graph_kernels = captured;
+            }
+            if (cudaGraphLaunch(pcg_graph[slot], st) != cudaSuccess) return -1;
+            count_launch(pcg_graph_kernels);
+            slot = 1 - slot;
+        }
+        return slot;
+    }
     cudaStream_t st = nullptr;
 
     ~Impl() override
@@ -232,6 +283,8 @@ struct Impl : ImplBase {
         cudaFree(dact);
         cudaFree(dactdone);
         cudaFree(dstage);
+        for (auto &gx : pcg_graph)
+            if (gx) cudaGraphExecDestroy(gx);
         cudaFree(drk);
         cudaFree(b.dcases);
         if (hsc) cudaFreeHost(hsc);
@@ -832,7 +885,8 @@ struct Impl : ImplBase {
                 }
                 for (; chunk > 0;) {
                     if ((rc = ev_begin())) return rc;
-                    slot = mg ? launch_pcg_iters<T>(b, chunk, slot, st) : launch_cg_iters<T>(b, chunk, slot, 1, st);
+                    slot = mg ? pcg_iters(chunk, slot) : launch_cg_iters<T>(b, chunk, slot, 1, st);
+                    if (slot < 0) return fail(SULI_CUDA_ERROR, "launching the CG iteration graph failed");
                     CKL();
                     if ((rc = ev_end())) return rc;
                     done += chunk;
