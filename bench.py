@@ -287,23 +287,20 @@ def e2e_run(args, cs, torch):
             h2d += a.nbytes
         host.append(d)
     g.synchronize()
+    items = [(n, c, a) for c, d in enumerate(host) for n, a in d.items()]
     ksteps = max(1, min(args.steps, 3))
     t0 = time.perf_counter()
     for _ in range(ksteps):
-        for c, d in enumerate(host):
-            for n, a in d.items():
-                g.upload(n, a, c)
+        g.upload_many(items)       # every field of every case, one call
         g.step(1)
-        for c, d in enumerate(host):
-            for n in d:
-                d[n][...] = g.download(n, c)
+        g.download_many(items)
     g.synchronize()
     dt = time.perf_counter() - t0
     cells = sum(c.cells for c in cs)
     g.close()
     return {"value": cells * ksteps / dt, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": h2d, "steps": ksteps,
-            "path": "suli_upload_field/suli_step/suli_download_field, pinned host buffers"}
+            "path": "suli_upload_fields/suli_step/suli_download_fields (C ABI), pinned host buffers"}
 
 
 def cpu_baseline(args, cs):

@@ -174,6 +174,14 @@ int suli_destroy(suli_handle *h);
  * int32 for id_ibm*, double otherwise (the mixed form converts). */
 int suli_upload_field(suli_handle *h, int icase, int field, const void *host);
 int suli_download_field(suli_handle *h, int icase, int field, void *host);
+/* The same copies for n (case, field, buffer) triples in one call: all are
+ * queued on the handle's stream and the call synchronises once, at its end
+ * (the per-field calls synchronise each).  The buffers must stay valid until
+ * the call returns.  For a host that moves a batch's state every step (the
+ * reference keeps everything in host memory, so it has no counterpart). */
+int suli_upload_fields(suli_handle *h, int n, const int32_t *cases, const int32_t *fields,
+                       const void *const *host);
+int suli_download_fields(suli_handle *h, int n, const int32_t *cases, const int32_t *fields, void *const *host);
 int suli_set_scalar(suli_handle *h, int icase, int scalar, double value);
 int suli_get_scalar(suli_handle *h, int icase, int scalar, double *value);
 

@@ -137,6 +137,7 @@ static int validate(const suli_params &p)
 struct ImplBase {
     virtual ~ImplBase() {}
     virtual int copy_field(int icase, int f, void *host, bool up) = 0;
+    virtual int copy_fields(int n, const int32_t *cases, const int32_t *fields, void *const *hosts, bool up) = 0;
     virtual int heaviside_init() = 0;
     virtual int level_set() = 0;
     virtual int contorno(int nlock) = 0;
@@ -626,7 +627,44 @@ struct Impl : ImplBase {
         }
     }
 
+    // one field transfer, synchronous: the caller may reuse its buffer (or
+    // read the data) once the call returns
     int copy_field(int icase, int f, void *host, bool up) override
+    {
+        bool p64reset = false;
+        int rc = enqueue_copy(icase, f, host, up, p64reset);
+        if (rc) return rc;
+        CK(cudaStreamSynchronize(st));
+        // a pressure from the host replaces the FP64 pressure of the last solve
+        if (p64reset) return write_case_scalar(icase, S_P64OK, 0.0);
+        return SULI_OK;
+    }
+
+    // several transfers queued on the library's stream, one synchronisation
+    int copy_fields(int n, const int32_t *cases, const int32_t *fields, void *const *hosts, bool up) override
+    {
+        if (n < 0 || (n > 0 && (!cases || !fields || !hosts))) return fail(SULI_BAD_ARG, "bad transfer list");
+        std::vector<int> reset;
+        for (int q = 0; q < n; ++q) {
+            if (!hosts[q]) return fail(SULI_BAD_ARG, "null host pointer");
+            bool p64reset = false;
+            int rc = enqueue_copy(cases[q], fields[q], hosts[q], up, p64reset);
+            if (rc) {
+                cudaStreamSynchronize(st);
+                return rc;
+            }
+            if (p64reset) reset.push_back(cases[q]);
+        }
+        CK(cudaStreamSynchronize(st));
+        for (int c : reset) {
+            int rc = write_case_scalar(c, S_P64OK, 0.0);
+            if (rc) return rc;
+        }
+        return SULI_OK;
+    }
+
+    // queue one transfer on the library's stream (no synchronisation)
+    int enqueue_copy(int icase, int f, void *host, bool up, bool &p64reset)
     {
         if (icase < 0 || icase >= ncases) return fail(SULI_BAD_ARG, "case index out of range");
         int lo[3], hi[3];
@@ -655,13 +693,7 @@ struct Impl : ImplBase {
                     k_unpack_field<double><<<nb, 256, 0, st>>>(dstage, master, (long long)n, (int)e0, (int)e1, lo[0],
                                                                lo[1], lo[2], (long long)dpitch_el, (long long)dheight);
                 CKL();
-                // the caller may reuse its buffer once the call returns
-                CK(cudaStreamSynchronize(st));
-                if (f == SULI_F_PRD1) {
-                    // a pressure from the host replaces the FP64 pressure of the last solve
-                    int rc2 = write_case_scalar(icase, S_P64OK, 0.0);
-                    if (rc2) return rc2;
-                }
+                p64reset = (f == SULI_F_PRD1);
             } else {
                 if (master)
                     k_pack_field<double><<<nb, 256, 0, st>>>(master, dstage, (long long)n, (int)e0, (int)e1, lo[0],
@@ -671,7 +703,6 @@ struct Impl : ImplBase {
                                                         lo[1], lo[2], (long long)dpitch_el, (long long)dheight);
                 CKL();
                 CK(cudaMemcpyAsync(host, dstage, n * sizeof(double), cudaMemcpyDeviceToHost, st));
-                CK(cudaStreamSynchronize(st));
             }
             return SULI_OK;
         }
@@ -694,7 +725,6 @@ struct Impl : ImplBase {
             m.kind = cudaMemcpyDeviceToHost;
         }
         CK(cudaMemcpy3DAsync(&m, st));
-        CK(cudaStreamSynchronize(st));
         return SULI_OK;
     }
 
@@ -1061,6 +1091,20 @@ extern "C" int suli_download_field(suli_handle *h, int icase, int field, void *h
     HCHK();
     if (!host) return fail(SULI_BAD_ARG, "null host pointer");
     return h->impl->copy_field(icase, field, host, false);
+}
+
+extern "C" int suli_upload_fields(suli_handle *h, int n, const int32_t *cases, const int32_t *fields,
+                                  const void *const *host)
+{
+    HCHK();
+    return h->impl->copy_fields(n, cases, fields, const_cast<void *const *>(host), true);
+}
+
+extern "C" int suli_download_fields(suli_handle *h, int n, const int32_t *cases, const int32_t *fields,
+                                    void *const *host)
+{
+    HCHK();
+    return h->impl->copy_fields(n, cases, fields, host, false);
 }
 
 extern "C" int suli_set_scalar(suli_handle *h, int icase, int s, double v)

@@ -28,7 +28,8 @@ EXPORTS = [
     "suli_convdiff", "suli_complementos", "suli_tempo", "suli_graddin", "suli_posdin", "suli_conmassa",
     "suli_mms_error", "suli_set_stage", "suli_step", "suli_diagnostics", "suli_synchronize",
     "suli_last_error", "suli_device_info", "suli_get_stream", "suli_profile", "suli_profile_read",
-    "suli_ibm_setup", "suli_conmassa_noalloc", "suli_time_kernel",
+    "suli_ibm_setup", "suli_conmassa_noalloc", "suli_time_kernel", "suli_upload_fields",
+    "suli_download_fields",
 ]
 
 
@@ -82,6 +83,8 @@ def load_library(path: str = LIB_PATH):
     L.suli_get_stream.argtypes = [C.c_void_p, P(C.c_void_p)]
     L.suli_profile.argtypes = [C.c_void_p, C.c_int]
     L.suli_profile_read.argtypes = [C.c_void_p, P(SuliProfile)]
+    L.suli_upload_fields.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.suli_download_fields.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
     L.suli_time_kernel.argtypes = [C.c_void_p, C.c_int, C.c_int, P(C.c_double), P(C.c_double)]
     L.suli_conmassa_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, i32, i32, i32, C.c_double,
                                         C.c_double, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]
@@ -156,6 +159,34 @@ class SuliGPU:
         a = np.zeros(field_shape(p, name), dtype=dt, order="F")
         _check(load_library().suli_download_field(self._h, case, FIELD_ID[name], a.ctypes.data))
         return a
+
+    def _batch(self, items, up):
+        """items: (field name, case, array) with each array already in the
+        field's Fortran-order shape and dtype (it is used in place, so a
+        pinned buffer stays pinned)."""
+        n = len(items)
+        cases = (C.c_int32 * n)()
+        fields = (C.c_int32 * n)()
+        ptrs = (C.c_void_p * n)()
+        for q, (name, case, a) in enumerate(items):
+            p = self.params[case]
+            dt = np.int32 if name in INT_FIELDS else np.float64
+            if a.dtype != dt or tuple(a.shape) != tuple(field_shape(p, name)) or not a.flags.f_contiguous:
+                raise ValueError("%s of case %d: need a Fortran-order %s array of shape %s"
+                                 % (name, case, np.dtype(dt).name, field_shape(p, name)))
+            cases[q] = case
+            fields[q] = FIELD_ID[name]
+            ptrs[q] = a.ctypes.data
+        fn = load_library().suli_upload_fields if up else load_library().suli_download_fields
+        _check(fn(self._h, n, cases, fields, ptrs))
+
+    def upload_many(self, items):
+        """Upload (field name, case, array) triples in one call (one sync)."""
+        self._batch(items, True)
+
+    def download_many(self, items):
+        """Download into (field name, case, array) triples in one call."""
+        self._batch(items, False)
 
     def scalar(self, name: str, case: int = 0) -> float:
         v = C.c_double()

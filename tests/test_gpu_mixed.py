@@ -1,6 +1,8 @@
-"""The mixed form (FP32 storage and stencils, restarted FP32 CG passes inside
-FP64 iterative refinement, FP64 sums) against the FP64 oracle, and the batched form (uneven
-cases in one launch) against single-case runs."""
+"""The mixed form (FP32 storage and stencils, FP32 pressure passes --
+multigrid-preconditioned or Jacobi-scaled CG -- inside FP64 iterative
+refinement, FP64 masters of the accumulated state, FP64 sums) against the
+FP64 oracle; the batched form (uneven cases in one launch) against single-case
+runs; the batched host transfers against the per-field ones."""
 import numpy as np
 import pytest
 
@@ -140,3 +142,31 @@ def test_multigrid_passes_match_jacobi_passes(gpu_lib, mk):
     ub = np.concatenate([b.ravel() for b in res[1][1]])
     assert rel_l2(ua, ub) < 1e-5
     assert sum(res[1][2]) < sum(res[0][2]), (res[0][2], res[1][2])
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batched_transfers_match_single(gpu_lib, precision):
+    """suli_upload_fields / suli_download_fields (one call, one sync) move the
+    same bits as the per-field calls, in both forms and across cases."""
+    dims, hcol, amp = cases.ensemble_dims(3, seed=5, lo=12, hi=20)
+    cs = [cases.ensemble_case(i, dims, hcol, amp, precision=precision) for i in range(3)]
+    g = gpu_lib.SuliGPU([c.params for c in cs])
+    g.start([c.fields for c in cs])
+    g.step(1)
+    names = ("U", "V", "W", "LS", "PRD1", "ID_IBM")
+    single = {(n, i): g.download(n, i) for i in range(3) for n in names}
+    out = {k: np.zeros_like(v, order="F") for k, v in single.items()}
+    g.download_many([(n, i, out[(n, i)]) for (n, i) in out])
+    for k in single:
+        assert np.array_equal(out[k], single[k]), k
+    # upload changed fields in one call, read back one by one
+    rng = np.random.default_rng(3)
+    new = {k: np.asfortranarray(v + rng.standard_normal(v.shape)) for k, v in single.items() if k[0] != "ID_IBM"}
+    g.upload_many([(n, i, a) for (n, i), a in new.items()])
+    for (n, i), a in new.items():
+        b = g.download(n, i)
+        if precision == 0 or n in ("U", "V", "W", "LS"):   # FP64 form, or FP64 masters
+            assert np.array_equal(b, a), (n, i)
+        else:                                              # FP32 storage
+            assert np.array_equal(b, a.astype(np.float32).astype(np.float64)), (n, i)
+    g.close()
