@@ -28,6 +28,8 @@
 // cases that have converged cost nothing.
 #include "suli_kernels.cuh"
 
+#include <cstdlib>
+
 namespace suli {
 
 #define LAT(arr, i, j, k) (arr)[g.at((i), (j), (k))]
@@ -326,8 +328,16 @@ template <typename T> void launch_mg_vcycle(const Batch<T> &b, const int *tab, i
     static const int gR = occupancy_grid((const void *)k_mg_restrict<T>);
     static const int gP = occupancy_grid((const void *)k_mg_prolong<T>);
     const int N = b.ncases, NL = b.nlev;
-    const int nu = 2, ncoarse = 6;
+    // sweeps before and after the coarse correction: two on every level, the
+    // case grid's count settable (SULI_MG_NU0 = 1 or 2) to trade smoothing
+    // work on the largest level against iterations
+    static const int nu0 = [] {
+        const char *e = std::getenv("SULI_MG_NU0");
+        return (e && std::atoi(e) == 1) ? 1 : 2;
+    }();
+    const int ncoarse = 6;
     for (int l = 0; l + 1 < NL; ++l) {
+        const int nu = (l == 0) ? nu0 : 2;
         for (int it = 0; it < nu; ++it) {
             k_mg_smooth<T><<<gS, b.cblock(), 0, s>>>(b.dcases, tab, N, l, 0, it == 0);
             k_mg_smooth<T><<<gS, b.cblock(), 0, s>>>(b.dcases, tab, N, l, 1, 0);
@@ -342,6 +352,7 @@ template <typename T> void launch_mg_vcycle(const Batch<T> &b, const int *tab, i
     count_launch(2 * ncoarse);
     for (int l = NL - 2; l >= 0; --l) {
         k_mg_prolong<T><<<gP, b.cblock(), 0, s>>>(b.dcases, tab, N, l);
+        const int nu = (l == 0) ? nu0 : 2;
         for (int it = 0; it < nu; ++it) {
             k_mg_smooth<T><<<gS, b.cblock(), 0, s>>>(b.dcases, tab, N, l, 1, 0);
             k_mg_smooth<T><<<gS, b.cblock(), 0, s>>>(b.dcases, tab, N, l, 0, 0);

@@ -422,7 +422,10 @@ struct Impl : ImplBase {
         b.max_plane = maxplane;
         CK(cudaMalloc(&dsc, sizeof(double) * S_NSCAL * n));
         CK(cudaMemsetAsync(dsc, 0, sizeof(double) * S_NSCAL * n, st));
-        CK(cudaMalloc(&dpart, sizeof(double) * NSLOT * (size_t)tiles));
+        // reduction partials: one per tile (tile kernels) or one per warp of
+        // a column unit (persistent kernels), whichever needs more
+        const int pstride = std::max(tiles, chunks * (NTHREADS / 32));
+        CK(cudaMalloc(&dpart, sizeof(double) * NSLOT * (size_t)pstride));
         CK(cudaMalloc(&dcnt, sizeof(unsigned) * n));
         CK(cudaMemsetAsync(dcnt, 0, sizeof(unsigned) * n, st));
         // tables 0 and 1: the CG iteration; table 2: single-kernel profiling
@@ -445,6 +448,7 @@ struct Impl : ImplBase {
         for (int c = 0; c < n; ++c) {
             hc[c].sc = dsc + (size_t)c * S_NSCAL;
             hc[c].partials = dpart;
+            hc[c].pstride = pstride;
             hc[c].counter = dcnt + c;
             hc[c].total_tiles = tiles;
         }

@@ -137,7 +137,8 @@ struct CaseDev {
     MgLev<T> mg[MG_MAXL];
     // reductions
     double *sc;                 // S_NSCAL scalars of this case
-    double *partials;           // NSLOT * total_tiles (global base, slot-major)
+    double *partials;           // NSLOT * pstride (global base, slot-major)
+    int pstride;                // slot stride of partials: max(tiles, 8 x column units) of the batch
     unsigned int *counter;      // one per case
     int total_tiles;            // of the whole launch (slot stride)
 };
@@ -230,7 +231,7 @@ __device__ bool unit_reduce(const CaseDev<T> &c, int gunit, int ubegin, int nuni
     int t = tid_lin();
     if (t == 0) {
 #pragma unroll
-        for (int s = 0; s < NS; ++s) c.partials[(long long)s * c.total_tiles + gunit] = bv[s];
+        for (int s = 0; s < NS; ++s) c.partials[(long long)s * c.pstride + gunit] = bv[s];
         __threadfence();
         unsigned prev = atomicAdd(c.counter, 1u);
         amlast = (prev == (unsigned)(nunits - 1));
@@ -242,7 +243,7 @@ __device__ bool unit_reduce(const CaseDev<T> &c, int gunit, int ubegin, int nuni
     for (int s = 0; s < NS; ++s) {
         bool ismax = (maxmask >> s) & 1u;
         double a = ismax ? 0.0 : 0.0;
-        const double *src = c.partials + (long long)s * c.total_tiles + ubegin;
+        const double *src = c.partials + (long long)s * c.pstride + ubegin;
         for (int q = t; q < nunits; q += NTHREADS) {
             double x = __ldcg(src + q);
             a = ismax ? fmax(a, x) : a + x;
@@ -422,43 +423,45 @@ __device__ __forceinline__ void for_active_units_seg(const int *__restrict__ tab
     if (cnt > 0) seg(ids[a], cnt);
 }
 
-// the partials of one column unit (no fence, no counter: see seg_reduce)
+// the partials of one column unit: one per warp (a shuffle sum, no block
+// barrier), at (unit, warp) of the case; no fence, no counter (seg_reduce)
+constexpr int UNIT_WARPS = NTHREADS / 32;
 template <typename T, int NS>
 __device__ __forceinline__ void unit_partial(const CaseDev<T> &c, int u, const double (&vals)[NS])
 {
-    __shared__ double sh[32];
-    double bv[NS];
+    const int t = tid_lin();
 #pragma unroll
-    for (int s = 0; s < NS; ++s) bv[s] = block_sum(vals[s], sh);
-    if (tid_lin() == 0) {
-#pragma unroll
-        for (int s = 0; s < NS; ++s) c.partials[(long long)s * c.total_tiles + c.chunk_begin + u] = bv[s];
+    for (int s = 0; s < NS; ++s) {
+        const double v = warp_sum(vals[s]);
+        if ((t & 31) == 0)
+            c.partials[(long long)s * c.pstride + (long long)(c.chunk_begin + u) * UNIT_WARPS + (t >> 5)] = v;
     }
 }
 
 // end of a segment of `cnt` units of case c: returns true in every thread of
 // the block that completes the case's last unit, with the totals over the
-// case's unit partials (summed in unit order) in tot
+// case's warp partials (summed in (unit, warp) order) in tot
 template <typename T, int NS>
 __device__ bool seg_reduce(const CaseDev<T> &c, int cnt, double (&tot)[NS])
 {
     __shared__ double sh[32];
     __shared__ bool amlast;
     const int t = tid_lin();
+    if ((t & 31) == 0) __threadfence();   // this warp's partials of the segment
     __syncthreads();
     if (t == 0) {
-        __threadfence();
         const unsigned prev = atomicAdd(c.counter, (unsigned)cnt);
         amlast = (prev + (unsigned)cnt == (unsigned)c.nchunks);
     }
     __syncthreads();
     if (!amlast) return false;
     __threadfence();
+    const int np = c.nchunks * UNIT_WARPS;
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
         double a = 0.0;
-        const double *src = c.partials + (long long)s * c.total_tiles + c.chunk_begin;
-        for (int q = t; q < c.nchunks; q += NTHREADS) a += __ldcg(src + q);
+        const double *src = c.partials + (long long)s * c.pstride + (long long)c.chunk_begin * UNIT_WARPS;
+        for (int q = t; q < np; q += NTHREADS) a += __ldcg(src + q);
         tot[s] = block_sum(a, sh);
     }
     if (t == 0) *c.counter = 0u;
