@@ -411,8 +411,14 @@ def main():
              1: "k_mg_smooth on the case grid (one red-black half-sweep)"}[kern]
     ms_k, bytes_k = gm.time_kernel(kern, 20)
     ach = bytes_k / (ms_k / 1e3) / 1e9
+    # DRAM bytes per cell of one launch (dram__bytes_read.sum +
+    # dram__bytes_write.sum over cells) from an ncu capture of the same
+    # kernel on the first 24 cases of this ensemble; times this workload's cells
+    traffic_per_cell = {0: 166.6e6 / 6914626, 1: 233.2e6 / 6914626}[kern]
     line["roofline"] = {"bound": "hbm", "kernel": kname, "achieved": ach, "peak": peak, "unit": "GB/s",
-                        "frac": ach / peak, "traffic": None, "peak_source": peak_src,
+                        "frac": ach / peak, "traffic": traffic_per_cell * cells,
+                        "traffic_source": "ncu capture on the 24-case ensemble, bytes per cell x cells",
+                        "peak_source": peak_src,
                         "algorithmic_bytes_per_launch": bytes_k, "ms_per_launch": ms_k,
                         "timing": "kernel alone, 20 launches between CUDA events, all cases of the workload"}
     ms_a, bytes_a = gm.time_kernel(0, 20)
