@@ -586,15 +586,31 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_true_residual(const CaseDev<T> 
     if (i <= nx && j <= ny && k <= nz) {
         long long q = g.at(i, j, k);
         const double *e = c.e64;
-        auto E = [&](int a, int b2, int d) -> double {
-            int ma = bmap(a, nx, px), mb = bmap(b2, ny, py), md = bmap(d, nz, false);
-            if (first && !(ma == a && mb == b2 && md == d))
-                return (double)AT(c.prd1, a, b2, d) * sqrt(AT(c.dpr64, ma, mb, md));
-            return AT(e, ma, mb, md);
-        };
-        double r = E(i, j, k) - c.spi64[q + 1] * E(i + 1, j, k) - c.spi64[q] * E(i - 1, j, k) -
-                   c.spj64[q + g.sx] * E(i, j + 1, k) - c.spj64[q] * E(i, j - 1, k) -
-                   c.spk64[q + g.sxy] * E(i, j, k + 1) - c.spk64[q] * E(i, j, k - 1) - c.qpr64[q];
+        double r;
+        if (first) {
+            // the solve's first residual: ghost values from prd1 as the
+            // reference's warm start has them (matepr = prd1 sqrt(matdpr))
+            auto E = [&](int a, int b2, int d) -> double {
+                int ma = bmap(a, nx, px), mb = bmap(b2, ny, py), md = bmap(d, nz, false);
+                if (!(ma == a && mb == b2 && md == d))
+                    return (double)AT(c.prd1, a, b2, d) * sqrt(AT(c.dpr64, ma, mb, md));
+                return AT(e, ma, mb, md);
+            };
+            r = E(i, j, k) - c.spi64[q + 1] * E(i + 1, j, k) - c.spi64[q] * E(i - 1, j, k) -
+                c.spj64[q + g.sx] * E(i, j + 1, k) - c.spj64[q] * E(i, j - 1, k) -
+                c.spk64[q + g.sxy] * E(i, j, k + 1) - c.spk64[q] * E(i, j, k - 1) - c.qpr64[q];
+        } else {
+            // later passes: Neumann neighbours are the cell itself, periodic
+            // ones the opposite end -- fixed offsets, no branch
+            const long long qxp = (i < nx) ? q + 1 : (px ? q - (nx - 1) : q);
+            const long long qxm = (i > 1) ? q - 1 : (px ? q + (nx - 1) : q);
+            const long long qyp = (j < ny) ? q + g.sx : (py ? q - (long long)(ny - 1) * g.sx : q);
+            const long long qym = (j > 1) ? q - g.sx : (py ? q + (long long)(ny - 1) * g.sx : q);
+            const long long qzp = (k < nz) ? q + g.sxy : q;
+            const long long qzm = (k > 1) ? q - g.sxy : q;
+            r = e[q] - c.spi64[q + 1] * e[qxp] - c.spi64[q] * e[qxm] - c.spj64[q + g.sx] * e[qyp] -
+                c.spj64[q] * e[qym] - c.spk64[q + g.sxy] * e[qzp] - c.spk64[q] * e[qzm] - c.qpr64[q];
+        }
         T r32 = T(r);
         c.r[q] = r32;
         c.p[q] = r32;
@@ -623,7 +639,7 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_true_residual(const CaseDev<T> 
         // inner target: a residual reduction of 1e3 (Jacobi-scaled passes) or
         // 1e4 (multigrid-preconditioned passes), but no further than half the
         // outer target; a pass also ends after MG_PASS_MAX iterations
-        c.sc[S_RRREF] = fmax((c.nlev > 0 ? 1e-8 : 1e-6) * tot[1], 0.25 * c.sc[S_THR]);
+        c.sc[S_RRREF] = fmax((c.nlev > 0 ? 1e-10 : 1e-6) * tot[1], 0.25 * c.sc[S_THR]);
         c.sc[S_PASS0] = c.sc[S_CGITER];
         if (conv) {
             c.sc[S_OUTER] = -passes;           // negative: done after `passes` FP64 residuals

@@ -32,33 +32,6 @@
 
 namespace suli {
 
-#define LAT(arr, i, j, k) (arr)[g.at((i), (j), (k))]
-
-// sum of c_f z_nb over the faces of cell (i,j,k); `smooth` drops the wrap
-// couplings of odd periodic dimensions (see above)
-template <typename T>
-__device__ __forceinline__ T mg_nbsum(const MgLev<T> &L, int i, int j, int k, long long q, bool px, bool py,
-                                      bool smooth)
-{
-    const Geo &g = L.g;
-    const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const T *z = L.z;
-    const bool wx = px && !(smooth && (nx & 1)) && nx > 1;
-    const bool wy = py && !(smooth && (ny & 1)) && ny > 1;
-    T s = T(0);
-    // x faces: face i (to i-1) and face i+1 (to i+1)
-    if (i > 1) s += L.cx[q] * z[q - 1];
-    else if (wx) s += L.cx[q] * LAT(z, nx, j, k);
-    if (i < nx) s += L.cx[q + 1] * z[q + 1];
-    else if (wx) s += L.cx[q + 1] * LAT(z, 1, j, k);
-    if (j > 1) s += L.cy[q] * z[q - g.sx];
-    else if (wy) s += L.cy[q] * LAT(z, i, ny, k);
-    if (j < ny) s += L.cy[q + g.sx] * z[q + g.sx];
-    else if (wy) s += L.cy[q + g.sx] * LAT(z, i, 1, k);
-    if (k > 1) s += L.cz[q] * z[q - g.sxy];
-    if (k < nz) s += L.cz[q + g.sxy] * z[q + g.sxy];
-    return s;
-}
 
 // one colour of red-black Gauss-Seidel on L z = f; zero != 0: the sweep
 // starts from z = 0 (this colour gets f / dg, the other colour 0).  The cells
@@ -187,21 +160,28 @@ __global__ void __launch_bounds__(NTHREADS) k_mg_restrict(const CaseDev<T> *__re
         int I, J, K;
         tile_cell(C.ntx, C.nty, lt, I, J, K);
         if (I > C.g.nx || J > C.g.ny || K > C.g.nz) return;
-        const bool px = c.ccx0 == 0, py = c.ccy0 == 0;
+        // the full operator (wrap kept on any periodic length); a wall
+        // neighbour is a never-written ghost of z (zero) against a zero
+        // conductance, and a child beyond an odd fine size is read at a
+        // clamped cell and weighted out, so the eight loads need no branch
+        const int fx = F.g.nx, fy = F.g.ny, fz = F.g.nz;
+        const int sx = (int)F.g.sx, sxy = (int)F.g.sxy;
+        const bool wx = c.ccx0 == 0 && fx > 1, wy = c.ccy0 == 0 && fy > 1;
+        const T *__restrict__ z = F.z;
         T acc = T(0);
-        for (int dk = 0; dk < 2; ++dk) {
-            const int k = 2 * K - 1 + dk;
-            if (k > F.g.nz) continue;
-            for (int dj = 0; dj < 2; ++dj) {
-                const int j = 2 * J - 1 + dj;
-                if (j > F.g.ny) continue;
-                for (int di = 0; di < 2; ++di) {
-                    const int i = 2 * I - 1 + di;
-                    if (i > F.g.nx) continue;
-                    const long long q = F.g.at(i, j, k);
-                    acc += F.f[q] - F.dg[q] * F.z[q] + mg_nbsum(F, i, j, k, q, px, py, false);
-                }
-            }
+#pragma unroll
+        for (int d = 0; d < 8; ++d) {
+            const int i0 = 2 * I - 1 + (d & 1), j0 = 2 * J - 1 + ((d >> 1) & 1), k0 = 2 * K - 1 + (d >> 2);
+            const bool in = i0 <= fx && j0 <= fy && k0 <= fz;
+            const int i = min(i0, fx), j = min(j0, fy), k = min(k0, fz);
+            const int q = (int)F.g.at(i, j, k);
+            const int qxm = (wx && i == 1) ? q + (fx - 1) : q - 1;
+            const int qxp = (wx && i == fx) ? q - (fx - 1) : q + 1;
+            const int qym = (wy && j == 1) ? q + (fy - 1) * sx : q - sx;
+            const int qyp = (wy && j == fy) ? q - (fy - 1) * sx : q + sx;
+            const T r = F.f[q] - F.dg[q] * z[q] + F.cx[q] * z[qxm] + F.cx[q + 1] * z[qxp] + F.cy[q] * z[qym] +
+                        F.cy[q + sx] * z[qyp] + F.cz[q] * z[q - sxy] + F.cz[q + sxy] * z[q + sxy];
+            acc += in ? r : T(0);
         }
         C.f[C.g.at(I, J, K)] = acc;
     });
