@@ -57,7 +57,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--profile-kernel", type=int, default=-1,
                     help="profiling mode: after the warm-up steps of the mixed form, one launch of kernel K "
-                         "(0 CG matrix-vector, 1 smoother half-sweep, 2 CG update) between "
+                         "(0 CG matrix-vector, 1 smoother half-sweep, 2 CG update, 3 one-pass smoother sweep) between "
                          "cudaProfilerStart/Stop, for ncu --profile-from-start off; prints its time")
     ap.add_argument("--mms-steps", type=int, default=100,
                     help="steps of the manufactured-solution runs at 32^3, 64^3, 128^3 (0: skip)")
@@ -406,17 +406,22 @@ def main():
     }
     # roofline of the dominant kernel, timed alone over every case of the
     # workload with CUDA events on the library's stream (burst peak)
-    kern = 1 if args.precond == "multigrid" else 0
+    if args.precond == "multigrid":
+        kern = 1 if os.environ.get("SULI_MG_FUSED") == "0" else 3
+    else:
+        kern = 0
     kname = {0: "k_cgi_A (CG matrix-vector product + p.Ap)",
-             1: "k_mg_smooth on the case grid (one red-black half-sweep)"}[kern]
+             1: "k_mg_smooth on the case grid (one red-black half-sweep)",
+             3: "k_mg_sweep0 on the case grid (one whole red-black sweep in one pass)"}[kern]
     ms_k, bytes_k = gm.time_kernel(kern, 20)
     ach = bytes_k / (ms_k / 1e3) / 1e9
     # DRAM bytes per cell of one launch (dram__bytes_read.sum +
     # dram__bytes_write.sum over cells) from an ncu capture of the same
     # kernel on the first 24 cases of this ensemble; times this workload's cells
-    traffic_per_cell = {0: 166.6e6 / 6914626, 1: 233.2e6 / 6914626}[kern]
+    traffic_per_cell = {0: 166.6e6 / 6914626, 1: 233.2e6 / 6914626, 3: 362.5e6 / 6914626}[kern]
     line["roofline"] = {"bound": "hbm", "kernel": kname, "achieved": ach, "peak": peak, "unit": "GB/s",
-                        "frac": ach / peak, "traffic": traffic_per_cell * cells,
+                        "frac": ach / peak,
+                        "traffic": traffic_per_cell * cells if traffic_per_cell is not None else None,
                         "traffic_source": "ncu capture on the 24-case ensemble, bytes per cell x cells",
                         "peak_source": peak_src,
                         "algorithmic_bytes_per_launch": bytes_k, "ms_per_launch": ms_k,

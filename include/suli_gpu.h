@@ -42,6 +42,9 @@ extern "C" {
 #define SULI_CUDA_ERROR      6
 #define SULI_NO_DEVICE       7
 #define SULI_OUT_OF_MEMORY   8
+#define SULI_CG_STALLED      9  /* warning (mixed form, no counterpart in the reference): the FP64
+                                   residual of the pressure refinement stopped falling before the
+                                   tolerance; the solve kept its best iterate */
 
 /* ---- precision of a case ----------------------------------------------- */
 #define SULI_PREC_FP64   0  /* plain form: FP64 storage and arithmetic */
@@ -237,7 +240,9 @@ int suli_profile_read(suli_handle *h, suli_profile_t *out);
  * over every case of the handle, `reps` launches between CUDA events on the
  * handle's stream.  kernel 0: the CG matrix-vector product (k_cgi_A),
  * 1: one red half-sweep of the multigrid smoother on the case grid (mixed form
- * with mixed_precond = 1 only), 2: the CG direction update (k_cgi_C).
+ * with mixed_precond = 1 only), 2: the CG direction update (k_cgi_C),
+ * 3: one whole one-pass red-black sweep of the smoother on the case grid
+ * (mixed form with mixed_precond = 1 only).
  * Returns the mean time per launch and the algorithmic bytes one launch
  * moves.  The solver work arrays it touches are rebuilt by the next
  * suli_graddin. */

@@ -16,6 +16,7 @@ SULI_BAD_ARG = 5
 SULI_CUDA_ERROR = 6
 SULI_NO_DEVICE = 7
 SULI_OUT_OF_MEMORY = 8
+SULI_CG_STALLED = 9
 
 PREC_FP64 = 0
 PREC_MIXED = 1

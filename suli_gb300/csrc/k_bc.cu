@@ -18,14 +18,14 @@ namespace suli {
 
 #define AT(arr, i, j, k) (arr)[g.at((i), (j), (k))]
 
-template <typename T>
-__global__ void k_bc_phase(const CaseDev<T> *__restrict__ cs, int ncases, int phase)
+// one phase on velocity arrays u, v, w of value type V and (p != nullptr)
+// the pressure
+template <typename T, typename V>
+__device__ __forceinline__ void bc_phase(const CaseDev<T> &c, int phase, V *u, V *v, V *w, V *p)
 {
-    const CaseDev<T> &c = cs[blockIdx.y];
     const Geo &g = c.g;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     const int nx1 = nx + 1, ny1 = ny + 1, nz1 = nz + 1;
-    T *u = c.u, *v = c.v, *w = c.w, *p = c.prd1;
     const bool perx = (c.ccx0 == 0 && c.ccxf == 0);
     const bool pery = (c.ccy0 == 0 && c.ccyf == 0);
     long long nvel, nprd;
@@ -33,6 +33,7 @@ __global__ void k_bc_phase(const CaseDev<T> *__restrict__ cs, int ncases, int ph
     else if (phase == 1) { nvel = (long long)(nx + 3) * (ny + 3); nprd = (long long)(nx + 2) * (nz + 2); }
     else if (phase == 2) { nvel = (long long)(ny + 3) * (nz + 3); nprd = (long long)(nx + 2) * (ny + 2); }
     else { nvel = (long long)(nx + 2) * (nz + 2) + (long long)(nx + 2) * (ny + 2) + (long long)(ny + 2) * (nz + 2); nprd = 0; }
+    if (p == nullptr) nprd = 0;
     const long long ntot = nvel > nprd ? nvel : nprd;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ntot; t += (long long)gridDim.x * blockDim.x) {
         // ---- pressure ghosts (:99-116): x in phase 0, y in phase 1, z in phase 2
@@ -132,11 +133,11 @@ __global__ void k_bc_phase(const CaseDev<T> *__restrict__ cs, int ncases, int ph
                 if (iw) AT(w, 0, j, k) = -AT(w, 1, j, k);
             }
             if (c.ccx0 == 3) {       // prescribed: bxy0 = bxz0 = 0 (2_iniciais.f90:384-385); u by k_inflow
-                if (iv) AT(v, 0, j, k) = T(0.);
-                if (iw) AT(w, 0, j, k) = T(0.);
+                if (iv) AT(v, 0, j, k) = V(0.);
+                if (iw) AT(w, 0, j, k) = V(0.);
             }
             if (c.ccx0 == 4) {       // validation inflow (:333-348)
-                if (iv) AT(v, 0, j, k) = T(0.);
+                if (iv) AT(v, 0, j, k) = V(0.);
                 if (iw) AT(w, 0, j, k) = AT(w, 1, j, k);
             }
             // x = lx wall (:350-384)
@@ -167,24 +168,40 @@ __global__ void k_bc_phase(const CaseDev<T> *__restrict__ cs, int ncases, int ph
             if (t < nvp) {
                 int i = (int)(t % (nx + 2)), k = (int)(t / (nx + 2));
                 if (pery) AT(v, i, 1, k) = AT(v, i, ny1, k);
-                if (c.ccy0 == 1 || c.ccy0 == 2) AT(v, i, 1, k) = T(0.);
+                if (c.ccy0 == 1 || c.ccy0 == 2) AT(v, i, 1, k) = V(0.);
                 if (pery) AT(v, i, ny1, k) = AT(v, i, 1, k);
-                if (c.ccyf == 1 || c.ccyf == 2) AT(v, i, ny1, k) = T(0.);
+                if (c.ccyf == 1 || c.ccyf == 2) AT(v, i, ny1, k) = V(0.);
             } else if (t < nvp + nwp) {
                 long long s = t - nvp;
                 int i = (int)(s % (nx + 2)), j = (int)(s / (nx + 2));
-                if (c.ccz0 == 1 || c.ccz0 == 2 || c.ccz0 == 4) AT(w, i, j, 1) = T(0.);
-                if (c.cczf == 1 || c.cczf == 2) AT(w, i, j, nz1) = T(0.);
+                if (c.ccz0 == 1 || c.ccz0 == 2 || c.ccz0 == 4) AT(w, i, j, 1) = V(0.);
+                if (c.cczf == 1 || c.cczf == 2) AT(w, i, j, nz1) = V(0.);
             } else {
                 long long s = t - nvp - nwp;
                 int j = (int)(s % (ny + 2)), k = (int)(s / (ny + 2));
                 if (perx) AT(u, 1, j, k) = AT(u, nx1, j, k);
-                if (c.ccx0 == 1 || c.ccx0 == 2) AT(u, 1, j, k) = T(0.);
+                if (c.ccx0 == 1 || c.ccx0 == 2) AT(u, 1, j, k) = V(0.);
                 if (perx) AT(u, nx1, j, k) = AT(u, 1, j, k);
-                if (c.ccxf == 1 || c.ccxf == 2) AT(u, nx1, j, k) = T(0.);
+                if (c.ccxf == 1 || c.ccxf == 2) AT(u, nx1, j, k) = V(0.);
                 if (c.ccxf == 4) AT(u, nx1, j, k) = AT(u, nx1 - 1, j, k);
             }
         }
+    }
+}
+
+// masters != 0: the same fills on the FP64 masters of the mixed form (after
+// they took the values the FP32 fills and the inflow wrote), so that a ghost
+// master is the FP64 copy of the master it mirrors, not a rounded one: the
+// periodic or wall-symmetric sums that cancel in the pressure equation's
+// right-hand side then cancel in FP64 as well
+template <typename T>
+__global__ void k_bc_phase(const CaseDev<T> *__restrict__ cs, int ncases, int phase, int masters)
+{
+    const CaseDev<T> &c = cs[blockIdx.y];
+    if (masters) {
+        if (c.u64 != nullptr) bc_phase<T, double>(c, phase, c.u64, c.v64, c.w64, (double *)nullptr);
+    } else {
+        bc_phase<T, T>(c, phase, c.u, c.v, c.w, c.prd1);
     }
 }
 
@@ -254,19 +271,35 @@ void launch_contorno(const Batch<T> &b, int nlock, cudaStream_t s, unsigned long
     bool inflow = false;
     for (int c = 0; c < b.ncases; ++c) inflow |= (b.hcases[c].ccx0 == 3);
     for (int ph = 0; ph < 3; ++ph) {
-        k_bc_phase<T><<<grid, 256, 0, s>>>(b.dcases, b.ncases, ph); count_launch();
+        k_bc_phase<T><<<grid, 256, 0, s>>>(b.dcases, b.ncases, ph, 0); count_launch();
     }
     if (inflow) {
         k_inflow<T><<<b.ncases, 256, 0, s>>>(b.dcases, b.ncases, 0, 1.0, rng_call); count_launch();
     }
     if (nlock == 2) {
-        k_bc_phase<T><<<grid, 256, 0, s>>>(b.dcases, b.ncases, 3); count_launch();
+        k_bc_phase<T><<<grid, 256, 0, s>>>(b.dcases, b.ncases, 3, 0); count_launch();
         if (inflow) {
             k_inflow<T><<<b.ncases, 256, 0, s>>>(b.dcases, b.ncases, 1, 2.0, rng_call + 1); count_launch();
         }
     }
 }
 
+// the velocity fills of contorno(nlock) on the FP64 masters (mixed form),
+// after the masters took the FP32 results
+template <typename T> void launch_contorno_masters(const Batch<T> &b, int nlock, cudaStream_t s)
+{
+    if (nlock != 1 && nlock != 2) return;
+    int nb = (b.max_plane + 255) / 256;
+    if (nb < 1) nb = 1;
+    if (nb > 1024) nb = 1024;
+    dim3 grid(nb, b.ncases);
+    for (int ph = 0; ph < (nlock == 2 ? 4 : 3); ++ph) {
+        k_bc_phase<T><<<grid, 256, 0, s>>>(b.dcases, b.ncases, ph, 1); count_launch();
+    }
+}
+
+template void launch_contorno_masters<float>(const Batch<float> &, int, cudaStream_t);
+template void launch_contorno_masters<double>(const Batch<double> &, int, cudaStream_t);
 template void launch_contorno<double>(const Batch<double> &, int, cudaStream_t, unsigned long long);
 template void launch_contorno<float>(const Batch<float> &, int, cudaStream_t, unsigned long long);
 

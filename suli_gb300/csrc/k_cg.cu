@@ -142,7 +142,13 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_setup1m(const CaseDev<T> *__res
     if (i == nx) c.spi64[q + 1] = aux1 / icf<double>(nx + 1, nx, px, [&](int m) { return AT(rho, m, j, k); });
     if (j == ny) c.spj64[q + g.sx] = aux2 / icf<double>(ny + 1, ny, false, [&](int m) { return AT(rho, i, m, k); });
     if (k == nz) c.spk64[q + g.sxy] = aux3 / icf<double>(nz + 1, nz, false, [&](int m) { return AT(rho, i, j, m); });
-    double ua = c.u[q], ub = c.u[q + 1], va = c.v[q], vb = c.v[q + g.sx], wa = c.w[q], wb = c.w[q + g.sxy];
+    // the divergence of the FP64 masters: the field that posdin corrects
+    double ua, ub, va, vb, wa, wb;
+    if (c.u64 != nullptr) {
+        ua = c.u64[q]; ub = c.u64[q + 1]; va = c.v64[q]; vb = c.v64[q + g.sx]; wa = c.w64[q]; wb = c.w64[q + g.sxy];
+    } else {
+        ua = c.u[q]; ub = c.u[q + 1]; va = c.v[q]; vb = c.v[q + g.sx]; wa = c.w[q]; wb = c.w[q + g.sxy];
+    }
     if (c.obst_t != 0 && c.ibm_t == 2) {
         if (c.obs_lsx[q] >= T(0.)) ua = 0.;
         if (c.obs_lsx[q + 1] >= T(0.)) ub = 0.;
@@ -185,7 +191,9 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_setup1mb(const CaseDev<T> *__re
         if (i == nx) L.cx[q + 1] = x1;
         if (j == ny) L.cy[q + g.sx] = y1;
         if (k == nz) L.cz[q + g.sxy] = z1;
-        L.dg[q] = x0 + x1 + y0 + y1 + z0 + z1;
+        const T dq = x0 + x1 + y0 + y1 + z0 + z1;
+        L.dg[q] = dq;
+        L.dgi[q] = (dq > T(0)) ? T(1) / dq : T(0);
     }
 }
 
@@ -623,7 +631,13 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_true_residual(const CaseDev<T> 
     double vals[3] = {rr, rr32, bb}, tot[3];
     if (last_block_reduce<T, 3>(c, vals, tot) && tid_lin() == 0) {
         double rrt = tot[0];
+        const double prev = c.sc[S_RRTRUE];
         c.sc[S_RRTRUE] = rrt;
+        // stagnation: FP32 passes cannot lower a residual whose worst mode
+        // has a condition number near 1/eps(FP32); after three passes that
+        // did not halve r.r the case stops with its best iterate
+        const double stall = first ? 0.0 : ((rrt > 0.5 * prev) ? c.sc[S_STALL] + 1.0 : 0.0);
+        c.sc[S_STALL] = stall;
         if (first) {
             double thr;
             if (c.cg_tol_mode == 1) thr = c.cg_tol * c.cg_tol * tot[2];
@@ -634,7 +648,9 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_true_residual(const CaseDev<T> 
             c.sc[S_CGITER] = 0.0;
         }
         double passes = c.sc[S_OUTER] + 1.0;
-        bool conv = !(rrt > c.sc[S_THR]) || c.sc[S_CGITER] >= c.sc[S_CGMAX];
+        const bool stalled = (rrt > c.sc[S_THR]) && stall >= 3.0;
+        c.sc[S_STALLED] = stalled ? 1.0 : 0.0;
+        bool conv = !(rrt > c.sc[S_THR]) || c.sc[S_CGITER] >= c.sc[S_CGMAX] || stalled;
         c.sc[S_RR] = tot[1];
         // inner target: a residual reduction of 1e3 (Jacobi-scaled passes) or
         // 1e4 (multigrid-preconditioned passes), but no further than half the
@@ -733,6 +749,7 @@ template <typename T> int launch_profile_kernel(const Batch<T> &b, int kernel, i
     if (kernel == 0) k_cgi_A<T><<<G.A, b.cblock(), 0, s>>>(b.dcases, tab, b.ncases, S_RR);
     else if (kernel == 1) return launch_mg_smooth0<T>(b, tab, 0, s);
     else if (kernel == 2) k_cgi_C<T><<<G.C, b.cblock(), 0, s>>>(b.dcases, tab, b.ncases);
+    else if (kernel == 3) return launch_mg_sweep0<T>(b, tab, s);
     else return -1;
     count_launch();
     return 0;

@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(NTHREADS, 4) k_mg_smooth(const CaseDev<T> *__r
             const int dym = (wy && j == 1) ? (ny - 1) * isx : -isx;
             const int dyp = (wy && j == ny) ? -(ny - 1) * isx : isx;
             const T *__restrict__ f = L.f;
-            const T *__restrict__ dg = L.dg;
+            const T *__restrict__ dgi = L.dgi;
             const T *__restrict__ cxa = L.cx;
             const T *__restrict__ cya = L.cy;
             const T *__restrict__ cza = L.cz;
@@ -84,7 +84,7 @@ __global__ void __launch_bounds__(NTHREADS, 4) k_mg_smooth(const CaseDev<T> *__r
                 for (int t = 0; t < COL_G; ++t) {
                     const int q = q0 + min(t, np - 1) * isxy;
                     fv[t] = f[q];
-                    dv[t] = dg[q];
+                    dv[t] = dgi[q];
                     a0[t] = cxa[q]; a1[t] = cxa[q + 1]; b0[t] = cya[q]; b1[t] = cya[q + isx];
                     za0[t] = z[q + dxm]; za1[t] = z[q + dxp]; zb0[t] = z[q + dym]; zb1[t] = z[q + dyp];
                 }
@@ -92,15 +92,15 @@ __global__ void __launch_bounds__(NTHREADS, 4) k_mg_smooth(const CaseDev<T> *__r
                 for (int t = 0; t < COL_G; ++t) {
                     if (t >= np || !cl.v) continue;
                     const bool mine = ((i + j + kb + t) & 1) == color;
-                    const T d = dv[t];
+                    const T di = dv[t];
                     T zn;
                     if (zero) {
-                        zn = (mine && d > T(0)) ? fv[t] / d : T(0);
+                        zn = mine ? fv[t] * di : T(0);
                     } else {
                         if (!mine) continue;
                         const T sm = fv[t] + a0[t] * za0[t] + a1[t] * za1[t] + b0[t] * zb0[t] + b1[t] * zb1[t] +
                                      czz[t] * zz[t] + czz[t + 1] * zz[t + 2];
-                        zn = (d > T(0)) ? sm / d : T(0);
+                        zn = sm * di;
                     }
                     zw[q0 + t * isxy] = zn;
                 }
@@ -120,8 +120,8 @@ __global__ void __launch_bounds__(NTHREADS, 4) k_mg_smooth(const CaseDev<T> *__r
 #pragma unroll
                 for (int a = 0; a < UW; ++a) {
                     const bool mine = ((ci[a] + cj[a] + ck[a]) & 1) == color;
-                    const T d = L.dg[q[a]], fv = L.f[q[a]];
-                    zn[a] = (mine && d > T(0)) ? fv / d : T(0);
+                    const T di = L.dgi[q[a]], fv = L.f[q[a]];
+                    zn[a] = mine ? fv * di : T(0);
                     wr[a] = v[a];
                 }
             } else {
@@ -133,10 +133,10 @@ __global__ void __launch_bounds__(NTHREADS, 4) k_mg_smooth(const CaseDev<T> *__r
                     const long long qxp = (wx && i == nx) ? qq - (nx - 1) : qq + 1;
                     const long long qym = (wy && j == 1) ? qq + (long long)(ny - 1) * sx : qq - sx;
                     const long long qyp = (wy && j == ny) ? qq - (long long)(ny - 1) * sx : qq + sx;
-                    const T d = L.dg[qq];
+                    const T di = L.dgi[qq];
                     const T s = L.f[qq] + L.cx[qq] * z[qxm] + L.cx[qq + 1] * z[qxp] + L.cy[qq] * z[qym] +
                                 L.cy[qq + sx] * z[qyp] + L.cz[qq] * z[qq - sxy] + L.cz[qq + sxy] * z[qq + sxy];
-                    zn[a] = (d > T(0)) ? s / d : T(0);
+                    zn[a] = s * di;
                     wr[a] = v[a] && (((i + j + ck[a]) & 1) == color);
                 }
             }
@@ -145,6 +145,232 @@ __global__ void __launch_bounds__(NTHREADS, 4) k_mg_smooth(const CaseDev<T> *__r
                 if (wr[a]) L.z[q[a]] = zn[a];
         }
     });
+}
+
+// One whole red-black sweep of the case grid (level 0) in one pass: colour
+// c1, then colour c2 = 1 - c1, reading z from buffer `src` and writing every
+// cell of the grid to buffer `dst` (0: z, 1: z2; src != dst unless zero, the
+// sweep from z = 0, which reads no z).  A block walks a column unit plane by
+// plane.  For each plane it computes the c1 values on the unit's 34 x 10
+// footprint (the unit and a one-cell ring, wrap neighbours resolved to the
+// cells they stand for) into a three-plane ring in shared memory, and then
+// updates the c2 cells of the plane below from those values.  The ring cells
+// are computed by both blocks that need them, from the same inputs, so the
+// two half-sweeps need one trip through memory instead of two; the results
+// are the two half-sweep launches' (same operands, same order).
+//
+// The inputs of a plane (z over the footprint and one more cell around it,
+// f, dg and the three conductances over the footprint) are staged in shared
+// memory by 16-byte asynchronous copies (cp.async), whole 40-float row
+// segments, in a ring of SW_NS planes issued three planes ahead of the one
+// being computed, so the loads of later planes are in flight while a plane
+// is computed.  Segments outside the case's box are not copied; only cells
+// outside the grid (never used) would read them.  Cells whose stencil
+// crosses a periodic wrap read their operands from global memory instead.
+constexpr int SW_X = COL_X + 2, SW_Y = COL_Y + 2, SW_N = SW_X * SW_Y;
+constexpr int SW_R = 40;                     // floats per staged row segment (10 x 16 B)
+constexpr int SW_ZR = COL_Y + 4;             // rows of z (j0-2 .. j0+9)
+constexpr int SW_CR = COL_Y + 2;             // rows of f, dg, cx, cz (j0-1 .. j0+8)
+constexpr int SW_YR = COL_Y + 3;             // rows of cy (j0-1 .. j0+9)
+constexpr int SW_OZ = 0, SW_OF = SW_OZ + SW_ZR * SW_R, SW_OD = SW_OF + SW_CR * SW_R, SW_OX = SW_OD + SW_CR * SW_R,
+              SW_OY = SW_OX + SW_CR * SW_R, SW_OC = SW_OY + SW_YR * SW_R, SW_STAGE = SW_OC + SW_CR * SW_R;
+constexpr int SW_CHUNKS = SW_STAGE / 4;      // 16-byte copies per plane
+constexpr int SW_NS = 5;                     // planes in the staging ring
+constexpr int SW_SLOTS = (SW_CHUNKS + NTHREADS - 1) / NTHREADS;
+constexpr size_t SW_SMEM = (size_t)SW_NS * SW_STAGE * 4;   // dynamic shared memory (T = float)
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS, 4) k_mg_sweep0(const CaseDev<T> *__restrict__ cs, const int *__restrict__ tab,
+                                                           int N, int c1, int zero, int src, int dst)
+{
+    static_assert(sizeof(T) == 4, "the staged sweep is the FP32 smoother");
+    extern __shared__ __align__(16) unsigned char sw_dyn[];
+    T *stg = reinterpret_cast<T *>(sw_dyn);
+    __shared__ T ring[3][SW_N];
+    const int t = tid_lin();
+    for_active_units(tab, N, 0, [&](int id, int u) {
+        const CaseDev<T> &c = cs[id];
+        const MgLev<T> &L = c.mg[0];
+        const Geo &g = L.g;
+        const int nx = g.nx, ny = g.ny, nz = g.nz;
+        const int isx = (int)g.sx, isxy = (int)g.sxy;
+        const bool wx = c.ccx0 == 0 && !(nx & 1) && nx > 1;
+        const bool wy = c.ccy0 == 0 && !(ny & 1) && ny > 1;
+        const T *__restrict__ zs = src ? L.z2 : L.z;
+        T *__restrict__ zd = dst ? L.z2 : L.z;
+        const int ux = (nx + COL_X - 1) / COL_X, uy = (ny + COL_Y - 1) / COL_Y;
+        const int i0 = 1 + (u % ux) * COL_X, j0 = 1 + ((u / ux) % uy) * COL_Y;
+        const int k0 = 1 + (u / (ux * uy)) * COL_Z, k1 = min(nz, k0 + COL_Z - 1);
+        const int c2 = 1 - c1;
+        const int X0 = i0 - 5;                   // x of a staged row's first float (a multiple of 4)
+        // this thread's copy slots: shared offset in a stage, source address
+        // of plane k0 - 2 (advanced one plane per issue), kind; a segment
+        // outside the box in x or y is never copied
+        int so[SW_SLOTS], sk[SW_SLOTS];
+        const T *gp[SW_SLOTS];
+        bool sv[SW_SLOTS];
+#pragma unroll
+        for (int s = 0; s < SW_SLOTS; ++s) {
+            const int ch = t + s * NTHREADS;
+            const int e = ch * 4;                // float offset in the stage
+            int base, rows0, kind;               // kind 0: z, 1: f, dgi, cx, cy, 2: cz
+            const T *arr;
+            if (e < SW_OF) { base = SW_OZ; rows0 = j0 - 2; arr = zs; kind = 0; }
+            else if (e < SW_OD) { base = SW_OF; rows0 = j0 - 1; arr = L.f; kind = 1; }
+            else if (e < SW_OX) { base = SW_OD; rows0 = j0 - 1; arr = L.dgi; kind = 1; }
+            else if (e < SW_OY) { base = SW_OX; rows0 = j0 - 1; arr = L.cx; kind = 1; }
+            else if (e < SW_OC) { base = SW_OY; rows0 = j0 - 1; arr = L.cy; kind = 1; }
+            else { base = SW_OC; rows0 = j0 - 1; arr = L.cz; kind = 2; }
+            const int r = (e - base) / SW_R, h = (e - base) % SW_R;
+            const int x = X0 + h, y = rows0 + r;
+            so[s] = e;
+            sk[s] = kind;
+            sv[s] = ch < SW_CHUNKS && x >= 0 && x + 4 <= isx && y >= 0 && y <= ny + 1 && !(zero && kind == 0);
+            gp[s] = arr + (x + isx * y) + (long long)isxy * (k0 - 2);
+        }
+        // plane p's copies into stage `st`: of plane k0 - 2 only z is read,
+        // of k1 + 2 only z and cz, nothing above k1 + 2
+        auto issue = [&](int p, int st) {
+            if (p >= 0 && p <= nz + 1 && p <= k1 + 2) {
+                T *S = stg + st * SW_STAGE;
+                const int kmax = (p == k0 - 2) ? 0 : (p == k1 + 2) ? 2 : 3;
+#pragma unroll
+                for (int s = 0; s < SW_SLOTS; ++s)
+                    if (sv[s] && (sk[s] == 0 || (sk[s] == 2 && kmax >= 2) || kmax == 3)) cp_async16(S + so[s], gp[s]);
+            }
+#pragma unroll
+            for (int s = 0; s < SW_SLOTS; ++s) gp[s] += isxy;
+            cp_async_commit();
+        };
+        auto wrap5 = [](int s) { return s >= SW_NS ? s - SW_NS : s; };
+        // this thread's first-colour footprint position (t < 170): row pj,
+        // column 2 pm + b with b the plane's parity choice; both choices
+        // resolved here (ring index, staged offset, in the grid, wrapped)
+        const bool pt = t < SW_Y * (SW_X / 2);
+        const int pj = t / (SW_X / 2), pm = t % (SW_X / 2);
+        const int lj = j0 - 1 + pj;
+        int rj = lj;
+        if (wy && lj == 0) rj = ny;
+        if (wy && lj == ny + 1) rj = 1;
+        const bool pvy = pt && rj >= 1 && rj <= ny;
+        const bool pwy = wy && (lj <= 1 || lj >= ny);
+        rj = max(1, min(rj, ny));
+        // flags of choice b in bit b; the offsets of choice 1 are those of
+        // choice 0 plus one
+        int pvb = 0, pwb = 0, pq0 = 0, pq1 = 0;
+#pragma unroll
+        for (int b = 0; b < 2; ++b) {
+            const int li = i0 - 1 + 2 * pm + b;
+            int ri = li;
+            if (wx && li == 0) ri = nx;
+            if (wx && li == nx + 1) ri = 1;
+            if (pvy && ri >= 1 && ri <= nx) pvb |= 1 << b;
+            if (pwy || (wx && (li <= 1 || li >= nx))) pwb |= 1 << b;
+            ri = max(1, min(ri, nx));
+            (b ? pq1 : pq0) = ri + isx * rj;
+        }
+        const int pr0 = pj * SW_X + 2 * pm, pe0 = pj * SW_R + 2 * pm + 4;
+        // this thread's own cell
+        const int oi = i0 + (t & (COL_X - 1)), oj = j0 + t / COL_X;
+        const bool ov = oi <= nx && oj <= ny;
+        const int op = (t & (COL_X - 1)) + 1 + SW_X * (t / COL_X + 1);
+        const int os = (t / COL_X + 1) * SW_R + (t & (COL_X - 1)) + 5;
+        T *zo = zd + (min(oi, nx) + isx * min(oj, ny)) + (long long)isxy * k0;
+        __syncthreads();          // the previous unit's stages and ring are consumed
+#pragma unroll 1
+        for (int p = k0 - 2; p <= k0 + 1; ++p) issue(p, p - (k0 - 2));
+        int sm1 = 0;              // stage of plane kk - 1
+        int rr = 2;               // ring slot of plane kk
+#pragma unroll 1
+        for (int kk = k0 - 1; kk <= k1 + 1; ++kk) {
+            cp_async_wait<1>();   // planes up to kk + 1 have landed (kk + 2 may be in flight)
+            __syncthreads();
+            issue(kk + 3, wrap5(sm1 + 4));   // into the stage of plane kk - 2, read for the last time above
+            const T *Sm = stg + sm1 * SW_STAGE, *S0 = stg + wrap5(sm1 + 1) * SW_STAGE,
+                    *Sp = stg + wrap5(sm1 + 2) * SW_STAGE;
+            // c1 values of plane kk on the footprint (zero outside the grid;
+            // the c2 positions of the ring are never read)
+            T *R = ring[rr];
+            if (pt) {
+                const int b = (c1 + lj + kk) & 1;                 // i0 - 1 is even
+                T zn = T(0);
+                if (((pvb >> b) & 1) && kk >= 1 && kk <= nz) {
+                    T fv, di, a0, a1, b0, b1, e0, e1, za0 = T(0), za1 = T(0), zb0 = T(0), zb1 = T(0), zc0 = T(0), zc1 = T(0);
+                    if ((pwb >> b) & 1) {
+                        const int q = (b ? pq1 : pq0) + isxy * kk;
+                        const int ri = q % isx;
+                        const int pxm = (wx && ri == 1) ? (nx - 1) : -1;
+                        const int pxp = (wx && ri == nx) ? -(nx - 1) : 1;
+                        const int pym = (wy && rj == 1) ? (ny - 1) * isx : -isx;
+                        const int pyp = (wy && rj == ny) ? -(ny - 1) * isx : isx;
+                        fv = L.f[q]; di = L.dgi[q];
+                        a0 = L.cx[q]; a1 = L.cx[q + 1]; b0 = L.cy[q]; b1 = L.cy[q + isx]; e0 = L.cz[q]; e1 = L.cz[q + isxy];
+                        if (!zero) {
+                            za0 = zs[q + pxm]; za1 = zs[q + pxp]; zb0 = zs[q + pym]; zb1 = zs[q + pyp];
+                            zc0 = zs[q - isxy]; zc1 = zs[q + isxy];
+                        }
+                    } else {
+                        const int e = pe0 + b;
+                        fv = S0[SW_OF + e]; di = S0[SW_OD + e];
+                        a0 = S0[SW_OX + e]; a1 = S0[SW_OX + e + 1]; b0 = S0[SW_OY + e]; b1 = S0[SW_OY + e + SW_R];
+                        e0 = S0[SW_OC + e]; e1 = Sp[SW_OC + e];
+                        if (!zero) {
+                            const int ez = e + SW_R;     // z rows start one row lower
+                            za0 = S0[SW_OZ + ez - 1]; za1 = S0[SW_OZ + ez + 1];
+                            zb0 = S0[SW_OZ + ez - SW_R]; zb1 = S0[SW_OZ + ez + SW_R];
+                            zc0 = Sm[SW_OZ + ez]; zc1 = Sp[SW_OZ + ez];
+                        }
+                    }
+                    if (zero) {
+                        zn = fv * di;
+                    } else {
+                        const T sm = fv + a0 * za0 + a1 * za1 + b0 * zb0 + b1 * zb1 + e0 * zc0 + e1 * zc1;
+                        zn = sm * di;
+                    }
+                }
+                R[pr0 + b] = zn;
+            }
+            __syncthreads();
+            // plane kb = kk - 1: c2 cells from the ring, c1 cells copied out
+            const int kb = kk - 1;
+            if (kb >= k0) {
+                if (ov) {
+                    // ring slots of planes kb - 1 (= kk - 2) and kb (= kk - 1)
+                    const T *Rm = ring[rr == 2 ? 0 : rr + 1], *R0 = ring[rr == 0 ? 2 : rr - 1], *Rp = R;
+                    T zn;
+                    if (((oi + oj + kb) & 1) == c2) {
+                        const T sm = Sm[SW_OF + os] + Sm[SW_OX + os] * R0[op - 1] + Sm[SW_OX + os + 1] * R0[op + 1] +
+                                     Sm[SW_OY + os] * R0[op - SW_X] + Sm[SW_OY + os + SW_R] * R0[op + SW_X] +
+                                     Sm[SW_OC + os] * Rm[op] + S0[SW_OC + os] * Rp[op];
+                        zn = sm * Sm[SW_OD + os];
+                    } else {
+                        zn = R0[op];
+                    }
+                    *zo = zn;
+                }
+                zo += isxy;
+            }
+            sm1 = wrap5(sm1 + 1);
+            rr = (rr == 2) ? 0 : rr + 1;
+        }
+        cp_async_wait<0>();       // no copy of this unit is left in flight
+    });
+}
+
+// the one-pass sweep's grid: its dynamic shared memory opted in, every SM
+// filled to the occupancy that memory allows
+template <typename T> int sweep0_grid()
+{
+    cudaFuncSetAttribute((const void *)k_mg_sweep0<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SW_SMEM);
+    return occupancy_grid((const void *)k_mg_sweep0<T>, SW_SMEM);
 }
 
 // f(l) = P^T (f - L z)(l-1): the coarse right-hand side, each coarse cell
@@ -187,10 +413,10 @@ __global__ void __launch_bounds__(NTHREADS) k_mg_restrict(const CaseDev<T> *__re
     });
 }
 
-// z(l) += P z(l+1)
+// z(l) += P z(l+1); on level 0 with to2 the sum goes to z2 (z unchanged)
 template <typename T>
 __global__ void __launch_bounds__(NTHREADS) k_mg_prolong(const CaseDev<T> *__restrict__ cs,
-                                                         const int *__restrict__ tab, int N, int l)
+                                                         const int *__restrict__ tab, int N, int l, int to2)
 {
     for_active_units(tab, N, l, [&](int id, int u) {
         const CaseDev<T> &c = cs[id];
@@ -199,9 +425,10 @@ __global__ void __launch_bounds__(NTHREADS) k_mg_prolong(const CaseDev<T> *__res
         if (l == 0) {
             const Column cl = column_of(F.g, u);
             if (!cl.v) return;
+            T *out = to2 ? F.z2 : F.z;
             long long q = F.g.at(cl.i, cl.j, cl.k0);
             for (int k = cl.k0; k <= cl.k1; ++k, q += F.g.sxy)
-                F.z[q] += C.z[C.g.at((cl.i + 1) >> 1, (cl.j + 1) >> 1, (k + 1) >> 1)];
+                out[q] = F.z[q] + C.z[C.g.at((cl.i + 1) >> 1, (cl.j + 1) >> 1, (k + 1) >> 1)];
             return;
         }
         const int t0 = u, t1 = u + 1;
@@ -287,7 +514,9 @@ __global__ void __launch_bounds__(NTHREADS) k_mg_coarsen(const CaseDev<T> *__res
     if (K == mz) C.cz[q + g.sxy] = z1;
     // a wrap face joins cells 1 and m: it enters both diagonals; a Neumann
     // wall face is zero already
-    C.dg[q] = x0 + x1 + y0 + y1 + z0 + z1;
+    const T dq = x0 + x1 + y0 + y1 + z0 + z1;
+    C.dg[q] = dq;
+    C.dgi[q] = (dq > T(0)) ? T(1) / dq : T(0);
 }
 
 // ---- launchers ---------------------------------------------------------------
@@ -315,9 +544,24 @@ template <typename T> void launch_mg_vcycle(const Batch<T> &b, const int *tab, i
         const char *e = std::getenv("SULI_MG_NU0");
         return (e && std::atoi(e) == 1) ? 1 : 2;
     }();
+    // the case grid's sweeps as one-pass whole sweeps, or (SULI_MG_FUSED=0)
+    // as two half-sweep launches each: the same arithmetic
+    const char *fe = std::getenv("SULI_MG_FUSED");
+    const bool fused = !(fe && std::atoi(fe) == 0);
+    static const int gW = sweep0_grid<T>();
     const int ncoarse = 6;
     for (int l = 0; l + 1 < NL; ++l) {
         const int nu = (l == 0) ? nu0 : 2;
+        if (l == 0 && fused) {
+            // the buffers alternate so that the last sweep writes z
+            for (int it = 0; it < nu; ++it) {
+                const int dst = (nu - 1 - it) & 1;
+                k_mg_sweep0<T><<<gW, b.cblock(), SW_SMEM, s>>>(b.dcases, tab, N, 0, it == 0, 1 - dst, dst);
+            }
+            k_mg_restrict<T><<<gR, b.cblock(), 0, s>>>(b.dcases, tab, N, l + 1);
+            count_launch(nu + 1);
+            continue;
+        }
         for (int it = 0; it < nu; ++it) {
             k_mg_smooth<T><<<gS, b.cblock(), 0, s>>>(b.dcases, tab, N, l, 0, it == 0);
             k_mg_smooth<T><<<gS, b.cblock(), 0, s>>>(b.dcases, tab, N, l, 1, 0);
@@ -331,8 +575,19 @@ template <typename T> void launch_mg_vcycle(const Batch<T> &b, const int *tab, i
     }
     count_launch(2 * ncoarse);
     for (int l = NL - 2; l >= 0; --l) {
-        k_mg_prolong<T><<<gP, b.cblock(), 0, s>>>(b.dcases, tab, N, l);
         const int nu = (l == 0) ? nu0 : 2;
+        if (l == 0 && fused) {
+            // black then red; the prolongation writes the buffer the first
+            // sweep reads, chosen so that the last sweep writes z
+            k_mg_prolong<T><<<gP, b.cblock(), 0, s>>>(b.dcases, tab, N, l, nu & 1);
+            for (int it = 0; it < nu; ++it) {
+                const int dst = (nu - 1 - it) & 1;
+                k_mg_sweep0<T><<<gW, b.cblock(), SW_SMEM, s>>>(b.dcases, tab, N, 1, 0, 1 - dst, dst);
+            }
+            count_launch(nu + 1);
+            continue;
+        }
+        k_mg_prolong<T><<<gP, b.cblock(), 0, s>>>(b.dcases, tab, N, l, 0);
         for (int it = 0; it < nu; ++it) {
             k_mg_smooth<T><<<gS, b.cblock(), 0, s>>>(b.dcases, tab, N, l, 1, 0);
             k_mg_smooth<T><<<gS, b.cblock(), 0, s>>>(b.dcases, tab, N, l, 0, 0);
@@ -353,8 +608,20 @@ template <typename T> int launch_mg_smooth0(const Batch<T> &b, const int *tab, i
 }
 template <> int launch_mg_smooth0<double>(const Batch<double> &, const int *, int, cudaStream_t) { return -1; }
 
+// profiling: one whole one-pass sweep on level 0 (z -> z2) over table `tab`
+template <typename T> int launch_mg_sweep0(const Batch<T> &b, const int *tab, cudaStream_t s)
+{
+    if (b.nlev < 2) return -1;
+    static const int gW = sweep0_grid<T>();
+    k_mg_sweep0<T><<<gW, b.cblock(), SW_SMEM, s>>>(b.dcases, tab, b.ncases, 0, 0, 0, 1);
+    count_launch();
+    return 0;
+}
+template <> int launch_mg_sweep0<double>(const Batch<double> &, const int *, cudaStream_t) { return -1; }
+
 template void launch_mg_coarsen<float>(const Batch<float> &, cudaStream_t);
 template int launch_mg_smooth0<float>(const Batch<float> &, const int *, int, cudaStream_t);
+template int launch_mg_sweep0<float>(const Batch<float> &, const int *, cudaStream_t);
 template void launch_mg_vcycle<float>(const Batch<float> &, const int *, int, cudaStream_t);
 
 }  // namespace suli

@@ -352,7 +352,7 @@ struct Impl : ImplBase {
             T **ptf[] = {&cd.bxx0, &cd.bxx1, &cd.blx1};
             const bool mixed = (sizeof(T) == 4);
             const bool mg = mixed && q.mixed_precond == 1;
-            size_t bytes = fb * ntf + ib * 4 + pb * 3 + (mixed ? 17 * db : 0) + (mg ? 6 * fb : 0);
+            size_t bytes = fb * ntf + ib * 4 + pb * 3 + (mixed ? 17 * db : 0) + (mg ? 8 * fb : 0);
             void *slab = nullptr;
             CK(cudaMalloc(&slab, bytes));
             slabs.push_back(slab);
@@ -372,8 +372,8 @@ struct Impl : ImplBase {
                 MgLev<T> &L = cd.mg[0];
                 L.g = g;
                 L.ntx = cd.ntx; L.nty = cd.nty; L.ntz = cd.ntz; L.ntiles = cd.ntiles;
-                T **lf[] = {&L.cx, &L.cy, &L.cz, &L.dg, &L.z, &L.f};
-                for (int f = 0; f < 6; ++f) { *lf[f] = (T *)cur; cur += fb; }
+                T **lf[] = {&L.cx, &L.cy, &L.cz, &L.dg, &L.z, &L.f, &L.z2, &L.dgi};
+                for (int f = 0; f < 8; ++f) { *lf[f] = (T *)cur; cur += fb; }
             }
         }
         // multigrid levels: halve every dimension until the largest is at most
@@ -400,7 +400,7 @@ struct Impl : ImplBase {
                     L.g.total = L.g.sxy * (dz + 2);
                     L.ntx = (dx + TX - 1) / TX; L.nty = (dy + TY - 1) / TY; L.ntz = (dz + TZ - 1) / TZ;
                     L.ntiles = L.ntx * L.nty * L.ntz;
-                    bytes += 6 * (((size_t)L.g.total * sizeof(T) + 255) / 256 * 256);
+                    bytes += 7 * (((size_t)L.g.total * sizeof(T) + 255) / 256 * 256);
                     b.mg_tiles[l] += L.ntiles;
                 }
                 void *slab = nullptr;
@@ -411,8 +411,8 @@ struct Impl : ImplBase {
                 for (int l = 1; l < nlev; ++l) {
                     MgLev<T> &L = cd.mg[l];
                     const size_t lb = ((size_t)L.g.total * sizeof(T) + 255) / 256 * 256;
-                    T **lf[] = {&L.cx, &L.cy, &L.cz, &L.dg, &L.z, &L.f};
-                    for (int f = 0; f < 6; ++f) { *lf[f] = (T *)cur; cur += lb; }
+                    T **lf[] = {&L.cx, &L.cy, &L.cz, &L.dg, &L.z, &L.f, &L.dgi};
+                    for (int f = 0; f < 7; ++f) { *lf[f] = (T *)cur; cur += lb; }
                 }
             }
         }
@@ -515,7 +515,7 @@ struct Impl : ImplBase {
     int time_kernel(int kernel, int reps, double *ms, double *bytes) override
     {
         if (reps < 1) return fail(SULI_BAD_ARG, "reps must be >= 1");
-        if (kernel == 1 && b.nlev < 2) return fail(SULI_BAD_ARG, "kernel 1 needs the multigrid mixed form");
+        if ((kernel == 1 || kernel == 3) && b.nlev < 2) return fail(SULI_BAD_ARG, "kernels 1 and 3 need the multigrid mixed form");
         if (launch_profile_kernel<T>(b, kernel, 1, st) != 0) return fail(SULI_BAD_ARG, "unknown kernel id");
         launch_profile_kernel<T>(b, kernel, 0, st);
         cudaEvent_t e0, e1;
@@ -535,8 +535,10 @@ struct Impl : ImplBase {
         // algorithmic bytes per cell: A reads p and the three scaled
         // coefficients and writes mp (5 arrays); a red half-sweep streams z, f,
         // dg and the three conductances (shared cache lines: both colours) and
-        // writes half of z (6.5); C reads r and p and writes p (3)
-        const double per[3] = {5.0, 6.5, 3.0};
+        // writes half of z (6.5); C reads r and p and writes p (3); a whole
+        // one-pass sweep reads z, f, dg and the three conductances and writes
+        // the other z buffer (7)
+        const double per[4] = {5.0, 6.5, 3.0, 7.0};
         *ms = (double)t / reps;
         *bytes = cells * per[kernel] * (double)sizeof(T);
         return SULI_OK;
@@ -798,8 +800,12 @@ struct Impl : ImplBase {
         launch_contorno<T>(b, nlock, st, inflow_calls);
         if (any_inflow()) inflow_calls += (nlock == 2) ? 2 : 1;
         // values the boundary conditions wrote (ghosts, walls, inflow, IBM
-        // images) into the FP64 masters of the mixed form
-        if (sizeof(T) == 4) launch_sync_masters<T>(b, st);
+        // images) into the FP64 masters of the mixed form, then the ghost
+        // fills redone on the masters in FP64
+        if (sizeof(T) == 4) {
+            launch_sync_masters<T>(b, st);
+            launch_contorno_masters<T>(b, nlock, st);
+        }
         CKL();
         return SULI_OK;
     }
@@ -856,6 +862,16 @@ struct Impl : ImplBase {
             cg_path = (env && std::string(env) == "clusters" && cluster_cg_size<T>() > 0) ? 1 : 0;
         }
         return cg_path == 1;
+    }
+
+    // SULI_CG_TRACE=1: one line per FP64 refinement pass of case 0 on stderr
+    static bool cg_trace()
+    {
+        static const bool on = [] {
+            const char *e = std::getenv("SULI_CG_TRACE");
+            return e && std::atoi(e) == 1;
+        }();
+        return on;
     }
 
     int graddin(int32_t *iters) override
@@ -934,6 +950,9 @@ struct Impl : ImplBase {
                 launch_cg_refine_next<T>(b, st);
                 CKL();
                 if ((rc = read_scalars())) return rc;
+                if (cg_trace())
+                    std::fprintf(stderr, "suli cg trace: stage %d pass %d iterations %d fp64 r.r %.3e threshold %.3e fp32 r.r %.3e\n",
+                                 tt, (int)std::fabs(sc(0, S_OUTER)), pass_done, sc(0, S_RRTRUE), sc(0, S_THR), sc(0, S_RR));
                 bool all = true;
                 passes = 0;
                 for (int c = 0; c < ncases; ++c) {
@@ -944,7 +963,10 @@ struct Impl : ImplBase {
             }
             launch_cg_refine_finish<T>(b, st);
             CKL();
-            for (int c = 0; c < ncases; ++c) maxit = std::max(maxit, (int)sc(c, S_CGITER));
+            for (int c = 0; c < ncases; ++c) {
+                maxit = std::max(maxit, (int)sc(c, S_CGITER));
+                if (sc(c, S_STALLED) != 0.0) warn |= (1 << SULI_CG_STALLED);
+            }
             cg_outer[si] = passes;
         }
         if (prof)

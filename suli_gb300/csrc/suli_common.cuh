@@ -63,6 +63,8 @@ enum Scal {
     S_RZ,          // mixed form, multigrid-preconditioned passes: r.z
     S_P64OK,       // mixed form: r64 holds the FP64 pressure of the last solve
     S_PASS0,       // mixed form: CG iteration count at the start of the pass
+    S_STALL,       // mixed form: consecutive passes whose FP64 r.r did not halve
+    S_STALLED,     // mixed form: 1 when the refinement ended on stagnation
     S_NSCAL
 };
 
@@ -87,6 +89,8 @@ struct MgLev {
     Geo g;
     int ntx, nty, ntz, ntiles;
     T *cx, *cy, *cz, *dg, *z, *f;
+    T *dgi;    // 1 / dg (0 where dg = 0): the smoothers multiply instead of divide
+    T *z2;     // level 0: the second buffer of the one-pass sweeps (null above)
 };
 
 template <typename T>

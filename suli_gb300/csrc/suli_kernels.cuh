@@ -10,12 +10,12 @@ namespace suli {
 
 // grid of a persistent kernel: every SM filled to the kernel's own occupancy
 // (256 threads per block)
-inline int occupancy_grid(const void *fn)
+inline int occupancy_grid(const void *fn, size_t dyn_smem = 0)
 {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, dyn_smem);
     return (sms > 0 ? sms : 1) * (per > 0 ? per : 1);
 }
 
@@ -57,6 +57,7 @@ template <typename T> void launch_mms_error(const Batch<T> &b, cudaStream_t s);
 
 // boundary conditions (k_bc.cu)
 template <typename T> void launch_contorno(const Batch<T> &b, int nlock, cudaStream_t s, unsigned long long rng_call = 0);
+template <typename T> void launch_contorno_masters(const Batch<T> &b, int nlock, cudaStream_t s);
 // mixed form: FP32 velocity values changed outside tempo/posdin -> FP64 masters
 template <typename T> void launch_sync_masters(const Batch<T> &b, cudaStream_t s);
 
@@ -81,6 +82,7 @@ template <typename T> int launch_pcg_iters(const Batch<T> &b, int n, int slot, c
 // prepare != 0 builds that table first); returns -1 for an unknown kernel
 template <typename T> int launch_profile_kernel(const Batch<T> &b, int kernel, int prepare, cudaStream_t s);
 template <typename T> int launch_mg_smooth0(const Batch<T> &b, const int *tab, int grid, cudaStream_t s);
+template <typename T> int launch_mg_sweep0(const Batch<T> &b, const int *tab, cudaStream_t s);
 
 // multigrid (k_mg.cu): coarse operators from level 0, one V-cycle over a table
 template <typename T> void launch_mg_coarsen(const Batch<T> &b, cudaStream_t s);

@@ -110,10 +110,11 @@ def test_cluster_cg_matches_tile_cg(gpu_lib, monkeypatch, precision):
 
 @pytest.mark.parametrize("mk", ["periodic_mms", "uneven_batch"])
 def test_multigrid_passes_match_jacobi_passes(gpu_lib, mk):
-    """Both inner solvers of the mixed form meet the same FP64 residual test,
-    so their pressures agree to that tolerance; the multigrid passes take far
-    fewer iterations.  Covers periodic x/y of odd coarse length and a batch of
-    uneven grids."""
+    """Both inner solvers of the mixed form meet the same FP64 residual test
+    (or, for the periodic manufactured solution from its second step, stop on
+    the same stagnation floor near 2e-9), so their pressures agree to that
+    tolerance; the multigrid passes take far fewer iterations.  Covers
+    periodic x/y of odd coarse length and a batch of uneven grids."""
     if mk == "periodic_mms":
         mk_cases = lambda: [cases.mms_case(24, precision=PREC_MIXED)]
     else:
@@ -142,6 +143,75 @@ def test_multigrid_passes_match_jacobi_passes(gpu_lib, mk):
     ub = np.concatenate([b.ravel() for b in res[1][1]])
     assert rel_l2(ua, ub) < 1e-5
     assert sum(res[1][2]) < sum(res[0][2]), (res[0][2], res[1][2])
+
+
+@pytest.mark.parametrize("precond", [0, 1], ids=["jacobi", "multigrid"])
+def test_refinement_stops_when_the_fp64_residual_stagnates(gpu_lib, precond):
+    """The periodic manufactured solution at a relative 1e-9: from the second
+    step on its pressure system has a mode that FP32 passes cannot reduce
+    (the FP64 residual sits near 2e-9 of the right-hand side, pass after
+    pass).  The refinement stops after three passes without progress and
+    raises SULI_CG_STALLED instead of iterating to the cap."""
+    from suli_gb300._abi import SULI_CG_STALLED
+    c = cases.mms_case(24, precision=PREC_MIXED)
+    c.params.mixed_precond = precond
+    c.params.cg_tol_mode = 1
+    c.params.cg_tol = 1e-9
+    c.params.project_under_mms = 1
+    g = gpu_lib.SuliGPU(c.params)
+    g.start(c.fields)
+    flags = 0
+    for _ in range(3):
+        g.step(1)
+        d = g.diag()
+        flags |= d.status_flags
+        print("iterations %s passes %s fp64 r.r %s flags %#x" % (list(d.cg_iters), list(d.cg_outer),
+                                                                 ["%.2e" % x for x in d.cg_res], d.status_flags))
+        # a stopped stage costs a few passes (multigrid ~15, Jacobi ~100
+        # iterations each), not the ~2900 iterations to the cap
+        assert all(n < (200 if precond else 1000) for n in d.cg_iters)
+        assert max(d.cg_res) < 1e-12
+    g.close()
+    assert flags & (1 << SULI_CG_STALLED)
+
+
+@pytest.mark.parametrize("mk", ["periodic_even", "periodic_odd", "uneven_batch"])
+def test_one_pass_sweeps_match_half_sweeps(gpu_lib, monkeypatch, mk):
+    """The case grid's one-pass whole sweeps (the default; the first colour
+    recomputed on a one-cell ring, two z buffers) do the arithmetic of the two
+    half-sweep launches (SULI_MG_FUSED=0): same pressures and velocities, same
+    iteration counts.  Covers
+    the kept wrap (even periodic length), the dropped wrap (odd) and a batch
+    of uneven grids (partial column units)."""
+    def mk_cases():
+        if mk == "periodic_even":
+            return [cases.mms_case(24, precision=PREC_MIXED)]
+        if mk == "periodic_odd":
+            return [cases.mms_case(25, precision=PREC_MIXED)]
+        dims, hcol, amp = cases.ensemble_dims(5, seed=11, lo=13, hi=40)
+        return [cases.ensemble_case(i, dims, hcol, amp, precision=PREC_MIXED) for i in range(5)]
+    out = {}
+    for fused in ("0", "1"):
+        monkeypatch.setenv("SULI_MG_FUSED", fused)
+        cs = mk_cases()
+        for c in cs:
+            c.params.mixed_precond = 1
+            c.params.cg_tol_mode = 1
+            c.params.cg_tol = 1e-9
+        g = gpu_lib.SuliGPU([c.params for c in cs])
+        g.start([c.fields for c in cs])
+        g.step(2)
+        out[fused] = ([g.download("PRD1", i)[1:-1, 1:-1, 1:-1] for i in range(len(cs))],
+                      np.concatenate([g.download("U", i).ravel() for i in range(len(cs))]),
+                      list(g.diag(0).cg_iters))
+        g.close()
+    same = all(np.array_equal(a, b) for a, b in zip(out["0"][0], out["1"][0]))
+    print("one-pass vs half-sweep (%s): bit-identical pressure: %s, iterations %s / %s"
+          % (mk, same, out["0"][2], out["1"][2]))
+    for a, b in zip(out["0"][0], out["1"][0]):
+        assert rel_l2(a - a.mean(), b - b.mean()) < 1e-6
+    assert rel_l2(out["0"][1], out["1"][1]) < 1e-6
+    assert all(abs(x - y) <= 1 for x, y in zip(out["0"][2], out["1"][2]))
 
 
 @pytest.mark.parametrize("precision", [0, 1])
