@@ -133,15 +133,16 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_setup1m(const CaseDev<T> *__res
     if (i == 1 && j == 1 && k == 1) c.sc[S_P64OK] = 0.0;   // r64 is reused below
     const bool px = (c.ccx0 == 0);
     const double dt = c.sc[S_DT];
-    const double aux1 = dt / (c.dx * c.dx), aux2 = dt / (c.dy * c.dy), aux3 = dt / (c.dz * c.dz);
+    const double aux1 = dt * c.idx * c.idx, aux2 = dt * c.idy * c.idy, aux3 = dt * c.idz * c.idz;
     const double *rho = c.rho64;
     const long long q = g.at(i, j, k);
-    c.spi64[q] = aux1 / icf<double>(i, nx, px, [&](int m) { return AT(rho, m, j, k); });
-    c.spj64[q] = aux2 / icf<double>(j, ny, false, [&](int m) { return AT(rho, i, m, k); });
-    c.spk64[q] = aux3 / icf<double>(k, nz, false, [&](int m) { return AT(rho, i, j, m); });
-    if (i == nx) c.spi64[q + 1] = aux1 / icf<double>(nx + 1, nx, px, [&](int m) { return AT(rho, m, j, k); });
-    if (j == ny) c.spj64[q + g.sx] = aux2 / icf<double>(ny + 1, ny, false, [&](int m) { return AT(rho, i, m, k); });
-    if (k == nz) c.spk64[q + g.sxy] = aux3 / icf<double>(nz + 1, nz, false, [&](int m) { return AT(rho, i, j, m); });
+    // aux / face density, by reciprocal (no FP64 divide)
+    c.spi64[q] = aux1 * rcp_nr64(icf<double>(i, nx, px, [&](int m) { return AT(rho, m, j, k); }));
+    c.spj64[q] = aux2 * rcp_nr64(icf<double>(j, ny, false, [&](int m) { return AT(rho, i, m, k); }));
+    c.spk64[q] = aux3 * rcp_nr64(icf<double>(k, nz, false, [&](int m) { return AT(rho, i, j, m); }));
+    if (i == nx) c.spi64[q + 1] = aux1 * rcp_nr64(icf<double>(nx + 1, nx, px, [&](int m) { return AT(rho, m, j, k); }));
+    if (j == ny) c.spj64[q + g.sx] = aux2 * rcp_nr64(icf<double>(ny + 1, ny, false, [&](int m) { return AT(rho, i, m, k); }));
+    if (k == nz) c.spk64[q + g.sxy] = aux3 * rcp_nr64(icf<double>(nz + 1, nz, false, [&](int m) { return AT(rho, i, j, m); }));
     // the divergence of the FP64 masters: the field that posdin corrects
     double ua, ub, va, vb, wa, wb;
     if (c.u64 != nullptr) {
@@ -157,7 +158,7 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_setup1m(const CaseDev<T> *__res
         if (c.obs_lsz[q] >= T(0.)) wa = 0.;
         if (c.obs_lsz[q + g.sxy] >= T(0.)) wb = 0.;
     }
-    c.qpr64[q] = (ua - ub) / c.dx + (va - vb) / c.dy + (wa - wb) / c.dz;
+    c.qpr64[q] = (ua - ub) * c.idx + (va - vb) * c.idy + (wa - wb) * c.idz;
 }
 
 template <typename T>
@@ -175,7 +176,7 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_setup1mb(const CaseDev<T> *__re
     const double D = si1 + si0 + sj1 + sj0 + sk1 + sk0;
     c.dpr64[q] = D;
     c.dpr[q] = T(D);
-    c.r64[q] = 1.0 / sqrt(D);
+    c.r64[q] = rsqrt(D);
     if (c.nlev > 0) {
         // level 0 of the multigrid preconditioner: the unscaled face
         // conductances, zero on Neumann walls (the wall's ghost copy cancels
@@ -580,11 +581,53 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_finish(const CaseDev<T> *__rest
 // follows FP64 CG iteration for iteration down to ~1e-5 relative residual and
 // stalls below, so each pass asks for 1e-3; the FP64 residual of the next
 // pass removes the FP32 drift.
+// A case's scalars after an FP64 residual (thread 0 of its last block):
+// convergence, stagnation and the next pass's inner target; bb (the
+// right-hand side's r.r) is read on the first residual only
 template <typename T>
-__global__ void __launch_bounds__(NTHREADS) k_cg_true_residual(const CaseDev<T> *__restrict__ cs, int ncases, int first)
+__device__ void true_residual_update(const CaseDev<T> &c, int first, double rrt, double rr32, double bb)
+{
+    const double prev = c.sc[S_RRTRUE];
+    c.sc[S_RRTRUE] = rrt;
+    // stagnation: FP32 passes cannot lower a residual whose worst mode has a
+    // condition number near 1/eps(FP32); after three passes that did not
+    // halve r.r the case stops with its best iterate
+    const double stall = first ? 0.0 : ((rrt > 0.5 * prev) ? c.sc[S_STALL] + 1.0 : 0.0);
+    c.sc[S_STALL] = stall;
+    if (first) {
+        double thr;
+        if (c.cg_tol_mode == 1) thr = c.cg_tol * c.cg_tol * bb;
+        else thr = c.cg_tol / ((double)c.g.nx * c.g.ny * c.g.nz);
+        c.sc[S_THR] = thr;
+        c.sc[S_RR0] = rrt;
+        c.sc[S_OUTER] = 0.0;
+        c.sc[S_CGITER] = 0.0;
+    }
+    const double passes = c.sc[S_OUTER] + 1.0;
+    const bool stalled = (rrt > c.sc[S_THR]) && stall >= 3.0;
+    c.sc[S_STALLED] = stalled ? 1.0 : 0.0;
+    const bool conv = !(rrt > c.sc[S_THR]) || c.sc[S_CGITER] >= c.sc[S_CGMAX] || stalled;
+    c.sc[S_RR] = rr32;
+    // inner target: a residual reduction of 1e3 (Jacobi-scaled passes) or
+    // 1e5 (multigrid-preconditioned passes), but no further than half the
+    // outer target; a pass also ends after MG_PASS_MAX iterations
+    c.sc[S_RRREF] = fmax((c.nlev > 0 ? 1e-10 : 1e-6) * rr32, 0.25 * c.sc[S_THR]);
+    c.sc[S_PASS0] = c.sc[S_CGITER];
+    if (conv) {
+        c.sc[S_OUTER] = -passes;           // negative: done after `passes` FP64 residuals
+        c.sc[S_CGACTIVE] = 0.0;
+    } else {
+        c.sc[S_OUTER] = passes;
+        c.sc[S_CGACTIVE] = 1.0;
+    }
+}
+
+// The solve's first FP64 residual (tile form, one cell per thread); the
+// later passes are k_cg_true_residual_cols.
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_cg_true_residual(const CaseDev<T> *__restrict__ cs, int ncases)
 {
     const CaseDev<T> &c = cs[find_case(cs, ncases)];
-    if (!first && c.sc[S_OUTER] < 0.0) return;     // converged earlier
     int i, j, k;
     tile_ijk(c, i, j, k);
     const Geo &g = c.g;
@@ -594,31 +637,17 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_true_residual(const CaseDev<T> 
     if (i <= nx && j <= ny && k <= nz) {
         long long q = g.at(i, j, k);
         const double *e = c.e64;
-        double r;
-        if (first) {
-            // the solve's first residual: ghost values from prd1 as the
-            // reference's warm start has them (matepr = prd1 sqrt(matdpr))
-            auto E = [&](int a, int b2, int d) -> double {
-                int ma = bmap(a, nx, px), mb = bmap(b2, ny, py), md = bmap(d, nz, false);
-                if (!(ma == a && mb == b2 && md == d))
-                    return (double)AT(c.prd1, a, b2, d) * sqrt(AT(c.dpr64, ma, mb, md));
-                return AT(e, ma, mb, md);
-            };
-            r = E(i, j, k) - c.spi64[q + 1] * E(i + 1, j, k) - c.spi64[q] * E(i - 1, j, k) -
-                c.spj64[q + g.sx] * E(i, j + 1, k) - c.spj64[q] * E(i, j - 1, k) -
-                c.spk64[q + g.sxy] * E(i, j, k + 1) - c.spk64[q] * E(i, j, k - 1) - c.qpr64[q];
-        } else {
-            // later passes: Neumann neighbours are the cell itself, periodic
-            // ones the opposite end -- fixed offsets, no branch
-            const long long qxp = (i < nx) ? q + 1 : (px ? q - (nx - 1) : q);
-            const long long qxm = (i > 1) ? q - 1 : (px ? q + (nx - 1) : q);
-            const long long qyp = (j < ny) ? q + g.sx : (py ? q - (long long)(ny - 1) * g.sx : q);
-            const long long qym = (j > 1) ? q - g.sx : (py ? q + (long long)(ny - 1) * g.sx : q);
-            const long long qzp = (k < nz) ? q + g.sxy : q;
-            const long long qzm = (k > 1) ? q - g.sxy : q;
-            r = e[q] - c.spi64[q + 1] * e[qxp] - c.spi64[q] * e[qxm] - c.spj64[q + g.sx] * e[qyp] -
-                c.spj64[q] * e[qym] - c.spk64[q + g.sxy] * e[qzp] - c.spk64[q] * e[qzm] - c.qpr64[q];
-        }
+        // ghost values from prd1 as the reference's warm start has them
+        // (matepr = prd1 sqrt(matdpr))
+        auto E = [&](int a, int b2, int d) -> double {
+            int ma = bmap(a, nx, px), mb = bmap(b2, ny, py), md = bmap(d, nz, false);
+            if (!(ma == a && mb == b2 && md == d))
+                return (double)AT(c.prd1, a, b2, d) * sqrt(AT(c.dpr64, ma, mb, md));
+            return AT(e, ma, mb, md);
+        };
+        const double r = E(i, j, k) - c.spi64[q + 1] * E(i + 1, j, k) - c.spi64[q] * E(i - 1, j, k) -
+                         c.spj64[q + g.sx] * E(i, j + 1, k) - c.spj64[q] * E(i, j - 1, k) -
+                         c.spk64[q + g.sxy] * E(i, j, k + 1) - c.spk64[q] * E(i, j, k - 1) - c.qpr64[q];
         T r32 = T(r);
         c.r[q] = r32;
         c.p[q] = r32;
@@ -629,41 +658,58 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_true_residual(const CaseDev<T> 
         bb = c.qpr64[q] * c.qpr64[q];
     }
     double vals[3] = {rr, rr32, bb}, tot[3];
-    if (last_block_reduce<T, 3>(c, vals, tot) && tid_lin() == 0) {
-        double rrt = tot[0];
-        const double prev = c.sc[S_RRTRUE];
-        c.sc[S_RRTRUE] = rrt;
-        // stagnation: FP32 passes cannot lower a residual whose worst mode
-        // has a condition number near 1/eps(FP32); after three passes that
-        // did not halve r.r the case stops with its best iterate
-        const double stall = first ? 0.0 : ((rrt > 0.5 * prev) ? c.sc[S_STALL] + 1.0 : 0.0);
-        c.sc[S_STALL] = stall;
-        if (first) {
-            double thr;
-            if (c.cg_tol_mode == 1) thr = c.cg_tol * c.cg_tol * tot[2];
-            else thr = c.cg_tol / (double)(nx * ny * nz);
-            c.sc[S_THR] = thr;
-            c.sc[S_RR0] = rrt;
-            c.sc[S_OUTER] = 0.0;
-            c.sc[S_CGITER] = 0.0;
+    if (last_block_reduce<T, 3>(c, vals, tot) && tid_lin() == 0) true_residual_update(c, 1, tot[0], tot[1], tot[2]);
+}
+
+// Later passes as columns: a thread walks the COL_Z planes of a column
+// unit, so the FP64 sums cost one block reduction per COL_Z cells (in the
+// tile form above, one cell per thread, the per-cell share of the FP64
+// reductions cost more than the residual itself on GB300's FP64 units)
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_cg_true_residual_cols(const CaseDev<T> *__restrict__ cs, int ncases,
+                                                                     int nunits)
+{
+    for (int gu = blockIdx.x; gu < nunits; gu += gridDim.x) {
+        int lo = 0, hi = ncases - 1;             // the case of unit gu
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (cs[mid].chunk_begin <= gu) lo = mid; else hi = mid - 1;
         }
-        double passes = c.sc[S_OUTER] + 1.0;
-        const bool stalled = (rrt > c.sc[S_THR]) && stall >= 3.0;
-        c.sc[S_STALLED] = stalled ? 1.0 : 0.0;
-        bool conv = !(rrt > c.sc[S_THR]) || c.sc[S_CGITER] >= c.sc[S_CGMAX] || stalled;
-        c.sc[S_RR] = tot[1];
-        // inner target: a residual reduction of 1e3 (Jacobi-scaled passes) or
-        // 1e4 (multigrid-preconditioned passes), but no further than half the
-        // outer target; a pass also ends after MG_PASS_MAX iterations
-        c.sc[S_RRREF] = fmax((c.nlev > 0 ? 1e-10 : 1e-6) * tot[1], 0.25 * c.sc[S_THR]);
-        c.sc[S_PASS0] = c.sc[S_CGITER];
-        if (conv) {
-            c.sc[S_OUTER] = -passes;           // negative: done after `passes` FP64 residuals
-            c.sc[S_CGACTIVE] = 0.0;
-        } else {
-            c.sc[S_OUTER] = passes;
-            c.sc[S_CGACTIVE] = 1.0;
+        const CaseDev<T> &c = cs[lo];
+        if (c.sc[S_OUTER] < 0.0) continue;      // converged earlier (uniform over the block)
+        const Geo &g = c.g;
+        const int nx = g.nx, ny = g.ny, nz = g.nz;
+        const bool px = (c.ccx0 == 0), py = (c.ccy0 == 0);
+        const Column cl = column_of(g, gu - c.chunk_begin);
+        const int i = cl.i, j = cl.j;
+        const long long sx = g.sx, sxy = g.sxy;
+        // Neumann neighbours are the cell itself, periodic ones the opposite end
+        const long long dxp = (i < nx) ? 1 : (px ? -(long long)(nx - 1) : 0);
+        const long long dxm = (i > 1) ? -1 : (px ? (long long)(nx - 1) : 0);
+        const long long dyp = (j < ny) ? sx : (py ? -(long long)(ny - 1) * sx : 0);
+        const long long dym = (j > 1) ? -sx : (py ? (long long)(ny - 1) * sx : 0);
+        const double *__restrict__ e = c.e64;
+        double rr = 0.0, rr32 = 0.0;
+        if (cl.v) {
+            long long q = g.at(i, j, cl.k0);
+            for (int k = cl.k0; k <= cl.k1; ++k, q += sxy) {
+                const long long qzp = (k < nz) ? q + sxy : q;
+                const long long qzm = (k > 1) ? q - sxy : q;
+                const double r = e[q] - c.spi64[q + 1] * e[q + dxp] - c.spi64[q] * e[q + dxm] -
+                                 c.spj64[q + sx] * e[q + dyp] - c.spj64[q] * e[q + dym] - c.spk64[q + sxy] * e[qzp] -
+                                 c.spk64[q] * e[qzm] - c.qpr64[q];
+                const T r32 = T(r);
+                c.r[q] = r32;
+                c.p[q] = r32;
+                c.e[q] = T(0.);
+                if (c.nlev > 0) c.mg[0].f[q] = sqrt(c.dpr[q]) * r32;   // V-cycle right-hand side D^1/2 r
+                rr += r * r;
+                rr32 += (double)r32 * (double)r32;
+            }
         }
+        double vals[2] = {rr, rr32}, tot[2];
+        if (unit_reduce<T, 2>(c, gu, c.chunk_begin, c.nchunks, vals, tot) && tid_lin() == 0)
+            true_residual_update(c, 0, tot[0], tot[1], 0.0);
     }
 }
 
@@ -814,12 +860,14 @@ template <typename T> void launch_cg_refine_setup(const Batch<T> &b, cudaStream_
     k_cg_setup1m<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
     k_cg_setup1mb<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
     k_cg_setup2m<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
-    k_cg_true_residual<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, 1); count_launch();
+    k_cg_true_residual<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
 }
 template <typename T> void launch_cg_refine_next(const Batch<T> &b, cudaStream_t s)
 {
+    static const int gR = occupancy_grid((const void *)k_cg_true_residual_cols<T>);
     k_cg_fold<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
-    k_cg_true_residual<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, 0); count_launch();
+    k_cg_true_residual_cols<T><<<std::min(gR, b.total_units), b.cblock(), 0, s>>>(b.dcases, b.ncases, b.total_units);
+    count_launch();
 }
 template <typename T> void launch_cg_refine_finish(const Batch<T> &b, cudaStream_t s)
 {

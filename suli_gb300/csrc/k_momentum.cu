@@ -392,25 +392,26 @@ __global__ void __launch_bounds__(NTHREADS) k_posdin(const CaseDev<T> *__restric
             if (p64) return c.r64[g.at(mi(i1), mj(j1), mk(k1))] - c.r64[g.at(mi(i0), mj(j0), mk(k0))];
             return (double)AT(p, i1, j1, k1) - (double)AT(p, i0, j0, k0);
         };
-        // one FP64 division per face (GB300's FP64 divide is a long sequence)
+        // no FP64 divide (a long sequence on GB300's FP64 units): the face
+        // density by reciprocal, the spacings' reciprocals from the host
         if (i <= nx + 1 && j <= ny && k <= nz) {
             const double rx = interp_cf<double>(i, nx, px, [&](int m) { return AT(r64, m, j, k); });
             const long long q = g.at(i, j, k);
-            const double x = c.u64[q] - dp64(i, j, k, i - 1, j, k) * ddt / (c.dx * rx);
+            const double x = c.u64[q] - dp64(i, j, k, i - 1, j, k) * (ddt * c.idx) * rcp_nr64(rx);
             c.u64[q] = x;
             c.u[q] = T(x);
         }
         if (i <= nx && j <= ny + 1 && k <= nz) {
             const double ry = interp_cf<double>(j, ny, false, [&](int m) { return AT(r64, i, m, k); });
             const long long q = g.at(i, j, k);
-            const double x = c.v64[q] - dp64(i, j, k, i, j - 1, k) * ddt / (c.dy * ry);
+            const double x = c.v64[q] - dp64(i, j, k, i, j - 1, k) * (ddt * c.idy) * rcp_nr64(ry);
             c.v64[q] = x;
             c.v[q] = T(x);
         }
         if (i <= nx && j <= ny && k <= nz + 1) {
             const double rz = interp_cf<double>(k, nz, false, [&](int m) { return AT(r64, i, j, m); });
             const long long q = g.at(i, j, k);
-            const double x = c.w64[q] - dp64(i, j, k, i, j, k - 1) * ddt / (c.dz * rz);
+            const double x = c.w64[q] - dp64(i, j, k, i, j, k - 1) * (ddt * c.idz) * rcp_nr64(rz);
             c.w64[q] = x;
             c.w[q] = T(x);
         }

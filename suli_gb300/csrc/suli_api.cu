@@ -327,6 +327,7 @@ struct Impl : ImplBase {
             cd.dx1 = std::max({q.dx, q.dy, q.dz});
             cd.dt1 = 0.1 * cd.dx1;
             cd.deltai = std::pow(q.dx * q.dy * q.dz, 1. / 3.);
+            cd.idx = 1.0 / q.dx; cd.idy = 1.0 / q.dy; cd.idz = 1.0 / q.dz;
             cd.alpha1 = q.alpha1;
             cd.rho_f1 = q.rho_f1; cd.mu_f1 = q.mu_f1; cd.rho_f2 = q.rho_f2; cd.mu_f2 = q.mu_f2;
             cd.gx = q.gx; cd.gz = q.gz;
@@ -419,6 +420,7 @@ struct Impl : ImplBase {
         b.nlev = nlev;
         b.ncases = n;
         b.total_tiles = tiles;
+        b.total_units = chunks;
         b.max_plane = maxplane;
         CK(cudaMalloc(&dsc, sizeof(double) * S_NSCAL * n));
         CK(cudaMemsetAsync(dsc, 0, sizeof(double) * S_NSCAL * n, st));

@@ -68,6 +68,19 @@ enum Scal {
     S_NSCAL
 };
 
+// 1/x in FP64 without a division, for the mixed form's FP64 kernels (an
+// FP64 divide is a long instruction sequence on GB300's FP64 units): an FP32
+// reciprocal as seed and two Newton-Raphson steps r <- r + r (1 - x r), each
+// doubling the correct bits (24 -> 48 -> FP64, within a few ulps).  x must
+// be a normal number inside the FP32 range (densities, face conductances).
+__device__ __forceinline__ double rcp_nr64(double x)
+{
+    double r = (double)__frcp_rn((float)x);
+    r = fma(r, fma(-x, r, 1.0), r);
+    r = fma(r, fma(-x, r, 1.0), r);
+    return r;
+}
+
 struct Geo {
     int nx, ny, nz;
     int pad;
@@ -103,6 +116,7 @@ struct CaseDev {
     int chunk_begin, nchunks;
     // discretisation / physics (double in both forms)
     double dx, dy, dz, dx1, dt1, deltai;
+    double idx, idy, idz;       // 1/dx, 1/dy, 1/dz (mixed-form kernels multiply)
     double alpha1, rho_f1, mu_f1, rho_f2, mu_f2, gx, gz;
     double cles;         // (dx*dy*dz)^(2/3) * csmag * csmag
     double pi;

@@ -30,6 +30,7 @@ struct Batch {
     CaseDev<T> *hcases = nullptr;     // host mirror
     int ncases = 0;
     int total_tiles = 0;
+    int total_units = 0;              // column units of the case grids (all cases)
     int max_plane = 0;                // largest boundary plane (elements)
     double *drk = nullptr;            // TVD-RK3 coefficients a[3], b[3], g[3]
     int *act = nullptr;               // two active-case tables of the CG iteration
