@@ -158,15 +158,31 @@ def start_gpu(cs):
     return g
 
 
+def _nvtx(torch):
+    """(push, pop) of torch's NVTX ranges, or no-ops where they are missing."""
+    try:
+        push, pop = torch.cuda.nvtx.range_push, torch.cuda.nvtx.range_pop
+        push("probe")
+        pop()
+        return push, pop
+    except Exception:
+        return (lambda name: None), (lambda: None)
+
+
 def timed_steps(g, k, torch):
-    """Time k steps with CUDA events on the library's stream (synchronized on both sides)."""
+    """Time k steps with CUDA events on the library's stream (synchronized on
+    both sides), inside an NVTX range "timed_steps" (so a profiler can keep
+    to the timed launches: ncu --nvtx --nvtx-include "timed_steps/")."""
     s = torch.cuda.ExternalStream(g.stream_handle())
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     g.synchronize()
+    nvtx = _nvtx(torch)
+    nvtx[0]("timed_steps")
     e0.record(s)
     g.step(k)
     e1.record(s)
+    nvtx[1]()
     g.synchronize()
     e1.synchronize()
     return e0.elapsed_time(e1)

@@ -574,13 +574,14 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_finish(const CaseDev<T> *__rest
 }
 
 // ---- mixed form: FP32 CG passes inside FP64 iterative refinement -------------
-// Each pass: the FP64 residual A e64 - b (k_cg_true_residual, which also
-// tests convergence on its FP64 norm), then an FP32 CG started from x = 0 on
-// A x = r (k_cgi_A, k_cgi_B<1>, k_cgi_C) until its residual has dropped by
-// 1e3 (or reaches the outer target), then e64 -= x (k_cg_fold).  FP32 CG
-// follows FP64 CG iteration for iteration down to ~1e-5 relative residual and
-// stalls below, so each pass asks for 1e-3; the FP64 residual of the next
-// pass removes the FP32 drift.
+// Each pass: the FP64 residual b - A e64 (k_cg_true_residual_cols, which
+// also tests convergence on its FP64 norm), then an FP32 CG started from
+// x = 0 on A x = r (Jacobi-scaled: k_cgi_A, k_cgi_B<1>, k_cgi_C; multigrid-
+// preconditioned: the k_pcg kernels around a V-cycle) until its residual has
+// dropped by 1e3 (Jacobi) or 1e5 (multigrid), or reaches the outer target,
+// then e64 += x (k_cg_fold).  Jacobi-scaled FP32 CG follows FP64 CG
+// iteration for iteration down to ~1e-5 relative residual and stalls below;
+// the FP64 residual of the next pass removes the FP32 drift.
 // A case's scalars after an FP64 residual (thread 0 of its last block):
 // convergence, stagnation and the next pass's inner target; bb (the
 // right-hand side's r.r) is read on the first residual only
@@ -622,52 +623,17 @@ __device__ void true_residual_update(const CaseDev<T> &c, int first, double rrt,
     }
 }
 
-// The solve's first FP64 residual (tile form, one cell per thread); the
-// later passes are k_cg_true_residual_cols.
-template <typename T>
-__global__ void __launch_bounds__(NTHREADS) k_cg_true_residual(const CaseDev<T> *__restrict__ cs, int ncases)
-{
-    const CaseDev<T> &c = cs[find_case(cs, ncases)];
-    int i, j, k;
-    tile_ijk(c, i, j, k);
-    const Geo &g = c.g;
-    const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const bool px = (c.ccx0 == 0), py = (c.ccy0 == 0);
-    double rr = 0.0, rr32 = 0.0, bb = 0.0;
-    if (i <= nx && j <= ny && k <= nz) {
-        long long q = g.at(i, j, k);
-        const double *e = c.e64;
-        // ghost values from prd1 as the reference's warm start has them
-        // (matepr = prd1 sqrt(matdpr))
-        auto E = [&](int a, int b2, int d) -> double {
-            int ma = bmap(a, nx, px), mb = bmap(b2, ny, py), md = bmap(d, nz, false);
-            if (!(ma == a && mb == b2 && md == d))
-                return (double)AT(c.prd1, a, b2, d) * sqrt(AT(c.dpr64, ma, mb, md));
-            return AT(e, ma, mb, md);
-        };
-        const double r = E(i, j, k) - c.spi64[q + 1] * E(i + 1, j, k) - c.spi64[q] * E(i - 1, j, k) -
-                         c.spj64[q + g.sx] * E(i, j + 1, k) - c.spj64[q] * E(i, j - 1, k) -
-                         c.spk64[q + g.sxy] * E(i, j, k + 1) - c.spk64[q] * E(i, j, k - 1) - c.qpr64[q];
-        T r32 = T(r);
-        c.r[q] = r32;
-        c.p[q] = r32;
-        c.e[q] = T(0.);
-        if (c.nlev > 0) c.mg[0].f[q] = sqrt(c.dpr[q]) * r32;   // V-cycle right-hand side D^1/2 r
-        rr = r * r;
-        rr32 = (double)r32 * (double)r32;
-        bb = c.qpr64[q] * c.qpr64[q];
-    }
-    double vals[3] = {rr, rr32, bb}, tot[3];
-    if (last_block_reduce<T, 3>(c, vals, tot) && tid_lin() == 0) true_residual_update(c, 1, tot[0], tot[1], tot[2]);
-}
-
-// Later passes as columns: a thread walks the COL_Z planes of a column
-// unit, so the FP64 sums cost one block reduction per COL_Z cells (in the
-// tile form above, one cell per thread, the per-cell share of the FP64
-// reductions cost more than the residual itself on GB300's FP64 units)
-template <typename T>
-__global__ void __launch_bounds__(NTHREADS) k_cg_true_residual_cols(const CaseDev<T> *__restrict__ cs, int ncases,
-                                                                     int nunits)
+// The FP64 residual of each refinement pass, over column units: a thread
+// walks the COL_Z planes of a column, so the FP64 sums cost one block
+// reduction per COL_Z cells (with one cell per thread, the per-cell share of
+// the FP64 reductions cost more than the residual itself on GB300's FP64
+// units).  first != 0: the solve's first residual, ghost values from prd1 as
+// the reference's warm start has them (matepr = prd1 sqrt(matdpr)), and the
+// right-hand side's r.r for the relative tolerance; later passes skip the
+// cases that have converged.
+template <typename T, int first>
+__global__ void __launch_bounds__(NTHREADS, first ? 2 : 3) k_cg_true_residual_cols(const CaseDev<T> *__restrict__ cs, int ncases,
+                                                                        int nunits)
 {
     for (int gu = blockIdx.x; gu < nunits; gu += gridDim.x) {
         int lo = 0, hi = ncases - 1;             // the case of unit gu
@@ -676,28 +642,44 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_true_residual_cols(const CaseDe
             if (cs[mid].chunk_begin <= gu) lo = mid; else hi = mid - 1;
         }
         const CaseDev<T> &c = cs[lo];
-        if (c.sc[S_OUTER] < 0.0) continue;      // converged earlier (uniform over the block)
+        if (!first && c.sc[S_OUTER] < 0.0) continue;      // converged (uniform over the block)
         const Geo &g = c.g;
         const int nx = g.nx, ny = g.ny, nz = g.nz;
         const bool px = (c.ccx0 == 0), py = (c.ccy0 == 0);
         const Column cl = column_of(g, gu - c.chunk_begin);
         const int i = cl.i, j = cl.j;
         const long long sx = g.sx, sxy = g.sxy;
-        // Neumann neighbours are the cell itself, periodic ones the opposite end
-        const long long dxp = (i < nx) ? 1 : (px ? -(long long)(nx - 1) : 0);
-        const long long dxm = (i > 1) ? -1 : (px ? (long long)(nx - 1) : 0);
-        const long long dyp = (j < ny) ? sx : (py ? -(long long)(ny - 1) * sx : 0);
-        const long long dym = (j > 1) ? -sx : (py ? (long long)(ny - 1) * sx : 0);
+        // neighbour offsets (interior) and, past the grid, the cell a ghost
+        // stands for: the opposite end (periodic) or the cell itself (Neumann)
+        const bool bxm = i == 1, bxp = i == nx, bym = j == 1, byp = j == ny;
+        const long long mxm = px ? (long long)(nx - 1) : 0, mxp = px ? -(long long)(nx - 1) : 0;
+        const long long mym = py ? (long long)(ny - 1) * sx : 0, myp = py ? -(long long)(ny - 1) * sx : 0;
         const double *__restrict__ e = c.e64;
-        double rr = 0.0, rr32 = 0.0;
+        double rr = 0.0, rr32 = 0.0, bb = 0.0;
         if (cl.v) {
             long long q = g.at(i, j, cl.k0);
             for (int k = cl.k0; k <= cl.k1; ++k, q += sxy) {
-                const long long qzp = (k < nz) ? q + sxy : q;
-                const long long qzm = (k > 1) ? q - sxy : q;
-                const double r = e[q] - c.spi64[q + 1] * e[q + dxp] - c.spi64[q] * e[q + dxm] -
-                                 c.spj64[q + sx] * e[q + dyp] - c.spj64[q] * e[q + dym] - c.spk64[q + sxy] * e[qzp] -
-                                 c.spk64[q] * e[qzm] - c.qpr64[q];
+                const bool bzm = k == 1, bzp = k == nz;
+                double exm, exp_, eym, eyp, ezm, ezp;
+                if constexpr (first != 0) {
+                    // a ghost neighbour: prd1 there times sqrt(D) of the cell it stands for
+                    auto G = [&](long long qg, long long qm) { return (double)c.prd1[qg] * sqrt(c.dpr64[qm]); };
+                    exm = bxm ? G(q - 1, q + mxm) : e[q - 1];
+                    exp_ = bxp ? G(q + 1, q + mxp) : e[q + 1];
+                    eym = bym ? G(q - sx, q + mym) : e[q - sx];
+                    eyp = byp ? G(q + sx, q + myp) : e[q + sx];
+                    ezm = bzm ? G(q - sxy, q) : e[q - sxy];
+                    ezp = bzp ? G(q + sxy, q) : e[q + sxy];
+                } else {
+                    exm = e[bxm ? q + mxm : q - 1];
+                    exp_ = e[bxp ? q + mxp : q + 1];
+                    eym = e[bym ? q + mym : q - sx];
+                    eyp = e[byp ? q + myp : q + sx];
+                    ezm = e[bzm ? q : q - sxy];
+                    ezp = e[bzp ? q : q + sxy];
+                }
+                const double r = e[q] - c.spi64[q + 1] * exp_ - c.spi64[q] * exm - c.spj64[q + sx] * eyp -
+                                 c.spj64[q] * eym - c.spk64[q + sxy] * ezp - c.spk64[q] * ezm - c.qpr64[q];
                 const T r32 = T(r);
                 c.r[q] = r32;
                 c.p[q] = r32;
@@ -705,11 +687,18 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_true_residual_cols(const CaseDe
                 if (c.nlev > 0) c.mg[0].f[q] = sqrt(c.dpr[q]) * r32;   // V-cycle right-hand side D^1/2 r
                 rr += r * r;
                 rr32 += (double)r32 * (double)r32;
+                if constexpr (first != 0) bb += c.qpr64[q] * c.qpr64[q];
             }
         }
-        double vals[2] = {rr, rr32}, tot[2];
-        if (unit_reduce<T, 2>(c, gu, c.chunk_begin, c.nchunks, vals, tot) && tid_lin() == 0)
-            true_residual_update(c, 0, tot[0], tot[1], 0.0);
+        if constexpr (first != 0) {
+            double vals[3] = {rr, rr32, bb}, tot[3];
+            if (unit_reduce<T, 3>(c, gu, c.chunk_begin, c.nchunks, vals, tot) && tid_lin() == 0)
+                true_residual_update(c, 1, tot[0], tot[1], tot[2]);
+        } else {
+            double vals[2] = {rr, rr32}, tot[2];
+            if (unit_reduce<T, 2>(c, gu, c.chunk_begin, c.nchunks, vals, tot) && tid_lin() == 0)
+                true_residual_update(c, 0, tot[0], tot[1], 0.0);
+        }
     }
 }
 
@@ -819,7 +808,7 @@ template <typename T> int launch_cg_iters(const Batch<T> &b, int n, int slot, in
 }
 
 // start of a preconditioned pass on table `slot` (r and the V-cycle's
-// right-hand side written by k_cg_true_residual): z = M r, r.z, p = z
+// right-hand side written by k_cg_true_residual_cols): z = M r, r.z, p = z
 template <typename T> void launch_pcg_start(const Batch<T> &b, int slot, cudaStream_t s)
 {
     const CgGrids<T> &G = cg_grids<T>();
@@ -860,13 +849,15 @@ template <typename T> void launch_cg_refine_setup(const Batch<T> &b, cudaStream_
     k_cg_setup1m<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
     k_cg_setup1mb<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
     k_cg_setup2m<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
-    k_cg_true_residual<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
+    static const int gR = occupancy_grid((const void *)k_cg_true_residual_cols<T, 1>);
+    k_cg_true_residual_cols<T, 1><<<std::min(gR, b.total_units), b.cblock(), 0, s>>>(b.dcases, b.ncases, b.total_units);
+    count_launch();
 }
 template <typename T> void launch_cg_refine_next(const Batch<T> &b, cudaStream_t s)
 {
-    static const int gR = occupancy_grid((const void *)k_cg_true_residual_cols<T>);
+    static const int gR = occupancy_grid((const void *)k_cg_true_residual_cols<T, 0>);
     k_cg_fold<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
-    k_cg_true_residual_cols<T><<<std::min(gR, b.total_units), b.cblock(), 0, s>>>(b.dcases, b.ncases, b.total_units);
+    k_cg_true_residual_cols<T, 0><<<std::min(gR, b.total_units), b.cblock(), 0, s>>>(b.dcases, b.ncases, b.total_units);
     count_launch();
 }
 template <typename T> void launch_cg_refine_finish(const Batch<T> &b, cudaStream_t s)

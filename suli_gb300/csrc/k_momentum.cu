@@ -342,8 +342,15 @@ __global__ void k_sync_masters(const CaseDev<T> *__restrict__ cs, int ncases)
 {
     const CaseDev<T> &c = cs[blockIdx.y];
     if (c.u64 == nullptr) return;
-    const long long n = c.g.total;
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+    // contorno's plane fills are replayed on the masters in FP64; the FP32
+    // writes left to copy are the IBM image points (anywhere in the box) and
+    // the prescribed inflow (planes i = 0 and 1)
+    const bool ibm = (c.obst_t != 0 && c.ibm_t == 2);
+    if (!ibm && c.ccx0 != 3) return;
+    const long long rows = c.g.sxy / c.g.sx * (long long)(c.g.nz + 3);
+    const long long n = ibm ? c.g.total : 2 * rows;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const long long q = ibm ? t : (t % 2) + c.g.sx * (t / 2);
         const T u = c.u[q], v = c.v[q], w = c.w[q], l = c.ls[q];
         if (T(c.u64[q]) != u) c.u64[q] = (double)u;
         if (T(c.v64[q]) != v) c.v64[q] = (double)v;
