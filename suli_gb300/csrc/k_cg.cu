@@ -133,16 +133,22 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_setup1m(const CaseDev<T> *__res
     if (i == 1 && j == 1 && k == 1) c.sc[S_P64OK] = 0.0;   // r64 is reused below
     const bool px = (c.ccx0 == 0);
     const double dt = c.sc[S_DT];
-    const double aux1 = dt * c.idx * c.idx, aux2 = dt * c.idy * c.idy, aux3 = dt * c.idz * c.idz;
     const double *rho = c.rho64;
     const long long q = g.at(i, j, k);
-    // aux / face density, by reciprocal (no FP64 divide)
-    c.spi64[q] = aux1 * rcp_nr64(icf<double>(i, nx, px, [&](int m) { return AT(rho, m, j, k); }));
-    c.spj64[q] = aux2 * rcp_nr64(icf<double>(j, ny, false, [&](int m) { return AT(rho, i, m, k); }));
-    c.spk64[q] = aux3 * rcp_nr64(icf<double>(k, nz, false, [&](int m) { return AT(rho, i, j, m); }));
-    if (i == nx) c.spi64[q + 1] = aux1 * rcp_nr64(icf<double>(nx + 1, nx, px, [&](int m) { return AT(rho, m, j, k); }));
-    if (j == ny) c.spj64[q + g.sx] = aux2 * rcp_nr64(icf<double>(ny + 1, ny, false, [&](int m) { return AT(rho, i, m, k); }));
-    if (k == nz) c.spk64[q + g.sxy] = aux3 * rcp_nr64(icf<double>(nz + 1, nz, false, [&](int m) { return AT(rho, i, j, m); }));
+    // per face: the projection's factor dt / (h rho_face), by reciprocal (no
+    // FP64 divide), kept for posdin; the operator's coefficient is it / h
+    auto face = [&](double *pf, double *sp, long long qf, double a, double ih, double rf) {
+        const double f = a * rcp_nr64(rf);
+        pf[qf] = f;
+        sp[qf] = f * ih;
+    };
+    const double fa = dt * c.idx, fb = dt * c.idy, fc = dt * c.idz;
+    face(c.pfx64, c.spi64, q, fa, c.idx, icf<double>(i, nx, px, [&](int m) { return AT(rho, m, j, k); }));
+    face(c.pfy64, c.spj64, q, fb, c.idy, icf<double>(j, ny, false, [&](int m) { return AT(rho, i, m, k); }));
+    face(c.pfz64, c.spk64, q, fc, c.idz, icf<double>(k, nz, false, [&](int m) { return AT(rho, i, j, m); }));
+    if (i == nx) face(c.pfx64, c.spi64, q + 1, fa, c.idx, icf<double>(nx + 1, nx, px, [&](int m) { return AT(rho, m, j, k); }));
+    if (j == ny) face(c.pfy64, c.spj64, q + g.sx, fb, c.idy, icf<double>(ny + 1, ny, false, [&](int m) { return AT(rho, i, m, k); }));
+    if (k == nz) face(c.pfz64, c.spk64, q + g.sxy, fc, c.idz, icf<double>(nz + 1, nz, false, [&](int m) { return AT(rho, i, j, m); }));
     // the divergence of the FP64 masters: the field that posdin corrects
     double ua, ub, va, vb, wa, wb;
     if (c.u64 != nullptr) {
@@ -547,7 +553,7 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_finish(const CaseDev<T> *__rest
     if (from64) {
         // keep the FP64 pressure too (in r64, free after the solve): posdin
         // forms its pressure differences from it
-        const double p64 = c.e64[q] / sqrt(c.dpr64[q]);
+        const double p64 = c.e64[q] * c.r64[q];     // r64 holds 1/sqrt(D) until here
         c.r64[q] = p64;
         val = T(p64);
         if (i == 1 && j == 1 && k == 1) c.sc[S_P64OK] = 1.0;
@@ -627,12 +633,15 @@ __device__ void true_residual_update(const CaseDev<T> &c, int first, double rrt,
 // walks the COL_Z planes of a column, so the FP64 sums cost one block
 // reduction per COL_Z cells (with one cell per thread, the per-cell share of
 // the FP64 reductions cost more than the residual itself on GB300's FP64
-// units).  first != 0: the solve's first residual, ghost values from prd1 as
-// the reference's warm start has them (matepr = prd1 sqrt(matdpr)), and the
-// right-hand side's r.r for the relative tolerance; later passes skip the
-// cases that have converged.
+// units).  Every pass applies the operator the passes solve: a Neumann
+// neighbour is the cell itself, a periodic one the opposite end.  (The
+// reference's first residual takes the ghost values of the warm start,
+// prd1 sqrt(D) there; the mixed form starts from the same interior values and
+// reads no ghost, which changes only the initial guess.)  first != 0: the
+// solve's first residual, with the right-hand side's r.r for the relative
+// tolerance; later passes skip the cases that have converged.
 template <typename T, int first>
-__global__ void __launch_bounds__(NTHREADS, first ? 2 : 3) k_cg_true_residual_cols(const CaseDev<T> *__restrict__ cs, int ncases,
+__global__ void __launch_bounds__(NTHREADS, 3) k_cg_true_residual_cols(const CaseDev<T> *__restrict__ cs, int ncases,
                                                                         int nunits)
 {
     for (int gu = blockIdx.x; gu < nunits; gu += gridDim.x) {
@@ -660,24 +669,12 @@ __global__ void __launch_bounds__(NTHREADS, first ? 2 : 3) k_cg_true_residual_co
             long long q = g.at(i, j, cl.k0);
             for (int k = cl.k0; k <= cl.k1; ++k, q += sxy) {
                 const bool bzm = k == 1, bzp = k == nz;
-                double exm, exp_, eym, eyp, ezm, ezp;
-                if constexpr (first != 0) {
-                    // a ghost neighbour: prd1 there times sqrt(D) of the cell it stands for
-                    auto G = [&](long long qg, long long qm) { return (double)c.prd1[qg] * sqrt(c.dpr64[qm]); };
-                    exm = bxm ? G(q - 1, q + mxm) : e[q - 1];
-                    exp_ = bxp ? G(q + 1, q + mxp) : e[q + 1];
-                    eym = bym ? G(q - sx, q + mym) : e[q - sx];
-                    eyp = byp ? G(q + sx, q + myp) : e[q + sx];
-                    ezm = bzm ? G(q - sxy, q) : e[q - sxy];
-                    ezp = bzp ? G(q + sxy, q) : e[q + sxy];
-                } else {
-                    exm = e[bxm ? q + mxm : q - 1];
-                    exp_ = e[bxp ? q + mxp : q + 1];
-                    eym = e[bym ? q + mym : q - sx];
-                    eyp = e[byp ? q + myp : q + sx];
-                    ezm = e[bzm ? q : q - sxy];
-                    ezp = e[bzp ? q : q + sxy];
-                }
+                const double exm = e[bxm ? q + mxm : q - 1];
+                const double exp_ = e[bxp ? q + mxp : q + 1];
+                const double eym = e[bym ? q + mym : q - sx];
+                const double eyp = e[byp ? q + myp : q + sx];
+                const double ezm = e[bzm ? q : q - sxy];
+                const double ezp = e[bzp ? q : q + sxy];
                 const double r = e[q] - c.spi64[q + 1] * exp_ - c.spi64[q] * exm - c.spj64[q + sx] * eyp -
                                  c.spj64[q] * eym - c.spk64[q + sxy] * ezp - c.spk64[q] * ezm - c.qpr64[q];
                 const T r32 = T(r);

@@ -95,12 +95,12 @@ __device__ __forceinline__ void load_line(const T *__restrict__ a, long long bas
     }
 }
 
+// rh = 1/h (the host's 1.0 / h, rounded to T)
 template <typename T>
-__device__ __forceinline__ void weno_pm(const T (&L)[7], T h, T &dp, T &dn)
+__device__ __forceinline__ void weno_pm(const T (&L)[7], T rh, T &dp, T &dn)
 {
     T D[6];
 #pragma unroll
-    const T rh = T(1.) / h;
     for (int t = 0; t < 6; ++t) D[t] = (L[t + 1] - L[t]) * rh;
     dp = weno5<T>(D[5], D[4], D[3], D[2], D[1]);
     dn = weno5<T>(D[0], D[1], D[2], D[3], D[4]);
@@ -115,11 +115,11 @@ __device__ __forceinline__ void der_weno_at(const CaseDev<T> &c, const T *__rest
     const Geo &g = c.g;
     T L[7];
     load_line<T>(a, g.at(0, j, k), 1, i, n0, c.ccx0 == 0 ? 0 : 2, L);
-    weno_pm<T>(L, T(c.dx), xp, xm);
+    weno_pm<T>(L, T(c.idx), xp, xm);
     load_line<T>(a, g.at(i, 0, k), g.sx, j, n1, c.ccy0 == 0 ? 0 : 2, L);
-    weno_pm<T>(L, T(c.dy), yp, ym);
+    weno_pm<T>(L, T(c.idy), yp, ym);
     load_line<T>(a, g.at(i, j, 0), g.sxy, k, n2, 2, L);
-    weno_pm<T>(L, T(c.dz), zp, zm);
+    weno_pm<T>(L, T(c.idz), zp, zm);
 }
 template <typename T>
 __device__ __forceinline__ void der_weno_at(const CaseDev<T> &c, const T *__restrict__ a, int i, int j, int k,

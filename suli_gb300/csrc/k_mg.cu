@@ -35,8 +35,10 @@ namespace suli {
 
 // one colour of red-black Gauss-Seidel on L z = f; zero != 0: the sweep
 // starts from z = 0 (this colour gets f / dg, the other colour 0).  The cells
-// of UW tiles are loaded before any is written.
-template <typename T>
+// of UW tiles are loaded before any is written.  L0: the case grid's column
+// path (level 0 only), else the tile path of the coarser levels -- two
+// instantiations, so each keeps its own registers.
+template <typename T, bool L0>
 __global__ void __launch_bounds__(NTHREADS, 4) k_mg_smooth(const CaseDev<T> *__restrict__ cs, const int *__restrict__ tab,
                                                            int N, int l, int color, int zero)
 {
@@ -52,7 +54,7 @@ __global__ void __launch_bounds__(NTHREADS, 4) k_mg_smooth(const CaseDev<T> *__r
         const bool wx = c.ccx0 == 0 && !(nx & 1) && nx > 1;
         const bool wy = c.ccy0 == 0 && !(ny & 1) && ny > 1;
         const T *z = L.z;
-        if (l == 0) {
+        if constexpr (L0) {
             // case grid: one column of COL_Z planes per thread, COL_G planes
             // at a time with every load of a group issued before any
             // arithmetic (the z-neighbours of a cell of this colour have the
@@ -106,45 +108,56 @@ __global__ void __launch_bounds__(NTHREADS, 4) k_mg_smooth(const CaseDev<T> *__r
                 }
             }
             return;
-        }
-        const int t0 = u, t1 = u + 1;
-        TileWalk w(t0, L.ntx, L.nty);
-        for (int lt = t0; lt < t1; lt += UW) {
-            long long q[UW];
-            int ci[UW], cj[UW], ck[UW];
-            bool v[UW];
-            w.next<UW>(lt, t1, g, q, ci, cj, ck, v);
-            T zn[UW];
-            bool wr[UW];
-            if (zero) {
+        } else {
+            const int t0 = u, t1 = u + 1;
+            TileWalk w(t0, L.ntx, L.nty);
+            for (int lt = t0; lt < t1; lt += UW) {
+                long long q[UW];
+                int ci[UW], cj[UW], ck[UW];
+                bool v[UW];
+                w.next<UW>(lt, t1, g, q, ci, cj, ck, v);
+                T zn[UW];
+                bool wr[UW];
+                if (zero) {
 #pragma unroll
-                for (int a = 0; a < UW; ++a) {
-                    const bool mine = ((ci[a] + cj[a] + ck[a]) & 1) == color;
-                    const T di = L.dgi[q[a]], fv = L.f[q[a]];
-                    zn[a] = mine ? fv * di : T(0);
-                    wr[a] = v[a];
-                }
-            } else {
+                    for (int a = 0; a < UW; ++a) {
+                        const bool mine = ((ci[a] + cj[a] + ck[a]) & 1) == color;
+                        const T di = L.dgi[q[a]], fv = L.f[q[a]];
+                        zn[a] = mine ? fv * di : T(0);
+                        wr[a] = v[a];
+                    }
+                } else {
 #pragma unroll
-                for (int a = 0; a < UW; ++a) {
-                    const int i = ci[a], j = cj[a];
-                    const long long qq = q[a];
-                    const long long qxm = (wx && i == 1) ? qq + (nx - 1) : qq - 1;
-                    const long long qxp = (wx && i == nx) ? qq - (nx - 1) : qq + 1;
-                    const long long qym = (wy && j == 1) ? qq + (long long)(ny - 1) * sx : qq - sx;
-                    const long long qyp = (wy && j == ny) ? qq - (long long)(ny - 1) * sx : qq + sx;
-                    const T di = L.dgi[qq];
-                    const T s = L.f[qq] + L.cx[qq] * z[qxm] + L.cx[qq + 1] * z[qxp] + L.cy[qq] * z[qym] +
-                                L.cy[qq + sx] * z[qyp] + L.cz[qq] * z[qq - sxy] + L.cz[qq + sxy] * z[qq + sxy];
-                    zn[a] = s * di;
-                    wr[a] = v[a] && (((i + j + ck[a]) & 1) == color);
+                    for (int a = 0; a < UW; ++a) {
+                        const int i = ci[a], j = cj[a];
+                        const long long qq = q[a];
+                        const long long qxm = (wx && i == 1) ? qq + (nx - 1) : qq - 1;
+                        const long long qxp = (wx && i == nx) ? qq - (nx - 1) : qq + 1;
+                        const long long qym = (wy && j == 1) ? qq + (long long)(ny - 1) * sx : qq - sx;
+                        const long long qyp = (wy && j == ny) ? qq - (long long)(ny - 1) * sx : qq + sx;
+                        const T di = L.dgi[qq];
+                        const T s = L.f[qq] + L.cx[qq] * z[qxm] + L.cx[qq + 1] * z[qxp] + L.cy[qq] * z[qym] +
+                                    L.cy[qq + sx] * z[qyp] + L.cz[qq] * z[qq - sxy] + L.cz[qq + sxy] * z[qq + sxy];
+                        zn[a] = s * di;
+                        wr[a] = v[a] && (((i + j + ck[a]) & 1) == color);
+                    }
                 }
+#pragma unroll
+                for (int a = 0; a < UW; ++a)
+                    if (wr[a]) L.z[q[a]] = zn[a];
             }
-#pragma unroll
-            for (int a = 0; a < UW; ++a)
-                if (wr[a]) L.z[q[a]] = zn[a];
         }
     });
+}
+
+// one half-sweep on level l (the column kernel on the case grid)
+template <typename T>
+void launch_smooth(const Batch<T> &b, const int *tab, int l, int color, int zero, cudaStream_t s)
+{
+    static const int g0 = occupancy_grid((const void *)k_mg_smooth<T, true>);
+    static const int g1 = occupancy_grid((const void *)k_mg_smooth<T, false>);
+    if (l == 0) k_mg_smooth<T, true><<<g0, b.cblock(), 0, s>>>(b.dcases, tab, b.ncases, 0, color, zero);
+    else k_mg_smooth<T, false><<<g1, b.cblock(), 0, s>>>(b.dcases, tab, b.ncases, l, color, zero);
 }
 
 // One whole red-black sweep of the case grid (level 0) in one pass: colour
@@ -533,7 +546,6 @@ template <typename T> void launch_mg_coarsen(const Batch<T> &b, cudaStream_t s)
 template <typename T> void launch_mg_vcycle(const Batch<T> &b, const int *tab, int grid, cudaStream_t s)
 {
     (void)grid;
-    static const int gS = occupancy_grid((const void *)k_mg_smooth<T>);
     static const int gR = occupancy_grid((const void *)k_mg_restrict<T>);
     static const int gP = occupancy_grid((const void *)k_mg_prolong<T>);
     const int N = b.ncases, NL = b.nlev;
@@ -544,6 +556,11 @@ template <typename T> void launch_mg_vcycle(const Batch<T> &b, const int *tab, i
         const char *e = std::getenv("SULI_MG_NU0");
         return (e && std::atoi(e) == 1) ? 1 : 2;
     }();
+    // the same for the coarser levels (SULI_MG_NUC = 1 or 2)
+    static const int nuc = [] {
+        const char *e = std::getenv("SULI_MG_NUC");
+        return (e && std::atoi(e) == 1) ? 1 : 2;
+    }();
     // the case grid's sweeps as one-pass whole sweeps, or (SULI_MG_FUSED=0)
     // as two half-sweep launches each: the same arithmetic
     const char *fe = std::getenv("SULI_MG_FUSED");
@@ -551,7 +568,7 @@ template <typename T> void launch_mg_vcycle(const Batch<T> &b, const int *tab, i
     static const int gW = sweep0_grid<T>();
     const int ncoarse = 6;
     for (int l = 0; l + 1 < NL; ++l) {
-        const int nu = (l == 0) ? nu0 : 2;
+        const int nu = (l == 0) ? nu0 : nuc;
         if (l == 0 && fused) {
             // the buffers alternate so that the last sweep writes z
             for (int it = 0; it < nu; ++it) {
@@ -563,19 +580,19 @@ template <typename T> void launch_mg_vcycle(const Batch<T> &b, const int *tab, i
             continue;
         }
         for (int it = 0; it < nu; ++it) {
-            k_mg_smooth<T><<<gS, b.cblock(), 0, s>>>(b.dcases, tab, N, l, 0, it == 0);
-            k_mg_smooth<T><<<gS, b.cblock(), 0, s>>>(b.dcases, tab, N, l, 1, 0);
+            launch_smooth<T>(b, tab, l, 0, it == 0, s);
+            launch_smooth<T>(b, tab, l, 1, 0, s);
         }
         k_mg_restrict<T><<<gR, b.cblock(), 0, s>>>(b.dcases, tab, N, l + 1);
         count_launch(2 * nu + 1);
     }
     for (int it = 0; it < ncoarse; ++it) {
-        k_mg_smooth<T><<<gS, b.cblock(), 0, s>>>(b.dcases, tab, N, NL - 1, 0, it == 0);
-        k_mg_smooth<T><<<gS, b.cblock(), 0, s>>>(b.dcases, tab, N, NL - 1, 1, 0);
+        launch_smooth<T>(b, tab, NL - 1, 0, it == 0, s);
+        launch_smooth<T>(b, tab, NL - 1, 1, 0, s);
     }
     count_launch(2 * ncoarse);
     for (int l = NL - 2; l >= 0; --l) {
-        const int nu = (l == 0) ? nu0 : 2;
+        const int nu = (l == 0) ? nu0 : nuc;
         if (l == 0 && fused) {
             // black then red; the prolongation writes the buffer the first
             // sweep reads, chosen so that the last sweep writes z
@@ -589,8 +606,8 @@ template <typename T> void launch_mg_vcycle(const Batch<T> &b, const int *tab, i
         }
         k_mg_prolong<T><<<gP, b.cblock(), 0, s>>>(b.dcases, tab, N, l, 0);
         for (int it = 0; it < nu; ++it) {
-            k_mg_smooth<T><<<gS, b.cblock(), 0, s>>>(b.dcases, tab, N, l, 1, 0);
-            k_mg_smooth<T><<<gS, b.cblock(), 0, s>>>(b.dcases, tab, N, l, 0, 0);
+            launch_smooth<T>(b, tab, l, 1, 0, s);
+            launch_smooth<T>(b, tab, l, 0, 0, s);
         }
         count_launch(2 * nu + 1);
     }
@@ -601,8 +618,7 @@ template <typename T> int launch_mg_smooth0(const Batch<T> &b, const int *tab, i
 {
     (void)grid;
     if (b.nlev < 2) return -1;
-    static const int gS = occupancy_grid((const void *)k_mg_smooth<T>);
-    k_mg_smooth<T><<<gS, b.cblock(), 0, s>>>(b.dcases, tab, b.ncases, 0, 0, 0);
+    launch_smooth<T>(b, tab, 0, 0, 0, s);
     count_launch();
     return 0;
 }

@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(NTHREADS) k_convdiff(const CaseDev<T> *__restr
     const T *__restrict__ xmu = c.xmu;
     const T *__restrict__ ymu = c.ymu;
     const T *__restrict__ zmu = c.zmu;
-    const T dx = T(1.0 / c.dx), dy = T(1.0 / c.dy), dz = T(1.0 / c.dz);   // reciprocal spacings
+    const T dx = T(c.idx), dy = T(c.idy), dz = T(c.idz);   // reciprocal spacings (1.0 / dx from the host)
     const bool px = (c.ccx0 == 0);
 
     // ---- Fu at x-face (i,j,k), i in 1..nx+1 ----
@@ -399,26 +399,30 @@ __global__ void __launch_bounds__(NTHREADS) k_posdin(const CaseDev<T> *__restric
             if (p64) return c.r64[g.at(mi(i1), mj(j1), mk(k1))] - c.r64[g.at(mi(i0), mj(j0), mk(k0))];
             return (double)AT(p, i1, j1, k1) - (double)AT(p, i0, j0, k0);
         };
-        // no FP64 divide (a long sequence on GB300's FP64 units): the face
-        // density by reciprocal, the spacings' reciprocals from the host
+        // the face factor dt / (h rho_face): stored by the solve's setup when
+        // its pressure is current, else formed here (by reciprocal: no FP64
+        // divide, a long sequence on GB300's FP64 units)
+        auto factor = [&](const double *pf, long long q, double ih, double rf) {
+            return p64 ? pf[q] : (ddt * ih) * rcp_nr64(rf);
+        };
         if (i <= nx + 1 && j <= ny && k <= nz) {
-            const double rx = interp_cf<double>(i, nx, px, [&](int m) { return AT(r64, m, j, k); });
             const long long q = g.at(i, j, k);
-            const double x = c.u64[q] - dp64(i, j, k, i - 1, j, k) * (ddt * c.idx) * rcp_nr64(rx);
+            const double f = factor(c.pfx64, q, c.idx, p64 ? 1.0 : interp_cf<double>(i, nx, px, [&](int m) { return AT(r64, m, j, k); }));
+            const double x = c.u64[q] - dp64(i, j, k, i - 1, j, k) * f;
             c.u64[q] = x;
             c.u[q] = T(x);
         }
         if (i <= nx && j <= ny + 1 && k <= nz) {
-            const double ry = interp_cf<double>(j, ny, false, [&](int m) { return AT(r64, i, m, k); });
             const long long q = g.at(i, j, k);
-            const double x = c.v64[q] - dp64(i, j, k, i, j - 1, k) * (ddt * c.idy) * rcp_nr64(ry);
+            const double f = factor(c.pfy64, q, c.idy, p64 ? 1.0 : interp_cf<double>(j, ny, false, [&](int m) { return AT(r64, i, m, k); }));
+            const double x = c.v64[q] - dp64(i, j, k, i, j - 1, k) * f;
             c.v64[q] = x;
             c.v[q] = T(x);
         }
         if (i <= nx && j <= ny && k <= nz + 1) {
-            const double rz = interp_cf<double>(k, nz, false, [&](int m) { return AT(r64, i, j, m); });
             const long long q = g.at(i, j, k);
-            const double x = c.w64[q] - dp64(i, j, k, i, j, k - 1) * (ddt * c.idz) * rcp_nr64(rz);
+            const double f = factor(c.pfz64, q, c.idz, p64 ? 1.0 : interp_cf<double>(k, nz, false, [&](int m) { return AT(r64, i, j, m); }));
+            const double x = c.w64[q] - dp64(i, j, k, i, j, k - 1) * f;
             c.w64[q] = x;
             c.w[q] = T(x);
         }
@@ -451,8 +455,8 @@ __global__ void __launch_bounds__(NTHREADS) k_conmassa(const CaseDev<T> *__restr
         double d;
         if (c.u64 != nullptr) {   // mixed form: the FP64 masters
             const double *u = c.u64, *v = c.v64, *w = c.w64;
-            d = (AT(u, i + 1, j, k) - AT(u, i, j, k)) / c.dx + (AT(v, i, j + 1, k) - AT(v, i, j, k)) / c.dy +
-                (AT(w, i, j, k + 1) - AT(w, i, j, k)) / c.dz;
+            d = (AT(u, i + 1, j, k) - AT(u, i, j, k)) * c.idx + (AT(v, i, j + 1, k) - AT(v, i, j, k)) * c.idy +
+                (AT(w, i, j, k + 1) - AT(w, i, j, k)) * c.idz;
         } else {
             const T *u = c.u, *v = c.v, *w = c.w;
             d = ((double)AT(u, i + 1, j, k) - (double)AT(u, i, j, k)) / c.dx +

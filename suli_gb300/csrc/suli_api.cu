@@ -353,7 +353,7 @@ struct Impl : ImplBase {
             T **ptf[] = {&cd.bxx0, &cd.bxx1, &cd.blx1};
             const bool mixed = (sizeof(T) == 4);
             const bool mg = mixed && q.mixed_precond == 1;
-            size_t bytes = fb * ntf + ib * 4 + pb * 3 + (mixed ? 17 * db : 0) + (mg ? 8 * fb : 0);
+            size_t bytes = fb * ntf + ib * 4 + pb * 3 + (mixed ? 20 * db : 0) + (mg ? 8 * fb : 0);
             void *slab = nullptr;
             CK(cudaMalloc(&slab, bytes));
             slabs.push_back(slab);
@@ -365,8 +365,8 @@ struct Impl : ImplBase {
             if (mixed) {
                 double **d64[] = {&cd.e64, &cd.r64, &cd.rho64, &cd.spi64, &cd.spj64, &cd.spk64, &cd.dpr64, &cd.qpr64,
                                   &cd.u64, &cd.v64, &cd.w64, &cd.u064, &cd.v064, &cd.w064,
-                                  &cd.ls64, &cd.lsb64, &cd.lsc64};
-                for (int f = 0; f < 17; ++f) { *d64[f] = (double *)cur; cur += db; }
+                                  &cd.ls64, &cd.lsb64, &cd.lsc64, &cd.pfx64, &cd.pfy64, &cd.pfz64};
+                for (int f = 0; f < 20; ++f) { *d64[f] = (double *)cur; cur += db; }
             }
             if (mg) {
                 // multigrid level 0: the case grid, its box and its tiles

@@ -146,6 +146,9 @@ struct CaseDev {
     // gravity increment, and rounding it leaves noise that the variable-
     // density projection moves into the light phase)
     double *u64, *v64, *w64, *u064, *v064, *w064;
+    // mixed form: the projection's FP64 face factors dt / (h rho_face) of the
+    // last pressure solve (written by k_cg_setup1m, read by posdin)
+    double *pfx64, *pfy64, *pfz64;
     // mixed form: FP64 masters of the level set and its two RK stage buffers
     // (WENO reads the FP32 copies; the stage combinations of advection,
     // reinitialisation and the volume correction accumulate in FP64)
