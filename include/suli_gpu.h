@@ -44,7 +44,7 @@ extern "C" {
 #define SULI_OUT_OF_MEMORY   8
 #define SULI_CG_STALLED      9  /* warning (mixed form, no counterpart in the reference): the FP64
                                    residual of the pressure refinement stopped falling before the
-                                   tolerance; the solve kept its best iterate */
+                                   tolerance; the solve ends on its last pass */
 
 /* ---- precision of a case ----------------------------------------------- */
 #define SULI_PREC_FP64   0  /* plain form: FP64 storage and arithmetic */

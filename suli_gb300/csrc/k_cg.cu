@@ -115,14 +115,19 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_setup2(const CaseDev<T> *__rest
     c.qpr[q] = c.qpr[q] / sD;
 }
 
-// Mixed form: the operator in FP64 from rho64.  setup1m forms each face
-// conductance once (the cell's low faces, and the high faces on the last
-// cell of a line) and the right-hand side; setup1mb sums the diagonal, keeps
-// 1/sqrt(D) in r64 (free until the solve's end) and writes the multigrid's
-// level 0; setup2m scales by products of 1/sqrt(D).  The FP32 iteration uses
-// the rounded scaled coefficients.
+// Mixed form: the operator in FP64 from rho64, built for dt = 1 and kept
+// while the density is unchanged (the three RK stages of a step share it).
+// The stage's operator is dt times it, so each stage solves the unit system
+// L1 p = b / dt for the same pressure, and posdin multiplies the unit face
+// factors by dt; the Jacobi scaling and the multigrid preconditioner do not
+// see a scalar factor.  op1m forms each face conductance once (the cell's
+// low faces, and the high faces on the last cell of a line) with the
+// projection's face factor 1 / (h rho_face); op1mb sums the diagonal,
+// keeps 1/sqrt(D) in r64 and writes the multigrid's level 0; op2m scales by
+// products of 1/sqrt(D).  k_cg_rhs_m then forms each stage's right-hand
+// side.  The FP32 iteration uses the rounded scaled coefficients.
 template <typename T>
-__global__ void __launch_bounds__(NTHREADS) k_cg_setup1m(const CaseDev<T> *__restrict__ cs, int ncases)
+__global__ void __launch_bounds__(NTHREADS) k_cg_op1m(const CaseDev<T> *__restrict__ cs, int ncases)
 {
     const CaseDev<T> &c = cs[find_case(cs, ncases)];
     int i, j, k;
@@ -130,45 +135,26 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_setup1m(const CaseDev<T> *__res
     const Geo &g = c.g;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     if (i > nx || j > ny || k > nz) return;
-    if (i == 1 && j == 1 && k == 1) c.sc[S_P64OK] = 0.0;   // r64 is reused below
     const bool px = (c.ccx0 == 0);
-    const double dt = c.sc[S_DT];
     const double *rho = c.rho64;
     const long long q = g.at(i, j, k);
-    // per face: the projection's factor dt / (h rho_face), by reciprocal (no
-    // FP64 divide), kept for posdin; the operator's coefficient is it / h
-    auto face = [&](double *pf, double *sp, long long qf, double a, double ih, double rf) {
-        const double f = a * rcp_nr64(rf);
+    // per face: the projection's unit factor 1 / (h rho_face), by reciprocal
+    // (no FP64 divide), kept for posdin; the operator's coefficient is it / h
+    auto face = [&](double *pf, double *sp, long long qf, double ih, double rf) {
+        const double f = ih * rcp_nr64(rf);
         pf[qf] = f;
         sp[qf] = f * ih;
     };
-    const double fa = dt * c.idx, fb = dt * c.idy, fc = dt * c.idz;
-    face(c.pfx64, c.spi64, q, fa, c.idx, icf<double>(i, nx, px, [&](int m) { return AT(rho, m, j, k); }));
-    face(c.pfy64, c.spj64, q, fb, c.idy, icf<double>(j, ny, false, [&](int m) { return AT(rho, i, m, k); }));
-    face(c.pfz64, c.spk64, q, fc, c.idz, icf<double>(k, nz, false, [&](int m) { return AT(rho, i, j, m); }));
-    if (i == nx) face(c.pfx64, c.spi64, q + 1, fa, c.idx, icf<double>(nx + 1, nx, px, [&](int m) { return AT(rho, m, j, k); }));
-    if (j == ny) face(c.pfy64, c.spj64, q + g.sx, fb, c.idy, icf<double>(ny + 1, ny, false, [&](int m) { return AT(rho, i, m, k); }));
-    if (k == nz) face(c.pfz64, c.spk64, q + g.sxy, fc, c.idz, icf<double>(nz + 1, nz, false, [&](int m) { return AT(rho, i, j, m); }));
-    // the divergence of the FP64 masters: the field that posdin corrects
-    double ua, ub, va, vb, wa, wb;
-    if (c.u64 != nullptr) {
-        ua = c.u64[q]; ub = c.u64[q + 1]; va = c.v64[q]; vb = c.v64[q + g.sx]; wa = c.w64[q]; wb = c.w64[q + g.sxy];
-    } else {
-        ua = c.u[q]; ub = c.u[q + 1]; va = c.v[q]; vb = c.v[q + g.sx]; wa = c.w[q]; wb = c.w[q + g.sxy];
-    }
-    if (c.obst_t != 0 && c.ibm_t == 2) {
-        if (c.obs_lsx[q] >= T(0.)) ua = 0.;
-        if (c.obs_lsx[q + 1] >= T(0.)) ub = 0.;
-        if (c.obs_lsy[q] >= T(0.)) va = 0.;
-        if (c.obs_lsy[q + g.sx] >= T(0.)) vb = 0.;
-        if (c.obs_lsz[q] >= T(0.)) wa = 0.;
-        if (c.obs_lsz[q + g.sxy] >= T(0.)) wb = 0.;
-    }
-    c.qpr64[q] = (ua - ub) * c.idx + (va - vb) * c.idy + (wa - wb) * c.idz;
+    face(c.pfx64, c.spi64, q, c.idx, icf<double>(i, nx, px, [&](int m) { return AT(rho, m, j, k); }));
+    face(c.pfy64, c.spj64, q, c.idy, icf<double>(j, ny, false, [&](int m) { return AT(rho, i, m, k); }));
+    face(c.pfz64, c.spk64, q, c.idz, icf<double>(k, nz, false, [&](int m) { return AT(rho, i, j, m); }));
+    if (i == nx) face(c.pfx64, c.spi64, q + 1, c.idx, icf<double>(nx + 1, nx, px, [&](int m) { return AT(rho, m, j, k); }));
+    if (j == ny) face(c.pfy64, c.spj64, q + g.sx, c.idy, icf<double>(ny + 1, ny, false, [&](int m) { return AT(rho, i, m, k); }));
+    if (k == nz) face(c.pfz64, c.spk64, q + g.sxy, c.idz, icf<double>(nz + 1, nz, false, [&](int m) { return AT(rho, i, j, m); }));
 }
 
 template <typename T>
-__global__ void __launch_bounds__(NTHREADS) k_cg_setup1mb(const CaseDev<T> *__restrict__ cs, int ncases)
+__global__ void __launch_bounds__(NTHREADS) k_cg_op1mb(const CaseDev<T> *__restrict__ cs, int ncases)
 {
     const CaseDev<T> &c = cs[find_case(cs, ncases)];
     int i, j, k;
@@ -205,7 +191,7 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_setup1mb(const CaseDev<T> *__re
 }
 
 template <typename T>
-__global__ void __launch_bounds__(NTHREADS) k_cg_setup2m(const CaseDev<T> *__restrict__ cs, int ncases)
+__global__ void __launch_bounds__(NTHREADS) k_cg_op2m(const CaseDev<T> *__restrict__ cs, int ncases)
 {
     const CaseDev<T> &c = cs[find_case(cs, ncases)];
     int i, j, k;
@@ -235,8 +221,41 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_setup2m(const CaseDev<T> *__res
         double x = c.spk64[q + g.sxy] * (AT(R, i, j, bmap(nz + 1, nz, false)) * rc);
         c.spk64[q + g.sxy] = x; c.spk[q + g.sxy] = T(x);
     }
-    c.qpr64[q] = c.qpr64[q] * rc;
-    c.qpr[q] = T(c.qpr64[q]);
+}
+
+// A stage's right-hand side on the cached unit operator: the divergence of
+// the FP64 velocity masters (the field that posdin corrects) over dt, scaled
+// by 1/sqrt(D); the warm start prd1 sqrt(D).  e64 stops holding the last
+// pressure here.
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_cg_rhs_m(const CaseDev<T> *__restrict__ cs, int ncases)
+{
+    const CaseDev<T> &c = cs[find_case(cs, ncases)];
+    int i, j, k;
+    tile_ijk(c, i, j, k);
+    const Geo &g = c.g;
+    if (i > g.nx || j > g.ny || k > g.nz) return;
+    if (i == 1 && j == 1 && k == 1) c.sc[S_P64OK] = 0.0;
+    const long long q = g.at(i, j, k);
+    double ua, ub, va, vb, wa, wb;
+    if (c.u64 != nullptr) {
+        ua = c.u64[q]; ub = c.u64[q + 1]; va = c.v64[q]; vb = c.v64[q + g.sx]; wa = c.w64[q]; wb = c.w64[q + g.sxy];
+    } else {
+        ua = c.u[q]; ub = c.u[q + 1]; va = c.v[q]; vb = c.v[q + g.sx]; wa = c.w[q]; wb = c.w[q + g.sxy];
+    }
+    if (c.obst_t != 0 && c.ibm_t == 2) {
+        if (c.obs_lsx[q] >= T(0.)) ua = 0.;
+        if (c.obs_lsx[q + 1] >= T(0.)) ub = 0.;
+        if (c.obs_lsy[q] >= T(0.)) va = 0.;
+        if (c.obs_lsy[q + g.sx] >= T(0.)) vb = 0.;
+        if (c.obs_lsz[q] >= T(0.)) wa = 0.;
+        if (c.obs_lsz[q + g.sxy] >= T(0.)) wb = 0.;
+    }
+    const double rc = c.r64[q];
+    const double b = ((ua - ub) * c.idx + (va - vb) * c.idy + (wa - wb) * c.idz) * c.sc[S_IDT];
+    const double qs = b * rc;
+    c.qpr64[q] = qs;
+    c.qpr[q] = T(qs);
     c.e64[q] = (double)c.prd1[q] * (c.dpr64[q] * rc);   // prd1 sqrt(D)
 }
 
@@ -551,10 +570,10 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_finish(const CaseDev<T> *__rest
     long long q = g.at(i, j, k);
     T val;
     if (from64) {
-        // keep the FP64 pressure too (in r64, free after the solve): posdin
-        // forms its pressure differences from it
-        const double p64 = c.e64[q] * c.r64[q];     // r64 holds 1/sqrt(D) until here
-        c.r64[q] = p64;
+        // keep the FP64 pressure too (in e64, whose scaled solution is not
+        // needed after this): posdin forms its pressure differences from it
+        const double p64 = c.e64[q] * c.r64[q];     // r64: 1/sqrt(D) of the cached operator
+        c.e64[q] = p64;
         val = T(p64);
         if (i == 1 && j == 1 && k == 1) c.sc[S_P64OK] = 1.0;
     } else {
@@ -594,17 +613,20 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_finish(const CaseDev<T> *__rest
 template <typename T>
 __device__ void true_residual_update(const CaseDev<T> &c, int first, double rrt, double rr32, double bb)
 {
-    const double prev = c.sc[S_RRTRUE];
     c.sc[S_RRTRUE] = rrt;
     // stagnation: FP32 passes cannot lower a residual whose worst mode has a
     // condition number near 1/eps(FP32); after three passes that did not
-    // halve r.r the case stops with its best iterate
-    const double stall = first ? 0.0 : ((rrt > 0.5 * prev) ? c.sc[S_STALL] + 1.0 : 0.0);
+    // halve the best r.r so far (the floor is noisy: against the previous
+    // pass a lucky low would restart the count) the case stops
+    const double best = first ? rrt : c.sc[S_RRBEST];
+    const double stall = first ? 0.0 : ((rrt > 0.5 * best) ? c.sc[S_STALL] + 1.0 : 0.0);
     c.sc[S_STALL] = stall;
+    c.sc[S_RRBEST] = fmin(best, rrt);
     if (first) {
         double thr;
         if (c.cg_tol_mode == 1) thr = c.cg_tol * c.cg_tol * bb;
-        else thr = c.cg_tol / ((double)c.g.nx * c.g.ny * c.g.nz);
+        // (the unit operator's r.r is the stage's over dt)
+        else thr = c.cg_tol / ((double)c.g.nx * c.g.ny * c.g.nz) * c.sc[S_IDT];
         c.sc[S_THR] = thr;
         c.sc[S_RR0] = rrt;
         c.sc[S_OUTER] = 0.0;
@@ -841,11 +863,17 @@ template <typename T> void launch_cg_finish(const Batch<T> &b, cudaStream_t s)
 }
 
 // mixed-form pieces
+// the unit-dt FP64 operator (kept while the density is unchanged)
+template <typename T> void launch_cg_refine_operator(const Batch<T> &b, cudaStream_t s)
+{
+    k_cg_op1m<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
+    k_cg_op1mb<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
+    k_cg_op2m<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
+}
+// a stage's right-hand side and first FP64 residual
 template <typename T> void launch_cg_refine_setup(const Batch<T> &b, cudaStream_t s)
 {
-    k_cg_setup1m<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
-    k_cg_setup1mb<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
-    k_cg_setup2m<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
+    k_cg_rhs_m<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
     static const int gR = occupancy_grid((const void *)k_cg_true_residual_cols<T, 1>);
     k_cg_true_residual_cols<T, 1><<<std::min(gR, b.total_units), b.cblock(), 0, s>>>(b.dcases, b.ncases, b.total_units);
     count_launch();
@@ -874,6 +902,7 @@ template int launch_cg_iters<float>(const Batch<float> &, int, int, int, cudaStr
 template void launch_pcg_start<float>(const Batch<float> &, int, cudaStream_t);
 template int launch_pcg_iters<float>(const Batch<float> &, int, int, cudaStream_t);
 template void launch_cg_finish<float>(const Batch<float> &, cudaStream_t);
+template void launch_cg_refine_operator<float>(const Batch<float> &, cudaStream_t);
 template void launch_cg_refine_setup<float>(const Batch<float> &, cudaStream_t);
 template void launch_cg_refine_next<float>(const Batch<float> &, cudaStream_t);
 template void launch_cg_refine_finish<float>(const Batch<float> &, cudaStream_t);

@@ -378,13 +378,13 @@ __global__ void __launch_bounds__(NTHREADS) k_posdin(const CaseDev<T> *__restric
     // pressure of the last solve when it is current (the FP32 pressure loses
     // a digit to cancellation where the hydrostatic part dominates); ghost
     // indices map to the interior cell their Neumann copy / periodic wrap holds
-    const bool p64 = (sizeof(T) == 4) && c.r64 != nullptr && c.sc[S_P64OK] != 0.0;
+    const bool p64 = (sizeof(T) == 4) && c.e64 != nullptr && c.sc[S_P64OK] != 0.0;
     auto dp = [&](int i1, int j1, int k1, int i0, int j0, int k0) -> T {
         if (!p64) return AT(p, i1, j1, k1) - AT(p, i0, j0, k0);
         auto mi = [&](int a) { return a < 1 ? (px ? nx : 1) : (a > nx ? (px ? 1 : nx) : a); };
         auto mj = [&](int a) { return a < 1 ? (py ? ny : 1) : (a > ny ? (py ? 1 : ny) : a); };
         auto mk = [&](int a) { return a < 1 ? 1 : (a > nz ? nz : a); };
-        return T(c.r64[g.at(mi(i1), mj(j1), mk(k1))] - c.r64[g.at(mi(i0), mj(j0), mk(k0))]);
+        return T(c.e64[g.at(mi(i1), mj(j1), mk(k1))] - c.e64[g.at(mi(i0), mj(j0), mk(k0))]);
     };
     if (c.u64 != nullptr) {
         // mixed form: the whole correction in FP64 on the masters, with the
@@ -396,14 +396,15 @@ __global__ void __launch_bounds__(NTHREADS) k_posdin(const CaseDev<T> *__restric
             auto mi = [&](int a) { return a < 1 ? (px ? nx : 1) : (a > nx ? (px ? 1 : nx) : a); };
             auto mj = [&](int a) { return a < 1 ? (py ? ny : 1) : (a > ny ? (py ? 1 : ny) : a); };
             auto mk = [&](int a) { return a < 1 ? 1 : (a > nz ? nz : a); };
-            if (p64) return c.r64[g.at(mi(i1), mj(j1), mk(k1))] - c.r64[g.at(mi(i0), mj(j0), mk(k0))];
+            if (p64) return c.e64[g.at(mi(i1), mj(j1), mk(k1))] - c.e64[g.at(mi(i0), mj(j0), mk(k0))];
             return (double)AT(p, i1, j1, k1) - (double)AT(p, i0, j0, k0);
         };
-        // the face factor dt / (h rho_face): stored by the solve's setup when
-        // its pressure is current, else formed here (by reciprocal: no FP64
-        // divide, a long sequence on GB300's FP64 units)
+        // the face factor dt / (h rho_face): dt times the unit factor the
+        // solve's operator stored, when its pressure is current, else formed
+        // here (by reciprocal: no FP64 divide, a long sequence on GB300's
+        // FP64 units)
         auto factor = [&](const double *pf, long long q, double ih, double rf) {
-            return p64 ? pf[q] : (ddt * ih) * rcp_nr64(rf);
+            return p64 ? ddt * pf[q] : (ddt * ih) * rcp_nr64(rf);
         };
         if (i <= nx + 1 && j <= ny && k <= nz) {
             const long long q = g.at(i, j, k);

@@ -168,6 +168,9 @@ struct ImplBase {
     int replay_cg[3] = {-1, -1, -1}, replay_reinit = -1;
     int reinit_iters = 0, vol_loops = 0;
     int warn = 0;
+    // mixed form: the unit-dt FP64 pressure operator on the device matches
+    // the current density (cleared by every call that may change it)
+    bool op_valid = false;
     // measurement
     bool prof = false;
     unsigned long long launch0 = 0;
@@ -477,6 +480,7 @@ struct Impl : ImplBase {
         double *s = hsc + (size_t)c * S_NSCAL;
         std::memset(s, 0, sizeof(double) * S_NSCAL);
         s[S_DT] = dt;
+        s[S_IDT] = (dt != 0.0) ? 1.0 / dt : 0.0;
         s[S_DTADV] = dt;
         s[S_RINREPLAY] = -1.0;
         s[S_CGREPLAY] = -1.0;
@@ -639,6 +643,7 @@ struct Impl : ImplBase {
     // read the data) once the call returns
     int copy_field(int icase, int f, void *host, bool up) override
     {
+        if (up) op_valid = false;
         bool p64reset = false;
         int rc = enqueue_copy(icase, f, host, up, p64reset);
         if (rc) return rc;
@@ -652,6 +657,7 @@ struct Impl : ImplBase {
     int copy_fields(int n, const int32_t *cases, const int32_t *fields, void *const *hosts, bool up) override
     {
         if (n < 0 || (n > 0 && (!cases || !fields || !hosts))) return fail(SULI_BAD_ARG, "bad transfer list");
+        if (up) op_valid = false;
         std::vector<int> reset;
         for (int q = 0; q < n; ++q) {
             if (!hosts[q]) return fail(SULI_BAD_ARG, "null host pointer");
@@ -739,6 +745,7 @@ struct Impl : ImplBase {
     // ---- routines -------------------------------------------------------------
     int heaviside_init() override
     {
+        op_valid = false;
         launch_heaviside<T>(b, 1, st);
         CKL();
         return read_scalars();
@@ -746,6 +753,7 @@ struct Impl : ImplBase {
 
     int level_set() override
     {
+        op_valid = false;
         int rc;
         if ((rc = setsc(S_DTADV, dt))) return rc;
         if ((rc = setsc(S_RINREPLAY, (double)replay_reinit))) return rc;
@@ -789,6 +797,7 @@ struct Impl : ImplBase {
         if (nlock == 3) {
             // level-set IBM (3_contorno.f90:651-659); nothing without an obstacle
             if (!any_ibm()) return SULI_OK;
+            op_valid = false;
             int rc = setsc(S_RINREPLAY, -1.0);
             if (rc) return rc;
             launch_ibm_levelset<T>(b, st);
@@ -814,6 +823,7 @@ struct Impl : ImplBase {
 
     int ibm_setup() override
     {
+        op_valid = false;
         // obstaculo() for ibm_t = 2 (3_contorno.f90:991-1002): reinitialise the
         // four obstacle level sets, then mark the image points
         for (int t = 1; t <= 4; ++t) launch_reinit<T>(b, P[0].reinit_max_iter, st, t);
@@ -851,7 +861,9 @@ struct Impl : ImplBase {
         if (tt_ < 1 || tt_ > 3) return fail(SULI_BAD_ARG, "stage must be 1..3");
         tt = tt_;
         dt = a_dt[tt - 1];
-        return setsc(S_DT, dt);
+        int rc = setsc(S_DT, dt);
+        if (rc) return rc;
+        return setsc(S_IDT, (dt != 0.0) ? 1.0 / dt : 0.0);
     }
 
     // CG loop: the persistent tile kernels over the active cases (default), or
@@ -915,8 +927,12 @@ struct Impl : ImplBase {
             cg_outer[si] = 0;
         } else {
             const bool mg = b.nlev > 1;
+            if (!op_valid) {
+                launch_cg_refine_operator<T>(b, st);
+                if (mg) launch_mg_coarsen<T>(b, st);
+                op_valid = true;
+            }
             launch_cg_refine_setup<T>(b, st);
-            if (mg) launch_mg_coarsen<T>(b, st);
             CKL();
             int done = 0;
             int passes = 0;
@@ -974,7 +990,8 @@ struct Impl : ImplBase {
         if (prof)
             for (int c = 0; c < ncases; ++c) cg_cell_iters += cells(c) * sc(c, S_CGITER);
         cg_iters[si] = maxit;
-        cg_res[si] = sc(0, sizeof(T) == sizeof(double) ? S_RR : S_RRTRUE);
+        // (the mixed form's r.r is the unit operator's: the stage's over dt)
+        cg_res[si] = (sizeof(T) == sizeof(double)) ? sc(0, S_RR) : sc(0, S_RRTRUE) * dt;
         prev_cg[si] = std::max(1, sizeof(T) == sizeof(double) ? maxit : maxit / std::max(1, cg_outer[si]));
         if (iters) *iters = maxit;
         if (maxit >= cgmax && replay_cg[si] < 0) {

@@ -61,9 +61,11 @@ enum Scal {
     S_RRREF,       // mixed form: FP32 r.r at the last update
     S_RRPREV,      // mixed form: r.r before the pending update
     S_RZ,          // mixed form, multigrid-preconditioned passes: r.z
-    S_P64OK,       // mixed form: r64 holds the FP64 pressure of the last solve
+    S_P64OK,       // mixed form: e64 holds the FP64 pressure of the last solve
     S_PASS0,       // mixed form: CG iteration count at the start of the pass
-    S_STALL,       // mixed form: consecutive passes whose FP64 r.r did not halve
+    S_IDT,         // 1 / dt of the stage (host-set beside S_DT)
+    S_STALL,       // mixed form: consecutive passes that did not halve the best FP64 r.r
+    S_RRBEST,      // mixed form: the lowest FP64 r.r of the solve so far
     S_STALLED,     // mixed form: 1 when the refinement ended on stagnation
     S_NSCAL
 };
@@ -136,7 +138,8 @@ struct CaseDev {
     T *bxx0, *bxx1, *blx1;      // inflow planes, indexed at(0, j, k)
     // CG work arrays
     T *spi, *spj, *spk, *dpr, *e, *r, *p, *mp, *qpr;
-    double *e64, *r64;          // mixed form: FP64 refined solution; FP64 pressure of the last solve
+    double *e64, *r64;          // mixed form: FP64 refined solution (after the solve: the FP64
+                                // pressure); 1/sqrt(D) of the cached operator
     // mixed form: FP64 pressure operator for the refinement residual (density
     // from the FP32 level set in FP64, scaled face coefficients, diagonal, rhs)
     double *rho64, *spi64, *spj64, *spk64, *dpr64, *qpr64;
@@ -146,8 +149,8 @@ struct CaseDev {
     // gravity increment, and rounding it leaves noise that the variable-
     // density projection moves into the light phase)
     double *u64, *v64, *w64, *u064, *v064, *w064;
-    // mixed form: the projection's FP64 face factors dt / (h rho_face) of the
-    // last pressure solve (written by k_cg_setup1m, read by posdin)
+    // mixed form: the projection's FP64 unit face factors 1 / (h rho_face) of
+    // the cached pressure operator (written by k_cg_op1m, read by posdin)
     double *pfx64, *pfy64, *pfz64;
     // mixed form: FP64 masters of the level set and its two RK stage buffers
     // (WENO reads the FP32 copies; the stage combinations of advection,

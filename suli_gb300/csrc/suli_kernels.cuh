@@ -90,6 +90,7 @@ template <typename T> void launch_mg_coarsen(const Batch<T> &b, cudaStream_t s);
 template <typename T> void launch_mg_vcycle(const Batch<T> &b, const int *tab, int grid, cudaStream_t s);
 template <typename T> void launch_cg_finish(const Batch<T> &b, cudaStream_t s);
 // mixed form: FP64 residual recomputation and correction around the FP32 inner CG
+template <typename T> void launch_cg_refine_operator(const Batch<T> &b, cudaStream_t s);
 template <typename T> void launch_cg_refine_setup(const Batch<T> &b, cudaStream_t s);
 template <typename T> void launch_cg_refine_next(const Batch<T> &b, cudaStream_t s);
 template <typename T> void launch_cg_refine_finish(const Batch<T> &b, cudaStream_t s);
