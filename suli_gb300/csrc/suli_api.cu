@@ -927,6 +927,10 @@ struct Impl : ImplBase {
             cg_outer[si] = 0;
         } else {
             const bool mg = b.nlev > 1;
+            // SULI_OP_CACHE=0: rebuild the operator in every solve (the
+            // reference's order of work; the same bits)
+            const char *oc = std::getenv("SULI_OP_CACHE");
+            if (oc && std::atoi(oc) == 0) op_valid = false;
             if (!op_valid) {
                 launch_cg_refine_operator<T>(b, st);
                 if (mg) launch_mg_coarsen<T>(b, st);

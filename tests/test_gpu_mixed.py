@@ -175,6 +175,29 @@ def test_refinement_stops_when_the_fp64_residual_stagnates(gpu_lib, precond):
     assert flags & (1 << SULI_CG_STALLED)
 
 
+def test_cached_operator_matches_rebuilt_operator(gpu_lib, monkeypatch):
+    """The mixed form builds its FP64 pressure operator once per density and
+    reuses it across RK stages; SULI_OP_CACHE=0 rebuilds it in every solve.
+    Both give the same bits, also across a level-set upload and Heaviside
+    recompute in mid-run (which must mark the cached operator stale)."""
+    dims, hcol, amp = cases.ensemble_dims(2, seed=4, lo=16, hi=28)
+    out = {}
+    for mode in ("1", "0"):
+        monkeypatch.setenv("SULI_OP_CACHE", mode)
+        cs = [cases.ensemble_case(i, dims, hcol, amp, precision=PREC_MIXED) for i in range(2)]
+        g = gpu_lib.SuliGPU([c.params for c in cs])
+        g.start([c.fields for c in cs])
+        g.step(2)
+        ls = g.download("LS", 0)
+        g.upload("LS", ls + 0.02 * ls.max(), 0)       # the free surface moves: new density
+        g.heaviside_init()
+        g.step(2)
+        out[mode] = [g.download(n, i) for i in range(2) for n in ("U", "V", "W", "PRD1")]
+        g.close()
+    for a, b in zip(out["1"], out["0"]):
+        assert np.array_equal(a, b)
+
+
 @pytest.mark.parametrize("mk", ["periodic_even", "periodic_odd", "uneven_batch"])
 def test_one_pass_sweeps_match_half_sweeps(gpu_lib, monkeypatch, mk):
     """The case grid's one-pass whole sweeps (the default; the first colour
