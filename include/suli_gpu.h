@@ -129,6 +129,8 @@ enum suli_field {
     SULI_F_BXX0,     /* bxx0 (0:ny+1, 0:nz+1) inflow u at i = 0 */
     SULI_F_BXX1,     /* bxx1 (0:ny+1, 0:nz+1) inflow u at i = 1 */
     SULI_F_BLX1,     /* blx1 (ny, nz) inflow ls at i = 1 */
+    SULI_F_OBS_LS,   /* obs_ls (nx1, ny1, nz1) obstacle level set at the cell corners, written by
+                        obstaculo() for the field output (3_contorno.f90:905-911, 4_plot.f90:570) */
     SULI_F_COUNT
 };
 
@@ -247,6 +249,30 @@ int suli_profile_read(suli_handle *h, suli_profile_t *out);
  * moves.  The solver work arrays it touches are rebuilt by the next
  * suli_graddin. */
 int suli_time_kernel(suli_handle *h, int kernel, int reps, double *ms_per_launch, double *bytes_per_launch);
+/* PRTSCR (4_plot.f90:501-635), the field record of one case: written to
+ * `path` as one Fortran unformatted sequential record (gfortran framing: a
+ * 4-byte little-endian byte count before and after) of float32 arrays in
+ * Fortran order -- x, y, z of the cell corners (nx+1, ny+1, nz+1), u, v, w
+ * averaged to the corners, ls (nx, ny, nz), obs_ls at the corners (zero
+ * without an obstacle), and with t_plot = 1 the pressure minus its value at
+ * cell (nx, 1, nz), the three vorticity components, nut and ka (zeros: the
+ * k-equation model is not part of this library).  The record is formed on
+ * the device and copied once into pinned host memory.  The file name and the
+ * output cadence (dt_frame) are the caller's, as is the XDMF index (visu,
+ * 12_paraview_3D.f90).  SULI_BAD_ARG when the file cannot be written or the
+ * record exceeds 2^31 - 1 bytes. */
+int suli_write_fields(suli_handle *h, int icase, const char *path, int t_plot);
+/* restart_salva / restart_ini (11_diversos.f90:500-599, called from
+ * 1_principal.f90:38 and :120-122) as a binary file: every field of every
+ * case in the reference layouts (FP64; the IBM masks int32), t, it, dt, the
+ * inflow draws and the stage, and per case vol_ini / vol_ins.  Unlike the
+ * reference, which reads its text dump back and then resets t and it to
+ * zero, suli_restart_load restores them, so a run that is saved, loaded into
+ * a handle created with the same parameters and continued matches the run
+ * that was never interrupted.  SULI_BAD_CONFIG when the file is not a
+ * restart of this library or was written for other cases. */
+int suli_restart_save(suli_handle *h, const char *path);
+int suli_restart_load(suli_handle *h, const char *path);
 
 /* Divergence and max|div| of a velocity field held in caller-owned device
  * memory, computing exactly what suli_conmassa computes, but allocating no

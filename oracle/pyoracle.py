@@ -56,6 +56,8 @@ def lib():
         L.or_graddin.restype = C.c_int
         L.or_conmassa.argtypes = [C.c_void_p]
         L.or_conmassa.restype = C.c_double
+        L.or_prtscr_write.argtypes = [C.c_void_p, C.c_char_p, C.c_int]
+        L.or_prtscr_write.restype = C.c_int
         L.or_mms_error.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.or_set_stage.argtypes = [C.c_void_p, C.c_int]
         L.or_diag.argtypes = [C.c_void_p, C.POINTER(SuliDiag)]
@@ -167,6 +169,12 @@ class Oracle:
 
     def conmassa(self) -> float:
         return lib().or_conmassa(self._h)
+
+    def prtscr_write(self, path: str, t_plot: int = 0):
+        """The PRTSCR field record (4_plot.f90:547-615) as a Fortran
+        unformatted file."""
+        if lib().or_prtscr_write(self._h, str(path).encode(), int(t_plot)) != 0:
+            raise OSError("or_prtscr_write failed for %s" % path)
 
     def mms_error(self):
         e = (C.c_double * 4)()

@@ -96,6 +96,7 @@ struct or_case {
     F3 Fu, Fv, Fw, u0, v0, w0, fu0, fv0, fw0, fu1, fv1, fw1, div;
     F3 tf_u, tf_v, tf_w;
     F3 obs_lsx, obs_lsy, obs_lsz, obs_lss;
+    F3 obs_ls;                 /* obs_ls (nx1, ny1, nz1), cell corners: field output only */
     I3 id_ibmx, id_ibmy, id_ibmz, id_ibm;
     F3 bxx0, bxx1, blx1;
 
@@ -148,6 +149,7 @@ or_case *or_create(const suli_params *pp)
     F3 *fz[] = {&c->Fw, &c->w0, &c->fw0, &c->fw1, &c->tf_w, &c->obs_lsz};
     for (int q = 0; q < 6; ++q) f3_init(fz[q], 1, nx, 1, ny, 1, nz1);
     f3_init(&c->obs_lss, 1, nx, 1, ny, 1, nz);
+    f3_init(&c->obs_ls, 1, nx1, 1, ny1, 1, nz1);
     i3_init(&c->id_ibmx, 1, nx1, 1, ny, 1, nz);
     i3_init(&c->id_ibmy, 1, nx, 1, ny1, 1, nz);
     i3_init(&c->id_ibmz, 1, nx, 1, ny, 1, nz1);
@@ -188,7 +190,7 @@ void or_destroy(or_case *c)
                  &c->mu, &c->mut, &c->xmu, &c->ymu, &c->zmu, &c->Fu, &c->Fv, &c->Fw, &c->u0,
                  &c->v0, &c->w0, &c->fu0, &c->fv0, &c->fw0, &c->fu1, &c->fv1, &c->fw1, &c->div,
                  &c->tf_u, &c->tf_v, &c->tf_w, &c->obs_lsx, &c->obs_lsy, &c->obs_lsz,
-                 &c->obs_lss, &c->bxx0, &c->bxx1, &c->blx1};
+                 &c->obs_lss, &c->bxx0, &c->bxx1, &c->blx1, &c->obs_ls};
     for (unsigned q = 0; q < sizeof(all) / sizeof(all[0]); ++q) free(all[q]->p);
     free(c->id_ibmx.p); free(c->id_ibmy.p); free(c->id_ibmz.p); free(c->id_ibm.p);
     free(c);
@@ -233,6 +235,7 @@ void *or_field(or_case *c, int f, int lo[3], int hi[3])
     case SULI_F_OBS_LSY: a = &c->obs_lsy; break;
     case SULI_F_OBS_LSZ: a = &c->obs_lsz; break;
     case SULI_F_OBS_LSS: a = &c->obs_lss; break;
+    case SULI_F_OBS_LS: a = &c->obs_ls; break;
     case SULI_F_ID_IBMX: ia = &c->id_ibmx; break;
     case SULI_F_ID_IBMY: ia = &c->id_ibmy; break;
     case SULI_F_ID_IBMZ: ia = &c->id_ibmz; break;
@@ -1543,6 +1546,73 @@ double or_conmassa(or_case *c)
             }
     c->maxdiv = m;
     return m;
+}
+
+/* PRTSCR field record, 4_plot.f90:547-615 (prd0 = 0: it changes only with
+ * the IPA pressure option; nut and ka belong to the k-equation model and are
+ * written as zeros; the manufactured-solution variant that writes error
+ * fields is not restated).  One Fortran unformatted sequential record of
+ * float32 arrays, gfortran framing (a 4-byte little-endian byte count before
+ * and after).  Returns 0, or -1 when the file cannot be written or the
+ * record exceeds 2^31 - 1 bytes. */
+int or_prtscr_write(or_case *c, const char *path, int t_plot)
+{
+    const int nx = c->nx, ny = c->ny, nz = c->nz, nx1 = c->nx1, ny1 = c->ny1, nz1 = c->nz1;
+    const long n1 = (long)nx1 * ny1 * nz1, nc = (long)nx * ny * nz;
+    const long nf = 7 * n1 + nc + (t_plot ? 6 * nc : 0);
+    if (nf * 4 > 2147483647L) return -1;
+    float *r = (float *)calloc((size_t)nf, sizeof(float));
+    if (!r) return -1;
+    float *x11 = r, *y11 = r + n1, *z11 = r + 2 * n1, *ua = r + 3 * n1, *va = r + 4 * n1, *wa = r + 5 * n1;
+    float *lso = r + 6 * n1, *obs = lso + nc;
+    /* node coordinates by running sums from -dx, -dy, -dz (:553-569) */
+    double *x1 = (double *)malloc(sizeof(double) * (nx1 + 1)), *y1 = (double *)malloc(sizeof(double) * (ny1 + 1)),
+           *z1 = (double *)malloc(sizeof(double) * (nz1 + 1));
+    x1[0] = -c->dx; y1[0] = -c->dy; z1[0] = -c->dz;
+    for (int i = 1; i <= nx1; ++i) x1[i] = x1[i - 1] + c->dx;
+    for (int j = 1; j <= ny1; ++j) y1[j] = y1[j - 1] + c->dy;
+    for (int k = 1; k <= nz1; ++k) z1[k] = z1[k - 1] + c->dz;
+    for (int k = 1; k <= nz1; ++k)
+        for (int j = 1; j <= ny1; ++j)
+            for (int i = 1; i <= nx1; ++i) {
+                const long q = (i - 1) + (long)nx1 * ((j - 1) + (long)ny1 * (k - 1));
+                x11[q] = (float)x1[i];
+                y11[q] = (float)y1[j];
+                z11[q] = (float)z1[k];
+                ua[q] = (float)((A(c->u, i, j, k) + A(c->u, i, j - 1, k) + A(c->u, i, j, k - 1) + A(c->u, i, j - 1, k - 1)) * 0.25);
+                va[q] = (float)((A(c->v, i, j, k) + A(c->v, i - 1, j, k) + A(c->v, i, j, k - 1) + A(c->v, i - 1, j, k - 1)) * 0.25);
+                wa[q] = (float)((A(c->w, i, j, k) + A(c->w, i, j - 1, k) + A(c->w, i - 1, j, k) + A(c->w, i - 1, j - 1, k)) * 0.25);
+                obs[q] = (c->p.obst_t == 0) ? 0.0f : (float)A(c->obs_ls, i, j, k);
+            }
+    free(x1); free(y1); free(z1);
+    float *pr = obs + n1, *vi = pr + nc, *vj = vi + nc, *vk = vj + nc;   /* nut, ka: zeros */
+    const double pref = A(c->prd1, nx, 1, nz);
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i) {
+                const long q = (i - 1) + (long)nx * ((j - 1) + (long)ny * (k - 1));
+                lso[q] = (float)A(c->ls, i, j, k);
+                if (!t_plot) continue;
+                pr[q] = (float)(A(c->prd1, i, j, k) - pref);
+                const double dudy = (A(c->u, i, j + 1, k) - A(c->u, i, j, k)) / c->dy;
+                const double dudz = (A(c->u, i, j, k + 1) - A(c->u, i, j, k)) / c->dz;
+                const double dvdx = (A(c->v, i + 1, j, k) - A(c->v, i, j, k)) / c->dx;
+                const double dvdz = (A(c->v, i, j, k + 1) - A(c->v, i, j, k)) / c->dz;
+                const double dwdx = (A(c->w, i + 1, j, k) - A(c->w, i, j, k)) / c->dx;
+                const double dwdy = (A(c->w, i, j + 1, k) - A(c->w, i, j, k)) / c->dy;
+                vi[q] = (float)(dwdy - dvdz);
+                vj[q] = (float)(dudz - dwdx);
+                vk[q] = (float)(dvdx - dudy);
+            }
+    FILE *fp = fopen(path, "wb");
+    int rc = -1;
+    if (fp) {
+        const int32_t len = (int32_t)(nf * 4);
+        if (fwrite(&len, 4, 1, fp) == 1 && fwrite(r, 4, (size_t)nf, fp) == (size_t)nf && fwrite(&len, 4, 1, fp) == 1) rc = 0;
+        if (fclose(fp) != 0) rc = -1;
+    }
+    free(r);
+    return rc;
 }
 
 /* ------------------------------------------------------------------------ */

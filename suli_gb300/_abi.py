@@ -111,7 +111,7 @@ FIELDS = [
     "FW0", "FU1", "FV1", "FW1", "DIV", "TF_U", "TF_V", "TF_W",
     "OBS_LSX", "OBS_LSY", "OBS_LSZ", "OBS_LSS",
     "ID_IBMX", "ID_IBMY", "ID_IBMZ", "ID_IBM",
-    "BXX0", "BXX1", "BLX1",
+    "BXX0", "BXX1", "BLX1", "OBS_LS",
 ]
 FIELD_ID = {name: i for i, name in enumerate(FIELDS)}
 INT_FIELDS = {"ID_IBMX", "ID_IBMY", "ID_IBMZ", "ID_IBM"}
@@ -137,6 +137,7 @@ def field_bounds(p: SuliParams, name: str):
         "BXX0": ((0, 0, 0), (ny + 1, nz + 1, 0)),
         "BXX1": ((0, 0, 0), (ny + 1, nz + 1, 0)),
         "BLX1": ((1, 1, 0), (ny, nz, 0)),
+        "OBS_LS": ((1, 1, 1), (nx1, ny1, nz1)),
     }
     if name in table:
         return table[name]

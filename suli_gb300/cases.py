@@ -171,11 +171,15 @@ def cylinder_obstacle(p: SuliParams, xc: float, yc: float, radius: float) -> dic
         out[...] = phi(fi(i), fj(j))
         return out
 
+    # obs_ls at the cell corners for the field output: the sub-grid's odd
+    # points 2i-1 (3_contorno.f90:905-911)
+
     return {
         "OBS_LSX": field(nx + 1, ny, nz, lambda i: 2 * i - 1, lambda j: 2 * j),
         "OBS_LSY": field(nx, ny + 1, nz, lambda i: 2 * i, lambda j: 2 * j - 1),
         "OBS_LSZ": field(nx, ny, nz + 1, lambda i: 2 * i, lambda j: 2 * j),
         "OBS_LSS": field(nx, ny, nz, lambda i: 2 * i, lambda j: 2 * j),
+        "OBS_LS": field(nx + 1, ny + 1, nz + 1, lambda i: 2 * i - 1, lambda j: 2 * j - 1),
     }
 
 

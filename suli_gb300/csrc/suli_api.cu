@@ -96,6 +96,7 @@ extern "C" int suli_field_shape(const suli_params *p, int f, int lo[3], int hi[3
         set(1, nx, 1, ny, 1, nz1); break;
     case SULI_F_BXX0: case SULI_F_BXX1: set(0, ny + 1, 0, nz + 1, 0, 0); break;
     case SULI_F_BLX1: set(1, ny, 1, nz, 0, 0); break;
+    case SULI_F_OBS_LS: set(1, nx1, 1, ny1, 1, nz1); break;
     default: return fail(SULI_BAD_ARG, "unknown field id " + std::to_string(f));
     }
     return SULI_OK;
@@ -155,6 +156,7 @@ struct ImplBase {
     virtual int write_case_scalar(int icase, int slot, double v) = 0;
     virtual int sync() = 0;
     virtual int time_kernel(int kernel, int reps, double *ms, double *bytes) = 0;
+    virtual int write_fields(int icase, const char *path, int t_plot) = 0;
     virtual int ibm_setup() = 0;
     unsigned long long inflow_calls = 0;
     int ncases = 0;
@@ -292,7 +294,66 @@ struct Impl : ImplBase {
         cudaFree(drk);
         cudaFree(b.dcases);
         if (hsc) cudaFreeHost(hsc);
+        cudaFree(out_dev);
+        if (out_host) cudaFreeHost(out_host);
         if (st) cudaStreamDestroy(st);
+    }
+
+    // field output (PRTSCR record): device staging and pinned host buffers,
+    // grown on demand
+    float *out_dev = nullptr, *out_host = nullptr;
+    size_t out_dev_cap = 0, out_host_cap = 0;
+
+    int write_fields(int icase, const char *path, int t_plot) override
+    {
+        if (icase < 0 || icase >= ncases) return fail(SULI_BAD_ARG, "case index out of range");
+        if (!path || (t_plot != 0 && t_plot != 1)) return fail(SULI_BAD_ARG, "bad path or t_plot (0 or 1)");
+        const suli_params &q = P[icase];
+        const long long nx1 = q.nx + 1, ny1 = q.ny + 1, nz1 = q.nz + 1;
+        const long long n1 = nx1 * ny1 * nz1, nc = (long long)q.nx * q.ny * q.nz;
+        const long long ndev = 4 * n1 + nc + (t_plot ? 6 * nc : 0), nf = 3 * n1 + ndev;
+        if (nf * 4 > 2147483647LL) return fail(SULI_BAD_ARG, "the record exceeds one Fortran record (2^31 - 1 bytes)");
+        if ((size_t)ndev > out_dev_cap) {
+            cudaFree(out_dev);
+            out_dev = nullptr;
+            out_dev_cap = 0;
+            CK(cudaMalloc(&out_dev, sizeof(float) * ndev));
+            out_dev_cap = (size_t)ndev;
+        }
+        if ((size_t)nf > out_host_cap) {
+            if (out_host) cudaFreeHost(out_host);
+            out_host = nullptr;
+            out_host_cap = 0;
+            CK(cudaMallocHost(&out_host, sizeof(float) * nf));
+            out_host_cap = (size_t)nf;
+        }
+        launch_prtscr<T>(b, icase, out_dev, t_plot, st);
+        CK(cudaMemcpyAsync(out_host + 3 * n1, out_dev, sizeof(float) * ndev, cudaMemcpyDeviceToHost, st));
+        // node coordinates while the copy is in flight: running sums from -dx,
+        // -dy, -dz as the reference forms them (4_plot.f90:553-564)
+        std::vector<double> x1(nx1 + 1), y1(ny1 + 1), z1(nz1 + 1);
+        x1[0] = -q.dx; y1[0] = -q.dy; z1[0] = -q.dz;
+        for (long long i = 1; i <= nx1; ++i) x1[i] = x1[i - 1] + q.dx;
+        for (long long j = 1; j <= ny1; ++j) y1[j] = y1[j - 1] + q.dy;
+        for (long long k = 1; k <= nz1; ++k) z1[k] = z1[k - 1] + q.dz;
+        float *xo = out_host, *yo = out_host + n1, *zo = out_host + 2 * n1;
+        for (long long k = 1, o = 0; k <= nz1; ++k)
+            for (long long j = 1; j <= ny1; ++j)
+                for (long long i = 1; i <= nx1; ++i, ++o) {
+                    xo[o] = (float)x1[i];
+                    yo[o] = (float)y1[j];
+                    zo[o] = (float)z1[k];
+                }
+        CK(cudaStreamSynchronize(st));
+        CKL();
+        std::FILE *fp = std::fopen(path, "wb");
+        if (!fp) return fail(SULI_BAD_ARG, std::string("cannot open ") + path);
+        const int32_t len = (int32_t)(nf * 4);
+        bool ok = std::fwrite(&len, 4, 1, fp) == 1 && std::fwrite(out_host, 4, (size_t)nf, fp) == (size_t)nf &&
+                  std::fwrite(&len, 4, 1, fp) == 1;
+        ok = (std::fclose(fp) == 0) && ok;
+        if (!ok) return fail(SULI_BAD_ARG, std::string("writing ") + path + " failed");
+        return SULI_OK;
     }
 
     int create(const suli_params *p, int n)
@@ -350,7 +411,7 @@ struct Impl : ImplBase {
                         &cd.rho, &cd.ls_mu, &cd.mu, &cd.mut, &cd.xmu, &cd.ymu, &cd.zmu, &cd.Fu, &cd.Fv, &cd.Fw,
                         &cd.u0, &cd.v0, &cd.w0, &cd.fu0, &cd.fv0, &cd.fw0, &cd.fu1, &cd.fv1, &cd.fw1, &cd.div,
                         &cd.tf_u, &cd.tf_v, &cd.tf_w, &cd.obs_lsx, &cd.obs_lsy, &cd.obs_lsz, &cd.obs_lss,
-                        &cd.spi, &cd.spj, &cd.spk, &cd.dpr, &cd.e, &cd.r, &cd.p, &cd.mp, &cd.qpr};
+                        &cd.spi, &cd.spj, &cd.spk, &cd.dpr, &cd.e, &cd.r, &cd.p, &cd.mp, &cd.qpr, &cd.obs_ls};
             const int ntf = sizeof(tf) / sizeof(tf[0]);
             int **itf[] = {&cd.id_ibmx, &cd.id_ibmy, &cd.id_ibmz, &cd.id_ibm};
             T **ptf[] = {&cd.bxx0, &cd.bxx1, &cd.blx1};
@@ -628,6 +689,7 @@ struct Impl : ImplBase {
         case SULI_F_OBS_LSY: return c.obs_lsy;
         case SULI_F_OBS_LSZ: return c.obs_lsz;
         case SULI_F_OBS_LSS: return c.obs_lss;
+        case SULI_F_OBS_LS: return c.obs_ls;
         case SULI_F_ID_IBMX: return c.id_ibmx;
         case SULI_F_ID_IBMY: return c.id_ibmy;
         case SULI_F_ID_IBMZ: return c.id_ibmz;
@@ -1301,6 +1363,159 @@ extern "C" int suli_time_kernel(suli_handle *h, int kernel, int reps, double *ms
     HCHK();
     if (!ms_per_launch || !bytes_per_launch) return fail(SULI_BAD_ARG, "null pointer");
     return h->impl->time_kernel(kernel, reps, ms_per_launch, bytes_per_launch);
+}
+
+extern "C" int suli_write_fields(suli_handle *h, int icase, const char *path, int t_plot)
+{
+    HCHK();
+    return h->impl->write_fields(icase, path, t_plot);
+}
+
+// ---- restart: a binary replacement of restart_salva / restart_ini
+// (11_diversos.f90:500-599), which write every state array as formatted text
+// and, on reading, reset t and it to zero.  The file holds, little-endian:
+// "SULIRST1", int32 version (1), int32 cases, int32 field count, double t,
+// int64 it, double dt, uint64 inflow draws, int32 stage; per case int32
+// nx, ny, nz, double vol_ini, vol_ins; per case and field int32 id, int64
+// count, then the values in the reference layout (double; int32 for the IBM
+// masks).  Loading restores the fields, t, it, dt and the counters, so the
+// run continues exactly where it was saved.
+static const char kRestartMagic[8] = {'S', 'U', 'L', 'I', 'R', 'S', 'T', '1'};
+
+static long long field_count(const suli_params &p, int f)
+{
+    int lo[3], hi[3];
+    if (suli_field_shape(&p, f, lo, hi) != SULI_OK) return -1;
+    long long n = 1;
+    for (int d = 0; d < 3; ++d) n *= (long long)(hi[d] - lo[d] + 1);
+    return n;
+}
+
+// every field of case c through one batched transfer (up: host -> device)
+static int restart_fields(ImplBase *im, int c, std::vector<std::vector<double>> &dv,
+                          std::vector<std::vector<int32_t>> &iv, bool up)
+{
+    std::vector<int32_t> cases, fields;
+    std::vector<void *> hosts;
+    dv.resize(SULI_F_COUNT);
+    iv.resize(SULI_F_COUNT);
+    for (int f = 0; f < SULI_F_COUNT; ++f) {
+        const long long n = field_count(im->P[c], f);
+        if (n < 0) return fail(SULI_BAD_ARG, "field shape");
+        if (is_int_field(f)) {
+            iv[f].resize((size_t)n);
+            hosts.push_back(iv[f].data());
+        } else {
+            dv[f].resize((size_t)n);
+            hosts.push_back(dv[f].data());
+        }
+        cases.push_back(c);
+        fields.push_back(f);
+    }
+    if (up) return SULI_OK;    // the caller fills the buffers, then transfers
+    return im->copy_fields((int)fields.size(), cases.data(), fields.data(), hosts.data(), false);
+}
+
+extern "C" int suli_restart_save(suli_handle *h, const char *path)
+{
+    HCHK();
+    ImplBase *im = h->impl;
+    if (!path) return fail(SULI_BAD_ARG, "null path");
+    int rc = im->read_scalars();
+    if (rc) return rc;
+    std::FILE *fp = std::fopen(path, "wb");
+    if (!fp) return fail(SULI_BAD_ARG, std::string("cannot open ") + path);
+    bool ok = true;
+    auto put = [&](const void *p, size_t n) { ok = ok && std::fwrite(p, 1, n, fp) == n; };
+    const int32_t version = 1, nc = im->ncases, nf = SULI_F_COUNT, tt = im->tt;
+    const int64_t it = im->it;
+    const uint64_t draws = im->inflow_calls;
+    put(kRestartMagic, 8); put(&version, 4); put(&nc, 4); put(&nf, 4);
+    put(&im->t, 8); put(&it, 8); put(&im->dt, 8); put(&draws, 8); put(&tt, 4);
+    for (int c = 0; c < nc; ++c) {
+        const int32_t d[3] = {im->P[c].nx, im->P[c].ny, im->P[c].nz};
+        const double *sc = im->hsc + (size_t)c * S_NSCAL;
+        put(d, 12); put(&sc[S_VOLINI], 8); put(&sc[S_VOLINS], 8);
+    }
+    for (int c = 0; c < nc && ok; ++c) {
+        std::vector<std::vector<double>> dv;
+        std::vector<std::vector<int32_t>> iv;
+        rc = restart_fields(im, c, dv, iv, false);
+        if (rc) { std::fclose(fp); return rc; }
+        for (int f = 0; f < SULI_F_COUNT; ++f) {
+            const int32_t id = f;
+            const int64_t n = is_int_field(f) ? (int64_t)iv[f].size() : (int64_t)dv[f].size();
+            put(&id, 4); put(&n, 8);
+            if (is_int_field(f)) put(iv[f].data(), (size_t)n * 4);
+            else put(dv[f].data(), (size_t)n * 8);
+        }
+    }
+    ok = (std::fclose(fp) == 0) && ok;
+    if (!ok) return fail(SULI_BAD_ARG, std::string("writing ") + path + " failed");
+    return SULI_OK;
+}
+
+extern "C" int suli_restart_load(suli_handle *h, const char *path)
+{
+    HCHK();
+    ImplBase *im = h->impl;
+    if (!path) return fail(SULI_BAD_ARG, "null path");
+    std::FILE *fp = std::fopen(path, "rb");
+    if (!fp) return fail(SULI_BAD_ARG, std::string("cannot open ") + path);
+    bool ok = true;
+    auto get = [&](void *p, size_t n) { ok = ok && std::fread(p, 1, n, fp) == n; };
+    auto bad = [&](const std::string &why) { std::fclose(fp); return fail(SULI_BAD_CONFIG, path + std::string(": ") + why); };
+    char magic[8];
+    int32_t version = 0, nc = 0, nf = 0, tt = 1;
+    int64_t it = 0;
+    uint64_t draws = 0;
+    double t = 0.0, dt = 0.0;
+    get(magic, 8); get(&version, 4); get(&nc, 4); get(&nf, 4);
+    if (!ok || std::memcmp(magic, kRestartMagic, 8) != 0 || version != 1) return bad("not a restart file of this library");
+    if (nc != im->ncases || nf != SULI_F_COUNT) return bad("written for another batch");
+    get(&t, 8); get(&it, 8); get(&dt, 8); get(&draws, 8); get(&tt, 4);
+    std::vector<double> vini(nc), vins(nc);
+    for (int c = 0; c < nc; ++c) {
+        int32_t d[3];
+        get(d, 12); get(&vini[c], 8); get(&vins[c], 8);
+        if (ok && (d[0] != im->P[c].nx || d[1] != im->P[c].ny || d[2] != im->P[c].nz))
+            return bad("case " + std::to_string(c) + " has other dimensions");
+    }
+    for (int c = 0; c < nc && ok; ++c) {
+        std::vector<std::vector<double>> dv;
+        std::vector<std::vector<int32_t>> iv;
+        int rc = restart_fields(im, c, dv, iv, true);
+        if (rc) { std::fclose(fp); return rc; }
+        std::vector<int32_t> cases, fields;
+        std::vector<void *> hosts;
+        for (int f = 0; f < SULI_F_COUNT && ok; ++f) {
+            int32_t id = -1;
+            int64_t n = -1;
+            get(&id, 4); get(&n, 8);
+            const int64_t want = is_int_field(f) ? (int64_t)iv[f].size() : (int64_t)dv[f].size();
+            if (!ok || id != f || n != want) return bad("field " + std::to_string(f) + " of case " + std::to_string(c));
+            if (is_int_field(f)) { get(iv[f].data(), (size_t)n * 4); hosts.push_back(iv[f].data()); }
+            else { get(dv[f].data(), (size_t)n * 8); hosts.push_back(dv[f].data()); }
+            cases.push_back(c);
+            fields.push_back(f);
+        }
+        if (!ok) break;
+        rc = im->copy_fields((int)fields.size(), cases.data(), fields.data(), hosts.data(), true);
+        if (rc) { std::fclose(fp); return rc; }
+    }
+    std::fclose(fp);
+    if (!ok) return fail(SULI_BAD_CONFIG, std::string(path) + ": truncated restart file");
+    im->t = t;
+    im->it = (int)it;
+    im->dt = dt;
+    im->inflow_calls = draws;
+    im->tt = tt;
+    for (int c = 0; c < nc; ++c) {
+        int rc = im->write_case_scalar(c, S_VOLINI, vini[c]);
+        if (!rc) rc = im->write_case_scalar(c, S_VOLINS, vins[c]);
+        if (rc) return rc;
+    }
+    return SULI_OK;
 }
 
 extern "C" int suli_last_error(char *buf, size_t len)

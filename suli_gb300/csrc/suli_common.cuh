@@ -134,6 +134,7 @@ struct CaseDev {
     T *Fu, *Fv, *Fw, *u0, *v0, *w0, *fu0, *fv0, *fw0, *fu1, *fv1, *fw1;
     T *div, *tf_u, *tf_v, *tf_w;
     T *obs_lsx, *obs_lsy, *obs_lsz, *obs_lss;
+    T *obs_ls;                  // obstacle level set at the cell corners (field output only)
     int *id_ibmx, *id_ibmy, *id_ibmz, *id_ibm;
     T *bxx0, *bxx1, *blx1;      // inflow planes, indexed at(0, j, k)
     // CG work arrays

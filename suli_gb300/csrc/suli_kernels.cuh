@@ -90,6 +90,8 @@ template <typename T> void launch_mg_coarsen(const Batch<T> &b, cudaStream_t s);
 template <typename T> void launch_mg_vcycle(const Batch<T> &b, const int *tab, int grid, cudaStream_t s);
 template <typename T> void launch_cg_finish(const Batch<T> &b, cudaStream_t s);
 // mixed form: FP64 residual recomputation and correction around the FP32 inner CG
+// field output (k_output.cu)
+template <typename T> void launch_prtscr(const Batch<T> &b, int icase, float *out, int t_plot, cudaStream_t s);
 template <typename T> void launch_cg_refine_operator(const Batch<T> &b, cudaStream_t s);
 template <typename T> void launch_cg_refine_setup(const Batch<T> &b, cudaStream_t s);
 template <typename T> void launch_cg_refine_next(const Batch<T> &b, cudaStream_t s);

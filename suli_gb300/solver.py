@@ -29,7 +29,7 @@ EXPORTS = [
     "suli_mms_error", "suli_set_stage", "suli_step", "suli_diagnostics", "suli_synchronize",
     "suli_last_error", "suli_device_info", "suli_get_stream", "suli_profile", "suli_profile_read",
     "suli_ibm_setup", "suli_conmassa_noalloc", "suli_time_kernel", "suli_upload_fields",
-    "suli_download_fields",
+    "suli_download_fields", "suli_write_fields", "suli_restart_save", "suli_restart_load",
 ]
 
 
@@ -86,6 +86,9 @@ def load_library(path: str = LIB_PATH):
     L.suli_upload_fields.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
     L.suli_download_fields.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
     L.suli_time_kernel.argtypes = [C.c_void_p, C.c_int, C.c_int, P(C.c_double), P(C.c_double)]
+    L.suli_write_fields.argtypes = [C.c_void_p, C.c_int, C.c_char_p, C.c_int]
+    L.suli_restart_save.argtypes = [C.c_void_p, C.c_char_p]
+    L.suli_restart_load.argtypes = [C.c_void_p, C.c_char_p]
     L.suli_conmassa_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, i32, i32, i32, C.c_double,
                                         C.c_double, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]
     _lib = L
@@ -275,6 +278,21 @@ class SuliGPU:
         ms, by = C.c_double(), C.c_double()
         _check(load_library().suli_time_kernel(self._h, kernel, reps, C.byref(ms), C.byref(by)))
         return ms.value, by.value
+
+    # ---- output and restart --------------------------------------------------
+    def write_fields(self, path, case: int = 0, t_plot: int = 0):
+        """PRTSCR's field record of one case (4_plot.f90:501-635) as a
+        Fortran unformatted file at `path`."""
+        _check(load_library().suli_write_fields(self._h, case, str(path).encode(), int(t_plot)))
+
+    def restart_save(self, path):
+        """Every field, t, it and the counters of the batch (restart_salva)."""
+        _check(load_library().suli_restart_save(self._h, str(path).encode()))
+
+    def restart_load(self, path):
+        """Restore a restart_save file into this handle (restart_ini, with t
+        and it kept)."""
+        _check(load_library().suli_restart_load(self._h, str(path).encode()))
 
     def diag(self, case: int = 0) -> SuliDiag:
         d = SuliDiag()
