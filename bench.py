@@ -15,9 +15,10 @@ beside it ("fp64"), the e2e figure goes through the C ABI with host
 buffers (state uploaded from pinned host memory and read back every step),
 the roofline entry is the dominant kernel timed alone over every case
 (CUDA events on the library's stream), "accuracy" is the mixed form against
-the FP64 form on the 64x32x32 dam break after 200 steps, and cpu_baseline
-is the oracle (a port of the reference, OpenMP where the reference has it)
-on a bounded sample.
+the FP64 form on the 64x32x32 dam break after 200 steps, "output" times
+the field records (PRTSCR) of 16 cases and a restart save + load outside
+the timed region, and cpu_baseline is the oracle (a port of the reference,
+OpenMP where the reference has it) on a bounded sample.
 
 --impl reference times the reference's CPU implementation (the oracle port:
 no Fortran compiler exists on either machine) on the same workload.
@@ -61,6 +62,8 @@ def parse():
                          "cudaProfilerStart/Stop, for ncu --profile-from-start off; prints its time")
     ap.add_argument("--mms-steps", type=int, default=100,
                     help="steps of the manufactured-solution runs at 32^3, 64^3, 128^3 (0: skip)")
+    ap.add_argument("--no-output", action="store_true",
+                    help="skip the field-output and restart measurement")
     ap.add_argument("--accuracy-steps", type=int, default=200,
                     help="steps of the dam-break mixed-vs-FP64 accuracy run (0: skip)")
     return ap.parse_args()
@@ -261,6 +264,50 @@ def accuracy_run(args):
         g.close()
     out.update({"rel_l2_" + k: v for k, v in errs.items()})
     return out
+
+
+def output_run(gm, ncases):
+    """The output path outside any timed region: PRTSCR records (t_plot = 1)
+    of the first `ncases` cases of the mixed handle (device kernel, one copy
+    to pinned memory, file write), and a restart save + load of a 4-case
+    mixed batch, into a temporary directory.  Wall time, bytes, GB/s."""
+    import shutil
+    import tempfile
+    from suli_gb300 import cases
+    from suli_gb300._abi import PREC_MIXED
+    from suli_gb300 import solver
+    d = tempfile.mkdtemp(prefix="suli_out_")
+    try:
+        out = {}
+        gm.synchronize()
+        t0 = time.perf_counter()
+        nbytes = 0
+        for c in range(ncases):
+            path = os.path.join(d, "campos_%05d" % (10 + c))
+            gm.write_fields(path, c, 1)
+            nbytes += os.path.getsize(path)
+        dt_w = time.perf_counter() - t0
+        out["fields"] = {"cases": ncases, "t_plot": 1, "bytes": nbytes, "s": dt_w, "GB_s": nbytes / dt_w / 1e9}
+        dims, hcol, amp = cases.ensemble_dims(4, seed=0)
+        cs = [cases.ensemble_case(i, dims, hcol, amp, precision=PREC_MIXED) for i in range(4)]
+        g = solver.SuliGPU([c.params for c in cs])
+        g.start([c.fields for c in cs])
+        g.step(1)
+        path = os.path.join(d, "restart.bin")
+        t0 = time.perf_counter()
+        g.restart_save(path)
+        dt_s = time.perf_counter() - t0
+        size = os.path.getsize(path)
+        t0 = time.perf_counter()
+        g.restart_load(path)
+        dt_l = time.perf_counter() - t0
+        g.close()
+        out["restart"] = {"cases": 4, "bytes": size, "save_s": dt_s, "load_s": dt_l,
+                          "save_GB_s": size / dt_s / 1e9, "load_GB_s": size / dt_l / 1e9}
+        out["dir"] = "temporary directory (tmpfs or local disk of the host)"
+        return out
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
 
 
 def mms_run(args):
@@ -464,6 +511,11 @@ def main():
             g64.close()
         except Exception as e:  # reported, not hidden
             line["fp64"] = {"error": repr(e)}
+    if rank == 0 and not args.no_output:
+        try:
+            line["output"] = output_run(gm, min(16, len(cs_m)))
+        except Exception as e:
+            line["output"] = {"error": repr(e)}
     gm.close()
     if args.accuracy_steps > 0 and rank == 0:
         try:
