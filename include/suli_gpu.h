@@ -92,6 +92,9 @@ typedef struct suli_params {
     int32_t mixed_precond;         /* mixed form: FP32 passes as 0 Jacobi-scaled CG (graddin's own
                                       iteration), 1 CG preconditioned by a multigrid V-cycle */
     uint64_t seed;                 /* counter-based RNG seed for the inflow perturbation */
+    int32_t t_tens;                /* 0 none, 1 surface tension (2_iniciais.f90:56; 14_level_set.f90:519-567,
+                                      :660-704; 11_diversos.f90:383-395) */
+    double  sigma;                 /* surface tension coefficient, N/m (reference: 0.0728) */
 } suli_params;
 
 /* ---- field ids (reference module arrays) -------------------------------- */
@@ -131,6 +134,10 @@ enum suli_field {
     SULI_F_BLX1,     /* blx1 (ny, nz) inflow ls at i = 1 */
     SULI_F_OBS_LS,   /* obs_ls (nx1, ny1, nz1) obstacle level set at the cell corners, written by
                         obstaculo() for the field output (3_contorno.f90:905-911, 4_plot.f90:570) */
+    SULI_F_HSX,      /* hsx (nx, ny, nz) surface-tension weight, heaviside (14_level_set.f90:563-567) */
+    SULI_F_HSY,
+    SULI_F_HSZ,
+    SULI_F_KURV,     /* kurv (nx, ny, nz) interface curvature, curv_ls1 (14_level_set.f90:660-704) */
     SULI_F_COUNT
 };
 

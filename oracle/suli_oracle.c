@@ -97,6 +97,7 @@ struct or_case {
     F3 tf_u, tf_v, tf_w;
     F3 obs_lsx, obs_lsy, obs_lsz, obs_lss;
     F3 obs_ls;                 /* obs_ls (nx1, ny1, nz1), cell corners: field output only */
+    F3 hsx, hsy, hsz, kurv;    /* surface tension (t_tens = 1), cells */
     I3 id_ibmx, id_ibmy, id_ibmz, id_ibm;
     F3 bxx0, bxx1, blx1;
 
@@ -150,6 +151,10 @@ or_case *or_create(const suli_params *pp)
     for (int q = 0; q < 6; ++q) f3_init(fz[q], 1, nx, 1, ny, 1, nz1);
     f3_init(&c->obs_lss, 1, nx, 1, ny, 1, nz);
     f3_init(&c->obs_ls, 1, nx1, 1, ny1, 1, nz1);
+    f3_init(&c->hsx, 1, nx, 1, ny, 1, nz);
+    f3_init(&c->hsy, 1, nx, 1, ny, 1, nz);
+    f3_init(&c->hsz, 1, nx, 1, ny, 1, nz);
+    f3_init(&c->kurv, 1, nx, 1, ny, 1, nz);
     i3_init(&c->id_ibmx, 1, nx1, 1, ny, 1, nz);
     i3_init(&c->id_ibmy, 1, nx, 1, ny1, 1, nz);
     i3_init(&c->id_ibmz, 1, nx, 1, ny, 1, nz1);
@@ -190,7 +195,7 @@ void or_destroy(or_case *c)
                  &c->mu, &c->mut, &c->xmu, &c->ymu, &c->zmu, &c->Fu, &c->Fv, &c->Fw, &c->u0,
                  &c->v0, &c->w0, &c->fu0, &c->fv0, &c->fw0, &c->fu1, &c->fv1, &c->fw1, &c->div,
                  &c->tf_u, &c->tf_v, &c->tf_w, &c->obs_lsx, &c->obs_lsy, &c->obs_lsz,
-                 &c->obs_lss, &c->bxx0, &c->bxx1, &c->blx1, &c->obs_ls};
+                 &c->obs_lss, &c->bxx0, &c->bxx1, &c->blx1, &c->obs_ls, &c->hsx, &c->hsy, &c->hsz, &c->kurv};
     for (unsigned q = 0; q < sizeof(all) / sizeof(all[0]); ++q) free(all[q]->p);
     free(c->id_ibmx.p); free(c->id_ibmy.p); free(c->id_ibmz.p); free(c->id_ibm.p);
     free(c);
@@ -236,6 +241,10 @@ void *or_field(or_case *c, int f, int lo[3], int hi[3])
     case SULI_F_OBS_LSZ: a = &c->obs_lsz; break;
     case SULI_F_OBS_LSS: a = &c->obs_lss; break;
     case SULI_F_OBS_LS: a = &c->obs_ls; break;
+    case SULI_F_HSX: a = &c->hsx; break;
+    case SULI_F_HSY: a = &c->hsy; break;
+    case SULI_F_HSZ: a = &c->hsz; break;
+    case SULI_F_KURV: a = &c->kurv; break;
     case SULI_F_ID_IBMX: ia = &c->id_ibmx; break;
     case SULI_F_ID_IBMY: ia = &c->id_ibmy; break;
     case SULI_F_ID_IBMZ: ia = &c->id_ibmz; break;
@@ -411,7 +420,9 @@ static inline double weno5(double v0, double v1, double v2, double v3, double v4
 
 /* One grid line a(1..n) (stride in elements).  ihs = 0: periodic with the
  * reference's node-style wrap phi(0)=phi(n-1) (:702-714); ihs = 2: cubic
- * extrapolation (:742-756).  dp = dphi+ ("dphidxp"), dn = dphi- ("dphidxn"). */
+ * extrapolation (:742-756); ihs = 1 (curv_ls1 only): the low end with the
+ * weights (12, -9, 2) / 5, the high end as ihs = 2 (:716-725).  dp = dphi+
+ * ("dphidxp"), dn = dphi- ("dphidxn"). */
 void or_weno_line(const double *a, long s, int n, double h, int ihs, double *dp, double *dn)
 {
     double stackbuf[1024];
@@ -427,10 +438,16 @@ void or_weno_line(const double *a, long s, int n, double h, int ihs, double *dp,
         phi[n + 2] = phi[3];
         phi[n + 3] = phi[4];
     } else {
-        const double c11 = 1. / 11.;
-        phi[0] = c11 * (18. * phi[1] - 9. * phi[2] + 2. * phi[3]);
-        phi[-1] = c11 * (18. * phi[0] - 9. * phi[1] + 2. * phi[2]);
-        phi[-2] = c11 * (18. * phi[-1] - 9. * phi[0] + 2. * phi[1]);
+        const double c11 = 1. / 11., c5 = 1. / 5.;
+        if (ihs == 1) {
+            phi[0] = c5 * (12. * phi[1] - 9. * phi[2] + 2. * phi[3]);
+            phi[-1] = c5 * (12. * phi[0] - 9. * phi[1] + 2. * phi[2]);
+            phi[-2] = c5 * (12. * phi[-1] - 9. * phi[0] + 2. * phi[1]);
+        } else {
+            phi[0] = c11 * (18. * phi[1] - 9. * phi[2] + 2. * phi[3]);
+            phi[-1] = c11 * (18. * phi[0] - 9. * phi[1] + 2. * phi[2]);
+            phi[-2] = c11 * (18. * phi[-1] - 9. * phi[0] + 2. * phi[1]);
+        }
         phi[n + 1] = c11 * (18. * phi[n] - 9. * phi[n - 1] + 2. * phi[n - 2]);
         phi[n + 2] = c11 * (18. * phi[n + 1] - 9. * phi[n] + 2. * phi[n - 1]);
         phi[n + 3] = c11 * (18. * phi[n + 2] - 9. * phi[n + 1] + 2. * phi[n]);
@@ -584,17 +601,42 @@ static int reinic_weno(or_case *c, F3 *ls1, int dimx, int dimy, int dimz, int ma
 static void heaviside(or_case *c)
 {
     const double a = c->p.alpha1, dx1 = c->dx1, pi = c->pi;
+    const int nx = c->nx, ny = c->ny, nz = c->nz, st = c->p.t_tens == 1;
+    /* t_tens = 1: the surface-tension weights hsx, hsy, hsz from the larger
+     * one-sided WENO derivative of ls (:519-546, :563-567) */
+    F3 ta = {0}, tb = {0}, tc = {0}, td = {0}, te = {0}, tf = {0};
+    if (st) {
+        ta = tmp3(1, nx, 1, ny, 1, nz); tb = tmp3(1, nx, 1, ny, 1, nz); tc = tmp3(1, nx, 1, ny, 1, nz);
+        td = tmp3(1, nx, 1, ny, 1, nz); te = tmp3(1, nx, 1, ny, 1, nz); tf = tmp3(1, nx, 1, ny, 1, nz);
+        der_weno(c, &c->ls, nx, ny, nz, &ta, &tb, &tc, &td, &te, &tf);
+    }
     for (int k = 1; k <= c->nz; ++k)
         for (int j = 1; j <= c->ny; ++j)
             for (int i = 1; i <= c->nx; ++i) {
                 double l = A(c->ls, i, j, k), h;
+                double gxv = 0., gyv = 0., gzv = 0.;
+                if (st) {
+                    gxv = A(ta, i, j, k); gyv = A(tb, i, j, k); gzv = A(tc, i, j, k);
+                    if (!(fabs(gxv) > fabs(A(td, i, j, k)))) gxv = A(td, i, j, k);
+                    if (!(fabs(gyv) > fabs(A(te, i, j, k)))) gyv = A(te, i, j, k);
+                    if (!(fabs(gzv) > fabs(A(tf, i, j, k)))) gzv = A(tf, i, j, k);
+                    A(c->hsx, i, j, k) = 0.; A(c->hsy, i, j, k) = 0.; A(c->hsz, i, j, k) = 0.;
+                }
                 if (l < -a * dx1) h = 0.;
                 else if (l > a * dx1) h = 1.;
-                else h = 0.5 * (1. + l / (a * dx1) + 1. / pi * sin(pi * l / (a * dx1)));
+                else {
+                    h = 0.5 * (1. + l / (a * dx1) + 1. / pi * sin(pi * l / (a * dx1)));
+                    if (st) {
+                        A(c->hsx, i, j, k) = 0.5 * gxv * (1. + cos(pi * l / (a * dx1))) / (a * dx1);
+                        A(c->hsy, i, j, k) = 0.5 * gyv * (1. + cos(pi * l / (a * dx1))) / (a * dx1);
+                        A(c->hsz, i, j, k) = 0.5 * gzv * (1. + cos(pi * l / (a * dx1))) / (a * dx1);
+                    }
+                }
                 A(c->hs, i, j, k) = h;
                 A(c->rho, i, j, k) = c->p.rho_f1 * (1. - h) + c->p.rho_f2 * h;
                 A(c->ls_mu, i, j, k) = c->p.mu_f1 * (1. - h) + c->p.mu_f2 * h;
             }
+    if (st) { fr(&ta); fr(&tb); fr(&tc); fr(&td); fr(&te); fr(&tf); }
 }
 
 static double volume(const or_case *c)
@@ -630,6 +672,34 @@ static void mod_ls1(or_case *c, const F3 *ls1, F3 *mod, F3 *nxo, F3 *nyo, F3 *nz
                         A(*nxo, i, j, k) = a / m; A(*nyo, i, j, k) = b / m; A(*nzo, i, j, k) = cc / m;
                     }
                 }
+            }
+    fr(&ta); fr(&tb); fr(&tc); fr(&td); fr(&te); fr(&tf);
+}
+
+/* curv_ls1, :660-704: the curvature from the unit normals, each
+ * differentiated along its own axis with ihs = 1, the larger one-sided
+ * derivative of each (ties to the + side) */
+static void curv_ls1(or_case *c, const F3 *nxv, const F3 *nyv, const F3 *nzv)
+{
+    const int nx = c->nx, ny = c->ny, nz = c->nz;
+    F3 ta = tmp3(1, nx, 1, ny, 1, nz), tb = tmp3(1, nx, 1, ny, 1, nz), tc = tmp3(1, nx, 1, ny, 1, nz),
+       td = tmp3(1, nx, 1, ny, 1, nz), te = tmp3(1, nx, 1, ny, 1, nz), tf = tmp3(1, nx, 1, ny, 1, nz);
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j)
+            or_weno_line(&A(*nxv, 1, j, k), 1, nx, c->dx, 1, &A(ta, 1, j, k), &A(td, 1, j, k));
+    for (int k = 1; k <= nz; ++k)
+        for (int i = 1; i <= nx; ++i)
+            or_weno_line(&A(*nyv, i, 1, k), nyv->s1, ny, c->dy, 1, &A(tb, i, 1, k), &A(te, i, 1, k));
+    for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i)
+            or_weno_line(&A(*nzv, i, j, 1), nzv->s2, nz, c->dz, 1, &A(tc, i, j, 1), &A(tf, i, j, 1));
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i) {
+                const double ddx = (fabs(A(td, i, j, k)) > fabs(A(ta, i, j, k))) ? A(td, i, j, k) : A(ta, i, j, k);
+                const double ddy = (fabs(A(te, i, j, k)) > fabs(A(tb, i, j, k))) ? A(te, i, j, k) : A(tb, i, j, k);
+                const double ddz = (fabs(A(tf, i, j, k)) > fabs(A(tc, i, j, k))) ? A(tf, i, j, k) : A(tc, i, j, k);
+                A(c->kurv, i, j, k) = ddx + ddy + ddz;
             }
     fr(&ta); fr(&tb); fr(&tc); fr(&td); fr(&te); fr(&tf);
 }
@@ -673,7 +743,14 @@ void or_level_set(or_case *c)
         }
         fr(&mod);
     }
-    /* mod_ls1 at :269 only feeds curv_ls1 (t_tens = 1): not needed here */
+    /* mod_ls1 at :269 feeds curv_ls1 (t_tens = 1) */
+    if (c->p.t_tens == 1) {
+        F3 mod = tmp3(1, nx, 1, ny, 1, nz), nxv = tmp3(1, nx, 1, ny, 1, nz), nyv = tmp3(1, nx, 1, ny, 1, nz),
+           nzv = tmp3(1, nx, 1, ny, 1, nz);
+        mod_ls1(c, &c->ls, &mod, &nxv, &nyv, &nzv, nx, ny, nz);
+        curv_ls1(c, &nxv, &nyv, &nzv);
+        fr(&mod); fr(&nxv); fr(&nyv); fr(&nzv);
+    }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -934,8 +1011,35 @@ void or_convdiff(or_case *c)
 void or_complementos(or_case *c)
 {
     int nx = c->nx, ny = c->ny, nz = c->nz, nx1 = c->nx1, ny1 = c->ny1, nz1 = c->nz1;
-    /* gravity and MMS source; the surface-tension and k-gradient terms are
-     * exact zeros for t_tens = 0 and ka = 0 */
+    /* gravity, surface tension (t_tens = 1: sigma times the face value of
+     * hs_x kurv / rho, :383-390) and MMS source; the k-gradient term is an
+     * exact zero for ka = 0, and so is the surface-tension term for
+     * t_tens = 0 */
+    if (c->p.t_tens == 1) {
+        F3 aux = tmp3(1, nx, 1, ny, 1, nz), dx_ = tmp3(1, nx1, 1, ny, 1, nz), dy_ = tmp3(1, nx, 1, ny1, 1, nz),
+           dz_ = tmp3(1, nx, 1, ny, 1, nz1);
+        const double sg = c->p.sigma;
+        for (long q = 0; q < f3_size(&aux); ++q) aux.p[q] = c->hsx.p[q] * c->kurv.p[q] / c->rho.p[q];
+        interpx_cf(c, &aux, nx, ny, nz, &dx_);
+        for (long q = 0; q < f3_size(&aux); ++q) aux.p[q] = c->hsy.p[q] * c->kurv.p[q] / c->rho.p[q];
+        interpy_cf(&aux, nx, ny, nz, &dy_);
+        for (long q = 0; q < f3_size(&aux); ++q) aux.p[q] = c->hsz.p[q] * c->kurv.p[q] / c->rho.p[q];
+        interpz_cf(&aux, nx, ny, nz, &dz_);
+        for (int k = 1; k <= nz; ++k)
+            for (int j = 1; j <= ny; ++j)
+                for (int i = 1; i <= nx1; ++i)
+                    A(c->Fu, i, j, k) = A(c->Fu, i, j, k) + c->p.gx - sg * A(dx_, i, j, k) + A(c->tf_u, i, j, k);
+        for (int k = 1; k <= nz; ++k)
+            for (int j = 1; j <= ny1; ++j)
+                for (int i = 1; i <= nx; ++i)
+                    A(c->Fv, i, j, k) = A(c->Fv, i, j, k) - sg * A(dy_, i, j, k) + A(c->tf_v, i, j, k);
+        for (int k = 1; k <= nz1; ++k)
+            for (int j = 1; j <= ny; ++j)
+                for (int i = 1; i <= nx; ++i)
+                    A(c->Fw, i, j, k) = A(c->Fw, i, j, k) - c->p.gz - sg * A(dz_, i, j, k) + A(c->tf_w, i, j, k);
+        fr(&aux); fr(&dx_); fr(&dy_); fr(&dz_);
+        return;
+    }
     for (int k = 1; k <= nz; ++k)
         for (int j = 1; j <= ny; ++j)
             for (int i = 1; i <= nx1; ++i)

@@ -50,6 +50,8 @@ class SuliParams(C.Structure):
         ("vol_loop_max", C.c_int32),
         ("mixed_precond", C.c_int32),
         ("seed", C.c_uint64),
+        ("t_tens", C.c_int32),
+        ("sigma", C.c_double),
     ]
 
     def copy(self) -> "SuliParams":
@@ -96,6 +98,8 @@ def default_params(**kw) -> SuliParams:
     p.cg_tol = 1e-4
     p.precision = PREC_FP64
     p.vol_loop_max = 1000
+    p.t_tens = 0
+    p.sigma = 0.0728
     p.mixed_precond = 1
     for k, v in kw.items():
         if not hasattr(p, k):
@@ -111,7 +115,7 @@ FIELDS = [
     "FW0", "FU1", "FV1", "FW1", "DIV", "TF_U", "TF_V", "TF_W",
     "OBS_LSX", "OBS_LSY", "OBS_LSZ", "OBS_LSS",
     "ID_IBMX", "ID_IBMY", "ID_IBMZ", "ID_IBM",
-    "BXX0", "BXX1", "BLX1", "OBS_LS",
+    "BXX0", "BXX1", "BLX1", "OBS_LS", "HSX", "HSY", "HSZ", "KURV",
 ]
 FIELD_ID = {name: i for i, name in enumerate(FIELDS)}
 INT_FIELDS = {"ID_IBMX", "ID_IBMY", "ID_IBMZ", "ID_IBM"}
@@ -141,7 +145,7 @@ def field_bounds(p: SuliParams, name: str):
     }
     if name in table:
         return table[name]
-    if name in ("LS", "HS", "RHO", "LS_MU", "MU", "MUT", "DIV", "OBS_LSS", "ID_IBM"):
+    if name in ("LS", "HS", "RHO", "LS_MU", "MU", "MUT", "DIV", "OBS_LSS", "ID_IBM", "HSX", "HSY", "HSZ", "KURV"):
         return cell
     if name in ("XMU", "FU", "U0", "FU0", "FU1", "TF_U", "OBS_LSX", "ID_IBMX"):
         return xface

@@ -271,3 +271,20 @@ def ensemble_case(i, dims, hcol, amp, precision=PREC_FP64, dt=1e-4, cg_tol=1e-10
     layer = level_set_tipo(p, 1, ampl=float(amp[i]) * lz, lambdax=2.0 * lx, prof=0.25 * lz)
     ls = np.maximum(col, layer)
     return Case("ensemble_%d" % i, p, _base_fields(p, ls), steps=500)
+
+
+def capillary_column(n=48, ny=4, radius=0.25, precision=PREC_FP64, dt=2e-4) -> Case:
+    """A water column of circular section (axis along y) at rest in air, with
+    surface tension (t_tens = 1, 14_level_set.f90:519-567, :660-704): ls =
+    R - |(x, z) - centre| on a 1 x 1 x-z box, walls all round (y periodic),
+    gravity off.  Its curvature is -1/R; the Laplace pressure jump sigma/R
+    drives the flow."""
+    h = 1.0 / n
+    p = default_params(nx=n, ny=ny, nz=n, dx=h, dy=h, dz=h, dt=dt, ccy0=0, ccyf=0,
+                       gx=0.0, gz=0.0, precision=precision, cg_tol_mode=CG_TOL_REL, cg_tol=1e-10)
+    p.t_tens = 1
+    x = _centres(n, h)[:, None, None]
+    z = _centres(n, h)[None, None, :]
+    ls = np.empty((n, ny, n), order="F")
+    ls[...] = radius - np.sqrt((x - 0.5) ** 2 + (z - 0.5) ** 2)
+    return Case("capillary_%d" % n, p, _base_fields(p, ls), steps=20)

@@ -41,6 +41,7 @@ __device__ __forceinline__ T weno5(T v0, T v1, T v2, T v3, T v4)
 }
 
 // Load phi(m), m = i-3..i+3, of one grid line (element m at base + m*st),
+// (ihs = 1, the curvature's mode, extrapolates the low end differently),
 // building the out-of-range values as wenox/y/z do: ihs = 0 periodic with
 // phi(0) = phi(n-1) etc. (:702-714), otherwise cubic extrapolation (:742-756).
 template <typename T>
@@ -66,10 +67,13 @@ __device__ __forceinline__ void load_line(const T *__restrict__ a, long long bas
     if (ihs != 0) {
         const T c11 = T(1. / 11.);
         if (i - 3 < 1) {
+            // ihs = 1 (curv_ls1): the low end's weights are (12, -9, 2) / 5
+            // (8_derivadas.f90:716-721); ihs = 2: (18, -9, 2) / 11
+            const T cl = (ihs == 1) ? T(1. / 5.) : c11, w0 = (ihs == 1) ? T(12.) : T(18.);
             T p1 = a[base + st], p2 = a[base + 2 * st], p3 = a[base + 3 * st];
-            T g0 = c11 * (T(18.) * p1 - T(9.) * p2 + T(2.) * p3);
-            T gm1 = c11 * (T(18.) * g0 - T(9.) * p1 + T(2.) * p2);
-            T gm2 = c11 * (T(18.) * gm1 - T(9.) * g0 + T(2.) * p1);
+            T g0 = cl * (w0 * p1 - T(9.) * p2 + T(2.) * p3);
+            T gm1 = cl * (w0 * g0 - T(9.) * p1 + T(2.) * p2);
+            T gm2 = cl * (w0 * gm1 - T(9.) * g0 + T(2.) * p1);
 #pragma unroll
             for (int t = 0; t < 7; ++t) {
                 int m = i - 3 + t;
@@ -343,6 +347,25 @@ __global__ void __launch_bounds__(NTHREADS) k_heaviside_vol(const CaseDev<T> *__
             hv = h64;
         }
         c.ls_mu[q] = T(c.mu_f1) * (T(1.) - h) + T(c.mu_f2) * h;
+        if (c.t_tens == 1) {
+            // surface-tension weights (14_level_set.f90:519-546, :563-567):
+            // the larger one-sided WENO derivative of ls times the smoothed
+            // delta, zero outside the band
+            T ta, td, tb, te, tc, tf;
+            der_weno_at<T>(c, c.ls, i, j, k, ta, td, tb, te, tc, tf);
+            const T ga = (fabs(ta) > fabs(td)) ? ta : td;
+            const T gb = (fabs(tb) > fabs(te)) ? tb : te;
+            const T gc = (fabs(tc) > fabs(tf)) ? tc : tf;
+            T sx = T(0.), sy = T(0.), sz = T(0.);
+            if (!(l < -ad) && !(l > ad)) {
+                sx = T(0.5) * ga * (T(1.) + cos(T(c.pi) * l / ad)) / ad;
+                sy = T(0.5) * gb * (T(1.) + cos(T(c.pi) * l / ad)) / ad;
+                sz = T(0.5) * gc * (T(1.) + cos(T(c.pi) * l / ad)) / ad;
+            }
+            c.hsx[q] = sx;
+            c.hsy[q] = sy;
+            c.hsz[q] = sz;
+        }
         vol = (1. - (1. - hv)) * c.dx * c.dy * c.dz;
     }
     if (set_ini < 0) return;     // properties only (heaviside after the level-set IBM)
@@ -398,7 +421,65 @@ __global__ void __launch_bounds__(NTHREADS) k_volcorr_copy(const CaseDev<T> *__r
     if (c.ls64 != nullptr) c.ls64[q] = c.lsb64[q];
 }
 
+// ---- surface tension (t_tens = 1) -------------------------------------------
+// mod_ls1 (14_level_set.f90:598-655) on ls: the unit normal from the larger
+// one-sided WENO derivatives (zero where the gradient vanishes)
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_ls_normals(const CaseDev<T> *__restrict__ cs, int ncases)
+{
+    const CaseDev<T> &c = cs[find_case(cs, ncases)];
+    if (c.t_tens != 1) return;
+    int i, j, k;
+    tile_ijk(c, i, j, k);
+    const Geo &g = c.g;
+    if (i > g.nx || j > g.ny || k > g.nz) return;
+    T ta, td, tb, te, tc, tf;
+    der_weno_at<T>(c, c.ls, i, j, k, ta, td, tb, te, tc, tf);
+    const T a = (fabs(ta) > fabs(td)) ? ta : td;
+    const T b = (fabs(tb) > fabs(te)) ? tb : te;
+    const T cc = (fabs(tc) > fabs(tf)) ? tc : tf;
+    const T m = sqrt(a * a + b * b + cc * cc);
+    const long long q = g.at(i, j, k);
+    if (m == T(0)) {
+        c.nlx[q] = T(0.); c.nly[q] = T(0.); c.nlz[q] = T(0.);
+    } else {
+        c.nlx[q] = a / m; c.nly[q] = b / m; c.nlz[q] = cc / m;
+    }
+}
+
+// curv_ls1 (14_level_set.f90:660-704): each normal component differentiated
+// along its own axis by WENO with the low end extrapolated as ihs = 1, the
+// larger one-sided derivative of each (ties to the + side), summed
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_ls_curv(const CaseDev<T> *__restrict__ cs, int ncases)
+{
+    const CaseDev<T> &c = cs[find_case(cs, ncases)];
+    if (c.t_tens != 1) return;
+    int i, j, k;
+    tile_ijk(c, i, j, k);
+    const Geo &g = c.g;
+    if (i > g.nx || j > g.ny || k > g.nz) return;
+    T L[7], p, n;
+    load_line<T>(c.nlx, g.at(0, j, k), 1, i, g.nx, 1, L);
+    weno_pm<T>(L, T(c.idx), p, n);
+    const T ddx = (fabs(n) > fabs(p)) ? n : p;
+    load_line<T>(c.nly, g.at(i, 0, k), g.sx, j, g.ny, 1, L);
+    weno_pm<T>(L, T(c.idy), p, n);
+    const T ddy = (fabs(n) > fabs(p)) ? n : p;
+    load_line<T>(c.nlz, g.at(i, j, 0), g.sxy, k, g.nz, 1, L);
+    weno_pm<T>(L, T(c.idz), p, n);
+    const T ddz = (fabs(n) > fabs(p)) ? n : p;
+    c.kurv[g.at(i, j, k)] = ddx + ddy + ddz;
+}
+
 // ---- host launchers -------------------------------------------------------
+template <typename T>
+void launch_curvature(const Batch<T> &b, cudaStream_t s)
+{
+    k_ls_normals<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
+    k_ls_curv<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
+}
+
 template <typename T>
 void launch_level_set_adv(const Batch<T> &b, cudaStream_t s)
 {
@@ -439,5 +520,7 @@ template void launch_level_set_adv<float>(const Batch<float> &, cudaStream_t);
 template void launch_reinit<float>(const Batch<float> &, int, cudaStream_t, int);
 template void launch_heaviside<float>(const Batch<float> &, int, cudaStream_t);
 template void launch_volcorr<float>(const Batch<float> &, cudaStream_t);
+template void launch_curvature<double>(const Batch<double> &, cudaStream_t);
+template void launch_curvature<float>(const Batch<float> &, cudaStream_t);
 
 }  // namespace suli

@@ -33,6 +33,21 @@ __device__ __forceinline__ T interp_cf(int f, int n, bool periodic, F get)
 
 __device__ __forceinline__ int clampi(int a, int lo, int hi) { return a < lo ? lo : (a > hi ? hi : a); }
 
+// surface tension (t_tens = 1): sigma times the face value of hs_a kurv / rho
+// on the axis-0/1/2 face (i, j, k) (11_diversos.f90:383-390; interpx_cf wraps
+// on a periodic x, interpy_cf / interpz_cf never wrap)
+template <typename T>
+__device__ __forceinline__ T tension_face(const CaseDev<T> &c, int axis, int i, int j, int k)
+{
+    const Geo &g = c.g;
+    auto v = [&](const T *hs, long long q) { return hs[q] * c.kurv[q] / c.rho[q]; };
+    T f;
+    if (axis == 0) f = interp_cf<T>(i, g.nx, c.ccx0 == 0, [&](int m) { return v(c.hsx, g.at(m, j, k)); });
+    else if (axis == 1) f = interp_cf<T>(j, g.ny, false, [&](int m) { return v(c.hsy, g.at(i, m, k)); });
+    else f = interp_cf<T>(k, g.nz, false, [&](int m) { return v(c.hsz, g.at(i, j, m)); });
+    return T(c.sigma) * f;
+}
+
 template <typename T>
 __device__ __forceinline__ T upw(T vel, T dneg, T dpos)
 {
@@ -159,7 +174,11 @@ __global__ void __launch_bounds__(NTHREADS) k_convdiff(const CaseDev<T> *__restr
                d1 * ((U(i, j, k + 1) - uc) * dz + (AT(w, i, j, k + 1) - AT(w, i - 1, j, k + 1)) * dx) -
                d0 * ((uc - U(i, j, k - 1)) * dz + (AT(w, i, j, k) - AT(w, i - 1, j, k)) * dx)) *
                   rrho;
-        if (fuse) F = F + T(c.gx) + AT(c.tf_u, i, j, k);
+        if (fuse) {
+            F = F + T(c.gx);
+            if (c.t_tens == 1) F = F - tension_face(c, 0, i, j, k);
+            F = F + AT(c.tf_u, i, j, k);
+        }
         AT(c.Fu, i, j, k) = F;
     }
     // ---- Fv at y-face (i,j,k), j in 1..ny+1 ----
@@ -189,7 +208,10 @@ __global__ void __launch_bounds__(NTHREADS) k_convdiff(const CaseDev<T> *__restr
                d1 * ((V(i, j, k + 1) - vc) * dz + (AT(w, i, j, k + 1) - AT(w, i, j - 1, k + 1)) * dy) -
                d0 * ((vc - V(i, j, k - 1)) * dz + (AT(w, i, j, k) - AT(w, i, j - 1, k)) * dy)) /
                   rhoy;
-        if (fuse) F = F + AT(c.tf_v, i, j, k);
+        if (fuse) {
+            if (c.t_tens == 1) F = F - tension_face(c, 1, i, j, k);
+            F = F + AT(c.tf_v, i, j, k);
+        }
         AT(c.Fv, i, j, k) = F;
     }
     // ---- Fw at z-face (i,j,k), k in 1..nz+1 ----
@@ -219,7 +241,11 @@ __global__ void __launch_bounds__(NTHREADS) k_convdiff(const CaseDev<T> *__restr
                b0 * ((wc - W(i, j - 1, k)) * dy + (AT(v, i, j, k) - AT(v, i, j, k - 1)) * dz) +
                (dmd_k * T(2.) * (W(i, j, k + 1) - wc) - dmd_m * T(2.) * (wc - W(i, j, k - 1))) * dz) /
                   rhoz;
-        if (fuse) F = F - T(c.gz) + AT(c.tf_w, i, j, k);
+        if (fuse) {
+            F = F - T(c.gz);
+            if (c.t_tens == 1) F = F - tension_face(c, 2, i, j, k);
+            F = F + AT(c.tf_w, i, j, k);
+        }
         AT(c.Fw, i, j, k) = F;
     }
 }
@@ -232,6 +258,15 @@ __global__ void __launch_bounds__(NTHREADS) k_complementos(const CaseDev<T> *__r
     tile_ijk(c, i, j, k);
     const Geo &g = c.g;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
+    if (c.t_tens == 1) {     // the surface-tension term sits between gravity and the MMS source
+        if (i <= nx + 1 && j <= ny && k <= nz)
+            AT(c.Fu, i, j, k) = AT(c.Fu, i, j, k) + T(c.gx) - tension_face(c, 0, i, j, k) + AT(c.tf_u, i, j, k);
+        if (i <= nx && j <= ny + 1 && k <= nz)
+            AT(c.Fv, i, j, k) = AT(c.Fv, i, j, k) - tension_face(c, 1, i, j, k) + AT(c.tf_v, i, j, k);
+        if (i <= nx && j <= ny && k <= nz + 1)
+            AT(c.Fw, i, j, k) = AT(c.Fw, i, j, k) - T(c.gz) - tension_face(c, 2, i, j, k) + AT(c.tf_w, i, j, k);
+        return;
+    }
     if (i <= nx + 1 && j <= ny && k <= nz) AT(c.Fu, i, j, k) = AT(c.Fu, i, j, k) + T(c.gx) + AT(c.tf_u, i, j, k);
     if (i <= nx && j <= ny + 1 && k <= nz) AT(c.Fv, i, j, k) = AT(c.Fv, i, j, k) + AT(c.tf_v, i, j, k);
     if (i <= nx && j <= ny && k <= nz + 1) AT(c.Fw, i, j, k) = AT(c.Fw, i, j, k) - T(c.gz) + AT(c.tf_w, i, j, k);

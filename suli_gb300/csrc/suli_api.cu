@@ -68,6 +68,8 @@ extern "C" void suli_default_params(suli_params *p)
     p->precision = SULI_PREC_FP64;
     p->vol_loop_max = 1000;
     p->mixed_precond = 1;
+    p->t_tens = 0;
+    p->sigma = 0.0728;
 }
 
 extern "C" int suli_field_shape(const suli_params *p, int f, int lo[3], int hi[3])
@@ -84,6 +86,7 @@ extern "C" int suli_field_shape(const suli_params *p, int f, int lo[3], int hi[3
     case SULI_F_PRD1: case SULI_F_PRD: set(0, nx + 1, 0, ny + 1, 0, nz + 1); break;
     case SULI_F_LS: case SULI_F_HS: case SULI_F_RHO: case SULI_F_LS_MU: case SULI_F_MU: case SULI_F_MUT:
     case SULI_F_DIV: case SULI_F_OBS_LSS: case SULI_F_ID_IBM:
+    case SULI_F_HSX: case SULI_F_HSY: case SULI_F_HSZ: case SULI_F_KURV:
         set(1, nx, 1, ny, 1, nz); break;
     case SULI_F_XMU: case SULI_F_FU: case SULI_F_U0: case SULI_F_FU0: case SULI_F_FU1: case SULI_F_TF_U:
     case SULI_F_OBS_LSX: case SULI_F_ID_IBMX:
@@ -130,6 +133,7 @@ static int validate(const suli_params &p)
     if ((p.ccy0 == 0) != (p.ccyf == 0)) return bad("periodic y must be set at both ends");
     if (p.reinit_max_iter < 1) return bad("reinit_max_iter must be >= 1");
     if (p.cg_max_iter < 1) return bad("cg_max_iter must be >= 1");
+    if (p.t_tens != 0 && p.t_tens != 1) return bad("t_tens must be 0 or 1");
     if ((long long)p.nx * p.ny * p.nz > (1LL << 31) - 1) return bad("grid larger than 2^31 cells");
     return SULI_OK;
 }
@@ -400,6 +404,7 @@ struct Impl : ImplBase {
             cd.uinicial = q.uinicial; cd.iturb = q.iturb; cd.seed = q.seed;
             cd.ccx0 = q.ccx0; cd.ccxf = q.ccxf; cd.ccy0 = q.ccy0; cd.ccyf = q.ccyf; cd.ccz0 = q.ccz0; cd.cczf = q.cczf;
             cd.t_tempo = q.t_tempo; cd.m_turb = q.m_turb; cd.mms_t = q.mms_t; cd.ibm_t = q.ibm_t; cd.obst_t = q.obst_t;
+            cd.t_tens = q.t_tens; cd.sigma = q.sigma;
             cd.reinit_max = q.reinit_max_iter; cd.cg_max = q.cg_max_iter; cd.cg_tol_mode = q.cg_tol_mode;
             cd.cg_tol = q.cg_tol;
             // one slab per case: every field of the case in the common box layout
@@ -411,7 +416,8 @@ struct Impl : ImplBase {
                         &cd.rho, &cd.ls_mu, &cd.mu, &cd.mut, &cd.xmu, &cd.ymu, &cd.zmu, &cd.Fu, &cd.Fv, &cd.Fw,
                         &cd.u0, &cd.v0, &cd.w0, &cd.fu0, &cd.fv0, &cd.fw0, &cd.fu1, &cd.fv1, &cd.fw1, &cd.div,
                         &cd.tf_u, &cd.tf_v, &cd.tf_w, &cd.obs_lsx, &cd.obs_lsy, &cd.obs_lsz, &cd.obs_lss,
-                        &cd.spi, &cd.spj, &cd.spk, &cd.dpr, &cd.e, &cd.r, &cd.p, &cd.mp, &cd.qpr, &cd.obs_ls};
+                        &cd.spi, &cd.spj, &cd.spk, &cd.dpr, &cd.e, &cd.r, &cd.p, &cd.mp, &cd.qpr, &cd.obs_ls,
+                        &cd.hsx, &cd.hsy, &cd.hsz, &cd.kurv, &cd.nlx, &cd.nly, &cd.nlz};
             const int ntf = sizeof(tf) / sizeof(tf[0]);
             int **itf[] = {&cd.id_ibmx, &cd.id_ibmy, &cd.id_ibmz, &cd.id_ibm};
             T **ptf[] = {&cd.bxx0, &cd.bxx1, &cd.blx1};
@@ -690,6 +696,10 @@ struct Impl : ImplBase {
         case SULI_F_OBS_LSZ: return c.obs_lsz;
         case SULI_F_OBS_LSS: return c.obs_lss;
         case SULI_F_OBS_LS: return c.obs_ls;
+        case SULI_F_HSX: return c.hsx;
+        case SULI_F_HSY: return c.hsy;
+        case SULI_F_HSZ: return c.hsz;
+        case SULI_F_KURV: return c.kurv;
         case SULI_F_ID_IBMX: return c.id_ibmx;
         case SULI_F_ID_IBMY: return c.id_ibmy;
         case SULI_F_ID_IBMZ: return c.id_ibmz;
@@ -839,7 +849,18 @@ struct Impl : ImplBase {
             if ((rc = read_scalars())) return rc;
         }
         reinit_iters = (int)sc(0, S_RINITER);
+        // curv_ls1 after the volume correction (14_level_set.f90:269-270)
+        if (any_tens()) {
+            launch_curvature<T>(b, st);
+            CKL();
+        }
         return SULI_OK;
+    }
+
+    bool any_tens() const
+    {
+        for (const auto &q : P) if (q.t_tens == 1) return true;
+        return false;
     }
 
     bool any_ibm() const

@@ -120,12 +120,13 @@ struct CaseDev {
     double dx, dy, dz, dx1, dt1, deltai;
     double idx, idy, idz;       // 1/dx, 1/dy, 1/dz (mixed-form kernels multiply)
     double alpha1, rho_f1, mu_f1, rho_f2, mu_f2, gx, gz;
+    double sigma;               // surface tension coefficient (t_tens = 1)
     double cles;         // (dx*dy*dz)^(2/3) * csmag * csmag
     double pi;
     double uinicial, iturb;
     unsigned long long seed;
     int ccx0, ccxf, ccy0, ccyf, ccz0, cczf;
-    int t_tempo, m_turb, mms_t, ibm_t, obst_t;
+    int t_tempo, m_turb, mms_t, ibm_t, obst_t, t_tens;
     int reinit_max, cg_max, cg_tol_mode;
     double cg_tol;
     // fields (reference module arrays)
@@ -135,6 +136,8 @@ struct CaseDev {
     T *div, *tf_u, *tf_v, *tf_w;
     T *obs_lsx, *obs_lsy, *obs_lsz, *obs_lss;
     T *obs_ls;                  // obstacle level set at the cell corners (field output only)
+    T *hsx, *hsy, *hsz, *kurv;  // surface tension (t_tens = 1): weights, curvature
+    T *nlx, *nly, *nlz;         // surface tension: the interface normal (curvature input)
     int *id_ibmx, *id_ibmy, *id_ibmz, *id_ibm;
     T *bxx0, *bxx1, *blx1;      // inflow planes, indexed at(0, j, k)
     // CG work arrays

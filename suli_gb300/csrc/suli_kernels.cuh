@@ -45,6 +45,7 @@ struct Batch {
 template <typename T> void launch_level_set_adv(const Batch<T> &b, cudaStream_t s);
 template <typename T> void launch_reinit(const Batch<T> &b, int max_iter, cudaStream_t s, int target = 0);
 template <typename T> void launch_heaviside(const Batch<T> &b, int set_ini, cudaStream_t s);
+template <typename T> void launch_curvature(const Batch<T> &b, cudaStream_t s);
 template <typename T> void launch_volcorr(const Batch<T> &b, cudaStream_t s);
 
 // momentum (k_momentum.cu)

@@ -27,6 +27,8 @@ def _configs():
         ("mms_periodic", cases.mms_case(16)),
         ("channel_ibm", cases.open_channel(48, 16, 16, dt=2e-3, radius=0.25, cg_tol=1e-10, periodic=True)),
         ("inflow_ibm", cases.open_channel(48, 16, 16, dt=2e-3, radius=0.25, cg_tol=1e-10)),
+        # surface tension (t_tens = 1): weights, curvature, the momentum term
+        ("capillary", cases.capillary_column(32, 4, 0.25)),
     ]
 
 
@@ -63,6 +65,9 @@ def test_level_set(pair):
     g.level_set()
     g.set_replay(None, -1)
     compare(o, g, ["LS", "HS", "RHO", "LS_MU"], TOL)
+    if case.params.t_tens:
+        compare(o, g, ["HSX", "HSZ", "KURV"], TOL)
+        assert np.abs(g.download("KURV")).max() > 0
     assert g.diag().reinit_iters == o.diag().reinit_iters
     assert abs(g.scalar("VOL_INS") - o.scalar("VOL_INS")) <= 1e-12 * abs(o.scalar("VOL_INS"))
 
