@@ -17,7 +17,8 @@ the roofline entry is the dominant kernel timed alone over every case
 (CUDA events on the library's stream), "accuracy" is the mixed form against
 the FP64 form on the 64x32x32 dam break after 200 steps, "output" times
 the field records (PRTSCR) of 16 cases and a restart save + load outside
-the timed region, and cpu_baseline is the oracle (a port of the reference,
+the timed region, "surface_tension" the capillary column with and without
+t_tens, and cpu_baseline is the oracle (a port of the reference,
 OpenMP where the reference has it) on a bounded sample.
 
 --impl reference times the reference's CPU implementation (the oracle port:
@@ -310,6 +311,24 @@ def output_run(gm, ncases):
         shutil.rmtree(d, ignore_errors=True)
 
 
+def tension_run(torch, steps=10, warmup=3):
+    """Surface tension's cost outside the timed region: the capillary column
+    (64^3, mixed form) with t_tens = 1 and with t_tens = 0, cell-steps/s."""
+    from suli_gb300 import cases
+    from suli_gb300._abi import PREC_MIXED
+    out = {"workload": "capillary_column_64x64x64", "steps": steps}
+    for tens in (1, 0):
+        c = cases.capillary_column(64, 64, 0.25, precision=PREC_MIXED)
+        c.params.t_tens = tens
+        g = start_gpu([c])
+        g.step(warmup)
+        ms = timed_steps(g, steps, torch)
+        g.close()
+        out["t_tens_%d" % tens] = {"value": c.cells * steps / (ms / 1e3), "ms_per_step": ms / steps}
+    out["overhead"] = out["t_tens_0"]["value"] / out["t_tens_1"]["value"] - 1.0
+    return out
+
+
 def mms_run(args):
     """The manufactured solution (13_mms.f90, steady) at 32^3, 64^3, 128^3 in
     both forms, args.mms_steps steps each, outside any timed region: RMS
@@ -516,6 +535,10 @@ def main():
             line["output"] = output_run(gm, min(16, len(cs_m)))
         except Exception as e:
             line["output"] = {"error": repr(e)}
+        try:
+            line["surface_tension"] = tension_run(torch)
+        except Exception as e:
+            line["surface_tension"] = {"error": repr(e)}
     gm.close()
     if args.accuracy_steps > 0 and rank == 0:
         try:
