@@ -48,9 +48,14 @@ template <typename T>
 __device__ __forceinline__ void load_line(const T *__restrict__ a, long long base, long long st, int i, int n,
                                           int ihs, T (&L)[7])
 {
+    // one 64-bit base, then 32-bit offsets: a case box holds fewer than 2^31
+    // elements (suli_create refuses larger ones)
+    const T *__restrict__ p = a + base;
+    const int s = (int)st;
     if (i >= 4 && i <= n - 3) {
+        const T *__restrict__ q = p + (i - 3) * s;
 #pragma unroll
-        for (int t = 0; t < 7; ++t) L[t] = a[base + (long long)(i - 3 + t) * st];
+        for (int t = 0; t < 7; ++t) L[t] = q[t * s];
         return;
     }
 #pragma unroll
@@ -59,9 +64,9 @@ __device__ __forceinline__ void load_line(const T *__restrict__ a, long long bas
         if (ihs == 0) {
             if (m < 1) m += n - 1;
             else if (m > n) m -= n - 1;
-            L[t] = a[base + (long long)m * st];
+            L[t] = p[m * s];
         } else if (m >= 1 && m <= n) {
-            L[t] = a[base + (long long)m * st];
+            L[t] = p[m * s];
         }
     }
     if (ihs != 0) {
@@ -70,7 +75,7 @@ __device__ __forceinline__ void load_line(const T *__restrict__ a, long long bas
             // ihs = 1 (curv_ls1): the low end's weights are (12, -9, 2) / 5
             // (8_derivadas.f90:716-721); ihs = 2: (18, -9, 2) / 11
             const T cl = (ihs == 1) ? T(1. / 5.) : c11, w0 = (ihs == 1) ? T(12.) : T(18.);
-            T p1 = a[base + st], p2 = a[base + 2 * st], p3 = a[base + 3 * st];
+            T p1 = p[s], p2 = p[2 * s], p3 = p[3 * s];
             T g0 = cl * (w0 * p1 - T(9.) * p2 + T(2.) * p3);
             T gm1 = cl * (w0 * g0 - T(9.) * p1 + T(2.) * p2);
             T gm2 = cl * (w0 * gm1 - T(9.) * g0 + T(2.) * p1);
@@ -83,8 +88,7 @@ __device__ __forceinline__ void load_line(const T *__restrict__ a, long long bas
             }
         }
         if (i + 3 > n) {
-            T pn = a[base + (long long)n * st], pn1 = a[base + (long long)(n - 1) * st],
-              pn2 = a[base + (long long)(n - 2) * st];
+            T pn = p[n * s], pn1 = p[(n - 1) * s], pn2 = p[(n - 2) * s];
             T g1 = c11 * (T(18.) * pn - T(9.) * pn1 + T(2.) * pn2);
             T g2 = c11 * (T(18.) * g1 - T(9.) * pn + T(2.) * pn1);
             T g3 = c11 * (T(18.) * g2 - T(9.) * g1 + T(2.) * pn);
