@@ -70,8 +70,11 @@ typedef struct suli_params {
     int32_t adv_type;              /* 1 = classical advective form */
     int32_t ibm_t;                 /* 0 none, 2 image-point IBM */
     int32_t obst_t;                /* 0 none, nonzero: obstacle fields uploaded */
-    int32_t m_turb;                /* 0 none, 1 Smagorinsky */
-    int32_t t_press;               /* 1 projection */
+    int32_t m_turb;                /* 0 none, 1 Smagorinsky, 2 k-equation LES, 3 k-equation DES
+                                      (5_viscosidade.f90:74-145) */
+    int32_t t_press;               /* 1 projection, 2 implicit pressure algorithm (IPA: exp_press,
+                                      11_diversos.f90:455-495; graddin after the RK loop with the
+                                      density rho_f1, 9_grad.f90:103-115; 1_principal.f90:82,111) */
     int32_t mms_t;                 /* 0 none, 1 steady MMS source */
     int32_t ccx0, ccxf, ccy0, ccyf, ccz0, cczf;  /* 0 periodic,1 free-slip,2 no-slip,3 prescribed,4 outflow(xf) */
     double  gx, gz;                /* gravity components (reference: 9.80665*sin/cos(atan(decliv))) */
@@ -95,6 +98,10 @@ typedef struct suli_params {
     int32_t t_tens;                /* 0 none, 1 surface tension (2_iniciais.f90:56; 14_level_set.f90:519-567,
                                       :660-704; 11_diversos.f90:383-395) */
     double  sigma;                 /* surface tension coefficient, N/m (reference: 0.0728) */
+    double  cmu, cdes;             /* k-equation constants: nut = cmu sqrt(ka) delta; DES limiter
+                                      constant (2_iniciais.f90:79-80) */
+    double  lcar;                  /* k-equation dissipation length: the reference's max(prof, ampl)
+                                      (5_viscosidade.f90:94) */
 } suli_params;
 
 /* ---- field ids (reference module arrays) -------------------------------- */
@@ -138,6 +145,13 @@ enum suli_field {
     SULI_F_HSY,
     SULI_F_HSZ,
     SULI_F_KURV,     /* kurv (nx, ny, nz) interface curvature, curv_ls1 (14_level_set.f90:660-704) */
+    SULI_F_KA,       /* ka (0:nx+1, 0:ny+1, 0:nz+1) turbulent kinetic energy, les; stored for
+                        m_turb >= 2 only ("field not stored" otherwise, where the reference's ka is 0) */
+    SULI_F_NUT,      /* nut (nx, ny, nz) modelled kinematic viscosity; stored for m_turb >= 2 */
+    SULI_F_PRD0,     /* prd0 (0:nx+1, 0:ny+1, 0:nz+1) accumulated pressure of the IPA; t_press = 2 */
+    SULI_F_PX,       /* px (nx1, ny, nz) explicit pressure force of the IPA (exp_press); t_press = 2 */
+    SULI_F_PY,       /* py (nx, ny1, nz) */
+    SULI_F_PZ,       /* pz (nx, ny, nz1) */
     SULI_F_COUNT
 };
 
@@ -219,6 +233,16 @@ int suli_complementos(suli_handle *h);           /* 11_diversos.f90:355-450 */
 int suli_tempo(suli_handle *h);                  /* 11_diversos.f90:10-296 (uses stage tt, dt) */
 int suli_graddin(suli_handle *h, int32_t *iters_out); /* 9_grad.f90:10-663 */
 int suli_posdin(suli_handle *h);                 /* 10_pos.f90:1-99 */
+/* exp_press (11_diversos.f90:455-495), t_press = 2 only: prd0 += prd1 and the
+ * explicit pressure force px/py/pz from prd0 + prd1 over the face density,
+ * which tempo adds to Fu/Fv/Fw (11_diversos.f90:21-45).  The IPA step calls it
+ * before visco and graddin once after the RK loop, without posdin
+ * (1_principal.f90:82,111).  SULI_BAD_CONFIG for t_press != 2. */
+int suli_exp_press(suli_handle *h);
+/* contorno_les (3_contorno.f90:666-790): the ghost values of ka, for the
+ * cases with m_turb >= 2 (the k-equation loop of visco calls it on every
+ * sub-stage; iniciais calls it once after setting ka, 2_iniciais.f90:216-235). */
+int suli_contorno_les(suli_handle *h);
 int suli_conmassa(suli_handle *h, double *maxdiv_out); /* 4_plot.f90:386-394 */
 int suli_mms_error(suli_handle *h, double err_out[4]); /* 13_mms.f90:391-451 */
 /* Sets tt (1..ntt) and dt = a_dt(tt), as the RK loop of 1_principal.f90:86-87. */
@@ -262,8 +286,8 @@ int suli_time_kernel(suli_handle *h, int kernel, int reps, double *ms_per_launch
  * Fortran order -- x, y, z of the cell corners (nx+1, ny+1, nz+1), u, v, w
  * averaged to the corners, ls (nx, ny, nz), obs_ls at the corners (zero
  * without an obstacle), and with t_plot = 1 the pressure minus its value at
- * cell (nx, 1, nz), the three vorticity components, nut and ka (zeros: the
- * k-equation model is not part of this library).  The record is formed on
+ * cell (nx, 1, nz) (prd0 + prd1 under the IPA), the three vorticity
+ * components, nut and ka (zeros for m_turb < 2, as in the reference).  The record is formed on
  * the device and copied once into pinned host memory.  The file name and the
  * output cadence (dt_frame) are the caller's, as is the XDMF index (visu,
  * 12_paraview_3D.f90).  SULI_BAD_ARG when the file cannot be written or the

@@ -47,7 +47,7 @@ def lib():
         L.or_level_set_ini.argtypes = [C.c_void_p, C.c_int] + [C.c_double] * 5
         for name in ("or_heaviside_init", "or_iniciais_velocity", "or_mms_init", "or_termo_fonte1",
                      "or_ibm_setup", "or_level_set", "or_visco", "or_convdiff", "or_complementos",
-                     "or_tempo", "or_posdin", "or_step"):
+                     "or_tempo", "or_posdin", "or_step", "or_exp_press", "or_contorno_les"):
             getattr(L, name).argtypes = [C.c_void_p]
             getattr(L, name).restype = None
         L.or_obstaculo_cylinder.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double]
@@ -166,6 +166,12 @@ class Oracle:
 
     def posdin(self):
         lib().or_posdin(self._h)
+
+    def exp_press(self):
+        lib().or_exp_press(self._h)
+
+    def contorno_les(self):
+        lib().or_contorno_les(self._h)
 
     def conmassa(self) -> float:
         return lib().or_conmassa(self._h)

@@ -98,6 +98,8 @@ struct or_case {
     F3 obs_lsx, obs_lsy, obs_lsz, obs_lss;
     F3 obs_ls;                 /* obs_ls (nx1, ny1, nz1), cell corners: field output only */
     F3 hsx, hsy, hsz, kurv;    /* surface tension (t_tens = 1), cells */
+    F3 ka, nut;                /* k equation (m_turb >= 2): ka (0:nx+1, 0:ny+1, 0:nz+1), nut cells */
+    F3 prd0, px, py, pz;       /* IPA (t_press = 2): prd0 like prd1, px/py/pz on the faces */
     I3 id_ibmx, id_ibmy, id_ibmz, id_ibm;
     F3 bxx0, bxx1, blx1;
 
@@ -155,6 +157,12 @@ or_case *or_create(const suli_params *pp)
     f3_init(&c->hsy, 1, nx, 1, ny, 1, nz);
     f3_init(&c->hsz, 1, nx, 1, ny, 1, nz);
     f3_init(&c->kurv, 1, nx, 1, ny, 1, nz);
+    f3_init(&c->ka, 0, nx + 1, 0, ny + 1, 0, nz + 1);     /* 0_modules.f90:274 */
+    f3_init(&c->nut, 1, nx, 1, ny, 1, nz);
+    f3_init(&c->prd0, 0, nx + 1, 0, ny + 1, 0, nz + 1);   /* :188 */
+    f3_init(&c->px, 1, nx1, 1, ny, 1, nz);                /* :191 */
+    f3_init(&c->py, 1, nx, 1, ny1, 1, nz);
+    f3_init(&c->pz, 1, nx, 1, ny, 1, nz1);
     i3_init(&c->id_ibmx, 1, nx1, 1, ny, 1, nz);
     i3_init(&c->id_ibmy, 1, nx, 1, ny1, 1, nz);
     i3_init(&c->id_ibmz, 1, nx, 1, ny, 1, nz1);
@@ -195,7 +203,8 @@ void or_destroy(or_case *c)
                  &c->mu, &c->mut, &c->xmu, &c->ymu, &c->zmu, &c->Fu, &c->Fv, &c->Fw, &c->u0,
                  &c->v0, &c->w0, &c->fu0, &c->fv0, &c->fw0, &c->fu1, &c->fv1, &c->fw1, &c->div,
                  &c->tf_u, &c->tf_v, &c->tf_w, &c->obs_lsx, &c->obs_lsy, &c->obs_lsz,
-                 &c->obs_lss, &c->bxx0, &c->bxx1, &c->blx1, &c->obs_ls, &c->hsx, &c->hsy, &c->hsz, &c->kurv};
+                 &c->obs_lss, &c->bxx0, &c->bxx1, &c->blx1, &c->obs_ls, &c->hsx, &c->hsy, &c->hsz, &c->kurv,
+                 &c->ka, &c->nut, &c->prd0, &c->px, &c->py, &c->pz};
     for (unsigned q = 0; q < sizeof(all) / sizeof(all[0]); ++q) free(all[q]->p);
     free(c->id_ibmx.p); free(c->id_ibmy.p); free(c->id_ibmz.p); free(c->id_ibm.p);
     free(c);
@@ -245,6 +254,12 @@ void *or_field(or_case *c, int f, int lo[3], int hi[3])
     case SULI_F_HSY: a = &c->hsy; break;
     case SULI_F_HSZ: a = &c->hsz; break;
     case SULI_F_KURV: a = &c->kurv; break;
+    case SULI_F_KA: a = &c->ka; break;
+    case SULI_F_NUT: a = &c->nut; break;
+    case SULI_F_PRD0: a = &c->prd0; break;
+    case SULI_F_PX: a = &c->px; break;
+    case SULI_F_PY: a = &c->py; break;
+    case SULI_F_PZ: a = &c->pz; break;
     case SULI_F_ID_IBMX: ia = &c->id_ibmx; break;
     case SULI_F_ID_IBMY: ia = &c->id_ibmy; break;
     case SULI_F_ID_IBMZ: ia = &c->id_ibmz; break;
@@ -754,11 +769,14 @@ void or_level_set(or_case *c)
 }
 
 /* ------------------------------------------------------------------------ */
-/* 5_viscosidade.f90:11-157 (m_turb 0 / 1)                                   */
+/* 5_viscosidade.f90:11-157 (m_turb 0 none, 1 Smagorinsky, 2/3 k equation)  */
 /* ------------------------------------------------------------------------ */
+static void keq(or_case *c, const F3 *sij);
+
 void or_visco(or_case *c)
 {
     int nx = c->nx, ny = c->ny, nz = c->nz, nx1 = c->nx1, ny1 = c->ny1, nz1 = c->nz1;
+    if (c->p.m_turb < 2) memset(c->ka.p, 0, sizeof(double) * (size_t)f3_size(&c->ka));   /* :47, :76 */
     if (c->p.m_turb == 0) {
         memset(c->mut.p, 0, sizeof(double) * (size_t)f3_size(&c->mut));
     } else {
@@ -794,17 +812,30 @@ void or_visco(or_case *c)
         interpx_fc(&ux, nx1, ny, nz, &dudx); interpx_fc(&uy, nx1, ny, nz, &dudy); interpx_fc(&uz, nx1, ny, nz, &dudz);
         interpy_fc(&vx, nx, ny1, nz, &dvdx); interpy_fc(&vy, nx, ny1, nz, &dvdy); interpy_fc(&vz, nx, ny1, nz, &dvdz);
         interpz_fc(&wx, nx, ny, nz1, &dwdx); interpz_fc(&wy, nx, ny, nz1, &dwdy); interpz_fc(&wz, nx, ny, nz1, &dwdz);
-        /* Smagorinsky, :78-88 */
-        double cl = pow(c->dx * c->dy * c->dz, 2. / 3.);
-        double cs = c->p.csmag;
+        /* p1 + p2 + p3 of :81-83 (and :117-119), per cell */
+        F3 sij = tmp3(1, nx, 1, ny, 1, nz);
         for (int k = 1; k <= nz; ++k)
             for (int j = 1; j <= ny; ++j)
                 for (int i = 1; i <= nx; ++i) {
                     double p1 = A(dudx, i, j, k) + 0.5 * (A(dudy, i, j, k) + A(dvdx, i, j, k) + A(dudz, i, j, k) + A(dwdx, i, j, k));
                     double p2 = A(dvdy, i, j, k) + 0.5 * (A(dvdx, i, j, k) + A(dudy, i, j, k) + A(dvdz, i, j, k) + A(dwdy, i, j, k));
                     double p3 = A(dwdz, i, j, k) + 0.5 * (A(dwdy, i, j, k) + A(dvdz, i, j, k) + A(dudz, i, j, k) + A(dwdx, i, j, k));
-                    A(c->mut, i, j, k) = cl * cs * cs * sqrt(2. * (p1 + p2 + p3) * (p1 + p2 + p3)) * A(c->rho, i, j, k);
+                    A(sij, i, j, k) = p1 + p2 + p3;
                 }
+        if (c->p.m_turb == 1) {
+            /* Smagorinsky, :74-88 */
+            double cl = pow(c->dx * c->dy * c->dz, 2. / 3.);
+            double cs = c->p.csmag;
+            for (int k = 1; k <= nz; ++k)
+                for (int j = 1; j <= ny; ++j)
+                    for (int i = 1; i <= nx; ++i) {
+                        double sm = A(sij, i, j, k);
+                        A(c->mut, i, j, k) = cl * cs * cs * sqrt(2. * sm * sm) * A(c->rho, i, j, k);
+                    }
+        } else {
+            keq(c, &sij);
+        }
+        fr(&sij);
         fr(&ux); fr(&uy); fr(&uz); fr(&vx); fr(&vy); fr(&vz); fr(&wx); fr(&wy); fr(&wz);
         fr(&dudx); fr(&dudy); fr(&dudz); fr(&dvdx); fr(&dvdy); fr(&dvdz); fr(&dwdx); fr(&dwdy); fr(&dwdz);
     }
@@ -858,6 +889,146 @@ static inline double upw(double vel, double dneg, double dpos)
     double a1 = vel > 0. ? vel : 0.;
     double a2 = vel < 0. ? vel : 0.;
     return a1 * dneg + a2 * dpos;
+}
+
+/* ------------------------------------------------------------------------ */
+/* The k equation of visco for m_turb = 2 (LES) and 3 (DES),                 */
+/* 5_viscosidade.f90:91-145, with its helpers                                */
+/* ------------------------------------------------------------------------ */
+/* contorno_les, 3_contorno.f90:666-790: y planes, then z, then x, each over
+ * the whole extent of the other two indices (ghosts included) */
+static void setx(F3 *a, int I, const F3 *b, int I2, double s);
+static void sety(F3 *a, int J, const F3 *b, int J2, double s);
+static void setz(F3 *a, int K, const F3 *b, int K2, double s);
+
+void or_contorno_les(or_case *c)
+{
+    F3 *k = &c->ka;
+    const int nx = c->nx, ny = c->ny, nz = c->nz;
+    const suli_params *p = &c->p;
+    if (p->ccy0 == 0 && p->ccyf == 0) { sety(k, ny + 1, k, 1, 1.); sety(k, 0, k, ny, 1.); }
+    if (p->ccy0 == 1) sety(k, 0, k, 1, 1.);
+    if (p->ccyf == 1) sety(k, ny + 1, k, ny, 1.);
+    if (p->ccy0 == 2) sety(k, 0, k, 1, -1.);
+    if (p->ccyf == 2) sety(k, ny + 1, k, ny, -1.);
+    if (p->ccz0 == 1) setz(k, 0, k, 1, 1.);
+    if (p->cczf == 1) setz(k, nz + 1, k, nz, 1.);
+    if (p->ccz0 == 2) setz(k, 0, k, 1, -1.);
+    if (p->ccz0 == 4) setz(k, 0, k, 1, -1.);
+    if (p->ccx0 == 0 && p->ccxf == 0) { setx(k, nx + 1, k, 1, 1.); setx(k, 0, k, nx, 1.); }
+    if (p->ccx0 == 1) setx(k, 0, k, 1, 1.);
+    if (p->ccxf == 1 || p->ccxf == 4) setx(k, nx + 1, k, nx, 1.);
+    if (p->ccx0 == 2) setx(k, 0, k, 1, -1.);
+    if (p->ccxf == 2) setx(k, nx + 1, k, nx, -1.);
+    if (p->ccx0 == 3) {
+        const double kin = p->iturb * p->iturb * p->uinicial * p->uinicial * 1.5;
+        for (int kk = 1; kk <= nz; ++kk)
+            for (int j = 1; j <= ny; ++j) A(*k, 0, j, kk) = kin;
+    }
+    if (p->ccxf == 3) setx(k, nx + 1, k, nx, 1.);
+}
+
+/* convdiff_les, 6_convdiff.f90:171-205: Fka = -adv_esc(ka) (7_advectivo.f90:654-706,
+ * 2nd-order upwind with the face velocities averaged to the centre) plus the
+ * diffusion with mu = ls_mu + nut rho at the faces, over rho */
+static void convdiff_les(or_case *c, F3 *fka)
+{
+    const int nx = c->nx, ny = c->ny, nz = c->nz, nx1 = c->nx1, ny1 = c->ny1, nz1 = c->nz1;
+    F3 uc = tmp3(1, nx, 1, ny, 1, nz), vc = tmp3(1, nx, 1, ny, 1, nz), wc = tmp3(1, nx, 1, ny, 1, nz);
+    F3 uin = c->u, vin = c->v, win = c->w;
+    interpx_fc(&uin, nx1, ny, nz, &uc);
+    interpy_fc(&vin, nx, ny1, nz, &vc);
+    interpz_fc(&win, nx, ny, nz1, &wc);
+    F3 mua = tmp3(1, nx, 1, ny, 1, nz);
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i)
+                A(mua, i, j, k) = A(c->ls_mu, i, j, k) + A(c->nut, i, j, k) * A(c->rho, i, j, k);
+    F3 am = tmp3(1, nx1, 1, ny, 1, nz), bm = tmp3(1, nx, 1, ny1, 1, nz), dm = tmp3(1, nx, 1, ny, 1, nz1);
+    interpx_cf(c, &mua, nx, ny, nz, &am);
+    interpy_cf(&mua, nx, ny, nz, &bm);
+    interpz_cf(&mua, nx, ny, nz, &dm);
+    const F3 *ka = &c->ka;
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i) {
+                double adv = upw(A(uc, i, j, k), d2n_x(c, ka, i, j, k, nx), d2p_x(c, ka, i, j, k, nx)) +
+                             upw(A(vc, i, j, k), d2n_y(c, ka, i, j, k), d2p_y(c, ka, i, j, k, ny)) +
+                             upw(A(wc, i, j, k), d2n_z(c, ka, i, j, k), d2p_z(c, ka, i, j, k, nz));
+                double kc = A(*ka, i, j, k);
+                A(*fka, i, j, k) = -adv +
+                    ((A(am, i + 1, j, k) * (A(*ka, i + 1, j, k) - kc) - A(am, i, j, k) * (kc - A(*ka, i - 1, j, k))) / (c->dx * c->dx) +
+                     (A(bm, i, j + 1, k) * (A(*ka, i, j + 1, k) - kc) - A(bm, i, j, k) * (kc - A(*ka, i, j - 1, k))) / (c->dy * c->dy) +
+                     (A(dm, i, j, k + 1) * (A(*ka, i, j, k + 1) - kc) - A(dm, i, j, k) * (kc - A(*ka, i, j, k - 1))) / (c->dz * c->dz)) /
+                    A(c->rho, i, j, k);
+            }
+    fr(&uc); fr(&vc); fr(&wc); fr(&mua); fr(&am); fr(&bm); fr(&dm);
+}
+
+/* :91-145.  The sub-stages use the stage step a_dt(tt) of the RK scheme and
+ * tempo_esc's RK3 update (11_diversos.f90:300-351) whatever t_tempo is; the
+ * reference changes its global tt/dt there, which the RK loop of the time
+ * step sets again before use, so they stay local here. */
+static void keq(or_case *c, const F3 *sij)
+{
+    const int nx = c->nx, ny = c->ny, nz = c->nz;
+    double delta = c->dx;                              /* 2_iniciais.f90:112 */
+    if (c->dy > delta) delta = c->dy;
+    if (c->dz > delta) delta = c->dz;
+    const double cmu = c->p.cmu, cdes = c->p.cdes, lcar = c->p.lcar;
+    F3 fka = tmp3(1, nx, 1, ny, 1, nz), e0 = tmp3(1, nx, 1, ny, 1, nz), fe0 = tmp3(1, nx, 1, ny, 1, nz),
+       fe1 = tmp3(1, nx, 1, ny, 1, nz);
+    for (int tt = 1; tt <= c->ntt; ++tt) {
+        const double dt = c->a_dt[tt - 1];
+        for (int k = 1; k <= nz; ++k)
+            for (int j = 1; j <= ny; ++j)
+                for (int i = 1; i <= nx; ++i)
+                    A(c->nut, i, j, k) = cmu * pow(A(c->ka, i, j, k), 0.5) * delta;
+        convdiff_les(c, &fka);
+        for (int k = 1; k <= nz; ++k)
+            for (int j = 1; j <= ny; ++j)
+                for (int i = 1; i <= nx; ++i) {
+                    const double kk = A(c->ka, i, j, k);
+                    const double diss = pow(kk, 1.5) / lcar;
+                    double des = 1.;
+                    /* Fortran MAX returns the number when the other argument
+                     * is a NaN (ka = 0 gives 0/0), as fmax does */
+                    if (c->p.m_turb == 3) des = fmax(1., pow(kk, 1.5) / (cdes * delta * diss));
+                    const double sm = A(*sij, i, j, k);
+                    A(fka, i, j, k) = A(fka, i, j, k) + A(c->nut, i, j, k) * 2. * sm * sm - des * diss;
+                }
+        /* tempo_esc */
+        for (int k = 1; k <= nz; ++k)
+            for (int j = 1; j <= ny; ++j)
+                for (int i = 1; i <= nx; ++i) {
+                    double *e = &A(c->ka, i, j, k);
+                    const double F = A(fka, i, j, k);
+                    if (tt == 1) {
+                        A(e0, i, j, k) = *e;
+                        A(fe0, i, j, k) = F;
+                        *e = *e + dt * F;
+                    } else if (tt == 2) {
+                        const double aux1 = 2. * dt;
+                        A(fe1, i, j, k) = F;
+                        *e = A(e0, i, j, k) - dt * A(fe0, i, j, k) + aux1 * F;
+                    } else {
+                        const double aux1 = dt / 6.;
+                        *e = A(e0, i, j, k) + aux1 * (A(fe0, i, j, k) + 4. * A(fe1, i, j, k) + F);
+                    }
+                }
+        or_contorno_les(c);
+        for (int k = 1; k <= nz; ++k)
+            for (int j = 1; j <= ny; ++j)
+                for (int i = 1; i <= nx; ++i)
+                    if (A(c->ka, i, j, k) < 0) A(c->ka, i, j, k) = 0.;
+    }
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i) {
+                A(c->nut, i, j, k) = cmu * pow(A(c->ka, i, j, k), 0.5) * delta;
+                A(c->mut, i, j, k) = A(c->nut, i, j, k) * A(c->rho, i, j, k);
+            }
+    fr(&fka); fr(&e0); fr(&fe0); fr(&fe1);
 }
 
 static void classico(or_case *c, F3 *uint_, F3 *vint_, F3 *wint_)
@@ -1008,7 +1179,54 @@ void or_convdiff(or_case *c)
 /* ------------------------------------------------------------------------ */
 /* 11_diversos.f90:355-450 -- complementos (t_tens=0, m_turb<2, no sponge)   */
 /* ------------------------------------------------------------------------ */
+/* fantasmas_cf(rho) (8_derivadas.f90:625-671) at a point with at most one
+ * index on a ghost layer: y and z ghosts copy the adjacent cell, x ghosts
+ * wrap on a periodic x and copy otherwise */
+static double rhof_at(const or_case *c, int i, int j, int k)
+{
+    const int nx = c->nx, ny = c->ny, nz = c->nz, per = (c->p.ccx0 == 0);
+    if (j == 0) j = 1; else if (j == ny + 1) j = ny;
+    if (k == 0) k = 1; else if (k == nz + 1) k = nz;
+    if (i == 0) i = per ? nx : 1; else if (i == nx + 1) i = per ? 1 : nx;
+    return A(c->rho, i, j, k);
+}
+
+/* the turbulent kinetic energy term of complementos, 11_diversos.f90:403-444:
+ * - 2/3 (karho(i) - karho(i-1)) / (h rho_face) with karho = ka rhof, the
+ * last term of each sum (for m_turb < 2 ka is 0 and the term an exact zero) */
+static void complementos_ka(or_case *c)
+{
+    const int nx = c->nx, ny = c->ny, nz = c->nz, nx1 = c->nx1, ny1 = c->ny1, nz1 = c->nz1;
+    F3 xr = tmp3(1, nx1, 1, ny, 1, nz), yr = tmp3(1, nx, 1, ny1, 1, nz), zr = tmp3(1, nx, 1, ny, 1, nz1);
+    interpx_cf(c, &c->rho, nx, ny, nz, &xr);
+    interpy_cf(&c->rho, nx, ny, nz, &yr);
+    interpz_cf(&c->rho, nx, ny, nz, &zr);
+#define KR(i, j, k) (A(c->ka, i, j, k) * rhof_at(c, i, j, k))
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx1; ++i)
+                A(c->Fu, i, j, k) = A(c->Fu, i, j, k) - 2. / 3. * (KR(i, j, k) - KR(i - 1, j, k)) / (c->dx * A(xr, i, j, k));
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny1; ++j)
+            for (int i = 1; i <= nx; ++i)
+                A(c->Fv, i, j, k) = A(c->Fv, i, j, k) - 2. / 3. * (KR(i, j, k) - KR(i, j - 1, k)) / (c->dy * A(yr, i, j, k));
+    for (int k = 1; k <= nz1; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i)
+                A(c->Fw, i, j, k) = A(c->Fw, i, j, k) - 2. / 3. * (KR(i, j, k) - KR(i, j, k - 1)) / (c->dz * A(zr, i, j, k));
+#undef KR
+    fr(&xr); fr(&yr); fr(&zr);
+}
+
+static void complementos_main(or_case *c);
+
 void or_complementos(or_case *c)
+{
+    complementos_main(c);
+    if (c->p.m_turb >= 2) complementos_ka(c);
+}
+
+static void complementos_main(or_case *c)
 {
     int nx = c->nx, ny = c->ny, nz = c->nz, nx1 = c->nx1, ny1 = c->ny1, nz1 = c->nz1;
     /* gravity, surface tension (t_tens = 1: sigma times the face value of
@@ -1097,8 +1315,25 @@ static void tempo_one(or_case *c, F3 *u, F3 *F, F3 *u0, F3 *f0, F3 *f1, int di, 
             }
 }
 
+static int ipa(const or_case *c)
+{
+    return c->p.t_press == 2 && (c->p.mms_t == 0 || c->p.project_under_mms);
+}
+
 void or_tempo(or_case *c)
 {
+    if (ipa(c)) {   /* the IPA's explicit pressure force, :21-45 */
+        const int nx = c->nx, ny = c->ny, nz = c->nz, nx1 = c->nx1, ny1 = c->ny1, nz1 = c->nz1;
+        for (int k = 1; k <= nz; ++k)
+            for (int j = 1; j <= ny; ++j)
+                for (int i = 1; i <= nx1; ++i) A(c->Fu, i, j, k) = A(c->Fu, i, j, k) + A(c->px, i, j, k);
+        for (int k = 1; k <= nz; ++k)
+            for (int j = 1; j <= ny1; ++j)
+                for (int i = 1; i <= nx; ++i) A(c->Fv, i, j, k) = A(c->Fv, i, j, k) + A(c->py, i, j, k);
+        for (int k = 1; k <= nz1; ++k)
+            for (int j = 1; j <= ny; ++j)
+                for (int i = 1; i <= nx; ++i) A(c->Fw, i, j, k) = A(c->Fw, i, j, k) + A(c->pz, i, j, k);
+    }
     tempo_one(c, &c->u, &c->Fu, &c->u0, &c->fu0, &c->fu1, c->nx1, c->ny, c->nz);
     tempo_one(c, &c->v, &c->Fv, &c->v0, &c->fv0, &c->fv1, c->nx, c->ny1, c->nz);
     tempo_one(c, &c->w, &c->Fw, &c->w0, &c->fw0, &c->fw1, c->nx, c->ny, c->nz1);
@@ -1453,6 +1688,35 @@ static void ghost_fill_cg(const or_case *c, F3 *m)
         for (int i = 0; i <= nx1; ++i) { A(*m, i, j, 0) = A(*m, i, j, 1); A(*m, i, j, nz + 1) = A(*m, i, j, nz); }
 }
 
+/* exp_press, 11_diversos.f90:455-495 (t_press = 2) */
+void or_exp_press(or_case *c)
+{
+    const int nx = c->nx, ny = c->ny, nz = c->nz, nx1 = c->nx1, ny1 = c->ny1, nz1 = c->nz1;
+    const long n = f3_size(&c->prd0);
+    F3 pa = tmp3(0, nx + 1, 0, ny + 1, 0, nz + 1);
+    for (long q = 0; q < n; ++q) {
+        c->prd0.p[q] = c->prd1.p[q] + c->prd0.p[q];
+        pa.p[q] = c->prd1.p[q] + c->prd0.p[q];
+    }
+    F3 xr = tmp3(1, nx1, 1, ny, 1, nz), yr = tmp3(1, nx, 1, ny1, 1, nz), zr = tmp3(1, nx, 1, ny, 1, nz1);
+    interpx_cf(c, &c->rho, nx, ny, nz, &xr);
+    interpy_cf(&c->rho, nx, ny, nz, &yr);
+    interpz_cf(&c->rho, nx, ny, nz, &zr);
+    for (int k = 1; k <= nz; ++k) {
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx1; ++i)
+                A(c->px, i, j, k) = -(A(pa, i, j, k) - A(pa, i - 1, j, k)) / c->dx / A(xr, i, j, k);
+        for (int j = 1; j <= ny1; ++j)
+            for (int i = 1; i <= nx; ++i)
+                A(c->py, i, j, k) = -(A(pa, i, j, k) - A(pa, i, j - 1, k)) / c->dy / A(yr, i, j, k);
+    }
+    for (int k = 1; k <= nz1; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i)
+                A(c->pz, i, j, k) = -(A(pa, i, j, k) - A(pa, i, j, k - 1)) / c->dz / A(zr, i, j, k);
+    fr(&pa); fr(&xr); fr(&yr); fr(&zr);
+}
+
 int or_graddin(or_case *c)
 {
     int nx = c->nx, ny = c->ny, nz = c->nz, nx1 = c->nx1, ny1 = c->ny1, nz1 = c->nz1;
@@ -1466,9 +1730,16 @@ int or_graddin(or_case *c)
     int ibm_mask = (c->p.obst_t != 0 && c->p.ibm_t == 2);
 
     double aux1 = dt / (dx * dx), aux2 = dt / (dy * dy), aux3 = dt / (dz * dz);
-    interpx_cf(c, &c->rho, nx, ny, nz, &rhox);
-    interpy_cf(&c->rho, nx, ny, nz, &rhoy);
-    interpz_cf(&c->rho, nx, ny, nz, &rhoz);
+    if (c->p.t_press == 2) {
+        /* IPA: the operator of the density rho_f1 (:111-115) */
+        F3 *rr[] = {&rhox, &rhoy, &rhoz};
+        for (int q = 0; q < 3; ++q)
+            for (long m = 0; m < f3_size(rr[q]); ++m) rr[q]->p[m] = c->p.rho_f1;
+    } else {
+        interpx_cf(c, &c->rho, nx, ny, nz, &rhox);
+        interpy_cf(&c->rho, nx, ny, nz, &rhoy);
+        interpz_cf(&c->rho, nx, ny, nz, &rhoz);
+    }
 #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nz; ++k)
         for (int j = 1; j <= ny; ++j)
@@ -1689,15 +1960,17 @@ int or_prtscr_write(or_case *c, const char *path, int t_plot)
                 obs[q] = (c->p.obst_t == 0) ? 0.0f : (float)A(c->obs_ls, i, j, k);
             }
     free(x1); free(y1); free(z1);
-    float *pr = obs + n1, *vi = pr + nc, *vj = vi + nc, *vk = vj + nc;   /* nut, ka: zeros */
-    const double pref = A(c->prd1, nx, 1, nz);
+    float *pr = obs + n1, *vi = pr + nc, *vj = vi + nc, *vk = vj + nc, *nuo = vk + nc, *kao = nuo + nc;
+    const double pref = A(c->prd0, nx, 1, nz) + A(c->prd1, nx, 1, nz);   /* :573 */
     for (int k = 1; k <= nz; ++k)
         for (int j = 1; j <= ny; ++j)
             for (int i = 1; i <= nx; ++i) {
                 const long q = (i - 1) + (long)nx * ((j - 1) + (long)ny * (k - 1));
                 lso[q] = (float)A(c->ls, i, j, k);
                 if (!t_plot) continue;
-                pr[q] = (float)(A(c->prd1, i, j, k) - pref);
+                pr[q] = (float)(A(c->prd0, i, j, k) + A(c->prd1, i, j, k) - pref);
+                nuo[q] = (float)A(c->nut, i, j, k);
+                kao[q] = (float)A(c->ka, i, j, k);
                 const double dudy = (A(c->u, i, j + 1, k) - A(c->u, i, j, k)) / c->dy;
                 const double dudz = (A(c->u, i, j, k + 1) - A(c->u, i, j, k)) / c->dz;
                 const double dvdx = (A(c->v, i + 1, j, k) - A(c->v, i, j, k)) / c->dx;
@@ -1946,6 +2219,7 @@ void or_step(or_case *c)
     c->t = c->t + c->dt;
     or_level_set(c);
     or_contorno(c, 3);
+    if (ipa(c)) or_exp_press(c);
     or_visco(c);
     for (int tt = 1; tt <= c->ntt; ++tt) {
         or_set_stage(c, tt);
@@ -1954,10 +2228,13 @@ void or_step(or_case *c)
         or_tempo(c);
         or_contorno(c, 2);
         if (c->p.mms_t == 0 || c->p.project_under_mms) {
-            or_graddin(c);
-            or_posdin(c);
+            if (c->p.t_press == 1) {
+                or_graddin(c);
+                or_posdin(c);
+            }
             or_contorno(c, 1);
         }
     }
+    if (ipa(c)) or_graddin(c);      /* :111, after the RK loop, no posdin */
     or_conmassa(c);
 }

@@ -52,6 +52,9 @@ class SuliParams(C.Structure):
         ("seed", C.c_uint64),
         ("t_tens", C.c_int32),
         ("sigma", C.c_double),
+        ("cmu", C.c_double),
+        ("cdes", C.c_double),
+        ("lcar", C.c_double),
     ]
 
     def copy(self) -> "SuliParams":
@@ -100,6 +103,9 @@ def default_params(**kw) -> SuliParams:
     p.vol_loop_max = 1000
     p.t_tens = 0
     p.sigma = 0.0728
+    p.cmu = 0.05
+    p.cdes = 0.65
+    p.lcar = 0.05715
     p.mixed_precond = 1
     for k, v in kw.items():
         if not hasattr(p, k):
@@ -116,6 +122,7 @@ FIELDS = [
     "OBS_LSX", "OBS_LSY", "OBS_LSZ", "OBS_LSS",
     "ID_IBMX", "ID_IBMY", "ID_IBMZ", "ID_IBM",
     "BXX0", "BXX1", "BLX1", "OBS_LS", "HSX", "HSY", "HSZ", "KURV",
+    "KA", "NUT", "PRD0", "PX", "PY", "PZ",
 ]
 FIELD_ID = {name: i for i, name in enumerate(FIELDS)}
 INT_FIELDS = {"ID_IBMX", "ID_IBMY", "ID_IBMZ", "ID_IBM"}
@@ -138,6 +145,8 @@ def field_bounds(p: SuliParams, name: str):
         "W": ((0, 0, 0), (nx + 1, ny + 1, nz1 + 1)),
         "PRD1": ((0, 0, 0), (nx + 1, ny + 1, nz + 1)),
         "PRD": ((0, 0, 0), (nx + 1, ny + 1, nz + 1)),
+        "KA": ((0, 0, 0), (nx + 1, ny + 1, nz + 1)),
+        "PRD0": ((0, 0, 0), (nx + 1, ny + 1, nz + 1)),
         "BXX0": ((0, 0, 0), (ny + 1, nz + 1, 0)),
         "BXX1": ((0, 0, 0), (ny + 1, nz + 1, 0)),
         "BLX1": ((1, 1, 0), (ny, nz, 0)),
@@ -145,13 +154,14 @@ def field_bounds(p: SuliParams, name: str):
     }
     if name in table:
         return table[name]
-    if name in ("LS", "HS", "RHO", "LS_MU", "MU", "MUT", "DIV", "OBS_LSS", "ID_IBM", "HSX", "HSY", "HSZ", "KURV"):
+    if name in ("LS", "HS", "RHO", "LS_MU", "MU", "MUT", "DIV", "OBS_LSS", "ID_IBM", "HSX", "HSY", "HSZ", "KURV",
+                "NUT"):
         return cell
-    if name in ("XMU", "FU", "U0", "FU0", "FU1", "TF_U", "OBS_LSX", "ID_IBMX"):
+    if name in ("XMU", "FU", "U0", "FU0", "FU1", "TF_U", "OBS_LSX", "ID_IBMX", "PX"):
         return xface
-    if name in ("YMU", "FV", "V0", "FV0", "FV1", "TF_V", "OBS_LSY", "ID_IBMY"):
+    if name in ("YMU", "FV", "V0", "FV0", "FV1", "TF_V", "OBS_LSY", "ID_IBMY", "PY"):
         return yface
-    if name in ("ZMU", "FW", "W0", "FW0", "FW1", "TF_W", "OBS_LSZ", "ID_IBMZ"):
+    if name in ("ZMU", "FW", "W0", "FW0", "FW1", "TF_W", "OBS_LSZ", "ID_IBMZ", "PZ"):
         return zface
     raise KeyError(name)
 

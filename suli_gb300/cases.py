@@ -288,3 +288,59 @@ def capillary_column(n=48, ny=4, radius=0.25, precision=PREC_FP64, dt=2e-4) -> C
     ls = np.empty((n, ny, n), order="F")
     ls[...] = radius - np.sqrt((x - 0.5) ** 2 + (z - 0.5) ** 2)
     return Case("capillary_%d" % n, p, _base_fields(p, ls), steps=20)
+
+
+def k_channel(nx=32, ny=8, nz=16, m_turb=2, precision=PREC_FP64, dt=2e-4, seed=7) -> Case:
+    """Open-channel flow with the k-equation model (m_turb = 2, LES with the
+    turbulent kinetic energy equation, or 3, DES; 5_viscosidade.f90:91-145):
+    a 2 x 0.5 x 1 m box periodic in x, water below z = 0.6 m, no-slip bed,
+    free-slip side walls and lid, driven by a bed slope of 0.01 (gx).  The initial state
+    is iniciais() for m_turb >= 2 (2_iniciais.f90:216-235): u = uinicial = 0.5
+    m/s, ka = 1.5 iturb^2 (uinicial^2 + 1e-6) in every cell and each velocity
+    component perturbed by sqrt(ka) times a uniform draw (seeded here, as
+    random_number is upstream); the ghost values of ka come from
+    contorno_les, which the caller applies once (suli_contorno_les)."""
+    lx = 2.0
+    h = lx / nx
+    slope = 0.01
+    g = 9.80665
+    p = default_params(nx=nx, ny=ny, nz=nz, dx=h, dy=h, dz=h, dt=dt,
+                       ccx0=0, ccxf=0, ccy0=1, ccyf=1, ccz0=2, cczf=1,
+                       gx=g * math.sin(math.atan(slope)), gz=g * math.cos(math.atan(slope)),
+                       m_turb=m_turb, uinicial=0.5, iturb=0.05, reinit_max_iter=3,
+                       cg_tol_mode=CG_TOL_REL, cg_tol=1e-10, precision=precision)
+    p.lcar = 0.6
+    z = _centres(nz, h)[None, None, :]
+    ls = np.empty((nx, ny, nz), order="F")
+    ls[...] = 0.6 - z
+    f = _base_fields(p, ls)
+    aux1 = p.iturb * p.iturb * (p.uinicial * p.uinicial + 1e-6) * 1.5
+    rng = np.random.default_rng(seed)
+    ka = _zeros(p, "KA")
+    ka[1:nx + 1, 1:ny + 1, 1:nz + 1] = aux1
+    f["KA"] = ka
+    for name in ("U", "V", "W"):
+        a = f[name]
+        a[1:nx + 1, 1:ny + 1, 1:nz + 1] += math.sqrt(aux1) * rng.random((nx, ny, nz))
+    return Case("k_channel_m%d_%dx%dx%d" % (m_turb, nx, ny, nz), p, f, steps=200)
+
+
+def ipa_tank(nx=24, ny=8, nz=16, precision=PREC_FP64, dt=1e-4) -> Case:
+    """Still water in a closed tank under the implicit pressure algorithm
+    (t_press = 2: exp_press before visco, graddin with the density rho_f1
+    after the RK loop and no posdin; 1_principal.f90:82,111, 11_diversos.f90:
+    455-495, 9_grad.f90:103-115): a 1.5 x 0.5 x 1 m box with a slightly
+    tilted free surface (eta = 0.02 (x - 0.75)) at 0.5 m depth, free-slip
+    walls.  The pressure accumulates in prd0 towards the hydrostatic one."""
+    h = 1.5 / nx
+    p = default_params(nx=nx, ny=ny, nz=nz, dx=h, dy=h, dz=h, dt=dt,
+                       ccx0=1, ccxf=1, ccy0=1, ccyf=1, ccz0=1, cczf=1,
+                       gz=9.80665, t_press=2, reinit_max_iter=3,
+                       cg_tol_mode=CG_TOL_REL, cg_tol=1e-10, precision=precision)
+    x = _centres(nx, h)[:, None, None]
+    z = _centres(nz, h)[None, None, :]
+    ls = np.empty((nx, ny, nz), order="F")
+    ls[...] = 0.5 + 0.02 * (x - 0.75) - z
+    f = _base_fields(p, ls)
+    f["PRD0"] = _zeros(p, "PRD0")
+    return Case("ipa_tank_%dx%dx%d" % (nx, ny, nz), p, f, steps=200)

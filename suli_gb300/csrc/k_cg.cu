@@ -64,12 +64,15 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_setup1(const CaseDev<T> *__rest
     const double dt = c.sc[S_DT];
     const T aux1 = T(dt / (c.dx * c.dx)), aux2 = T(dt / (c.dy * c.dy)), aux3 = T(dt / (c.dz * c.dz));
     const T *rho = c.rho;
-    T si0 = aux1 / icf<T>(i, nx, px, [&](int m) { return AT(rho, m, j, k); });
-    T si1 = aux1 / icf<T>(i + 1, nx, px, [&](int m) { return AT(rho, m, j, k); });
-    T sj0 = aux2 / icf<T>(j, ny, false, [&](int m) { return AT(rho, i, m, k); });
-    T sj1 = aux2 / icf<T>(j + 1, ny, false, [&](int m) { return AT(rho, i, m, k); });
-    T sk0 = aux3 / icf<T>(k, nz, false, [&](int m) { return AT(rho, i, j, m); });
-    T sk1 = aux3 / icf<T>(k + 1, nz, false, [&](int m) { return AT(rho, i, j, m); });
+    // face densities: interp?_cf of rho, or rho_f1 for the IPA (:103-115)
+    const bool ipa = (c.t_press == 2);
+    const T r1 = T(c.rho_f1);
+    T si0 = aux1 / (ipa ? r1 : icf<T>(i, nx, px, [&](int m) { return AT(rho, m, j, k); }));
+    T si1 = aux1 / (ipa ? r1 : icf<T>(i + 1, nx, px, [&](int m) { return AT(rho, m, j, k); }));
+    T sj0 = aux2 / (ipa ? r1 : icf<T>(j, ny, false, [&](int m) { return AT(rho, i, m, k); }));
+    T sj1 = aux2 / (ipa ? r1 : icf<T>(j + 1, ny, false, [&](int m) { return AT(rho, i, m, k); }));
+    T sk0 = aux3 / (ipa ? r1 : icf<T>(k, nz, false, [&](int m) { return AT(rho, i, j, m); }));
+    T sk1 = aux3 / (ipa ? r1 : icf<T>(k + 1, nz, false, [&](int m) { return AT(rho, i, j, m); }));
     long long q = g.at(i, j, k);
     c.spi[q] = si0;
     c.spj[q] = sj0;
@@ -141,6 +144,7 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_op1m(const CaseDev<T> *__restri
     // per face: the projection's unit factor 1 / (h rho_face), by reciprocal
     // (no FP64 divide), kept for posdin; the operator's coefficient is it / h
     auto face = [&](double *pf, double *sp, long long qf, double ih, double rf) {
+        if (c.t_press == 2) rf = c.rho_f1;   // the IPA's operator (9_grad.f90:111-115)
         const double f = ih * rcp_nr64(rf);
         pf[qf] = f;
         sp[qf] = f * ih;

@@ -1,6 +1,7 @@
 // k_momentum.cu -- momentum-side kernels.
 //
 //   k_visco_mu      5_viscosidade.f90:11-151  Smagorinsky mu_t, mu = ls_mu + mu_t
+//                   (m_turb >= 2: the strain sum for the k equation of k_keq.cu)
 //   k_visco_faces   5_viscosidade.f90:153-155 mu -> xmu/ymu/zmu (interp*_cf)
 //   k_convdiff      6_convdiff.f90:14-167 with classico der=3 (7_advectivo.f90:171-284);
 //                   optionally fused with complementos (11_diversos.f90:355-450)
@@ -48,6 +49,40 @@ __device__ __forceinline__ T tension_face(const CaseDev<T> &c, int axis, int i, 
     return T(c.sigma) * f;
 }
 
+// the kinetic-energy term of complementos (m_turb >= 2, 11_diversos.f90:403-444):
+// 2/3 (karho(m) - karho(m-1)) / (h rho_face) on the axis-0/1/2 face (i, j, k),
+// karho = ka rhof with rhof = fantasmas_cf(rho) (8_derivadas.f90:625-671: y and
+// z ghosts copy the adjacent cell, x ghosts wrap on a periodic x)
+template <typename T>
+__device__ __forceinline__ T ka_face(const CaseDev<T> &c, int axis, int i, int j, int k)
+{
+    const Geo &g = c.g;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const bool per = (c.ccx0 == 0);
+    auto kr = [&](int a, int b, int d) {
+        const T kv = c.ka[g.at(a, b, d)];
+        if (b == 0) b = 1; else if (b == ny + 1) b = ny;
+        if (d == 0) d = 1; else if (d == nz + 1) d = nz;
+        if (a == 0) a = per ? nx : 1; else if (a == nx + 1) a = per ? 1 : nx;
+        return kv * c.rho[g.at(a, b, d)];
+    };
+    T diff, rf, h;
+    if (axis == 0) {
+        diff = kr(i, j, k) - kr(i - 1, j, k);
+        rf = interp_cf<T>(i, nx, per, [&](int m) { return c.rho[g.at(m, j, k)]; });
+        h = T(c.dx);
+    } else if (axis == 1) {
+        diff = kr(i, j, k) - kr(i, j - 1, k);
+        rf = interp_cf<T>(j, ny, false, [&](int m) { return c.rho[g.at(i, m, k)]; });
+        h = T(c.dy);
+    } else {
+        diff = kr(i, j, k) - kr(i, j, k - 1);
+        rf = interp_cf<T>(k, nz, false, [&](int m) { return c.rho[g.at(i, j, m)]; });
+        h = T(c.dz);
+    }
+    return T(2. / 3.) * diff / (h * rf);
+}
+
 template <typename T>
 __device__ __forceinline__ T upw(T vel, T dneg, T dpos)
 {
@@ -86,7 +121,7 @@ __global__ void __launch_bounds__(NTHREADS) k_visco_mu(const CaseDev<T> *__restr
     if (i > g.nx || j > g.ny || k > g.nz) return;
     long long q = g.at(i, j, k);
     T mut = T(0.);
-    if (c.m_turb == 1) {
+    if (c.m_turb >= 1) {
         const T *u = c.u, *v = c.v, *w = c.w;
         const T tdx = T(1.0 / (2. * c.dx)), tdy = T(1.0 / (2. * c.dy)), tdz = T(1.0 / (2. * c.dz));
         // derivax/y/z on the staggered arrays then interp?_fc to the centre
@@ -102,7 +137,12 @@ __global__ void __launch_bounds__(NTHREADS) k_visco_mu(const CaseDev<T> *__restr
         T p1 = dudx + T(0.5) * (dudy + dvdx + dudz + dwdx);
         T p2 = dvdy + T(0.5) * (dvdx + dudy + dvdz + dwdy);
         T p3 = dwdz + T(0.5) * (dwdy + dvdz + dudz + dwdx);
-        mut = T(c.cles) * sqrt(T(2.) * (p1 + p2 + p3) * (p1 + p2 + p3)) * c.rho[q];
+        const T sm = p1 + p2 + p3;
+        if (c.m_turb >= 2) {   // the k equation's production term uses it (:117-122); mut comes after its loop
+            c.sij[q] = sm;
+            return;
+        }
+        mut = T(c.cles) * sqrt(T(2.) * sm * sm) * c.rho[q];
     }
     c.mut[q] = mut;
     c.mu[q] = c.ls_mu[q] + mut;
@@ -178,6 +218,7 @@ __global__ void __launch_bounds__(NTHREADS) k_convdiff(const CaseDev<T> *__restr
             F = F + T(c.gx);
             if (c.t_tens == 1) F = F - tension_face(c, 0, i, j, k);
             F = F + AT(c.tf_u, i, j, k);
+            if (c.m_turb >= 2) F = F - ka_face(c, 0, i, j, k);
         }
         AT(c.Fu, i, j, k) = F;
     }
@@ -211,6 +252,7 @@ __global__ void __launch_bounds__(NTHREADS) k_convdiff(const CaseDev<T> *__restr
         if (fuse) {
             if (c.t_tens == 1) F = F - tension_face(c, 1, i, j, k);
             F = F + AT(c.tf_v, i, j, k);
+            if (c.m_turb >= 2) F = F - ka_face(c, 1, i, j, k);
         }
         AT(c.Fv, i, j, k) = F;
     }
@@ -245,6 +287,7 @@ __global__ void __launch_bounds__(NTHREADS) k_convdiff(const CaseDev<T> *__restr
             F = F - T(c.gz);
             if (c.t_tens == 1) F = F - tension_face(c, 2, i, j, k);
             F = F + AT(c.tf_w, i, j, k);
+            if (c.m_turb >= 2) F = F - ka_face(c, 2, i, j, k);
         }
         AT(c.Fw, i, j, k) = F;
     }
@@ -258,18 +301,30 @@ __global__ void __launch_bounds__(NTHREADS) k_complementos(const CaseDev<T> *__r
     tile_ijk(c, i, j, k);
     const Geo &g = c.g;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
-    if (c.t_tens == 1) {     // the surface-tension term sits between gravity and the MMS source
-        if (i <= nx + 1 && j <= ny && k <= nz)
-            AT(c.Fu, i, j, k) = AT(c.Fu, i, j, k) + T(c.gx) - tension_face(c, 0, i, j, k) + AT(c.tf_u, i, j, k);
-        if (i <= nx && j <= ny + 1 && k <= nz)
-            AT(c.Fv, i, j, k) = AT(c.Fv, i, j, k) - tension_face(c, 1, i, j, k) + AT(c.tf_v, i, j, k);
-        if (i <= nx && j <= ny && k <= nz + 1)
-            AT(c.Fw, i, j, k) = AT(c.Fw, i, j, k) - T(c.gz) - tension_face(c, 2, i, j, k) + AT(c.tf_w, i, j, k);
-        return;
+    // the surface-tension term sits between gravity and the MMS source, the
+    // kinetic-energy term (m_turb >= 2) comes last
+    const bool ten = (c.t_tens == 1), kt = (c.m_turb >= 2);
+    if (i <= nx + 1 && j <= ny && k <= nz) {
+        T F = AT(c.Fu, i, j, k) + T(c.gx);
+        if (ten) F = F - tension_face(c, 0, i, j, k);
+        F = F + AT(c.tf_u, i, j, k);
+        if (kt) F = F - ka_face(c, 0, i, j, k);
+        AT(c.Fu, i, j, k) = F;
     }
-    if (i <= nx + 1 && j <= ny && k <= nz) AT(c.Fu, i, j, k) = AT(c.Fu, i, j, k) + T(c.gx) + AT(c.tf_u, i, j, k);
-    if (i <= nx && j <= ny + 1 && k <= nz) AT(c.Fv, i, j, k) = AT(c.Fv, i, j, k) + AT(c.tf_v, i, j, k);
-    if (i <= nx && j <= ny && k <= nz + 1) AT(c.Fw, i, j, k) = AT(c.Fw, i, j, k) - T(c.gz) + AT(c.tf_w, i, j, k);
+    if (i <= nx && j <= ny + 1 && k <= nz) {
+        T F = AT(c.Fv, i, j, k);
+        if (ten) F = F - tension_face(c, 1, i, j, k);
+        F = F + AT(c.tf_v, i, j, k);
+        if (kt) F = F - ka_face(c, 1, i, j, k);
+        AT(c.Fv, i, j, k) = F;
+    }
+    if (i <= nx && j <= ny && k <= nz + 1) {
+        T F = AT(c.Fw, i, j, k) - T(c.gz);
+        if (ten) F = F - tension_face(c, 2, i, j, k);
+        F = F + AT(c.tf_w, i, j, k);
+        if (kt) F = F - ka_face(c, 2, i, j, k);
+        AT(c.Fw, i, j, k) = F;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -355,6 +410,11 @@ __global__ void __launch_bounds__(NTHREADS) k_tempo(const CaseDev<T> *__restrict
     const Geo &g = c.g;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     long long q = g.at(i, j, k);
+    if (c.ipa) {   // the IPA's explicit pressure force first (:21-45), kept in F as upstream
+        if (i <= nx + 1 && j <= ny && k <= nz) c.Fu[q] = c.Fu[q] + c.px[q];
+        if (i <= nx && j <= ny + 1 && k <= nz) c.Fv[q] = c.Fv[q] + c.py[q];
+        if (i <= nx && j <= ny && k <= nz + 1) c.Fw[q] = c.Fw[q] + c.pz[q];
+    }
     if (c.u64 != nullptr) {
         const double dt = c.sc[S_DT];
         if (i <= nx + 1 && j <= ny && k <= nz) tempo_one_m<T>(c, tt, it, dt, q, c.u, c.u64, c.Fu, c.u0, c.u064, c.fu0, c.fu1);
@@ -567,9 +627,10 @@ __global__ void k_set_scalar(const CaseDev<T> *__restrict__ cs, int ncases, int 
 }
 
 // ---- launchers -------------------------------------------------------------
-template <typename T> void launch_visco(const Batch<T> &b, cudaStream_t s)
+template <typename T> void launch_visco(const Batch<T> &b, int keq_stages, const double *a_dt, cudaStream_t s)
 {
     k_visco_mu<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
+    if (keq_stages > 0) launch_keq<T>(b, keq_stages, a_dt, s);   // m_turb >= 2 cases
     k_visco_faces<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
 }
 template <typename T> void launch_convdiff(const Batch<T> &b, int fuse, cudaStream_t s)
@@ -608,7 +669,7 @@ template <typename T> void launch_set_scalar(const Batch<T> &b, int slot, double
 }
 
 #define INST(T)                                                              \
-    template void launch_visco<T>(const Batch<T> &, cudaStream_t);          \
+    template void launch_visco<T>(const Batch<T> &, int, const double *, cudaStream_t); \
     template void launch_convdiff<T>(const Batch<T> &, int, cudaStream_t);  \
     template void launch_complementos<T>(const Batch<T> &, cudaStream_t);   \
     template void launch_tempo<T>(const Batch<T> &, int, int, cudaStream_t);          \

@@ -1,9 +1,9 @@
 // k_output.cu -- the field record of PRTSCR (4_plot.f90:501-635) formed on
 // the device: velocities averaged to the cell corners, the level set, the
 // obstacle's corner level set, and with t_plot = 1 the pressure relative to
-// the cell (nx, 1, nz) and the vorticity (prd0 = 0: it changes only with the
-// IPA pressure option; nut and ka belong to the k-equation model and are
-// zeros).  Values are formed in FP64 (from the FP64 masters in the mixed form)
+// the cell (nx, 1, nz) (prd0 + prd1; prd0 exists with the IPA only), the
+// vorticity, nut and ka (zeros without the k equation, as upstream, where
+// visco sets ka = 0 and never assigns nut).  Values are formed in FP64 (from the FP64 masters in the mixed form)
 // and rounded once to float32, as real(x, 4) does.  The node coordinates are
 // written by the host.
 #include "suli_kernels.cuh"
@@ -27,7 +27,8 @@ __global__ void k_prtscr(const CaseDev<T> *__restrict__ cs, int icase, float *__
     auto W = [&](long long q) { return mixed ? c.w64[q] : (double)c.w[q]; };
     float *ua = out, *va = out + n1, *wa = out + 2 * n1, *lso = out + 3 * n1, *obs = lso + nc;
     float *pr = obs + n1, *vi = pr + nc, *vj = vi + nc, *vk = vj + nc, *nut = vk + nc, *ka = nut + nc;
-    const double pref = (double)c.prd1[g.at(nx, 1, nz)];
+    const long long qref = g.at(nx, 1, nz);
+    const double pref = c.prd0 ? (double)c.prd0[qref] + (double)c.prd1[qref] : (double)c.prd1[qref];
     const long long n = n1 > nc ? n1 : nc;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
         if (t < n1) {       // corner (i, j, k), 1..nx1 x 1..ny1 x 1..nz1 (4_plot.f90:556-566)
@@ -47,15 +48,15 @@ __global__ void k_prtscr(const CaseDev<T> *__restrict__ cs, int icase, float *__
             const long long q = g.at(i, j, k);
             lso[t] = (float)(mixed ? c.ls64[q] : (double)c.ls[q]);
             if (t_plot) {
-                pr[t] = (float)((double)c.prd1[q] - pref);
+                pr[t] = (float)((c.prd0 ? (double)c.prd0[q] + (double)c.prd1[q] : (double)c.prd1[q]) - pref);
                 const double dudy = (U(q + sx) - U(q)) * c.idy, dudz = (U(q + sxy) - U(q)) * c.idz;
                 const double dvdx = (V(q + 1) - V(q)) * c.idx, dvdz = (V(q + sxy) - V(q)) * c.idz;
                 const double dwdx = (W(q + 1) - W(q)) * c.idx, dwdy = (W(q + sx) - W(q)) * c.idy;
                 vi[t] = (float)(dwdy - dvdz);
                 vj[t] = (float)(dudz - dwdx);
                 vk[t] = (float)(dvdx - dudy);
-                nut[t] = 0.0f;
-                ka[t] = 0.0f;
+                nut[t] = c.nut ? (float)c.nut[q] : 0.0f;
+                ka[t] = c.ka ? (float)c.ka[q] : 0.0f;
             }
         }
     }

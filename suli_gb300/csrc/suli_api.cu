@@ -69,6 +69,9 @@ extern "C" void suli_default_params(suli_params *p)
     p->vol_loop_max = 1000;
     p->mixed_precond = 1;
     p->t_tens = 0;
+    p->cmu = 0.05;
+    p->cdes = 0.65;
+    p->lcar = 0.05715;
     p->sigma = 0.0728;
 }
 
@@ -83,19 +86,20 @@ extern "C" int suli_field_shape(const suli_params *p, int f, int lo[3], int hi[3
     case SULI_F_U: set(0, nx1 + 1, 0, ny + 1, 0, nz + 1); break;
     case SULI_F_V: set(0, nx + 1, 0, ny1 + 1, 0, nz + 1); break;
     case SULI_F_W: set(0, nx + 1, 0, ny + 1, 0, nz1 + 1); break;
-    case SULI_F_PRD1: case SULI_F_PRD: set(0, nx + 1, 0, ny + 1, 0, nz + 1); break;
+    case SULI_F_PRD1: case SULI_F_PRD: case SULI_F_KA: case SULI_F_PRD0:
+        set(0, nx + 1, 0, ny + 1, 0, nz + 1); break;
     case SULI_F_LS: case SULI_F_HS: case SULI_F_RHO: case SULI_F_LS_MU: case SULI_F_MU: case SULI_F_MUT:
     case SULI_F_DIV: case SULI_F_OBS_LSS: case SULI_F_ID_IBM:
-    case SULI_F_HSX: case SULI_F_HSY: case SULI_F_HSZ: case SULI_F_KURV:
+    case SULI_F_HSX: case SULI_F_HSY: case SULI_F_HSZ: case SULI_F_KURV: case SULI_F_NUT:
         set(1, nx, 1, ny, 1, nz); break;
     case SULI_F_XMU: case SULI_F_FU: case SULI_F_U0: case SULI_F_FU0: case SULI_F_FU1: case SULI_F_TF_U:
-    case SULI_F_OBS_LSX: case SULI_F_ID_IBMX:
+    case SULI_F_OBS_LSX: case SULI_F_ID_IBMX: case SULI_F_PX:
         set(1, nx1, 1, ny, 1, nz); break;
     case SULI_F_YMU: case SULI_F_FV: case SULI_F_V0: case SULI_F_FV0: case SULI_F_FV1: case SULI_F_TF_V:
-    case SULI_F_OBS_LSY: case SULI_F_ID_IBMY:
+    case SULI_F_OBS_LSY: case SULI_F_ID_IBMY: case SULI_F_PY:
         set(1, nx, 1, ny1, 1, nz); break;
     case SULI_F_ZMU: case SULI_F_FW: case SULI_F_W0: case SULI_F_FW0: case SULI_F_FW1: case SULI_F_TF_W:
-    case SULI_F_OBS_LSZ: case SULI_F_ID_IBMZ:
+    case SULI_F_OBS_LSZ: case SULI_F_ID_IBMZ: case SULI_F_PZ:
         set(1, nx, 1, ny, 1, nz1); break;
     case SULI_F_BXX0: case SULI_F_BXX1: set(0, ny + 1, 0, nz + 1, 0, 0); break;
     case SULI_F_BLX1: set(1, ny, 1, nz, 0, 0); break;
@@ -118,8 +122,10 @@ static int validate(const suli_params &p)
     if (!(p.dx > 0 && p.dy > 0 && p.dz > 0 && p.dt > 0)) return bad("dx, dy, dz, dt must be > 0");
     if (p.der != 3) return bad("only der = 3 (2nd-order upwind) is supported");
     if (p.adv_type != 1) return bad("only adv_type = 1 (classical advection) is supported");
-    if (p.t_press != 1) return bad("only t_press = 1 (projection) is supported");
-    if (p.m_turb != 0 && p.m_turb != 1) return bad("m_turb must be 0 or 1");
+    if (p.t_press != 1 && p.t_press != 2)
+        return bad("t_press must be 1 (projection) or 2 (IPA); the hydrostatic t_press = 0 is not supported");
+    if (p.m_turb < 0 || p.m_turb > 3) return bad("m_turb must be 0..3");
+    if (p.m_turb >= 2 && !(p.lcar > 0 && p.cmu >= 0 && p.cdes > 0)) return bad("m_turb >= 2 needs lcar > 0, cmu >= 0, cdes > 0");
     if (p.mms_t != 0 && p.mms_t != 1) return bad("mms_t must be 0 or 1");
     if (p.ibm_t != 0 && p.ibm_t != 2) return bad("ibm_t must be 0 or 2 (image-point IBM)");
     if (p.ibm_t == 2 && p.obst_t == 0) return bad("ibm_t = 2 needs an obstacle (obst_t != 0, obstacle fields uploaded)");
@@ -162,6 +168,9 @@ struct ImplBase {
     virtual int time_kernel(int kernel, int reps, double *ms, double *bytes) = 0;
     virtual int write_fields(int icase, const char *path, int t_plot) = 0;
     virtual int ibm_setup() = 0;
+    virtual int exp_press() = 0;
+    virtual int contorno_les() = 0;
+    virtual bool stored(int icase, int f) = 0;
     unsigned long long inflow_calls = 0;
     int ncases = 0;
     std::vector<suli_params> P;
@@ -405,6 +414,9 @@ struct Impl : ImplBase {
             cd.ccx0 = q.ccx0; cd.ccxf = q.ccxf; cd.ccy0 = q.ccy0; cd.ccyf = q.ccyf; cd.ccz0 = q.ccz0; cd.cczf = q.cczf;
             cd.t_tempo = q.t_tempo; cd.m_turb = q.m_turb; cd.mms_t = q.mms_t; cd.ibm_t = q.ibm_t; cd.obst_t = q.obst_t;
             cd.t_tens = q.t_tens; cd.sigma = q.sigma;
+            cd.cmu = q.cmu; cd.cdes = q.cdes; cd.lcar = q.lcar; cd.delta = cd.dx1;
+            cd.t_press = q.t_press;
+            cd.ipa = (q.t_press == 2 && (q.mms_t == 0 || q.project_under_mms)) ? 1 : 0;
             cd.reinit_max = q.reinit_max_iter; cd.cg_max = q.cg_max_iter; cd.cg_tol_mode = q.cg_tol_mode;
             cd.cg_tol = q.cg_tol;
             // one slab per case: every field of the case in the common box layout
@@ -423,7 +435,11 @@ struct Impl : ImplBase {
             T **ptf[] = {&cd.bxx0, &cd.bxx1, &cd.blx1};
             const bool mixed = (sizeof(T) == 4);
             const bool mg = mixed && q.mixed_precond == 1;
-            size_t bytes = fb * ntf + ib * 4 + pb * 3 + (mixed ? 20 * db : 0) + (mg ? 8 * fb : 0);
+            // k equation (m_turb >= 2) and IPA (t_press = 2) arrays only where used
+            T **kf[] = {&cd.ka, &cd.nut, &cd.sij, &cd.ka0, &cd.fk0, &cd.fk1, &cd.fka};
+            T **af[] = {&cd.prd0, &cd.px, &cd.py, &cd.pz};
+            const int nkf = (q.m_turb >= 2) ? 7 : 0, naf = (q.t_press == 2) ? 4 : 0;
+            size_t bytes = fb * (ntf + nkf + naf) + ib * 4 + pb * 3 + (mixed ? 20 * db : 0) + (mg ? 8 * fb : 0);
             void *slab = nullptr;
             CK(cudaMalloc(&slab, bytes));
             slabs.push_back(slab);
@@ -432,6 +448,8 @@ struct Impl : ImplBase {
             for (int f = 0; f < ntf; ++f) { *tf[f] = (T *)cur; cur += fb; }
             for (int f = 0; f < 4; ++f) { *itf[f] = (int *)cur; cur += ib; }
             for (int f = 0; f < 3; ++f) { *ptf[f] = (T *)cur; cur += pb; }
+            for (int f = 0; f < nkf; ++f) { *kf[f] = (T *)cur; cur += fb; }
+            for (int f = 0; f < naf; ++f) { *af[f] = (T *)cur; cur += fb; }
             if (mixed) {
                 double **d64[] = {&cd.e64, &cd.r64, &cd.rho64, &cd.spi64, &cd.spj64, &cd.spk64, &cd.dpr64, &cd.qpr64,
                                   &cd.u64, &cd.v64, &cd.w64, &cd.u064, &cd.v064, &cd.w064,
@@ -700,6 +718,12 @@ struct Impl : ImplBase {
         case SULI_F_HSY: return c.hsy;
         case SULI_F_HSZ: return c.hsz;
         case SULI_F_KURV: return c.kurv;
+        case SULI_F_KA: return c.ka;
+        case SULI_F_NUT: return c.nut;
+        case SULI_F_PRD0: return c.prd0;
+        case SULI_F_PX: return c.px;
+        case SULI_F_PY: return c.py;
+        case SULI_F_PZ: return c.pz;
         case SULI_F_ID_IBMX: return c.id_ibmx;
         case SULI_F_ID_IBMY: return c.id_ibmy;
         case SULI_F_ID_IBMZ: return c.id_ibmz;
@@ -915,12 +939,33 @@ struct Impl : ImplBase {
         return sync();
     }
 
+    bool any_keq() const
+    {
+        for (const auto &q : P) if (q.m_turb >= 2) return true;
+        return false;
+    }
+    bool ipa() const { return P[0].t_press == 2 && (P[0].mms_t == 0 || P[0].project_under_mms); }
+
     int visco() override
     {
-        launch_visco<T>(b, st);
+        launch_visco<T>(b, any_keq() ? ntt : 0, a_dt, st);
         CKL();
         return SULI_OK;
     }
+    int exp_press() override
+    {
+        if (P[0].t_press != 2) return fail(SULI_BAD_CONFIG, "exp_press belongs to the IPA (t_press = 2)");
+        launch_exp_press<T>(b, st);
+        CKL();
+        return SULI_OK;
+    }
+    int contorno_les() override
+    {
+        launch_contorno_les<T>(b, st);
+        CKL();
+        return SULI_OK;
+    }
+    bool stored(int icase, int f) override { return dev_ptr(icase, f) != nullptr; }
     int convdiff(int fuse) override
     {
         launch_convdiff<T>(b, fuse, st);
@@ -1090,6 +1135,8 @@ struct Impl : ImplBase {
 
     int posdin() override
     {
+        if (P[0].t_press != 1)
+            return fail(SULI_BAD_CONFIG, "posdin projects for t_press = 1 only (the IPA step has no posdin)");
         launch_posdin<T>(b, st);
         CKL();
         for (int c = 0; c < ncases; ++c)
@@ -1128,6 +1175,7 @@ struct Impl : ImplBase {
             t = t + dt;
             if ((rc = level_set())) return rc;
             if ((rc = contorno(3))) return rc;
+            if (ipa() && (rc = exp_press())) return rc;          // 1_principal.f90:82
             if ((rc = visco())) return rc;
             for (int q = 1; q <= ntt; ++q) {
                 if ((rc = set_stage(q))) return rc;
@@ -1135,11 +1183,17 @@ struct Impl : ImplBase {
                 if ((rc = tempo())) return rc;
                 if ((rc = contorno(2))) return rc;
                 if (P[0].mms_t == 0 || P[0].project_under_mms) {
-                    rc = graddin(nullptr);
-                    if (rc && rc != SULI_CG_MAXITER) return rc;
-                    if ((rc = posdin())) return rc;
+                    if (P[0].t_press == 1) {
+                        rc = graddin(nullptr);
+                        if (rc && rc != SULI_CG_MAXITER) return rc;
+                        if ((rc = posdin())) return rc;
+                    }
                     if ((rc = contorno(1))) return rc;
                 }
+            }
+            if (ipa()) {                                          // :111, no posdin
+                rc = graddin(nullptr);
+                if (rc && rc != SULI_CG_MAXITER) return rc;
             }
             if ((rc = conmassa(nullptr))) return rc;
         }
@@ -1166,8 +1220,8 @@ extern "C" int suli_create_batch(const suli_params *p, int ncases, suli_handle *
         if (rc) return rc;
         if (p[c].precision != p[0].precision || p[c].t_tempo != p[0].t_tempo || p[c].mms_t != p[0].mms_t ||
             p[c].dt != p[0].dt || p[c].reinit_max_iter != p[0].reinit_max_iter ||
-            p[c].project_under_mms != p[0].project_under_mms)
-            return fail(SULI_BAD_CONFIG, "cases of a batch must share precision, t_tempo, mms_t, dt and reinit_max_iter");
+            p[c].project_under_mms != p[0].project_under_mms || p[c].t_press != p[0].t_press)
+            return fail(SULI_BAD_CONFIG, "cases of a batch must share precision, t_tempo, mms_t, t_press, dt and reinit_max_iter");
     }
     int rc = check_device();
     if (rc) return rc;
@@ -1301,6 +1355,8 @@ extern "C" int suli_complementos(suli_handle *h) { HCHK(); return h->impl->compl
 extern "C" int suli_tempo(suli_handle *h) { HCHK(); return h->impl->tempo(); }
 extern "C" int suli_graddin(suli_handle *h, int32_t *iters) { HCHK(); return h->impl->graddin(iters); }
 extern "C" int suli_posdin(suli_handle *h) { HCHK(); return h->impl->posdin(); }
+extern "C" int suli_exp_press(suli_handle *h) { HCHK(); return h->impl->exp_press(); }
+extern "C" int suli_contorno_les(suli_handle *h) { HCHK(); return h->impl->contorno_les(); }
 extern "C" int suli_conmassa(suli_handle *h, double *m) { HCHK(); return h->impl->conmassa(m); }
 extern "C" int suli_mms_error(suli_handle *h, double err[4])
 {
@@ -1421,6 +1477,9 @@ static int restart_fields(ImplBase *im, int c, std::vector<std::vector<double>> 
     dv.resize(SULI_F_COUNT);
     iv.resize(SULI_F_COUNT);
     for (int f = 0; f < SULI_F_COUNT; ++f) {
+        // fields of a model the case does not run (k equation, IPA) are not
+        // stored: an empty record
+        if (!im->stored(c, f)) continue;
         const long long n = field_count(im->P[c], f);
         if (n < 0) return fail(SULI_BAD_ARG, "field shape");
         if (is_int_field(f)) {
@@ -1515,6 +1574,7 @@ extern "C" int suli_restart_load(suli_handle *h, const char *path)
             get(&id, 4); get(&n, 8);
             const int64_t want = is_int_field(f) ? (int64_t)iv[f].size() : (int64_t)dv[f].size();
             if (!ok || id != f || n != want) return bad("field " + std::to_string(f) + " of case " + std::to_string(c));
+            if (n == 0) continue;
             if (is_int_field(f)) { get(iv[f].data(), (size_t)n * 4); hosts.push_back(iv[f].data()); }
             else { get(dv[f].data(), (size_t)n * 8); hosts.push_back(dv[f].data()); }
             cases.push_back(c);

@@ -124,9 +124,11 @@ struct CaseDev {
     double cles;         // (dx*dy*dz)^(2/3) * csmag * csmag
     double pi;
     double uinicial, iturb;
+    double cmu, cdes, lcar, delta;   // k equation (m_turb >= 2); delta = max(dx, dy, dz)
     unsigned long long seed;
     int ccx0, ccxf, ccy0, ccyf, ccz0, cczf;
     int t_tempo, m_turb, mms_t, ibm_t, obst_t, t_tens;
+    int t_press, ipa;           // ipa: t_press = 2 and the step projects (exp_press / IPA graddin)
     int reinit_max, cg_max, cg_tol_mode;
     double cg_tol;
     // fields (reference module arrays)
@@ -138,6 +140,12 @@ struct CaseDev {
     T *obs_ls;                  // obstacle level set at the cell corners (field output only)
     T *hsx, *hsy, *hsz, *kurv;  // surface tension (t_tens = 1): weights, curvature
     T *nlx, *nly, *nlz;         // surface tension: the interface normal (curvature input)
+    // k equation (m_turb >= 2, else null): ka with its ghosts, nut, the strain
+    // sum p1 + p2 + p3 of visco, and the sub-stage buffers of tempo_esc (e0,
+    // fe0, fe1) and of the stage's right-hand side
+    T *ka, *nut, *sij, *ka0, *fk0, *fk1, *fka;
+    // IPA (t_press = 2, else null): accumulated pressure and the explicit force
+    T *prd0, *px, *py, *pz;
     int *id_ibmx, *id_ibmy, *id_ibmz, *id_ibm;
     T *bxx0, *bxx1, *blx1;      // inflow planes, indexed at(0, j, k)
     // CG work arrays

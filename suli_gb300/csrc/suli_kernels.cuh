@@ -49,7 +49,13 @@ template <typename T> void launch_curvature(const Batch<T> &b, cudaStream_t s);
 template <typename T> void launch_volcorr(const Batch<T> &b, cudaStream_t s);
 
 // momentum (k_momentum.cu)
-template <typename T> void launch_visco(const Batch<T> &b, cudaStream_t s);
+// visco; keq_stages > 0 runs the k equation's sub-stages (a_dt[0..]) for the
+// m_turb >= 2 cases between the strain and the face viscosities
+template <typename T> void launch_visco(const Batch<T> &b, int keq_stages, const double *a_dt, cudaStream_t s);
+// k equation and IPA (k_keq.cu)
+template <typename T> void launch_keq(const Batch<T> &b, int ntt, const double *a_dt, cudaStream_t s);
+template <typename T> void launch_contorno_les(const Batch<T> &b, cudaStream_t s);
+template <typename T> void launch_exp_press(const Batch<T> &b, cudaStream_t s);
 template <typename T> void launch_convdiff(const Batch<T> &b, int fuse_compl, cudaStream_t s);
 template <typename T> void launch_complementos(const Batch<T> &b, cudaStream_t s);
 template <typename T> void launch_tempo(const Batch<T> &b, int tt, int it, cudaStream_t s);

@@ -30,6 +30,7 @@ EXPORTS = [
     "suli_last_error", "suli_device_info", "suli_get_stream", "suli_profile", "suli_profile_read",
     "suli_ibm_setup", "suli_conmassa_noalloc", "suli_time_kernel", "suli_upload_fields",
     "suli_download_fields", "suli_write_fields", "suli_restart_save", "suli_restart_load",
+    "suli_exp_press", "suli_contorno_les",
 ]
 
 
@@ -69,7 +70,8 @@ def load_library(path: str = LIB_PATH):
     L.suli_get_scalar.argtypes = [C.c_void_p, C.c_int, C.c_int, P(C.c_double)]
     L.suli_set_replay.argtypes = [C.c_void_p, P(i32), i32]
     for name in ("suli_heaviside_init", "suli_ibm_setup", "suli_level_set", "suli_visco", "suli_convdiff",
-                 "suli_complementos", "suli_tempo", "suli_posdin", "suli_synchronize"):
+                 "suli_complementos", "suli_tempo", "suli_posdin", "suli_synchronize", "suli_exp_press",
+                 "suli_contorno_les"):
         getattr(L, name).argtypes = [C.c_void_p]
     L.suli_contorno.argtypes = [C.c_void_p, C.c_int]
     L.suli_graddin.argtypes = [C.c_void_p, P(i32)]
@@ -241,6 +243,14 @@ class SuliGPU:
     def posdin(self):
         _check(load_library().suli_posdin(self._h))
 
+    def exp_press(self):
+        """exp_press (11_diversos.f90:455-495), t_press = 2."""
+        _check(load_library().suli_exp_press(self._h))
+
+    def contorno_les(self):
+        """contorno_les (3_contorno.f90:666-790) on the m_turb >= 2 cases."""
+        _check(load_library().suli_contorno_les(self._h))
+
     def conmassa(self) -> float:
         m = C.c_double()
         _check(load_library().suli_conmassa(self._h, C.byref(m)))
@@ -302,12 +312,16 @@ class SuliGPU:
     # ---- set-up ------------------------------------------------------------
     def start(self, fields_per_case):
         """Upload initial fields and run the start-up of 1_principal.f90:50-53:
-        heaviside + vol_ini, then contorno(1), (2), (3)."""
+        heaviside + vol_ini, then contorno(1), (2), (3); with the k equation
+        (m_turb >= 2) first the ghost values of ka, as iniciais does
+        (2_iniciais.f90:216-235)."""
         if isinstance(fields_per_case, dict):
             fields_per_case = [fields_per_case]
         for c, fields in enumerate(fields_per_case):
             for name, arr in fields.items():
                 self.upload(name, arr, case=c)
+        if any(p.m_turb >= 2 for p in self.params):
+            self.contorno_les()
         self.heaviside_init()
         if any(p.ibm_t == 2 for p in self.params):
             self.ibm_setup()          # obstaculo(): reinit obstacle level sets, image masks

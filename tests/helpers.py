@@ -23,6 +23,8 @@ def oracle_for(case, warm_steps=0):
         o.set_field(k, v)
     if case.params.mms_t:
         o.termo_fonte1()
+    if case.params.m_turb >= 2:
+        o.contorno_les()             # iniciais, 2_iniciais.f90:216-235
     o.heaviside_init()
     if case.params.ibm_t == 2:
         ob = case.obstacle
@@ -35,8 +37,23 @@ def oracle_for(case, warm_steps=0):
     return o
 
 
+KEQ_FIELDS = ["KA", "NUT"]
+IPA_FIELDS = ["PRD0", "PX", "PY", "PZ"]
+
+
+def model_fields(p):
+    """The fields of the k equation / the IPA, stored for those cases only."""
+    return (KEQ_FIELDS if p.m_turb >= 2 else []) + (IPA_FIELDS if p.t_press == 2 else [])
+
+
+def model_compare(p):
+    """The same fields as compare() names: the IPA force as one vector (its
+    y component is round-off in a y-uniform flow)."""
+    return (KEQ_FIELDS if p.m_turb >= 2 else []) + (["PRD0", "pforce"] if p.t_press == 2 else [])
+
+
 def copy_state(o, g, case=0):
-    for name in STATE_FIELDS:
+    for name in STATE_FIELDS + model_fields(g.params[case]):
         g.upload(name, o.field(name), case=case)
     g.set_scalar("VOL_INI", o.scalar("VOL_INI"), case=case)
     g.set_scalar("VOL_INS", o.scalar("VOL_INS"), case=case)
@@ -45,7 +62,8 @@ def copy_state(o, g, case=0):
     g.set_scalar("RNG", o.scalar("RNG"))
 
 
-VECTORS = {"velocity": ("U", "V", "W"), "F": ("FU", "FV", "FW"), "visc": ("XMU", "YMU", "ZMU")}
+VECTORS = {"velocity": ("U", "V", "W"), "F": ("FU", "FV", "FW"), "visc": ("XMU", "YMU", "ZMU"),
+           "pforce": ("PX", "PY", "PZ")}
 
 
 def compare(o, g, names, tol, case=0):

@@ -3,7 +3,7 @@ restart_ini, 11_diversos.f90:500-599) through the C ABI on the GPU."""
 import numpy as np
 import pytest
 
-from helpers import copy_state, oracle_for
+from helpers import copy_state, model_fields, oracle_for
 from suli_gb300 import cases
 from suli_gb300._abi import PREC_FP64, PREC_MIXED, SULI_BAD_CONFIG
 from test_output import read_fortran_record, split_record
@@ -14,12 +14,16 @@ pytestmark = pytest.mark.gpu
 def _case(kind, precision):
     if kind == "dam_break":
         return cases.dam_break(24, 12, 10, precision=precision)
+    if kind == "k_les":      # nut and ka in the record
+        return cases.k_channel(24, 6, 12, m_turb=2, precision=precision)
+    if kind == "ipa":        # prd0 + prd1 in the record
+        return cases.ipa_tank(16, 6, 12, precision=precision)
     return cases.open_channel(32, 12, 12, dt=2e-3, radius=0.25, periodic=True, precision=precision)
 
 
 @pytest.mark.parametrize("t_plot", [0, 1])
 @pytest.mark.parametrize("precision", [PREC_FP64, PREC_MIXED], ids=["fp64", "mixed"])
-@pytest.mark.parametrize("kind", ["dam_break", "channel_ibm"])
+@pytest.mark.parametrize("kind", ["dam_break", "channel_ibm", "k_les", "ipa"])
 def test_write_fields_matches_oracle(gpu_lib, tmp_path, kind, precision, t_plot):
     """The device-formed record equals the oracle's for the same state: same
     framing and sizes, the same float32 values up to one rounding of values
@@ -44,7 +48,7 @@ def test_write_fields_matches_oracle(gpu_lib, tmp_path, kind, precision, t_plot)
 
 
 @pytest.mark.parametrize("precision", [PREC_FP64, PREC_MIXED], ids=["fp64", "mixed"])
-@pytest.mark.parametrize("kind", ["dam_break", "batch"])
+@pytest.mark.parametrize("kind", ["dam_break", "batch", "k_les", "ipa"])
 def test_restart_continues_exactly(gpu_lib, tmp_path, kind, precision):
     """N steps, save, a new handle with the same parameters loads the file and
     runs M steps: the fields, t and it equal those of N + M uninterrupted
@@ -52,11 +56,13 @@ def test_restart_continues_exactly(gpu_lib, tmp_path, kind, precision):
     def mk():
         if kind == "dam_break":
             return [cases.dam_break(24, 12, 12, precision=precision)]
+        if kind in ("k_les", "ipa"):
+            return [_case(kind, precision)]
         dims, hcol, amp = cases.ensemble_dims(2, seed=9, lo=14, hi=24)
         return [cases.ensemble_case(i, dims, hcol, amp, precision=precision) for i in range(2)]
 
-    names = ("U", "V", "W", "PRD1", "LS", "HS", "RHO")
     cs = mk()
+    names = ["U", "V", "W", "PRD1", "LS", "HS", "RHO"] + model_fields(cs[0].params)
     ga = gpu_lib.SuliGPU([c.params for c in cs])
     ga.start([c.fields for c in cs])
     ga.step(4)

@@ -9,7 +9,7 @@ that both sides take the same control path.  Bar: relative L2 <= 1e-10.
 import numpy as np
 import pytest
 
-from helpers import compare, copy_state, oracle_for, rel_l2
+from helpers import compare, copy_state, model_compare, oracle_for, rel_l2
 from suli_gb300 import cases
 
 pytestmark = pytest.mark.gpu
@@ -29,6 +29,11 @@ def _configs():
         ("inflow_ibm", cases.open_channel(48, 16, 16, dt=2e-3, radius=0.25, cg_tol=1e-10)),
         # surface tension (t_tens = 1): weights, curvature, the momentum term
         ("capillary", cases.capillary_column(32, 4, 0.25)),
+        # k equation: LES (m_turb = 2) and DES (m_turb = 3), no-slip bed
+        ("k_les", cases.k_channel(24, 6, 12, m_turb=2)),
+        ("k_des", cases.k_channel(24, 6, 12, m_turb=3)),
+        # implicit pressure algorithm (t_press = 2)
+        ("ipa", cases.ipa_tank(16, 6, 12)),
     ]
 
 
@@ -91,6 +96,36 @@ def test_visco(pair):
     compare(o, g, ["MU", "visc"], TOL)
     if case.params.m_turb:
         compare(o, g, ["MUT"], TOL)
+    if case.params.m_turb >= 2:
+        compare(o, g, ["KA", "NUT"], TOL)
+        assert g.download("KA").max() > 0
+
+
+def test_contorno_les(pair):
+    """The ghost fills of ka: exact copies (negated for no-slip), edges in the
+    reference's plane order."""
+    case, o, g = pair
+    if case.params.m_turb < 2:
+        pytest.skip("no k equation")
+    _sync(o, g)
+    rng = np.random.default_rng(5)
+    ka = rng.random(o.field("KA").shape)
+    o.set_field("KA", np.asfortranarray(ka))
+    g.upload("KA", np.asfortranarray(ka))
+    o.contorno_les()
+    g.contorno_les()
+    assert np.array_equal(g.download("KA"), o.field("KA"))
+
+
+def test_exp_press(pair):
+    case, o, g = pair
+    if case.params.t_press != 2:
+        pytest.skip("no IPA")
+    _sync(o, g)
+    o.exp_press()
+    g.exp_press()
+    compare(o, g, ["PRD0", "pforce"], TOL)
+    assert np.abs(g.download("PZ")).max() > 0
 
 
 @pytest.mark.parametrize("tt", [1, 2, 3])
@@ -156,8 +191,9 @@ def test_graddin_posdin(pair):
         g.set_replay(None, -1)
         assert it_g == it_o
         compare(o, g, ["PRD1"], TOL)
-        o.posdin(); g.posdin()
-        compare(o, g, ["velocity", "PRD"], TOL)
+        if case.params.t_press == 1:   # the IPA step has no posdin
+            o.posdin(); g.posdin()
+            compare(o, g, ["velocity", "PRD"], TOL)
         o.contorno(1); g.contorno(1)
     m_o = o.conmassa()
     m_g = g.conmassa()
@@ -197,7 +233,7 @@ def test_steps_replayed(pair):
         g.set_replay(list(d.cg_iters), d.reinit_iters)
         g.step(1)
     g.set_replay(None, -1)
-    compare(o, g, ["velocity", "PRD1", "LS", "RHO"], TOL)
+    compare(o, g, ["velocity", "PRD1", "LS", "RHO"] + model_compare(case.params), TOL)
     # max|div| after the projection is the CG residual: same order, not same bits
     assert abs(g.diag().maxdiv - o.diag().maxdiv) <= 0.25 * o.diag().maxdiv + 1e-13
 

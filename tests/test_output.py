@@ -50,7 +50,7 @@ def expected(o, p, t_plot):
     arrs = [X, Y, Z, ua, va, wa, o.field("LS"), obs]
     if t_plot:
         c = slice(1, nx + 1), slice(1, ny + 1), slice(1, nz + 1)
-        pr = o.field("PRD1")
+        pr = o.field("PRD0") + o.field("PRD1")          # prd0 = 0 unless the IPA ran (4_plot.f90:573)
         i, j, k = c
         ip, jp, kp = slice(2, nx + 2), slice(2, ny + 2), slice(2, nz + 2)
         dudy = (u[i, jp, k] - u[i, j, k]) / p.dy
@@ -59,16 +59,20 @@ def expected(o, p, t_plot):
         dvdz = (v[i, j, kp] - v[i, j, k]) / p.dz
         dwdx = (w[ip, j, k] - w[i, j, k]) / p.dx
         dwdy = (w[i, jp, k] - w[i, j, k]) / p.dy
-        zero = np.zeros((nx, ny, nz))
-        arrs += [pr[c] - pr[nx, 1, nz], dwdy - dvdz, dudz - dwdx, dvdx - dudy, zero, zero]
+        arrs += [pr[c] - pr[nx, 1, nz], dwdy - dvdz, dudz - dwdx, dvdx - dudy, o.field("NUT"),
+                 o.field("KA")[c]]
     return arrs
 
 
 @pytest.mark.parametrize("t_plot", [0, 1])
-@pytest.mark.parametrize("kind", ["dam_break", "channel_ibm"])
+@pytest.mark.parametrize("kind", ["dam_break", "channel_ibm", "k_les", "ipa"])
 def test_oracle_prtscr_record(tmp_path, kind, t_plot):
     if kind == "dam_break":
         case = cases.dam_break(12, 8, 6)
+    elif kind == "k_les":
+        case = cases.k_channel(16, 6, 10, m_turb=2)
+    elif kind == "ipa":
+        case = cases.ipa_tank(12, 6, 10)
     else:
         case = cases.open_channel(24, 8, 8, dt=2e-3, radius=0.25, periodic=True)
     o = oracle_for(case, warm_steps=1)
