@@ -18,7 +18,9 @@ the roofline entry is the dominant kernel timed alone over every case
 the FP64 form on the 64x32x32 dam break after 200 steps, "output" times
 the field records (PRTSCR) of 16 cases and a restart save + load outside
 the timed region, "surface_tension" the capillary column with and without
-t_tens, and cpu_baseline is the oracle (a port of the reference,
+t_tens, "models" the open channel under each visco model (none, Smagorinsky,
+k-equation LES, DES) and the still-water tank under the projection and the
+IPA, and cpu_baseline is the oracle (a port of the reference,
 OpenMP where the reference has it) on a bounded sample.
 
 --impl reference times the reference's CPU implementation (the oracle port:
@@ -329,6 +331,41 @@ def tension_run(torch, steps=10, warmup=3):
     return out
 
 
+def models_run(torch, steps=10, warmup=3):
+    """The k-equation model and the implicit pressure algorithm outside the
+    timed region, mixed form, cell-steps/s: the open channel (256 x 64 x 128)
+    with m_turb = 0 (none), 1 (Smagorinsky), 2 (k-equation LES), 3 (DES); the
+    tilted still-water tank (256 x 64 x 128) with t_press = 1 (projection,
+    three graddin + posdin per step) and 2 (IPA: exp_press, one graddin)."""
+    from suli_gb300 import cases
+    from suli_gb300._abi import PREC_MIXED
+    out = {"k_equation": {"workload": "k_channel_256x64x128", "steps": steps},
+           "ipa": {"workload": "ipa_tank_256x64x128", "steps": steps}}
+    for m in (0, 1, 2, 3):
+        c = cases.k_channel(256, 64, 128, m_turb=max(m, 2), precision=PREC_MIXED)
+        c.params.m_turb = m
+        if m < 2:
+            del c.fields["KA"]
+        g = start_gpu([c])
+        g.step(warmup)
+        ms = timed_steps(g, steps, torch)
+        g.close()
+        out["k_equation"]["m_turb_%d" % m] = {"value": c.cells * steps / (ms / 1e3), "ms_per_step": ms / steps}
+    for tp in (1, 2):
+        c = cases.ipa_tank(256, 64, 128, precision=PREC_MIXED)
+        c.params.t_press = tp
+        if tp == 1:
+            del c.fields["PRD0"]
+        g = start_gpu([c])
+        g.step(warmup)
+        ms = timed_steps(g, steps, torch)
+        d = g.diag()
+        g.close()
+        out["ipa"]["t_press_%d" % tp] = {"value": c.cells * steps / (ms / 1e3), "ms_per_step": ms / steps,
+                                         "cg_iters_last_step": list(d.cg_iters)}
+    return out
+
+
 def mms_run(args):
     """The manufactured solution (13_mms.f90, steady) at 32^3, 64^3, 128^3 in
     both forms, args.mms_steps steps each, outside any timed region: RMS
@@ -539,6 +576,10 @@ def main():
             line["surface_tension"] = tension_run(torch)
         except Exception as e:
             line["surface_tension"] = {"error": repr(e)}
+        try:
+            line["models"] = models_run(torch)
+        except Exception as e:
+            line["models"] = {"error": repr(e)}
     gm.close()
     if args.accuracy_steps > 0 and rank == 0:
         try:

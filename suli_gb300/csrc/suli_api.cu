@@ -186,6 +186,12 @@ struct ImplBase {
     // mixed form: the unit-dt FP64 pressure operator on the device matches
     // the current density (cleared by every call that may change it)
     bool op_valid = false;
+    // the density changed: the projection's operator follows it; the IPA's
+    // (t_press = 2, the constant density rho_f1) does not
+    void density_changed()
+    {
+        if (P[0].t_press != 2) op_valid = false;
+    }
     // measurement
     bool prof = false;
     unsigned long long launch0 = 0;
@@ -841,7 +847,7 @@ struct Impl : ImplBase {
     // ---- routines -------------------------------------------------------------
     int heaviside_init() override
     {
-        op_valid = false;
+        density_changed();
         launch_heaviside<T>(b, 1, st);
         CKL();
         return read_scalars();
@@ -849,7 +855,7 @@ struct Impl : ImplBase {
 
     int level_set() override
     {
-        op_valid = false;
+        density_changed();
         int rc;
         if ((rc = setsc(S_DTADV, dt))) return rc;
         if ((rc = setsc(S_RINREPLAY, (double)replay_reinit))) return rc;
@@ -904,7 +910,7 @@ struct Impl : ImplBase {
         if (nlock == 3) {
             // level-set IBM (3_contorno.f90:651-659); nothing without an obstacle
             if (!any_ibm()) return SULI_OK;
-            op_valid = false;
+            density_changed();
             int rc = setsc(S_RINREPLAY, -1.0);
             if (rc) return rc;
             launch_ibm_levelset<T>(b, st);
@@ -930,7 +936,7 @@ struct Impl : ImplBase {
 
     int ibm_setup() override
     {
-        op_valid = false;
+        density_changed();
         // obstaculo() for ibm_t = 2 (3_contorno.f90:991-1002): reinitialise the
         // four obstacle level sets, then mark the image points
         for (int t = 1; t <= 4; ++t) launch_reinit<T>(b, P[0].reinit_max_iter, st, t);
