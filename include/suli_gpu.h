@@ -102,6 +102,8 @@ typedef struct suli_params {
                                       constant (2_iniciais.f90:79-80) */
     double  lcar;                  /* k-equation dissipation length: the reference's max(prof, ampl)
                                       (5_viscosidade.f90:94) */
+    int32_t esp_type;              /* sponge layer over the last 1 m in x: 0 none, 1 graded with the
+                                      depth, 2 linear (3_contorno.f90:1011-1103) */
 } suli_params;
 
 /* ---- field ids (reference module arrays) -------------------------------- */

@@ -1179,6 +1179,51 @@ void or_convdiff(or_case *c)
 /* ------------------------------------------------------------------------ */
 /* 11_diversos.f90:355-450 -- complementos (t_tens=0, m_turb<2, no sponge)   */
 /* ------------------------------------------------------------------------ */
+/* sponge_layer, 3_contorno.f90:1011-1103: the permeability epis_z on the w
+ * faces (nx, ny, nz1) of the last l_sponge = 1 m of the domain.  esp_type 1
+ * grades it with the depth below the interface zpfs(i), which the reference
+ * takes from the last (j, k) of the column plane where ls changes sign; a
+ * plane without a sign change leaves zpfs unset upstream, here the domain
+ * height when the plane's first cell is water, else 0.  The start column
+ * nint(x_inicial / dx) + 1 is clamped to 1 for a domain shorter than 1 m
+ * (the reference would index below the array). */
+static void sponge_layer(const or_case *c, F3 *ep)
+{
+    const int nx = c->nx, ny = c->ny, nz = c->nz;
+    const double dx = c->dx, dz = c->dz;
+    memset(ep->p, 0, sizeof(double) * (size_t)f3_size(ep));
+    const double l_sponge = 1., x_inicial = nx * dx - l_sponge;
+    const double alfa = 60., alfa0 = 0., alfa1 = 30.;
+    int i0 = (int)lround(x_inicial / dx) + 1;
+    if (i0 < 1) i0 = 1;
+    for (int i = i0; i <= nx; ++i) {
+        const double zpt = dz * nz;
+        double zpfs = (A(c->ls, i, 1, 1) >= 0.) ? zpt : 0.;
+        if (c->p.esp_type == 1)
+            for (int j = 1; j <= ny; ++j)
+                for (int k = 1; k <= nz - 1; ++k)
+                    if (A(c->ls, i, j, k) * A(c->ls, i, j, k + 1) <= 0) {
+                        const double alt1 = dz * (k - 0.5) + A(c->ls, i, j, k);
+                        const double alt2 = dz * (k + 0.5) + A(c->ls, i, j, k + 1);
+                        zpfs = alt1 > alt2 ? alt1 : alt2;
+                    }
+        const double xp = (i - 0.5) * dx;
+        const double aux1 = (xp - x_inicial) / l_sponge;
+        for (int j = 1; j <= ny; ++j) {
+            double zx = -dz;
+            for (int k = 1; k <= nz; ++k) {
+                zx = zx + dz;
+                if (c->p.esp_type == 1) {
+                    if (A(c->ls, i, j, k) >= 0.) A(*ep, i, j, k) = alfa * aux1 * aux1 * (0. - zx) / (0. - zpfs);
+                    else A(*ep, i, j, k) = alfa * aux1 * aux1 * (zx - zpt) / (zpfs - zpt);
+                } else {
+                    A(*ep, i, j, k) = alfa0 + aux1 * (alfa1 - alfa0);
+                }
+            }
+        }
+    }
+}
+
 /* fantasmas_cf(rho) (8_derivadas.f90:625-671) at a point with at most one
  * index on a ghost layer: y and z ghosts copy the adjacent cell, x ghosts
  * wrap on a periodic x and copy otherwise */
@@ -1229,6 +1274,12 @@ void or_complementos(or_case *c)
 static void complementos_main(or_case *c)
 {
     int nx = c->nx, ny = c->ny, nz = c->nz, nx1 = c->nx1, ny1 = c->ny1, nz1 = c->nz1;
+    /* sponge layer (esp_type > 0, :380-386): epis_z on the w faces, zero
+     * without it (the term is then -(w) * 0, which changes no sum) */
+    F3 ep = tmp3(1, nx, 1, ny, 1, nz1);
+    const int sponge = c->p.esp_type > 0;
+    if (sponge) sponge_layer(c, &ep);
+#define SPONGE(i, j, k) (sponge ? A(ep, i, j, k) : 0.)
     /* gravity, surface tension (t_tens = 1: sigma times the face value of
      * hs_x kurv / rho, :383-390) and MMS source; the k-gradient term is an
      * exact zero for ka = 0, and so is the surface-tension term for
@@ -1254,8 +1305,9 @@ static void complementos_main(or_case *c)
         for (int k = 1; k <= nz1; ++k)
             for (int j = 1; j <= ny; ++j)
                 for (int i = 1; i <= nx; ++i)
-                    A(c->Fw, i, j, k) = A(c->Fw, i, j, k) - c->p.gz - sg * A(dz_, i, j, k) + A(c->tf_w, i, j, k);
-        fr(&aux); fr(&dx_); fr(&dy_); fr(&dz_);
+                    A(c->Fw, i, j, k) = A(c->Fw, i, j, k) - c->p.gz - (A(c->w, i, j, k) - 0.) * SPONGE(i, j, k) -
+                                        sg * A(dz_, i, j, k) + A(c->tf_w, i, j, k);
+        fr(&aux); fr(&dx_); fr(&dy_); fr(&dz_); fr(&ep);
         return;
     }
     for (int k = 1; k <= nz; ++k)
@@ -1269,7 +1321,10 @@ static void complementos_main(or_case *c)
     for (int k = 1; k <= nz1; ++k)
         for (int j = 1; j <= ny; ++j)
             for (int i = 1; i <= nx; ++i)
-                A(c->Fw, i, j, k) = A(c->Fw, i, j, k) - c->p.gz + A(c->tf_w, i, j, k);
+                A(c->Fw, i, j, k) = A(c->Fw, i, j, k) - c->p.gz - (A(c->w, i, j, k) - 0.) * SPONGE(i, j, k) +
+                                    A(c->tf_w, i, j, k);
+#undef SPONGE
+    fr(&ep);
 }
 
 /* ------------------------------------------------------------------------ */

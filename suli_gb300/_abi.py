@@ -55,6 +55,7 @@ class SuliParams(C.Structure):
         ("cmu", C.c_double),
         ("cdes", C.c_double),
         ("lcar", C.c_double),
+        ("esp_type", C.c_int32),
     ]
 
     def copy(self) -> "SuliParams":
@@ -106,6 +107,7 @@ def default_params(**kw) -> SuliParams:
     p.cmu = 0.05
     p.cdes = 0.65
     p.lcar = 0.05715
+    p.esp_type = 0
     p.mixed_precond = 1
     for k, v in kw.items():
         if not hasattr(p, k):

@@ -344,3 +344,22 @@ def ipa_tank(nx=24, ny=8, nz=16, precision=PREC_FP64, dt=1e-4) -> Case:
     f = _base_fields(p, ls)
     f["PRD0"] = _zeros(p, "PRD0")
     return Case("ipa_tank_%dx%dx%d" % (nx, ny, nz), p, f, steps=200)
+
+
+def sponge_tank(nx=32, ny=4, nz=16, esp_type=1, precision=PREC_FP64, dt=2e-4, cg_tol=1e-10) -> Case:
+    """Sloshing in a 2 x 0.25 x 1 m tank with a sponge layer over its last
+    metre (esp_type 1: graded with the depth below the interface, 2: linear;
+    3_contorno.f90:1011-1103): water 0.5 m deep under a cosine surface of
+    amplitude 0.05 m, free-slip walls."""
+    lx = 2.0
+    h = lx / nx
+    p = default_params(nx=nx, ny=ny, nz=nz, dx=h, dy=h, dz=1.0 / nz, dt=dt,
+                       ccx0=1, ccxf=1, ccy0=1, ccyf=1, ccz0=1, cczf=1,
+                       gz=9.80665, reinit_max_iter=3, cg_tol_mode=CG_TOL_REL, cg_tol=cg_tol,
+                       precision=precision)
+    p.esp_type = esp_type
+    x = _centres(nx, h)[:, None, None]
+    z = _centres(nz, p.dz)[None, None, :]
+    ls = np.empty((nx, ny, nz), order="F")
+    ls[...] = 0.5 + 0.05 * np.cos(math.pi * x / lx) - z
+    return Case("sponge_tank_%dx%dx%d" % (nx, ny, nz), p, _base_fields(p, ls), steps=200)

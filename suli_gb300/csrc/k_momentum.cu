@@ -285,6 +285,7 @@ __global__ void __launch_bounds__(NTHREADS) k_convdiff(const CaseDev<T> *__restr
                   rhoz;
         if (fuse) {
             F = F - T(c.gz);
+            if (c.epis) F = F - (wc - T(0.)) * AT(c.epis, i, j, k);
             if (c.t_tens == 1) F = F - tension_face(c, 2, i, j, k);
             F = F + AT(c.tf_w, i, j, k);
             if (c.m_turb >= 2) F = F - ka_face(c, 2, i, j, k);
@@ -320,10 +321,84 @@ __global__ void __launch_bounds__(NTHREADS) k_complementos(const CaseDev<T> *__r
     }
     if (i <= nx && j <= ny && k <= nz + 1) {
         T F = AT(c.Fw, i, j, k) - T(c.gz);
+        if (c.epis) F = F - (AT(c.w, i, j, k) - T(0.)) * AT(c.epis, i, j, k);
         if (ten) F = F - tension_face(c, 2, i, j, k);
         F = F + AT(c.tf_w, i, j, k);
         if (kt) F = F - ka_face(c, 2, i, j, k);
         AT(c.Fw, i, j, k) = F;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// sponge_layer (3_contorno.f90:1011-1103), called by complementos: epis_z on
+// the w faces of the columns i >= nint(x_inicial / dx) + 1 (x_inicial = nx dx
+// - 1 m; clamped to 1), in FP64 and stored once rounded.  esp_type 1 grades
+// it with the interface height zpfs(i) of the last (j, k) of the plane where
+// ls changes sign (a block max-reduction of the loop index; no sign change:
+// the domain height when the plane's first cell is water, else 0, for the
+// value the reference leaves unset); the heights z_x are the reference's
+// running sums.  Grid: x = column i - 1, y = case.
+template <typename T>
+__global__ void __launch_bounds__(256) k_sponge(const CaseDev<T> *__restrict__ cs, int ncases)
+{
+    const CaseDev<T> &c = cs[blockIdx.y];
+    if (c.esp_type <= 0) return;
+    const Geo &g = c.g;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const int i = blockIdx.x + 1;
+    if (i > nx) return;
+    const double dx = c.dx, dz = c.dz;
+    const double l_sponge = 1., x_inicial = nx * dx - l_sponge;
+    const double alfa = 60., alfa0 = 0., alfa1 = 30.;
+    int i0 = (int)llround(x_inicial / dx) + 1;
+    if (i0 < 1) i0 = 1;
+    if (i < i0) return;
+    const double zpt = dz * nz;
+    __shared__ long long red[32];
+    __shared__ double zpfs_s;
+    if (c.esp_type == 1) {
+        long long best = -1;
+        const long long nk = nz - 1, n = (long long)ny * nk;
+        for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+            const int j = (int)(t / nk) + 1, k = (int)(t % nk) + 1;
+            if (AT(c.ls, i, j, k) * AT(c.ls, i, j, k + 1) <= T(0.)) best = t;   // t grows per thread
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const long long v = __shfl_down_sync(0xffffffffu, best, o);
+            best = v > best ? v : best;
+        }
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = best;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            long long b = -1;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b = red[w] > b ? red[w] : b;
+            double z = ((double)AT(c.ls, i, 1, 1) >= 0.) ? zpt : 0.;
+            if (b >= 0) {
+                const int j = (int)(b / nk) + 1, k = (int)(b % nk) + 1;
+                const double alt1 = dz * (k - 0.5) + (double)AT(c.ls, i, j, k);
+                const double alt2 = dz * (k + 0.5) + (double)AT(c.ls, i, j, k + 1);
+                z = alt1 > alt2 ? alt1 : alt2;
+            }
+            zpfs_s = z;
+        }
+        __syncthreads();
+    }
+    const double zpfs = (c.esp_type == 1) ? zpfs_s : 0.;
+    const double xp = (i - 0.5) * dx;
+    const double aux1 = (xp - x_inicial) / l_sponge;
+    for (int j = 1 + threadIdx.x; j <= ny; j += blockDim.x) {
+        double zx = -dz;
+        for (int k = 1; k <= nz; ++k) {
+            zx = zx + dz;
+            double e;
+            if (c.esp_type == 1) {
+                if (AT(c.ls, i, j, k) >= T(0.)) e = alfa * aux1 * aux1 * (0. - zx) / (0. - zpfs);
+                else e = alfa * aux1 * aux1 * (zx - zpt) / (zpfs - zpt);
+            } else {
+                e = alfa0 + aux1 * (alfa1 - alfa0);
+            }
+            AT(c.epis, i, j, k) = T(e);
+        }
     }
 }
 
@@ -633,6 +708,17 @@ template <typename T> void launch_visco(const Batch<T> &b, int keq_stages, const
     if (keq_stages > 0) launch_keq<T>(b, keq_stages, a_dt, s);   // m_turb >= 2 cases
     k_visco_faces<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();
 }
+template <typename T> void launch_sponge(const Batch<T> &b, cudaStream_t s)
+{
+    int nxmax = 1;
+    bool any = false;
+    for (int c = 0; c < b.ncases; ++c) {
+        nxmax = b.hcases[c].g.nx > nxmax ? b.hcases[c].g.nx : nxmax;
+        any |= b.hcases[c].esp_type > 0;
+    }
+    if (!any) return;
+    k_sponge<T><<<dim3(nxmax, b.ncases), 256, 0, s>>>(b.dcases, b.ncases); count_launch();
+}
 template <typename T> void launch_convdiff(const Batch<T> &b, int fuse, cudaStream_t s)
 {
     k_convdiff<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, fuse); count_launch();
@@ -671,6 +757,7 @@ template <typename T> void launch_set_scalar(const Batch<T> &b, int slot, double
 #define INST(T)                                                              \
     template void launch_visco<T>(const Batch<T> &, int, const double *, cudaStream_t); \
     template void launch_convdiff<T>(const Batch<T> &, int, cudaStream_t);  \
+    template void launch_sponge<T>(const Batch<T> &, cudaStream_t);         \
     template void launch_complementos<T>(const Batch<T> &, cudaStream_t);   \
     template void launch_tempo<T>(const Batch<T> &, int, int, cudaStream_t);          \
     template void launch_posdin<T>(const Batch<T> &, cudaStream_t);         \

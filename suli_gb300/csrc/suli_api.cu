@@ -140,6 +140,7 @@ static int validate(const suli_params &p)
     if (p.reinit_max_iter < 1) return bad("reinit_max_iter must be >= 1");
     if (p.cg_max_iter < 1) return bad("cg_max_iter must be >= 1");
     if (p.t_tens != 0 && p.t_tens != 1) return bad("t_tens must be 0 or 1");
+    if (p.esp_type < 0 || p.esp_type > 2) return bad("esp_type must be 0, 1 or 2");
     if ((long long)p.nx * p.ny * p.nz > (1LL << 31) - 1) return bad("grid larger than 2^31 cells");
     return SULI_OK;
 }
@@ -422,6 +423,7 @@ struct Impl : ImplBase {
             cd.t_tens = q.t_tens; cd.sigma = q.sigma;
             cd.cmu = q.cmu; cd.cdes = q.cdes; cd.lcar = q.lcar; cd.delta = cd.dx1;
             cd.t_press = q.t_press;
+            cd.esp_type = q.esp_type;
             cd.ipa = (q.t_press == 2 && (q.mms_t == 0 || q.project_under_mms)) ? 1 : 0;
             cd.reinit_max = q.reinit_max_iter; cd.cg_max = q.cg_max_iter; cd.cg_tol_mode = q.cg_tol_mode;
             cd.cg_tol = q.cg_tol;
@@ -444,8 +446,8 @@ struct Impl : ImplBase {
             // k equation (m_turb >= 2) and IPA (t_press = 2) arrays only where used
             T **kf[] = {&cd.ka, &cd.nut, &cd.sij, &cd.ka0, &cd.fk0, &cd.fk1, &cd.fka};
             T **af[] = {&cd.prd0, &cd.px, &cd.py, &cd.pz};
-            const int nkf = (q.m_turb >= 2) ? 7 : 0, naf = (q.t_press == 2) ? 4 : 0;
-            size_t bytes = fb * (ntf + nkf + naf) + ib * 4 + pb * 3 + (mixed ? 20 * db : 0) + (mg ? 8 * fb : 0);
+            const int nkf = (q.m_turb >= 2) ? 7 : 0, naf = (q.t_press == 2) ? 4 : 0, nsf = (q.esp_type > 0) ? 1 : 0;
+            size_t bytes = fb * (ntf + nkf + naf + nsf) + ib * 4 + pb * 3 + (mixed ? 20 * db : 0) + (mg ? 8 * fb : 0);
             void *slab = nullptr;
             CK(cudaMalloc(&slab, bytes));
             slabs.push_back(slab);
@@ -456,6 +458,7 @@ struct Impl : ImplBase {
             for (int f = 0; f < 3; ++f) { *ptf[f] = (T *)cur; cur += pb; }
             for (int f = 0; f < nkf; ++f) { *kf[f] = (T *)cur; cur += fb; }
             for (int f = 0; f < naf; ++f) { *af[f] = (T *)cur; cur += fb; }
+            if (nsf) { cd.epis = (T *)cur; cur += fb; }
             if (mixed) {
                 double **d64[] = {&cd.e64, &cd.r64, &cd.rho64, &cd.spi64, &cd.spj64, &cd.spk64, &cd.dpr64, &cd.qpr64,
                                   &cd.u64, &cd.v64, &cd.w64, &cd.u064, &cd.v064, &cd.w064,
@@ -974,12 +977,14 @@ struct Impl : ImplBase {
     bool stored(int icase, int f) override { return dev_ptr(icase, f) != nullptr; }
     int convdiff(int fuse) override
     {
+        if (fuse) launch_sponge<T>(b, st);     // complementos' sponge_layer call
         launch_convdiff<T>(b, fuse, st);
         CKL();
         return SULI_OK;
     }
     int complementos() override
     {
+        launch_sponge<T>(b, st);
         launch_complementos<T>(b, st);
         CKL();
         return SULI_OK;

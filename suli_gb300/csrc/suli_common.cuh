@@ -129,6 +129,7 @@ struct CaseDev {
     int ccx0, ccxf, ccy0, ccyf, ccz0, cczf;
     int t_tempo, m_turb, mms_t, ibm_t, obst_t, t_tens;
     int t_press, ipa;           // ipa: t_press = 2 and the step projects (exp_press / IPA graddin)
+    int esp_type;               // sponge layer (0 none)
     int reinit_max, cg_max, cg_tol_mode;
     double cg_tol;
     // fields (reference module arrays)
@@ -146,6 +147,8 @@ struct CaseDev {
     T *ka, *nut, *sij, *ka0, *fk0, *fk1, *fka;
     // IPA (t_press = 2, else null): accumulated pressure and the explicit force
     T *prd0, *px, *py, *pz;
+    // sponge layer (esp_type > 0, else null): epis_z on the w faces
+    T *epis;
     int *id_ibmx, *id_ibmy, *id_ibmz, *id_ibm;
     T *bxx0, *bxx1, *blx1;      // inflow planes, indexed at(0, j, k)
     // CG work arrays

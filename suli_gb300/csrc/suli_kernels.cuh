@@ -57,6 +57,8 @@ template <typename T> void launch_keq(const Batch<T> &b, int ntt, const double *
 template <typename T> void launch_contorno_les(const Batch<T> &b, cudaStream_t s);
 template <typename T> void launch_exp_press(const Batch<T> &b, cudaStream_t s);
 template <typename T> void launch_convdiff(const Batch<T> &b, int fuse_compl, cudaStream_t s);
+// sponge_layer's epis_z for the esp_type > 0 cases (before complementos)
+template <typename T> void launch_sponge(const Batch<T> &b, cudaStream_t s);
 template <typename T> void launch_complementos(const Batch<T> &b, cudaStream_t s);
 template <typename T> void launch_tempo(const Batch<T> &b, int tt, int it, cudaStream_t s);
 template <typename T> void launch_posdin(const Batch<T> &b, cudaStream_t s);

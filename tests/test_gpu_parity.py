@@ -34,6 +34,10 @@ def _configs():
         ("k_des", cases.k_channel(24, 6, 12, m_turb=3)),
         # implicit pressure algorithm (t_press = 2)
         ("ipa", cases.ipa_tank(16, 6, 12)),
+        # sponge layer over the last metre (esp_type 1 graded, 2 linear); a
+        # tank near rest, solved to 1e-12 like wave_les
+        ("sponge1", cases.sponge_tank(32, 4, 16, esp_type=1, cg_tol=1e-12)),
+        ("sponge2", cases.sponge_tank(32, 4, 16, esp_type=2, cg_tol=1e-12)),
     ]
 
 

@@ -139,3 +139,48 @@ def test_ipa_tank_builds_hydrostatic_pressure():
     water = int(0.45 / p.dz)                        # cells below the surface
     assert np.all(np.diff(col[:water]) < 0), col[:water]
     assert np.abs(o.field("W")).max() < p.gz * steps * p.dt
+
+
+@pytest.mark.parametrize("esp_type", [1, 2])
+def test_sponge_layer_profile(esp_type):
+    """sponge_layer (3_contorno.f90:1011-1103) through complementos: Fw loses
+    w epis_z, epis_z = 30 a over the last metre for esp_type 2 and 60 a^2
+    times the relative depth (water) or height (air) for esp_type 1, with a
+    the distance into the layer in metres."""
+    case = cases.sponge_tank(32, 4, 16, esp_type=esp_type)
+    p = case.params
+    o = pyoracle.Oracle(p)
+    flat = np.empty((p.nx, p.ny, p.nz), order="F")
+    z = (np.arange(1, p.nz + 1) - 0.5) * p.dz
+    flat[...] = 0.5 - z[None, None, :]
+    o.set_field("LS", flat)
+    o.heaviside_init()
+    rng = np.random.default_rng(1)
+    w = np.asfortranarray(rng.standard_normal(o.field("W").shape))
+    o.set_field("W", w)
+    fw0 = np.asfortranarray(rng.standard_normal(o.field("FW").shape))
+    p0 = p.copy()
+    p0.esp_type = 0
+    o0 = pyoracle.Oracle(p0)
+    o0.set_field("LS", flat)
+    o0.heaviside_init()
+    o0.set_field("W", w)
+    o0.set_field("FW", fw0)
+    o0.complementos()
+    o.set_field("FW", fw0)
+    o.complementos()
+    d = o0.field("FW") - o.field("FW")                 # = w epis_z (w faces 1..nz1)
+    xc = (np.arange(1, p.nx + 1) - 0.5) * p.dx
+    a = np.maximum(xc - (p.nx * p.dx - 1.0), 0.0)[:, None, None]
+    zx = ((np.arange(1, p.nz + 1) - 1) * p.dz)[None, None, :]
+    if esp_type == 2:
+        ep = 30.0 * a * np.ones((1, p.ny, p.nz))
+    else:
+        zpfs, zpt = 0.5, p.dz * p.nz
+        water = flat >= 0
+        ep = np.where(water, 60.0 * a * a * zx / zpfs, 60.0 * a * a * (zx - zpt) / (zpfs - zpt))
+    ep[xc <= p.nx * p.dx - 1.0] = 0.0
+    want = w[1:p.nx + 1, 1:p.ny + 1, 1:p.nz + 1] * ep
+    assert np.allclose(d[:, :, :p.nz], want, rtol=1e-9, atol=1e-12)
+    assert np.all(d[:, :, p.nz] == 0.0)
+    assert np.abs(want).max() > 1.0
