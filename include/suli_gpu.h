@@ -104,6 +104,12 @@ typedef struct suli_params {
                                       (5_viscosidade.f90:94) */
     int32_t esp_type;              /* sponge layer over the last 1 m in x: 0 none, 1 graded with the
                                       depth, 2 linear (3_contorno.f90:1011-1103) */
+    int32_t wave_t;                /* inflow waves for ccx0 = 3: 0 none, 1 Stokes I, 2 Stokes II,
+                                      5 Stokes V (boundary_waves, 3_contorno.f90:1189-1319) */
+    double  a_w, f_w, n_w, h0_f;   /* wave amplitude, angular frequency, wave number, still depth:
+                                      waves_coef's results (3_contorno.f90:1323-1445, run by the
+                                      host's iniciais, 2_iniciais.f90:241-245) */
+    double  aeta[5], avel[5];      /* Stokes V surface and velocity coefficients (waves_coef) */
 } suli_params;
 
 /* ---- field ids (reference module arrays) -------------------------------- */
@@ -154,6 +160,7 @@ enum suli_field {
     SULI_F_PX,       /* px (nx1, ny, nz) explicit pressure force of the IPA (exp_press); t_press = 2 */
     SULI_F_PY,       /* py (nx, ny1, nz) */
     SULI_F_PZ,       /* pz (nx, ny, nz1) */
+    SULI_F_BXZ0,     /* bxz0 (0:ny+1, 0:nz+1) inflow w at i = 0 (ccx0 = 3; the waves set it) */
     SULI_F_COUNT
 };
 
@@ -245,6 +252,10 @@ int suli_exp_press(suli_handle *h);
  * cases with m_turb >= 2 (the k-equation loop of visco calls it on every
  * sub-stage; iniciais calls it once after setting ka, 2_iniciais.f90:216-235). */
 int suli_contorno_les(suli_handle *h);
+/* boundary_waves (3_contorno.f90:1189-1319), wave_t > 0: the inflow planes
+ * bxx0, bxx1, bxz0 and ls(1, :, :) of the wave at the current time t; the
+ * step calls it after tempo in every RK stage (1_principal.f90:93). */
+int suli_boundary_waves(suli_handle *h);
 int suli_conmassa(suli_handle *h, double *maxdiv_out); /* 4_plot.f90:386-394 */
 int suli_mms_error(suli_handle *h, double err_out[4]); /* 13_mms.f90:391-451 */
 /* Sets tt (1..ntt) and dt = a_dt(tt), as the RK loop of 1_principal.f90:86-87. */

@@ -47,7 +47,8 @@ def lib():
         L.or_level_set_ini.argtypes = [C.c_void_p, C.c_int] + [C.c_double] * 5
         for name in ("or_heaviside_init", "or_iniciais_velocity", "or_mms_init", "or_termo_fonte1",
                      "or_ibm_setup", "or_level_set", "or_visco", "or_convdiff", "or_complementos",
-                     "or_tempo", "or_posdin", "or_step", "or_exp_press", "or_contorno_les"):
+                     "or_tempo", "or_posdin", "or_step", "or_exp_press", "or_contorno_les",
+                     "or_boundary_waves"):
             getattr(L, name).argtypes = [C.c_void_p]
             getattr(L, name).restype = None
         L.or_obstaculo_cylinder.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double]
@@ -172,6 +173,9 @@ class Oracle:
 
     def contorno_les(self):
         lib().or_contorno_les(self._h)
+
+    def boundary_waves(self):
+        lib().or_boundary_waves(self._h)
 
     def conmassa(self) -> float:
         return lib().or_conmassa(self._h)

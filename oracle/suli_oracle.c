@@ -101,7 +101,7 @@ struct or_case {
     F3 ka, nut;                /* k equation (m_turb >= 2): ka (0:nx+1, 0:ny+1, 0:nz+1), nut cells */
     F3 prd0, px, py, pz;       /* IPA (t_press = 2): prd0 like prd1, px/py/pz on the faces */
     I3 id_ibmx, id_ibmy, id_ibmz, id_ibm;
-    F3 bxx0, bxx1, blx1;
+    F3 bxx0, bxx1, blx1, bxz0;
 
     int cg_iters[3];
     double cg_res[3];
@@ -169,6 +169,7 @@ or_case *or_create(const suli_params *pp)
     i3_init(&c->id_ibm, 1, nx, 1, ny, 1, nz);
     f3_init(&c->bxx0, 0, ny + 1, 0, nz + 1, 0, 0);
     f3_init(&c->bxx1, 0, ny + 1, 0, nz + 1, 0, 0);
+    f3_init(&c->bxz0, 0, ny + 1, 0, nz + 1, 0, 0);
     f3_init(&c->blx1, 1, ny, 1, nz, 0, 0);
 
     /* level_set_ini coefficients, 14_level_set.f90:29-42 */
@@ -203,7 +204,7 @@ void or_destroy(or_case *c)
                  &c->mu, &c->mut, &c->xmu, &c->ymu, &c->zmu, &c->Fu, &c->Fv, &c->Fw, &c->u0,
                  &c->v0, &c->w0, &c->fu0, &c->fv0, &c->fw0, &c->fu1, &c->fv1, &c->fw1, &c->div,
                  &c->tf_u, &c->tf_v, &c->tf_w, &c->obs_lsx, &c->obs_lsy, &c->obs_lsz,
-                 &c->obs_lss, &c->bxx0, &c->bxx1, &c->blx1, &c->obs_ls, &c->hsx, &c->hsy, &c->hsz, &c->kurv,
+                 &c->obs_lss, &c->bxx0, &c->bxx1, &c->blx1, &c->bxz0, &c->obs_ls, &c->hsx, &c->hsy, &c->hsz, &c->kurv,
                  &c->ka, &c->nut, &c->prd0, &c->px, &c->py, &c->pz};
     for (unsigned q = 0; q < sizeof(all) / sizeof(all[0]); ++q) free(all[q]->p);
     free(c->id_ibmx.p); free(c->id_ibmy.p); free(c->id_ibmz.p); free(c->id_ibm.p);
@@ -266,6 +267,7 @@ void *or_field(or_case *c, int f, int lo[3], int hi[3])
     case SULI_F_ID_IBM: ia = &c->id_ibm; break;
     case SULI_F_BXX0: a = &c->bxx0; break;
     case SULI_F_BXX1: a = &c->bxx1; break;
+    case SULI_F_BXZ0: a = &c->bxz0; break;
     case SULI_F_BLX1: a = &c->blx1; break;
     default: return NULL;
     }
@@ -1493,8 +1495,12 @@ void or_contorno(or_case *c, int nlock)
         if (p->ccx0 == 0 && p->ccxf == 0) { setx(u, 0, u, nx1 - 1, 1.); setx(v, 0, v, nx, 1.); setx(w, 0, w, nx, 1.); }
         if (p->ccx0 == 1) { setx(u, 0, u, 2, -1.); setx(v, 0, v, 1, 1.); setx(w, 0, w, 1, 1.); }
         if (p->ccx0 == 2) { setx(u, 0, u, 2, 1.); setx(v, 0, v, 1, -1.); setx(w, 0, w, 1, -1.); }
-        if (p->ccx0 == 3) {   /* bxy0 = bxz0 = 0 (2_iniciais.f90:384-385) */
-            zerox(v, 0); zerox(w, 0);
+        if (p->ccx0 == 3) {   /* v = bxy0 = 0 (2_iniciais.f90:384-385; the waves leave it unset);
+                                 w = bxz0, whose plane is one row shorter than w's: the top
+                                 row w(0, :, nz+2) reads past it upstream, 0 here */
+            zerox(v, 0);
+            for (int k = 0; k <= nz1 + 1; ++k)
+                for (int j = 0; j <= ny + 1; ++j) A(*w, 0, j, k) = (k <= nz + 1) ? A(c->bxz0, j, k, 0) : 0.;
             inflow_plane(c, 0, &c->bxx0, 1.0);
         }
         /* x = lx, :350-384 */
@@ -1741,6 +1747,58 @@ static void ghost_fill_cg(const or_case *c, F3 *m)
 #pragma omp parallel for schedule(static)
     for (int j = 0; j <= ny1; ++j)
         for (int i = 0; i <= nx1; ++i) { A(*m, i, j, 0) = A(*m, i, j, 1); A(*m, i, j, nz + 1) = A(*m, i, j, nz); }
+}
+
+/* boundary_waves, 3_contorno.f90:1189-1319 (Stokes I, II, V) at time t:
+ * ls1, u1, w1 on the columns i = 0, 1; ls(1, :, :) = ls1(1), bxx0 = u1(0),
+ * bxz0 = w1(0), bxx1 = u1(1) */
+void or_boundary_waves(or_case *c)
+{
+    const suli_params *p = &c->p;
+    if (p->wave_t <= 0) return;
+    const int ny = c->ny, nz = c->nz;
+    const double dx = c->dx, dz = c->dz, t = c->t;
+    const double a_w = p->a_w, f_w = p->f_w, n_w = p->n_w, h0 = p->h0_f;
+    for (int k = 0; k <= nz + 1; ++k)
+        for (int j = 0; j <= ny + 1; ++j)
+            for (int i = 0; i <= 1; ++i) {
+                const double kp = (k - 0.5) * dz;                 /* waves_coef, :1336-1338 */
+                const double aux2 = n_w * dx * (i - 0.5) - f_w * t, aux3 = n_w * dx * (i - 1.) - f_w * t;
+                double h_f, u1 = 0., w1 = 0.;
+                if (p->wave_t == 1) {
+                    h_f = h0 + a_w * cos(aux2);
+                    if (h_f - kp >= 0.) {
+                        u1 = a_w * f_w * cosh(n_w * kp) / sinh(n_w * h0) * cos(aux3);
+                        w1 = a_w * f_w * sinh(n_w * (kp - 0.5 * dz)) / sinh(n_w * h0) * sin(aux2);
+                    }
+                } else if (p->wave_t == 2) {
+                    const double aux1 = tanh(n_w * h0);
+                    h_f = h0 + a_w * cos(aux2) + n_w * a_w * a_w * (3. - aux1 * aux1) / (4. * aux1 * aux1 * aux1) * cos(2. * aux2);
+                    if (h_f - kp >= 0.) {
+                        const double s4 = pow(sinh(n_w * h0), 4.);
+                        u1 = a_w * f_w * cosh(n_w * kp) / sinh(n_w * h0) * cos(aux3) +
+                             3. / 4. * a_w * a_w * f_w * n_w * cosh(2. * n_w * kp) / s4 * cos(2 * aux3);
+                        w1 = a_w * f_w * sinh(n_w * (kp - 0.5 * dz)) / sinh(n_w * h0) * sin(aux2) +
+                             3. / 4. * a_w * a_w * f_w * n_w * sinh(2. * n_w * (kp - 0.5 * dz)) / s4 * sin(2. * aux3);
+                    }
+                } else {
+                    const double aux4 = n_w * kp, aux5 = n_w * (kp - 0.5 * dz);
+                    const double *ae = p->aeta, *av = p->avel;
+                    h_f = h0 + ae[0] * cos(aux2) + ae[1] * cos(2. * aux2) + ae[2] * cos(3. * aux2) + ae[3] * cos(4. * aux2) +
+                          ae[4] * cos(5. * aux2);
+                    if (h_f - kp >= 0.) {
+                        u1 = av[0] * cosh(aux4) * cos(aux3) + av[1] * cosh(2 * aux4) * cos(2 * aux3) +
+                             av[2] * cosh(3 * aux4) * cos(3 * aux3) + av[3] * cosh(4 * aux4) * cos(4 * aux3) +
+                             av[4] * cosh(5 * aux4) * cos(5 * aux3);
+                        w1 = av[0] * sinh(aux5) * sin(aux2) + av[1] * sinh(2 * aux5) * sin(2 * aux2) +
+                             av[2] * sinh(3 * aux5) * sin(3 * aux2) + av[3] * sinh(4 * aux5) * sin(4 * aux2) +
+                             av[4] * sinh(5 * aux5) * sin(5 * aux2);
+                    }
+                }
+                if (i == 1 && j >= 1 && j <= ny && k >= 1 && k <= nz) A(c->ls, 1, j, k) = h_f - kp;
+                if (i == 0) { A(c->bxx0, j, k, 0) = u1; A(c->bxz0, j, k, 0) = w1; }
+                else A(c->bxx1, j, k, 0) = u1;
+            }
 }
 
 /* exp_press, 11_diversos.f90:455-495 (t_press = 2) */
@@ -2281,6 +2339,7 @@ void or_step(or_case *c)
         or_convdiff(c);
         or_complementos(c);
         or_tempo(c);
+        if (c->p.wave_t > 0) or_boundary_waves(c);   /* :93 */
         or_contorno(c, 2);
         if (c->p.mms_t == 0 || c->p.project_under_mms) {
             if (c->p.t_press == 1) {

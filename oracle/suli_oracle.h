@@ -59,6 +59,7 @@ int  or_graddin(or_case *c);                  /* 9_grad.f90:10-663, returns iter
 void or_posdin(or_case *c);                   /* 10_pos.f90:1-99 */
 void or_exp_press(or_case *c);                /* 11_diversos.f90:455-495 (t_press = 2) */
 void or_contorno_les(or_case *c);             /* 3_contorno.f90:666-790 */
+void or_boundary_waves(or_case *c);           /* 3_contorno.f90:1189-1319 */
 double or_conmassa(or_case *c);               /* 4_plot.f90:386-394, returns max|div| */
 int  or_prtscr_write(or_case *c, const char *path, int t_plot); /* 4_plot.f90:547-615 */
 void or_mms_error(or_case *c, double err[4]); /* 13_mms.f90:391-451 */

@@ -56,6 +56,13 @@ class SuliParams(C.Structure):
         ("cdes", C.c_double),
         ("lcar", C.c_double),
         ("esp_type", C.c_int32),
+        ("wave_t", C.c_int32),
+        ("a_w", C.c_double),
+        ("f_w", C.c_double),
+        ("n_w", C.c_double),
+        ("h0_f", C.c_double),
+        ("aeta", C.c_double * 5),
+        ("avel", C.c_double * 5),
     ]
 
     def copy(self) -> "SuliParams":
@@ -108,6 +115,7 @@ def default_params(**kw) -> SuliParams:
     p.cdes = 0.65
     p.lcar = 0.05715
     p.esp_type = 0
+    p.wave_t = 0
     p.mixed_precond = 1
     for k, v in kw.items():
         if not hasattr(p, k):
@@ -124,7 +132,7 @@ FIELDS = [
     "OBS_LSX", "OBS_LSY", "OBS_LSZ", "OBS_LSS",
     "ID_IBMX", "ID_IBMY", "ID_IBMZ", "ID_IBM",
     "BXX0", "BXX1", "BLX1", "OBS_LS", "HSX", "HSY", "HSZ", "KURV",
-    "KA", "NUT", "PRD0", "PX", "PY", "PZ",
+    "KA", "NUT", "PRD0", "PX", "PY", "PZ", "BXZ0",
 ]
 FIELD_ID = {name: i for i, name in enumerate(FIELDS)}
 INT_FIELDS = {"ID_IBMX", "ID_IBMY", "ID_IBMZ", "ID_IBM"}
@@ -151,6 +159,7 @@ def field_bounds(p: SuliParams, name: str):
         "PRD0": ((0, 0, 0), (nx + 1, ny + 1, nz + 1)),
         "BXX0": ((0, 0, 0), (ny + 1, nz + 1, 0)),
         "BXX1": ((0, 0, 0), (ny + 1, nz + 1, 0)),
+        "BXZ0": ((0, 0, 0), (ny + 1, nz + 1, 0)),
         "BLX1": ((1, 1, 0), (ny, nz, 0)),
         "OBS_LS": ((1, 1, 1), (nx1, ny1, nz1)),
     }

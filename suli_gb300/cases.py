@@ -363,3 +363,117 @@ def sponge_tank(nx=32, ny=4, nz=16, esp_type=1, precision=PREC_FP64, dt=2e-4, cg
     ls = np.empty((nx, ny, nz), order="F")
     ls[...] = 0.5 + 0.05 * np.cos(math.pi * x / lx) - z
     return Case("sponge_tank_%dx%dx%d" % (nx, ny, nz), p, _base_fields(p, ls), steps=200)
+
+
+def waves_coef(gz: float, wave_t: int) -> dict:
+    """waves_coef (3_contorno.f90:1323-1445), the host set-up of the inflow
+    waves that iniciais runs once (2_iniciais.f90:241-245): amplitude 0.03 m,
+    period 2.5 s, still depth 1 m as upstream; the wave length from the
+    linear dispersion relation by 1000 fixed-point steps (Stokes I, II), or
+    for Stokes V the length and the expansion parameter lambda where the two
+    fixed-point estimates of lambda agree best over 10000 trial lengths
+    (10000 steps each, vectorised over the trials).  Returns the suli_params
+    fields a_w, f_w, n_w, h0_f, aeta, avel."""
+    pi = math.pi
+    a_w, p_w, h0_f = 0.03, 2.5, 1.0
+    l0_w = gz * p_w * p_w / (2.0 * pi)
+    out = {"a_w": a_w, "h0_f": h0_f, "aeta": [0.0] * 5, "avel": [0.0] * 5}
+    if wave_t <= 2:
+        l_w = gz * p_w * p_w / (2.0 * pi)
+        for _ in range(1000):
+            l_w = gz * p_w * p_w / (2.0 * pi) * math.tanh(2.0 * pi * h0_f / l_w)
+        out.update(f_w=2.0 * pi / p_w, n_w=2.0 * pi / l_w)
+        return out
+
+    def coefs(s, c):
+        b33 = 3.0 * (8.0 * c ** 6.0 + 1.0) / (64.0 * s ** 6.0)
+        b35 = (88128.0 * c ** 14.0 - 208224.0 * c ** 12 + 70848.0 * c ** 10.0 + 54000.0 * c ** 8.0
+               - 21816.0 * c ** 6.0 + 6264.0 * c ** 4.0 - 54.0 * c * c - 81.0) / (12288.0 * s ** 12.0 * (6.0 * c * c - 1.0))
+        b55 = (192000.0 * c ** 16.0 - 262720.0 * c ** 14.0 + 83680.0 * c ** 12 + 20160.0 * c ** 10.0
+               - 7280.0 * c ** 8.0 + 7160.0 * c ** 6.0 - 1800.0 * c ** 4.0 - 1050.0 * c * c + 225.0) / \
+            (12288 * s ** 10.0 * (6.0 * c * c - 1.0) * (8.0 * c ** 4.0 - 11.0 * c * c + 3.0))
+        c1 = (8.0 * c ** 4.0 - 8.0 * c * c + 9.0) / (8.0 * s ** 4.0)
+        c2 = (3840.0 * c ** 12.0 - 4096.0 * c ** 10.0 + 2592.0 * c ** 8.0 - 1008.0 * c ** 6.0 + 5944.0 * c ** 4.0
+              - 1830.0 * c * c + 147.0) / (512.0 * s ** 10.0 * (6.0 * c * c - 1.0))
+        return b33, b35, b55, c1, c2
+
+    ii = np.arange(1, 10001, dtype=np.float64)
+    l_w1 = l0_w * 0.5 + l0_w * (ii / 10000) * 2.5
+    s = np.sinh(2.0 * pi * h0_f / l_w1)
+    c = np.cosh(2.0 * pi * h0_f / l_w1)
+    b33, b35, b55, c1, c2 = coefs(s, c)
+    with np.errstate(all="ignore"):
+        lamb1 = np.zeros_like(l_w1)
+        for _ in range(10000):
+            lamb1 = pi * a_w * 2.0 / l_w1 - lamb1 ** 3.0 * b33 - lamb1 ** 5.0 * (b35 + b55)
+        lamb2 = np.zeros_like(l_w1)
+        for _ in range(10000):
+            lamb2 = np.sqrt((l_w1 / (l0_w * np.tanh(2.0 * pi * h0_f / l_w1)) - 1.0) / (c1 + lamb2 ** 2.0 * c2))
+        erro = np.abs(lamb1 - lamb2)
+    best = int(np.nanargmin(erro))      # the first of the smallest, as the strict < of the search
+    lamb, l_w = float(lamb1[best]), float(l_w1[best])
+    f_w, n_w = 2.0 * pi / p_w, 2.0 * pi / l_w
+    s = math.sinh(2.0 * pi * h0_f / l_w)
+    c = math.cosh(2.0 * pi * h0_f / l_w)
+    b33, b35, b55, c1, c2 = coefs(s, c)
+    a11 = 1.0 / s
+    a13 = -c * c * (5.0 * c * c + 1.0) / (8.0 * s ** 5.0)
+    a15 = -(1184.0 * c ** 10.0 - 1440.0 * c ** 8.0 - 1992.0 * c ** 6.0 + 2641.0 * c ** 4.0 - 249.0 * c ** 2.0 + 18.0) \
+        / (1536.0 * s ** 11.0)
+    a22 = 3.0 / (8.0 * s ** 4.0)
+    a24 = (192.0 * c ** 8.0 - 424.0 * c ** 6.0 - 312.0 * c ** 4.0 + 480.0 * c * c - 17.0) / (768.0 * s ** 10.0)
+    a33 = (13.0 - 4.0 * c * c) / (64.0 * s ** 7.0)
+    a35 = (512.0 * c ** 12.0 + 4224.0 * c ** 10.0 - 6800.0 * c ** 8.0 - 12808.0 * c ** 6.0 + 16704.0 * c ** 4.0
+           - 3154.0 * c * c + 107.0) / (4096.0 * s ** 13.0 * (6.0 * c * c - 1.0))
+    a44 = (80.0 * c ** 6.0 - 816.0 * c ** 4.0 + 1338.0 * c * c - 197.0) / (1536.0 * s ** 10.0 * (6.0 * c * c - 1.0))
+    a55 = -(2880.0 * c ** 10.0 - 72480.0 * c ** 8.0 + 324000.0 * c ** 6.0 - 432000.0 * c ** 4.0 + 163470.0 * c * c
+            - 16245.0) / (61440.0 * s ** 11.0 * (6.0 * c * c - 1.0) * (8.0 * c ** 4.0 - 11.0 * c * c + 3.0))
+    b22 = c * (2.0 * c * c + 1.0) / (4.0 * s ** 3.0)
+    b24 = c * (272.0 * c ** 8.0 - 504.0 * c ** 6.0 - 192.0 * c ** 4.0 + 322 * c * c + 21.0) / (384.0 * s ** 9.0)
+    b44 = c * (768.0 * c ** 10.0 - 448.0 * c ** 8.0 - 48.0 * c ** 6.0 + 48.0 * c ** 4.0 + 106.0 * c * c - 21.0) / \
+        (384.0 * s ** 9.0 * (6.0 * c * c - 1.0))
+    aeta = [lamb / n_w,
+            (lamb * lamb * b22 + lamb ** 4.0 * b24) / n_w,
+            (lamb ** 3.0 * b33 + lamb ** 5.0 * b35) / n_w,
+            lamb ** 4.0 * b44 / n_w,
+            lamb ** 5.0 * b55 / n_w]
+    k0 = 2.0 * pi / (p_w * n_w)
+    avel = [1.0 * k0 * (lamb * a11 + lamb ** 3.0 * a13 + lamb ** 5.0 * a15),
+            2.0 * k0 * (lamb ** 2.0 * a22 + lamb ** 4.0 * a24),
+            3.0 * k0 * (lamb ** 3.0 * a33 + lamb ** 5.0 * a35),
+            4.0 * k0 * (lamb ** 4.0 * a44),
+            5.0 * k0 * (lamb ** 5.0 * a55)]
+    out.update(f_w=f_w, n_w=n_w, aeta=aeta, avel=avel, lamb=lamb)
+    return out
+
+
+def set_waves(p: SuliParams, wave_t: int) -> dict:
+    """waves_coef's results into the suli_params of a case."""
+    w = waves_coef(p.gz, wave_t)
+    p.wave_t = wave_t
+    p.a_w, p.f_w, p.n_w, p.h0_f = w["a_w"], w["f_w"], w["n_w"], w["h0_f"]
+    for m in range(5):
+        p.aeta[m] = w["aeta"][m]
+        p.avel[m] = w["avel"][m]
+    return w
+
+
+def wave_flume(nx=48, ny=4, nz=24, wave_t=1, precision=PREC_FP64, dt=2e-4, esp_type=1) -> Case:
+    """A wave flume: still water 1 m deep (waves_coef's h0_f) in a 6 x 0.5 x
+    1.5 m box, waves entering through the prescribed inflow face (ccx0 = 3,
+    boundary_waves, 3_contorno.f90:1189-1319) and absorbed by the sponge
+    layer over the last metre (esp_type 1) before the free outflow at x = 6 m
+    (ccxf = 4).  The wave's net inflow makes the all-Neumann pressure
+    equation incompatible, as upstream: the reference's absolute stopping
+    test (1e-4) ends each solve at the compatible part."""
+    h = 6.0 / nx
+    p = default_params(nx=nx, ny=ny, nz=nz, dx=h, dy=0.5 / ny, dz=1.5 / nz, dt=dt,
+                       ccx0=3, ccxf=4, ccy0=1, ccyf=1, ccz0=1, cczf=1, gz=9.80665,
+                       uinicial=0.0, iturb=0.0, reinit_max_iter=3, cg_tol_mode=CG_TOL_ABS, cg_tol=1e-4,
+                       precision=precision)
+    p.esp_type = esp_type
+    set_waves(p, wave_t)
+    z = _centres(nz, p.dz)[None, None, :]
+    ls = np.empty((nx, ny, nz), order="F")
+    ls[...] = p.h0_f - z
+    return Case("wave_flume_s%d_%dx%dx%d" % (wave_t, nx, ny, nz), p, _base_fields(p, ls), steps=2000)

@@ -132,9 +132,11 @@ __device__ __forceinline__ void bc_phase(const CaseDev<T> &c, int phase, V *u, V
                 if (iv) AT(v, 0, j, k) = -AT(v, 1, j, k);
                 if (iw) AT(w, 0, j, k) = -AT(w, 1, j, k);
             }
-            if (c.ccx0 == 3) {       // prescribed: bxy0 = bxz0 = 0 (2_iniciais.f90:384-385); u by k_inflow
+            if (c.ccx0 == 3) {       // prescribed: v = bxy0 = 0 (2_iniciais.f90:384-385), w = bxz0
+                                     // (the waves set it; its plane is one row shorter than w's,
+                                     // the top row reads past it upstream: 0 here); u by k_inflow
                 if (iv) AT(v, 0, j, k) = V(0.);
-                if (iw) AT(w, 0, j, k) = V(0.);
+                if (iw) AT(w, 0, j, k) = (k <= nz + 1) ? V(c.bxz0[j + (long long)(ny + 3) * k]) : V(0.);
             }
             if (c.ccx0 == 4) {       // validation inflow (:333-348)
                 if (iv) AT(v, 0, j, k) = V(0.);

@@ -1,6 +1,7 @@
 // k_keq.cu -- the k-equation model of visco (m_turb = 2 LES, 3 DES;
-// 5_viscosidade.f90:91-145) and the explicit pressure force of the implicit
-// pressure algorithm (exp_press, 11_diversos.f90:455-495).
+// 5_viscosidade.f90:91-145), the explicit pressure force of the implicit
+// pressure algorithm (exp_press, 11_diversos.f90:455-495) and the inflow
+// waves (boundary_waves, 3_contorno.f90:1189-1319).
 //
 // k equation, per RK sub-stage tt = 1..ntt of visco's own loop (velocity,
 // density and the strain sum p1 + p2 + p3 fixed over the loop; k_visco_mu
@@ -267,6 +268,72 @@ __global__ void k_exp_press_acc(const CaseDev<T> *__restrict__ cs, int ncases)
 }
 
 // ---------------------------------------------------------------------------
+// boundary_waves (3_contorno.f90:1189-1319) at time t: the wave on the columns
+// i = 0, 1 over j = 0..ny+1, k = 0..nz+1 (kp(k) = (k - 0.5) dz), in FP64;
+// ls(1, :, :) takes the surface (and its FP64 master in the mixed form),
+// bxx0 / bxz0 the i = 0 velocities, bxx1 the i = 1 u.  Grid: x strides the
+// plane, y = case.
+template <typename T>
+__global__ void k_waves(const CaseDev<T> *__restrict__ cs, int ncases, double t)
+{
+    const CaseDev<T> &c = cs[blockIdx.y];
+    if (c.wave_t <= 0) return;
+    const Geo &g = c.g;
+    const int ny = g.ny, nz = g.nz;
+    const long long pl = ny + 3;
+    const double dx = c.dx, dz = c.dz, a_w = c.a_w, f_w = c.f_w, n_w = c.n_w, h0 = c.h0_f;
+    const long long n = (long long)(ny + 2) * (nz + 2);
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int j = (int)(q % (ny + 2)), k = (int)(q / (ny + 2));
+        const double kp = (k - 0.5) * dz;
+        for (int i = 0; i <= 1; ++i) {
+            const double aux2 = n_w * dx * (i - 0.5) - f_w * t, aux3 = n_w * dx * (i - 1.) - f_w * t;
+            double h_f, u1 = 0., w1 = 0.;
+            if (c.wave_t == 1) {
+                h_f = h0 + a_w * cos(aux2);
+                if (h_f - kp >= 0.) {
+                    u1 = a_w * f_w * cosh(n_w * kp) / sinh(n_w * h0) * cos(aux3);
+                    w1 = a_w * f_w * sinh(n_w * (kp - 0.5 * dz)) / sinh(n_w * h0) * sin(aux2);
+                }
+            } else if (c.wave_t == 2) {
+                const double aux1 = tanh(n_w * h0);
+                h_f = h0 + a_w * cos(aux2) + n_w * a_w * a_w * (3. - aux1 * aux1) / (4. * aux1 * aux1 * aux1) * cos(2. * aux2);
+                if (h_f - kp >= 0.) {
+                    const double s4 = pow(sinh(n_w * h0), 4.);
+                    u1 = a_w * f_w * cosh(n_w * kp) / sinh(n_w * h0) * cos(aux3) +
+                         3. / 4. * a_w * a_w * f_w * n_w * cosh(2. * n_w * kp) / s4 * cos(2. * aux3);
+                    w1 = a_w * f_w * sinh(n_w * (kp - 0.5 * dz)) / sinh(n_w * h0) * sin(aux2) +
+                         3. / 4. * a_w * a_w * f_w * n_w * sinh(2. * n_w * (kp - 0.5 * dz)) / s4 * sin(2. * aux3);
+                }
+            } else {
+                const double aux4 = n_w * kp, aux5 = n_w * (kp - 0.5 * dz);
+                h_f = h0 + c.aeta[0] * cos(aux2) + c.aeta[1] * cos(2. * aux2) + c.aeta[2] * cos(3. * aux2) +
+                      c.aeta[3] * cos(4. * aux2) + c.aeta[4] * cos(5. * aux2);
+                if (h_f - kp >= 0.) {
+                    u1 = c.avel[0] * cosh(aux4) * cos(aux3) + c.avel[1] * cosh(2. * aux4) * cos(2. * aux3) +
+                         c.avel[2] * cosh(3. * aux4) * cos(3. * aux3) + c.avel[3] * cosh(4. * aux4) * cos(4. * aux3) +
+                         c.avel[4] * cosh(5. * aux4) * cos(5. * aux3);
+                    w1 = c.avel[0] * sinh(aux5) * sin(aux2) + c.avel[1] * sinh(2. * aux5) * sin(2. * aux2) +
+                         c.avel[2] * sinh(3. * aux5) * sin(3. * aux2) + c.avel[3] * sinh(4. * aux5) * sin(4. * aux2) +
+                         c.avel[4] * sinh(5. * aux5) * sin(5. * aux2);
+                }
+            }
+            if (i == 1 && j >= 1 && j <= ny && k >= 1 && k <= nz) {
+                const long long qq = g.at(1, j, k);
+                c.ls[qq] = T(h_f - kp);
+                if (c.ls64) c.ls64[qq] = h_f - kp;
+            }
+            if (i == 0) {
+                c.bxx0[j + pl * k] = T(u1);
+                c.bxz0[j + pl * k] = T(w1);
+            } else {
+                c.bxx1[j + pl * k] = T(u1);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 static int plane_blocks(int max_plane)
 {
     int nb = (max_plane + 255) / 256;
@@ -299,6 +366,14 @@ template <typename T> void launch_exp_press(const Batch<T> &b, cudaStream_t s)
     k_exp_press_acc<T><<<grid, 256, 0, s>>>(b.dcases, b.ncases); count_launch();
 }
 
+template <typename T> void launch_waves(const Batch<T> &b, double t, cudaStream_t s)
+{
+    dim3 grid(plane_blocks(b.max_plane), b.ncases);
+    k_waves<T><<<grid, 256, 0, s>>>(b.dcases, b.ncases, t); count_launch();
+}
+
+template void launch_waves<float>(const Batch<float> &, double, cudaStream_t);
+template void launch_waves<double>(const Batch<double> &, double, cudaStream_t);
 template void launch_contorno_les<float>(const Batch<float> &, cudaStream_t);
 template void launch_contorno_les<double>(const Batch<double> &, cudaStream_t);
 template void launch_keq<float>(const Batch<float> &, int, const double *, cudaStream_t);

@@ -101,7 +101,7 @@ extern "C" int suli_field_shape(const suli_params *p, int f, int lo[3], int hi[3
     case SULI_F_ZMU: case SULI_F_FW: case SULI_F_W0: case SULI_F_FW0: case SULI_F_FW1: case SULI_F_TF_W:
     case SULI_F_OBS_LSZ: case SULI_F_ID_IBMZ: case SULI_F_PZ:
         set(1, nx, 1, ny, 1, nz1); break;
-    case SULI_F_BXX0: case SULI_F_BXX1: set(0, ny + 1, 0, nz + 1, 0, 0); break;
+    case SULI_F_BXX0: case SULI_F_BXX1: case SULI_F_BXZ0: set(0, ny + 1, 0, nz + 1, 0, 0); break;
     case SULI_F_BLX1: set(1, ny, 1, nz, 0, 0); break;
     case SULI_F_OBS_LS: set(1, nx1, 1, ny1, 1, nz1); break;
     default: return fail(SULI_BAD_ARG, "unknown field id " + std::to_string(f));
@@ -113,7 +113,10 @@ static bool is_int_field(int f)
 {
     return f == SULI_F_ID_IBMX || f == SULI_F_ID_IBMY || f == SULI_F_ID_IBMZ || f == SULI_F_ID_IBM;
 }
-static bool is_plane_field(int f) { return f == SULI_F_BXX0 || f == SULI_F_BXX1 || f == SULI_F_BLX1; }
+static bool is_plane_field(int f)
+{
+    return f == SULI_F_BXX0 || f == SULI_F_BXX1 || f == SULI_F_BLX1 || f == SULI_F_BXZ0;
+}
 
 static int validate(const suli_params &p)
 {
@@ -141,6 +144,8 @@ static int validate(const suli_params &p)
     if (p.cg_max_iter < 1) return bad("cg_max_iter must be >= 1");
     if (p.t_tens != 0 && p.t_tens != 1) return bad("t_tens must be 0 or 1");
     if (p.esp_type < 0 || p.esp_type > 2) return bad("esp_type must be 0, 1 or 2");
+    if (!(p.wave_t == 0 || p.wave_t == 1 || p.wave_t == 2 || p.wave_t == 5)) return bad("wave_t must be 0, 1, 2 or 5");
+    if (p.wave_t > 0 && !(p.n_w > 0 && p.h0_f > 0)) return bad("wave_t > 0 needs waves_coef's n_w > 0 and h0_f > 0");
     if ((long long)p.nx * p.ny * p.nz > (1LL << 31) - 1) return bad("grid larger than 2^31 cells");
     return SULI_OK;
 }
@@ -172,6 +177,7 @@ struct ImplBase {
     virtual int exp_press() = 0;
     virtual int contorno_les() = 0;
     virtual bool stored(int icase, int f) = 0;
+    virtual int boundary_waves() = 0;
     unsigned long long inflow_calls = 0;
     int ncases = 0;
     std::vector<suli_params> P;
@@ -424,6 +430,9 @@ struct Impl : ImplBase {
             cd.cmu = q.cmu; cd.cdes = q.cdes; cd.lcar = q.lcar; cd.delta = cd.dx1;
             cd.t_press = q.t_press;
             cd.esp_type = q.esp_type;
+            cd.wave_t = q.wave_t;
+            cd.a_w = q.a_w; cd.f_w = q.f_w; cd.n_w = q.n_w; cd.h0_f = q.h0_f;
+            for (int m = 0; m < 5; ++m) { cd.aeta[m] = q.aeta[m]; cd.avel[m] = q.avel[m]; }
             cd.ipa = (q.t_press == 2 && (q.mms_t == 0 || q.project_under_mms)) ? 1 : 0;
             cd.reinit_max = q.reinit_max_iter; cd.cg_max = q.cg_max_iter; cd.cg_tol_mode = q.cg_tol_mode;
             cd.cg_tol = q.cg_tol;
@@ -440,14 +449,14 @@ struct Impl : ImplBase {
                         &cd.hsx, &cd.hsy, &cd.hsz, &cd.kurv, &cd.nlx, &cd.nly, &cd.nlz};
             const int ntf = sizeof(tf) / sizeof(tf[0]);
             int **itf[] = {&cd.id_ibmx, &cd.id_ibmy, &cd.id_ibmz, &cd.id_ibm};
-            T **ptf[] = {&cd.bxx0, &cd.bxx1, &cd.blx1};
+            T **ptf[] = {&cd.bxx0, &cd.bxx1, &cd.blx1, &cd.bxz0};
             const bool mixed = (sizeof(T) == 4);
             const bool mg = mixed && q.mixed_precond == 1;
             // k equation (m_turb >= 2) and IPA (t_press = 2) arrays only where used
             T **kf[] = {&cd.ka, &cd.nut, &cd.sij, &cd.ka0, &cd.fk0, &cd.fk1, &cd.fka};
             T **af[] = {&cd.prd0, &cd.px, &cd.py, &cd.pz};
             const int nkf = (q.m_turb >= 2) ? 7 : 0, naf = (q.t_press == 2) ? 4 : 0, nsf = (q.esp_type > 0) ? 1 : 0;
-            size_t bytes = fb * (ntf + nkf + naf + nsf) + ib * 4 + pb * 3 + (mixed ? 20 * db : 0) + (mg ? 8 * fb : 0);
+            size_t bytes = fb * (ntf + nkf + naf + nsf) + ib * 4 + pb * 4 + (mixed ? 20 * db : 0) + (mg ? 8 * fb : 0);
             void *slab = nullptr;
             CK(cudaMalloc(&slab, bytes));
             slabs.push_back(slab);
@@ -455,7 +464,7 @@ struct Impl : ImplBase {
             char *cur = (char *)slab;
             for (int f = 0; f < ntf; ++f) { *tf[f] = (T *)cur; cur += fb; }
             for (int f = 0; f < 4; ++f) { *itf[f] = (int *)cur; cur += ib; }
-            for (int f = 0; f < 3; ++f) { *ptf[f] = (T *)cur; cur += pb; }
+            for (int f = 0; f < 4; ++f) { *ptf[f] = (T *)cur; cur += pb; }
             for (int f = 0; f < nkf; ++f) { *kf[f] = (T *)cur; cur += fb; }
             for (int f = 0; f < naf; ++f) { *af[f] = (T *)cur; cur += fb; }
             if (nsf) { cd.epis = (T *)cur; cur += fb; }
@@ -739,6 +748,7 @@ struct Impl : ImplBase {
         case SULI_F_ID_IBM: return c.id_ibm;
         case SULI_F_BXX0: return c.bxx0;
         case SULI_F_BXX1: return c.bxx1;
+        case SULI_F_BXZ0: return c.bxz0;
         case SULI_F_BLX1: return c.blx1;
         default: return nullptr;
         }
@@ -975,6 +985,18 @@ struct Impl : ImplBase {
         return SULI_OK;
     }
     bool stored(int icase, int f) override { return dev_ptr(icase, f) != nullptr; }
+    bool any_waves() const
+    {
+        for (const auto &q : P) if (q.wave_t > 0) return true;
+        return false;
+    }
+    int boundary_waves() override
+    {
+        if (!any_waves()) return SULI_OK;
+        launch_waves<T>(b, t, st);
+        CKL();
+        return SULI_OK;
+    }
     int convdiff(int fuse) override
     {
         if (fuse) launch_sponge<T>(b, st);     // complementos' sponge_layer call
@@ -1192,6 +1214,7 @@ struct Impl : ImplBase {
                 if ((rc = set_stage(q))) return rc;
                 if ((rc = convdiff(1))) return rc;
                 if ((rc = tempo())) return rc;
+                if ((rc = boundary_waves())) return rc;          // wave_t > 0, :93
                 if ((rc = contorno(2))) return rc;
                 if (P[0].mms_t == 0 || P[0].project_under_mms) {
                     if (P[0].t_press == 1) {
@@ -1368,6 +1391,7 @@ extern "C" int suli_graddin(suli_handle *h, int32_t *iters) { HCHK(); return h->
 extern "C" int suli_posdin(suli_handle *h) { HCHK(); return h->impl->posdin(); }
 extern "C" int suli_exp_press(suli_handle *h) { HCHK(); return h->impl->exp_press(); }
 extern "C" int suli_contorno_les(suli_handle *h) { HCHK(); return h->impl->contorno_les(); }
+extern "C" int suli_boundary_waves(suli_handle *h) { HCHK(); return h->impl->boundary_waves(); }
 extern "C" int suli_conmassa(suli_handle *h, double *m) { HCHK(); return h->impl->conmassa(m); }
 extern "C" int suli_mms_error(suli_handle *h, double err[4])
 {

@@ -130,6 +130,8 @@ struct CaseDev {
     int t_tempo, m_turb, mms_t, ibm_t, obst_t, t_tens;
     int t_press, ipa;           // ipa: t_press = 2 and the step projects (exp_press / IPA graddin)
     int esp_type;               // sponge layer (0 none)
+    int wave_t;                 // inflow waves (0 none, 1/2 Stokes I/II, 5 Stokes V)
+    double a_w, f_w, n_w, h0_f, aeta[5], avel[5];   // waves_coef's results
     int reinit_max, cg_max, cg_tol_mode;
     double cg_tol;
     // fields (reference module arrays)
@@ -150,7 +152,7 @@ struct CaseDev {
     // sponge layer (esp_type > 0, else null): epis_z on the w faces
     T *epis;
     int *id_ibmx, *id_ibmy, *id_ibmz, *id_ibm;
-    T *bxx0, *bxx1, *blx1;      // inflow planes, indexed at(0, j, k)
+    T *bxx0, *bxx1, *blx1, *bxz0;   // inflow planes, element (j, k) at j + (ny + 3) k
     // CG work arrays
     T *spi, *spj, *spk, *dpr, *e, *r, *p, *mp, *qpr;
     double *e64, *r64;          // mixed form: FP64 refined solution (after the solve: the FP64

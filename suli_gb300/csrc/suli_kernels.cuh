@@ -56,6 +56,7 @@ template <typename T> void launch_visco(const Batch<T> &b, int keq_stages, const
 template <typename T> void launch_keq(const Batch<T> &b, int ntt, const double *a_dt, cudaStream_t s);
 template <typename T> void launch_contorno_les(const Batch<T> &b, cudaStream_t s);
 template <typename T> void launch_exp_press(const Batch<T> &b, cudaStream_t s);
+template <typename T> void launch_waves(const Batch<T> &b, double t, cudaStream_t s);
 template <typename T> void launch_convdiff(const Batch<T> &b, int fuse_compl, cudaStream_t s);
 // sponge_layer's epis_z for the esp_type > 0 cases (before complementos)
 template <typename T> void launch_sponge(const Batch<T> &b, cudaStream_t s);

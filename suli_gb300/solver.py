@@ -30,7 +30,7 @@ EXPORTS = [
     "suli_last_error", "suli_device_info", "suli_get_stream", "suli_profile", "suli_profile_read",
     "suli_ibm_setup", "suli_conmassa_noalloc", "suli_time_kernel", "suli_upload_fields",
     "suli_download_fields", "suli_write_fields", "suli_restart_save", "suli_restart_load",
-    "suli_exp_press", "suli_contorno_les",
+    "suli_exp_press", "suli_contorno_les", "suli_boundary_waves",
 ]
 
 
@@ -71,7 +71,7 @@ def load_library(path: str = LIB_PATH):
     L.suli_set_replay.argtypes = [C.c_void_p, P(i32), i32]
     for name in ("suli_heaviside_init", "suli_ibm_setup", "suli_level_set", "suli_visco", "suli_convdiff",
                  "suli_complementos", "suli_tempo", "suli_posdin", "suli_synchronize", "suli_exp_press",
-                 "suli_contorno_les"):
+                 "suli_contorno_les", "suli_boundary_waves"):
         getattr(L, name).argtypes = [C.c_void_p]
     L.suli_contorno.argtypes = [C.c_void_p, C.c_int]
     L.suli_graddin.argtypes = [C.c_void_p, P(i32)]
@@ -250,6 +250,10 @@ class SuliGPU:
     def contorno_les(self):
         """contorno_les (3_contorno.f90:666-790) on the m_turb >= 2 cases."""
         _check(load_library().suli_contorno_les(self._h))
+
+    def boundary_waves(self):
+        """boundary_waves (3_contorno.f90:1189-1319) on the wave_t > 0 cases."""
+        _check(load_library().suli_boundary_waves(self._h))
 
     def conmassa(self) -> float:
         m = C.c_double()

@@ -6,7 +6,7 @@ import pyoracle
 
 STATE_FIELDS = ["U", "V", "W", "PRD1", "PRD", "LS", "HS", "RHO", "LS_MU", "MU", "MUT", "XMU", "YMU", "ZMU",
                 "FU", "FV", "FW", "U0", "V0", "W0", "FU0", "FV0", "FW0", "FU1", "FV1", "FW1",
-                "TF_U", "TF_V", "TF_W", "HSX", "HSY", "HSZ", "KURV"]
+                "TF_U", "TF_V", "TF_W", "HSX", "HSY", "HSZ", "KURV", "BXX0", "BXX1", "BXZ0", "BLX1"]
 
 
 def rel_l2(a, b):

@@ -54,7 +54,10 @@ def test_default_params_agree(lib):
     lib.suli_default_params(C.byref(a))
     b = _abi.default_params()
     for name, _ in _abi.SuliParams._fields_:
-        assert getattr(a, name) == getattr(b, name), name
+        x, y = getattr(a, name), getattr(b, name)
+        if hasattr(x, "__len__"):        # fixed-size arrays (the Stokes V coefficients)
+            x, y = list(x), list(y)
+        assert x == y, name
 
 
 def test_no_cpu_fallback_without_device(lib):
