@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="ensemble", choices=["ensemble", "wave_tank", "dam_break"])
+    ap.add_argument("--workload", default="ensemble", choices=["ensemble", "wave_tank", "dam_break", "k_channel"])
     ap.add_argument("--ncases", type=int, default=256)
     ap.add_argument("--precond", default="multigrid", choices=["multigrid", "jacobi"],
                     help="inner FP32 passes of the mixed form")
@@ -82,6 +82,9 @@ def make_cases(args, precision, rank=0):
     elif args.workload == "wave_tank":
         cs = [cases.wave_tank(precision=precision)]
         name = "wave_tank_1024x256x256"
+    elif args.workload == "k_channel":
+        cs = [cases.k_channel(256, 64, 128, m_turb=2, precision=precision)]
+        name = "k_channel_les_256x64x128"
     else:
         cs = [cases.dam_break(precision=precision)]
         name = "dam_break_64x32x32"

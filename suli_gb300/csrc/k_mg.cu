@@ -28,6 +28,7 @@
 // cases that have converged cost nothing.
 #include "suli_kernels.cuh"
 
+#include <algorithm>
 #include <cstdlib>
 
 namespace suli {
@@ -462,6 +463,145 @@ __global__ void __launch_bounds__(NTHREADS) k_mg_prolong(const CaseDev<T> *__res
     });
 }
 
+// The coarse end of the V-cycle in one thread block per active case: from
+// level lc (small enough for one SM) down to the coarsest and back, each
+// half-sweep, restriction and prolongation a block-wide loop over the
+// level's cells with a barrier between them (a block's global writes are
+// visible to the block after __syncthreads).  Per cell the same arithmetic
+// as k_mg_smooth's tile path, k_mg_restrict and k_mg_prolong, in the same
+// order of phases; it replaces about ten launches per level.
+template <typename T>
+__device__ __forceinline__ void mg_cell_ijk(const Geo &g, int t, int &i, int &j, int &k)
+{
+    i = 1 + t % g.nx;
+    const int r = t / g.nx;
+    j = 1 + r % g.ny;
+    k = 1 + r / g.ny;
+}
+
+template <typename T>
+__device__ void mg_block_smooth(const CaseDev<T> &c, const MgLev<T> &L, int color, int zero)
+{
+    const Geo &g = L.g;
+    const int nx = g.nx, ny = g.ny, n = nx * ny * g.nz;
+    const long long sx = g.sx, sxy = g.sxy;
+    const bool wx = c.ccx0 == 0 && !(nx & 1) && nx > 1;
+    const bool wy = c.ccy0 == 0 && !(ny & 1) && ny > 1;
+    const T *z = L.z;
+    for (int t = threadIdx.x + blockDim.x * threadIdx.y; t < n; t += blockDim.x * blockDim.y) {
+        int i, j, k;
+        mg_cell_ijk<T>(g, t, i, j, k);
+        const long long qq = g.at(i, j, k);
+        const bool mine = ((i + j + k) & 1) == color;
+        if (zero) {
+            const T di = L.dgi[qq], fv = L.f[qq];
+            L.z[qq] = mine ? fv * di : T(0);
+            continue;
+        }
+        if (!mine) continue;
+        const long long qxm = (wx && i == 1) ? qq + (nx - 1) : qq - 1;
+        const long long qxp = (wx && i == nx) ? qq - (nx - 1) : qq + 1;
+        const long long qym = (wy && j == 1) ? qq + (long long)(ny - 1) * sx : qq - sx;
+        const long long qyp = (wy && j == ny) ? qq - (long long)(ny - 1) * sx : qq + sx;
+        const T di = L.dgi[qq];
+        const T sm = L.f[qq] + L.cx[qq] * z[qxm] + L.cx[qq + 1] * z[qxp] + L.cy[qq] * z[qym] + L.cy[qq + sx] * z[qyp] +
+                     L.cz[qq] * z[qq - sxy] + L.cz[qq + sxy] * z[qq + sxy];
+        L.z[qq] = sm * di;
+    }
+    __syncthreads();
+}
+
+template <typename T>
+__device__ void mg_block_restrict(const CaseDev<T> &c, const MgLev<T> &F, const MgLev<T> &C)
+{
+    const int fx = F.g.nx, fy = F.g.ny, fz = F.g.nz;
+    const int sx = (int)F.g.sx, sxy = (int)F.g.sxy;
+    const bool wx = c.ccx0 == 0 && fx > 1, wy = c.ccy0 == 0 && fy > 1;
+    const T *__restrict__ z = F.z;
+    const int n = C.g.nx * C.g.ny * C.g.nz;
+    for (int t = threadIdx.x + blockDim.x * threadIdx.y; t < n; t += blockDim.x * blockDim.y) {
+        int I, J, K;
+        mg_cell_ijk<T>(C.g, t, I, J, K);
+        T acc = T(0);
+#pragma unroll
+        for (int d = 0; d < 8; ++d) {
+            const int i0 = 2 * I - 1 + (d & 1), j0 = 2 * J - 1 + ((d >> 1) & 1), k0 = 2 * K - 1 + (d >> 2);
+            const bool in = i0 <= fx && j0 <= fy && k0 <= fz;
+            const int i = min(i0, fx), j = min(j0, fy), k = min(k0, fz);
+            const int q = (int)F.g.at(i, j, k);
+            const int qxm = (wx && i == 1) ? q + (fx - 1) : q - 1;
+            const int qxp = (wx && i == fx) ? q - (fx - 1) : q + 1;
+            const int qym = (wy && j == 1) ? q + (fy - 1) * sx : q - sx;
+            const int qyp = (wy && j == fy) ? q - (fy - 1) * sx : q + sx;
+            const T r = F.f[q] - F.dg[q] * z[q] + F.cx[q] * z[qxm] + F.cx[q + 1] * z[qxp] + F.cy[q] * z[qym] +
+                        F.cy[q + sx] * z[qyp] + F.cz[q] * z[q - sxy] + F.cz[q + sxy] * z[q + sxy];
+            acc += in ? r : T(0);
+        }
+        C.f[C.g.at(I, J, K)] = acc;
+    }
+    __syncthreads();
+}
+
+template <typename T>
+__device__ void mg_block_prolong(const MgLev<T> &F, const MgLev<T> &C)
+{
+    const int n = F.g.nx * F.g.ny * F.g.nz;
+    for (int t = threadIdx.x + blockDim.x * threadIdx.y; t < n; t += blockDim.x * blockDim.y) {
+        int i, j, k;
+        mg_cell_ijk<T>(F.g, t, i, j, k);
+        const long long q = F.g.at(i, j, k);
+        F.z[q] = F.z[q] + C.z[C.g.at((i + 1) >> 1, (j + 1) >> 1, (k + 1) >> 1)];
+    }
+    __syncthreads();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_mg_coarse(const CaseDev<T> *__restrict__ cs, const int *__restrict__ tab,
+                                                        int lc, int NL, int nuc, int ncoarse)
+{
+    const int n = tab[0];
+    for (int a = blockIdx.x; a < n; a += gridDim.x) {
+        const CaseDev<T> &c = cs[tab[1 + a]];
+        for (int l = lc; l + 1 < NL; ++l) {
+            for (int it = 0; it < nuc; ++it) {
+                mg_block_smooth<T>(c, c.mg[l], 0, it == 0);
+                mg_block_smooth<T>(c, c.mg[l], 1, 0);
+            }
+            mg_block_restrict<T>(c, c.mg[l], c.mg[l + 1]);
+        }
+        for (int it = 0; it < ncoarse; ++it) {
+            mg_block_smooth<T>(c, c.mg[NL - 1], 0, it == 0);
+            mg_block_smooth<T>(c, c.mg[NL - 1], 1, 0);
+        }
+        for (int l = NL - 2; l >= lc; --l) {
+            mg_block_prolong<T>(c.mg[l], c.mg[l + 1]);
+            for (int it = 0; it < nuc; ++it) {
+                mg_block_smooth<T>(c, c.mg[l], 1, 0);
+                mg_block_smooth<T>(c, c.mg[l], 0, 0);
+            }
+        }
+    }
+}
+
+// first level handled by k_mg_coarse: the first whose largest grid over the
+// batch has at most SULI_MG_CTA_CELLS cells (default 16384; 0: none, every
+// level by whole-grid launches); at least 1, at most NL (none)
+template <typename T> int mg_block_level(const Batch<T> &b)
+{
+    const char *e = std::getenv("SULI_MG_CTA_CELLS");
+    const int limit = e ? std::atoi(e) : 16384;
+    if (limit <= 0) return b.nlev;
+    for (int l = 1; l < b.nlev; ++l) {
+        long long mx = 0;
+        for (int c = 0; c < b.ncases; ++c) {
+            const Geo &g = b.hcases[c].mg[l].g;
+            mx = std::max<long long>(mx, (long long)g.nx * g.ny * g.nz);
+        }
+        if (mx <= limit) return l;
+    }
+    return b.nlev;
+}
+
 // coarse conductances of level l from level l-1 (all cases of the batch;
 // once per pressure solve, after the case grid's level 0 is written)
 template <typename T>
@@ -567,7 +707,11 @@ template <typename T> void launch_mg_vcycle(const Batch<T> &b, const int *tab, i
     const bool fused = !(fe && std::atoi(fe) == 0);
     static const int gW = sweep0_grid<T>();
     const int ncoarse = 6;
-    for (int l = 0; l + 1 < NL; ++l) {
+    // levels lc.. in one block per case (k_mg_coarse), the finer ones by
+    // whole-grid launches
+    const int lc = mg_block_level<T>(b);
+    const int ldown = (lc < NL) ? lc : NL - 1;    // levels smoothed by launches before the coarse end
+    for (int l = 0; l < ldown; ++l) {
         const int nu = (l == 0) ? nu0 : nuc;
         if (l == 0 && fused) {
             // the buffers alternate so that the last sweep writes z
@@ -586,12 +730,17 @@ template <typename T> void launch_mg_vcycle(const Batch<T> &b, const int *tab, i
         k_mg_restrict<T><<<gR, b.cblock(), 0, s>>>(b.dcases, tab, N, l + 1);
         count_launch(2 * nu + 1);
     }
-    for (int it = 0; it < ncoarse; ++it) {
-        launch_smooth<T>(b, tab, NL - 1, 0, it == 0, s);
-        launch_smooth<T>(b, tab, NL - 1, 1, 0, s);
+    if (lc < NL) {
+        k_mg_coarse<T><<<N, b.cblock(), 0, s>>>(b.dcases, tab, lc, NL, nuc, ncoarse);
+        count_launch();
+    } else {
+        for (int it = 0; it < ncoarse; ++it) {
+            launch_smooth<T>(b, tab, NL - 1, 0, it == 0, s);
+            launch_smooth<T>(b, tab, NL - 1, 1, 0, s);
+        }
+        count_launch(2 * ncoarse);
     }
-    count_launch(2 * ncoarse);
-    for (int l = NL - 2; l >= 0; --l) {
+    for (int l = ldown - 1; l >= 0; --l) {
         const int nu = (l == 0) ? nu0 : nuc;
         if (l == 0 && fused) {
             // black then red; the prolongation writes the buffer the first

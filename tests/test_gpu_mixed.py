@@ -349,3 +349,40 @@ def test_batched_transfers_match_single(gpu_lib, precision):
         else:                                              # FP32 storage
             assert np.array_equal(b, a.astype(np.float32).astype(np.float64)), (n, i)
     g.close()
+
+
+@pytest.mark.parametrize("mk", ["periodic_odd", "uneven_batch", "k_channel"])
+def test_block_coarse_levels_match_launches(gpu_lib, monkeypatch, mk):
+    """The coarse end of the V-cycle in one thread block per case (default:
+    the levels of at most 16384 cells) does the arithmetic of the whole-grid
+    launches (SULI_MG_CTA_CELLS=0): same pressures and velocities to FP32
+    round-off, same iteration counts."""
+    def mk_cases():
+        if mk == "periodic_odd":
+            return [cases.mms_case(25, precision=PREC_MIXED)]
+        if mk == "k_channel":
+            return [cases.k_channel(64, 16, 32, m_turb=2, precision=PREC_MIXED)]
+        dims, hcol, amp = cases.ensemble_dims(5, seed=11, lo=13, hi=40)
+        return [cases.ensemble_case(i, dims, hcol, amp, precision=PREC_MIXED) for i in range(5)]
+    out = {}
+    for cells in ("0", "16384"):
+        monkeypatch.setenv("SULI_MG_CTA_CELLS", cells)
+        cs = mk_cases()
+        for c in cs:
+            c.params.mixed_precond = 1
+            c.params.cg_tol_mode = 1
+            c.params.cg_tol = 1e-9
+        g = gpu_lib.SuliGPU([c.params for c in cs])
+        g.start([c.fields for c in cs])
+        g.step(2)
+        out[cells] = ([g.download("PRD1", i)[1:-1, 1:-1, 1:-1] for i in range(len(cs))],
+                      np.concatenate([g.download("U", i).ravel() for i in range(len(cs))]),
+                      list(g.diag(0).cg_iters))
+        g.close()
+    same = all(np.array_equal(a, b) for a, b in zip(out["0"][0], out["16384"][0]))
+    print("block coarse levels vs launches (%s): bit-identical pressure: %s, iterations %s / %s"
+          % (mk, same, out["0"][2], out["16384"][2]))
+    for a, b in zip(out["0"][0], out["16384"][0]):
+        assert rel_l2(a - a.mean(), b - b.mean()) < 1e-6
+    assert rel_l2(out["0"][1], out["16384"][1]) < 1e-6
+    assert all(abs(x - y) <= 1 for x, y in zip(out["0"][2], out["16384"][2]))
