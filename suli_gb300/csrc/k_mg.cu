@@ -555,8 +555,10 @@ __device__ void mg_block_prolong(const MgLev<T> &F, const MgLev<T> &C)
     __syncthreads();
 }
 
+constexpr int MG_COARSE_THREADS = 1024;   // per block: a few cells per thread on a 16k-cell level
+
 template <typename T>
-__global__ void __launch_bounds__(NTHREADS) k_mg_coarse(const CaseDev<T> *__restrict__ cs, const int *__restrict__ tab,
+__global__ void __launch_bounds__(MG_COARSE_THREADS) k_mg_coarse(const CaseDev<T> *__restrict__ cs, const int *__restrict__ tab,
                                                         int lc, int NL, int nuc, int ncoarse)
 {
     const int n = tab[0];
@@ -731,7 +733,7 @@ template <typename T> void launch_mg_vcycle(const Batch<T> &b, const int *tab, i
         count_launch(2 * nu + 1);
     }
     if (lc < NL) {
-        k_mg_coarse<T><<<N, b.cblock(), 0, s>>>(b.dcases, tab, lc, NL, nuc, ncoarse);
+        k_mg_coarse<T><<<N, MG_COARSE_THREADS, 0, s>>>(b.dcases, tab, lc, NL, nuc, ncoarse);
         count_launch();
     } else {
         for (int it = 0; it < ncoarse; ++it) {
