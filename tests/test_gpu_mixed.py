@@ -63,15 +63,18 @@ def test_mixed_surface_tension_against_oracle(gpu_lib):
     assert ev <= 3e-5 and els <= 1e-7 and ek <= 1e-5
 
 
-@pytest.mark.parametrize("which", ["k_les", "k_des", "ipa"])
+@pytest.mark.parametrize("which", ["k_les", "k_des", "ipa", "sponge"])
 def test_mixed_keq_ipa_against_oracle(gpu_lib, which):
-    """The k equation (FP32 ka, nut and sub-stage buffers) and the IPA (FP32
-    prd0 and force) in the mixed form, 10 steps, against the FP64 oracle."""
+    """The k equation (FP32 ka, nut and sub-stage buffers), the IPA (FP32
+    prd0 and force) and the sponge layer (FP32 epis_z) in the mixed form, 10
+    steps, against the FP64 oracle."""
     nsteps = 10
 
     def make(prec):
         if which == "ipa":
             return cases.ipa_tank(16, 6, 12, precision=prec)
+        if which == "sponge":
+            return cases.sponge_tank(32, 4, 16, esp_type=1, precision=prec)
         return cases.k_channel(24, 6, 12, m_turb=2 if which == "k_les" else 3, precision=prec)
 
     case = make(PREC_FP64)
@@ -88,6 +91,8 @@ def test_mixed_keq_ipa_against_oracle(gpu_lib, which):
         # at different values: compare it without its mean
         a, b = g.download("PRD0")[1:-1, 1:-1, 1:-1], o.field("PRD0")[1:-1, 1:-1, 1:-1]
         extra = {"PRD0": rel_l2(a - a.mean(), b - b.mean())}
+    elif which == "sponge":
+        extra = {"LS": rel_l2(g.download("LS"), o.field("LS"))}
     else:
         extra = {n: rel_l2(g.download(n), o.field(n)) for n in ("KA", "NUT")}
     g.close()
@@ -135,6 +140,24 @@ def test_batch_equals_single_cases(gpu_lib):
             assert np.array_equal(a, b) or rel_l2(a, b) < 1e-12, (i, name, rel_l2(a, b))
         gs.close()
     gb.close()
+
+
+def test_mixed_boundary_waves(gpu_lib):
+    """The Stokes V inflow planes in the mixed form (FP64 wave, stored once
+    rounded) against the oracle's."""
+    case = cases.wave_flume(24, 4, 16, wave_t=5)
+    o = oracle_for(case)
+    cm = cases.wave_flume(24, 4, 16, wave_t=5, precision=PREC_MIXED)
+    g = gpu_lib.SuliGPU(cm.params)
+    g.start(cm.fields)
+    for t in (0.2, 1.1):
+        o.set_scalar("T", t)
+        g.set_scalar("T", t)
+        o.boundary_waves()
+        g.boundary_waves()
+        for n in ("BXX0", "BXX1", "BXZ0"):
+            assert rel_l2(g.download(n), o.field(n)) <= 1e-7, n
+    g.close()
 
 
 def test_batch_mixes_turbulence_models(gpu_lib):
