@@ -19,8 +19,9 @@ the FP64 form on the 64x32x32 dam break after 200 steps, "output" times
 the field records (PRTSCR) of 16 cases and a restart save + load outside
 the timed region, "surface_tension" the capillary column with and without
 t_tens, "models" the open channel under each visco model (none, Smagorinsky,
-k-equation LES, DES) and the still-water tank under the projection and the
-IPA, and cpu_baseline is the oracle (a port of the reference,
+k-equation LES, DES), the still-water tank under the projection and the
+IPA and the sloshing tank with and without a sponge layer, and cpu_baseline
+is the oracle (a port of the reference,
 OpenMP where the reference has it) on a bounded sample.
 
 --impl reference times the reference's CPU implementation (the oracle port:
@@ -335,15 +336,18 @@ def tension_run(torch, steps=10, warmup=3):
 
 
 def models_run(torch, steps=10, warmup=3):
-    """The k-equation model and the implicit pressure algorithm outside the
-    timed region, mixed form, cell-steps/s: the open channel (256 x 64 x 128)
-    with m_turb = 0 (none), 1 (Smagorinsky), 2 (k-equation LES), 3 (DES); the
-    tilted still-water tank (256 x 64 x 128) with t_press = 1 (projection,
-    three graddin + posdin per step) and 2 (IPA: exp_press, one graddin)."""
+    """The k-equation model, the implicit pressure algorithm and the sponge
+    layer outside the timed region, mixed form, cell-steps/s: the open
+    channel (256 x 64 x 128) with m_turb = 0 (none), 1 (Smagorinsky), 2
+    (k-equation LES), 3 (DES); the tilted still-water tank (256 x 64 x 128)
+    with t_press = 1 (projection, three graddin + posdin per step) and 2
+    (IPA: exp_press, one graddin); the sloshing tank (256 x 32 x 128) with
+    esp_type = 0, 1, 2."""
     from suli_gb300 import cases
     from suli_gb300._abi import PREC_MIXED
     out = {"k_equation": {"workload": "k_channel_256x64x128", "steps": steps},
-           "ipa": {"workload": "ipa_tank_256x64x128", "steps": steps}}
+           "ipa": {"workload": "ipa_tank_256x64x128", "steps": steps},
+           "sponge": {"workload": "sponge_tank_256x32x128", "steps": steps}}
     for m in (0, 1, 2, 3):
         c = cases.k_channel(256, 64, 128, m_turb=max(m, 2), precision=PREC_MIXED)
         c.params.m_turb = m
@@ -366,6 +370,19 @@ def models_run(torch, steps=10, warmup=3):
         g.close()
         out["ipa"]["t_press_%d" % tp] = {"value": c.cells * steps / (ms / 1e3), "ms_per_step": ms / steps,
                                          "cg_iters_last_step": list(d.cg_iters)}
+    for esp in (0, 1, 2):
+        c = cases.sponge_tank(256, 32, 128, esp_type=esp, precision=PREC_MIXED)
+        g = start_gpu([c])
+        g.step(warmup)
+        ms = timed_steps(g, steps, torch)
+        d = g.diag()
+        t0 = time.perf_counter()
+        g.complementos()                      # the sponge kernel and the momentum sources alone
+        g.synchronize()
+        g.close()
+        out["sponge"]["esp_type_%d" % esp] = {"value": c.cells * steps / (ms / 1e3), "ms_per_step": ms / steps,
+                                              "cg_iters_last_step": list(d.cg_iters),
+                                              "complementos_ms_host": (time.perf_counter() - t0) * 1e3}
     return out
 
 
