@@ -25,7 +25,15 @@ is the oracle (a port of the reference,
 OpenMP where the reference has it) on a bounded sample.
 
 --impl reference times the reference's CPU implementation (the oracle port:
-no Fortran compiler exists on either machine) on the same workload.
+no Fortran compiler exists on either machine) on the same workload: each
+step is one time step of one case of the workload (a bounded sample), and
+the line reports the same metric, unit and config as this arm.
+
+--gpus N without torchrun starts N ranks itself (torch.distributed.run).
+The ensemble is partitioned: an ensemble of 256 x N cases drawn from seed 0,
+rank r advancing cases r, r + N, r + 2N, ... (256 per rank) with no
+data-path collective; value = all ranks' cell-steps over the slowest rank's
+time (weak scaling: the per-GPU work is fixed as N grows).
 """
 from __future__ import annotations
 
@@ -44,6 +52,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 FALLBACK_HBM_GBS = 6800.0
+# the headline metric, printed identically by both arms
+METRIC = "cell-steps/s, mixed vs FP64 on one GB300 at \u22641e-6 rel L2; CG HBM GB/s"
 
 
 def parse():
@@ -52,11 +62,19 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="ensemble", choices=["ensemble", "wave_tank", "dam_break", "k_channel"])
+    ap.add_argument("--workload", default="ensemble",
+                    choices=["ensemble", "wave_tank", "dam_break", "k_channel", "open_channel"])
     ap.add_argument("--ncases", type=int, default=256)
     ap.add_argument("--precond", default="multigrid", choices=["multigrid", "jacobi"],
                     help="inner FP32 passes of the mixed form")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-jacobi", action="store_true",
+                    help="skip the mixed form with Jacobi-scaled FP32 passes (the precision-only ratio)")
+    ap.add_argument("--side-steps", type=int, default=5,
+                    help="timed steps of the FP64 and Jacobi legs (at most --steps)")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the single-grid configurations (the 512x128x128 open channel with IBM and "
+                         "LES, the 1024x256x256 wave tank) timed in both forms")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -74,24 +92,46 @@ def parse():
 
 
 # ---------------------------------------------------------------------------
-def make_cases(args, precision, rank=0):
+def make_cases(args, precision, rank=0, world=1, precond=None):
+    """The cases rank `rank` of `world` advances.  The ensemble is one draw
+    of ncases x world cases (seed 0) partitioned round-robin across the
+    ranks; the single-grid workloads run as replicas, one per rank."""
     from suli_gb300 import cases
     if args.workload == "ensemble":
-        dims, hcol, amp = cases.ensemble_dims(args.ncases, seed=rank)
-        cs = [cases.ensemble_case(i, dims, hcol, amp, precision=precision) for i in range(args.ncases)]
-        name = "ensemble_%d_U32-96_seed%d" % (args.ncases, rank)
+        n = args.ncases * world
+        cs = ensemble_share(n, rank, world, precision)
+        name = "ensemble_%d_U32-96_seed0" % n
     elif args.workload == "wave_tank":
         cs = [cases.wave_tank(precision=precision)]
         name = "wave_tank_1024x256x256"
     elif args.workload == "k_channel":
         cs = [cases.k_channel(256, 64, 128, m_turb=2, precision=precision)]
         name = "k_channel_les_256x64x128"
+    elif args.workload == "open_channel":
+        cs = [cases.open_channel(512, 128, 128, precision=precision, balanced=True)]
+        name = "open_channel_ibm_les_512x128x128"
     else:
         cs = [cases.dam_break(precision=precision)]
         name = "dam_break_64x32x32"
+    pc = args.precond if precond is None else precond
     for c in cs:
-        c.params.mixed_precond = 1 if args.precond == "multigrid" else 0
+        c.params.mixed_precond = 1 if pc == "multigrid" else 0
     return name, cs
+
+
+def ensemble_share(n, rank, world, precision, lo=32, hi=96):
+    """Rank `rank`'s share of an n-case ensemble (dims U{lo..hi}, seed 0):
+    cases rank, rank + world, rank + 2 world, ... (round-robin, so every rank
+    gets the same mix of sizes)."""
+    from suli_gb300 import cases
+    dims, hcol, amp = cases.ensemble_dims(n, seed=0, lo=lo, hi=hi)
+    return [cases.ensemble_case(i, dims, hcol, amp, precision=precision) for i in range(rank, n, world)]
+
+
+def config_of(args, name, world):
+    """The config object both arms print (the driver compares them)."""
+    return {"workload": name, "cases_per_gpu": args.ncases if args.workload == "ensemble" else 1,
+            "l2": "inputs larger than L2 (working set of GBs per GPU)"}
 
 
 class ClockSampler:
@@ -212,16 +252,18 @@ def job_totals(cells, ms, dist=None, torch=None):
     return float(c.item()), float(m.item())
 
 
-def run_form(args, cs, torch, sampler=None, dist=None):
+def run_form(args, cs, torch, sampler=None, dist=None, steps=None, warmup=None):
+    steps = args.steps if steps is None else steps
+    warmup = args.warmup if warmup is None else warmup
     g = start_gpu(cs)
-    g.step(args.warmup)
+    g.step(warmup)
     g.synchronize()
     if dist is not None:
         dist.barrier()
     g.profile(True)
     if sampler:
         sampler.start()
-    ms = timed_steps(g, args.steps, torch)
+    ms = timed_steps(g, steps, torch)
     clocks = sampler.stop() if sampler else None
     prof = g.profile_read()
     cells = sum(c.cells for c in cs)
@@ -386,6 +428,51 @@ def models_run(torch, steps=10, warmup=3):
     return out
 
 
+def configs_run(args, torch):
+    """The two single-grid configurations outside the timed region, each in
+    the mixed form and the plain FP64 form on the same initial state (3
+    warm-up and a few timed steps each): cell-steps/s of both, their ratio,
+    the pressure iterations, and the mixed form's relative L2 difference from
+    the FP64 form after the last step (the FP64 form is the one held to the
+    oracle at 1e-10 on reduced grids).
+      open channel 512 x 128 x 128, 4 x 1 x 1 m, depth 0.6 m, inflow 0.5 m/s
+        with a seeded 5 % perturbation, balanced free outflow, IBM cylinder
+        D = 0.1 m at x = 1.0, Smagorinsky Cs = 0.1, CG tol 1e-8 relative;
+      wave tank 1024 x 256 x 256 (67 M cells), 8 x 2 x 2 m, depth 1.0 m,
+        surface 0.05 sin(pi x), still water, Smagorinsky LES, CG tol 1e-8
+        relative."""
+    from suli_gb300 import cases
+    from suli_gb300._abi import PREC_FP64, PREC_MIXED
+    builders = {
+        "open_channel_ibm_les_512x128x128": (lambda prec: cases.open_channel(512, 128, 128, precision=prec,
+                                                                             balanced=True), 5),
+        "wave_tank_les_1024x256x256": (lambda prec: cases.wave_tank(precision=prec), 3),
+    }
+    out = {}
+    for name, (make, k) in builders.items():
+        row = {"steps": k, "warmup": 3}
+        gs = {}
+        try:
+            for form, prec in (("mixed", PREC_MIXED), ("fp64", PREC_FP64)):
+                c = make(prec)
+                c.params.mixed_precond = 1 if args.precond == "multigrid" else 0
+                g = start_gpu([c])
+                g.step(3)
+                ms = timed_steps(g, k, torch)
+                d = g.diag()
+                row[form] = {"value": c.cells * k / (ms / 1e3), "ms_per_step": ms / k,
+                             "cg_iters_last_step": list(d.cg_iters), "cg_outer_last_step": list(d.cg_outer)}
+                gs[form] = g
+            row["mixed_over_fp64"] = row["mixed"]["value"] / row["fp64"]["value"]
+            row["mixed_vs_fp64_rel_l2"] = compare_forms(gs["mixed"], gs["fp64"], 1)
+        except Exception as e:  # reported, not hidden
+            row["error"] = repr(e)
+        for g in gs.values():
+            g.close()
+        out[name] = row
+    return out
+
+
 def mms_run(args):
     """The manufactured solution (13_mms.f90, steady) at 32^3, 64^3, 128^3 in
     both forms, args.mms_steps steps each, outside any timed region: RMS
@@ -442,41 +529,125 @@ def e2e_run(args, cs, torch):
             "path": "suli_upload_fields/suli_step/suli_download_fields (C ABI), pinned host buffers"}
 
 
-def cpu_baseline(args, cs):
-    """The oracle (port of the reference) on a bounded sample: the first case
-    of the workload, stepped until ~cpu_seconds of work have been done."""
+def _oracle_case(c):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
-    cores = os.cpu_count() or 1
-    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
-    pyoracle.Oracle.set_threads(cores)
-    c = cs[0]
     p = c.params.copy()
     p.precision = 0
     o = pyoracle.Oracle(p)
     for k, v in c.fields.items():
         o.set_field(k, v)
     o.heaviside_init()
+    if p.ibm_t == 2 and c.obstacle:
+        ob = c.obstacle
+        o.obstaculo_cylinder(ob["xc"], ob["yc"], ob["radius"])
+        o.ibm_setup()
     for n in (1, 2, 3):
         o.contorno(n)
-    o.step(1)
-    steps = 0
+    return o, p
+
+
+def cpu_baseline(args, cs, steps=None, warmup=1):
+    """The oracle (port of the reference, OpenMP where the reference has it)
+    on a bounded sample of the workload: its first case, `warmup` untimed
+    steps, then either exactly `steps` timed steps or, when steps is None,
+    steps until ~cpu_seconds of work have been done.  Wall time per step."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    pyoracle.Oracle.set_threads(cores)
+    c = cs[0]
+    o, p = _oracle_case(c)
+    o.step(max(1, warmup))
+    n = 0
     t0 = time.perf_counter()
     while True:
         o.step(1)
-        steps += 1
-        if time.perf_counter() - t0 > args.cpu_seconds or steps >= 50:
+        n += 1
+        if steps is not None:
+            if n >= steps:
+                break
+        elif time.perf_counter() - t0 > args.cpu_seconds or n >= 50:
             break
     dt = time.perf_counter() - t0
-    return {"value": c.cells * steps / dt, "unit": "cell-steps/s", "cores": cores, "kind": "port",
-            "sample": "%s: %d steps of one %dx%dx%d case, FP64 oracle, OpenMP in CG/interp as upstream"
-                      % (c.name, steps, p.nx, p.ny, p.nz)}
+    return {"value": c.cells * n / dt, "unit": "cell-steps/s", "cores": cores, "kind": "port",
+            "sample": "%s: %d steps of one %dx%dx%d case after %d untimed, FP64 oracle, OpenMP in CG/interp "
+                      "as upstream" % (c.name, n, p.nx, p.ny, p.nz, max(1, warmup)),
+            "steps": n, "ms_per_step": dt * 1e3 / n}
+
+
+def side_legs(args, torch, dist, rank, world, value):
+    """The plain FP64 form and the mixed form with Jacobi-scaled FP32 passes
+    (the reference's own CG in FP32 inside FP64 refinement) on the same
+    workload: the FP64 form's speed, mixed over FP64 (multigrid passes: the
+    precision change plus the preconditioner) and mixed-Jacobi over FP64
+    (the precision change alone)."""
+    from suli_gb300._abi import PREC_FP64, PREC_MIXED
+    out = {}
+    k = max(1, min(args.side_steps, args.steps))
+    legs = []
+    if not args.no_fp64:
+        legs.append(("fp64", PREC_FP64, args.precond))
+    if not args.no_jacobi and args.precond == "multigrid":
+        legs.append(("mixed_jacobi", PREC_MIXED, "jacobi"))
+    for key, prec, pc in legs:
+        try:
+            _, cs = make_cases(args, prec, rank, world, precond=pc)
+            g, ms, prof, _ = run_form(args, cs, torch, None, dist, steps=k, warmup=3)
+            v = g.job_cells * k / (ms / 1e3)
+            leg = {"value": v, "ms_per_step": ms / k, "steps": k, "gpu_launches": int(prof.launches),
+                   "cg_iters_case0": list(g.diag(0).cg_iters)}
+            if key == "fp64":
+                leg["cg_GBs_algorithmic"] = (7 * 8.0 * prof.cg_cell_iters / (prof.cg_ms / 1e3) / 1e9
+                                             if prof.cg_ms > 0 else None)
+            out[key] = (leg, g)
+        except Exception as e:  # reported, not hidden
+            out[key] = ({"error": repr(e)}, None)
+    return out
 
 
 # ---------------------------------------------------------------------------
+def relaunch_distributed(args):
+    """--gpus N > 1 without torchrun: start N ranks (one per GPU) through
+    torch.distributed.run on 127.0.0.1 and return its exit code."""
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", str(args.gpus),
+           "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__)] + sys.argv[1:]
+    return subprocess.call(cmd)
+
+
+def reference_arm(args, rank, world):
+    """--impl reference: the oracle port on this host's cores, on the same
+    metric, unit and config as this arm; each step one time step of the
+    workload's first case (rank 0 only)."""
+    from suli_gb300._abi import PREC_FP64
+    if rank != 0:
+        return
+    name, cs = make_cases(args, PREC_FP64, 0, world)
+    res = cpu_baseline(args, cs, steps=args.steps, warmup=args.warmup)
+    line = {"metric": METRIC, "value": res["value"], "unit": "cell-steps/s", "n_gpus": world,
+            "steps": res["steps"], "warmup": args.warmup, "ms_per_step": res["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": config_of(args, name, world),
+            "e2e": {"value": res["value"], "unit": "cell-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "cpu_baseline": {k: res[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "note": "the reference Fortran cannot be built (no Fortran compiler on either machine): its "
+                    "line-faithful C restatement runs instead; a step is one time step of one case of "
+                    "the workload, so ms_per_step is per case-step"}
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
     assert args.warmup >= 3 or args.impl == "reference", "at least 3 warm-up steps"
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(relaunch_distributed(args))
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -486,22 +657,13 @@ def main():
         import torch.distributed as dist
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
         dist.init_process_group("gloo")
-    from suli_gb300._abi import PREC_FP64, PREC_MIXED
+    from suli_gb300._abi import PREC_MIXED
 
     if args.impl == "reference":
-        if rank != 0:
-            return
-        name, cs = make_cases(args, PREC_FP64)
-        res = cpu_baseline(args, cs) if True else None
-        line = {"metric": "cell-steps/s", "value": res["value"], "unit": "cell-steps/s", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "impl": "reference",
-                "config": {"workload": name, "sample": res["sample"]},
-                "cpu_baseline": res,
-                "e2e": {"value": res["value"], "unit": "cell-steps/s", "h2d_bytes_per_step": 0,
-                        "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
+        reference_arm(args, rank, world)
+        if dist is not None:
+            dist.barrier()
+            dist.destroy_process_group()
         return
 
     import torch
@@ -510,7 +672,7 @@ def main():
     from suli_gb300 import solver
     sms, devname = solver.device_info()
 
-    name, cs_m = make_cases(args, PREC_MIXED, rank)
+    name, cs_m = make_cases(args, PREC_MIXED, rank, world)
     cells = sum(c.cells for c in cs_m)
     if args.profile_kernel >= 0:
         g = start_gpu(cs_m)
@@ -531,17 +693,21 @@ def main():
     value = gm.job_cells * args.steps / (ms_m / 1e3)
     peak, peak_src = measured_peak_hbm()
     line = {
-        "metric": "cell-steps/s (mixed-precision batched SuLi steps)",
+        "metric": METRIC,
         "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_m / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64", "data": "synthetic",
-        "config": {"workload": name, "cases": len(cs_m), "cells_per_gpu": cells, "precision": "mixed",
-                   "mixed_passes": "FP32 CG preconditioned by a multigrid V-cycle" if args.precond == "multigrid"
-                   else "FP32 Jacobi-scaled CG",
-                   "l2": "inputs larger than L2 (working set %.1f GB)" % (cells * 4 * 46 / 1e9),
-                   "device": devname, "sms": sms},
+        "config": config_of(args, name, world),
+        "e2e": None, "roofline": None, "cpu_baseline": None,
+        "fp64": None, "mixed_over_fp64": None, "mixed_jacobi": None, "mixed_jacobi_over_fp64": None,
         "gpu_launches": int(prof_m.launches),
         "clocks": clocks,
+        "run": {"cases": len(cs_m), "cells_per_gpu": cells, "precision": "mixed",
+                "mixed_passes": "FP32 CG preconditioned by a multigrid V-cycle" if args.precond == "multigrid"
+                else "FP32 Jacobi-scaled CG",
+                "working_set_GB": cells * 4 * 46 / 1e9, "device": devname, "sms": sms,
+                "partition": "cases r, r+N, ... of one ensemble on rank r" if args.workload == "ensemble"
+                else "replicas"},
     }
     # roofline of the dominant kernel, timed alone over every case of the
     # workload with CUDA events on the library's stream (burst peak)
@@ -572,21 +738,22 @@ def main():
     diag = gm.diag(0)
     line["cg_iters_case0"] = list(diag.cg_iters)
     line["cg_outer_case0"] = list(diag.cg_outer)
-    if not args.no_fp64:
-        try:
-            name64, cs_64 = make_cases(args, PREC_FP64, rank)
-            g64, ms_64, prof_64, _ = run_form(args, cs_64, torch, None, dist)
-            v64 = g64.job_cells * args.steps / (ms_64 / 1e3)
-            line["fp64"] = {"value": v64, "ms_per_step": ms_64 / args.steps,
-                            "cg_GBs_algorithmic": (7 * 8.0 * prof_64.cg_cell_iters / (prof_64.cg_ms / 1e3) / 1e9)
-                            if prof_64.cg_ms > 0 else None,
-                            "gpu_launches": int(prof_64.launches),
-                            "cg_iters_case0": list(g64.diag(0).cg_iters)}
-            line["mixed_over_fp64"] = value / v64
+    legs = side_legs(args, torch, dist, rank, world, value)
+    g64 = None
+    if "fp64" in legs:
+        line["fp64"], g64 = legs["fp64"]
+        if g64 is not None:
+            line["mixed_over_fp64"] = value / line["fp64"]["value"]
             line["mixed_vs_fp64_rel_l2"] = compare_forms(gm, g64, min(4, len(cs_m)))
-            g64.close()
-        except Exception as e:  # reported, not hidden
-            line["fp64"] = {"error": repr(e)}
+    if "mixed_jacobi" in legs:
+        line["mixed_jacobi"], gj = legs["mixed_jacobi"]
+        if gj is not None:
+            if g64 is not None:
+                line["mixed_jacobi_over_fp64"] = line["mixed_jacobi"]["value"] / line["fp64"]["value"]
+                line["mixed_jacobi_vs_fp64_rel_l2"] = compare_forms(gj, g64, min(4, len(cs_m)))
+            gj.close()
+    if g64 is not None:
+        g64.close()
     if rank == 0 and not args.no_output:
         try:
             line["output"] = output_run(gm, min(16, len(cs_m)))
@@ -601,6 +768,11 @@ def main():
         except Exception as e:
             line["models"] = {"error": repr(e)}
     gm.close()
+    if rank == 0 and not args.no_configs:
+        try:
+            line["configs"] = configs_run(args, torch)
+        except Exception as e:
+            line["configs"] = {"error": repr(e)}
     if args.accuracy_steps > 0 and rank == 0:
         try:
             line["accuracy"] = accuracy_run(args)

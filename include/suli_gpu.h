@@ -6,8 +6,8 @@
  * module globals (SuLi-IC/0_modules.f90:2-325) and are called from the time
  * loop in SuLi-IC/1_principal.f90:69-124.  This header replaces each of them
  * with one entry point that acts on a device-resident case held by a handle.
- * A Fortran shim (ISO_C_BINDING, shown in INTEGRATION.md) keeps the original
- * subroutine names so the time loop is unchanged.
+ * A Fortran shim (ISO_C_BINDING interfaces over these entry points) keeps the
+ * original subroutine names so the time loop is unchanged.
  *
  * Conventions
  *   - Every entry point returns an int status: 0 = SULI_OK, >0 an error or
@@ -36,7 +36,8 @@ extern "C" {
 #define SULI_OK              0
 #define SULI_CG_MAXITER      1  /* warning: "pulou pressao", 9_grad.f90:590 */
 #define SULI_VOL_LOOP_CAP    2  /* volume-correction loop capped, 14_level_set.f90:243 */
-#define SULI_DEVICE_TIMEOUT  3  /* a bounded device wait gave up */
+#define SULI_DEVICE_TIMEOUT  3  /* reserved for a bounded device wait that gives up; no kernel of
+                                   this library waits on a flag, so no entry point returns it */
 #define SULI_BAD_CONFIG      4  /* replaces the reference's STOPs */
 #define SULI_BAD_ARG         5
 #define SULI_CUDA_ERROR      6
@@ -45,6 +46,10 @@ extern "C" {
 #define SULI_CG_STALLED      9  /* warning (mixed form, no counterpart in the reference): the FP64
                                    residual of the pressure refinement stopped falling before the
                                    tolerance; the solve ends on its last pass */
+#define SULI_NONFINITE      10  /* a case's state holds NaN or Inf: its volume integral or its
+                                   max|div| is not finite (checked by suli_level_set, i.e. once per
+                                   step of suli_step, and by suli_conmassa); the reference has no
+                                   such check and runs on with the NaNs */
 
 /* ---- precision of a case ----------------------------------------------- */
 #define SULI_PREC_FP64   0  /* plain form: FP64 storage and arithmetic */
@@ -110,6 +115,12 @@ typedef struct suli_params {
                                       waves_coef's results (3_contorno.f90:1323-1445, run by the
                                       host's iniciais, 2_iniciais.f90:241-245) */
     double  aeta[5], avel[5];      /* Stokes V surface and velocity coefficients (waves_coef) */
+    int32_t outflow_flux;          /* with ccxf = 4 (free outflow), 1: contorno(2) adds one uniform
+                                      correction to the outflow faces u(nx+1, 1:ny, 1:nz) so that their
+                                      flux equals the inflow faces' u(1, 1:ny, 1:nz) (no counterpart in
+                                      the reference, whose free outflow leaves a net boundary flux that
+                                      the all-Neumann pressure equation of graddin cannot absorb);
+                                      0: the reference's free outflow */
 } suli_params;
 
 /* ---- field ids (reference module arrays) -------------------------------- */
@@ -319,7 +330,8 @@ int suli_restart_save(suli_handle *h, const char *path);
 int suli_restart_load(suli_handle *h, const char *path);
 
 /* Divergence and max|div| of a velocity field held in caller-owned device
- * memory, computing exactly what suli_conmassa computes, but allocating no
+ * memory: the reference CONMASSA divergence in FP64 (what suli_conmassa gives
+ * for an FP64 handle; a mixed handle stores its div in FP32), allocating no
  * device memory (no counterpart in the reference: it exists for callers that
  * own every device buffer through their own allocator or memory budget, e.g.
  * a Fortran host whose arrays live in CUDA Fortran / OpenACC data regions).

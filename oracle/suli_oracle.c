@@ -1459,6 +1459,35 @@ static void inflow_plane(or_case *c, int I, const F3 *bplane, double lsthr_fac)
     c->rng_counter += (unsigned long long)ny * (unsigned long long)nz;
 }
 
+/* Balanced free outflow (outflow_flux = 1 with ccxf = 4; no counterpart in
+ * the reference, whose free outflow u(nx1) = u(nx1-1), 3_contorno.f90:380-384
+ * and :603-605, leaves a net boundary flux that the all-Neumann pressure
+ * equation of graddin cannot absorb): after contorno(2), the outflow faces
+ * u(nx1, 1:ny, 1:nz) take one uniform correction so that their sum equals the
+ * inflow faces' u(1, 1:ny, 1:nz).  The sum of the differences d = u(1) -
+ * u(nx1) over the plane runs in a fixed order, the one the GPU kernel uses:
+ * 256 strided partial sums over q = (j-1) + (k-1) ny (partial t takes q = t,
+ * t + 256, ... in turn), then halving pairs s[t] += s[t + h], h = 128 .. 1. */
+static void outflow_balance(or_case *c, F3 *u)
+{
+    const int ny = c->ny, nz = c->nz, nx1 = c->nx1;
+    const long n = (long)ny * nz;
+    double s[256];
+    for (int t = 0; t < 256; ++t) {
+        double a = 0.;
+        for (long q = t; q < n; q += 256) {
+            const int j = 1 + (int)(q % ny), k = 1 + (int)(q / ny);
+            a += A(*u, 1, j, k) - A(*u, nx1, j, k);
+        }
+        s[t] = a;
+    }
+    for (int h = 128; h > 0; h >>= 1)
+        for (int t = 0; t < h; ++t) s[t] += s[t + h];
+    const double corr = s[0] / (double)n;
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j) A(*u, nx1, j, k) = A(*u, nx1, j, k) + corr;
+}
+
 void or_contorno(or_case *c, int nlock)
 {
     int nx = c->nx, ny = c->ny, nz = c->nz, nx1 = c->nx1, ny1 = c->ny1, nz1 = c->nz1;
@@ -1527,6 +1556,7 @@ void or_contorno(or_case *c, int nlock)
         if (p->ccx0 == 0 && p->ccxf == 0) setx(u, nx1, u, 1, 1.);
         if (p->ccxf == 1 || p->ccxf == 2) zerox(u, nx1);
         if (p->ccxf == 4) setx(u, nx1, u, nx1 - 1, 1.);
+        if (p->ccxf == 4 && p->outflow_flux == 1) outflow_balance(c, u);
     } else if (nlock == 3 && p->ibm_t == 2) {
         /* level-set IBM, :651-659 */
         F3 lsv = tmp3(0, nx + 1, 0, ny + 1, 0, nz + 1);

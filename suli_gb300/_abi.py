@@ -17,6 +17,7 @@ SULI_CUDA_ERROR = 6
 SULI_NO_DEVICE = 7
 SULI_OUT_OF_MEMORY = 8
 SULI_CG_STALLED = 9
+SULI_NONFINITE = 10
 
 PREC_FP64 = 0
 PREC_MIXED = 1
@@ -63,6 +64,7 @@ class SuliParams(C.Structure):
         ("h0_f", C.c_double),
         ("aeta", C.c_double * 5),
         ("avel", C.c_double * 5),
+        ("outflow_flux", C.c_int32),
     ]
 
     def copy(self) -> "SuliParams":

@@ -218,7 +218,7 @@ def inflow_profile(p: SuliParams, ls: np.ndarray, seed: int) -> np.ndarray:
 
 
 def open_channel(nx=512, ny=128, nz=128, precision=PREC_FP64, dt=1e-3, seed=1234, radius=0.05,
-                 cg_tol=1e-8, periodic=False) -> Case:
+                 cg_tol=1e-8, periodic=False, balanced=False) -> Case:
     """Open channel, 4 x 1 x 1 m, depth 0.6 m flat surface, inflow u = 0.5 m/s
     with a seeded uniform 5 % perturbation (ccx0 = 3), free outflow, no-slip
     bed, Smagorinsky LES Cs = 0.1, vertical cylinder D = 0.1 m at x = 1.0
@@ -228,19 +228,22 @@ def open_channel(nx=512, ny=128, nz=128, precision=PREC_FP64, dt=1e-3, seed=1234
     periodic=True closes the channel in x (ccx0 = ccxf = 0): the pressure
     equation then has a solution (zero net boundary flux), where prescribed
     inflow with free outflow leaves the all-Neumann system of graddin with
-    a net flux that its CG cannot remove."""
+    a net flux that its CG cannot remove.  balanced=True keeps the inflow
+    and the free outflow but has contorno(2) correct the outflow faces to the
+    inflow's flux (outflow_flux = 1), which makes the pressure equation
+    solvable too."""
     h = 4.0 / nx
     cx = (0, 0) if periodic else (3, 4)
     p = default_params(nx=nx, ny=ny, nz=nz, dx=h, dy=h, dz=h, dt=dt,
                        ccx0=cx[0], ccxf=cx[1], ccy0=1, ccyf=1, ccz0=2, cczf=1,
                        gz=9.80665, m_turb=1, csmag=0.1, uinicial=0.5, iturb=0.05,
                        ibm_t=2, obst_t=4, reinit_max_iter=3, cg_tol_mode=CG_TOL_REL, cg_tol=cg_tol,
-                       precision=precision, seed=seed)
+                       precision=precision, seed=seed, outflow_flux=1 if (balanced and not periodic) else 0)
     ls = level_set_tipo(p, 1, ampl=0.0, lambdax=0.0, lambday=0.0, prof=0.6)
     f = _base_fields(p, ls)
     f["U"] = inflow_profile(p, ls, seed)
     f.update(cylinder_obstacle(p, 1.0, 0.5, radius))
-    name = "periodic_channel" if periodic else "open_channel"
+    name = "periodic_channel" if periodic else ("balanced_channel" if balanced else "open_channel")
     return Case("%s_%dx%dx%d" % (name, nx, ny, nz), p, f, steps=2000,
                 obstacle={"kind": "cylinder", "xc": 1.0, "yc": 0.5, "radius": radius})
 

@@ -300,6 +300,67 @@ template <typename T> void launch_contorno_masters(const Batch<T> &b, int nlock,
     }
 }
 
+// Balanced free outflow (outflow_flux = 1 with ccxf = 4; no counterpart in
+// the reference, whose zero-gradient outflow leaves a net boundary flux that
+// the all-Neumann pressure equation of graddin cannot absorb): the outflow
+// faces u(nx+1, 1:ny, 1:nz) take one uniform correction so that their sum
+// equals the inflow faces' u(1, 1:ny, 1:nz).  One 256-thread block per case;
+// the plane sum runs in a fixed order (thread t sums q = t, t + 256, ... of
+// q = (j-1) + (k-1) ny, then halving pairs in shared memory), so its bits do
+// not depend on scheduling.  The mixed form balances the FP64 masters (the
+// pressure right-hand side is taken from them) and rounds the faces once.
+template <typename T>
+__global__ void __launch_bounds__(256) k_outflow_balance(const CaseDev<T> *__restrict__ cs, int ncases)
+{
+    const CaseDev<T> &c = cs[blockIdx.x];
+    if (c.ccxf != 4 || c.outflow_flux != 1) return;
+    const Geo &g = c.g;
+    const int ny = g.ny, nz = g.nz, nx1 = g.nx + 1;
+    const long long n = (long long)ny * nz;
+    __shared__ double sh[256];
+    const int t = threadIdx.x;
+    double a = 0.0;
+    if (c.u64 != nullptr) {
+        for (long long q = t; q < n; q += 256) {
+            const int j = 1 + (int)(q % ny), k = 1 + (int)(q / ny);
+            a += c.u64[g.at(1, j, k)] - c.u64[g.at(nx1, j, k)];
+        }
+    } else {
+        for (long long q = t; q < n; q += 256) {
+            const int j = 1 + (int)(q % ny), k = 1 + (int)(q / ny);
+            a += (double)c.u[g.at(1, j, k)] - (double)c.u[g.at(nx1, j, k)];
+        }
+    }
+    sh[t] = a;
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+        if (t < h) sh[t] += sh[t + h];
+        __syncthreads();
+    }
+    const double corr = sh[0] / (double)n;
+    for (long long q = t; q < n; q += 256) {
+        const int j = 1 + (int)(q % ny), k = 1 + (int)(q / ny);
+        const long long o = g.at(nx1, j, k);
+        if (c.u64 != nullptr) {
+            const double x = c.u64[o] + corr;
+            c.u64[o] = x;
+            c.u[o] = T(x);
+        } else {
+            c.u[o] = T((double)c.u[o] + corr);
+        }
+    }
+}
+
+template <typename T> void launch_outflow_balance(const Batch<T> &b, cudaStream_t s)
+{
+    bool any = false;
+    for (int c = 0; c < b.ncases; ++c) any |= (b.hcases[c].ccxf == 4 && b.hcases[c].outflow_flux == 1);
+    if (!any) return;
+    k_outflow_balance<T><<<b.ncases, 256, 0, s>>>(b.dcases, b.ncases); count_launch();
+}
+
+template void launch_outflow_balance<float>(const Batch<float> &, cudaStream_t);
+template void launch_outflow_balance<double>(const Batch<double> &, cudaStream_t);
 template void launch_contorno_masters<float>(const Batch<float> &, int, cudaStream_t);
 template void launch_contorno_masters<double>(const Batch<double> &, int, cudaStream_t);
 template void launch_contorno<double>(const Batch<double> &, int, cudaStream_t, unsigned long long);

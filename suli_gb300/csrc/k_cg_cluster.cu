@@ -22,6 +22,8 @@
 // barriers, so no barrier can wait forever.
 #include "suli_kernels.cuh"
 
+#include <mutex>
+
 #include <cooperative_groups.h>
 
 namespace cgrp = cooperative_groups;
@@ -162,11 +164,27 @@ __global__ void __launch_bounds__(CL_THREADS) k_cg_cluster(const CaseDev<T> *__r
     }
 }
 
+// the cluster size of the current device, chosen once per device and element
+// type under a lock (handles may be created from several host threads, and
+// the devices of one process may differ)
 template <typename T>
 int cluster_cg_size()
 {
-    static int g_cluster_size = -1;   // chosen once per process and element type
-    if (g_cluster_size >= 0) return g_cluster_size;
+    constexpr int kMaxDev = 64;
+    static std::mutex mu;
+    static int chosen[kMaxDev];
+    static bool init = false;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) {
+        cudaGetLastError();
+        return 0;
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    if (!init) {
+        for (int d = 0; d < kMaxDev; ++d) chosen[d] = -1;
+        init = true;
+    }
+    if (chosen[dev] >= 0) return chosen[dev];
     int best = 0;
     for (int cl : {16, 8}) {
         cudaFuncSetAttribute(k_cg_cluster<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, cl > 8 ? 1 : 0);
@@ -187,7 +205,7 @@ int cluster_cg_size()
         }
         cudaGetLastError();
     }
-    g_cluster_size = best;
+    chosen[dev] = best;
     return best;
 }
 

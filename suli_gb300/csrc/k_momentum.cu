@@ -354,6 +354,13 @@ __global__ void __launch_bounds__(256) k_sponge(const CaseDev<T> *__restrict__ c
     if (i0 < 1) i0 = 1;
     if (i < i0) return;
     const double zpt = dz * nz;
+    // the level set in FP64: the mixed form's FP64 master (an FP32 product of
+    // two small values near the interface can underflow to 0 and count as a
+    // crossing), else the FP64 field itself
+    auto lsd = [&](int a, int bb, int d) -> double {
+        const long long q = g.at(a, bb, d);
+        return c.ls64 != nullptr ? c.ls64[q] : (double)c.ls[q];
+    };
     __shared__ long long red[32];
     __shared__ double zpfs_s;
     if (c.esp_type == 1) {
@@ -361,7 +368,7 @@ __global__ void __launch_bounds__(256) k_sponge(const CaseDev<T> *__restrict__ c
         const long long nk = nz - 1, n = (long long)ny * nk;
         for (long long t = threadIdx.x; t < n; t += blockDim.x) {
             const int j = (int)(t / nk) + 1, k = (int)(t % nk) + 1;
-            if (AT(c.ls, i, j, k) * AT(c.ls, i, j, k + 1) <= T(0.)) best = t;   // t grows per thread
+            if (lsd(i, j, k) * lsd(i, j, k + 1) <= 0.) best = t;   // t grows per thread
         }
         for (int o = 16; o > 0; o >>= 1) {
             const long long v = __shfl_down_sync(0xffffffffu, best, o);
@@ -372,11 +379,11 @@ __global__ void __launch_bounds__(256) k_sponge(const CaseDev<T> *__restrict__ c
         if (threadIdx.x == 0) {
             long long b = -1;
             for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b = red[w] > b ? red[w] : b;
-            double z = ((double)AT(c.ls, i, 1, 1) >= 0.) ? zpt : 0.;
+            double z = (lsd(i, 1, 1) >= 0.) ? zpt : 0.;
             if (b >= 0) {
                 const int j = (int)(b / nk) + 1, k = (int)(b % nk) + 1;
-                const double alt1 = dz * (k - 0.5) + (double)AT(c.ls, i, j, k);
-                const double alt2 = dz * (k + 0.5) + (double)AT(c.ls, i, j, k + 1);
+                const double alt1 = dz * (k - 0.5) + lsd(i, j, k);
+                const double alt2 = dz * (k + 0.5) + lsd(i, j, k + 1);
                 z = alt1 > alt2 ? alt1 : alt2;
             }
             zpfs_s = z;
@@ -392,7 +399,7 @@ __global__ void __launch_bounds__(256) k_sponge(const CaseDev<T> *__restrict__ c
             zx = zx + dz;
             double e;
             if (c.esp_type == 1) {
-                if (AT(c.ls, i, j, k) >= T(0.)) e = alfa * aux1 * aux1 * (0. - zx) / (0. - zpfs);
+                if (lsd(i, j, k) >= 0.) e = alfa * aux1 * aux1 * (0. - zx) / (0. - zpfs);
                 else e = alfa * aux1 * aux1 * (zx - zpt) / (zpfs - zpt);
             } else {
                 e = alfa0 + aux1 * (alfa1 - alfa0);
@@ -636,6 +643,7 @@ __global__ void __launch_bounds__(NTHREADS) k_conmassa(const CaseDev<T> *__restr
         }
         AT(c.div, i, j, k) = T(d);
         m = fabs(d);
+        if (!(m <= 1.79769313486231570e308)) m = INFINITY;   // NaN counts as infinite: fmax would drop it
     }
     double vals[1] = {m}, tot[1];
     if (last_block_reduce<T, 1>(c, vals, tot, 1u) && tid_lin() == 0) c.sc[S_MAXDIV] = tot[0];

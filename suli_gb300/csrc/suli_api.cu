@@ -146,6 +146,9 @@ static int validate(const suli_params &p)
     if (p.esp_type < 0 || p.esp_type > 2) return bad("esp_type must be 0, 1 or 2");
     if (!(p.wave_t == 0 || p.wave_t == 1 || p.wave_t == 2 || p.wave_t == 5)) return bad("wave_t must be 0, 1, 2 or 5");
     if (p.wave_t > 0 && !(p.n_w > 0 && p.h0_f > 0)) return bad("wave_t > 0 needs waves_coef's n_w > 0 and h0_f > 0");
+    if (p.outflow_flux != 0 && p.outflow_flux != 1) return bad("outflow_flux must be 0 or 1");
+    if (p.outflow_flux == 1 && !(p.ccxf == 4 && p.ccx0 == 3))
+        return bad("outflow_flux = 1 balances a free outflow (ccxf = 4) against a prescribed inflow (ccx0 = 3)");
     if ((long long)p.nx * p.ny * p.nz > (1LL << 31) - 1) return bad("grid larger than 2^31 cells");
     return SULI_OK;
 }
@@ -431,6 +434,7 @@ struct Impl : ImplBase {
             cd.t_press = q.t_press;
             cd.esp_type = q.esp_type;
             cd.wave_t = q.wave_t;
+            cd.outflow_flux = q.outflow_flux;
             cd.a_w = q.a_w; cd.f_w = q.f_w; cd.n_w = q.n_w; cd.h0_f = q.h0_f;
             for (int m = 0; m < 5; ++m) { cd.aeta[m] = q.aeta[m]; cd.avel[m] = q.avel[m]; }
             cd.ipa = (q.t_press == 2 && (q.mms_t == 0 || q.project_under_mms)) ? 1 : 0;
@@ -877,6 +881,7 @@ struct Impl : ImplBase {
         launch_heaviside<T>(b, 0, st);
         CKL();
         if ((rc = read_scalars())) return rc;
+        if ((rc = check_finite())) return rc;
         vol_loops = 0;
         for (;;) {
             bool any = false;
@@ -896,6 +901,21 @@ struct Impl : ImplBase {
         if (any_tens()) {
             launch_curvature<T>(b, st);
             CKL();
+        }
+        return SULI_OK;
+    }
+
+    // a NaN or Inf anywhere in a case's velocity or level set reaches its
+    // volume integral (this step's heaviside) or its max|div| (the last
+    // conmassa, which counts a NaN divergence as infinite); reads the host
+    // mirror of the scalars, so call it after read_scalars()
+    int check_finite()
+    {
+        for (int c = 0; c < ncases; ++c) {
+            const double v = sc(c, S_VOLINS), m = sc(c, S_MAXDIV);
+            if (!std::isfinite(v) || !std::isfinite(m))
+                return fail(SULI_NONFINITE, "case " + std::to_string(c) + ": non-finite state (vol_ins " +
+                                                std::to_string(v) + ", max|div| " + std::to_string(m) + ")");
         }
         return SULI_OK;
     }
@@ -943,6 +963,7 @@ struct Impl : ImplBase {
             launch_sync_masters<T>(b, st);
             launch_contorno_masters<T>(b, nlock, st);
         }
+        if (nlock == 2) launch_outflow_balance<T>(b, st);
         CKL();
         return SULI_OK;
     }
@@ -1185,6 +1206,7 @@ struct Impl : ImplBase {
             int rc = read_scalars();
             if (rc) return rc;
             *maxdiv = sc(0, S_MAXDIV);
+            if ((rc = check_finite())) return rc;
         }
         return SULI_OK;
     }
@@ -1596,6 +1618,26 @@ extern "C" int suli_restart_load(suli_handle *h, const char *path)
         if (ok && (d[0] != im->P[c].nx || d[1] != im->P[c].ny || d[2] != im->P[c].nz))
             return bad("case " + std::to_string(c) + " has other dimensions");
     }
+    if (!ok) return bad("truncated restart file");
+    // first pass over the record headers: every record present with the
+    // expected id and length and the file long enough, before anything is
+    // uploaded (a refused file leaves the handle as it was)
+    const long data0 = std::ftell(fp);
+    if (data0 < 0 || std::fseek(fp, 0, SEEK_END) != 0) return bad("cannot seek");
+    const long long fsize = (long long)std::ftell(fp);
+    long long pos = data0;
+    for (int c = 0; c < nc; ++c)
+        for (int f = 0; f < SULI_F_COUNT; ++f) {
+            int32_t id = -1;
+            int64_t n = -1;
+            if (pos + 12 > fsize || std::fseek(fp, (long)pos, SEEK_SET) != 0) return bad("truncated restart file");
+            get(&id, 4); get(&n, 8);
+            const int64_t want = im->stored(c, f) ? field_count(im->P[c], f) : 0;
+            if (!ok || id != f || n != want) return bad("field " + std::to_string(f) + " of case " + std::to_string(c));
+            pos += 12 + n * (is_int_field(f) ? 4 : 8);
+            if (pos > fsize) return bad("truncated restart file");
+        }
+    if (std::fseek(fp, data0, SEEK_SET) != 0) return bad("cannot seek");
     for (int c = 0; c < nc && ok; ++c) {
         std::vector<std::vector<double>> dv;
         std::vector<std::vector<int32_t>> iv;

@@ -131,6 +131,7 @@ struct CaseDev {
     int t_press, ipa;           // ipa: t_press = 2 and the step projects (exp_press / IPA graddin)
     int esp_type;               // sponge layer (0 none)
     int wave_t;                 // inflow waves (0 none, 1/2 Stokes I/II, 5 Stokes V)
+    int outflow_flux;           // 1: contorno(2) balances the free-outflow faces' flux to the inflow's
     double a_w, f_w, n_w, h0_f, aeta[5], avel[5];   // waves_coef's results
     int reinit_max, cg_max, cg_tol_mode;
     double cg_tol;

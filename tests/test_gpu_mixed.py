@@ -63,6 +63,28 @@ def test_mixed_surface_tension_against_oracle(gpu_lib):
     assert ev <= 3e-5 and els <= 1e-7 and ek <= 1e-5
 
 
+def test_mixed_balanced_channel_against_oracle(gpu_lib):
+    """The open channel at 64 x 16 x 16 -- prescribed perturbed inflow,
+    balanced free outflow, IBM cylinder, Smagorinsky LES -- in the mixed form,
+    10 steps, against the FP64 oracle."""
+    nsteps = 10
+    case = cases.open_channel(64, 16, 16, dt=2e-3, radius=0.25, cg_tol=1e-10, balanced=True)
+    o = oracle_for(case)
+    o.step(nsteps)
+    cm = cases.open_channel(64, 16, 16, dt=2e-3, radius=0.25, cg_tol=1e-10, balanced=True, precision=PREC_MIXED)
+    g = gpu_lib.SuliGPU(cm.params)
+    g.start(cm.fields)
+    g.step(nsteps)
+    ev = rel_l2(_vel(g.download), _vel(o.field))
+    els = rel_l2(g.download("LS"), o.field("LS"))
+    pg = g.download("PRD1")[1:-1, 1:-1, 1:-1]
+    po = o.field("PRD1")[1:-1, 1:-1, 1:-1]
+    ep = rel_l2(pg - pg.mean(), po - po.mean())
+    g.close()
+    print("balanced channel, mixed vs oracle after %d steps: velocity %.2e ls %.2e p %.2e" % (nsteps, ev, els, ep))
+    assert ev <= 1e-6 and els <= 1e-6 and ep <= 1e-6
+
+
 @pytest.mark.parametrize("which", ["k_les", "k_des", "ipa", "sponge"])
 def test_mixed_keq_ipa_against_oracle(gpu_lib, which):
     """The k equation (FP32 ka, nut and sub-stage buffers), the IPA (FP32

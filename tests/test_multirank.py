@@ -1,6 +1,7 @@
-"""bench.py's multi-GPU path on CPU: two gloo ranks on 127.0.0.1, each
-advancing its own ensemble (seed = rank) with no data-path collective; the
-job's work is the sum of the ranks' cells and its time the slowest rank's."""
+"""bench.py's multi-rank path on CPU: two gloo ranks on 127.0.0.1 split one
+ensemble round-robin (no data-path collective), each advances its share
+(with the CPU oracle standing in for the GPU), and the job's work is the sum
+of the ranks' cells and its time the slowest rank's."""
 import socket
 
 import pytest
@@ -12,9 +13,12 @@ def _free_port():
         return s.getsockname()[1]
 
 
-def test_two_ranks_shard_the_ensemble():
+def test_two_ranks_partition_the_ensemble():
     mp = pytest.importorskip("torch.multiprocessing")
-    from multirank_worker import rank_main
+    import bench
+    import pyoracle
+    from multirank_worker import NCASES, STEPS, rank_main
+    from suli_gb300._abi import PREC_FP64
 
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
@@ -25,7 +29,7 @@ def test_two_ranks_shard_the_ensemble():
     res = {}
     try:
         for _ in range(2):
-            r = q.get(timeout=120)
+            r = q.get(timeout=300)
             res[r[0]] = r
     finally:
         for p in procs:
@@ -33,7 +37,17 @@ def test_two_ranks_shard_the_ensemble():
             if p.is_alive():
                 p.terminate()
     assert all(p.exitcode == 0 for p in procs)
-    (_, n0, c0, t0, m0, d0), (_, n1, c1, t1, m1, d1) = res[0], res[1]
-    assert n0 != n1 and d0 != d1          # each rank has its own seeded ensemble
-    assert t0 == t1 == float(c0 + c1)     # job work: the sum over ranks
-    assert m0 == m1 == 11.0               # job time: the slowest rank
+    (_, s0, c0, m0, t0, j0), (_, s1, c1, m1, t1, j1) = res[0], res[1]
+    # every case of the ensemble advanced exactly once, by one rank
+    assert set(s0).isdisjoint(s1)
+    assert sorted(set(s0) | set(s1)) == sorted("ensemble_%d" % i for i in range(NCASES))
+    # each rank's results are the case's own (the same as a serial run)
+    pyoracle.Oracle.set_threads(1)
+    for c in bench.ensemble_share(NCASES, 0, 1, PREC_FP64, lo=8, hi=12):
+        c.params.omp_t = 0
+        o, _ = bench._oracle_case(c)
+        o.step(STEPS)
+        got = s0.get(c.name, s1.get(c.name))
+        assert got == (float(o.scalar("VOL_INS")), float(abs(o.field("W")).sum())), c.name
+    assert t0 == t1 == float(c0 + c1)          # job work: the sum over ranks
+    assert j0 == j1 == max(m0, m1)             # job time: the slowest rank

@@ -140,3 +140,25 @@ def test_mms_error_decreases_with_resolution():
         o.step(10)
         errs.append(o.mms_error())
     assert errs[1][0] < errs[0][0] and errs[1][1] < errs[0][1], errs
+
+
+def test_balanced_outflow_makes_the_pressure_equation_solvable():
+    """outflow_flux = 1: after contorno(2) the outflow faces carry the inflow
+    faces' flux (to round-off), and graddin's CG then converges, where the
+    reference's free outflow leaves a net flux its CG cannot remove."""
+    import pyoracle
+    from helpers import oracle_for
+    from suli_gb300 import cases
+    pyoracle.Oracle.set_threads(4)
+    iters = {}
+    for bal in (False, True):
+        c = cases.open_channel(48, 16, 16, dt=2e-3, radius=0.25, cg_tol=1e-10, balanced=bal)
+        c.params.cg_max_iter = 2000
+        o = oracle_for(c)
+        u = o.field("U")
+        if bal:
+            qi, qo = u[1, 1:-1, 1:-1].sum(), u[49, 1:-1, 1:-1].sum()
+            assert abs(qi - qo) <= 1e-12 * abs(qi)
+        o.step()
+        iters[bal] = list(o.diag().cg_iters)
+    assert max(iters[True]) < 400 and min(iters[False]) >= 1000, iters
