@@ -224,14 +224,24 @@ __global__ void k_inflow(const CaseDev<T> *__restrict__ cs, int ncases, int I, d
     const unsigned long long base = call * (unsigned long long)ny * (unsigned long long)nz;
     const long long pl = ny + 3;
     T *u = c.u;
+    // mixed form: the inflow is formed in FP64 on the masters (velocity and
+    // level set) and rounded once into the FP32 copies
+    double *u64 = c.u64;
+    const bool m = (u64 != nullptr);
     const T *bx = (I == 0) ? c.bxx0 : c.bxx1;
     if (I == 1) {
         for (int t = threadIdx.x; t < ny * nz; t += blockDim.x) {
             int j = 1 + t % ny, k = 1 + t / ny;
             AT(c.ls, 1, j, k) = c.blx1[j + pl * k];
+            if (c.ls64 != nullptr) AT(c.ls64, 1, j, k) = (double)c.blx1[j + pl * k];
         }
         __syncthreads();
     }
+    // the inflow test on the face level set, (ls(2) + ls(1)) / 2
+    auto lsx = [&](int j, int k) -> double {
+        if (c.ls64 != nullptr) return (AT(c.ls64, 2, j, k) + AT(c.ls64, 1, j, k)) * 0.5;
+        return (double)((AT(c.ls, 2, j, k) + AT(c.ls, 1, j, k)) * T(0.5));
+    };
     __shared__ int firstw, lastw;
     if (threadIdx.x == 0) lastw = 0;
     __syncthreads();
@@ -240,20 +250,31 @@ __global__ void k_inflow(const CaseDev<T> *__restrict__ cs, int ncases, int I, d
         if (threadIdx.x == 0) firstw = ny + 1;
         __syncthreads();
         for (int j = 1 + threadIdx.x; j <= ny; j += blockDim.x) {
-            T lsx = (AT(c.ls, 2, j, k) + AT(c.ls, 1, j, k)) * T(0.5);
-            if ((double)lsx >= -thr_dz * c.dz) atomicMin(&firstw, j);
+            if (lsx(j, k) >= -thr_dz * c.dz) atomicMin(&firstw, j);
         }
         __syncthreads();
         for (int j = 1 + threadIdx.x; j <= ny; j += blockDim.x) {
-            T lsx = (AT(c.ls, 2, j, k) + AT(c.ls, 1, j, k)) * T(0.5);
-            if ((double)lsx >= -thr_dz * c.dz) {
+            const double lx = lsx(j, k);
+            if (lx >= -thr_dz * c.dz) {
                 double r = rng_uniform(c.seed, base + (unsigned long long)((k - 1) * ny + (j - 1)));
                 r = 2. * (r - 0.5);
                 T v = bx[j + pl * k];
-                AT(u, I, j, k) = v * (T(1.) + T(r) * T(c.iturb));
-            } else if (lsx < T(0)) {
+                if (m) {
+                    const double x = (double)v * (1. + r * c.iturb);
+                    AT(u64, I, j, k) = x;
+                    AT(u, I, j, k) = T(x);
+                } else {
+                    AT(u, I, j, k) = v * (T(1.) + T(r) * T(c.iturb));
+                }
+            } else if (lx < 0.) {
                 int iik = (firstw < j) ? k : lastw;
-                AT(u, I, j, k) = AT(u, I, j, iik) * (T(1.) + T(tanh(c.pi * (double)(iik - k - 1) / 2.)));
+                if (m) {
+                    const double x = AT(u64, I, j, iik) * (1. + tanh(c.pi * (double)(iik - k - 1) / 2.));
+                    AT(u64, I, j, k) = x;
+                    AT(u, I, j, k) = T(x);
+                } else {
+                    AT(u, I, j, k) = AT(u, I, j, iik) * (T(1.) + T(tanh(c.pi * (double)(iik - k - 1) / 2.)));
+                }
             }
         }
         __syncthreads();
@@ -272,31 +293,24 @@ void launch_contorno(const Batch<T> &b, int nlock, cudaStream_t s, unsigned long
     dim3 grid(nb, b.ncases);
     bool inflow = false;
     for (int c = 0; c < b.ncases; ++c) inflow |= (b.hcases[c].ccx0 == 3);
-    for (int ph = 0; ph < 3; ++ph) {
+    // mixed form: every phase runs on the FP32 fields and then on the FP64
+    // velocity masters, in the same place relative to the inflow as the FP32
+    // fills (the inflow writes both), so a ghost master is the FP64 copy of
+    // the master it mirrors at the time the reference copies it
+    const bool masters = (sizeof(T) == 4);
+    auto phase = [&](int ph) {
         k_bc_phase<T><<<grid, 256, 0, s>>>(b.dcases, b.ncases, ph, 0); count_launch();
-    }
+        if (masters) { k_bc_phase<T><<<grid, 256, 0, s>>>(b.dcases, b.ncases, ph, 1); count_launch(); }
+    };
+    for (int ph = 0; ph < 3; ++ph) phase(ph);
     if (inflow) {
         k_inflow<T><<<b.ncases, 256, 0, s>>>(b.dcases, b.ncases, 0, 1.0, rng_call); count_launch();
     }
     if (nlock == 2) {
-        k_bc_phase<T><<<grid, 256, 0, s>>>(b.dcases, b.ncases, 3, 0); count_launch();
+        phase(3);
         if (inflow) {
             k_inflow<T><<<b.ncases, 256, 0, s>>>(b.dcases, b.ncases, 1, 2.0, rng_call + 1); count_launch();
         }
-    }
-}
-
-// the velocity fills of contorno(nlock) on the FP64 masters (mixed form),
-// after the masters took the FP32 results
-template <typename T> void launch_contorno_masters(const Batch<T> &b, int nlock, cudaStream_t s)
-{
-    if (nlock != 1 && nlock != 2) return;
-    int nb = (b.max_plane + 255) / 256;
-    if (nb < 1) nb = 1;
-    if (nb > 1024) nb = 1024;
-    dim3 grid(nb, b.ncases);
-    for (int ph = 0; ph < (nlock == 2 ? 4 : 3); ++ph) {
-        k_bc_phase<T><<<grid, 256, 0, s>>>(b.dcases, b.ncases, ph, 1); count_launch();
     }
 }
 
@@ -361,8 +375,6 @@ template <typename T> void launch_outflow_balance(const Batch<T> &b, cudaStream_
 
 template void launch_outflow_balance<float>(const Batch<float> &, cudaStream_t);
 template void launch_outflow_balance<double>(const Batch<double> &, cudaStream_t);
-template void launch_contorno_masters<float>(const Batch<float> &, int, cudaStream_t);
-template void launch_contorno_masters<double>(const Batch<double> &, int, cudaStream_t);
 template void launch_contorno<double>(const Batch<double> &, int, cudaStream_t, unsigned long long);
 template void launch_contorno<float>(const Batch<float> &, int, cudaStream_t, unsigned long long);
 

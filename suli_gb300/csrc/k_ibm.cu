@@ -195,11 +195,16 @@ __global__ void __launch_bounds__(NTHREADS) k_ibm_image(const CaseDev<T> *__rest
         double nxv, nyv, nzv, dummy0, dummy1;
         obs_normal<T>(c, t.obs, i, j, k, t.n0, t.n1, t.n2, nxv, nyv, nzv);
         if (k == 1 && t.n2 >= 2) obs_normal<T>(c, t.obs, i, j, k + 1, t.n0, t.n1, t.n2, dummy0, dummy1, nzv);
-        // a component below 1e-9 is roundoff of an exact zero (z of an obstacle
-        // extruded along z); its sign would pick the image cell through floor()
-        nxv = fabs(nxv) < 1e-9 ? 0.0 : nxv;
-        nyv = fabs(nyv) < 1e-9 ? 0.0 : nyv;
-        nzv = fabs(nzv) < 1e-9 ? 0.0 : nzv;
+        // a component below the round-off of the obstacle level set is an
+        // exact zero (z of an obstacle extruded along z); its sign would pick
+        // the image cell through floor().  FP64 obstacle: 1e-9.  The mixed
+        // form's FP32 obstacle, reinitialised in FP32 (the WENO end
+        // extrapolation multiplies by a rounded 1/11), carries ~1e-6 of such
+        // round-off near the bed: 1e-4 there
+        const double zr = (sizeof(T) == 4) ? 1e-4 : 1e-9;
+        nxv = fabs(nxv) < zr ? 0.0 : nxv;
+        nyv = fabs(nyv) < zr ? 0.0 : nyv;
+        nzv = fabs(nzv) < zr ? 0.0 : nzv;
         auto XC = [&](int a) { return __dmul_rn((double)a - t.ox, dx); };
         auto YC = [&](int a) { return __dmul_rn((double)a - t.oy, dy); };
         auto ZC = [&](int a) { return __dmul_rn((double)a - t.oz, dz); };

@@ -519,9 +519,10 @@ __global__ void k_sync_masters(const CaseDev<T> *__restrict__ cs, int ncases)
 {
     const CaseDev<T> &c = cs[blockIdx.y];
     if (c.u64 == nullptr) return;
-    // contorno's plane fills are replayed on the masters in FP64; the FP32
-    // writes left to copy are the IBM image points (anywhere in the box) and
-    // the prescribed inflow (planes i = 0 and 1)
+    // contorno's plane fills run on the masters in FP64 and the inflow
+    // writes them too; the FP32 writes left to copy are the IBM image points
+    // (anywhere in the box; before the plane fills) and, for callers that
+    // run it after contorno, the inflow planes i = 0 and 1
     const bool ibm = (c.obst_t != 0 && c.ibm_t == 2);
     if (!ibm && c.ccx0 != 3) return;
     const long long rows = c.g.sxy / c.g.sx * (long long)(c.g.nz + 3);

@@ -954,15 +954,11 @@ struct Impl : ImplBase {
             return SULI_OK;
         }
         if (any_ibm()) launch_ibm_velocity<T>(b, st);     // 3_contorno.f90:85-90
+        // mixed form: the IBM image values (FP32) into the FP64 masters before
+        // the plane fills, which run on both (the inflow writes both)
+        if (sizeof(T) == 4) launch_sync_masters<T>(b, st);
         launch_contorno<T>(b, nlock, st, inflow_calls);
         if (any_inflow()) inflow_calls += (nlock == 2) ? 2 : 1;
-        // values the boundary conditions wrote (ghosts, walls, inflow, IBM
-        // images) into the FP64 masters of the mixed form, then the ghost
-        // fills redone on the masters in FP64
-        if (sizeof(T) == 4) {
-            launch_sync_masters<T>(b, st);
-            launch_contorno_masters<T>(b, nlock, st);
-        }
         if (nlock == 2) launch_outflow_balance<T>(b, st);
         CKL();
         return SULI_OK;

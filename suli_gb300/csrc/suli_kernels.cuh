@@ -68,11 +68,10 @@ template <typename T> void launch_mms_error(const Batch<T> &b, cudaStream_t s);
 
 // boundary conditions (k_bc.cu)
 template <typename T> void launch_contorno(const Batch<T> &b, int nlock, cudaStream_t s, unsigned long long rng_call = 0);
-template <typename T> void launch_contorno_masters(const Batch<T> &b, int nlock, cudaStream_t s);
 // balanced free outflow (outflow_flux = 1, ccxf = 4): after contorno(2), on the
 // FP64 masters where the mixed form has them, then their FP32 copies
 template <typename T> void launch_outflow_balance(const Batch<T> &b, cudaStream_t s);
-// mixed form: FP32 velocity values changed outside tempo/posdin -> FP64 masters
+// mixed form: FP32 velocity and level-set values the IBM images wrote -> FP64 masters
 template <typename T> void launch_sync_masters(const Batch<T> &b, cudaStream_t s);
 
 // immersed boundary (k_ibm.cu)

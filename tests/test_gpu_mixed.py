@@ -63,15 +63,20 @@ def test_mixed_surface_tension_against_oracle(gpu_lib):
     assert ev <= 3e-5 and els <= 1e-7 and ek <= 1e-5
 
 
-def test_mixed_balanced_channel_against_oracle(gpu_lib):
-    """The open channel at 64 x 16 x 16 -- prescribed perturbed inflow,
-    balanced free outflow, IBM cylinder, Smagorinsky LES -- in the mixed form,
-    10 steps, against the FP64 oracle."""
+@pytest.mark.parametrize("kind", ["balanced", "periodic"])
+def test_mixed_channel_ibm_against_oracle(gpu_lib, kind):
+    """The open channel at 64 x 16 x 16 with the IBM cylinder and
+    Smagorinsky LES -- prescribed perturbed inflow with the balanced free
+    outflow, or closed periodically in x -- in the mixed form, 10 steps,
+    against the FP64 oracle.  (The image normals' round-off threshold and the
+    inflow written on the FP64 masters are what this pins: without them the
+    mixed form was 3e-2 away in velocity at the cylinder's foot.)"""
     nsteps = 10
-    case = cases.open_channel(64, 16, 16, dt=2e-3, radius=0.25, cg_tol=1e-10, balanced=True)
+    kw = dict(dt=2e-3, radius=0.25, cg_tol=1e-10, balanced=(kind == "balanced"), periodic=(kind == "periodic"))
+    case = cases.open_channel(64, 16, 16, **kw)
     o = oracle_for(case)
     o.step(nsteps)
-    cm = cases.open_channel(64, 16, 16, dt=2e-3, radius=0.25, cg_tol=1e-10, balanced=True, precision=PREC_MIXED)
+    cm = cases.open_channel(64, 16, 16, precision=PREC_MIXED, **kw)
     g = gpu_lib.SuliGPU(cm.params)
     g.start(cm.fields)
     g.step(nsteps)
@@ -81,7 +86,7 @@ def test_mixed_balanced_channel_against_oracle(gpu_lib):
     po = o.field("PRD1")[1:-1, 1:-1, 1:-1]
     ep = rel_l2(pg - pg.mean(), po - po.mean())
     g.close()
-    print("balanced channel, mixed vs oracle after %d steps: velocity %.2e ls %.2e p %.2e" % (nsteps, ev, els, ep))
+    print("%s channel, mixed vs oracle after %d steps: velocity %.2e ls %.2e p %.2e" % (kind, nsteps, ev, els, ep))
     assert ev <= 1e-6 and els <= 1e-6 and ep <= 1e-6
 
 
