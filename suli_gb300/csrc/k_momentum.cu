@@ -15,100 +15,11 @@
 // temporaries (advecting-velocity averages, interpolated viscosities, face
 // densities, upwind derivatives) are recomputed in registers with the same
 // operations and boundary copies as the Fortran helpers.
-#include "suli_kernels.cuh"
+#include "conv_faces.cuh"
 
 namespace suli {
 
 #define AT(arr, i, j, k) (arr)[g.at((i), (j), (k))]
-
-// interp?_cf at face f (1..n+1) of a centre quantity get(m), m in 1..n
-// (8_derivadas.f90:305-479); `periodic` only for x (interpx_cf).
-template <typename T, typename F>
-__device__ __forceinline__ T interp_cf(int f, int n, bool periodic, F get)
-{
-    if (f >= 2 && f <= n) return (get(f) + get(f - 1)) * T(0.5);
-    if (periodic) return (get(1) + get(n)) * T(0.5);
-    if (f == 1) return (get(2) + get(1)) * T(0.5);
-    return (get(n) + get(n - 1)) * T(0.5);
-}
-
-__device__ __forceinline__ int clampi(int a, int lo, int hi) { return a < lo ? lo : (a > hi ? hi : a); }
-
-// surface tension (t_tens = 1): sigma times the face value of hs_a kurv / rho
-// on the axis-0/1/2 face (i, j, k) (11_diversos.f90:383-390; interpx_cf wraps
-// on a periodic x, interpy_cf / interpz_cf never wrap)
-template <typename T>
-__device__ __forceinline__ T tension_face(const CaseDev<T> &c, int axis, int i, int j, int k)
-{
-    const Geo &g = c.g;
-    auto v = [&](const T *hs, long long q) { return hs[q] * c.kurv[q] / c.rho[q]; };
-    T f;
-    if (axis == 0) f = interp_cf<T>(i, g.nx, c.ccx0 == 0, [&](int m) { return v(c.hsx, g.at(m, j, k)); });
-    else if (axis == 1) f = interp_cf<T>(j, g.ny, false, [&](int m) { return v(c.hsy, g.at(i, m, k)); });
-    else f = interp_cf<T>(k, g.nz, false, [&](int m) { return v(c.hsz, g.at(i, j, m)); });
-    return T(c.sigma) * f;
-}
-
-// the kinetic-energy term of complementos (m_turb >= 2, 11_diversos.f90:403-444):
-// 2/3 (karho(m) - karho(m-1)) / (h rho_face) on the axis-0/1/2 face (i, j, k),
-// karho = ka rhof with rhof = fantasmas_cf(rho) (8_derivadas.f90:625-671: y and
-// z ghosts copy the adjacent cell, x ghosts wrap on a periodic x)
-template <typename T>
-__device__ __forceinline__ T ka_face(const CaseDev<T> &c, int axis, int i, int j, int k)
-{
-    const Geo &g = c.g;
-    const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const bool per = (c.ccx0 == 0);
-    auto kr = [&](int a, int b, int d) {
-        const T kv = c.ka[g.at(a, b, d)];
-        if (b == 0) b = 1; else if (b == ny + 1) b = ny;
-        if (d == 0) d = 1; else if (d == nz + 1) d = nz;
-        if (a == 0) a = per ? nx : 1; else if (a == nx + 1) a = per ? 1 : nx;
-        return kv * c.rho[g.at(a, b, d)];
-    };
-    T diff, rf, h;
-    if (axis == 0) {
-        diff = kr(i, j, k) - kr(i - 1, j, k);
-        rf = interp_cf<T>(i, nx, per, [&](int m) { return c.rho[g.at(m, j, k)]; });
-        h = T(c.dx);
-    } else if (axis == 1) {
-        diff = kr(i, j, k) - kr(i, j - 1, k);
-        rf = interp_cf<T>(j, ny, false, [&](int m) { return c.rho[g.at(i, m, k)]; });
-        h = T(c.dy);
-    } else {
-        diff = kr(i, j, k) - kr(i, j, k - 1);
-        rf = interp_cf<T>(k, nz, false, [&](int m) { return c.rho[g.at(i, j, m)]; });
-        h = T(c.dz);
-    }
-    return T(2. / 3.) * diff / (h * rf);
-}
-
-template <typename T>
-__device__ __forceinline__ T upw(T vel, T dneg, T dpos)
-{
-    T a1 = vel > T(0.) ? vel : T(0.);
-    T a2 = vel < T(0.) ? vel : T(0.);
-    return a1 * dneg + a2 * dpos;
-}
-
-// derivaxu2n / derivaxu2p etc. (8_derivadas.f90:75-300) on a haloed array
-// whose interior extent along the axis is `dim`.
-// (divisions by the fixed spacing are multiplications by its reciprocal rh;
-// GB300's FP64 divide is a long instruction sequence)
-template <typename T, typename F>
-__device__ __forceinline__ T d2n(int m, int dim, bool perx, T rh, F a)
-{
-    if (m >= 2) return T(0.5) * (a(m - 2) - 4 * a(m - 1) + 3 * a(m)) * rh;
-    if (!perx) return T(0.5) * (a(m + 1) - a(m - 1)) * rh;
-    return T(0.5) * (a(dim - 1) - 4 * a(dim) + 3 * a(m)) * rh;
-}
-template <typename T, typename F>
-__device__ __forceinline__ T d2p(int m, int dim, bool perx, T rh, F a)
-{
-    if (m <= dim - 1) return T(0.5) * (-a(m + 2) + 4 * a(m + 1) - 3 * a(m)) * rh;
-    if (!perx) return T(0.5) * (a(m + 1) - a(m - 1)) * rh;
-    return T(0.5) * (-a(2) + 4 * a(1) - 3 * a(m)) * rh;
-}
 
 // ---------------------------------------------------------------------------
 template <typename T>
@@ -167,6 +78,8 @@ __global__ void __launch_bounds__(NTHREADS) k_visco_faces(const CaseDev<T> *__re
 }
 
 // ---------------------------------------------------------------------------
+// the gather form (operands read from global memory, one thread per
+// (i, j, k)); the FP64 form's default and the fallback SULI_CONVDIFF=0
 template <typename T>
 __global__ void __launch_bounds__(NTHREADS) k_convdiff(const CaseDev<T> *__restrict__ cs, int ncases, int fuse)
 {
@@ -175,121 +88,20 @@ __global__ void __launch_bounds__(NTHREADS) k_convdiff(const CaseDev<T> *__restr
     tile_ijk(c, i, j, k);
     const Geo &g = c.g;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const T *__restrict__ u = c.u;
-    const T *__restrict__ v = c.v;
-    const T *__restrict__ w = c.w;
-    const T *__restrict__ mu = c.mu;
-    const T *__restrict__ rho = c.rho;
-    const T *__restrict__ xmu = c.xmu;
-    const T *__restrict__ ymu = c.ymu;
-    const T *__restrict__ zmu = c.zmu;
-    const T dx = T(c.idx), dy = T(c.idy), dz = T(c.idz);   // reciprocal spacings (1.0 / dx from the host)
-    const bool px = (c.ccx0 == 0);
-
-    // ---- Fu at x-face (i,j,k), i in 1..nx+1 ----
+    const GlobalAcc<T> X{c};
     if (i <= nx + 1 && j <= ny && k <= nz) {
-        auto U = [&](int a, int b, int cc) { return AT(u, a, b, cc); };
-        T bma = interp_cf<T>(i, nx, px, [&](int m) { return (AT(v, m, j, k) + AT(v, m, j + 1, k)) * T(0.5); });
-        T dma = interp_cf<T>(i, nx, px, [&](int m) { return (AT(w, m, j, k) + AT(w, m, j, k + 1)) * T(0.5); });
-        T ddx = upw<T>(U(i, j, k), d2n<T>(i, nx + 1, px, dx, [&](int m) { return U(m, j, k); }),
-                       d2p<T>(i, nx + 1, px, dx, [&](int m) { return U(m, j, k); }));
-        T ddy = upw<T>(bma, d2n<T>(j, ny, false, dy, [&](int m) { return U(i, m, k); }),
-                       d2p<T>(j, ny, false, dy, [&](int m) { return U(i, m, k); }));
-        T ddz = upw<T>(dma, d2n<T>(k, nz, false, dz, [&](int m) { return U(i, j, m); }),
-                       d2p<T>(k, nz, false, dz, [&](int m) { return U(i, j, m); }));
-        T uint_ = ddx + ddy + ddz;
-        T ama_i = AT(mu, clampi(i, 1, nx), j, k) * dx;
-        T ama_m = AT(mu, clampi(i - 1, 1, nx), j, k) * dx;
-        T b1 = interp_cf<T>(j + 1, ny, false, [&](int m) { return AT(xmu, i, m, k); }) * dy;
-        T b0 = interp_cf<T>(j, ny, false, [&](int m) { return AT(xmu, i, m, k); }) * dy;
-        T d1 = interp_cf<T>(k + 1, nz, false, [&](int m) { return AT(xmu, i, j, m); }) * dz;
-        T d0 = interp_cf<T>(k, nz, false, [&](int m) { return AT(xmu, i, j, m); }) * dz;
-        T rhox = interp_cf<T>(i, nx, px, [&](int m) { return AT(rho, m, j, k); });
-        T uc = U(i, j, k);
-        const T rrho = T(1.) / rhox;
-        T F = -uint_ +
-              ((ama_i * T(2.) * (U(i + 1, j, k) - uc) - ama_m * T(2.) * (uc - U(i - 1, j, k))) * dx +
-               b1 * ((U(i, j + 1, k) - uc) * dy + (AT(v, i, j + 1, k) - AT(v, i - 1, j + 1, k)) * dx) -
-               b0 * ((uc - U(i, j - 1, k)) * dy + (AT(v, i, j, k) - AT(v, i - 1, j, k)) * dx) +
-               d1 * ((U(i, j, k + 1) - uc) * dz + (AT(w, i, j, k + 1) - AT(w, i - 1, j, k + 1)) * dx) -
-               d0 * ((uc - U(i, j, k - 1)) * dz + (AT(w, i, j, k) - AT(w, i - 1, j, k)) * dx)) *
-                  rrho;
-        if (fuse) {
-            F = F + T(c.gx);
-            if (c.t_tens == 1) F = F - tension_face(c, 0, i, j, k);
-            F = F + AT(c.tf_u, i, j, k);
-            if (c.m_turb >= 2) F = F - ka_face(c, 0, i, j, k);
-        }
+        T F = face_fu<T>(c, X, i, j, k);
+        if (fuse) F = compl_fu<T>(c, F, i, j, k);
         AT(c.Fu, i, j, k) = F;
     }
-    // ---- Fv at y-face (i,j,k), j in 1..ny+1 ----
     if (i <= nx && j <= ny + 1 && k <= nz) {
-        auto V = [&](int a, int b, int cc) { return AT(v, a, b, cc); };
-        T amb = interp_cf<T>(j, ny, false, [&](int m) { return (AT(u, i, m, k) + AT(u, i + 1, m, k)) * T(0.5); });
-        T dmb = interp_cf<T>(j, ny, false, [&](int m) { return (AT(w, i, m, k) + AT(w, i, m, k + 1)) * T(0.5); });
-        T ddx = upw<T>(amb, d2n<T>(i, nx, px, dx, [&](int m) { return V(m, j, k); }),
-                       d2p<T>(i, nx, px, dx, [&](int m) { return V(m, j, k); }));
-        T ddy = upw<T>(V(i, j, k), d2n<T>(j, ny + 1, false, dy, [&](int m) { return V(i, m, k); }),
-                       d2p<T>(j, ny + 1, false, dy, [&](int m) { return V(i, m, k); }));
-        T ddz = upw<T>(dmb, d2n<T>(k, nz, false, dz, [&](int m) { return V(i, j, m); }),
-                       d2p<T>(k, nz, false, dz, [&](int m) { return V(i, j, m); }));
-        T vint = ddx + ddy + ddz;
-        T a1 = interp_cf<T>(i + 1, nx, px, [&](int m) { return AT(ymu, m, j, k); }) * dx;
-        T a0 = interp_cf<T>(i, nx, px, [&](int m) { return AT(ymu, m, j, k); }) * dx;
-        T bmb_j = AT(mu, i, clampi(j, 1, ny), k) * dy;
-        T bmb_m = AT(mu, i, clampi(j - 1, 1, ny), k) * dy;
-        T d1 = interp_cf<T>(k + 1, nz, false, [&](int m) { return AT(ymu, i, j, m); }) * dz;
-        T d0 = interp_cf<T>(k, nz, false, [&](int m) { return AT(ymu, i, j, m); }) * dz;
-        T rhoy = interp_cf<T>(j, ny, false, [&](int m) { return AT(rho, i, m, k); });
-        T vc = V(i, j, k);
-        T F = -vint +
-              (a1 * ((V(i + 1, j, k) - vc) * dx + (AT(u, i + 1, j, k) - AT(u, i + 1, j - 1, k)) * dy) -
-               a0 * ((vc - V(i - 1, j, k)) * dx + (AT(u, i, j, k) - AT(u, i, j - 1, k)) * dy) +
-               (bmb_j * T(2.) * (V(i, j + 1, k) - vc) - bmb_m * T(2.) * (vc - V(i, j - 1, k))) * dy +
-               d1 * ((V(i, j, k + 1) - vc) * dz + (AT(w, i, j, k + 1) - AT(w, i, j - 1, k + 1)) * dy) -
-               d0 * ((vc - V(i, j, k - 1)) * dz + (AT(w, i, j, k) - AT(w, i, j - 1, k)) * dy)) /
-                  rhoy;
-        if (fuse) {
-            if (c.t_tens == 1) F = F - tension_face(c, 1, i, j, k);
-            F = F + AT(c.tf_v, i, j, k);
-            if (c.m_turb >= 2) F = F - ka_face(c, 1, i, j, k);
-        }
+        T F = face_fv<T>(c, X, i, j, k);
+        if (fuse) F = compl_fv<T>(c, F, i, j, k);
         AT(c.Fv, i, j, k) = F;
     }
-    // ---- Fw at z-face (i,j,k), k in 1..nz+1 ----
     if (i <= nx && j <= ny && k <= nz + 1) {
-        auto W = [&](int a, int b, int cc) { return AT(w, a, b, cc); };
-        T amd = interp_cf<T>(k, nz, false, [&](int m) { return (AT(u, i, j, m) + AT(u, i + 1, j, m)) * T(0.5); });
-        T bmd = interp_cf<T>(k, nz, false, [&](int m) { return (AT(v, i, j, m) + AT(v, i, j + 1, m)) * T(0.5); });
-        T ddx = upw<T>(amd, d2n<T>(i, nx, px, dx, [&](int m) { return W(m, j, k); }),
-                       d2p<T>(i, nx, px, dx, [&](int m) { return W(m, j, k); }));
-        T ddy = upw<T>(bmd, d2n<T>(j, ny, false, dy, [&](int m) { return W(i, m, k); }),
-                       d2p<T>(j, ny, false, dy, [&](int m) { return W(i, m, k); }));
-        T ddz = upw<T>(W(i, j, k), d2n<T>(k, nz + 1, false, dz, [&](int m) { return W(i, j, m); }),
-                       d2p<T>(k, nz + 1, false, dz, [&](int m) { return W(i, j, m); }));
-        T wint = ddx + ddy + ddz;
-        T a1 = interp_cf<T>(i + 1, nx, px, [&](int m) { return AT(zmu, m, j, k); }) * dx;
-        T a0 = interp_cf<T>(i, nx, px, [&](int m) { return AT(zmu, m, j, k); }) * dx;
-        T b1 = interp_cf<T>(j + 1, ny, false, [&](int m) { return AT(zmu, i, m, k); }) * dy;
-        T b0 = interp_cf<T>(j, ny, false, [&](int m) { return AT(zmu, i, m, k); }) * dy;
-        T dmd_k = AT(mu, i, j, clampi(k, 1, nz)) * dz;
-        T dmd_m = AT(mu, i, j, clampi(k - 1, 1, nz)) * dz;
-        T rhoz = interp_cf<T>(k, nz, false, [&](int m) { return AT(rho, i, j, m); });
-        T wc = W(i, j, k);
-        T F = -wint +
-              (a1 * ((W(i + 1, j, k) - wc) * dx + (AT(u, i + 1, j, k) - AT(u, i + 1, j, k - 1)) * dz) -
-               a0 * ((wc - W(i - 1, j, k)) * dx + (AT(u, i, j, k) - AT(u, i, j, k - 1)) * dz) +
-               b1 * ((W(i, j + 1, k) - wc) * dy + (AT(v, i, j + 1, k) - AT(v, i, j + 1, k - 1)) * dz) -
-               b0 * ((wc - W(i, j - 1, k)) * dy + (AT(v, i, j, k) - AT(v, i, j, k - 1)) * dz) +
-               (dmd_k * T(2.) * (W(i, j, k + 1) - wc) - dmd_m * T(2.) * (wc - W(i, j, k - 1))) * dz) /
-                  rhoz;
-        if (fuse) {
-            F = F - T(c.gz);
-            if (c.epis) F = F - (wc - T(0.)) * AT(c.epis, i, j, k);
-            if (c.t_tens == 1) F = F - tension_face(c, 2, i, j, k);
-            F = F + AT(c.tf_w, i, j, k);
-            if (c.m_turb >= 2) F = F - ka_face(c, 2, i, j, k);
-        }
+        T F = face_fw<T>(c, X, i, j, k);
+        if (fuse) F = compl_fw<T>(c, F, AT(c.w, i, j, k), i, j, k);
         AT(c.Fw, i, j, k) = F;
     }
 }
@@ -732,6 +544,7 @@ template <typename T> void launch_convdiff(const Batch<T> &b, int fuse, cudaStre
 {
     k_convdiff<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases, fuse); count_launch();
 }
+
 template <typename T> void launch_complementos(const Batch<T> &b, cudaStream_t s)
 {
     k_complementos<T><<<b.total_tiles, b.block(), 0, s>>>(b.dcases, b.ncases); count_launch();

@@ -9,6 +9,8 @@
 #include "../../include/suli_gpu.h"
 #include "suli_kernels.cuh"
 
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -321,6 +323,7 @@ struct Impl : ImplBase {
         for (auto &gx : pcg_graph)
             if (gx) cudaGraphExecDestroy(gx);
         cudaFree(drk);
+        cudaFree(dtmaps);
         cudaFree(b.dcases);
         if (hsc) cudaFreeHost(hsc);
         cudaFree(out_dev);
@@ -391,7 +394,8 @@ struct Impl : ImplBase {
         P.assign(p, p + n);
         CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
         hc.resize(n);
-        int tiles = 0, chunks = 0, maxplane = 1;
+        int tiles = 0, chunks = 0, maxplane = 1, cd_units_total = 0;
+        long long cd_shell_total = 0;
         for (int c = 0; c < n; ++c) {
             const suli_params &q = P[c];
             CaseDev<T> &cd = hc[c];
@@ -411,6 +415,10 @@ struct Impl : ImplBase {
             cd.nchunks = col_units(q.nx, q.ny, q.nz);
             cd.chunk_begin = chunks;
             chunks += cd.nchunks;
+            cd.cd_begin = cd_units_total;
+            cd_units_total += convdiff_units(q.nx, q.ny, q.nz);
+            cd.cd_shell_begin = cd_shell_total;
+            cd_shell_total += convdiff_shell_positions(q.nx, q.ny, q.nz);
             long long mp = std::max({(long long)(q.nx + 3) * (q.nz + 3), (long long)(q.nx + 3) * (q.ny + 3),
                                      (long long)(q.ny + 3) * (q.nz + 3),
                                      (long long)(q.nx + 2) * (q.nz + 2) + (long long)(q.nx + 2) * (q.ny + 2) +
@@ -532,6 +540,8 @@ struct Impl : ImplBase {
         b.total_tiles = tiles;
         b.total_units = chunks;
         b.max_plane = maxplane;
+        b.total_cd_units = cd_units_total;
+        b.total_cd_shell = cd_shell_total;
         CK(cudaMalloc(&dsc, sizeof(double) * S_NSCAL * n));
         CK(cudaMemsetAsync(dsc, 0, sizeof(double) * S_NSCAL * n, st));
         // reduction partials: one per tile (tile kernels) or one per warp of
@@ -567,6 +577,7 @@ struct Impl : ImplBase {
         CK(cudaMalloc(&b.dcases, sizeof(CaseDev<T>) * n));
         CK(cudaMemcpyAsync(b.dcases, hc.data(), sizeof(CaseDev<T>) * n, cudaMemcpyHostToDevice, st));
         b.hcases = hc.data();
+        if (int rc = make_tensor_maps()) return rc;
         // time-integration coefficients, coef_tempo (2_iniciais.f90:278-312)
         dt0 = dt = P[0].dt;
         if (P[0].t_tempo == 1 || P[0].t_tempo == 2) {
@@ -579,6 +590,48 @@ struct Impl : ImplBase {
         for (int c = 0; c < n; ++c) setsc_host_init(c);
         CK(cudaMemcpyAsync(dsc, hsc, sizeof(double) * S_NSCAL * n, cudaMemcpyHostToDevice, st));
         CK(cudaStreamSynchronize(st));
+        return SULI_OK;
+    }
+
+    // Tensor maps of the TMA-staged convdiff: per case u, v, w, rho, mu, xmu,
+    // ymu, zmu, each its padded box (sx x (ny+3) x (nz+3) elements, x
+    // unit-stride) read in boxes of 40 x 12 x 1; out-of-box elements load as
+    // zeros.  Without the driver's encoder (or with SULI_CONVDIFF=0) the
+    // gather kernel runs instead.
+    CUtensorMap *dtmaps = nullptr;
+    int make_tensor_maps()
+    {
+        const char *env = std::getenv("SULI_CONVDIFF");
+        if (env && std::string(env) == "0") return SULI_OK;
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult qr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &qr) !=
+                cudaSuccess || qr != cudaDriverEntryPointSuccess || !fn) {
+            cudaGetLastError();
+            return SULI_OK;
+        }
+        auto encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+        std::vector<CUtensorMap> maps((size_t)ncases * 8);
+        for (int c = 0; c < ncases; ++c) {
+            const CaseDev<T> &cd = hc[c];
+            const T *arr[8] = {cd.u, cd.v, cd.w, cd.rho, cd.mu, cd.xmu, cd.ymu, cd.zmu};
+            const cuuint64_t dims[3] = {(cuuint64_t)cd.g.sx, (cuuint64_t)(cd.g.ny + 3), (cuuint64_t)(cd.g.nz + 3)};
+            const cuuint64_t strides[2] = {(cuuint64_t)cd.g.sx * sizeof(T), (cuuint64_t)cd.g.sxy * sizeof(T)};
+            const cuuint32_t box[3] = {(cuuint32_t)CD_MAP_BOX_X, (cuuint32_t)CD_MAP_BOX_Y, 1};
+            const cuuint32_t estr[3] = {1, 1, 1};
+            for (int a = 0; a < 8; ++a) {
+                CUresult r = encode(&maps[(size_t)c * 8 + a],
+                                    sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3,
+                                    (void *)arr[a], dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                if (r != CUDA_SUCCESS) return SULI_OK;   // no maps: the gather kernel runs
+            }
+        }
+        CK(cudaMalloc(&dtmaps, sizeof(CUtensorMap) * maps.size()));
+        CK(cudaMemcpyAsync(dtmaps, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice, st));
+        CK(cudaStreamSynchronize(st));
+        b.tmaps = dtmaps;
         return SULI_OK;
     }
 
@@ -913,6 +966,9 @@ struct Impl : ImplBase {
     {
         for (int c = 0; c < ncases; ++c) {
             const double v = sc(c, S_VOLINS), m = sc(c, S_MAXDIV);
+            if (sc(c, S_TMAERR) != 0.0)
+                return fail(SULI_DEVICE_TIMEOUT, "case " + std::to_string(c) +
+                                                     ": a bounded wait for a TMA copy gave up (convdiff)");
             if (!std::isfinite(v) || !std::isfinite(m))
                 return fail(SULI_NONFINITE, "case " + std::to_string(c) + ": non-finite state (vol_ins " +
                                                 std::to_string(v) + ", max|div| " + std::to_string(m) + ")");
@@ -1017,7 +1073,8 @@ struct Impl : ImplBase {
     int convdiff(int fuse) override
     {
         if (fuse) launch_sponge<T>(b, st);     // complementos' sponge_layer call
-        launch_convdiff<T>(b, fuse, st);
+        if (b.tmaps) launch_convdiff_tma<T>(b, fuse, st);
+        else launch_convdiff<T>(b, fuse, st);
         CKL();
         return SULI_OK;
     }

@@ -12,6 +12,7 @@
 // at 1), i (x) unit-stride as in the Fortran column-major originals.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -67,6 +68,7 @@ enum Scal {
     S_STALL,       // mixed form: consecutive passes that did not halve the best FP64 r.r
     S_RRBEST,      // mixed form: the lowest FP64 r.r of the solve so far
     S_STALLED,     // mixed form: 1 when the refinement ended on stagnation
+    S_TMAERR,      // 1 when a bounded wait for a TMA copy gave up (SULI_DEVICE_TIMEOUT)
     S_NSCAL
 };
 
@@ -116,6 +118,10 @@ struct CaseDev {
     // column units of the case grid (the unit of the persistent CG kernels
     // and of their reductions), see col_units
     int chunk_begin, nchunks;
+    // first unit of this case in the launch grid of the TMA-staged convdiff,
+    // and its first boundary-shell position in the shell kernel's grid
+    int cd_begin;
+    long long cd_shell_begin;
     // discretisation / physics (double in both forms)
     double dx, dy, dz, dx1, dt1, deltai;
     double idx, idy, idz;       // 1/dx, 1/dy, 1/dz (mixed-form kernels multiply)

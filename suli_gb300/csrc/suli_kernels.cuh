@@ -37,6 +37,9 @@ struct Batch {
     unsigned *act_done = nullptr;     // cases done with the current B phase
     int nlev = 1;                     // grid levels in the tables (multigrid levels, or 1)
     int mg_tiles[MG_MAXL] = {0};      // tiles of multigrid level l over all cases
+    const CUtensorMap *tmaps = nullptr;   // per case the tensor maps of the convdiff operands (or null)
+    int total_cd_units = 0;           // units of the TMA-staged convdiff over all cases
+    long long total_cd_shell = 0;     // boundary-shell positions of convdiff over all cases
     dim3 block() const { return dim3(TX, TY, TZ); }
     dim3 cblock() const { return dim3(COL_X, COL_Y, 1); }   // persistent (column) kernels
 };
@@ -58,6 +61,13 @@ template <typename T> void launch_contorno_les(const Batch<T> &b, cudaStream_t s
 template <typename T> void launch_exp_press(const Batch<T> &b, cudaStream_t s);
 template <typename T> void launch_waves(const Batch<T> &b, double t, cudaStream_t s);
 template <typename T> void launch_convdiff(const Batch<T> &b, int fuse_compl, cudaStream_t s);
+// convdiff (+ complementos) with its operands staged by TMA tensor loads
+// (k_convdiff_tma.cu): b.tmaps holds 8 maps per case (u, v, w, rho, mu, xmu,
+// ymu, zmu: each the case's padded box, box 40 x 12 x 1)
+template <typename T> void launch_convdiff_tma(const Batch<T> &b, int fuse_compl, cudaStream_t s);
+int convdiff_units(int nx, int ny, int nz);
+long long convdiff_shell_positions(int nx, int ny, int nz);
+constexpr int CD_MAP_BOX_X = 40, CD_MAP_BOX_Y = 12;
 // sponge_layer's epis_z for the esp_type > 0 cases (before complementos)
 template <typename T> void launch_sponge(const Batch<T> &b, cudaStream_t s);
 template <typename T> void launch_complementos(const Batch<T> &b, cudaStream_t s);
