@@ -735,6 +735,10 @@ def main():
     line["roofline_cg_matvec"] = {"kernel": "k_cgi_A", "achieved": bytes_a / (ms_a / 1e3) / 1e9,
                                   "ms_per_launch": ms_a, "algorithmic_bytes_per_launch": bytes_a}
     line["cg_loop"] = {"cell_iters": prof_m.cg_cell_iters, "ms": prof_m.cg_ms}
+    tun = gm.tuning()
+    tun["gain"] = tun["default_ms"] / tun["tuned_ms"] if tun["tuned_ms"] > 0 else None
+    tun["timed"] = "one convdiff, one V-cycle and one level-0 sweep over every case, defaults vs chosen shapes"
+    line["autotune"] = tun
     diag = gm.diag(0)
     line["cg_iters_case0"] = list(diag.cg_iters)
     line["cg_outer_case0"] = list(diag.cg_outer)

@@ -304,6 +304,29 @@ int suli_profile_read(suli_handle *h, suli_profile_t *out);
  * moves.  The solver work arrays it touches are rebuilt by the next
  * suli_graddin. */
 int suli_time_kernel(suli_handle *h, int kernel, int reps, double *ms_per_launch, double *bytes_per_launch);
+/* Autotuner (no counterpart in the reference).  Launch shapes of the hot
+ * kernels -- the planes per unit of the TMA-staged convdiff (8, 16, 32), the
+ * largest multigrid level handled by the one-block coarse end of the V-cycle,
+ * the blocks per SM of the one-pass level-0 smoother sweep -- are timed with
+ * CUDA events on the handle's stream and the fastest kept; every choice gives
+ * the same bits (only the partition of the work changes).  suli_step tunes a
+ * handle once, after its first time step (the operator and the work arrays
+ * exist by then; tuning touches only scratch arrays), unless the environment
+ * sets SULI_TUNE=0; the choice is cached per device and workload shape
+ * (precision, cases, cells, multigrid levels), so further handles of the same
+ * shape reuse it.  suli_autotune tunes now (or applies the cached choice);
+ * suli_get_tuning reports the current one. */
+typedef struct suli_tuning {
+    int32_t convdiff_planes;      /* planes per unit of the TMA-staged convdiff (0: gather kernel) */
+    int32_t mg_block_cells;       /* largest level (cells) of the one-block V-cycle end; 0: none */
+    int32_t sweep_blocks_per_sm;  /* blocks per SM of the level-0 sweep; 0: occupancy limit */
+    int32_t tuned;                /* 1: chosen by timing (this handle or the cache), 0: defaults */
+    double  default_ms;           /* the timed kernels at the defaults (one convdiff, one V-cycle, one sweep) */
+    double  tuned_ms;             /* the same at the chosen shapes */
+} suli_tuning;
+int suli_autotune(suli_handle *h, suli_tuning *out);
+int suli_get_tuning(suli_handle *h, suli_tuning *out);
+
 /* PRTSCR (4_plot.f90:501-635), the field record of one case: written to
  * `path` as one Fortran unformatted sequential record (gfortran framing: a
  * 4-byte little-endian byte count before and after) of float32 arrays in

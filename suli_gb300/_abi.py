@@ -90,6 +90,16 @@ class SuliDiag(C.Structure):
     ]
 
 
+class SuliTuning(C.Structure):
+    """suli_tuning: the autotuner's launch shapes and the timed gain."""
+    _fields_ = [("convdiff_planes", C.c_int32), ("mg_block_cells", C.c_int32),
+                ("sweep_blocks_per_sm", C.c_int32), ("tuned", C.c_int32),
+                ("default_ms", C.c_double), ("tuned_ms", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 def default_params(**kw) -> SuliParams:
     """Reference defaults (00_suli3d.prm / 2_iniciais.f90) plus build knobs."""
     p = SuliParams()

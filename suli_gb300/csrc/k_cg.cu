@@ -808,6 +808,7 @@ template <typename T> int launch_profile_kernel(const Batch<T> &b, int kernel, i
     else if (kernel == 1) return launch_mg_smooth0<T>(b, tab, 0, s);
     else if (kernel == 2) k_cgi_C<T><<<G.C, b.cblock(), 0, s>>>(b.dcases, tab, b.ncases);
     else if (kernel == 3) return launch_mg_sweep0<T>(b, tab, s);
+    else if (kernel == 4) return launch_mg_vcycle_prof<T>(b, tab, s);
     else return -1;
     count_launch();
     return 0;

@@ -10,8 +10,8 @@
 // Both run the per-face arithmetic of conv_faces.cuh.
 //
 // Work unit: a column of 32 x 8 positions (i, j) -- one per thread of a 32 x
-// 8 block -- and CD_Z planes k; each thread forms Fu, Fv and Fw at its (i, j,
-// k) for every k of the column.  The stencils reach two cells along every
+// 8 block -- and CD_Z planes k (8, 16 or 32: the autotuner's choice); each
+// thread forms Fu, Fv and Fw at its (i, j, k) for every k of the column.  The stencils reach two cells along every
 // axis, so for each plane p the block stages, for each of the eight operand
 // arrays (u, v, w, rho, mu, xmu, ymu, zmu), the box x in [i0 - 2, i0 + 38),
 // y in [j0 - 2, j0 + 10) of plane p: one 40 x 12 x 1 cp.async.bulk.tensor
@@ -29,7 +29,7 @@
 
 namespace suli {
 
-constexpr int CD_X = 32, CD_Y = 8, CD_Z = 16;    // unit: positions per thread block
+constexpr int CD_X = 32, CD_Y = 8;              // unit: positions per thread block (x, y)
 constexpr int CD_BX = CD_MAP_BOX_X, CD_BY = CD_MAP_BOX_Y;   // staged box of one array and plane
 constexpr int CD_BOX = CD_BX * CD_BY;
 constexpr int CD_NARR = 8;                       // u, v, w, rho, mu, xmu, ymu, zmu
@@ -37,9 +37,10 @@ constexpr int CD_RING = 6;                       // plane slots
 constexpr int CD_SLOT = CD_NARR * CD_BOX;        // elements of one slot
 constexpr unsigned CD_WAIT_MAX = 1u << 22;       // bounded mbarrier polls
 
-__host__ __device__ __forceinline__ int cd_units(int nx, int ny, int nz)
+// units of a case with kz planes a unit (kz = CD_PLANES[v], the tuner's choice)
+__host__ __device__ __forceinline__ int cd_units(int nx, int ny, int nz, int kz)
 {
-    return ((nx - 2 + CD_X - 1) / CD_X) * ((ny - 2 + CD_Y - 1) / CD_Y) * ((nz - 2 + CD_Z - 1) / CD_Z);
+    return ((nx - 2 + CD_X - 1) / CD_X) * ((ny - 2 + CD_Y - 1) / CD_Y) * ((nz - 2 + kz - 1) / kz);
 }
 
 template <typename T> constexpr size_t cd_smem() { return (size_t)CD_RING * CD_SLOT * sizeof(T) + 128; }
@@ -148,9 +149,9 @@ __device__ __forceinline__ void cd_interior_pos(const CaseDev<T> &c, const Stage
     c.Fw[q] = F;
 }
 
-template <typename T>
+template <typename T, int CD_Z>
 __global__ void __launch_bounds__(CD_X *CD_Y, sizeof(T) == 4 ? 2 : 1)
-    k_convdiff_tma(const CaseDev<T> *__restrict__ cs, int ncases, const CUtensorMap *__restrict__ maps, int fuse)
+    k_convdiff_tma(const CaseDev<T> *__restrict__ cs, int ncases, const CUtensorMap *__restrict__ maps, int fuse, int v)
 {
     extern __shared__ unsigned char cd_dyn[];
     __shared__ __align__(8) uint64_t bar[CD_RING];
@@ -159,10 +160,10 @@ __global__ void __launch_bounds__(CD_X *CD_Y, sizeof(T) == 4 ? 2 : 1)
     int lo = 0, hi = ncases - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        if (cs[mid].cd_begin <= (int)blockIdx.x) lo = mid; else hi = mid - 1;
+        if (cs[mid].cd_begin[v] <= (int)blockIdx.x) lo = mid; else hi = mid - 1;
     }
     const CaseDev<T> &c = cs[lo];
-    const int u = (int)blockIdx.x - c.cd_begin;
+    const int u = (int)blockIdx.x - c.cd_begin[v];
     const int nx = c.g.nx, ny = c.g.ny, nz = c.g.nz;
     const int ux = (nx - 2 + CD_X - 1) / CD_X, uy = (ny - 2 + CD_Y - 1) / CD_Y;
     const int ax = u % ux;
@@ -300,19 +301,28 @@ __global__ void __launch_bounds__(256) k_convdiff_shell(const CaseDev<T> *__rest
 
 long long convdiff_shell_positions(int nx, int ny, int nz) { return cd_shell_count(nx, ny, nz); }
 
+template <typename T, int KZ> static void launch_tma_kz(const Batch<T> &b, int fuse, int v, cudaStream_t s)
+{
+    cudaFuncSetAttribute((const void *)k_convdiff_tma<T, KZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)cd_smem<T>());
+    k_convdiff_tma<T, KZ><<<b.total_cd_units[v], dim3(CD_X, CD_Y), cd_smem<T>(), s>>>(b.dcases, b.ncases, b.tmaps,
+                                                                                      fuse, v);
+}
+
 template <typename T> void launch_convdiff_tma(const Batch<T> &b, int fuse, cudaStream_t s)
 {
-    cudaFuncSetAttribute((const void *)k_convdiff_tma<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)cd_smem<T>());
-    k_convdiff_tma<T><<<b.total_cd_units, dim3(CD_X, CD_Y), cd_smem<T>(), s>>>(b.dcases, b.ncases, b.tmaps, fuse);
+    const int v = b.tune.cd_variant;
+    if (v == 0) launch_tma_kz<T, 8>(b, fuse, 0, s);
+    else if (v == 2) launch_tma_kz<T, 32>(b, fuse, 2, s);
+    else launch_tma_kz<T, 16>(b, fuse, 1, s);
+    count_launch();
     // the boundary shell (i, j or k at the domain's edges): the general stencils
     const long long n = b.total_cd_shell;
     k_convdiff_shell<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b.dcases, b.ncases, fuse, n);
     count_launch();
-    count_launch();
 }
 
-int convdiff_units(int nx, int ny, int nz) { return cd_units(nx, ny, nz); }
+int convdiff_units(int nx, int ny, int nz, int variant) { return cd_units(nx, ny, nz, CD_PLANES[variant]); }
 
 template void launch_convdiff_tma<float>(const Batch<float> &, int, cudaStream_t);
 template void launch_convdiff_tma<double>(const Batch<double> &, int, cudaStream_t);

@@ -381,10 +381,21 @@ __global__ void __launch_bounds__(NTHREADS, 4) k_mg_sweep0(const CaseDev<T> *__r
 
 // the one-pass sweep's grid: its dynamic shared memory opted in, every SM
 // filled to the occupancy that memory allows
-template <typename T> int sweep0_grid()
+template <typename T> int sweep0_grid(const Batch<T> &b)
 {
-    cudaFuncSetAttribute((const void *)k_mg_sweep0<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SW_SMEM);
-    return occupancy_grid((const void *)k_mg_sweep0<T>, SW_SMEM);
+    static const int full = [] {
+        cudaFuncSetAttribute((const void *)k_mg_sweep0<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SW_SMEM);
+        return occupancy_grid((const void *)k_mg_sweep0<T>, SW_SMEM);
+    }();
+    static const int sms = [] {
+        int dev = 0, n = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        return n > 0 ? n : 1;
+    }();
+    // the autotuner may run fewer blocks per SM than the occupancy limit
+    const int per = b.tune.sweep_blocks_per_sm;
+    return (per > 0 && per * sms < full) ? per * sms : full;
 }
 
 // f(l) = P^T (f - L z)(l-1): the coarse right-hand side, each coarse cell
@@ -586,12 +597,12 @@ __global__ void __launch_bounds__(MG_COARSE_THREADS) k_mg_coarse(const CaseDev<T
 }
 
 // first level handled by k_mg_coarse: the first whose largest grid over the
-// batch has at most SULI_MG_CTA_CELLS cells (default 16384; 0: none, every
-// level by whole-grid launches); at least 1, at most NL (none)
+// batch has at most b.tune.mg_block_cells cells (the autotuner's choice,
+// default 16384; 0: none, every level by whole-grid launches); at least 1, at
+// most NL (none)
 template <typename T> int mg_block_level(const Batch<T> &b)
 {
-    const char *e = std::getenv("SULI_MG_CTA_CELLS");
-    const int limit = e ? std::atoi(e) : 16384;
+    const int limit = b.tune.mg_block_cells;
     if (limit <= 0) return b.nlev;
     for (int l = 1; l < b.nlev; ++l) {
         long long mx = 0;
@@ -707,7 +718,7 @@ template <typename T> void launch_mg_vcycle(const Batch<T> &b, const int *tab, i
     // as two half-sweep launches each: the same arithmetic
     const char *fe = std::getenv("SULI_MG_FUSED");
     const bool fused = !(fe && std::atoi(fe) == 0);
-    static const int gW = sweep0_grid<T>();
+    const int gW = sweep0_grid<T>(b);
     const int ncoarse = 6;
     // levels lc.. in one block per case (k_mg_coarse), the finer ones by
     // whole-grid launches
@@ -779,13 +790,24 @@ template <> int launch_mg_smooth0<double>(const Batch<double> &, const int *, in
 template <typename T> int launch_mg_sweep0(const Batch<T> &b, const int *tab, cudaStream_t s)
 {
     if (b.nlev < 2) return -1;
-    static const int gW = sweep0_grid<T>();
+    const int gW = sweep0_grid<T>(b);
     k_mg_sweep0<T><<<gW, b.cblock(), SW_SMEM, s>>>(b.dcases, tab, b.ncases, 0, 0, 0, 1);
     count_launch();
     return 0;
 }
 template <> int launch_mg_sweep0<double>(const Batch<double> &, const int *, cudaStream_t) { return -1; }
 
+// profiling and tuning: one V-cycle over table `tab` (mixed form with the
+// multigrid passes only)
+template <typename T> int launch_mg_vcycle_prof(const Batch<T> &b, const int *tab, cudaStream_t s)
+{
+    if (b.nlev < 2) return -1;
+    launch_mg_vcycle<T>(b, tab, 0, s);
+    return 0;
+}
+template <> int launch_mg_vcycle_prof<double>(const Batch<double> &, const int *, cudaStream_t) { return -1; }
+
+template int launch_mg_vcycle_prof<float>(const Batch<float> &, const int *, cudaStream_t);
 template void launch_mg_coarsen<float>(const Batch<float> &, cudaStream_t);
 template int launch_mg_smooth0<float>(const Batch<float> &, const int *, int, cudaStream_t);
 template int launch_mg_sweep0<float>(const Batch<float> &, const int *, cudaStream_t);

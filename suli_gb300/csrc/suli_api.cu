@@ -12,6 +12,9 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -183,6 +186,8 @@ struct ImplBase {
     virtual int contorno_les() = 0;
     virtual bool stored(int icase, int f) = 0;
     virtual int boundary_waves() = 0;
+    virtual int autotune(suli_tuning *out) = 0;
+    virtual int get_tuning(suli_tuning *out) = 0;
     unsigned long long inflow_calls = 0;
     int ncases = 0;
     std::vector<suli_params> P;
@@ -394,7 +399,7 @@ struct Impl : ImplBase {
         P.assign(p, p + n);
         CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
         hc.resize(n);
-        int tiles = 0, chunks = 0, maxplane = 1, cd_units_total = 0;
+        int tiles = 0, chunks = 0, maxplane = 1, cd_units_total[3] = {0, 0, 0};
         long long cd_shell_total = 0;
         for (int c = 0; c < n; ++c) {
             const suli_params &q = P[c];
@@ -415,8 +420,10 @@ struct Impl : ImplBase {
             cd.nchunks = col_units(q.nx, q.ny, q.nz);
             cd.chunk_begin = chunks;
             chunks += cd.nchunks;
-            cd.cd_begin = cd_units_total;
-            cd_units_total += convdiff_units(q.nx, q.ny, q.nz);
+            for (int v = 0; v < 3; ++v) {
+                cd.cd_begin[v] = cd_units_total[v];
+                cd_units_total[v] += convdiff_units(q.nx, q.ny, q.nz, v);
+            }
             cd.cd_shell_begin = cd_shell_total;
             cd_shell_total += convdiff_shell_positions(q.nx, q.ny, q.nz);
             long long mp = std::max({(long long)(q.nx + 3) * (q.nz + 3), (long long)(q.nx + 3) * (q.ny + 3),
@@ -540,7 +547,7 @@ struct Impl : ImplBase {
         b.total_tiles = tiles;
         b.total_units = chunks;
         b.max_plane = maxplane;
-        b.total_cd_units = cd_units_total;
+        for (int v = 0; v < 3; ++v) b.total_cd_units[v] = cd_units_total[v];
         b.total_cd_shell = cd_shell_total;
         CK(cudaMalloc(&dsc, sizeof(double) * S_NSCAL * n));
         CK(cudaMemsetAsync(dsc, 0, sizeof(double) * S_NSCAL * n, st));
@@ -578,6 +585,7 @@ struct Impl : ImplBase {
         CK(cudaMemcpyAsync(b.dcases, hc.data(), sizeof(CaseDev<T>) * n, cudaMemcpyHostToDevice, st));
         b.hcases = hc.data();
         if (int rc = make_tensor_maps()) return rc;
+        tune_defaults();
         // time-integration coefficients, coef_tempo (2_iniciais.f90:278-312)
         dt0 = dt = P[0].dt;
         if (P[0].t_tempo == 1 || P[0].t_tempo == 2) {
@@ -911,6 +919,148 @@ struct Impl : ImplBase {
             m.kind = cudaMemcpyDeviceToHost;
         }
         CK(cudaMemcpy3DAsync(&m, st));
+        return SULI_OK;
+    }
+
+    // ---- autotuner -------------------------------------------------------------
+    bool tuned = false, tune_locked_mg = false;
+    int tune_env = -1;                 // SULI_TUNE: 0 off
+    double tune_default_ms = 0.0, tune_tuned_ms = 0.0;
+    using TuneKey = std::tuple<int, int, int, long long, int>;   // device, precision, cases, cells, levels
+    struct TuneVal { Tuning t; double dms, tms; };
+    static std::map<TuneKey, TuneVal> &tune_cache()
+    {
+        static std::map<TuneKey, TuneVal> m;
+        return m;
+    }
+    static std::mutex &tune_mu()
+    {
+        static std::mutex m;
+        return m;
+    }
+    void tune_defaults()
+    {
+        // environment overrides, for comparisons and tests (SULI_MG_CTA_CELLS
+        // also keeps the tuner off that knob; forced shapes switch it off)
+        if (const char *e = std::getenv("SULI_MG_CTA_CELLS")) {
+            b.tune.mg_block_cells = std::atoi(e);
+            tune_locked_mg = true;
+        }
+        if (const char *e = std::getenv("SULI_TUNE_CD")) b.tune.cd_variant = std::max(0, std::min(2, std::atoi(e)));
+        if (const char *e = std::getenv("SULI_TUNE_SWEEP")) b.tune.sweep_blocks_per_sm = std::max(0, std::atoi(e));
+        const char *e = std::getenv("SULI_TUNE");
+        tune_env = (e && std::atoi(e) == 0) ? 0 : 1;
+        if (std::getenv("SULI_TUNE_CD") || std::getenv("SULI_TUNE_SWEEP")) tune_env = 0;
+    }
+    // mean time of `reps` calls of f on the stream, after one untimed call
+    template <typename F> double time_it(F f, int reps)
+    {
+        f();
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, st);
+        for (int r = 0; r < reps; ++r) f();
+        cudaEventRecord(e1, st);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return (double)ms / reps;
+    }
+    void drop_graphs()
+    {
+        for (auto &gx : pcg_graph)
+            if (gx) { cudaGraphExecDestroy(gx); gx = nullptr; }
+        pcg_plain_done = false;
+    }
+    int autotune(suli_tuning *out) override
+    {
+        int dev = 0;
+        CK(cudaGetDevice(&dev));
+        long long cells_all = 0;
+        for (int c = 0; c < ncases; ++c) cells_all += (long long)P[c].nx * P[c].ny * P[c].nz;
+        const TuneKey key{dev, (int)sizeof(T), ncases, cells_all, b.nlev};
+        {
+            std::lock_guard<std::mutex> lk(tune_mu());
+            auto it = tune_cache().find(key);
+            if (it != tune_cache().end()) {
+                const int mgc = b.tune.mg_block_cells;
+                b.tune = it->second.t;
+                if (tune_locked_mg) b.tune.mg_block_cells = mgc;
+                tune_default_ms = it->second.dms;
+                tune_tuned_ms = it->second.tms;
+                tuned = true;
+                drop_graphs();
+                return get_tuning(out);
+            }
+        }
+        CK(cudaStreamSynchronize(st));
+        const Tuning def;
+        double dms = 0.0, tms = 0.0;
+        // convdiff (+ complementos): planes per unit; writes only Fu, Fv, Fw,
+        // which every stage recomputes before it reads them
+        if (b.tmaps) {
+            double best = 1e30;
+            int bv = def.cd_variant;
+            for (int v = 0; v < 3; ++v) {
+                b.tune.cd_variant = v;
+                const double ms = time_it([&] { launch_convdiff_tma<T>(b, 1, st); }, 3);
+                if (v == def.cd_variant) dms += ms;
+                if (ms < best) { best = ms; bv = v; }
+            }
+            b.tune.cd_variant = bv;
+            tms += best;
+        }
+        // the multigrid V-cycle (mixed form): the coarse-end threshold, then
+        // the level-0 sweep's blocks per SM; both on the all-case table and
+        // touching only the V-cycle's own levels (rebuilt by the next solve)
+        if (b.nlev > 1 && op_valid) {
+            if (launch_profile_kernel<T>(b, 4, 1, st) != 0) return fail(SULI_CUDA_ERROR, "V-cycle timing");
+            if (!tune_locked_mg) {
+                double best = 1e30;
+                int bc = def.mg_block_cells;
+                for (int cells : {0, 4096, 16384, 65536}) {
+                    b.tune.mg_block_cells = cells;
+                    const double ms = time_it([&] { launch_profile_kernel<T>(b, 4, 0, st); }, 2);
+                    if (cells == def.mg_block_cells) dms += ms;
+                    if (ms < best) { best = ms; bc = cells; }
+                }
+                b.tune.mg_block_cells = bc;
+                tms += best;
+            }
+            double best = 1e30;
+            int bs = def.sweep_blocks_per_sm;
+            for (int per : {0, 3, 2}) {
+                b.tune.sweep_blocks_per_sm = per;
+                const double ms = time_it([&] { launch_profile_kernel<T>(b, 3, 0, st); }, 5);
+                if (per == def.sweep_blocks_per_sm) dms += ms;
+                if (ms < best) { best = ms; bs = per; }
+            }
+            b.tune.sweep_blocks_per_sm = bs;
+            tms += best;
+        }
+        CKL();
+        tune_default_ms = dms;
+        tune_tuned_ms = tms;
+        tuned = true;
+        drop_graphs();   // captured iterations hold the old launch shapes
+        {
+            std::lock_guard<std::mutex> lk(tune_mu());
+            tune_cache()[key] = TuneVal{b.tune, dms, tms};
+        }
+        return get_tuning(out);
+    }
+    int get_tuning(suli_tuning *out) override
+    {
+        if (!out) return SULI_OK;
+        out->convdiff_planes = b.tmaps ? CD_PLANES[b.tune.cd_variant] : 0;
+        out->mg_block_cells = b.tune.mg_block_cells;
+        out->sweep_blocks_per_sm = b.tune.sweep_blocks_per_sm;
+        out->tuned = tuned ? 1 : 0;
+        out->default_ms = tune_default_ms;
+        out->tuned_ms = tune_tuned_ms;
         return SULI_OK;
     }
 
@@ -1305,6 +1455,8 @@ struct Impl : ImplBase {
                 if (rc && rc != SULI_CG_MAXITER) return rc;
             }
             if ((rc = conmassa(nullptr))) return rc;
+            // the autotuner, once, after the handle's first step
+            if (!tuned && tune_env == 1 && (rc = autotune(nullptr))) return rc;
         }
         return SULI_OK;
     }
@@ -1509,6 +1661,9 @@ extern "C" int suli_diagnostics(suli_handle *h, int icase, suli_diag *d)
     im->warn = 0;
     return SULI_OK;
 }
+
+extern "C" int suli_autotune(suli_handle *h, suli_tuning *out) { HCHK(); return h->impl->autotune(out); }
+extern "C" int suli_get_tuning(suli_handle *h, suli_tuning *out) { HCHK(); return h->impl->get_tuning(out); }
 
 extern "C" int suli_get_stream(suli_handle *h, void **stream)
 {

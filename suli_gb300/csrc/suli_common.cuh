@@ -120,7 +120,7 @@ struct CaseDev {
     int chunk_begin, nchunks;
     // first unit of this case in the launch grid of the TMA-staged convdiff,
     // and its first boundary-shell position in the shell kernel's grid
-    int cd_begin;
+    int cd_begin[3];            // per unit height of the tuner's choice (8, 16, 32 planes)
     long long cd_shell_begin;
     // discretisation / physics (double in both forms)
     double dx, dy, dz, dx1, dt1, deltai;

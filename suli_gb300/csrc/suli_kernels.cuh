@@ -23,6 +23,15 @@ inline int occupancy_grid(const void *fn, size_t dyn_smem = 0)
 extern std::atomic<unsigned long long> g_launches;
 inline void count_launch(unsigned long long n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
+// Launch shapes that the autotuner picks per device and workload shape; every
+// choice gives the same bits (only the partition of the work changes).
+constexpr int CD_PLANES[3] = {8, 16, 32};   // planes per unit of the TMA-staged convdiff
+struct Tuning {
+    int cd_variant = 1;           // index into CD_PLANES
+    int mg_block_cells = 16384;   // largest level (cells) of the one-block coarse end of the V-cycle; 0: none
+    int sweep_blocks_per_sm = 0;  // blocks per SM of the one-pass level-0 sweep; 0: its occupancy limit
+};
+
 // A batch of cases with a device copy of their CaseDev table.
 template <typename T>
 struct Batch {
@@ -38,7 +47,8 @@ struct Batch {
     int nlev = 1;                     // grid levels in the tables (multigrid levels, or 1)
     int mg_tiles[MG_MAXL] = {0};      // tiles of multigrid level l over all cases
     const CUtensorMap *tmaps = nullptr;   // per case the tensor maps of the convdiff operands (or null)
-    int total_cd_units = 0;           // units of the TMA-staged convdiff over all cases
+    int total_cd_units[3] = {0, 0, 0};   // units of the TMA-staged convdiff over all cases, per unit height
+    Tuning tune;                      // the autotuner's launch shapes
     long long total_cd_shell = 0;     // boundary-shell positions of convdiff over all cases
     dim3 block() const { return dim3(TX, TY, TZ); }
     dim3 cblock() const { return dim3(COL_X, COL_Y, 1); }   // persistent (column) kernels
@@ -65,7 +75,7 @@ template <typename T> void launch_convdiff(const Batch<T> &b, int fuse_compl, cu
 // (k_convdiff_tma.cu): b.tmaps holds 8 maps per case (u, v, w, rho, mu, xmu,
 // ymu, zmu: each the case's padded box, box 40 x 12 x 1)
 template <typename T> void launch_convdiff_tma(const Batch<T> &b, int fuse_compl, cudaStream_t s);
-int convdiff_units(int nx, int ny, int nz);
+int convdiff_units(int nx, int ny, int nz, int variant);
 long long convdiff_shell_positions(int nx, int ny, int nz);
 constexpr int CD_MAP_BOX_X = 40, CD_MAP_BOX_Y = 12;
 // sponge_layer's epis_z for the esp_type > 0 cases (before complementos)
@@ -106,6 +116,7 @@ template <typename T> int launch_pcg_iters(const Batch<T> &b, int n, int slot, c
 template <typename T> int launch_profile_kernel(const Batch<T> &b, int kernel, int prepare, cudaStream_t s);
 template <typename T> int launch_mg_smooth0(const Batch<T> &b, const int *tab, int grid, cudaStream_t s);
 template <typename T> int launch_mg_sweep0(const Batch<T> &b, const int *tab, cudaStream_t s);
+template <typename T> int launch_mg_vcycle_prof(const Batch<T> &b, const int *tab, cudaStream_t s);
 
 // multigrid (k_mg.cu): coarse operators from level 0, one V-cycle over a table
 template <typename T> void launch_mg_coarsen(const Batch<T> &b, cudaStream_t s);

@@ -15,7 +15,7 @@ import os
 import numpy as np
 
 from ._abi import (FIELD_ID, INT_FIELDS, SCALAR_ID, SULI_CG_MAXITER, SuliDiag,
-                   SuliParams, field_shape)
+                   SuliParams, SuliTuning, field_shape)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libsuli_gpu.so")
@@ -30,7 +30,7 @@ EXPORTS = [
     "suli_last_error", "suli_device_info", "suli_get_stream", "suli_profile", "suli_profile_read",
     "suli_ibm_setup", "suli_conmassa_noalloc", "suli_time_kernel", "suli_upload_fields",
     "suli_download_fields", "suli_write_fields", "suli_restart_save", "suli_restart_load",
-    "suli_exp_press", "suli_contorno_les", "suli_boundary_waves",
+    "suli_exp_press", "suli_contorno_les", "suli_boundary_waves", "suli_autotune", "suli_get_tuning",
 ]
 
 
@@ -93,6 +93,8 @@ def load_library(path: str = LIB_PATH):
     L.suli_restart_load.argtypes = [C.c_void_p, C.c_char_p]
     L.suli_conmassa_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, i32, i32, i32, C.c_double,
                                         C.c_double, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.suli_autotune.argtypes = [C.c_void_p, P(SuliTuning)]
+    L.suli_get_tuning.argtypes = [C.c_void_p, P(SuliTuning)]
     _lib = L
     return L
 
@@ -292,6 +294,19 @@ class SuliGPU:
         ms, by = C.c_double(), C.c_double()
         _check(load_library().suli_time_kernel(self._h, kernel, reps, C.byref(ms), C.byref(by)))
         return ms.value, by.value
+
+    # ---- autotuner -------------------------------------------------------------
+    def autotune(self) -> dict:
+        """Tune the launch shapes now (or apply the cached choice for this
+        device and workload shape); returns suli_tuning as a dict."""
+        t = SuliTuning()
+        _check(load_library().suli_autotune(self._h, C.byref(t)))
+        return t.as_dict()
+
+    def tuning(self) -> dict:
+        t = SuliTuning()
+        _check(load_library().suli_get_tuning(self._h, C.byref(t)))
+        return t.as_dict()
 
     # ---- output and restart --------------------------------------------------
     def write_fields(self, path, case: int = 0, t_plot: int = 0):
