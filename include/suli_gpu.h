@@ -121,6 +121,15 @@ typedef struct suli_params {
                                       the reference, whose free outflow leaves a net boundary flux that
                                       the all-Neumann pressure equation of graddin cannot absorb);
                                       0: the reference's free outflow */
+    int32_t dz_t;                  /* z spacing: 0 uniform dz (SuLi-IC); 1 the variable spacing of
+                                      SuLi-ICdz, dz(k) = dzmin + (dzmax - dzmin) k / nz for k = 0..nz+1
+                                      (dz_dist, SuLi-ICdz/2_iniciais.f90:326-406), with the ICdz
+                                      stencils (weighted z interpolations, dz(k)/dzz(k) in the z
+                                      differences, graddin/posdin/CONMASSA, the WENO z lines);
+                                      supported for the plain two-fluid flow (m_turb = 0, no IBM,
+                                      surface tension, IPA, MMS, sponge, waves or inflow) */
+    double  dzmin, dzmax;          /* dz_t = 1: the spacing at k = 0 and at k = nz (dz is ignored;
+                                      max(dx, dy, dzmin) is the level set's dx1, as upstream) */
 } suli_params;
 
 /* ---- field ids (reference module arrays) -------------------------------- */

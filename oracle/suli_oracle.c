@@ -103,6 +103,12 @@ struct or_case {
     I3 id_ibmx, id_ibmy, id_ibmz, id_ibm;
     F3 bxx0, bxx1, blx1, bxz0;
 
+    /* SuLi-ICdz variable spacing (dz_t = 1): dz(0:nz+1), dzz(0:nz+1)
+     * (dz_dist, SuLi-ICdz/2_iniciais.f90:326-406) and the WENO z spacing
+     * dz11(-2:nz+3) (wenoz, SuLi-ICdz/8_derivadas.f90:968-1059) */
+    int vdz;
+    double *dzk, *dzzk, *dz11m;
+
     int cg_iters[3];
     double cg_res[3];
     int reinit_iters, vol_loops;
@@ -125,6 +131,31 @@ or_case *or_create(const suli_params *pp)
     c->nx1 = nx + 1; c->ny1 = ny + 1; c->nz1 = nz + 1;
     c->dx = pp->dx; c->dy = pp->dy; c->dz = pp->dz;
     c->dt0 = pp->dt; c->dt = pp->dt;
+    if (pp->dz_t == 1) {
+        /* dz_dist, SuLi-ICdz/2_iniciais.f90:326-406: the representative
+         * spacing dza is dzmin (it enters dx1 = max(dx, dy, dza)) */
+        c->vdz = 1;
+        c->dz = pp->dzmin;
+        c->dzk = (double *)calloc((size_t)nz + 2, sizeof(double));
+        c->dzzk = (double *)calloc((size_t)nz + 2, sizeof(double));
+        c->dz11m = (double *)calloc((size_t)nz + 6, sizeof(double));
+        for (int k = 0; k <= nz + 1; ++k) c->dzk[k] = pp->dzmin + (pp->dzmax - pp->dzmin) * k / nz;
+        for (int k = 1; k <= nz + 1; ++k) c->dzzk[k] = (c->dzk[k] + c->dzk[k - 1]) * 0.5;
+        c->dzzk[0] = c->dzzk[1];
+        c->dzzk[nz + 1] = c->dzzk[nz];
+        /* wenoz with ihs = 2 (the level set's z, 14_level_set.f90:351-353):
+         * dz11 = dz on 0..nz+1, then every ghost by the cubic extrapolation
+         * (the ends 0 and nz+1 included), SuLi-ICdz/8_derivadas.f90:1076-1084 */
+        double *d = c->dz11m + 2;   /* d[m], m = -2 .. nz+3 */
+        const double c11 = 1. / 11.;
+        for (int k = 0; k <= nz + 1; ++k) d[k] = c->dzk[k];
+        d[0] = c11 * (18. * d[1] - 9. * d[2] + 2. * d[3]);
+        d[-1] = c11 * (18. * d[0] - 9. * d[1] + 2. * d[2]);
+        d[-2] = c11 * (18. * d[-1] - 9. * d[0] + 2. * d[1]);
+        d[nz + 1] = c11 * (18. * d[nz] - 9. * d[nz - 1] + 2. * d[nz - 2]);
+        d[nz + 2] = c11 * (18. * d[nz + 1] - 9. * d[nz] + 2. * d[nz - 1]);
+        d[nz + 3] = c11 * (18. * d[nz + 2] - 9. * d[nz + 1] + 2. * d[nz]);
+    }
     c->pi = acos(-1.0);               /* 0_modules.f90:5 */
     c->t = 0.0; c->it = 0; c->tt = 1;
     int nx1 = c->nx1, ny1 = c->ny1, nz1 = c->nz1;
@@ -199,6 +230,7 @@ or_case *or_create(const suli_params *pp)
 
 void or_destroy(or_case *c)
 {
+    if (c) { free(c->dzk); free(c->dzzk); free(c->dz11m); }
     if (!c) return;
     F3 *all[] = {&c->u, &c->v, &c->w, &c->prd1, &c->prd, &c->ls, &c->hs, &c->rho, &c->ls_mu,
                  &c->mu, &c->mut, &c->xmu, &c->ymu, &c->zmu, &c->Fu, &c->Fv, &c->Fw, &c->u0,
@@ -407,6 +439,31 @@ static void interpz_fc(const F3 *a, int dimx, int dimy, int dimz, F3 *o)
                 A(*o, i, j, k) = (A(*a, i, j, k) + A(*a, i, j, k + 1)) * 0.5;
 }
 
+/* SuLi-ICdz's spacing-weighted z interpolations, d(0:..) the spacing:
+ * interpz_cf (SuLi-ICdz/8_derivadas.f90:450-479): face k in 2..dimz takes
+ * (a(k) d(k) + a(k-1) d(k-1)) / (d(k) + d(k-1)), faces 1 and dimz+1 copy
+ * their neighbours; interpz_fc (:491-511): centre k in 1..dimz-1 takes
+ * (a(k) d(k) + a(k+1) d(k+1)) / (d(k) + d(k+1)) */
+static void interpz_cf_d(const F3 *a, int dimx, int dimy, int dimz, const double *d, F3 *o)
+{
+    for (int k = 2; k <= dimz; ++k)
+        for (int j = 1; j <= dimy; ++j)
+            for (int i = 1; i <= dimx; ++i)
+                A(*o, i, j, k) = (A(*a, i, j, k) * d[k] + A(*a, i, j, k - 1) * d[k - 1]) / (d[k] + d[k - 1]);
+    for (int j = 1; j <= dimy; ++j)
+        for (int i = 1; i <= dimx; ++i) {
+            A(*o, i, j, 1) = A(*o, i, j, 2);
+            A(*o, i, j, dimz + 1) = A(*o, i, j, dimz);
+        }
+}
+static void interpz_fc_d(const F3 *a, int dimx, int dimy, int dimz, const double *d, F3 *o)
+{
+    for (int k = 1; k <= dimz - 1; ++k)
+        for (int j = 1; j <= dimy; ++j)
+            for (int i = 1; i <= dimx; ++i)
+                A(*o, i, j, k) = (A(*a, i, j, k) * d[k] + A(*a, i, j, k + 1) * d[k + 1]) / (d[k] + d[k + 1]);
+}
+
 /* ------------------------------------------------------------------------ */
 /* 8_derivadas.f90:675-1095 -- WENO5 one-sided derivatives                   */
 /* ------------------------------------------------------------------------ */
@@ -479,6 +536,32 @@ void or_weno_line(const double *a, long s, int n, double h, int ihs, double *dp,
     if (buf != stackbuf) free(buf);
 }
 
+/* The z line of SuLi-ICdz's wenoz with ihs = 2 (SuLi-ICdz/8_derivadas.f90:
+ * 968-1105): the same ghosts and weights, with the one-sided differences
+ * D(m) = (phi(m+1) - phi(m)) / dz11(m+1) over the extrapolated spacing
+ * (h[m], m = -2 .. n+3) instead of one dz. */
+static void or_weno_line_v(const double *a, long s, int n, const double *h, double *dp, double *dn)
+{
+    double stackbuf[1024];
+    double *buf = (2 * n + 16 <= 1024) ? stackbuf : (double *)malloc(sizeof(double) * (size_t)(2 * n + 16));
+    double *phi = buf + 3;
+    double *D = buf + n + 8 + 3;
+    for (int m = 1; m <= n; ++m) phi[m] = a[(long)(m - 1) * s];
+    const double c11 = 1. / 11.;
+    phi[0] = c11 * (18. * phi[1] - 9. * phi[2] + 2. * phi[3]);
+    phi[-1] = c11 * (18. * phi[0] - 9. * phi[1] + 2. * phi[2]);
+    phi[-2] = c11 * (18. * phi[-1] - 9. * phi[0] + 2. * phi[1]);
+    phi[n + 1] = c11 * (18. * phi[n] - 9. * phi[n - 1] + 2. * phi[n - 2]);
+    phi[n + 2] = c11 * (18. * phi[n + 1] - 9. * phi[n] + 2. * phi[n - 1]);
+    phi[n + 3] = c11 * (18. * phi[n + 2] - 9. * phi[n + 1] + 2. * phi[n]);
+    for (int m = -2; m <= n + 2; ++m) D[m] = (phi[m + 1] - phi[m]) / h[m + 1];
+    for (int i = 1; i <= n; ++i) {
+        dp[(long)(i - 1) * s] = weno5(D[i + 2], D[i + 1], D[i], D[i - 1], D[i - 2]);
+        dn[(long)(i - 1) * s] = weno5(D[i - 3], D[i - 2], D[i - 1], D[i], D[i + 1]);
+    }
+    if (buf != stackbuf) free(buf);
+}
+
 /* der_weno, 14_level_set.f90:338-370.  out: ta=phi_x+, td=phi_x-, tb=phi_y+,
  * te=phi_y-, tc=phi_z+, tf=phi_z-.  All arrays (1:dimx,1:dimy,1:dimz). */
 static void der_weno(const or_case *c, const F3 *ls, int dimx, int dimy, int dimz,
@@ -494,8 +577,10 @@ static void der_weno(const or_case *c, const F3 *ls, int dimx, int dimy, int dim
             or_weno_line(&A(*ls, i, 1, k), ls->s1, dimy, c->dy, ihs, &A(*tb, i, 1, k), &A(*te, i, 1, k));
     ihs = 2;   /* z is always extrapolated (:365-366) */
     for (int j = 1; j <= dimy; ++j)
-        for (int i = 1; i <= dimx; ++i)
-            or_weno_line(&A(*ls, i, j, 1), ls->s2, dimz, c->dz, ihs, &A(*tc, i, j, 1), &A(*tf, i, j, 1));
+        for (int i = 1; i <= dimx; ++i) {
+            if (c->vdz) or_weno_line_v(&A(*ls, i, j, 1), ls->s2, dimz, c->dz11m + 2, &A(*tc, i, j, 1), &A(*tf, i, j, 1));
+            else or_weno_line(&A(*ls, i, j, 1), ls->s2, dimz, c->dz, ihs, &A(*tc, i, j, 1), &A(*tf, i, j, 1));
+        }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -662,7 +747,7 @@ static double volume(const or_case *c)
     for (int k = 1; k <= c->nz; ++k)
         for (int j = 1; j <= c->ny; ++j)
             for (int i = 1; i <= c->nx; ++i)
-                vol = vol + (1. - (1. - A(c->hs, i, j, k))) * c->dx * c->dy * c->dz;
+                vol = vol + (1. - (1. - A(c->hs, i, j, k))) * c->dx * c->dy * (c->vdz ? c->dzk[k] : c->dz);
     return vol;
 }
 
@@ -846,7 +931,8 @@ void or_visco(or_case *c)
     for (long q = 0; q < n; ++q) c->mu.p[q] = c->ls_mu.p[q] + c->mut.p[q];
     interpx_cf(c, &c->mu, nx, ny, nz, &c->xmu);
     interpy_cf(&c->mu, nx, ny, nz, &c->ymu);
-    interpz_cf(&c->mu, nx, ny, nz, &c->zmu);
+    if (c->vdz) interpz_cf_d(&c->mu, nx, ny, nz, c->dzk, &c->zmu);   /* SuLi-ICdz/5_viscosidade.f90:155 */
+    else interpz_cf(&c->mu, nx, ny, nz, &c->zmu);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -875,15 +961,20 @@ static inline double d2p_y(const or_case *c, const F3 *a, int i, int j, int k, i
     if (j <= dimy - 1) return 0.5 * (-A(*a, i, j + 2, k) + 4 * A(*a, i, j + 1, k) - 3 * A(*a, i, j, k)) / c->dy;
     return 0.5 * (A(*a, i, j + 1, k) - A(*a, i, j - 1, k)) / c->dy;
 }
-static inline double d2n_z(const or_case *c, const F3 *a, int i, int j, int k)
+/* d: SuLi-ICdz's spacing of the array's own z points (dz for u, v and
+ * cells, dzz for w; "only the dz of the point computed", SuLi-ICdz/
+ * 8_derivadas.f90:158-186, :277-303), or null for the uniform dz */
+static inline double d2n_z(const or_case *c, const F3 *a, int i, int j, int k, const double *d)
 {   /* derivazu2n, :273-300 */
-    if (k >= 2) return 0.5 * (A(*a, i, j, k - 2) - 4 * A(*a, i, j, k - 1) + 3 * A(*a, i, j, k)) / c->dz;
-    return 0.5 * (A(*a, i, j, k + 1) - A(*a, i, j, k - 1)) / c->dz;
+    const double h = d ? d[k] : c->dz;
+    if (k >= 2) return 0.5 * (A(*a, i, j, k - 2) - 4 * A(*a, i, j, k - 1) + 3 * A(*a, i, j, k)) / h;
+    return 0.5 * (A(*a, i, j, k + 1) - A(*a, i, j, k - 1)) / h;
 }
-static inline double d2p_z(const or_case *c, const F3 *a, int i, int j, int k, int dimz)
+static inline double d2p_z(const or_case *c, const F3 *a, int i, int j, int k, int dimz, const double *d)
 {   /* derivazu2p, :157-186 */
-    if (k <= dimz - 1) return 0.5 * (-A(*a, i, j, k + 2) + 4 * A(*a, i, j, k + 1) - 3 * A(*a, i, j, k)) / c->dz;
-    return 0.5 * (A(*a, i, j, k + 1) - A(*a, i, j, k - 1)) / c->dz;
+    const double h = d ? d[k] : c->dz;
+    if (k <= dimz - 1) return 0.5 * (-A(*a, i, j, k + 2) + 4 * A(*a, i, j, k + 1) - 3 * A(*a, i, j, k)) / h;
+    return 0.5 * (A(*a, i, j, k + 1) - A(*a, i, j, k - 1)) / h;
 }
 
 static inline double upw(double vel, double dneg, double dpos)
@@ -956,7 +1047,7 @@ static void convdiff_les(or_case *c, F3 *fka)
             for (int i = 1; i <= nx; ++i) {
                 double adv = upw(A(uc, i, j, k), d2n_x(c, ka, i, j, k, nx), d2p_x(c, ka, i, j, k, nx)) +
                              upw(A(vc, i, j, k), d2n_y(c, ka, i, j, k), d2p_y(c, ka, i, j, k, ny)) +
-                             upw(A(wc, i, j, k), d2n_z(c, ka, i, j, k), d2p_z(c, ka, i, j, k, nz));
+                             upw(A(wc, i, j, k), d2n_z(c, ka, i, j, k, NULL), d2p_z(c, ka, i, j, k, nz, NULL));
                 double kc = A(*ka, i, j, k);
                 A(*fka, i, j, k) = -adv +
                     ((A(am, i + 1, j, k) * (A(*ka, i + 1, j, k) - kc) - A(am, i, j, k) * (kc - A(*ka, i - 1, j, k))) / (c->dx * c->dx) +
@@ -1042,12 +1133,22 @@ static void classico(or_case *c, F3 *uint_, F3 *vint_, F3 *wint_)
     F3 amd = tmp3(1, nx, 1, ny, 1, nz1), bmd = tmp3(1, nx, 1, ny, 1, nz1);
     /* advecting-velocity averages, :175-191 (interior slices of u, v, w) */
     F3 vin = c->v, win = c->w, uin = c->u;   /* views; interp reads indices >= 1 only */
-    interpy_fc(&vin, nx, ny1, nz, &aux); interpx_cf(c, &aux, nx, ny, nz, &bma);
-    interpz_fc(&win, nx, ny, nz1, &aux); interpx_cf(c, &aux, nx, ny, nz, &dma);
-    interpx_fc(&uin, nx1, ny, nz, &aux); interpy_cf(&aux, nx, ny, nz, &amb);
-    interpz_fc(&win, nx, ny, nz1, &aux); interpy_cf(&aux, nx, ny, nz, &dmb);
-    interpx_fc(&uin, nx1, ny, nz, &aux); interpz_cf(&aux, nx, ny, nz, &amd);
-    interpy_fc(&vin, nx, ny1, nz, &aux); interpz_cf(&aux, nx, ny, nz, &bmd);
+    const double *dzk = c->vdz ? c->dzk : NULL, *dzzk = c->vdz ? c->dzzk : NULL;
+    if (c->vdz) {   /* SuLi-ICdz/7_advectivo.f90:175-192: the z averages weighted */
+        interpy_fc(&vin, nx, ny1, nz, &aux); interpx_cf(c, &aux, nx, ny, nz, &bma);
+        interpz_fc_d(&win, nx, ny, nz1, dzzk, &aux); interpx_cf(c, &aux, nx, ny, nz, &dma);
+        interpx_fc(&uin, nx1, ny, nz, &aux); interpy_cf(&aux, nx, ny, nz, &amb);
+        interpz_fc_d(&win, nx, ny, nz1, dzzk, &aux); interpy_cf(&aux, nx, ny, nz, &dmb);
+        interpx_fc(&uin, nx1, ny, nz, &aux); interpz_cf_d(&aux, nx, ny, nz, dzk, &amd);
+        interpy_fc(&vin, nx, ny1, nz, &aux); interpz_cf_d(&aux, nx, ny, nz, dzk, &bmd);
+    } else {
+        interpy_fc(&vin, nx, ny1, nz, &aux); interpx_cf(c, &aux, nx, ny, nz, &bma);
+        interpz_fc(&win, nx, ny, nz1, &aux); interpx_cf(c, &aux, nx, ny, nz, &dma);
+        interpx_fc(&uin, nx1, ny, nz, &aux); interpy_cf(&aux, nx, ny, nz, &amb);
+        interpz_fc(&win, nx, ny, nz1, &aux); interpy_cf(&aux, nx, ny, nz, &dmb);
+        interpx_fc(&uin, nx1, ny, nz, &aux); interpz_cf(&aux, nx, ny, nz, &amd);
+        interpy_fc(&vin, nx, ny1, nz, &aux); interpz_cf(&aux, nx, ny, nz, &bmd);
+    }
 
     /* :216-236 */
     for (int k = 1; k <= nz; ++k)
@@ -1055,7 +1156,7 @@ static void classico(or_case *c, F3 *uint_, F3 *vint_, F3 *wint_)
             for (int i = 1; i <= nx1; ++i) {
                 double ddx = upw(A(c->u, i, j, k), d2n_x(c, &c->u, i, j, k, nx1), d2p_x(c, &c->u, i, j, k, nx1));
                 double ddy = upw(A(bma, i, j, k), d2n_y(c, &c->u, i, j, k), d2p_y(c, &c->u, i, j, k, ny));
-                double ddz = upw(A(dma, i, j, k), d2n_z(c, &c->u, i, j, k), d2p_z(c, &c->u, i, j, k, nz));
+                double ddz = upw(A(dma, i, j, k), d2n_z(c, &c->u, i, j, k, dzk), d2p_z(c, &c->u, i, j, k, nz, dzk));
                 A(*uint_, i, j, k) = ddx + ddy + ddz;
             }
     /* :238-258 */
@@ -1064,7 +1165,7 @@ static void classico(or_case *c, F3 *uint_, F3 *vint_, F3 *wint_)
             for (int i = 1; i <= nx; ++i) {
                 double ddx = upw(A(amb, i, j, k), d2n_x(c, &c->v, i, j, k, nx), d2p_x(c, &c->v, i, j, k, nx));
                 double ddy = upw(A(c->v, i, j, k), d2n_y(c, &c->v, i, j, k), d2p_y(c, &c->v, i, j, k, ny1));
-                double ddz = upw(A(dmb, i, j, k), d2n_z(c, &c->v, i, j, k), d2p_z(c, &c->v, i, j, k, nz));
+                double ddz = upw(A(dmb, i, j, k), d2n_z(c, &c->v, i, j, k, dzk), d2p_z(c, &c->v, i, j, k, nz, dzk));
                 A(*vint_, i, j, k) = ddx + ddy + ddz;
             }
     /* :260-280 */
@@ -1073,7 +1174,7 @@ static void classico(or_case *c, F3 *uint_, F3 *vint_, F3 *wint_)
             for (int i = 1; i <= nx; ++i) {
                 double ddx = upw(A(amd, i, j, k), d2n_x(c, &c->w, i, j, k, nx), d2p_x(c, &c->w, i, j, k, nx));
                 double ddy = upw(A(bmd, i, j, k), d2n_y(c, &c->w, i, j, k), d2p_y(c, &c->w, i, j, k, ny));
-                double ddz = upw(A(c->w, i, j, k), d2n_z(c, &c->w, i, j, k), d2p_z(c, &c->w, i, j, k, nz1));
+                double ddz = upw(A(c->w, i, j, k), d2n_z(c, &c->w, i, j, k, dzzk), d2p_z(c, &c->w, i, j, k, nz1, dzzk));
                 A(*wint_, i, j, k) = ddx + ddy + ddz;
             }
     fr(&aux); fr(&bma); fr(&dma); fr(&amb); fr(&dmb); fr(&amd); fr(&bmd);
@@ -1082,12 +1183,116 @@ static void classico(or_case *c, F3 *uint_, F3 *vint_, F3 *wint_)
 /* ------------------------------------------------------------------------ */
 /* 6_convdiff.f90:14-167                                                     */
 /* ------------------------------------------------------------------------ */
+/* SuLi-ICdz/6_convdiff.f90:75-176: the viscous terms of convdiff on the
+ * variable z spacing.  Kept as upstream: dma and dmb are divided by dz(k)
+ * only over i <= nx, j <= ny, k <= nz (the loop :118-126), so their last x
+ * (dma) or y (dmb) face and their top face nz+1 keep the undivided
+ * interpolated viscosity; the z differences of Fu and Fv divide by dz(k) of
+ * the face's own k, those of Fw by dz(k) and its last term by dzz(k). */
+static void convdiff_vdz(or_case *c, const F3 *ui, const F3 *vi, const F3 *wi)
+{
+    int nx = c->nx, ny = c->ny, nz = c->nz, nx1 = c->nx1, ny1 = c->ny1, nz1 = c->nz1;
+    const double dx = c->dx, dy = c->dy;
+    const double *dz = c->dzk, *dzz = c->dzzk;
+    F3 rhox = tmp3(1, nx1, 1, ny, 1, nz), rhoy = tmp3(1, nx, 1, ny1, 1, nz), rhoz = tmp3(1, nx, 1, ny, 1, nz1);
+    interpx_cf(c, &c->rho, nx, ny, nz, &rhox);
+    interpy_cf(&c->rho, nx, ny, nz, &rhoy);
+    interpz_cf_d(&c->rho, nx, ny, nz, dz, &rhoz);
+    F3 bma = tmp3(1, nx1, 1, ny1, 1, nz), dma = tmp3(1, nx1, 1, ny, 1, nz1);
+    F3 amb = tmp3(1, nx1, 1, ny1, 1, nz), dmb = tmp3(1, nx, 1, ny1, 1, nz1);
+    F3 amd = tmp3(1, nx1, 1, ny, 1, nz1), bmd = tmp3(1, nx, 1, ny1, 1, nz1);
+    interpy_cf(&c->xmu, nx1, ny, nz, &bma);
+    interpz_cf_d(&c->xmu, nx1, ny, nz, dz, &dma);
+    interpx_cf(c, &c->ymu, nx, ny1, nz, &amb);
+    interpz_cf_d(&c->ymu, nx, ny1, nz, dz, &dmb);
+    interpx_cf(c, &c->zmu, nx, ny, nz1, &amd);
+    interpy_cf(&c->zmu, nx, ny, nz1, &bmd);
+    F3 ama = tmp3(0, nx1, 1, ny, 1, nz), bmb = tmp3(1, nx, 0, ny1, 1, nz), dmd = tmp3(1, nx, 1, ny, 0, nz1);
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i) {
+                A(ama, i, j, k) = A(c->mu, i, j, k) / dx;
+                A(bmb, i, j, k) = A(c->mu, i, j, k) / dy;
+            }
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j) {
+            A(ama, 0, j, k) = A(ama, 1, j, k);
+            A(ama, nx1, j, k) = A(ama, nx, j, k);
+        }
+    for (int k = 1; k <= nz; ++k)
+        for (int i = 1; i <= nx; ++i) {
+            A(bmb, i, 0, k) = A(bmb, i, 1, k);
+            A(bmb, i, ny1, k) = A(bmb, i, ny, k);
+        }
+    for (int k = 1; k <= nz; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i) {
+                A(dmd, i, j, k) = A(c->mu, i, j, k) / dzz[k];
+                A(dma, i, j, k) = A(dma, i, j, k) / dz[k];
+                A(dmb, i, j, k) = A(dmb, i, j, k) / dz[k];
+            }
+    for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+            A(dmd, i, j, 0) = A(dmd, i, j, 1);
+            A(dmd, i, j, nz1) = A(dmd, i, j, nz);
+        }
+    long q, n;
+    n = f3_size(&amb); for (q = 0; q < n; ++q) amb.p[q] = amb.p[q] / dx;
+    n = f3_size(&amd); for (q = 0; q < n; ++q) amd.p[q] = amd.p[q] / dx;
+    n = f3_size(&bma); for (q = 0; q < n; ++q) bma.p[q] = bma.p[q] / dy;
+    n = f3_size(&bmd); for (q = 0; q < n; ++q) bmd.p[q] = bmd.p[q] / dy;
+    F3 u = c->u, v = c->v, w = c->w;
+    for (int k = 1; k <= nz; ++k) {
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx1; ++i) {
+                A(c->Fu, i, j, k) = -A(*ui, i, j, k) +
+                    ((A(ama, i, j, k) * 2. * (A(u, i + 1, j, k) - A(u, i, j, k)) -
+                      A(ama, i - 1, j, k) * 2. * (A(u, i, j, k) - A(u, i - 1, j, k))) / dx +
+                     A(bma, i, j + 1, k) * ((A(u, i, j + 1, k) - A(u, i, j, k)) / dy + (A(v, i, j + 1, k) - A(v, i - 1, j + 1, k)) / dx) -
+                     A(bma, i, j, k) * ((A(u, i, j, k) - A(u, i, j - 1, k)) / dy + (A(v, i, j, k) - A(v, i - 1, j, k)) / dx) +
+                     A(dma, i, j, k + 1) * ((A(u, i, j, k + 1) - A(u, i, j, k)) / dz[k] + (A(w, i, j, k + 1) - A(w, i - 1, j, k + 1)) / dx) -
+                     A(dma, i, j, k) * ((A(u, i, j, k) - A(u, i, j, k - 1)) / dz[k] + (A(w, i, j, k) - A(w, i - 1, j, k)) / dx)) /
+                    A(rhox, i, j, k);
+            }
+        for (int j = 1; j <= ny1; ++j)
+            for (int i = 1; i <= nx; ++i) {
+                A(c->Fv, i, j, k) = -A(*vi, i, j, k) +
+                    (A(amb, i + 1, j, k) * ((A(v, i + 1, j, k) - A(v, i, j, k)) / dx + (A(u, i + 1, j, k) - A(u, i + 1, j - 1, k)) / dy) -
+                     A(amb, i, j, k) * ((A(v, i, j, k) - A(v, i - 1, j, k)) / dx + (A(u, i, j, k) - A(u, i, j - 1, k)) / dy) +
+                     (A(bmb, i, j, k) * 2. * (A(v, i, j + 1, k) - A(v, i, j, k)) -
+                      A(bmb, i, j - 1, k) * 2. * (A(v, i, j, k) - A(v, i, j - 1, k))) / dy +
+                     A(dmb, i, j, k + 1) * ((A(v, i, j, k + 1) - A(v, i, j, k)) / dz[k] + (A(w, i, j, k + 1) - A(w, i, j - 1, k + 1)) / dy) -
+                     A(dmb, i, j, k) * ((A(v, i, j, k) - A(v, i, j, k - 1)) / dz[k] + (A(w, i, j, k) - A(w, i, j - 1, k)) / dy)) /
+                    A(rhoy, i, j, k);
+            }
+    }
+    for (int k = 1; k <= nz1; ++k)
+        for (int j = 1; j <= ny; ++j)
+            for (int i = 1; i <= nx; ++i) {
+                A(c->Fw, i, j, k) = -A(*wi, i, j, k) +
+                    (A(amd, i + 1, j, k) * ((A(w, i + 1, j, k) - A(w, i, j, k)) / dx + (A(u, i + 1, j, k) - A(u, i + 1, j, k - 1)) / dz[k]) -
+                     A(amd, i, j, k) * ((A(w, i, j, k) - A(w, i - 1, j, k)) / dx + (A(u, i, j, k) - A(u, i, j, k - 1)) / dz[k]) +
+                     A(bmd, i, j + 1, k) * ((A(w, i, j + 1, k) - A(w, i, j, k)) / dy + (A(v, i, j + 1, k) - A(v, i, j + 1, k - 1)) / dz[k]) -
+                     A(bmd, i, j, k) * ((A(w, i, j, k) - A(w, i, j - 1, k)) / dy + (A(v, i, j, k) - A(v, i, j, k - 1)) / dz[k]) +
+                     (A(dmd, i, j, k) * 2. * (A(w, i, j, k + 1) - A(w, i, j, k)) -
+                      A(dmd, i, j, k - 1) * 2. * (A(w, i, j, k) - A(w, i, j, k - 1))) / dzz[k]) /
+                    A(rhoz, i, j, k);
+            }
+    fr(&rhox); fr(&rhoy); fr(&rhoz);
+    fr(&bma); fr(&dma); fr(&amb); fr(&dmb); fr(&amd); fr(&bmd); fr(&ama); fr(&bmb); fr(&dmd);
+}
+
 void or_convdiff(or_case *c)
 {
     int nx = c->nx, ny = c->ny, nz = c->nz, nx1 = c->nx1, ny1 = c->ny1, nz1 = c->nz1;
     double dx = c->dx, dy = c->dy, dz = c->dz;
     F3 ui = tmp3(1, nx1, 1, ny, 1, nz), vi = tmp3(1, nx, 1, ny1, 1, nz), wi = tmp3(1, nx, 1, ny, 1, nz1);
     classico(c, &ui, &vi, &wi);
+    if (c->vdz) {
+        convdiff_vdz(c, &ui, &vi, &wi);
+        fr(&ui); fr(&vi); fr(&wi);
+        return;
+    }
 
     F3 rhox = tmp3(1, nx1, 1, ny, 1, nz), rhoy = tmp3(1, nx, 1, ny1, 1, nz), rhoz = tmp3(1, nx, 1, ny, 1, nz1);
     interpx_cf(c, &c->rho, nx, ny, nz, &rhox);
@@ -1881,7 +2086,8 @@ int or_graddin(or_case *c)
     } else {
         interpx_cf(c, &c->rho, nx, ny, nz, &rhox);
         interpy_cf(&c->rho, nx, ny, nz, &rhoy);
-        interpz_cf(&c->rho, nx, ny, nz, &rhoz);
+        if (c->vdz) interpz_cf_d(&c->rho, nx, ny, nz, c->dzk, &rhoz);   /* SuLi-ICdz/9_grad.f90:105 */
+        else interpz_cf(&c->rho, nx, ny, nz, &rhoz);
     }
 #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nz; ++k)
@@ -1894,7 +2100,9 @@ int or_graddin(or_case *c)
 #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nz1; ++k)
         for (int j = 1; j <= ny; ++j)
-            for (int i = 1; i <= nx; ++i) A(spk, i, j, k) = aux3 / A(rhoz, i, j, k);
+            for (int i = 1; i <= nx; ++i)
+                A(spk, i, j, k) = c->vdz ? dt / (c->dzk[k] * c->dzk[k] * A(rhoz, i, j, k))   /* SuLi-ICdz/9_grad.f90:141 */
+                                         : aux3 / A(rhoz, i, j, k);
 #pragma omp parallel for schedule(static)
     for (int k = 1; k <= nz; ++k)
         for (int j = 1; j <= ny; ++j)
@@ -1914,7 +2122,7 @@ int or_graddin(or_case *c)
                     v1a = A(c->v, i, j, k); v1b = A(c->v, i, j + 1, k);
                     w1a = A(c->w, i, j, k); w1b = A(c->w, i, j, k + 1);
                 }
-                A(qpr, i, j, k) = (u1a - u1b) / dx + (v1a - v1b) / dy + (w1a - w1b) / dz;
+                A(qpr, i, j, k) = (u1a - u1b) / dx + (v1a - v1b) / dy + (w1a - w1b) / (c->vdz ? c->dzzk[k] : dz);
             }
     ghost_fill_cg(c, &dpr);
 #pragma omp parallel for schedule(static)
@@ -2033,7 +2241,8 @@ void or_posdin(or_case *c)
     F3 rhox = tmp3(1, nx1, 1, ny, 1, nz), rhoy = tmp3(1, nx, 1, ny1, 1, nz), rhoz = tmp3(1, nx, 1, ny, 1, nz1);
     interpx_cf(c, &c->rho, nx, ny, nz, &rhox);
     interpy_cf(&c->rho, nx, ny, nz, &rhoy);
-    interpz_cf(&c->rho, nx, ny, nz, &rhoz);
+    if (c->vdz) interpz_cf_d(&c->rho, nx, ny, nz, c->dzk, &rhoz);   /* SuLi-ICdz/10_pos.f90:21 */
+    else interpz_cf(&c->rho, nx, ny, nz, &rhoz);
     for (int k = 1; k <= nz; ++k) {
         for (int j = 1; j <= ny; ++j)
             for (int i = 1; i <= nx1; ++i)
@@ -2045,7 +2254,8 @@ void or_posdin(or_case *c)
     for (int k = 1; k <= nz1; ++k)
         for (int j = 1; j <= ny; ++j)
             for (int i = 1; i <= nx; ++i)
-                A(c->w, i, j, k) = A(c->w, i, j, k) - c->dt / c->dz * (A(c->prd1, i, j, k) - A(c->prd1, i, j, k - 1)) / A(rhoz, i, j, k);
+                A(c->w, i, j, k) = A(c->w, i, j, k) - c->dt / (c->vdz ? c->dzzk[k] : c->dz) *
+                                                           (A(c->prd1, i, j, k) - A(c->prd1, i, j, k - 1)) / A(rhoz, i, j, k);
     f3_copy(&c->prd, &c->prd1);
     fr(&rhox); fr(&rhoy); fr(&rhoz);
 }
@@ -2058,7 +2268,7 @@ double or_conmassa(or_case *c)
         for (int j = 1; j <= c->ny; ++j)
             for (int i = 1; i <= c->nx; ++i) {
                 double d = (A(c->u, i + 1, j, k) - A(c->u, i, j, k)) / c->dx + (A(c->v, i, j + 1, k) - A(c->v, i, j, k)) / c->dy +
-                           (A(c->w, i, j, k + 1) - A(c->w, i, j, k)) / c->dz;
+                           (A(c->w, i, j, k + 1) - A(c->w, i, j, k)) / (c->vdz ? c->dzzk[k] : c->dz);   /* SuLi-ICdz/4_plot.f90:406 */
                 A(c->div, i, j, k) = d;
                 if (fabs(d) > m) m = fabs(d);
             }

@@ -65,6 +65,9 @@ class SuliParams(C.Structure):
         ("aeta", C.c_double * 5),
         ("avel", C.c_double * 5),
         ("outflow_flux", C.c_int32),
+        ("dz_t", C.c_int32),
+        ("dzmin", C.c_double),
+        ("dzmax", C.c_double),
     ]
 
     def copy(self) -> "SuliParams":

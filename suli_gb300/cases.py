@@ -98,6 +98,43 @@ def dam_break(nx=64, ny=32, nz=32, precision=PREC_FP64, reinit_iters=5, cg_tol=1
     return Case("dam_break_%dx%dx%d" % (nx, ny, nz), p, _base_fields(p, ls), steps=200)
 
 
+def z_centres_dz(nz, dzmin, dzmax):
+    """Cell-centre heights of the variable z spacing of SuLi-ICdz (dz_dist,
+    SuLi-ICdz/2_iniciais.f90:326-406, dz_t = 1): dz(k) = dzmin + (dzmax -
+    dzmin) k / nz, z(1) = dz(1) / 2, z(k) = z(k-1) + (dz(k-1) + dz(k)) / 2."""
+    dz = [dzmin + (dzmax - dzmin) * k / nz for k in range(nz + 2)]
+    z = np.empty(nz)
+    z[0] = dz[1] * 0.5
+    for k in range(2, nz + 1):
+        z[k - 1] = z[k - 2] + (dz[k - 1] + dz[k]) * 0.5
+    return z
+
+
+def dam_break_dz(nx=64, ny=32, nz=32, dzmin=None, dzmax=None, precision=PREC_FP64, reinit_iters=5,
+                 cg_tol=1e-10) -> Case:
+    """The dam break on SuLi-ICdz's stretched z grid (dz_t = 1): x, y as the
+    uniform dam break (1.0 x 0.5 m), dz growing linearly from dzmin at the
+    bed to dzmax at the top (defaults 0.6 and 1.4 times the uniform 0.5/nz:
+    the same height), water column x < 0.25, z < 0.25 (tipo 3 with the
+    variable grid's cell heights)."""
+    h = 1.0 / nx
+    dzmin = 0.6 * 0.5 / nz if dzmin is None else dzmin
+    dzmax = 1.4 * 0.5 / nz if dzmax is None else dzmax
+    p = default_params(nx=nx, ny=ny, nz=nz, dx=h, dy=h, dz=dzmin, dt=1e-4,
+                       ccx0=2, ccxf=2, ccy0=2, ccyf=2, ccz0=2, cczf=2,
+                       gx=0.0, gz=9.81, rho_f1=1.2, mu_f1=1.8e-5, rho_f2=1000.0, mu_f2=1e-3,
+                       m_turb=0, reinit_max_iter=reinit_iters, cg_tol_mode=CG_TOL_REL,
+                       cg_tol=cg_tol, precision=precision, dz_t=1, dzmin=dzmin, dzmax=dzmax)
+    x = _centres(nx, h)[:, None, None]
+    y = _centres(ny, h)[None, :, None]
+    z = z_centres_dz(nz, dzmin, dzmax)[None, None, :]
+    m = 30.0
+    lsaux = np.power(z, m) + np.power(x, m) + np.power(y, m) / np.power(10.0, m)
+    ls = np.empty((nx, ny, nz), order="F")
+    ls[...] = -np.power(lsaux, 1.0 / m) + 0.25
+    return Case("dam_break_dz_%dx%dx%d" % (nx, ny, nz), p, _base_fields(p, ls), steps=200)
+
+
 def wave_tank(nx=1024, ny=256, nz=256, precision=PREC_FP64, dt=2e-4, cg_tol=1e-8) -> Case:
     """Large wave tank: 8 x 2 x 2 m, depth 1.0 m, eta = 0.05 sin(2 pi x / 2),
     still water, Smagorinsky LES (Cs 0.1), closed free-slip tank; 1000 steps."""

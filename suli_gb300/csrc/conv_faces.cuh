@@ -9,7 +9,10 @@
 // included).  The face functions return F before the complementos terms.
 // IN = true states that the position is interior -- 2 <= i <= nx - 1,
 // 2 <= j <= ny - 1, 2 <= k <= nz - 1 -- where every boundary branch of the
-// stencils takes its interior case; the operations are the same.
+// stencils takes its interior case; the operations are the same.  VZ = true
+// is SuLi-ICdz's variable z spacing (c.dzk set): its z interpolations
+// weighted by the spacing and its z differences over dz(k) or dzz(k), as
+// SuLi-ICdz/6_convdiff.f90:75-176 and 7_advectivo.f90:175-250 have them.
 #pragma once
 
 #include "suli_kernels.cuh"
@@ -106,6 +109,24 @@ __device__ __forceinline__ T ka_face(const CaseDev<T> &c, int axis, int i, int j
     return T(2. / 3.) * diff / (h * rf);
 }
 
+// SuLi-ICdz's spacing-weighted interpz_cf (SuLi-ICdz/8_derivadas.f90:450-479)
+// at z face f of cells 1..n: (a(f) dz(f) + a(f-1) dz(f-1)) / (dz(f) +
+// dz(f-1)) for f in 2..n, faces 1 and n+1 the copies of faces 2 and n
+template <typename T, bool IN = false, typename F>
+__device__ __forceinline__ T zcf_w(const CaseDev<T> &c, int f, int n, F get)
+{
+    const int ff = IN ? f : (f < 2 ? 2 : (f > n ? n : f));
+    const double a = c.dzk[ff], b = c.dzk[ff - 1];
+    return (get(ff) * T(a) + get(ff - 1) * T(b)) / T(a + b);
+}
+// and interpz_fc (:491-511) of a w-like array at centre kk: weights dzz
+template <typename T>
+__device__ __forceinline__ T zfc_w(const CaseDev<T> &c, T lo, T hi, int kk)
+{
+    const double a = c.dzzk[kk], b = c.dzzk[kk + 1];
+    return (lo * T(a) + hi * T(b)) / T(a + b);
+}
+
 // operands gathered from the case's arrays in global memory
 template <typename T>
 struct GlobalAcc {
@@ -121,15 +142,18 @@ struct GlobalAcc {
 };
 
 // Fu at x-face (i, j, k), i in 1..nx+1 (convdiff + classico, before complementos)
-template <typename T, typename A, bool IN = false>
+template <typename T, typename A, bool IN = false, bool VZ = false>
 __device__ __forceinline__ T face_fu(const CaseDev<T> &c, const A &X, int i, int j, int k)
 {
     const int nx = c.g.nx, ny = c.g.ny, nz = c.g.nz;
-    const T dx = T(c.idx), dy = T(c.idy), dz = T(c.idz);   // reciprocal spacings (1.0 / dx from the host)
+    // reciprocal spacings (1.0 / dx from the host); VZ: 1 / dz(k) of u's own k
+    const T dx = T(c.idx), dy = T(c.idy), dz = VZ ? T(c.idzk[k]) : T(c.idz);
     const bool px = (c.ccx0 == 0);
     auto U = [&](int a, int b, int cc) { return X.u(a, b, cc); };
     T bma = interp_cf<T, IN>(i, nx, px, [&](int m) { return (X.v(m, j, k) + X.v(m, j + 1, k)) * T(0.5); });
-    T dma = interp_cf<T, IN>(i, nx, px, [&](int m) { return (X.w(m, j, k) + X.w(m, j, k + 1)) * T(0.5); });
+    T dma = interp_cf<T, IN>(i, nx, px, [&](int m) {
+        return VZ ? zfc_w<T>(c, X.w(m, j, k), X.w(m, j, k + 1), k) : (X.w(m, j, k) + X.w(m, j, k + 1)) * T(0.5);
+    });
     T ddx = upw<T>(U(i, j, k), d2n<T, IN>(i, nx + 1, px, dx, [&](int m) { return U(m, j, k); }),
                    d2p<T, IN>(i, nx + 1, px, dx, [&](int m) { return U(m, j, k); }));
     T ddy = upw<T>(bma, d2n<T, IN>(j, ny, false, dy, [&](int m) { return U(i, m, k); }),
@@ -141,8 +165,17 @@ __device__ __forceinline__ T face_fu(const CaseDev<T> &c, const A &X, int i, int
     T ama_m = X.mu(clampi_in<IN>(i - 1, 1, nx), j, k) * dx;
     T b1 = interp_cf<T, IN>(j + 1, ny, false, [&](int m) { return X.xmu(i, m, k); }) * dy;
     T b0 = interp_cf<T, IN>(j, ny, false, [&](int m) { return X.xmu(i, m, k); }) * dy;
-    T d1 = interp_cf<T, IN>(k + 1, nz, false, [&](int m) { return X.xmu(i, j, m); }) * dz;
-    T d0 = interp_cf<T, IN>(k, nz, false, [&](int m) { return X.xmu(i, j, m); }) * dz;
+    T d1, d0;
+    if (VZ) {
+        // dma over dz(k) only for i <= nx, j <= ny, k <= nz; the last x face and
+        // the top face keep the undivided viscosity (SuLi-ICdz/6_convdiff.f90:118-126)
+        auto xm = [&](int m) { return X.xmu(i, j, m); };
+        d1 = zcf_w<T, IN>(c, k + 1, nz, xm) * ((i <= nx && k + 1 <= nz) ? T(c.idzk[k + 1]) : T(1.));
+        d0 = zcf_w<T, IN>(c, k, nz, xm) * ((i <= nx) ? T(c.idzk[k]) : T(1.));
+    } else {
+        d1 = interp_cf<T, IN>(k + 1, nz, false, [&](int m) { return X.xmu(i, j, m); }) * dz;
+        d0 = interp_cf<T, IN>(k, nz, false, [&](int m) { return X.xmu(i, j, m); }) * dz;
+    }
     T rhox = interp_cf<T, IN>(i, nx, px, [&](int m) { return X.rho(m, j, k); });
     T uc = U(i, j, k);
     const T rrho = T(1.) / rhox;
@@ -156,15 +189,17 @@ __device__ __forceinline__ T face_fu(const CaseDev<T> &c, const A &X, int i, int
 }
 
 // Fv at y-face (i, j, k), j in 1..ny+1
-template <typename T, typename A, bool IN = false>
+template <typename T, typename A, bool IN = false, bool VZ = false>
 __device__ __forceinline__ T face_fv(const CaseDev<T> &c, const A &X, int i, int j, int k)
 {
     const int nx = c.g.nx, ny = c.g.ny, nz = c.g.nz;
-    const T dx = T(c.idx), dy = T(c.idy), dz = T(c.idz);
+    const T dx = T(c.idx), dy = T(c.idy), dz = VZ ? T(c.idzk[k]) : T(c.idz);
     const bool px = (c.ccx0 == 0);
     auto V = [&](int a, int b, int cc) { return X.v(a, b, cc); };
     T amb = interp_cf<T, IN>(j, ny, false, [&](int m) { return (X.u(i, m, k) + X.u(i + 1, m, k)) * T(0.5); });
-    T dmb = interp_cf<T, IN>(j, ny, false, [&](int m) { return (X.w(i, m, k) + X.w(i, m, k + 1)) * T(0.5); });
+    T dmb = interp_cf<T, IN>(j, ny, false, [&](int m) {
+        return VZ ? zfc_w<T>(c, X.w(i, m, k), X.w(i, m, k + 1), k) : (X.w(i, m, k) + X.w(i, m, k + 1)) * T(0.5);
+    });
     T ddx = upw<T>(amb, d2n<T, IN>(i, nx, px, dx, [&](int m) { return V(m, j, k); }),
                    d2p<T, IN>(i, nx, px, dx, [&](int m) { return V(m, j, k); }));
     T ddy = upw<T>(V(i, j, k), d2n<T, IN>(j, ny + 1, false, dy, [&](int m) { return V(i, m, k); }),
@@ -176,8 +211,16 @@ __device__ __forceinline__ T face_fv(const CaseDev<T> &c, const A &X, int i, int
     T a0 = interp_cf<T, IN>(i, nx, px, [&](int m) { return X.ymu(m, j, k); }) * dx;
     T bmb_j = X.mu(i, clampi_in<IN>(j, 1, ny), k) * dy;
     T bmb_m = X.mu(i, clampi_in<IN>(j - 1, 1, ny), k) * dy;
-    T d1 = interp_cf<T, IN>(k + 1, nz, false, [&](int m) { return X.ymu(i, j, m); }) * dz;
-    T d0 = interp_cf<T, IN>(k, nz, false, [&](int m) { return X.ymu(i, j, m); }) * dz;
+    T d1, d0;
+    if (VZ) {
+        // dmb over dz(k) only for j <= ny, k <= nz (SuLi-ICdz/6_convdiff.f90:118-126)
+        auto ym = [&](int m) { return X.ymu(i, j, m); };
+        d1 = zcf_w<T, IN>(c, k + 1, nz, ym) * ((j <= ny && k + 1 <= nz) ? T(c.idzk[k + 1]) : T(1.));
+        d0 = zcf_w<T, IN>(c, k, nz, ym) * ((j <= ny) ? T(c.idzk[k]) : T(1.));
+    } else {
+        d1 = interp_cf<T, IN>(k + 1, nz, false, [&](int m) { return X.ymu(i, j, m); }) * dz;
+        d0 = interp_cf<T, IN>(k, nz, false, [&](int m) { return X.ymu(i, j, m); }) * dz;
+    }
     T rhoy = interp_cf<T, IN>(j, ny, false, [&](int m) { return X.rho(i, m, k); });
     T vc = V(i, j, k);
     return -vint +
@@ -190,36 +233,43 @@ __device__ __forceinline__ T face_fv(const CaseDev<T> &c, const A &X, int i, int
 }
 
 // Fw at z-face (i, j, k), k in 1..nz+1
-template <typename T, typename A, bool IN = false>
+template <typename T, typename A, bool IN = false, bool VZ = false>
 __device__ __forceinline__ T face_fw(const CaseDev<T> &c, const A &X, int i, int j, int k)
 {
     const int nx = c.g.nx, ny = c.g.ny, nz = c.g.nz;
-    const T dx = T(c.idx), dy = T(c.idy), dz = T(c.idz);
+    // VZ: the z differences of u, v over dz(k), those of w over dzz(k)
+    const T dx = T(c.idx), dy = T(c.idy), dz = VZ ? T(c.idzk[k]) : T(c.idz);
+    const T dzw = VZ ? T(c.idzzk[k]) : dz;
     const bool px = (c.ccx0 == 0);
     auto W = [&](int a, int b, int cc) { return X.w(a, b, cc); };
-    T amd = interp_cf<T, IN>(k, nz, false, [&](int m) { return (X.u(i, j, m) + X.u(i + 1, j, m)) * T(0.5); });
-    T bmd = interp_cf<T, IN>(k, nz, false, [&](int m) { return (X.v(i, j, m) + X.v(i, j + 1, m)) * T(0.5); });
+    auto ua = [&](int m) { return (X.u(i, j, m) + X.u(i + 1, j, m)) * T(0.5); };
+    auto va = [&](int m) { return (X.v(i, j, m) + X.v(i, j + 1, m)) * T(0.5); };
+    T amd = VZ ? zcf_w<T, IN>(c, k, nz, ua) : interp_cf<T, IN>(k, nz, false, ua);
+    T bmd = VZ ? zcf_w<T, IN>(c, k, nz, va) : interp_cf<T, IN>(k, nz, false, va);
     T ddx = upw<T>(amd, d2n<T, IN>(i, nx, px, dx, [&](int m) { return W(m, j, k); }),
                    d2p<T, IN>(i, nx, px, dx, [&](int m) { return W(m, j, k); }));
     T ddy = upw<T>(bmd, d2n<T, IN>(j, ny, false, dy, [&](int m) { return W(i, m, k); }),
                    d2p<T, IN>(j, ny, false, dy, [&](int m) { return W(i, m, k); }));
-    T ddz = upw<T>(W(i, j, k), d2n<T, IN>(k, nz + 1, false, dz, [&](int m) { return W(i, j, m); }),
-                   d2p<T, IN>(k, nz + 1, false, dz, [&](int m) { return W(i, j, m); }));
+    T ddz = upw<T>(W(i, j, k), d2n<T, IN>(k, nz + 1, false, dzw, [&](int m) { return W(i, j, m); }),
+                   d2p<T, IN>(k, nz + 1, false, dzw, [&](int m) { return W(i, j, m); }));
     T wint = ddx + ddy + ddz;
     T a1 = interp_cf<T, IN>(i + 1, nx, px, [&](int m) { return X.zmu(m, j, k); }) * dx;
     T a0 = interp_cf<T, IN>(i, nx, px, [&](int m) { return X.zmu(m, j, k); }) * dx;
     T b1 = interp_cf<T, IN>(j + 1, ny, false, [&](int m) { return X.zmu(i, m, k); }) * dy;
     T b0 = interp_cf<T, IN>(j, ny, false, [&](int m) { return X.zmu(i, m, k); }) * dy;
-    T dmd_k = X.mu(i, j, clampi_in<IN>(k, 1, nz)) * dz;
-    T dmd_m = X.mu(i, j, clampi_in<IN>(k - 1, 1, nz)) * dz;
-    T rhoz = interp_cf<T, IN>(k, nz, false, [&](int m) { return X.rho(i, j, m); });
+    const int kc = clampi_in<IN>(k, 1, nz), km = clampi_in<IN>(k - 1, 1, nz);
+    // VZ: dmd = mu / dzz(k) (SuLi-ICdz/6_convdiff.f90:120)
+    T dmd_k = X.mu(i, j, kc) * (VZ ? T(c.idzzk[kc]) : dz);
+    T dmd_m = X.mu(i, j, km) * (VZ ? T(c.idzzk[km]) : dz);
+    auto rr = [&](int m) { return X.rho(i, j, m); };
+    T rhoz = VZ ? zcf_w<T, IN>(c, k, nz, rr) : interp_cf<T, IN>(k, nz, false, rr);
     T wc = W(i, j, k);
     return -wint +
            (a1 * ((W(i + 1, j, k) - wc) * dx + (X.u(i + 1, j, k) - X.u(i + 1, j, k - 1)) * dz) -
             a0 * ((wc - W(i - 1, j, k)) * dx + (X.u(i, j, k) - X.u(i, j, k - 1)) * dz) +
             b1 * ((W(i, j + 1, k) - wc) * dy + (X.v(i, j + 1, k) - X.v(i, j + 1, k - 1)) * dz) -
             b0 * ((wc - W(i, j - 1, k)) * dy + (X.v(i, j, k) - X.v(i, j, k - 1)) * dz) +
-            (dmd_k * T(2.) * (W(i, j, k + 1) - wc) - dmd_m * T(2.) * (wc - W(i, j, k - 1))) * dz) /
+            (dmd_k * T(2.) * (W(i, j, k + 1) - wc) - dmd_m * T(2.) * (wc - W(i, j, k - 1))) * dzw) /
                rhoz;
 }
 

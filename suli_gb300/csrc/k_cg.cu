@@ -71,8 +71,21 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_setup1(const CaseDev<T> *__rest
     T si1 = aux1 / (ipa ? r1 : icf<T>(i + 1, nx, px, [&](int m) { return AT(rho, m, j, k); }));
     T sj0 = aux2 / (ipa ? r1 : icf<T>(j, ny, false, [&](int m) { return AT(rho, i, m, k); }));
     T sj1 = aux2 / (ipa ? r1 : icf<T>(j + 1, ny, false, [&](int m) { return AT(rho, i, m, k); }));
-    T sk0 = aux3 / (ipa ? r1 : icf<T>(k, nz, false, [&](int m) { return AT(rho, i, j, m); }));
-    T sk1 = aux3 / (ipa ? r1 : icf<T>(k + 1, nz, false, [&](int m) { return AT(rho, i, j, m); }));
+    T sk0, sk1;
+    if (c.dzk) {
+        // SuLi-ICdz/9_grad.f90:105,141: dt / (dz(k) dz(k) rho_face), the face
+        // density weighted by the spacing
+        auto rz = [&](int f) {
+            const int ff = f < 2 ? 2 : (f > nz ? nz : f);
+            const double a = c.dzk[ff], b = c.dzk[ff - 1];
+            return (AT(rho, i, j, ff) * T(a) + AT(rho, i, j, ff - 1) * T(b)) / T(a + b);
+        };
+        sk0 = T(dt) / (T(c.dzk[k]) * T(c.dzk[k]) * rz(k));
+        sk1 = T(dt) / (T(c.dzk[k + 1]) * T(c.dzk[k + 1]) * rz(k + 1));
+    } else {
+        sk0 = aux3 / (ipa ? r1 : icf<T>(k, nz, false, [&](int m) { return AT(rho, i, j, m); }));
+        sk1 = aux3 / (ipa ? r1 : icf<T>(k + 1, nz, false, [&](int m) { return AT(rho, i, j, m); }));
+    }
     long long q = g.at(i, j, k);
     c.spi[q] = si0;
     c.spj[q] = sj0;
@@ -91,7 +104,7 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_setup1(const CaseDev<T> *__rest
         if (c.obs_lsz[q] >= T(0.)) wa = T(0.);
         if (c.obs_lsz[q + g.sxy] >= T(0.)) wb = T(0.);
     }
-    c.qpr[q] = (ua - ub) / T(c.dx) + (va - vb) / T(c.dy) + (wa - wb) / T(c.dz);
+    c.qpr[q] = (ua - ub) / T(c.dx) + (va - vb) / T(c.dy) + (wa - wb) / T(c.dzk ? c.dzzk[k] : c.dz);
 }
 
 template <typename T>
@@ -151,10 +164,25 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_op1m(const CaseDev<T> *__restri
     };
     face(c.pfx64, c.spi64, q, c.idx, icf<double>(i, nx, px, [&](int m) { return AT(rho, m, j, k); }));
     face(c.pfy64, c.spj64, q, c.idy, icf<double>(j, ny, false, [&](int m) { return AT(rho, i, m, k); }));
-    face(c.pfz64, c.spk64, q, c.idz, icf<double>(k, nz, false, [&](int m) { return AT(rho, i, j, m); }));
+    if (c.dzk) {
+        // SuLi-ICdz: conductance 1 / (dz(k)^2 rho_face) (9_grad.f90:141), the
+        // projection's factor 1 / (dzz(k) rho_face) (10_pos.f90:41), the face
+        // density weighted by the spacing
+        auto zface = [&](long long qf, int f) {
+            const int ff = f < 2 ? 2 : (f > nz ? nz : f);
+            const double a = c.dzk[ff], b = c.dzk[ff - 1];
+            const double ir = rcp_nr64((AT(rho, i, j, ff) * a + AT(rho, i, j, ff - 1) * b) / (a + b));
+            c.pfz64[qf] = c.idzzk[f] * ir;
+            c.spk64[qf] = (c.idzk[f] * c.idzk[f]) * ir;
+        };
+        zface(q, k);
+        if (k == nz) zface(q + g.sxy, nz + 1);
+    } else {
+        face(c.pfz64, c.spk64, q, c.idz, icf<double>(k, nz, false, [&](int m) { return AT(rho, i, j, m); }));
+    }
     if (i == nx) face(c.pfx64, c.spi64, q + 1, c.idx, icf<double>(nx + 1, nx, px, [&](int m) { return AT(rho, m, j, k); }));
     if (j == ny) face(c.pfy64, c.spj64, q + g.sx, c.idy, icf<double>(ny + 1, ny, false, [&](int m) { return AT(rho, i, m, k); }));
-    if (k == nz) face(c.pfz64, c.spk64, q + g.sxy, c.idz, icf<double>(nz + 1, nz, false, [&](int m) { return AT(rho, i, j, m); }));
+    if (k == nz && !c.dzk) face(c.pfz64, c.spk64, q + g.sxy, c.idz, icf<double>(nz + 1, nz, false, [&](int m) { return AT(rho, i, j, m); }));
 }
 
 template <typename T>
@@ -256,7 +284,7 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_rhs_m(const CaseDev<T> *__restr
         if (c.obs_lsz[q + g.sxy] >= T(0.)) wb = 0.;
     }
     const double rc = c.r64[q];
-    const double b = ((ua - ub) * c.idx + (va - vb) * c.idy + (wa - wb) * c.idz) * c.sc[S_IDT];
+    const double b = ((ua - ub) * c.idx + (va - vb) * c.idy + (wa - wb) * (c.dzk ? c.idzzk[k] : c.idz)) * c.sc[S_IDT];
     const double qs = b * rc;
     c.qpr64[q] = qs;
     c.qpr[q] = T(qs);

@@ -127,6 +127,17 @@ __device__ __forceinline__ void der_weno_at(const CaseDev<T> &c, const T *__rest
     load_line<T>(a, g.at(i, 0, k), g.sx, j, n1, c.ccy0 == 0 ? 0 : 2, L);
     weno_pm<T>(L, T(c.idy), yp, ym);
     load_line<T>(a, g.at(i, j, 0), g.sxy, k, n2, 2, L);
+    if (c.dz11 != nullptr) {
+        // SuLi-ICdz's wenoz: the differences over the extrapolated spacing,
+        // D = (phi(m+1) - phi(m)) / dz11(m+1), m = k-3 .. k+2
+        // (SuLi-ICdz/8_derivadas.f90:1090-1102)
+        T D[6];
+#pragma unroll
+        for (int t = 0; t < 6; ++t) D[t] = (L[t + 1] - L[t]) / T(c.dz11[k - 2 + t]);
+        zp = weno5<T>(D[5], D[4], D[3], D[2], D[1]);
+        zm = weno5<T>(D[0], D[1], D[2], D[3], D[4]);
+        return;
+    }
     weno_pm<T>(L, T(c.idz), zp, zm);
 }
 template <typename T>
@@ -370,7 +381,7 @@ __global__ void __launch_bounds__(NTHREADS) k_heaviside_vol(const CaseDev<T> *__
             c.hsy[q] = sy;
             c.hsz[q] = sz;
         }
-        vol = (1. - (1. - hv)) * c.dx * c.dy * c.dz;
+        vol = (1. - (1. - hv)) * c.dx * c.dy * (c.dzk ? c.dzk[k] : c.dz);   // SuLi-ICdz/14_level_set.f90:176,222
     }
     if (set_ini < 0) return;     // properties only (heaviside after the level-set IBM)
     double vals[1] = {vol}, tot[1];

@@ -73,8 +73,10 @@ __global__ void __launch_bounds__(NTHREADS) k_visco_faces(const CaseDev<T> *__re
         AT(c.xmu, i, j, k) = interp_cf<T>(i, nx, px, [&](int m) { return AT(mu, m, j, k); });
     if (i <= nx && j <= ny + 1 && k <= nz)
         AT(c.ymu, i, j, k) = interp_cf<T>(j, ny, false, [&](int m) { return AT(mu, i, m, k); });
-    if (i <= nx && j <= ny && k <= nz + 1)
-        AT(c.zmu, i, j, k) = interp_cf<T>(k, nz, false, [&](int m) { return AT(mu, i, j, m); });
+    if (i <= nx && j <= ny && k <= nz + 1) {
+        auto get = [&](int m) { return AT(mu, i, j, m); };
+        AT(c.zmu, i, j, k) = c.dzk ? zcf_w<T>(c, k, nz, get) : interp_cf<T>(k, nz, false, get);   // SuLi-ICdz/5_viscosidade.f90:155
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -89,18 +91,19 @@ __global__ void __launch_bounds__(NTHREADS) k_convdiff(const CaseDev<T> *__restr
     const Geo &g = c.g;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     const GlobalAcc<T> X{c};
+    const bool vz = (c.dzk != nullptr);   // SuLi-ICdz's variable z spacing
     if (i <= nx + 1 && j <= ny && k <= nz) {
-        T F = face_fu<T>(c, X, i, j, k);
+        T F = vz ? face_fu<T, GlobalAcc<T>, false, true>(c, X, i, j, k) : face_fu<T>(c, X, i, j, k);
         if (fuse) F = compl_fu<T>(c, F, i, j, k);
         AT(c.Fu, i, j, k) = F;
     }
     if (i <= nx && j <= ny + 1 && k <= nz) {
-        T F = face_fv<T>(c, X, i, j, k);
+        T F = vz ? face_fv<T, GlobalAcc<T>, false, true>(c, X, i, j, k) : face_fv<T>(c, X, i, j, k);
         if (fuse) F = compl_fv<T>(c, F, i, j, k);
         AT(c.Fv, i, j, k) = F;
     }
     if (i <= nx && j <= ny && k <= nz + 1) {
-        T F = face_fw<T>(c, X, i, j, k);
+        T F = vz ? face_fw<T, GlobalAcc<T>, false, true>(c, X, i, j, k) : face_fw<T>(c, X, i, j, k);
         if (fuse) F = compl_fw<T>(c, F, AT(c.w, i, j, k), i, j, k);
         AT(c.Fw, i, j, k) = F;
     }
@@ -412,7 +415,14 @@ __global__ void __launch_bounds__(NTHREADS) k_posdin(const CaseDev<T> *__restric
         }
         if (i <= nx && j <= ny && k <= nz + 1) {
             const long long q = g.at(i, j, k);
-            const double f = factor(c.pfz64, q, c.idz, p64 ? 1.0 : interp_cf<double>(k, nz, false, [&](int m) { return AT(r64, i, j, m); }));
+            double f;
+            if (c.dzk && !p64) {   // SuLi-ICdz/10_pos.f90:41: dt / dzz(k) over the spacing-weighted face density
+                const int ff = k < 2 ? 2 : (k > nz ? nz : k);
+                const double a = c.dzk[ff], b = c.dzk[ff - 1];
+                f = (ddt * c.idzzk[k]) * rcp_nr64((AT(r64, i, j, ff) * a + AT(r64, i, j, ff - 1) * b) / (a + b));
+            } else {
+                f = factor(c.pfz64, q, c.idz, p64 ? 1.0 : interp_cf<double>(k, nz, false, [&](int m) { return AT(r64, i, j, m); }));
+            }
             const double x = c.w64[q] - dp64(i, j, k, i, j, k - 1) * f;
             c.w64[q] = x;
             c.w[q] = T(x);
@@ -428,8 +438,14 @@ __global__ void __launch_bounds__(NTHREADS) k_posdin(const CaseDev<T> *__restric
         AT(c.v, i, j, k) = AT(c.v, i, j, k) - aux2 * dp(i, j, k, i, j - 1, k) / ry;
     }
     if (i <= nx && j <= ny && k <= nz + 1) {
-        T rz = interp_cf<T>(k, nz, false, [&](int m) { return AT(rho, i, j, m); });
-        AT(c.w, i, j, k) = AT(c.w, i, j, k) - dt / T(c.dz) * dp(i, j, k, i, j, k - 1) / rz;
+        auto get = [&](int m) { return AT(rho, i, j, m); };
+        if (c.dzk) {   // SuLi-ICdz/10_pos.f90:41
+            T rz = zcf_w<T>(c, k, nz, get);
+            AT(c.w, i, j, k) = AT(c.w, i, j, k) - dt / T(c.dzzk[k]) * dp(i, j, k, i, j, k - 1) / rz;
+        } else {
+            T rz = interp_cf<T>(k, nz, false, get);
+            AT(c.w, i, j, k) = AT(c.w, i, j, k) - dt / T(c.dz) * dp(i, j, k, i, j, k - 1) / rz;
+        }
     }
 }
 
@@ -447,12 +463,12 @@ __global__ void __launch_bounds__(NTHREADS) k_conmassa(const CaseDev<T> *__restr
         if (c.u64 != nullptr) {   // mixed form: the FP64 masters
             const double *u = c.u64, *v = c.v64, *w = c.w64;
             d = (AT(u, i + 1, j, k) - AT(u, i, j, k)) * c.idx + (AT(v, i, j + 1, k) - AT(v, i, j, k)) * c.idy +
-                (AT(w, i, j, k + 1) - AT(w, i, j, k)) * c.idz;
+                (AT(w, i, j, k + 1) - AT(w, i, j, k)) * (c.dzk ? c.idzzk[k] : c.idz);
         } else {
             const T *u = c.u, *v = c.v, *w = c.w;
             d = ((double)AT(u, i + 1, j, k) - (double)AT(u, i, j, k)) / c.dx +
                 ((double)AT(v, i, j + 1, k) - (double)AT(v, i, j, k)) / c.dy +
-                ((double)AT(w, i, j, k + 1) - (double)AT(w, i, j, k)) / c.dz;
+                ((double)AT(w, i, j, k + 1) - (double)AT(w, i, j, k)) / (c.dzk ? c.dzzk[k] : c.dz);   // SuLi-ICdz/4_plot.f90:406
         }
         AT(c.div, i, j, k) = T(d);
         m = fabs(d);

@@ -151,6 +151,14 @@ static int validate(const suli_params &p)
     if (p.esp_type < 0 || p.esp_type > 2) return bad("esp_type must be 0, 1 or 2");
     if (!(p.wave_t == 0 || p.wave_t == 1 || p.wave_t == 2 || p.wave_t == 5)) return bad("wave_t must be 0, 1, 2 or 5");
     if (p.wave_t > 0 && !(p.n_w > 0 && p.h0_f > 0)) return bad("wave_t > 0 needs waves_coef's n_w > 0 and h0_f > 0");
+    if (p.dz_t != 0 && p.dz_t != 1) return bad("dz_t must be 0 (uniform) or 1 (linear, SuLi-ICdz)");
+    if (p.dz_t == 1) {
+        if (!(p.dzmin > 0 && p.dzmax > 0)) return bad("dz_t = 1 needs dzmin > 0 and dzmax > 0");
+        if (p.m_turb != 0 || p.ibm_t != 0 || p.t_tens != 0 || p.t_press != 1 || p.mms_t != 0 || p.esp_type != 0 ||
+            p.wave_t != 0 || p.ccx0 == 3)
+            return bad("dz_t = 1 (variable dz) is built for the plain two-fluid flow: m_turb = 0, no IBM, surface "
+                       "tension, IPA, MMS, sponge, waves or inflow");
+    }
     if (p.outflow_flux != 0 && p.outflow_flux != 1) return bad("outflow_flux must be 0 or 1");
     if (p.outflow_flux == 1 && !(p.ccxf == 4 && p.ccx0 == 3))
         return bad("outflow_flux = 1 balances a free outflow (ccxf = 4) against a prescribed inflow (ccx0 = 3)");
@@ -346,6 +354,7 @@ struct Impl : ImplBase {
         if (icase < 0 || icase >= ncases) return fail(SULI_BAD_ARG, "case index out of range");
         if (!path || (t_plot != 0 && t_plot != 1)) return fail(SULI_BAD_ARG, "bad path or t_plot (0 or 1)");
         const suli_params &q = P[icase];
+        if (q.dz_t == 1) return fail(SULI_BAD_CONFIG, "the field record of a variable-dz grid (dz_t = 1) is not built");
         const long long nx1 = q.nx + 1, ny1 = q.ny + 1, nz1 = q.nz + 1;
         const long long n1 = nx1 * ny1 * nz1, nc = (long long)q.nx * q.ny * q.nz;
         const long long ndev = 4 * n1 + nc + (t_plot ? 6 * nc : 0), nf = 3 * n1 + ndev;
@@ -431,11 +440,11 @@ struct Impl : ImplBase {
                                      (long long)(q.nx + 2) * (q.nz + 2) + (long long)(q.nx + 2) * (q.ny + 2) +
                                          (long long)(q.ny + 2) * (q.nz + 2)});
             maxplane = (int)std::max<long long>(maxplane, mp);
-            cd.dx = q.dx; cd.dy = q.dy; cd.dz = q.dz;
-            cd.dx1 = std::max({q.dx, q.dy, q.dz});
+            cd.dx = q.dx; cd.dy = q.dy; cd.dz = (q.dz_t == 1) ? q.dzmin : q.dz;   // dza of SuLi-ICdz
+            cd.dx1 = std::max({q.dx, q.dy, cd.dz});
             cd.dt1 = 0.1 * cd.dx1;
-            cd.deltai = std::pow(q.dx * q.dy * q.dz, 1. / 3.);
-            cd.idx = 1.0 / q.dx; cd.idy = 1.0 / q.dy; cd.idz = 1.0 / q.dz;
+            cd.deltai = std::pow(q.dx * q.dy * cd.dz, 1. / 3.);
+            cd.idx = 1.0 / q.dx; cd.idy = 1.0 / q.dy; cd.idz = 1.0 / cd.dz;
             cd.alpha1 = q.alpha1;
             cd.rho_f1 = q.rho_f1; cd.mu_f1 = q.mu_f1; cd.rho_f2 = q.rho_f2; cd.mu_f2 = q.mu_f2;
             cd.gx = q.gx; cd.gz = q.gz;
@@ -475,7 +484,10 @@ struct Impl : ImplBase {
             T **kf[] = {&cd.ka, &cd.nut, &cd.sij, &cd.ka0, &cd.fk0, &cd.fk1, &cd.fka};
             T **af[] = {&cd.prd0, &cd.px, &cd.py, &cd.pz};
             const int nkf = (q.m_turb >= 2) ? 7 : 0, naf = (q.t_press == 2) ? 4 : 0, nsf = (q.esp_type > 0) ? 1 : 0;
-            size_t bytes = fb * (ntf + nkf + naf + nsf) + ib * 4 + pb * 4 + (mixed ? 20 * db : 0) + (mg ? 8 * fb : 0);
+            // SuLi-ICdz's z spacing arrays (dz_t = 1): dz, dzz, 1/dz, 1/dzz over
+            // 0..nz+1 and dz11 over -2..nz+3
+            const size_t zb = (q.dz_t == 1) ? ((size_t)5 * (q.nz + 6) * sizeof(double) + 255) / 256 * 256 : 0;
+            size_t bytes = fb * (ntf + nkf + naf + nsf) + ib * 4 + pb * 4 + (mixed ? 20 * db : 0) + (mg ? 8 * fb : 0) + zb;
             void *slab = nullptr;
             CK(cudaMalloc(&slab, bytes));
             slabs.push_back(slab);
@@ -487,6 +499,31 @@ struct Impl : ImplBase {
             for (int f = 0; f < nkf; ++f) { *kf[f] = (T *)cur; cur += fb; }
             for (int f = 0; f < naf; ++f) { *af[f] = (T *)cur; cur += fb; }
             if (nsf) { cd.epis = (T *)cur; cur += fb; }
+            if (zb) {
+                // dz_dist (SuLi-ICdz/2_iniciais.f90:326-406) and wenoz's extrapolated
+                // spacing (SuLi-ICdz/8_derivadas.f90:1076-1084), formed on the host
+                const int nz = q.nz, w = nz + 6;
+                std::vector<double> hz((size_t)5 * w, 0.0);
+                double *dzh = hz.data(), *dzzh = dzh + w, *idzh = dzzh + w, *idzzh = idzh + w, *d11 = idzzh + w + 2;
+                for (int k = 0; k <= nz + 1; ++k) dzh[k] = q.dzmin + (q.dzmax - q.dzmin) * k / nz;
+                for (int k = 1; k <= nz + 1; ++k) dzzh[k] = (dzh[k] + dzh[k - 1]) * 0.5;
+                dzzh[0] = dzzh[1];
+                dzzh[nz + 1] = dzzh[nz];
+                for (int k = 0; k <= nz + 1; ++k) { idzh[k] = 1.0 / dzh[k]; idzzh[k] = 1.0 / dzzh[k]; }
+                const double c11 = 1. / 11.;
+                for (int k = 0; k <= nz + 1; ++k) d11[k] = dzh[k];
+                d11[0] = c11 * (18. * d11[1] - 9. * d11[2] + 2. * d11[3]);
+                d11[-1] = c11 * (18. * d11[0] - 9. * d11[1] + 2. * d11[2]);
+                d11[-2] = c11 * (18. * d11[-1] - 9. * d11[0] + 2. * d11[1]);
+                d11[nz + 1] = c11 * (18. * d11[nz] - 9. * d11[nz - 1] + 2. * d11[nz - 2]);
+                d11[nz + 2] = c11 * (18. * d11[nz + 1] - 9. * d11[nz] + 2. * d11[nz - 1]);
+                d11[nz + 3] = c11 * (18. * d11[nz + 2] - 9. * d11[nz + 1] + 2. * d11[nz]);
+                double *dd = (double *)cur;
+                CK(cudaMemcpyAsync(dd, hz.data(), sizeof(double) * hz.size(), cudaMemcpyHostToDevice, st));
+                CK(cudaStreamSynchronize(st));   // the host vector dies with this scope
+                cd.dzk = dd; cd.dzzk = dd + w; cd.idzk = dd + 2 * w; cd.idzzk = dd + 3 * w; cd.dz11 = dd + 4 * w + 2;
+                cur += zb;
+            }
             if (mixed) {
                 double **d64[] = {&cd.e64, &cd.r64, &cd.rho64, &cd.spi64, &cd.spj64, &cd.spk64, &cd.dpr64, &cd.qpr64,
                                   &cd.u64, &cd.v64, &cd.w64, &cd.u064, &cd.v064, &cd.w064,
@@ -611,6 +648,8 @@ struct Impl : ImplBase {
     {
         const char *env = std::getenv("SULI_CONVDIFF");
         if (env && std::string(env) == "0") return SULI_OK;
+        for (int c = 0; c < ncases; ++c)
+            if (P[c].dz_t == 1) return SULI_OK;   // the variable-dz stencils run in the gather kernel
         void *fn = nullptr;
         cudaDriverEntryPointQueryResult qr;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &qr) !=

@@ -138,6 +138,10 @@ struct CaseDev {
     int esp_type;               // sponge layer (0 none)
     int wave_t;                 // inflow waves (0 none, 1/2 Stokes I/II, 5 Stokes V)
     int outflow_flux;           // 1: contorno(2) balances the free-outflow faces' flux to the inflow's
+    // SuLi-ICdz's variable z spacing (dz_t = 1, else all null): dz(k) and
+    // dzz(k) for k = 0..nz+1 with their reciprocals, and the WENO z
+    // spacing dz11(m), m = -2..nz+3 (dz11 points at m = 0)
+    const double *dzk, *dzzk, *idzk, *idzzk, *dz11;
     double a_w, f_w, n_w, h0_f, aeta[5], avel[5];   // waves_coef's results
     int reinit_max, cg_max, cg_tol_mode;
     double cg_tol;

@@ -90,6 +90,43 @@ def test_mixed_channel_ibm_against_oracle(gpu_lib, kind):
     assert ev <= 1e-6 and els <= 1e-6 and ep <= 1e-6
 
 
+def test_mixed_stretched_z_routines_against_oracle(gpu_lib):
+    """SuLi-ICdz's stretched z grid in the mixed form: the level set (WENO
+    z over the extrapolated spacing, the volume with dz(k)), visco's
+    spacing-weighted face viscosity and convdiff + tempo from the oracle's
+    state after two steps, against the oracle (FP32 storage: 1e-6)."""
+    from helpers import copy_state
+    case = cases.dam_break_dz(24, 12, 16)
+    case.params.cg_max_iter = 40
+    o = oracle_for(case, warm_steps=2)
+    cm = cases.dam_break_dz(24, 12, 16, precision=PREC_MIXED)
+    cm.params.cg_max_iter = 40
+    g = gpu_lib.SuliGPU(cm.params)
+    g.start(cm.fields)
+    copy_state(o, g)
+    g.set_scalar("DT", o.scalar("DT"))
+    o.level_set()
+    g.set_replay(None, o.diag().reinit_iters)
+    g.level_set()
+    g.set_replay(None, -1)
+    assert rel_l2(g.download("LS"), o.field("LS")) <= 1e-6
+    assert abs(g.scalar("VOL_INS") - o.scalar("VOL_INS")) <= 1e-6 * o.scalar("VOL_INS")
+    copy_state(o, g)
+    for x in (o, g):
+        x.visco()
+        x.set_stage(2)
+        x.convdiff()
+        x.complementos()
+    assert rel_l2(g.download("ZMU"), o.field("ZMU")) <= 1e-6
+    fg = np.concatenate([g.download(n).ravel() for n in ("FU", "FV", "FW")])
+    fo = np.concatenate([o.field(n).ravel() for n in ("FU", "FV", "FW")])
+    assert rel_l2(fg, fo) <= 1e-6
+    o.tempo()
+    g.tempo()
+    assert rel_l2(_vel(g.download), _vel(o.field)) <= 1e-6
+    g.close()
+
+
 @pytest.mark.parametrize("which", ["k_les", "k_des", "ipa", "sponge"])
 def test_mixed_keq_ipa_against_oracle(gpu_lib, which):
     """The k equation (FP32 ka, nut and sub-stage buffers), the IPA (FP32
