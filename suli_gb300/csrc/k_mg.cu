@@ -23,9 +23,9 @@
 // two cells of one colour couple; residuals and restriction use the full
 // operator.
 //
-// Every kernel runs on a fixed grid over the work units of level l (chunks of
-// tiles on level 0, tiles above) of the cases in an active-case table, so
-// cases that have converged cost nothing.
+// Every kernel runs on a fixed grid over the work units of level l (column
+// units of 32 x 8 cells and COL_Z planes) of the cases in an active-case
+// table, so cases that have converged cost nothing.
 #include "suli_kernels.cuh"
 
 #include <algorithm>
@@ -34,12 +34,12 @@
 namespace suli {
 
 
-// one colour of red-black Gauss-Seidel on L z = f; zero != 0: the sweep
-// starts from z = 0 (this colour gets f / dg, the other colour 0).  The cells
-// of UW tiles are loaded before any is written.  L0: the case grid's column
-// path (level 0 only), else the tile path of the coarser levels -- two
-// instantiations, so each keeps its own registers.
-template <typename T, bool L0>
+// one colour of red-black Gauss-Seidel on L z = f on level l; zero != 0:
+// the sweep starts from z = 0 (this colour gets f / dg, the other colour 0).
+// One column of COL_Z planes per thread, COL_G planes at a time with every
+// load of a group issued before any arithmetic (the z-neighbours of a cell of
+// this colour have the other colour, unchanged by this sweep).
+template <typename T>
 __global__ void __launch_bounds__(NTHREADS, 4) k_mg_smooth(const CaseDev<T> *__restrict__ cs, const int *__restrict__ tab,
                                                            int N, int l, int color, int zero)
 {
@@ -48,123 +48,75 @@ __global__ void __launch_bounds__(NTHREADS, 4) k_mg_smooth(const CaseDev<T> *__r
         const MgLev<T> &L = c.mg[l];
         const Geo &g = L.g;
         const int nx = g.nx, ny = g.ny;
-        const long long sx = g.sx, sxy = g.sxy;
         // wrap couplings the smoother keeps (even periodic length, see above);
         // elsewhere a wall neighbour is a ghost of z (never written: zero) and
         // the wall conductance is zero, so the stencil needs no branch
         const bool wx = c.ccx0 == 0 && !(nx & 1) && nx > 1;
         const bool wy = c.ccy0 == 0 && !(ny & 1) && ny > 1;
         const T *z = L.z;
-        if constexpr (L0) {
-            // case grid: one column of COL_Z planes per thread, COL_G planes
-            // at a time with every load of a group issued before any
-            // arithmetic (the z-neighbours of a cell of this colour have the
-            // other colour, unchanged by this sweep)
-            const Column cl = column_of(g, u);
-            const int i = cl.i, j = cl.j;
-            // 32-bit offsets: a case's box holds fewer than 2^31 elements
-            const int isx = (int)sx, isxy = (int)sxy;
-            const int dxm = (wx && i == 1) ? (nx - 1) : -1;
-            const int dxp = (wx && i == nx) ? -(nx - 1) : 1;
-            const int dym = (wy && j == 1) ? (ny - 1) * isx : -isx;
-            const int dyp = (wy && j == ny) ? -(ny - 1) * isx : isx;
-            const T *__restrict__ f = L.f;
-            const T *__restrict__ dgi = L.dgi;
-            const T *__restrict__ cxa = L.cx;
-            const T *__restrict__ cya = L.cy;
-            const T *__restrict__ cza = L.cz;
-            T *zw = L.z;
-            for (int kb = cl.k0; kb <= cl.k1; kb += COL_G) {
-                const int q0 = (int)g.at(i, j, kb);
-                const int np = min(COL_G, cl.k1 - kb + 1);
-                T zz[COL_G + 2], czz[COL_G + 1], fv[COL_G], dv[COL_G];
-                T a0[COL_G], a1[COL_G], b0[COL_G], b1[COL_G], za0[COL_G], za1[COL_G], zb0[COL_G], zb1[COL_G];
+        const Column cl = column_of(g, u);
+        const int i = cl.i, j = cl.j;
+        // 32-bit offsets: a case's box holds fewer than 2^31 elements
+        const int isx = (int)g.sx, isxy = (int)g.sxy;
+        const int dxm = (wx && i == 1) ? (nx - 1) : -1;
+        const int dxp = (wx && i == nx) ? -(nx - 1) : 1;
+        const int dym = (wy && j == 1) ? (ny - 1) * isx : -isx;
+        const int dyp = (wy && j == ny) ? -(ny - 1) * isx : isx;
+        const T *__restrict__ f = L.f;
+        const T *__restrict__ dgi = L.dgi;
+        const T *__restrict__ cxa = L.cx;
+        const T *__restrict__ cya = L.cy;
+        const T *__restrict__ cza = L.cz;
+        T *zw = L.z;
+        for (int kb = cl.k0; kb <= cl.k1; kb += COL_G) {
+            const int q0 = (int)g.at(i, j, kb);
+            const int np = min(COL_G, cl.k1 - kb + 1);
+            T zz[COL_G + 2], czz[COL_G + 1], fv[COL_G], dv[COL_G];
+            T a0[COL_G], a1[COL_G], b0[COL_G], b1[COL_G], za0[COL_G], za1[COL_G], zb0[COL_G], zb1[COL_G];
 #pragma unroll
-                for (int t = 0; t < COL_G + 2; ++t) zz[t] = z[q0 + (min(t, np + 1) - 1) * isxy];
+            for (int t = 0; t < COL_G + 2; ++t) zz[t] = z[q0 + (min(t, np + 1) - 1) * isxy];
 #pragma unroll
-                for (int t = 0; t < COL_G + 1; ++t) czz[t] = cza[q0 + min(t, np) * isxy];
+            for (int t = 0; t < COL_G + 1; ++t) czz[t] = cza[q0 + min(t, np) * isxy];
 #pragma unroll
-                for (int t = 0; t < COL_G; ++t) {
-                    const int q = q0 + min(t, np - 1) * isxy;
-                    fv[t] = f[q];
-                    dv[t] = dgi[q];
-                    a0[t] = cxa[q]; a1[t] = cxa[q + 1]; b0[t] = cya[q]; b1[t] = cya[q + isx];
-                    za0[t] = z[q + dxm]; za1[t] = z[q + dxp]; zb0[t] = z[q + dym]; zb1[t] = z[q + dyp];
-                }
-#pragma unroll
-                for (int t = 0; t < COL_G; ++t) {
-                    if (t >= np || !cl.v) continue;
-                    const bool mine = ((i + j + kb + t) & 1) == color;
-                    const T di = dv[t];
-                    T zn;
-                    if (zero) {
-                        zn = mine ? fv[t] * di : T(0);
-                    } else {
-                        if (!mine) continue;
-                        const T sm = fv[t] + a0[t] * za0[t] + a1[t] * za1[t] + b0[t] * zb0[t] + b1[t] * zb1[t] +
-                                     czz[t] * zz[t] + czz[t + 1] * zz[t + 2];
-                        zn = sm * di;
-                    }
-                    zw[q0 + t * isxy] = zn;
-                }
+            for (int t = 0; t < COL_G; ++t) {
+                const int q = q0 + min(t, np - 1) * isxy;
+                fv[t] = f[q];
+                dv[t] = dgi[q];
+                a0[t] = cxa[q]; a1[t] = cxa[q + 1]; b0[t] = cya[q]; b1[t] = cya[q + isx];
+                za0[t] = z[q + dxm]; za1[t] = z[q + dxp]; zb0[t] = z[q + dym]; zb1[t] = z[q + dyp];
             }
-            return;
-        } else {
-            const int t0 = u, t1 = u + 1;
-            TileWalk w(t0, L.ntx, L.nty);
-            for (int lt = t0; lt < t1; lt += UW) {
-                long long q[UW];
-                int ci[UW], cj[UW], ck[UW];
-                bool v[UW];
-                w.next<UW>(lt, t1, g, q, ci, cj, ck, v);
-                T zn[UW];
-                bool wr[UW];
+#pragma unroll
+            for (int t = 0; t < COL_G; ++t) {
+                if (t >= np || !cl.v) continue;
+                const bool mine = ((i + j + kb + t) & 1) == color;
+                const T di = dv[t];
+                T zn;
                 if (zero) {
-#pragma unroll
-                    for (int a = 0; a < UW; ++a) {
-                        const bool mine = ((ci[a] + cj[a] + ck[a]) & 1) == color;
-                        const T di = L.dgi[q[a]], fv = L.f[q[a]];
-                        zn[a] = mine ? fv * di : T(0);
-                        wr[a] = v[a];
-                    }
+                    zn = mine ? fv[t] * di : T(0);
                 } else {
-#pragma unroll
-                    for (int a = 0; a < UW; ++a) {
-                        const int i = ci[a], j = cj[a];
-                        const long long qq = q[a];
-                        const long long qxm = (wx && i == 1) ? qq + (nx - 1) : qq - 1;
-                        const long long qxp = (wx && i == nx) ? qq - (nx - 1) : qq + 1;
-                        const long long qym = (wy && j == 1) ? qq + (long long)(ny - 1) * sx : qq - sx;
-                        const long long qyp = (wy && j == ny) ? qq - (long long)(ny - 1) * sx : qq + sx;
-                        const T di = L.dgi[qq];
-                        const T s = L.f[qq] + L.cx[qq] * z[qxm] + L.cx[qq + 1] * z[qxp] + L.cy[qq] * z[qym] +
-                                    L.cy[qq + sx] * z[qyp] + L.cz[qq] * z[qq - sxy] + L.cz[qq + sxy] * z[qq + sxy];
-                        zn[a] = s * di;
-                        wr[a] = v[a] && (((i + j + ck[a]) & 1) == color);
-                    }
+                    if (!mine) continue;
+                    const T sm = fv[t] + a0[t] * za0[t] + a1[t] * za1[t] + b0[t] * zb0[t] + b1[t] * zb1[t] +
+                                 czz[t] * zz[t] + czz[t + 1] * zz[t + 2];
+                    zn = sm * di;
                 }
-#pragma unroll
-                for (int a = 0; a < UW; ++a)
-                    if (wr[a]) L.z[q[a]] = zn[a];
+                zw[q0 + t * isxy] = zn;
             }
         }
     });
 }
 
-// one half-sweep on level l (the column kernel on the case grid)
+// one half-sweep on level l
 template <typename T>
 void launch_smooth(const Batch<T> &b, const int *tab, int l, int color, int zero, cudaStream_t s)
 {
-    static const int g0 = occupancy_grid((const void *)k_mg_smooth<T, true>);
-    static const int g1 = occupancy_grid((const void *)k_mg_smooth<T, false>);
-    if (l == 0) k_mg_smooth<T, true><<<g0, b.cblock(), 0, s>>>(b.dcases, tab, b.ncases, 0, color, zero);
-    else k_mg_smooth<T, false><<<g1, b.cblock(), 0, s>>>(b.dcases, tab, b.ncases, l, color, zero);
+    static const int g0 = occupancy_grid((const void *)k_mg_smooth<T>);
+    k_mg_smooth<T><<<g0, b.cblock(), 0, s>>>(b.dcases, tab, b.ncases, l, color, zero);
 }
 
-// One whole red-black sweep of the case grid (level 0) in one pass: colour
-// c1, then colour c2 = 1 - c1, reading z from buffer `src` and writing every
-// cell of the grid to buffer `dst` (0: z, 1: z2; src != dst unless zero, the
-// sweep from z = 0, which reads no z).  A block walks a column unit plane by
+// One whole red-black sweep of level l in one pass: colour c1, then colour
+// c2 = 1 - c1, reading z from buffer `src` and writing every cell of the
+// grid to buffer `dst` (0: z, 1: z2; src != dst unless zero, the sweep from
+// z = 0, which reads no z).  A block walks a column unit plane by
 // plane.  For each plane it computes the c1 values on the unit's 34 x 10
 // footprint (the unit and a one-cell ring, wrap neighbours resolved to the
 // cells they stand for) into a three-plane ring in shared memory, and then
@@ -202,17 +154,17 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 template <typename T>
-__global__ void __launch_bounds__(NTHREADS, 4) k_mg_sweep0(const CaseDev<T> *__restrict__ cs, const int *__restrict__ tab,
-                                                           int N, int c1, int zero, int src, int dst)
+__global__ void __launch_bounds__(NTHREADS, 4) k_mg_sweep(const CaseDev<T> *__restrict__ cs, const int *__restrict__ tab,
+                                                          int N, int l, int c1, int zero, int src, int dst)
 {
     static_assert(sizeof(T) == 4, "the staged sweep is the FP32 smoother");
     extern __shared__ __align__(16) unsigned char sw_dyn[];
     T *stg = reinterpret_cast<T *>(sw_dyn);
     __shared__ T ring[3][SW_N];
     const int t = tid_lin();
-    for_active_units(tab, N, 0, [&](int id, int u) {
+    for_active_units(tab, N, l, [&](int id, int u) {
         const CaseDev<T> &c = cs[id];
-        const MgLev<T> &L = c.mg[0];
+        const MgLev<T> &L = c.mg[l];
         const Geo &g = L.g;
         const int nx = g.nx, ny = g.ny, nz = g.nz;
         const int isx = (int)g.sx, isxy = (int)g.sxy;
@@ -381,11 +333,11 @@ __global__ void __launch_bounds__(NTHREADS, 4) k_mg_sweep0(const CaseDev<T> *__r
 
 // the one-pass sweep's grid: its dynamic shared memory opted in, every SM
 // filled to the occupancy that memory allows
-template <typename T> int sweep0_grid(const Batch<T> &b)
+template <typename T> int sweep_grid(const Batch<T> &b)
 {
     static const int full = [] {
-        cudaFuncSetAttribute((const void *)k_mg_sweep0<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SW_SMEM);
-        return occupancy_grid((const void *)k_mg_sweep0<T>, SW_SMEM);
+        cudaFuncSetAttribute((const void *)k_mg_sweep<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SW_SMEM);
+        return occupancy_grid((const void *)k_mg_sweep<T>, SW_SMEM);
     }();
     static const int sms = [] {
         int dev = 0, n = 0;
@@ -399,18 +351,19 @@ template <typename T> int sweep0_grid(const Batch<T> &b)
 }
 
 // f(l) = P^T (f - L z)(l-1): the coarse right-hand side, each coarse cell
-// summing the residuals of its children
+// summing the residuals of its children; one column unit of level l per
+// unit of work (each thread a column of up to COL_Z coarse cells)
 template <typename T>
 __global__ void __launch_bounds__(NTHREADS) k_mg_restrict(const CaseDev<T> *__restrict__ cs,
                                                           const int *__restrict__ tab, int N, int l)
 {
-    for_active_units(tab, N, l, [&](int id, int lt) {     // l >= 1: one unit = one tile
+    for_active_units(tab, N, l, [&](int id, int u) {
         const CaseDev<T> &c = cs[id];
         const MgLev<T> &C = c.mg[l];
         const MgLev<T> &F = c.mg[l - 1];
-        int I, J, K;
-        tile_cell(C.ntx, C.nty, lt, I, J, K);
-        if (I > C.g.nx || J > C.g.ny || K > C.g.nz) return;
+        const Column cl = column_of(C.g, u);
+        if (!cl.v) return;
+        const int I = cl.i, J = cl.j;
         // the full operator (wrap kept on any periodic length); a wall
         // neighbour is a never-written ghost of z (zero) against a zero
         // conductance, and a child beyond an odd fine size is read at a
@@ -419,26 +372,35 @@ __global__ void __launch_bounds__(NTHREADS) k_mg_restrict(const CaseDev<T> *__re
         const int sx = (int)F.g.sx, sxy = (int)F.g.sxy;
         const bool wx = c.ccx0 == 0 && fx > 1, wy = c.ccy0 == 0 && fy > 1;
         const T *__restrict__ z = F.z;
-        T acc = T(0);
+        const T *__restrict__ ff = F.f;
+        const T *__restrict__ fdg = F.dg;
+        const T *__restrict__ fcx = F.cx;
+        const T *__restrict__ fcy = F.cy;
+        const T *__restrict__ fcz = F.cz;
+        T *__restrict__ cf = C.f;
+#pragma unroll 2
+        for (int K = cl.k0; K <= cl.k1; ++K) {
+            T acc = T(0);
 #pragma unroll
-        for (int d = 0; d < 8; ++d) {
-            const int i0 = 2 * I - 1 + (d & 1), j0 = 2 * J - 1 + ((d >> 1) & 1), k0 = 2 * K - 1 + (d >> 2);
-            const bool in = i0 <= fx && j0 <= fy && k0 <= fz;
-            const int i = min(i0, fx), j = min(j0, fy), k = min(k0, fz);
-            const int q = (int)F.g.at(i, j, k);
-            const int qxm = (wx && i == 1) ? q + (fx - 1) : q - 1;
-            const int qxp = (wx && i == fx) ? q - (fx - 1) : q + 1;
-            const int qym = (wy && j == 1) ? q + (fy - 1) * sx : q - sx;
-            const int qyp = (wy && j == fy) ? q - (fy - 1) * sx : q + sx;
-            const T r = F.f[q] - F.dg[q] * z[q] + F.cx[q] * z[qxm] + F.cx[q + 1] * z[qxp] + F.cy[q] * z[qym] +
-                        F.cy[q + sx] * z[qyp] + F.cz[q] * z[q - sxy] + F.cz[q + sxy] * z[q + sxy];
-            acc += in ? r : T(0);
+            for (int d = 0; d < 8; ++d) {
+                const int i0 = 2 * I - 1 + (d & 1), j0 = 2 * J - 1 + ((d >> 1) & 1), k0 = 2 * K - 1 + (d >> 2);
+                const bool in = i0 <= fx && j0 <= fy && k0 <= fz;
+                const int i = min(i0, fx), j = min(j0, fy), k = min(k0, fz);
+                const int q = (int)F.g.at(i, j, k);
+                const int qxm = (wx && i == 1) ? q + (fx - 1) : q - 1;
+                const int qxp = (wx && i == fx) ? q - (fx - 1) : q + 1;
+                const int qym = (wy && j == 1) ? q + (fy - 1) * sx : q - sx;
+                const int qyp = (wy && j == fy) ? q - (fy - 1) * sx : q + sx;
+                const T r = ff[q] - fdg[q] * z[q] + fcx[q] * z[qxm] + fcx[q + 1] * z[qxp] + fcy[q] * z[qym] +
+                            fcy[q + sx] * z[qyp] + fcz[q] * z[q - sxy] + fcz[q + sxy] * z[q + sxy];
+                acc += in ? r : T(0);
+            }
+            cf[C.g.at(I, J, K)] = acc;
         }
-        C.f[C.g.at(I, J, K)] = acc;
     });
 }
 
-// z(l) += P z(l+1); on level 0 with to2 the sum goes to z2 (z unchanged)
+// z(l) += P z(l+1); with to2 the sum goes to z2 (z unchanged)
 template <typename T>
 __global__ void __launch_bounds__(NTHREADS) k_mg_prolong(const CaseDev<T> *__restrict__ cs,
                                                          const int *__restrict__ tab, int N, int l, int to2)
@@ -447,30 +409,12 @@ __global__ void __launch_bounds__(NTHREADS) k_mg_prolong(const CaseDev<T> *__res
         const CaseDev<T> &c = cs[id];
         const MgLev<T> &F = c.mg[l];
         const MgLev<T> &C = c.mg[l + 1];
-        if (l == 0) {
-            const Column cl = column_of(F.g, u);
-            if (!cl.v) return;
-            T *out = to2 ? F.z2 : F.z;
-            long long q = F.g.at(cl.i, cl.j, cl.k0);
-            for (int k = cl.k0; k <= cl.k1; ++k, q += F.g.sxy)
-                out[q] = F.z[q] + C.z[C.g.at((cl.i + 1) >> 1, (cl.j + 1) >> 1, (k + 1) >> 1)];
-            return;
-        }
-        const int t0 = u, t1 = u + 1;
-        TileWalk w(t0, F.ntx, F.nty);
-        for (int lt = t0; lt < t1; lt += UW) {
-            long long q[UW];
-            int ci[UW], cj[UW], ck[UW];
-            bool v[UW];
-            w.next<UW>(lt, t1, F.g, q, ci, cj, ck, v);
-            T zn[UW];
-#pragma unroll
-            for (int a = 0; a < UW; ++a)
-                zn[a] = F.z[q[a]] + C.z[C.g.at((ci[a] + 1) >> 1, (cj[a] + 1) >> 1, (ck[a] + 1) >> 1)];
-#pragma unroll
-            for (int a = 0; a < UW; ++a)
-                if (v[a]) F.z[q[a]] = zn[a];
-        }
+        const Column cl = column_of(F.g, u);
+        if (!cl.v) return;
+        T *out = to2 ? F.z2 : F.z;
+        long long q = F.g.at(cl.i, cl.j, cl.k0);
+        for (int k = cl.k0; k <= cl.k1; ++k, q += F.g.sxy)
+            out[q] = F.z[q] + C.z[C.g.at((cl.i + 1) >> 1, (cl.j + 1) >> 1, (k + 1) >> 1)];
     });
 }
 
@@ -714,11 +658,12 @@ template <typename T> void launch_mg_vcycle(const Batch<T> &b, const int *tab, i
         const char *e = std::getenv("SULI_MG_NUC");
         return (e && std::atoi(e) == 1) ? 1 : 2;
     }();
-    // the case grid's sweeps as one-pass whole sweeps, or (SULI_MG_FUSED=0)
-    // as two half-sweep launches each: the same arithmetic
+    // the sweeps of the levels smoothed by launches as one-pass whole
+    // sweeps, or (SULI_MG_FUSED=0) as two half-sweep launches each: the same
+    // arithmetic
     const char *fe = std::getenv("SULI_MG_FUSED");
     const bool fused = !(fe && std::atoi(fe) == 0);
-    const int gW = sweep0_grid<T>(b);
+    const int gW = sweep_grid<T>(b);
     const int ncoarse = 6;
     // levels lc.. in one block per case (k_mg_coarse), the finer ones by
     // whole-grid launches
@@ -726,11 +671,11 @@ template <typename T> void launch_mg_vcycle(const Batch<T> &b, const int *tab, i
     const int ldown = (lc < NL) ? lc : NL - 1;    // levels smoothed by launches before the coarse end
     for (int l = 0; l < ldown; ++l) {
         const int nu = (l == 0) ? nu0 : nuc;
-        if (l == 0 && fused) {
+        if (fused) {
             // the buffers alternate so that the last sweep writes z
             for (int it = 0; it < nu; ++it) {
                 const int dst = (nu - 1 - it) & 1;
-                k_mg_sweep0<T><<<gW, b.cblock(), SW_SMEM, s>>>(b.dcases, tab, N, 0, it == 0, 1 - dst, dst);
+                k_mg_sweep<T><<<gW, b.cblock(), SW_SMEM, s>>>(b.dcases, tab, N, l, 0, it == 0, 1 - dst, dst);
             }
             k_mg_restrict<T><<<gR, b.cblock(), 0, s>>>(b.dcases, tab, N, l + 1);
             count_launch(nu + 1);
@@ -755,13 +700,13 @@ template <typename T> void launch_mg_vcycle(const Batch<T> &b, const int *tab, i
     }
     for (int l = ldown - 1; l >= 0; --l) {
         const int nu = (l == 0) ? nu0 : nuc;
-        if (l == 0 && fused) {
+        if (fused) {
             // black then red; the prolongation writes the buffer the first
             // sweep reads, chosen so that the last sweep writes z
             k_mg_prolong<T><<<gP, b.cblock(), 0, s>>>(b.dcases, tab, N, l, nu & 1);
             for (int it = 0; it < nu; ++it) {
                 const int dst = (nu - 1 - it) & 1;
-                k_mg_sweep0<T><<<gW, b.cblock(), SW_SMEM, s>>>(b.dcases, tab, N, 1, 0, 1 - dst, dst);
+                k_mg_sweep<T><<<gW, b.cblock(), SW_SMEM, s>>>(b.dcases, tab, N, l, 1, 0, 1 - dst, dst);
             }
             count_launch(nu + 1);
             continue;
@@ -790,8 +735,8 @@ template <> int launch_mg_smooth0<double>(const Batch<double> &, const int *, in
 template <typename T> int launch_mg_sweep0(const Batch<T> &b, const int *tab, cudaStream_t s)
 {
     if (b.nlev < 2) return -1;
-    const int gW = sweep0_grid<T>(b);
-    k_mg_sweep0<T><<<gW, b.cblock(), SW_SMEM, s>>>(b.dcases, tab, b.ncases, 0, 0, 0, 1);
+    const int gW = sweep_grid<T>(b);
+    k_mg_sweep<T><<<gW, b.cblock(), SW_SMEM, s>>>(b.dcases, tab, b.ncases, 0, 0, 0, 0, 1);
     count_launch();
     return 0;
 }

@@ -535,6 +535,7 @@ struct Impl : ImplBase {
                 MgLev<T> &L = cd.mg[0];
                 L.g = g;
                 L.ntx = cd.ntx; L.nty = cd.nty; L.ntz = cd.ntz; L.ntiles = cd.ntiles;
+                L.ncols = cd.nchunks;
                 T **lf[] = {&L.cx, &L.cy, &L.cz, &L.dg, &L.z, &L.f, &L.z2, &L.dgi};
                 for (int f = 0; f < 8; ++f) { *lf[f] = (T *)cur; cur += fb; }
             }
@@ -558,12 +559,13 @@ struct Impl : ImplBase {
                     dx = (dx + 1) / 2; dy = (dy + 1) / 2; dz = (dz + 1) / 2;
                     MgLev<T> &L = cd.mg[l];
                     L.g.nx = dx; L.g.ny = dy; L.g.nz = dz;
-                    L.g.sx = dx + 2;
-                    L.g.sxy = L.g.sx * (dy + 2);
-                    L.g.total = L.g.sxy * (dz + 2);
+                    L.g.sx = (dx + 3 + 7) / 8 * 8;
+                    L.g.sxy = L.g.sx * (dy + 3);
+                    L.g.total = L.g.sxy * (dz + 3);
                     L.ntx = (dx + TX - 1) / TX; L.nty = (dy + TY - 1) / TY; L.ntz = (dz + TZ - 1) / TZ;
                     L.ntiles = L.ntx * L.nty * L.ntz;
-                    bytes += 7 * (((size_t)L.g.total * sizeof(T) + 255) / 256 * 256);
+                    L.ncols = col_units(dx, dy, dz);
+                    bytes += 8 * (((size_t)L.g.total * sizeof(T) + 255) / 256 * 256);
                     b.mg_tiles[l] += L.ntiles;
                 }
                 void *slab = nullptr;
@@ -574,8 +576,8 @@ struct Impl : ImplBase {
                 for (int l = 1; l < nlev; ++l) {
                     MgLev<T> &L = cd.mg[l];
                     const size_t lb = ((size_t)L.g.total * sizeof(T) + 255) / 256 * 256;
-                    T **lf[] = {&L.cx, &L.cy, &L.cz, &L.dg, &L.z, &L.f, &L.dgi};
-                    for (int f = 0; f < 7; ++f) { *lf[f] = (T *)cur; cur += lb; }
+                    T **lf[] = {&L.cx, &L.cy, &L.cz, &L.dg, &L.z, &L.f, &L.dgi, &L.z2};
+                    for (int f = 0; f < 8; ++f) { *lf[f] = (T *)cur; cur += lb; }
                 }
             }
         }

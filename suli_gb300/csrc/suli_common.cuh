@@ -97,7 +97,9 @@ struct Geo {
 
 // One multigrid level of a case (mixed form).  Level 0 is the case's own grid
 // and box; coarser levels halve each dimension (n -> (n+1)/2, cell I owning
-// fine cells 2I-1 and 2I) in a compact box of sx = nx+2, sxy = sx (ny+2).
+// fine cells 2I-1 and 2I) in a box laid out like the case's (rows of a
+// multiple of 8 elements, 32-byte aligned, so the one-pass sweep's 16-byte
+// copies apply on every level).
 // cx(i,j,k) is the conductance of the face between cells i-1 and i (zero on
 // a Neumann wall), dg the sum of a cell's six face conductances.
 constexpr int MG_MAXL = 12;
@@ -105,9 +107,10 @@ template <typename T>
 struct MgLev {
     Geo g;
     int ntx, nty, ntz, ntiles;
+    int ncols;    // column units of the level (col_units): its active-table units
     T *cx, *cy, *cz, *dg, *z, *f;
     T *dgi;    // 1 / dg (0 where dg = 0): the smoothers multiply instead of divide
-    T *z2;     // level 0: the second buffer of the one-pass sweeps (null above)
+    T *z2;     // the second buffer of the one-pass sweeps
 };
 
 template <typename T>
@@ -572,7 +575,7 @@ __device__ void build_active_table(const CaseDev<T> *__restrict__ cs, int N, int
         int til = 0;
         for (int a = a0; a < a1; ++a) {
             const int id = in ? in[1 + a] : a;
-            if (all || __ldcg(&cs[id].sc[S_CGACTIVE]) != 0.0) til += (s == 0) ? cs[id].nchunks : cs[id].mg[s].ntiles;
+            if (all || __ldcg(&cs[id].sc[S_CGACTIVE]) != 0.0) til += (s == 0) ? cs[id].nchunks : cs[id].mg[s].ncols;
         }
         int ntil;
         int tpos = block_exscan(til, &ntil);
@@ -584,7 +587,7 @@ __device__ void build_active_table(const CaseDev<T> *__restrict__ cs, int N, int
                 if (s == 0) out[1 + pos] = id;
                 lv[1 + pos] = tpos;
                 ++pos;
-                tpos += (s == 0) ? cs[id].nchunks : cs[id].mg[s].ntiles;
+                tpos += (s == 0) ? cs[id].nchunks : cs[id].mg[s].ncols;
             }
         }
         if (t == 0) {

@@ -371,21 +371,28 @@ def test_cached_operator_matches_rebuilt_operator(gpu_lib, monkeypatch):
         assert np.array_equal(a, b)
 
 
-@pytest.mark.parametrize("mk", ["periodic_even", "periodic_odd", "uneven_batch"])
+@pytest.mark.parametrize("mk", ["periodic_even", "periodic_odd", "uneven_batch", "periodic_all_levels",
+                                "uneven_all_levels"])
 def test_one_pass_sweeps_match_half_sweeps(gpu_lib, monkeypatch, mk):
-    """The case grid's one-pass whole sweeps (the default; the first colour
-    recomputed on a one-cell ring, two z buffers) do the arithmetic of the two
-    half-sweep launches (SULI_MG_FUSED=0): same pressures and velocities, same
-    iteration counts.  Covers
-    the kept wrap (even periodic length), the dropped wrap (odd) and a batch
-    of uneven grids (partial column units)."""
+    """The one-pass whole sweeps (the default; the first colour recomputed on
+    a one-cell ring, two z buffers) do the arithmetic of the two half-sweep
+    launches (SULI_MG_FUSED=0): same pressures and velocities, same iteration
+    counts.  Covers the kept wrap (even periodic length), the dropped wrap
+    (odd) and a batch of uneven grids (partial column units); the *_all_levels
+    cases smooth every level by grid launches (SULI_MG_CTA_CELLS=0), so the
+    sweeps run on the coarse levels too (odd and even periodic lengths on
+    the levels of a 44-cell grid: 44, 22, 11, 6, 3)."""
     def mk_cases():
         if mk == "periodic_even":
             return [cases.mms_case(24, precision=PREC_MIXED)]
         if mk == "periodic_odd":
             return [cases.mms_case(25, precision=PREC_MIXED)]
+        if mk == "periodic_all_levels":
+            return [cases.mms_case(44, precision=PREC_MIXED)]
         dims, hcol, amp = cases.ensemble_dims(5, seed=11, lo=13, hi=40)
         return [cases.ensemble_case(i, dims, hcol, amp, precision=PREC_MIXED) for i in range(5)]
+    if mk.endswith("all_levels"):
+        monkeypatch.setenv("SULI_MG_CTA_CELLS", "0")
     out = {}
     for fused in ("0", "1"):
         monkeypatch.setenv("SULI_MG_FUSED", fused)
