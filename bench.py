@@ -717,13 +717,13 @@ def main():
         kern = 0
     kname = {0: "k_cgi_A (CG matrix-vector product + p.Ap)",
              1: "k_mg_smooth on the case grid (one red-black half-sweep)",
-             3: "k_mg_sweep0 on the case grid (one whole red-black sweep in one pass)"}[kern]
+             3: "k_mg_sweep on the case grid (one whole red-black sweep in one pass)"}[kern]
     ms_k, bytes_k = gm.time_kernel(kern, 20)
     ach = bytes_k / (ms_k / 1e3) / 1e9
     # DRAM bytes per cell of one launch (dram__bytes_read.sum +
     # dram__bytes_write.sum over cells) from an ncu capture of the same
     # kernel on the first 24 cases of this ensemble; times this workload's cells
-    traffic_per_cell = {0: 166.6e6 / 6914626, 1: 233.2e6 / 6914626, 3: 362.5e6 / 6914626}[kern]
+    traffic_per_cell = {0: 166.6e6 / 6914626, 1: 233.2e6 / 6914626, 3: 218.0e6 / 6914626}[kern]
     line["roofline"] = {"bound": "hbm", "kernel": kname, "achieved": ach, "peak": peak, "unit": "GB/s",
                         "frac": ach / peak,
                         "traffic": traffic_per_cell * cells if traffic_per_cell is not None else None,

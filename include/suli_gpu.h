@@ -36,8 +36,10 @@ extern "C" {
 #define SULI_OK              0
 #define SULI_CG_MAXITER      1  /* warning: "pulou pressao", 9_grad.f90:590 */
 #define SULI_VOL_LOOP_CAP    2  /* volume-correction loop capped, 14_level_set.f90:243 */
-#define SULI_DEVICE_TIMEOUT  3  /* reserved for a bounded device wait that gives up; no kernel of
-                                   this library waits on a flag, so no entry point returns it */
+#define SULI_DEVICE_TIMEOUT  3  /* a bounded device wait for a TMA copy (the staged convdiff)
+                                   gave up after one second; the step's results for that case
+                                   are not valid (checked where SULI_NONFINITE is and at the
+                                   end of suli_step) */
 #define SULI_BAD_CONFIG      4  /* replaces the reference's STOPs */
 #define SULI_BAD_ARG         5
 #define SULI_CUDA_ERROR      6
@@ -316,7 +318,7 @@ int suli_time_kernel(suli_handle *h, int kernel, int reps, double *ms_per_launch
 /* Autotuner (no counterpart in the reference).  Launch shapes of the hot
  * kernels -- the planes per unit of the TMA-staged convdiff (8, 16, 32), the
  * largest multigrid level handled by the one-block coarse end of the V-cycle,
- * the blocks per SM of the one-pass level-0 smoother sweep -- are timed with
+ * the blocks per SM of the one-pass multigrid smoother sweep -- are timed with
  * CUDA events on the handle's stream and the fastest kept; every choice gives
  * the same bits (only the partition of the work changes).  suli_step tunes a
  * handle once, after its first time step (the operator and the work arrays
@@ -328,7 +330,7 @@ int suli_time_kernel(suli_handle *h, int kernel, int reps, double *ms_per_launch
 typedef struct suli_tuning {
     int32_t convdiff_planes;      /* planes per unit of the TMA-staged convdiff (0: gather kernel) */
     int32_t mg_block_cells;       /* largest level (cells) of the one-block V-cycle end; 0: none */
-    int32_t sweep_blocks_per_sm;  /* blocks per SM of the level-0 sweep; 0: occupancy limit */
+    int32_t sweep_blocks_per_sm;  /* blocks per SM of the multigrid sweep; 0: occupancy limit */
     int32_t tuned;                /* 1: chosen by timing (this handle or the cache), 0: defaults */
     double  default_ms;           /* the timed kernels at the defaults (one convdiff, one V-cycle, one sweep) */
     double  tuned_ms;             /* the same at the chosen shapes */

@@ -24,8 +24,9 @@
 // thread arms with the slot's transaction bytes; every wait is bounded, and a
 // wait that gives up marks the case (S_TMAERR, reported as
 // SULI_DEVICE_TIMEOUT) and ends the unit after the copies it issued have
-// landed or their waits have run out.
+// landed or their waits have run out (each wait gives up after a second).
 #include "conv_faces.cuh"
+#include "tma_util.cuh"
 
 namespace suli {
 
@@ -35,7 +36,6 @@ constexpr int CD_BOX = CD_BX * CD_BY;
 constexpr int CD_NARR = 8;                       // u, v, w, rho, mu, xmu, ymu, zmu
 constexpr int CD_RING = 6;                       // plane slots
 constexpr int CD_SLOT = CD_NARR * CD_BOX;        // elements of one slot
-constexpr unsigned CD_WAIT_MAX = 1u << 22;       // bounded mbarrier polls
 
 // units of a case with kz planes a unit (kz = CD_PLANES[v], the tuner's choice)
 __host__ __device__ __forceinline__ int cd_units(int nx, int ny, int nz, int kz)
@@ -44,39 +44,6 @@ __host__ __device__ __forceinline__ int cd_units(int nx, int ny, int nz, int kz)
 }
 
 template <typename T> constexpr size_t cd_smem() { return (size_t)CD_RING * CD_SLOT * sizeof(T) + 128; }
-
-__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t *b, unsigned count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(b)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_arm(uint64_t *b, unsigned bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
-}
-// bounded wait for phase `parity` of barrier b: false when it gave up
-__device__ __forceinline__ bool mbar_wait(uint64_t *b, unsigned parity)
-{
-    const unsigned a = smem_u32(b);
-    for (unsigned it = 0; it < CD_WAIT_MAX; ++it) {
-        unsigned ok;
-        asm volatile("{\n .reg .pred P;\n mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n selp.b32 %0, 1, 0, P;\n}\n"
-                     : "=r"(ok)
-                     : "r"(a), "r"(parity)
-                     : "memory");
-        if (ok) return true;
-    }
-    return false;
-}
-__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z, uint64_t *bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(
-            smem_u32(dst)),
-        "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
-        : "memory");
-}
 
 // operands from the staged planes (CHK: positions outside the staged box read
 // global memory)
@@ -151,7 +118,8 @@ __device__ __forceinline__ void cd_interior_pos(const CaseDev<T> &c, const Stage
 
 template <typename T, int CD_Z>
 __global__ void __launch_bounds__(CD_X *CD_Y, sizeof(T) == 4 ? 2 : 1)
-    k_convdiff_tma(const CaseDev<T> *__restrict__ cs, int ncases, const CUtensorMap *__restrict__ maps, int fuse, int v)
+    k_convdiff_tma(const CaseDev<T> *__restrict__ cs, int ncases, const CUtensorMap *__restrict__ maps, int fuse, int v,
+                   int shortfall)
 {
     extern __shared__ unsigned char cd_dyn[];
     __shared__ __align__(8) uint64_t bar[CD_RING];
@@ -182,10 +150,15 @@ __global__ void __launch_bounds__(CD_X *CD_Y, sizeof(T) == 4 ? 2 : 1)
     }
     __syncthreads();
     const int pl = k1 + 2;   // last plane any position of the unit reads
+    // failure-path test hook (shortfall != 0): the unit's last plane is armed
+    // with 16 bytes that no copy delivers, so its bounded wait runs out --
+    // only while the case has no timeout recorded, so one launch pays the
+    // wait and the later ones run normally
+    const bool sf = shortfall != 0 && t == 0 && __ldcg(&c.sc[S_TMAERR]) == 0.0;
     auto slot = [](int p) { return (p + CD_RING) % CD_RING; };   // p >= -1
     auto issue = [&](int p) {
         const int s = slot(p);
-        mbar_arm(&bar[s], bytes);
+        mbar_arm(&bar[s], bytes + (sf && p == pl ? 16u : 0u));
         T *dst = S + (size_t)s * CD_SLOT;
         for (int a = 0; a < CD_NARR; ++a) tma_load_3d(dst + a * CD_BOX, tm + a, X0, Y0, p, &bar[s]);
     };
@@ -306,7 +279,7 @@ template <typename T, int KZ> static void launch_tma_kz(const Batch<T> &b, int f
     cudaFuncSetAttribute((const void *)k_convdiff_tma<T, KZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)cd_smem<T>());
     k_convdiff_tma<T, KZ><<<b.total_cd_units[v], dim3(CD_X, CD_Y), cd_smem<T>(), s>>>(b.dcases, b.ncases, b.tmaps,
-                                                                                      fuse, v);
+                                                                                      fuse, v, b.test_shortfall);
 }
 
 template <typename T> void launch_convdiff_tma(const Batch<T> &b, int fuse, cudaStream_t s)

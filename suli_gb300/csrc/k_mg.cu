@@ -123,7 +123,10 @@ void launch_smooth(const Batch<T> &b, const int *tab, int l, int color, int zero
 // updates the c2 cells of the plane below from those values.  The ring cells
 // are computed by both blocks that need them, from the same inputs, so the
 // two half-sweeps need one trip through memory instead of two; the results
-// are the two half-sweep launches' (same operands, same order).
+// are the two half-sweep launches' (same operands, same order).  The units
+// are dealt to the blocks round-robin (for_active_units_rr), so a unit's x-
+// and y-neighbours are swept at the same time by other blocks and the halo
+// rows they share come from DRAM once and hit in L2 for the other.
 //
 // The inputs of a plane (z over the footprint and one more cell around it,
 // f, dg and the three conductances over the footprint) are staged in shared
@@ -162,7 +165,7 @@ __global__ void __launch_bounds__(NTHREADS, 4) k_mg_sweep(const CaseDev<T> *__re
     T *stg = reinterpret_cast<T *>(sw_dyn);
     __shared__ T ring[3][SW_N];
     const int t = tid_lin();
-    for_active_units(tab, N, l, [&](int id, int u) {
+    for_active_units_rr(tab, N, l, [&](int id, int u) {
         const CaseDev<T> &c = cs[id];
         const MgLev<T> &L = c.mg[l];
         const Geo &g = L.g;

@@ -646,20 +646,26 @@ struct Impl : ImplBase {
     // zeros.  Without the driver's encoder (or with SULI_CONVDIFF=0) the
     // gather kernel runs instead.
     CUtensorMap *dtmaps = nullptr;
+    // the driver's tensor-map encoder (null when the driver has none)
+    static PFN_cuTensorMapEncodeTiled_v12000 tensor_encoder()
+    {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult qr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &qr) !=
+                cudaSuccess || qr != cudaDriverEntryPointSuccess || !fn) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        return (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    }
     int make_tensor_maps()
     {
         const char *env = std::getenv("SULI_CONVDIFF");
         if (env && std::string(env) == "0") return SULI_OK;
         for (int c = 0; c < ncases; ++c)
             if (P[c].dz_t == 1) return SULI_OK;   // the variable-dz stencils run in the gather kernel
-        void *fn = nullptr;
-        cudaDriverEntryPointQueryResult qr;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &qr) !=
-                cudaSuccess || qr != cudaDriverEntryPointSuccess || !fn) {
-            cudaGetLastError();
-            return SULI_OK;
-        }
-        auto encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+        auto encode = tensor_encoder();
+        if (!encode) return SULI_OK;
         std::vector<CUtensorMap> maps((size_t)ncases * 8);
         for (int c = 0; c < ncases; ++c) {
             const CaseDev<T> &cd = hc[c];
@@ -681,6 +687,10 @@ struct Impl : ImplBase {
         CK(cudaMemcpyAsync(dtmaps, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice, st));
         CK(cudaStreamSynchronize(st));
         b.tmaps = dtmaps;
+        // failure-path test hook: the staged convdiff's bounded TMA waits run
+        // out once per case (reported as SULI_DEVICE_TIMEOUT)
+        const char *e = std::getenv("SULI_TEST_TMA_SHORTFALL");
+        b.test_shortfall = (e && std::atoi(e) == 1) ? 1 : 0;
         return SULI_OK;
     }
 
@@ -1498,6 +1508,12 @@ struct Impl : ImplBase {
             if ((rc = conmassa(nullptr))) return rc;
             // the autotuner, once, after the handle's first step
             if (!tuned && tune_env == 1 && (rc = autotune(nullptr))) return rc;
+        }
+        // a TMA wait that gave up in the last step (the check in level_set
+        // covers the steps before it)
+        if (n > 0) {
+            if ((rc = read_scalars())) return rc;
+            if ((rc = check_finite())) return rc;
         }
         return SULI_OK;
     }

@@ -321,10 +321,10 @@ __device__ __forceinline__ bool last_block_reduce(const CaseDev<T> &c, const dou
 // ---- active-case tables (persistent CG iteration) ---------------------------
 // A table lists the cases whose CG still iterates and, per grid level s, the
 // prefix of their work-unit counts, so a fixed grid can walk exactly the
-// active units of a level.  Level 0 is the case grid and its unit a column
-// (column_of); level s > 0 is multigrid level s and its unit a tile:
+// active units of a level.  Level 0 is the case grid, level s > 0 multigrid
+// level s; the unit is a column unit of the level (column_of):
 //   tab[0] = n, tab[1 .. 1+n) = case ids,
-//   level s at B = 1 + N + s (N + 2): tab[B] = tiles, tab[B+1 .. B+1+n] = prefix
+//   level s at B = 1 + N + s (N + 2): tab[B] = units, tab[B+1 .. B+1+n] = prefix
 // (N = cases in the batch, NL = levels in the table).
 __host__ __device__ __forceinline__ int act_stride(int ncases, int nl) { return 1 + ncases + nl * (ncases + 2); }
 __host__ __device__ __forceinline__ int act_level(int ncases, int s) { return 1 + ncases + s * (ncases + 2); }
@@ -438,6 +438,29 @@ __device__ __forceinline__ void for_active_units(const int *__restrict__ tab, in
     int end = off[a + 1];
     for (int t = lo; t < hi; ++t) {
         while (t >= end) { ++a; end = off[a + 1]; }
+        f(ids[a], t - off[a]);
+    }
+}
+
+// The active units of level s dealt round-robin: block b takes units b,
+// b + G, b + 2G, ... (G blocks), so neighbouring units run at the same time
+// on different blocks (their shared halo is read from DRAM once and hits in
+// L2 for the other).  Every thread of the block makes the same calls.
+template <typename F>
+__device__ __forceinline__ void for_active_units_rr(const int *__restrict__ tab, int N, int s, F f)
+{
+    const int n = tab[0];
+    const int *ids = tab + 1;
+    const int *lv = tab + act_level(N, s);
+    const int units = lv[0];
+    const int *off = lv + 1;
+    int a = 0;
+    for (int t = blockIdx.x; t < units; t += gridDim.x) {
+        int a1 = n - 1;              // last slot with off <= t (at or after the previous one)
+        while (a < a1) {
+            const int mid = (a + a1 + 1) >> 1;
+            if (off[mid] <= t) a = mid; else a1 = mid - 1;
+        }
         f(ids[a], t - off[a]);
     }
 }
@@ -564,18 +587,30 @@ __device__ void build_active_table(const CaseDev<T> *__restrict__ cs, int N, int
     const int t = tid_lin();
     const int per = (nin + NTHREADS - 1) / NTHREADS;
     const int a0 = min(nin, t * per), a1 = min(nin, a0 + per);
+    // the active flags of this thread's cases, read once (bit a - a0; a
+    // thread with more than 64 cases re-reads them per level)
+    const bool cached = per <= 64;
+    unsigned long long am = 0ull;
     int cnt = 0;
     for (int a = a0; a < a1; ++a) {
         const int id = in ? in[1 + a] : a;
-        if (all || __ldcg(&cs[id].sc[S_CGACTIVE]) != 0.0) ++cnt;
+        if (all || __ldcg(&cs[id].sc[S_CGACTIVE]) != 0.0) {
+            if (cached) am |= 1ull << (a - a0);
+            ++cnt;
+        }
     }
+    auto active = [&](int a, int id) {
+        return cached ? ((am >> (a - a0)) & 1ull) != 0ull : (all || __ldcg(&cs[id].sc[S_CGACTIVE]) != 0.0);
+    };
     int ncnt;
     const int pos0 = block_exscan(cnt, &ncnt);
+    // units of level s of case id
+    auto units = [&](int id, int s) { return s == 0 ? cs[id].nchunks : cs[id].mg[s].ncols; };
     for (int s = 0; s < NL; ++s) {
         int til = 0;
         for (int a = a0; a < a1; ++a) {
             const int id = in ? in[1 + a] : a;
-            if (all || __ldcg(&cs[id].sc[S_CGACTIVE]) != 0.0) til += (s == 0) ? cs[id].nchunks : cs[id].mg[s].ncols;
+            if (active(a, id)) til += units(id, s);
         }
         int ntil;
         int tpos = block_exscan(til, &ntil);
@@ -583,11 +618,11 @@ __device__ void build_active_table(const CaseDev<T> *__restrict__ cs, int N, int
         int pos = pos0;
         for (int a = a0; a < a1; ++a) {
             const int id = in ? in[1 + a] : a;
-            if (all || __ldcg(&cs[id].sc[S_CGACTIVE]) != 0.0) {
+            if (active(a, id)) {
                 if (s == 0) out[1 + pos] = id;
                 lv[1 + pos] = tpos;
                 ++pos;
-                tpos += (s == 0) ? cs[id].nchunks : cs[id].mg[s].ncols;
+                tpos += units(id, s);
             }
         }
         if (t == 0) {

@@ -29,7 +29,7 @@ constexpr int CD_PLANES[3] = {8, 16, 32};   // planes per unit of the TMA-staged
 struct Tuning {
     int cd_variant = 1;           // index into CD_PLANES
     int mg_block_cells = 16384;   // largest level (cells) of the one-block coarse end of the V-cycle; 0: none
-    int sweep_blocks_per_sm = 0;  // blocks per SM of the one-pass level-0 sweep; 0: its occupancy limit
+    int sweep_blocks_per_sm = 0;  // blocks per SM of the one-pass multigrid sweep; 0: its occupancy limit
 };
 
 // A batch of cases with a device copy of their CaseDev table.
@@ -47,6 +47,7 @@ struct Batch {
     int nlev = 1;                     // grid levels in the tables (multigrid levels, or 1)
     int mg_tiles[MG_MAXL] = {0};      // tiles of multigrid level l over all cases
     const CUtensorMap *tmaps = nullptr;   // per case the tensor maps of the convdiff operands (or null)
+    int test_shortfall = 0;           // failure-path test hook of the staged convdiff (SULI_TEST_TMA_SHORTFALL=1)
     int total_cd_units[3] = {0, 0, 0};   // units of the TMA-staged convdiff over all cases, per unit height
     Tuning tune;                      // the autotuner's launch shapes
     long long total_cd_shell = 0;     // boundary-shell positions of convdiff over all cases

@@ -1,17 +1,19 @@
-"""The failure paths of the C ABI, each made on the host and none of them a
-GPU fault: the CG iteration cap (the reference's "pulou pressao",
-9_grad.f90:393-398,590), the cap of the volume-correction loop (unbounded
-upstream, 14_level_set.f90:243), a NaN in a host buffer before upload, and
-a truncated or foreign restart file (SULI_BAD_CONFIG, the handle left as it
-was)."""
+"""The failure paths of the C ABI, none of them a GPU fault: the CG
+iteration cap (the reference's "pulou pressao", 9_grad.f90:393-398,590), the
+cap of the volume-correction loop (unbounded upstream, 14_level_set.f90:243),
+a NaN in a host buffer before upload, a truncated or foreign restart file
+(SULI_BAD_CONFIG, the handle left as it was), and a bounded device wait that
+runs out (SULI_DEVICE_TIMEOUT: a wait on an mbarrier that no copy completes,
+given up after one second)."""
 import os
+import time
 
 import numpy as np
 import pytest
 
 from suli_gb300 import cases
-from suli_gb300._abi import (PREC_FP64, PREC_MIXED, SULI_BAD_CONFIG, SULI_CG_MAXITER, SULI_NONFINITE,
-                             SULI_VOL_LOOP_CAP)
+from suli_gb300._abi import (PREC_FP64, PREC_MIXED, SULI_BAD_CONFIG, SULI_CG_MAXITER, SULI_DEVICE_TIMEOUT,
+                             SULI_NONFINITE, SULI_VOL_LOOP_CAP)
 
 pytestmark = pytest.mark.gpu
 
@@ -75,6 +77,34 @@ def test_nan_in_host_buffer_is_reported(gpu_lib, precision):
     g.step(2)
     assert np.isfinite(g.conmassa())
     g.close()
+
+
+@pytest.mark.parametrize("precision", [PREC_FP64, PREC_MIXED])
+def test_tma_wait_timeout_is_reported(gpu_lib, monkeypatch, precision):
+    """SULI_TEST_TMA_SHORTFALL=1 (read at handle creation) arms the last
+    plane of each unit of the TMA-staged convdiff with 16 bytes more than its
+    copies deliver, while the case has no timeout recorded: the bounded
+    waits run out after a second, the kernel marks the case and returns, and
+    the step reports SULI_DEVICE_TIMEOUT -- no fault, no hang.  The context
+    stays usable: a fresh handle of the same case steps, twice to the same
+    bits."""
+    monkeypatch.setenv("SULI_TEST_TMA_SHORTFALL", "1")
+    g = _start(gpu_lib, cases.dam_break(40, 16, 24, precision=precision))
+    monkeypatch.delenv("SULI_TEST_TMA_SHORTFALL")
+    t0 = time.time()
+    with pytest.raises(gpu_lib.SuliError) as ei:
+        g.step(1)
+    assert ei.value.code == SULI_DEVICE_TIMEOUT
+    assert time.time() - t0 < 120
+    g.close()
+    out = []
+    for _ in range(2):
+        g = _start(gpu_lib, cases.dam_break(40, 16, 24, precision=precision))
+        g.step(2)
+        out.append(g.download("PRD1"))
+        g.close()
+    assert np.isfinite(out[0]).all()
+    assert np.array_equal(out[0], out[1])
 
 
 def test_bad_restart_files_leave_the_handle(gpu_lib, tmp_path):
