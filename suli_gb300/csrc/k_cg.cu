@@ -352,6 +352,10 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_setup3(const CaseDev<T> *__rest
 // reduction, the block that finished last writes the cases still iterating
 // to table `out`, which the rest of the iteration and the next k_cgi_A read.
 
+// planes of a column whose loads the streaming kernels issue together (all
+// eight in FP32, four in FP64: the registers of five arrays)
+template <typename T> constexpr int CG_G = sizeof(T) == 4 ? COL_Z : COL_G;
+
 // mp = A p, partial p.mp (:411-452); the case's last unit forms
 // alpha = sc[num] / p.mp (num = S_RR for CG, S_RZ for preconditioned CG).
 // Each thread owns a column of COL_Z planes, taken COL_G planes at a time: it
@@ -435,7 +439,7 @@ __global__ void __launch_bounds__(NTHREADS, 4) k_cgi_A(const CaseDev<T> *__restr
 //   MODE 2  as 1, preconditioned: also writes the V-cycle's right-hand side
 //           D^1/2 r (beta comes from r.z, k_pcg_dot)
 template <typename T, int MODE>
-__global__ void __launch_bounds__(NTHREADS) k_cgi_B(const CaseDev<T> *__restrict__ cs, const int *__restrict__ tab,
+__global__ void __launch_bounds__(NTHREADS, 2) k_cgi_B(const CaseDev<T> *__restrict__ cs, const int *__restrict__ tab,
                                                     int *__restrict__ out, unsigned *__restrict__ done, int N, int NL)
 {
     __shared__ bool compact;
@@ -458,17 +462,27 @@ __global__ void __launch_bounds__(NTHREADS) k_cgi_B(const CaseDev<T> *__restrict
         const T *__restrict__ dpr = c.dpr;
         T *__restrict__ f0 = (MODE == 2) ? c.mg[0].f : nullptr;
         const Column cl = column_of(g, u);
-        long long q = g.at(cl.i, cl.j, cl.k0);
+        // every load of the column (planes past the top clamped to the last)
+        // before any arithmetic; 32-bit offsets (a box holds < 2^31 elements)
+        const int q0 = (int)g.at(cl.i, cl.j, cl.k0), sxy = (int)g.sxy, np = cl.k1 - cl.k0 + 1;
         T rr = T(0);
-#pragma unroll 2
-        for (int k = cl.k0; k <= cl.k1; ++k, q += g.sxy) {
-            const T en = e[q] - alpha * p[q];
-            const T rn = r[q] - alpha * mp[q];
-            const T fn = (MODE == 2) ? sqrt(dpr[q]) * rn : T(0);
-            if (cl.v) {
+        for (int t0 = 0; t0 < np; t0 += CG_G<T>) {
+            T ev[CG_G<T>], pv[CG_G<T>], rv[CG_G<T>], mv[CG_G<T>], dv[CG_G<T>];
+#pragma unroll
+            for (int t = 0; t < CG_G<T>; ++t) {
+                const int q = q0 + min(t0 + t, np - 1) * sxy;
+                ev[t] = e[q]; pv[t] = p[q]; rv[t] = r[q]; mv[t] = mp[q];
+                if (MODE == 2) dv[t] = dpr[q];
+            }
+#pragma unroll
+            for (int t = 0; t < CG_G<T>; ++t) {
+                if (t0 + t >= np || !cl.v) continue;
+                const int q = q0 + (t0 + t) * sxy;
+                const T en = ev[t] - alpha * pv[t];
+                const T rn = rv[t] - alpha * mv[t];
                 e[q] = en;
                 r[q] = rn;
-                if (MODE == 2) f0[q] = fn;
+                if (MODE == 2) f0[q] = sqrt(dv[t]) * rn;
                 rr += rn * rn;
             }
         }
@@ -520,9 +534,18 @@ __global__ void __launch_bounds__(NTHREADS) k_cgi_C(const CaseDev<T> *__restrict
         T *__restrict__ p = c.p;
         const Column cl = column_of(g, u);
         if (!cl.v) return;
-        long long q = g.at(cl.i, cl.j, cl.k0);
-#pragma unroll 4
-        for (int k = cl.k0; k <= cl.k1; ++k, q += g.sxy) p[q] = r[q] + beta * p[q];
+        const int q0 = (int)g.at(cl.i, cl.j, cl.k0), sxy = (int)g.sxy, np = cl.k1 - cl.k0 + 1;
+        for (int t0 = 0; t0 < np; t0 += CG_G<T>) {
+            T rv[CG_G<T>], pv[CG_G<T>];
+#pragma unroll
+            for (int t = 0; t < CG_G<T>; ++t) {
+                const int q = q0 + min(t0 + t, np - 1) * sxy;
+                rv[t] = r[q]; pv[t] = p[q];
+            }
+#pragma unroll
+            for (int t = 0; t < CG_G<T>; ++t)
+                if (t0 + t < np) p[q0 + (t0 + t) * sxy] = rv[t] + beta * pv[t];
+        }
     });
 }
 
@@ -539,12 +562,20 @@ __global__ void __launch_bounds__(NTHREADS) k_pcg_dot(const CaseDev<T> *__restri
         const T *__restrict__ z0 = c.mg[0].z;
         const T *__restrict__ r = c.r;
         const Column cl = column_of(g, u);
-        long long q = g.at(cl.i, cl.j, cl.k0);
+        const int q0 = (int)g.at(cl.i, cl.j, cl.k0), sxy = (int)g.sxy, np = cl.k1 - cl.k0 + 1;
         T rz = T(0);
-#pragma unroll 4
-        for (int k = cl.k0; k <= cl.k1; ++k, q += g.sxy) {
-            const T z = sqrt(dpr[q]) * z0[q];
-            if (cl.v) rz += z * r[q];
+        for (int t0 = 0; t0 < np; t0 += CG_G<T>) {
+            T dv[CG_G<T>], zv[CG_G<T>], rv[CG_G<T>];
+#pragma unroll
+            for (int t = 0; t < CG_G<T>; ++t) {
+                const int q = q0 + min(t0 + t, np - 1) * sxy;
+                dv[t] = dpr[q]; zv[t] = z0[q]; rv[t] = r[q];
+            }
+#pragma unroll
+            for (int t = 0; t < CG_G<T>; ++t) {
+                const T z = sqrt(dv[t]) * zv[t];
+                if (t0 + t < np && cl.v) rz += z * rv[t];
+            }
         }
         double vals[1] = {(double)rz};
         unit_partial<T, 1>(c, u, vals);
@@ -572,9 +603,18 @@ __global__ void __launch_bounds__(NTHREADS) k_pcg_C(const CaseDev<T> *__restrict
         T *__restrict__ p = c.p;
         const Column cl = column_of(g, u);
         if (!cl.v) return;
-        long long q = g.at(cl.i, cl.j, cl.k0);
-#pragma unroll 4
-        for (int k = cl.k0; k <= cl.k1; ++k, q += g.sxy) p[q] = sqrt(dpr[q]) * z0[q] + beta * p[q];
+        const int q0 = (int)g.at(cl.i, cl.j, cl.k0), sxy = (int)g.sxy, np = cl.k1 - cl.k0 + 1;
+        for (int t0 = 0; t0 < np; t0 += CG_G<T>) {
+            T dv[CG_G<T>], zv[CG_G<T>], pv[CG_G<T>];
+#pragma unroll
+            for (int t = 0; t < CG_G<T>; ++t) {
+                const int q = q0 + min(t0 + t, np - 1) * sxy;
+                dv[t] = dpr[q]; zv[t] = z0[q]; pv[t] = p[q];
+            }
+#pragma unroll
+            for (int t = 0; t < CG_G<T>; ++t)
+                if (t0 + t < np) p[q0 + (t0 + t) * sxy] = sqrt(dv[t]) * zv[t] + beta * pv[t];
+        }
     });
 }
 

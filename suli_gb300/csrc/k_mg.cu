@@ -414,10 +414,23 @@ __global__ void __launch_bounds__(NTHREADS) k_mg_prolong(const CaseDev<T> *__res
         const MgLev<T> &C = c.mg[l + 1];
         const Column cl = column_of(F.g, u);
         if (!cl.v) return;
-        T *out = to2 ? F.z2 : F.z;
-        long long q = F.g.at(cl.i, cl.j, cl.k0);
-        for (int k = cl.k0; k <= cl.k1; ++k, q += F.g.sxy)
-            out[q] = F.z[q] + C.z[C.g.at((cl.i + 1) >> 1, (cl.j + 1) >> 1, (k + 1) >> 1)];
+        T *__restrict__ out = to2 ? F.z2 : F.z;
+        const T *__restrict__ zf = F.z;
+        const T *__restrict__ zc = C.z;
+        // every load of the column before any store (planes past the top
+        // clamped to the last); 32-bit offsets
+        const int q0 = (int)F.g.at(cl.i, cl.j, cl.k0), sxy = (int)F.g.sxy, np = cl.k1 - cl.k0 + 1;
+        const int c0 = (int)C.g.at((cl.i + 1) >> 1, (cl.j + 1) >> 1, 0), csxy = (int)C.g.sxy;
+        T fv[COL_Z], cv[COL_Z];
+#pragma unroll
+        for (int t = 0; t < COL_Z; ++t) {
+            const int k = cl.k0 + min(t, np - 1);
+            fv[t] = zf[q0 + min(t, np - 1) * sxy];
+            cv[t] = zc[c0 + ((k + 1) >> 1) * csxy];
+        }
+#pragma unroll
+        for (int t = 0; t < COL_Z; ++t)
+            if (t < np) out[q0 + t * sxy] = fv[t] + cv[t];
     });
 }
 
