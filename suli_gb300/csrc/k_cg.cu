@@ -358,14 +358,14 @@ template <typename T> constexpr int CG_G = sizeof(T) == 4 ? COL_Z : COL_G;
 
 // mp = A p, partial p.mp (:411-452); the case's last unit forms
 // alpha = sc[num] / p.mp (num = S_RR for CG, S_RZ for preconditioned CG).
-// Each thread owns a column of COL_Z planes, taken COL_G planes at a time: it
+// Each thread owns a column of COL_Z planes, taken CG_G planes at a time: it
 // issues every load of a group (the COL_G + 2 planes of p, the COL_G + 1
 // z-face coefficients and the x/y neighbours and coefficients of each plane)
 // before any arithmetic, then forms the products; wall and periodic
 // neighbours are fixed index offsets and planes past the top are predicated
 // off, so nothing branches.
 template <typename T>
-__global__ void __launch_bounds__(NTHREADS, 4) k_cgi_A(const CaseDev<T> *__restrict__ cs, const int *__restrict__ tab,
+__global__ void __launch_bounds__(NTHREADS, 2) k_cgi_A(const CaseDev<T> *__restrict__ cs, const int *__restrict__ tab,
                                                        int N, int num)
 {
     for_active_units_seg(tab, N, 0, [&](int id, int u) {
@@ -389,21 +389,21 @@ __global__ void __launch_bounds__(NTHREADS, 4) k_cgi_A(const CaseDev<T> *__restr
         // the mixed form: the FP64 units of GB300 are a small fraction of its
         // FP32 rate), the block tree and the case total in FP64
         T pm = T(0);
-        for (int kb = cl.k0; kb <= cl.k1; kb += COL_G) {
+        for (int kb = cl.k0; kb <= cl.k1; kb += CG_G<T>) {
             const int q0 = (int)g.at(cl.i, cl.j, kb);
-            const int np = min(COL_G, cl.k1 - kb + 1);
-            T pz[COL_G + 2], sk[COL_G + 1];
-            T vxp[COL_G], cxp[COL_G], vxm[COL_G], cxm[COL_G], vyp[COL_G], cyp[COL_G], vym[COL_G], cym[COL_G];
+            const int np = min(CG_G<T>, cl.k1 - kb + 1);
+            T pz[CG_G<T> + 2], sk[CG_G<T> + 1];
+            T vxp[CG_G<T>], cxp[CG_G<T>], vxm[CG_G<T>], cxm[CG_G<T>], vyp[CG_G<T>], cyp[CG_G<T>], vym[CG_G<T>], cym[CG_G<T>];
 #pragma unroll
-            for (int t = 0; t < COL_G + 2; ++t) {
+            for (int t = 0; t < CG_G<T> + 2; ++t) {
                 // plane kb-1+t, the Neumann copy at the bottom and top walls
                 const int k = min(max(kb - 1 + t, 1), nz);
                 pz[t] = p[q0 + (k - kb) * sxy];
             }
 #pragma unroll
-            for (int t = 0; t < COL_G + 1; ++t) sk[t] = spk[q0 + min(t, np) * sxy];
+            for (int t = 0; t < CG_G<T> + 1; ++t) sk[t] = spk[q0 + min(t, np) * sxy];
 #pragma unroll
-            for (int t = 0; t < COL_G; ++t) {
+            for (int t = 0; t < CG_G<T>; ++t) {
                 const int q = q0 + min(t, np - 1) * sxy;
                 vxp[t] = p[q + dxp]; cxp[t] = spi[q + 1];
                 vxm[t] = p[q + dxm]; cxm[t] = spi[q];
@@ -411,7 +411,7 @@ __global__ void __launch_bounds__(NTHREADS, 4) k_cgi_A(const CaseDev<T> *__restr
                 vym[t] = p[q + dym]; cym[t] = spj[q];
             }
 #pragma unroll
-            for (int t = 0; t < COL_G; ++t) {
+            for (int t = 0; t < CG_G<T>; ++t) {
                 if (t >= np || !cl.v) continue;
                 const T pc = pz[t + 1];
                 // the reference's order of operations (9_grad.f90:411-452)
@@ -421,8 +421,7 @@ __global__ void __launch_bounds__(NTHREADS, 4) k_cgi_A(const CaseDev<T> *__restr
                 pm += pc * m;
             }
         }
-        double vals[1] = {(double)pm};
-        unit_partial<T, 1>(c, u, vals);
+        unit_partial1<T>(c, u, pm);
     }, [&](int id, int cnt) {
         const CaseDev<T> &c = cs[id];
         double tot[1];
@@ -486,8 +485,7 @@ __global__ void __launch_bounds__(NTHREADS, 2) k_cgi_B(const CaseDev<T> *__restr
                 rr += rn * rn;
             }
         }
-        double vals[1] = {(double)rr};
-        unit_partial<T, 1>(c, u, vals);
+        unit_partial1<T>(c, u, rr);
     }, [&](int id, int cnt) {
         const CaseDev<T> &c = cs[id];
         double tot[1];
@@ -577,8 +575,7 @@ __global__ void __launch_bounds__(NTHREADS) k_pcg_dot(const CaseDev<T> *__restri
                 if (t0 + t < np && cl.v) rz += z * rv[t];
             }
         }
-        double vals[1] = {(double)rz};
-        unit_partial<T, 1>(c, u, vals);
+        unit_partial1<T>(c, u, rz);
     }, [&](int id, int cnt) {
         const CaseDev<T> &c = cs[id];
         double tot[1];
@@ -735,7 +732,7 @@ __device__ void true_residual_update(const CaseDev<T> &c, int first, double rrt,
 // solve's first residual, with the right-hand side's r.r for the relative
 // tolerance; later passes skip the cases that have converged.
 template <typename T, int first>
-__global__ void __launch_bounds__(NTHREADS, 3) k_cg_true_residual_cols(const CaseDev<T> *__restrict__ cs, int ncases,
+__global__ void __launch_bounds__(NTHREADS, 2) k_cg_true_residual_cols(const CaseDev<T> *__restrict__ cs, int ncases,
                                                                         int nunits)
 {
     for (int gu = blockIdx.x; gu < nunits; gu += gridDim.x) {
@@ -758,29 +755,61 @@ __global__ void __launch_bounds__(NTHREADS, 3) k_cg_true_residual_cols(const Cas
         const long long mxm = px ? (long long)(nx - 1) : 0, mxp = px ? -(long long)(nx - 1) : 0;
         const long long mym = py ? (long long)(ny - 1) * sx : 0, myp = py ? -(long long)(ny - 1) * sx : 0;
         const double *__restrict__ e = c.e64;
-        double rr = 0.0, rr32 = 0.0, bb = 0.0;
+        const double *__restrict__ spi = c.spi64;
+        const double *__restrict__ spj = c.spj64;
+        const double *__restrict__ spk = c.spk64;
+        const double *__restrict__ qpr = c.qpr64;
+        const T *__restrict__ dpr = c.dpr;
+        T *__restrict__ f0 = c.nlev > 0 ? c.mg[0].f : nullptr;
+        // the residual's norm from its FP32 rounding, summed per thread in
+        // FP32 (a relative 1e-7 on a stopping test; the FP64 pipe is a small
+        // fraction of GB300's FP32 rate); the first pass's |b|^2 in FP64
+        T rrf = T(0);
+        double bb = 0.0;
         if (cl.v) {
-            long long q = g.at(i, j, cl.k0);
-            for (int k = cl.k0; k <= cl.k1; ++k, q += sxy) {
-                const bool bzm = k == 1, bzp = k == nz;
-                const double exm = e[bxm ? q + mxm : q - 1];
-                const double exp_ = e[bxp ? q + mxp : q + 1];
-                const double eym = e[bym ? q + mym : q - sx];
-                const double eyp = e[byp ? q + myp : q + sx];
-                const double ezm = e[bzm ? q : q - sxy];
-                const double ezp = e[bzp ? q : q + sxy];
-                const double r = e[q] - c.spi64[q + 1] * exp_ - c.spi64[q] * exm - c.spj64[q + sx] * eyp -
-                                 c.spj64[q] * eym - c.spk64[q + sxy] * ezp - c.spk64[q] * ezm - c.qpr64[q];
-                const T r32 = T(r);
-                c.r[q] = r32;
-                c.p[q] = r32;
-                c.e[q] = T(0.);
-                if (c.nlev > 0) c.mg[0].f[q] = sqrt(c.dpr[q]) * r32;   // V-cycle right-hand side D^1/2 r
-                rr += r * r;
-                rr32 += (double)r32 * (double)r32;
-                if constexpr (first != 0) bb += c.qpr64[q] * c.qpr64[q];
+            // COL_G planes at a time, every load of a group before any
+            // arithmetic; the z-neighbours of the group's planes are the
+            // column's planes around it, clamped to the grid (a Neumann wall:
+            // the cell itself); 32-bit offsets (a box holds < 2^31 elements)
+            const int q0 = (int)g.at(i, j, cl.k0), isx = (int)sx, isxy = (int)sxy, np = cl.k1 - cl.k0 + 1;
+            const int dxm = bxm ? (int)mxm : -1, dxp = bxp ? (int)mxp : 1;
+            const int dym = bym ? (int)mym : -isx, dyp = byp ? (int)myp : isx;
+            for (int kb = 0; kb < np; kb += COL_G) {
+                double ec[COL_G + 2], sk[COL_G + 1], exm[COL_G], exq[COL_G], eym[COL_G], eyq[COL_G];
+                double sxa[COL_G], sxb[COL_G], sya[COL_G], syb[COL_G], qp[COL_G];
+                T dv[COL_G];
+#pragma unroll
+                for (int t = 0; t < COL_G + 2; ++t) {
+                    const int k = min(max(cl.k0 + kb - 1 + t, 1), nz);
+                    ec[t] = e[q0 + (k - cl.k0) * isxy];
+                }
+#pragma unroll
+                for (int t = 0; t < COL_G + 1; ++t) sk[t] = spk[q0 + min(kb + t, np) * isxy];
+#pragma unroll
+                for (int t = 0; t < COL_G; ++t) {
+                    const int q = q0 + min(kb + t, np - 1) * isxy;
+                    exm[t] = e[q + dxm]; exq[t] = e[q + dxp]; eym[t] = e[q + dym]; eyq[t] = e[q + dyp];
+                    sxa[t] = spi[q + 1]; sxb[t] = spi[q]; sya[t] = spj[q + isx]; syb[t] = spj[q];
+                    qp[t] = qpr[q];
+                    dv[t] = f0 ? dpr[q] : T(0);
+                }
+#pragma unroll
+                for (int t = 0; t < COL_G; ++t) {
+                    if (kb + t >= np) continue;
+                    const int q = q0 + (kb + t) * isxy;
+                    const double r = ec[t + 1] - sxa[t] * exq[t] - sxb[t] * exm[t] - sya[t] * eyq[t] - syb[t] * eym[t] -
+                                     sk[t + 1] * ec[t + 2] - sk[t] * ec[t] - qp[t];
+                    const T r32 = T(r);
+                    c.r[q] = r32;
+                    c.p[q] = r32;
+                    c.e[q] = T(0.);
+                    if (f0) f0[q] = sqrt(dv[t]) * r32;   // V-cycle right-hand side D^1/2 r
+                    rrf += r32 * r32;
+                    if constexpr (first != 0) bb += qp[t] * qp[t];
+                }
             }
         }
+        const double rr = (double)rrf, rr32 = rr;
         if constexpr (first != 0) {
             double vals[3] = {rr, rr32, bb}, tot[3];
             if (unit_reduce<T, 3>(c, gu, c.chunk_begin, c.nchunks, vals, tot) && tid_lin() == 0)

@@ -354,10 +354,15 @@ __global__ void __launch_bounds__(NTHREADS) k_heaviside_vol(const CaseDev<T> *__
         if (c.rho64) {
             // mixed form: Heaviside of the FP64 level-set master in FP64, for
             // the density of the FP64 pressure operator and the volume integral
+            // (l / ad by the reciprocal: no FP64 divide, a long sequence on
+            // GB300's FP64 units)
             double l64 = lm, ad64 = c.alpha1 * c.dx1, h64;
             if (l64 < -ad64) h64 = 0.;
             else if (l64 > ad64) h64 = 1.;
-            else h64 = 0.5 * (1. + l64 / ad64 + 1. / c.pi * sin(c.pi * l64 / ad64));
+            else {
+                const double la = l64 * rcp_nr64(ad64);
+                h64 = 0.5 * (1. + la + 1. / c.pi * sin(c.pi * la));
+            }
             c.rho64[q] = c.rho_f1 * (1. - h64) + c.rho_f2 * h64;
             hv = h64;
         }

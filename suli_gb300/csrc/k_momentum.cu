@@ -267,32 +267,37 @@ template <typename T>
 __device__ __forceinline__ void tempo_one_m(const CaseDev<T> &c, int tt, int it, double dt, long long q, T *u,
                                             double *um, const T *F, T *u0, double *u0m, T *f0, T *f1)
 {
+    // the increment of the scheme from the FP32 tendencies in FP32 (dt F is
+    // small against u: its FP32 rounding is far below the master's), added
+    // to the FP64 master: one widening, one FP64 add and one rounding per
+    // component on GB300's FP64 pipe
     const int tte = c.t_tempo;
-    const double Fv = (double)F[q];
+    const T Fv = F[q];
+    const T dtf = T(dt);
     double x = um[q];
     if ((tte == 0) || ((tte == 3) || ((tte == 4) && (it == 1)))) {
-        x = x + dt * Fv;
-        if (tte == 3 || tte == 4) f0[q] = F[q];
+        x = x + (double)(dtf * Fv);
+        if (tte == 3 || tte == 4) f0[q] = Fv;
     } else if (tte == 1) {
-        if (tt == 1) { u0m[q] = x; u0[q] = T(x); x = x + dt * Fv; }
-        else if (tt == 2) { x = u0m[q] + dt * Fv; }
+        if (tt == 1) { u0m[q] = x; u0[q] = T(x); x = x + (double)(dtf * Fv); }
+        else if (tt == 2) { x = u0m[q] + (double)(dtf * Fv); }
     } else if (tte == 2) {
         if (tt == 1) {
-            u0m[q] = x; u0[q] = T(x); f0[q] = F[q]; x = x + dt * Fv;
+            u0m[q] = x; u0[q] = T(x); f0[q] = Fv; x = x + (double)(dtf * Fv);
         } else if (tt == 2) {
-            f1[q] = F[q];
-            x = u0m[q] - dt * (double)f0[q] + (2. * dt) * Fv;
+            f1[q] = Fv;
+            x = u0m[q] + (double)(dtf * (T(2) * Fv - f0[q]));
         } else if (tt == 3) {
-            x = u0m[q] + (dt / 6.) * ((double)f0[q] + 4. * (double)f1[q] + Fv);
+            x = u0m[q] + (double)(T(dt / 6.) * (f0[q] + T(4) * f1[q] + Fv));
         }
     } else if (((tte == 3) && (it != 1)) || ((tte == 4) && (it == 2))) {
-        x = x + dt * 0.5 * (3. * Fv - (double)f0[q]);
-        f0[q] = F[q];
+        x = x + (double)(T(dt * 0.5) * (T(3) * Fv - f0[q]));
+        f0[q] = Fv;
         if (tte == 4) f1[q] = f0[q];
     } else if ((tte == 4) && (it >= 3)) {
-        x = x + (dt / 12.) * (23. * Fv - 16. * (double)f0[q] + 5. * (double)f1[q]);
+        x = x + (double)(T(dt / 12.) * (T(23) * Fv - T(16) * f0[q] + T(5) * f1[q]));
         f1[q] = f0[q];
-        f0[q] = F[q];
+        f0[q] = Fv;
     }
     um[q] = x;
     u[q] = T(x);

@@ -516,6 +516,24 @@ __device__ __forceinline__ void unit_partial(const CaseDev<T> &c, int u, const d
     }
 }
 
+// one partial of a unit from a thread value in the storage type: in FP32 the
+// warp sums in FP32 (a fixed shuffle order) and lane 0 widens the warp's sum
+// to the FP64 partial, so the FP64 pipe (a small fraction of GB300's FP32
+// rate) sees one conversion per warp; in FP64 as unit_partial
+template <typename T>
+__device__ __forceinline__ void unit_partial1(const CaseDev<T> &c, int u, T v)
+{
+    if constexpr (sizeof(T) == 4) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        const int t = tid_lin();
+        if ((t & 31) == 0) c.partials[(long long)(c.chunk_begin + u) * UNIT_WARPS + (t >> 5)] = (double)v;
+    } else {
+        const double vals[1] = {(double)v};
+        unit_partial<T, 1>(c, u, vals);
+    }
+}
+
 // end of a segment of `cnt` units of case c: returns true in every thread of
 // the block that completes the case's last unit, with the totals over the
 // case's warp partials (summed in (unit, warp) order) in tot
