@@ -35,7 +35,10 @@ __device__ __forceinline__ T weno5(T v0, T v1, T v2, T v3, T v4)
     T q2 = (aux6 + is2) * (aux6 + is2);
     T q3 = (aux6 + is3) * (aux6 + is3);
     T w1 = T(0.1) * (q2 * q3), w2 = T(0.6) * (q1 * q3), w3 = T(0.3) * (q1 * q2);
-    T inv = T(1.) / (w1 + w2 + w3);
+    // the correctly rounded reciprocal (the value of 1 / x)
+    T inv;
+    if constexpr (sizeof(T) == 4) inv = __frcp_rn(w1 + w2 + w3);
+    else inv = T(1.) / (w1 + w2 + w3);
     return aux3 * inv * (w1 * (2 * v0 - 7 * v1 + 11 * v2) + w2 * (-v1 + 5 * v2 + 2 * v3) +
                          w3 * (2 * v2 + 5 * v3 - v4));
 }

@@ -357,7 +357,7 @@ template <typename T> int sweep_grid(const Batch<T> &b)
 // summing the residuals of its children; one column unit of level l per
 // unit of work (each thread a column of up to COL_Z coarse cells)
 template <typename T>
-__global__ void __launch_bounds__(NTHREADS) k_mg_restrict(const CaseDev<T> *__restrict__ cs,
+__global__ void __launch_bounds__(NTHREADS, 2) k_mg_restrict(const CaseDev<T> *__restrict__ cs,
                                                           const int *__restrict__ tab, int N, int l)
 {
     for_active_units(tab, N, l, [&](int id, int u) {

@@ -337,6 +337,7 @@ struct Impl : ImplBase {
             if (gx) cudaGraphExecDestroy(gx);
         cudaFree(drk);
         cudaFree(dtmaps);
+        cudaFree(dtilecase);
         cudaFree(b.dcases);
         if (hsc) cudaFreeHost(hsc);
         cudaFree(out_dev);
@@ -620,6 +621,17 @@ struct Impl : ImplBase {
             hc[c].counter = dcnt + c;
             hc[c].total_tiles = tiles;
         }
+        // the case of every tile of the launch grid (one load instead of a
+        // search per block)
+        {
+            std::vector<int> tc((size_t)tiles);
+            for (int c = 0; c < n; ++c)
+                for (int t = 0; t < hc[c].ntiles; ++t) tc[(size_t)hc[c].tile_begin + t] = c;
+            CK(cudaMalloc(&dtilecase, sizeof(int) * (size_t)std::max(tiles, 1)));
+            CK(cudaMemcpyAsync(dtilecase, tc.data(), sizeof(int) * tc.size(), cudaMemcpyHostToDevice, st));
+            CK(cudaStreamSynchronize(st));
+            for (int c = 0; c < n; ++c) hc[c].tile_case = dtilecase;
+        }
         CK(cudaMalloc(&b.dcases, sizeof(CaseDev<T>) * n));
         CK(cudaMemcpyAsync(b.dcases, hc.data(), sizeof(CaseDev<T>) * n, cudaMemcpyHostToDevice, st));
         b.hcases = hc.data();
@@ -646,6 +658,7 @@ struct Impl : ImplBase {
     // zeros.  Without the driver's encoder (or with SULI_CONVDIFF=0) the
     // gather kernel runs instead.
     CUtensorMap *dtmaps = nullptr;
+    int *dtilecase = nullptr;
     // the driver's tensor-map encoder (null when the driver has none)
     static PFN_cuTensorMapEncodeTiled_v12000 tensor_encoder()
     {

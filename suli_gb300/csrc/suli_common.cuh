@@ -118,6 +118,7 @@ struct CaseDev {
     Geo g;
     // tiles of this case in the launch grid
     int tile_begin, ntiles, ntx, nty, ntz;
+    const int *tile_case;       // case of each tile of the launch grid (the same table in every case)
     // column units of the case grid (the unit of the persistent CG kernels
     // and of their reductions), see col_units
     int chunk_begin, nchunks;
@@ -202,6 +203,7 @@ struct CaseDev {
 template <typename T>
 __device__ __forceinline__ int find_case(const CaseDev<T> *cs, int ncases)
 {
+    if (const int *tc = cs[0].tile_case) return tc[blockIdx.x];
     int b = blockIdx.x;
     int lo = 0, hi = ncases - 1;
     while (lo < hi) {
