@@ -147,7 +147,7 @@ __device__ __forceinline__ T face_fu(const CaseDev<T> &c, const A &X, int i, int
 {
     const int nx = c.g.nx, ny = c.g.ny, nz = c.g.nz;
     // reciprocal spacings (1.0 / dx from the host); VZ: 1 / dz(k) of u's own k
-    const T dx = T(c.idx), dy = T(c.idy), dz = VZ ? T(c.idzk[k]) : T(c.idz);
+    const T dx = cval<T>(c.idx, c.fidx), dy = cval<T>(c.idy, c.fidy), dz = VZ ? T(c.idzk[k]) : cval<T>(c.idz, c.fidz);
     const bool px = (c.ccx0 == 0);
     auto U = [&](int a, int b, int cc) { return X.u(a, b, cc); };
     T bma = interp_cf<T, IN>(i, nx, px, [&](int m) { return (X.v(m, j, k) + X.v(m, j + 1, k)) * T(0.5); });
@@ -193,7 +193,7 @@ template <typename T, typename A, bool IN = false, bool VZ = false>
 __device__ __forceinline__ T face_fv(const CaseDev<T> &c, const A &X, int i, int j, int k)
 {
     const int nx = c.g.nx, ny = c.g.ny, nz = c.g.nz;
-    const T dx = T(c.idx), dy = T(c.idy), dz = VZ ? T(c.idzk[k]) : T(c.idz);
+    const T dx = cval<T>(c.idx, c.fidx), dy = cval<T>(c.idy, c.fidy), dz = VZ ? T(c.idzk[k]) : cval<T>(c.idz, c.fidz);
     const bool px = (c.ccx0 == 0);
     auto V = [&](int a, int b, int cc) { return X.v(a, b, cc); };
     T amb = interp_cf<T, IN>(j, ny, false, [&](int m) { return (X.u(i, m, k) + X.u(i + 1, m, k)) * T(0.5); });
@@ -238,7 +238,7 @@ __device__ __forceinline__ T face_fw(const CaseDev<T> &c, const A &X, int i, int
 {
     const int nx = c.g.nx, ny = c.g.ny, nz = c.g.nz;
     // VZ: the z differences of u, v over dz(k), those of w over dzz(k)
-    const T dx = T(c.idx), dy = T(c.idy), dz = VZ ? T(c.idzk[k]) : T(c.idz);
+    const T dx = cval<T>(c.idx, c.fidx), dy = cval<T>(c.idy, c.fidy), dz = VZ ? T(c.idzk[k]) : cval<T>(c.idz, c.fidz);
     const T dzw = VZ ? T(c.idzzk[k]) : dz;
     const bool px = (c.ccx0 == 0);
     auto W = [&](int a, int b, int cc) { return X.w(a, b, cc); };

@@ -126,9 +126,9 @@ __device__ __forceinline__ void der_weno_at(const CaseDev<T> &c, const T *__rest
     const Geo &g = c.g;
     T L[7];
     load_line<T>(a, g.at(0, j, k), 1, i, n0, c.ccx0 == 0 ? 0 : 2, L);
-    weno_pm<T>(L, T(c.idx), xp, xm);
+    weno_pm<T>(L, cval<T>(c.idx, c.fidx), xp, xm);
     load_line<T>(a, g.at(i, 0, k), g.sx, j, n1, c.ccy0 == 0 ? 0 : 2, L);
-    weno_pm<T>(L, T(c.idy), yp, ym);
+    weno_pm<T>(L, cval<T>(c.idy, c.fidy), yp, ym);
     load_line<T>(a, g.at(i, j, 0), g.sxy, k, n2, 2, L);
     if (c.dz11 != nullptr) {
         // SuLi-ICdz's wenoz: the differences over the extrapolated spacing,
@@ -141,7 +141,7 @@ __device__ __forceinline__ void der_weno_at(const CaseDev<T> &c, const T *__rest
         zm = weno5<T>(D[0], D[1], D[2], D[3], D[4]);
         return;
     }
-    weno_pm<T>(L, T(c.idz), zp, zm);
+    weno_pm<T>(L, cval<T>(c.idz, c.fidz), zp, zm);
 }
 template <typename T>
 __device__ __forceinline__ void der_weno_at(const CaseDev<T> &c, const T *__restrict__ a, int i, int j, int k,
@@ -484,13 +484,13 @@ __global__ void __launch_bounds__(NTHREADS) k_ls_curv(const CaseDev<T> *__restri
     if (i > g.nx || j > g.ny || k > g.nz) return;
     T L[7], p, n;
     load_line<T>(c.nlx, g.at(0, j, k), 1, i, g.nx, 1, L);
-    weno_pm<T>(L, T(c.idx), p, n);
+    weno_pm<T>(L, cval<T>(c.idx, c.fidx), p, n);
     const T ddx = (fabs(n) > fabs(p)) ? n : p;
     load_line<T>(c.nly, g.at(i, 0, k), g.sx, j, g.ny, 1, L);
-    weno_pm<T>(L, T(c.idy), p, n);
+    weno_pm<T>(L, cval<T>(c.idy, c.fidy), p, n);
     const T ddy = (fabs(n) > fabs(p)) ? n : p;
     load_line<T>(c.nlz, g.at(i, j, 0), g.sxy, k, g.nz, 1, L);
-    weno_pm<T>(L, T(c.idz), p, n);
+    weno_pm<T>(L, cval<T>(c.idz, c.fidz), p, n);
     const T ddz = (fabs(n) > fabs(p)) ? n : p;
     c.kurv[g.at(i, j, k)] = ddx + ddy + ddz;
 }

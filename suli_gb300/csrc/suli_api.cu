@@ -446,6 +446,7 @@ struct Impl : ImplBase {
             cd.dt1 = 0.1 * cd.dx1;
             cd.deltai = std::pow(q.dx * q.dy * cd.dz, 1. / 3.);
             cd.idx = 1.0 / q.dx; cd.idy = 1.0 / q.dy; cd.idz = 1.0 / cd.dz;
+            cd.fidx = (float)cd.idx; cd.fidy = (float)cd.idy; cd.fidz = (float)cd.idz;
             cd.alpha1 = q.alpha1;
             cd.rho_f1 = q.rho_f1; cd.mu_f1 = q.mu_f1; cd.rho_f2 = q.rho_f2; cd.mu_f2 = q.mu_f2;
             cd.gx = q.gx; cd.gz = q.gz;

@@ -129,6 +129,9 @@ struct CaseDev {
     // discretisation / physics (double in both forms)
     double dx, dy, dz, dx1, dt1, deltai;
     double idx, idy, idz;       // 1/dx, 1/dy, 1/dz (mixed-form kernels multiply)
+    // FP32 roundings of idx, idy, idz for the FP32 kernels (a conversion per
+    // thread runs on GB300's FP64 pipe)
+    float fidx, fidy, fidz;
     double alpha1, rho_f1, mu_f1, rho_f2, mu_f2, gx, gz;
     double sigma;               // surface tension coefficient (t_tens = 1)
     double cles;         // (dx*dy*dz)^(2/3) * csmag * csmag
@@ -200,6 +203,14 @@ struct CaseDev {
 };
 
 // ---- tile decode ---------------------------------------------------------
+// a per-case constant in the kernel's precision: the stored FP32 rounding
+// in FP32, the FP64 value in FP64
+template <typename T> __device__ __forceinline__ T cval(double d, float f)
+{
+    if constexpr (sizeof(T) == 4) return f;
+    else return d;
+}
+
 template <typename T>
 __device__ __forceinline__ int find_case(const CaseDev<T> *cs, int ncases)
 {
