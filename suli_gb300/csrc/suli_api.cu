@@ -321,11 +321,276 @@ struct Impl : ImplBase {
         }
         return slot;
     }
+    // ---- the whole time step as one CUDA graph -------------------------------
+    // Mixed form with multigrid passes (the ensemble's configuration): the
+    // loops the host drove by reading scalars -- the volume correction, the
+    // FP64 refinement passes of each graddin and the FP32 iterations inside
+    // a pass -- are conditional WHILE nodes whose conditions k_loop_cond sets
+    // from the same scalars (every loop also capped on the device); the
+    // straight-line stretches between them are captured launches.  Built
+    // once per handle, after the autotuner, and replayed every step: one
+    // launch and one host read per step.  SULI_STEP_GRAPH=0 keeps the host-
+    // driven step; configurations whose launches carry per-step host values
+    // (waves and the inflow take the time or a call count, the AB schemes
+    // the step number, replayed counts, the manufactured solution) keep it
+    // too.  Iterations past a case's convergence are no-ops (it has left the
+    // active tables), so both paths give the same bits.
+    cudaGraphExec_t step_exec = nullptr;
+    int step_graph_state = 0;      // 0 not built, 1 built, -1 not used by this handle
+    unsigned long long sg_static = 0, sg_vol = 0, sg_outer[3] = {0, 0, 0}, sg_inner[3] = {0, 0, 0};
+
+    bool graphs_enabled()
+    {
+        if (use_graphs < 0) {
+            const char *env = std::getenv("SULI_GRAPHS");
+            use_graphs = (env && std::string(env) == "0") ? 0 : 1;
+        }
+        return use_graphs == 1;
+    }
+    bool step_graph_eligible()
+    {
+        const char *env = std::getenv("SULI_STEP_GRAPH");
+        if (env && std::string(env) == "0") return false;
+        if (sizeof(T) != 4 || b.nlev < 2 || !graphs_enabled() || use_cluster()) return false;
+        if (P[0].t_press != 1 || P[0].t_tempo > 2) return false;
+        if (replay_reinit >= 0) return false;
+        for (int q = 0; q < 3; ++q)
+            if (replay_cg[q] >= 0) return false;
+        for (const auto &q : P)
+            if (q.wave_t > 0 || q.mms_t != 0 || q.ccx0 == 3) return false;
+        if (!tuned && tune_env == 1) return false;
+        return true;
+    }
+    // the launches fn makes on st, captured into a graph (they have not run:
+    // their count leaves the launch counter and comes back in n)
+    template <class F> cudaGraph_t capture_seg(F fn, unsigned long long &n)
+    {
+        const unsigned long long before = g_launches.load();
+        cudaGraph_t gph = nullptr;
+        n = 0;
+        if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        const int rc = fn();
+        const cudaError_t e = cudaStreamEndCapture(st, &gph);
+        n = g_launches.load() - before;
+        g_launches.fetch_sub(n);
+        if (rc != SULI_OK || e != cudaSuccess) {
+            cudaGetLastError();
+            if (gph) cudaGraphDestroy(gph);
+            return nullptr;
+        }
+        return gph;
+    }
+    // child graph `child` appended to g after node `last`
+    static bool add_child(cudaGraph_t g, cudaGraphNode_t &last, cudaGraph_t child)
+    {
+        if (!child) return false;
+        cudaGraphNode_t nd = nullptr;
+        const bool ok = cudaGraphAddChildGraphNode(&nd, g, last ? &last : nullptr, last ? 1 : 0, child) == cudaSuccess;
+        cudaGraphDestroy(child);
+        if (ok) last = nd;
+        return ok;
+    }
+    // a WHILE node on handle h appended to g after `last`; its body in *body
+    static bool add_while(cudaGraph_t g, cudaGraphNode_t &last, cudaGraphConditionalHandle h, cudaGraph_t *body)
+    {
+        // (the parameter union has no default constructor: zeroed storage)
+        alignas(cudaGraphNodeParams) unsigned char raw[sizeof(cudaGraphNodeParams)];
+        std::memset(raw, 0, sizeof(raw));
+        cudaGraphNodeParams *p = reinterpret_cast<cudaGraphNodeParams *>(raw);
+        p->type = cudaGraphNodeTypeConditional;
+        p->conditional.handle = h;
+        p->conditional.type = cudaGraphCondTypeWhile;
+        p->conditional.size = 1;
+        cudaGraphNode_t nd = nullptr;
+        if (cudaGraphAddNode(&nd, g, last ? &last : nullptr, nullptr, last ? 1 : 0, p) != cudaSuccess) return false;
+        *body = p->conditional.phGraph_out[0];
+        last = nd;
+        return true;
+    }
+    // the step's launches up to the first solve's loops, or between loops,
+    // as the host-driven step() makes them (no host reads)
+    int sg_level_set(cudaGraphConditionalHandle hvol)
+    {
+        launch_step_reset<T>(b, st);
+        density_changed();
+        int rc;
+        if ((rc = setsc(S_DTADV, dt))) return rc;
+        if ((rc = setsc(S_RINREPLAY, -1.0))) return rc;
+        launch_level_set_adv<T>(b, st);
+        launch_reinit<T>(b, P[0].reinit_max_iter, st);
+        launch_heaviside<T>(b, 0, st);
+        launch_loop_cond<T>(b, 2, S_TRIP_VOL, (double)P[0].vol_loop_max, hvol, st);
+        CKL();
+        return SULI_OK;
+    }
+    // stage q up to its solve's passes
+    int sg_stage_head(int q, cudaGraphConditionalHandle hout)
+    {
+        if constexpr (sizeof(T) != 4) return SULI_BAD_CONFIG;   // the mixed form's step only
+        int rc;
+        if ((rc = set_stage(q))) return rc;
+        if ((rc = convdiff(1))) return rc;
+        if ((rc = tempo())) return rc;
+        if ((rc = boundary_waves())) return rc;
+        if ((rc = contorno(2))) return rc;
+        if ((rc = setsc(S_CGREPLAY, -1.0))) return rc;
+        if (!op_valid) {
+            launch_cg_refine_operator<T>(b, st);
+            launch_mg_coarsen<T>(b, st);
+            op_valid = true;
+        }
+        launch_cg_refine_setup<T>(b, st);
+        launch_loop_cond<T>(b, 1, S_TRIP_OUT0 + q - 1, 64.0, hout, st);
+        CKL();
+        return SULI_OK;
+    }
+    int sg_build()
+    {
+        if constexpr (sizeof(T) != 4) return -1;   // the mixed form's step only
+        const int cgmax = P[0].cg_max_iter;
+        const double cap_pairs = (double)((cgmax + 256) / 2 + 1);
+        cudaGraph_t G = nullptr;
+        if (cudaGraphCreate(&G, 0) != cudaSuccess) return -1;
+        bool ok = true;
+        cudaGraphNode_t last = nullptr;
+        unsigned long long n = 0;
+        sg_static = 0;
+        cudaGraphConditionalHandle hvol;
+        ok = ok && cudaGraphConditionalHandleCreate(&hvol, G, 0, cudaGraphCondAssignDefault) == cudaSuccess;
+        ok = ok && add_child(G, last, capture_seg([&] { return sg_level_set(hvol); }, n));
+        sg_static += n;
+        cudaGraph_t vbody = nullptr;
+        ok = ok && add_while(G, last, hvol, &vbody);
+        if (ok) {
+            cudaGraphNode_t vl = nullptr;
+            ok = add_child(vbody, vl, capture_seg([&] {
+                launch_volcorr<T>(b, st);
+                launch_loop_cond<T>(b, 2, S_TRIP_VOL, (double)P[0].vol_loop_max, hvol, st);
+                CKL();
+                return SULI_OK;
+            }, n));
+            sg_vol = n;
+        }
+        for (int q = 1; q <= ntt && ok; ++q) {
+            const int si = q - 1;
+            cudaGraphConditionalHandle hout;
+            ok = cudaGraphConditionalHandleCreate(&hout, G, 0, cudaGraphCondAssignDefault) == cudaSuccess;
+            ok = ok && add_child(G, last, capture_seg([&] {
+                int rc;
+                if (q == 1) {
+                    if (any_tens()) launch_curvature<T>(b, st);   // after the volume correction
+                    if ((rc = contorno(3))) return rc;
+                    if ((rc = visco())) return rc;
+                }
+                return sg_stage_head(q, hout);
+            }, n));
+            sg_static += n;
+            cudaGraph_t obody = nullptr;
+            ok = ok && add_while(G, last, hout, &obody);
+            if (!ok) break;
+            cudaGraphNode_t ol = nullptr;
+            cudaGraphConditionalHandle hin;
+            ok = cudaGraphConditionalHandleCreate(&hin, obody, 0, cudaGraphCondAssignDefault) == cudaSuccess;
+            unsigned long long n1 = 0, n2 = 0;
+            ok = ok && add_child(obody, ol, capture_seg([&] {
+                launch_cg_table<T>(b, 0, st);
+                launch_pcg_start<T>(b, 0, st);
+                launch_loop_cond<T>(b, 0, S_TRIP_IN0 + si, cap_pairs, hin, st);
+                CKL();
+                return SULI_OK;
+            }, n1));
+            cudaGraph_t ibody = nullptr;
+            ok = ok && add_while(obody, ol, hin, &ibody);
+            if (!ok) break;
+            cudaGraphNode_t il = nullptr;
+            ok = add_child(ibody, il, capture_seg([&] {
+                launch_pcg_iters<T>(b, 1, 0, st);
+                launch_pcg_iters<T>(b, 1, 1, st);
+                launch_loop_cond<T>(b, 0, S_TRIP_IN0 + si, cap_pairs, hin, st);
+                CKL();
+                return SULI_OK;
+            }, n));
+            sg_inner[si] = n;
+            ok = ok && add_child(obody, ol, capture_seg([&] {
+                launch_cg_refine_next<T>(b, st);
+                launch_loop_cond<T>(b, 1, S_TRIP_OUT0 + si, 64.0, hout, st);
+                CKL();
+                return SULI_OK;
+            }, n2));
+            sg_outer[si] = n1 + n2;
+            ok = ok && add_child(G, last, capture_seg([&] {
+                launch_cg_refine_finish<T>(b, st);
+                launch_stage_record<T>(b, si, st);
+                int rc;
+                if ((rc = posdin())) return rc;
+                if ((rc = contorno(1))) return rc;
+                if (q == ntt) launch_conmassa<T>(b, st);
+                CKL();
+                return SULI_OK;
+            }, n));
+            sg_static += n;
+        }
+        if (ok) ok = cudaGraphInstantiate(&step_exec, G, 0) == cudaSuccess;
+        cudaGraphDestroy(G);
+        cudaGetLastError();
+        if (!ok) {
+            if (step_exec) { cudaGraphExecDestroy(step_exec); step_exec = nullptr; }
+            return -1;
+        }
+        return 0;
+    }
+    // one time step by the step graph (built on first use)
+    int step_by_graph()
+    {
+        if (!step_exec && sg_build() != 0) return -1;
+        it = it + 1;
+        t = t + dt;
+        CK(cudaGraphLaunch(step_exec, st));
+        count_launch(sg_static);
+        int rc;
+        if ((rc = read_scalars())) return rc;
+        unsigned long long dyn = (unsigned long long)sc(0, S_TRIP_VOL) * sg_vol;
+        for (int si = 0; si < ntt; ++si)
+            dyn += (unsigned long long)sc(0, S_TRIP_OUT0 + si) * sg_outer[si] +
+                   (unsigned long long)sc(0, S_TRIP_IN0 + si) * sg_inner[si];
+        count_launch(dyn);
+        vol_loops = (int)sc(0, S_TRIP_VOL);
+        reinit_iters = (int)sc(0, S_RINITER);
+        for (int c = 0; c < ncases; ++c)
+            if (sc(c, S_VOLACTIVE) != 0.0) warn |= (1 << SULI_VOL_LOOP_CAP);
+        const int cgmax = P[0].cg_max_iter;
+        for (int si = 0; si < ntt; ++si) {
+            int maxit = 0, passes = 0;
+            for (int c = 0; c < ncases; ++c) {
+                maxit = std::max(maxit, (int)sc(c, S_STIT0 + si));
+                passes = std::max(passes, (int)sc(c, S_STOUT0 + si));
+                if (prof) cg_cell_iters += cells(c) * sc(c, S_STIT0 + si);
+            }
+            cg_iters[si] = maxit;
+            cg_outer[si] = passes;
+            prev_cg[si] = std::max(1, maxit / std::max(1, passes));
+            if (maxit >= cgmax) warn |= (1 << SULI_CG_MAXITER);
+        }
+        cg_res[ntt - 1] = sc(0, S_RRTRUE) * dt;
+        for (int c = 0; c < ncases; ++c)
+            if (sc(c, S_STSTALL) != 0.0) warn |= (1 << SULI_CG_STALLED);
+        return check_finite();
+    }
+    void drop_step_graph()
+    {
+        if (step_exec) { cudaGraphExecDestroy(step_exec); step_exec = nullptr; }
+        step_graph_state = 0;
+    }
+
     cudaStream_t st = nullptr;
 
     ~Impl() override
     {
         if (st) cudaStreamSynchronize(st);
+        if (step_exec) cudaGraphExecDestroy(step_exec);
         for (void *p : slabs) cudaFree(p);
         cudaFree(dsc);
         cudaFree(dpart);
@@ -1039,6 +1304,7 @@ struct Impl : ImplBase {
         for (auto &gx : pcg_graph)
             if (gx) { cudaGraphExecDestroy(gx); gx = nullptr; }
         pcg_plain_done = false;
+        drop_step_graph();
     }
     int autotune(suli_tuning *out) override
     {
@@ -1494,6 +1760,12 @@ struct Impl : ImplBase {
     {
         int rc;
         for (int s = 0; s < n; ++s) {
+            if (step_graph_state >= 0 && step_graph_eligible()) {
+                rc = step_by_graph();
+                if (rc == 0) { step_graph_state = 1; continue; }
+                if (rc > 0) return rc;
+                step_graph_state = -1;    // the graph could not be built: the host-driven step
+            }
             it = it + 1;
             t = t + dt;
             if ((rc = level_set())) return rc;

@@ -69,6 +69,12 @@ enum Scal {
     S_RRBEST,      // mixed form: the lowest FP64 r.r of the solve so far
     S_STALLED,     // mixed form: 1 when the refinement ended on stagnation
     S_TMAERR,      // 1 when a bounded wait for a TMA copy gave up (SULI_DEVICE_TIMEOUT)
+    // whole-step graph: per stage the solve's iterations and FP64 passes,
+    // stagnation in any stage; in case 0 the device loops' trip counters
+    S_STIT0, S_STIT1, S_STIT2,
+    S_STOUT0, S_STOUT1, S_STOUT2,
+    S_STSTALL,
+    S_TRIP_VOL, S_TRIP_OUT0, S_TRIP_OUT1, S_TRIP_OUT2, S_TRIP_IN0, S_TRIP_IN1, S_TRIP_IN2,
     S_NSCAL
 };
 

@@ -137,5 +137,13 @@ template <typename T> int cluster_cg_size();
 
 // per-case scalar kernels
 template <typename T> void launch_set_scalar(const Batch<T> &b, int slot, double v, cudaStream_t s);
+// whole-step graph (k_stepgraph.cu): the condition of a device loop (mode 0:
+// any S_CGACTIVE, 1: any S_OUTER >= 0, 2: any S_VOLACTIVE; trip counter
+// slot `trip` of case 0 below cap), a stage's solve statistics, the reset
+// of the counters at the start of the step
+template <typename T> void launch_loop_cond(const Batch<T> &b, int mode, int trip, double cap,
+                                            cudaGraphConditionalHandle h, cudaStream_t s);
+template <typename T> void launch_stage_record(const Batch<T> &b, int si, cudaStream_t s);
+template <typename T> void launch_step_reset(const Batch<T> &b, cudaStream_t s);
 
 }  // namespace suli

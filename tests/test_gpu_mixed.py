@@ -480,3 +480,42 @@ def test_block_coarse_levels_match_launches(gpu_lib, monkeypatch, mk):
         assert rel_l2(a - a.mean(), b - b.mean()) < 1e-6
     assert rel_l2(out["0"][1], out["16384"][1]) < 1e-6
     assert all(abs(x - y) <= 1 for x, y in zip(out["0"][2], out["16384"][2]))
+
+
+@pytest.mark.parametrize("mk", ["uneven_batch", "k_channel_periodic", "capillary_sponge_batch"])
+def test_step_graph_matches_host_driven_step(gpu_lib, monkeypatch, mk):
+    """The whole time step as one CUDA graph (device-side WHILE loops for
+    the refinement passes, the FP32 iterations and the volume correction;
+    the default for the mixed form with multigrid passes) against the
+    host-driven step (SULI_STEP_GRAPH=0): the same bits in every field and
+    the same iteration counts and passes per stage, over several steps (the
+    graph is built after the first step and the autotuner).  Covers an uneven
+    batch, the periodic k-equation channel and a batch mixing surface
+    tension with a sponge layer (different grids and physics per case)."""
+    def mk_cases():
+        if mk == "uneven_batch":
+            dims, hcol, amp = cases.ensemble_dims(5, seed=21, lo=14, hi=44)
+            return [cases.ensemble_case(i, dims, hcol, amp, precision=PREC_MIXED) for i in range(5)]
+        if mk == "k_channel_periodic":
+            return [cases.k_channel(32, 8, 16, m_turb=2, precision=PREC_MIXED)]
+        return [cases.capillary_column(32, 4, 0.25, precision=PREC_MIXED),
+                cases.sponge_tank(32, 4, 16, esp_type=1, precision=PREC_MIXED)]
+    out = {}
+    for sg in ("0", "1"):
+        monkeypatch.setenv("SULI_STEP_GRAPH", sg)
+        cs = mk_cases()
+        for c in cs:
+            c.params.mixed_precond = 1
+        g = gpu_lib.SuliGPU([c.params for c in cs])
+        g.start([c.fields for c in cs])
+        its = []
+        for _ in range(4):
+            g.step(1)
+            d = g.diag(0)
+            its.append((list(d.cg_iters), list(d.cg_outer)))
+        out[sg] = ([{n: g.download(n, case=q) for n in ("U", "V", "W", "LS", "PRD1")} for q in range(len(cs))], its)
+        g.close()
+    for a, b in zip(out["0"][0], out["1"][0]):
+        for n in a:
+            assert np.array_equal(a[n], b[n]), (mk, n, float(np.abs(a[n] - b[n]).max()))
+    assert out["0"][1] == out["1"][1], (out["0"][1], out["1"][1])
