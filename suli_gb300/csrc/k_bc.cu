@@ -215,8 +215,9 @@ __global__ void k_bc_phase(const CaseDev<T> *__restrict__ cs, int ncases, int ph
 // indexed by (call, j, k), as in the oracle.
 template <typename T>
 __global__ void k_inflow(const CaseDev<T> *__restrict__ cs, int ncases, int I, double thr_dz,
-                         unsigned long long call)
+                         unsigned long long call, int cdev)
 {
+    if (cdev) call += (unsigned long long)cs[0].sc[S_RNGBASE];
     const CaseDev<T> &c = cs[blockIdx.x];
     if (c.ccx0 != 3) return;
     const Geo &g = c.g;
@@ -284,7 +285,7 @@ __global__ void k_inflow(const CaseDev<T> *__restrict__ cs, int ncases, int I, d
 }
 
 template <typename T>
-void launch_contorno(const Batch<T> &b, int nlock, cudaStream_t s, unsigned long long rng_call)
+void launch_contorno(const Batch<T> &b, int nlock, cudaStream_t s, unsigned long long rng_call, int cdev)
 {
     if (nlock != 1 && nlock != 2) return;   // nlock = 3 acts only with an IBM (handled by the caller)
     int nb = (b.max_plane + 255) / 256;
@@ -304,12 +305,12 @@ void launch_contorno(const Batch<T> &b, int nlock, cudaStream_t s, unsigned long
     };
     for (int ph = 0; ph < 3; ++ph) phase(ph);
     if (inflow) {
-        k_inflow<T><<<b.ncases, 256, 0, s>>>(b.dcases, b.ncases, 0, 1.0, rng_call); count_launch();
+        k_inflow<T><<<b.ncases, 256, 0, s>>>(b.dcases, b.ncases, 0, 1.0, rng_call, cdev); count_launch();
     }
     if (nlock == 2) {
         phase(3);
         if (inflow) {
-            k_inflow<T><<<b.ncases, 256, 0, s>>>(b.dcases, b.ncases, 1, 2.0, rng_call + 1); count_launch();
+            k_inflow<T><<<b.ncases, 256, 0, s>>>(b.dcases, b.ncases, 1, 2.0, rng_call + 1, cdev); count_launch();
         }
     }
 }
@@ -375,7 +376,7 @@ template <typename T> void launch_outflow_balance(const Batch<T> &b, cudaStream_
 
 template void launch_outflow_balance<float>(const Batch<float> &, cudaStream_t);
 template void launch_outflow_balance<double>(const Batch<double> &, cudaStream_t);
-template void launch_contorno<double>(const Batch<double> &, int, cudaStream_t, unsigned long long);
-template void launch_contorno<float>(const Batch<float> &, int, cudaStream_t, unsigned long long);
+template void launch_contorno<double>(const Batch<double> &, int, cudaStream_t, unsigned long long, int);
+template void launch_contorno<float>(const Batch<float> &, int, cudaStream_t, unsigned long long, int);
 
 }  // namespace suli

@@ -274,8 +274,9 @@ __global__ void k_exp_press_acc(const CaseDev<T> *__restrict__ cs, int ncases)
 // bxx0 / bxz0 the i = 0 velocities, bxx1 the i = 1 u.  Grid: x strides the
 // plane, y = case.
 template <typename T>
-__global__ void k_waves(const CaseDev<T> *__restrict__ cs, int ncases, double t)
+__global__ void k_waves(const CaseDev<T> *__restrict__ cs, int ncases, double t, int tdev)
 {
+    if (tdev) t = cs[0].sc[S_TIME];
     const CaseDev<T> &c = cs[blockIdx.y];
     if (c.wave_t <= 0) return;
     const Geo &g = c.g;
@@ -366,14 +367,14 @@ template <typename T> void launch_exp_press(const Batch<T> &b, cudaStream_t s)
     k_exp_press_acc<T><<<grid, 256, 0, s>>>(b.dcases, b.ncases); count_launch();
 }
 
-template <typename T> void launch_waves(const Batch<T> &b, double t, cudaStream_t s)
+template <typename T> void launch_waves(const Batch<T> &b, double t, cudaStream_t s, int tdev)
 {
     dim3 grid(plane_blocks(b.max_plane), b.ncases);
-    k_waves<T><<<grid, 256, 0, s>>>(b.dcases, b.ncases, t); count_launch();
+    k_waves<T><<<grid, 256, 0, s>>>(b.dcases, b.ncases, t, tdev); count_launch();
 }
 
-template void launch_waves<float>(const Batch<float> &, double, cudaStream_t);
-template void launch_waves<double>(const Batch<double> &, double, cudaStream_t);
+template void launch_waves<float>(const Batch<float> &, double, cudaStream_t, int);
+template void launch_waves<double>(const Batch<double> &, double, cudaStream_t, int);
 template void launch_contorno_les<float>(const Batch<float> &, cudaStream_t);
 template void launch_contorno_les<double>(const Batch<double> &, cudaStream_t);
 template void launch_keq<float>(const Batch<float> &, int, const double *, cudaStream_t);

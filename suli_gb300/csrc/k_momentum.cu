@@ -306,6 +306,7 @@ __device__ __forceinline__ void tempo_one_m(const CaseDev<T> &c, int tt, int it,
 template <typename T>
 __global__ void __launch_bounds__(NTHREADS) k_tempo(const CaseDev<T> *__restrict__ cs, int ncases, int tt, int it)
 {
+    if (it < 0) it = (int)cs[0].sc[S_ITSTEP];
     const CaseDev<T> &c = cs[find_case(cs, ncases)];
     int i, j, k;
     tile_ijk(c, i, j, k);

@@ -331,12 +331,17 @@ struct Impl : ImplBase {
     // once per handle, after the autotuner, and replayed every step: one
     // launch and one host read per step.  SULI_STEP_GRAPH=0 keeps the host-
     // driven step; configurations whose launches carry per-step host values
-    // (waves and the inflow take the time or a call count, the AB schemes
-    // the step number, replayed counts, the manufactured solution) keep it
-    // too.  Iterations past a case's convergence are no-ops (it has left the
+    // (replayed counts, the manufactured solution, the IPA, the waves) keep
+    // it too; the step number and the inflow's random-number call count,
+    // which the AB schemes and the inflow take, are copied into case 0's
+    // scalars before each launch and read there (the waves' time likewise,
+    // should they join).  Iterations past a case's convergence are no-ops (it has left the
     // active tables), so both paths give the same bits.
     cudaGraphExec_t step_exec = nullptr;
     int step_graph_state = 0;      // 0 not built, 1 built, -1 not used by this handle
+    bool sg_capturing = false;     // launches read the step's host values from case 0's scalars
+    unsigned long long sg_rng_per_step = 0;   // inflow calls of one step
+    double *sg_hvals = nullptr;    // pinned: the step number, time and inflow call count of the step
     unsigned long long sg_static = 0, sg_vol = 0, sg_outer[3] = {0, 0, 0}, sg_inner[3] = {0, 0, 0};
 
     bool graphs_enabled()
@@ -352,12 +357,12 @@ struct Impl : ImplBase {
         const char *env = std::getenv("SULI_STEP_GRAPH");
         if (env && std::string(env) == "0") return false;
         if (sizeof(T) != 4 || b.nlev < 2 || !graphs_enabled() || use_cluster()) return false;
-        if (P[0].t_press != 1 || P[0].t_tempo > 2) return false;
+        if (P[0].t_press != 1) return false;
         if (replay_reinit >= 0) return false;
         for (int q = 0; q < 3; ++q)
             if (replay_cg[q] >= 0) return false;
         for (const auto &q : P)
-            if (q.wave_t > 0 || q.mms_t != 0 || q.ccx0 == 3) return false;
+            if (q.mms_t != 0 || q.wave_t > 0) return false;
         if (!tuned && tune_env == 1) return false;
         return true;
     }
@@ -453,7 +458,17 @@ struct Impl : ImplBase {
         const int cgmax = P[0].cg_max_iter;
         const double cap_pairs = (double)((cgmax + 256) / 2 + 1);
         cudaGraph_t G = nullptr;
+        if (!sg_hvals && cudaMallocHost(&sg_hvals, 3 * sizeof(double)) != cudaSuccess) {
+            cudaGetLastError();
+            sg_hvals = nullptr;
+            return -1;
+        }
         if (cudaGraphCreate(&G, 0) != cudaSuccess) return -1;
+        // the captured launches take the step's host values from the device
+        // (inflow calls counted from the start of the step)
+        sg_capturing = true;
+        const unsigned long long rng0 = inflow_calls;
+        inflow_calls = 0;
         bool ok = true;
         cudaGraphNode_t last = nullptr;
         unsigned long long n = 0;
@@ -533,6 +548,9 @@ struct Impl : ImplBase {
             }, n));
             sg_static += n;
         }
+        sg_capturing = false;
+        sg_rng_per_step = inflow_calls;
+        inflow_calls = rng0;
         if (ok) ok = cudaGraphInstantiate(&step_exec, G, 0) == cudaSuccess;
         cudaGraphDestroy(G);
         cudaGetLastError();
@@ -548,7 +566,12 @@ struct Impl : ImplBase {
         if (!step_exec && sg_build() != 0) return -1;
         it = it + 1;
         t = t + dt;
+        sg_hvals[0] = (double)it;
+        sg_hvals[1] = t;
+        sg_hvals[2] = (double)inflow_calls;
+        CK(cudaMemcpyAsync(dsc + S_ITSTEP, sg_hvals, 3 * sizeof(double), cudaMemcpyHostToDevice, st));
         CK(cudaGraphLaunch(step_exec, st));
+        inflow_calls += sg_rng_per_step;
         count_launch(sg_static);
         int rc;
         if ((rc = read_scalars())) return rc;
@@ -591,6 +614,7 @@ struct Impl : ImplBase {
     {
         if (st) cudaStreamSynchronize(st);
         if (step_exec) cudaGraphExecDestroy(step_exec);
+        if (sg_hvals) cudaFreeHost(sg_hvals);
         for (void *p : slabs) cudaFree(p);
         cudaFree(dsc);
         cudaFree(dpart);
@@ -1494,7 +1518,7 @@ struct Impl : ImplBase {
         // mixed form: the IBM image values (FP32) into the FP64 masters before
         // the plane fills, which run on both (the inflow writes both)
         if (sizeof(T) == 4) launch_sync_masters<T>(b, st);
-        launch_contorno<T>(b, nlock, st, inflow_calls);
+        launch_contorno<T>(b, nlock, st, inflow_calls, sg_capturing ? 1 : 0);
         if (any_inflow()) inflow_calls += (nlock == 2) ? 2 : 1;
         if (nlock == 2) launch_outflow_balance<T>(b, st);
         CKL();
@@ -1547,7 +1571,7 @@ struct Impl : ImplBase {
     int boundary_waves() override
     {
         if (!any_waves()) return SULI_OK;
-        launch_waves<T>(b, t, st);
+        launch_waves<T>(b, t, st, sg_capturing ? 1 : 0);
         CKL();
         return SULI_OK;
     }
@@ -1568,7 +1592,7 @@ struct Impl : ImplBase {
     }
     int tempo() override
     {
-        launch_tempo<T>(b, tt, it, st);
+        launch_tempo<T>(b, tt, sg_capturing ? -1 : it, st);
         CKL();
         return SULI_OK;
     }

@@ -75,6 +75,10 @@ enum Scal {
     S_STOUT0, S_STOUT1, S_STOUT2,
     S_STSTALL,
     S_TRIP_VOL, S_TRIP_OUT0, S_TRIP_OUT1, S_TRIP_OUT2, S_TRIP_IN0, S_TRIP_IN1, S_TRIP_IN2,
+    // in case 0: the step's host values the step graph's launches read (the
+    // step number, the time, the inflow's random-number call count at the
+    // start of the step); contiguous, written by one copy per step
+    S_ITSTEP, S_TIME, S_RNGBASE,
     S_NSCAL
 };
 

@@ -70,7 +70,8 @@ template <typename T> void launch_visco(const Batch<T> &b, int keq_stages, const
 template <typename T> void launch_keq(const Batch<T> &b, int ntt, const double *a_dt, cudaStream_t s);
 template <typename T> void launch_contorno_les(const Batch<T> &b, cudaStream_t s);
 template <typename T> void launch_exp_press(const Batch<T> &b, cudaStream_t s);
-template <typename T> void launch_waves(const Batch<T> &b, double t, cudaStream_t s);
+// (tdev: the time from case 0's S_TIME instead of t, for the step graph)
+template <typename T> void launch_waves(const Batch<T> &b, double t, cudaStream_t s, int tdev = 0);
 template <typename T> void launch_convdiff(const Batch<T> &b, int fuse_compl, cudaStream_t s);
 // convdiff (+ complementos) with its operands staged by TMA tensor loads
 // (k_convdiff_tma.cu): b.tmaps holds 8 maps per case (u, v, w, rho, mu, xmu,
@@ -82,13 +83,16 @@ constexpr int CD_MAP_BOX_X = 40, CD_MAP_BOX_Y = 12;
 // sponge_layer's epis_z for the esp_type > 0 cases (before complementos)
 template <typename T> void launch_sponge(const Batch<T> &b, cudaStream_t s);
 template <typename T> void launch_complementos(const Batch<T> &b, cudaStream_t s);
+// (it < 0: the step number from case 0's S_ITSTEP, for the step graph)
 template <typename T> void launch_tempo(const Batch<T> &b, int tt, int it, cudaStream_t s);
 template <typename T> void launch_posdin(const Batch<T> &b, cudaStream_t s);
 template <typename T> void launch_conmassa(const Batch<T> &b, cudaStream_t s);
 template <typename T> void launch_mms_error(const Batch<T> &b, cudaStream_t s);
 
 // boundary conditions (k_bc.cu)
-template <typename T> void launch_contorno(const Batch<T> &b, int nlock, cudaStream_t s, unsigned long long rng_call = 0);
+// (cdev: the inflow's call count is case 0's S_RNGBASE plus rng_call, for the step graph)
+template <typename T> void launch_contorno(const Batch<T> &b, int nlock, cudaStream_t s, unsigned long long rng_call = 0,
+                                           int cdev = 0);
 // balanced free outflow (outflow_flux = 1, ccxf = 4): after contorno(2), on the
 // FP64 masters where the mixed form has them, then their FP32 copies
 template <typename T> void launch_outflow_balance(const Batch<T> &b, cudaStream_t s);

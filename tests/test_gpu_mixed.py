@@ -482,7 +482,8 @@ def test_block_coarse_levels_match_launches(gpu_lib, monkeypatch, mk):
     assert all(abs(x - y) <= 1 for x, y in zip(out["0"][2], out["16384"][2]))
 
 
-@pytest.mark.parametrize("mk", ["uneven_batch", "k_channel_periodic", "capillary_sponge_batch"])
+@pytest.mark.parametrize("mk", ["uneven_batch", "k_channel_periodic", "capillary_sponge_batch", "open_channel_inflow",
+                                "dam_break_ab3"])
 def test_step_graph_matches_host_driven_step(gpu_lib, monkeypatch, mk):
     """The whole time step as one CUDA graph (device-side WHILE loops for
     the refinement passes, the FP32 iterations and the volume correction;
@@ -490,14 +491,23 @@ def test_step_graph_matches_host_driven_step(gpu_lib, monkeypatch, mk):
     host-driven step (SULI_STEP_GRAPH=0): the same bits in every field and
     the same iteration counts and passes per stage, over several steps (the
     graph is built after the first step and the autotuner).  Covers an uneven
-    batch, the periodic k-equation channel and a batch mixing surface
-    tension with a sponge layer (different grids and physics per case)."""
+    batch, the periodic k-equation channel, a batch mixing surface tension
+    with a sponge layer (different grids and physics per case), and the
+    launches that take the step's host values from the device: the open
+    channel's perturbed inflow (the random-number call count) and the AB3
+    scheme (the step number)."""
     def mk_cases():
         if mk == "uneven_batch":
             dims, hcol, amp = cases.ensemble_dims(5, seed=21, lo=14, hi=44)
             return [cases.ensemble_case(i, dims, hcol, amp, precision=PREC_MIXED) for i in range(5)]
         if mk == "k_channel_periodic":
             return [cases.k_channel(32, 8, 16, m_turb=2, precision=PREC_MIXED)]
+        if mk == "open_channel_inflow":
+            return [cases.open_channel(64, 16, 16, precision=PREC_MIXED, balanced=True)]
+        if mk == "dam_break_ab3":
+            c = cases.dam_break(32, 16, 16, precision=PREC_MIXED)
+            c.params.t_tempo = 4
+            return [c]
         return [cases.capillary_column(32, 4, 0.25, precision=PREC_MIXED),
                 cases.sponge_tank(32, 4, 16, esp_type=1, precision=PREC_MIXED)]
     out = {}
