@@ -364,6 +364,21 @@ struct Impl : ImplBase {
         for (const auto &q : P)
             if (q.mms_t != 0 || q.wave_t > 0) return false;
         if (!tuned && tune_env == 1) return false;
+        return step_graph_eligible_shape();
+    }
+    // the configuration conditions of the step graph (not whether the
+    // autotuner has run)
+    bool step_graph_eligible_shape()
+    {
+        const char *env = std::getenv("SULI_STEP_GRAPH");
+        if (env && std::string(env) == "0") return false;
+        if (sizeof(T) != 4 || b.nlev < 2 || !graphs_enabled() || use_cluster()) return false;
+        if (P[0].t_press != 1) return false;
+        if (replay_reinit >= 0) return false;
+        for (int q = 0; q < 3; ++q)
+            if (replay_cg[q] >= 0) return false;
+        for (const auto &q : P)
+            if (q.mms_t != 0 || q.wave_t > 0) return false;
         return true;
     }
     // the launches fn makes on st, captured into a graph (they have not run:
@@ -1323,6 +1338,30 @@ struct Impl : ImplBase {
         cudaEventDestroy(e1);
         return (double)ms / reps;
     }
+    // as time_it, with the launches of f captured once into a graph and the
+    // graph replayed (how the step graph runs them); falls back to time_it
+    template <typename F> double time_graph(F f, int reps)
+    {
+        const unsigned long long before = g_launches.load();
+        cudaGraph_t gph = nullptr;
+        cudaGraphExec_t ex = nullptr;
+        bool ok = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+        if (ok) {
+            f();
+            ok = cudaStreamEndCapture(st, &gph) == cudaSuccess && gph &&
+                 cudaGraphInstantiate(&ex, gph, 0) == cudaSuccess;
+        }
+        g_launches.store(before);   // captured, not run
+        if (gph) cudaGraphDestroy(gph);
+        if (!ok) {
+            cudaGetLastError();
+            if (ex) cudaGraphExecDestroy(ex);
+            return time_it(f, reps);
+        }
+        const double ms = time_it([&] { cudaGraphLaunch(ex, st); }, reps);
+        cudaGraphExecDestroy(ex);
+        return ms;
+    }
     void drop_graphs()
     {
         for (auto &gx : pcg_graph)
@@ -1376,9 +1415,13 @@ struct Impl : ImplBase {
             if (!tune_locked_mg) {
                 double best = 1e30;
                 int bc = def.mg_block_cells;
+                // (inside a graph when the step runs as one: launches cost
+                // little there, which moves the balance towards grid launches)
+                const bool in_graph = step_graph_eligible_shape();
                 for (int cells : {0, 4096, 16384, 65536}) {
                     b.tune.mg_block_cells = cells;
-                    const double ms = time_it([&] { launch_profile_kernel<T>(b, 4, 0, st); }, 2);
+                    auto vc = [&] { launch_profile_kernel<T>(b, 4, 0, st); };
+                    const double ms = in_graph ? time_graph(vc, 3) : time_it(vc, 2);
                     if (cells == def.mg_block_cells) dms += ms;
                     if (ms < best) { best = ms; bc = cells; }
                 }
