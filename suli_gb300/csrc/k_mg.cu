@@ -183,9 +183,11 @@ __global__ void __launch_bounds__(NTHREADS, 4) k_mg_sweep(const CaseDev<T> *__re
         // this thread's copy slots: shared offset in a stage, source address
         // of plane k0 - 2 (advanced one plane per issue), kind; a segment
         // outside the box in x or y is never copied
-        int so[SW_SLOTS], sk[SW_SLOTS];
+        // (smask: bit t set when the slot copies in a plane of type t -- 0 the
+        // unit's first plane k0 - 2 (z only), 1 its last k1 + 2 (z and cz),
+        // 2 any other; a slot outside the box or the stage copies in none)
+        int so[SW_SLOTS], smask[SW_SLOTS];
         const T *gp[SW_SLOTS];
-        bool sv[SW_SLOTS];
 #pragma unroll
         for (int s = 0; s < SW_SLOTS; ++s) {
             const int ch = t + s * NTHREADS;
@@ -201,8 +203,8 @@ __global__ void __launch_bounds__(NTHREADS, 4) k_mg_sweep(const CaseDev<T> *__re
             const int r = (e - base) / SW_R, h = (e - base) % SW_R;
             const int x = X0 + h, y = rows0 + r;
             so[s] = e;
-            sk[s] = kind;
-            sv[s] = ch < SW_CHUNKS && x >= 0 && x + 4 <= isx && y >= 0 && y <= ny + 1 && !(zero && kind == 0);
+            const bool sv = ch < SW_CHUNKS && x >= 0 && x + 4 <= isx && y >= 0 && y <= ny + 1 && !(zero && kind == 0);
+            smask[s] = sv ? (kind == 0 ? 7 : (kind == 2 ? 6 : 4)) : 0;
             gp[s] = arr + (x + isx * y) + (long long)isxy * (k0 - 2);
         }
         // plane p's copies into stage `st`: of plane k0 - 2 only z is read,
@@ -210,10 +212,10 @@ __global__ void __launch_bounds__(NTHREADS, 4) k_mg_sweep(const CaseDev<T> *__re
         auto issue = [&](int p, int st) {
             if (p >= 0 && p <= nz + 1 && p <= k1 + 2) {
                 T *S = stg + st * SW_STAGE;
-                const int kmax = (p == k0 - 2) ? 0 : (p == k1 + 2) ? 2 : 3;
+                const int bit = (p == k0 - 2) ? 1 : (p == k1 + 2) ? 2 : 4;
 #pragma unroll
                 for (int s = 0; s < SW_SLOTS; ++s)
-                    if (sv[s] && (sk[s] == 0 || (sk[s] == 2 && kmax >= 2) || kmax == 3)) cp_async16(S + so[s], gp[s]);
+                    if (smask[s] & bit) cp_async16(S + so[s], gp[s]);
             }
 #pragma unroll
             for (int s = 0; s < SW_SLOTS; ++s) gp[s] += isxy;
@@ -312,18 +314,14 @@ __global__ void __launch_bounds__(NTHREADS, 4) k_mg_sweep(const CaseDev<T> *__re
             const int kb = kk - 1;
             if (kb >= k0) {
                 if (ov) {
-                    // ring slots of planes kb - 1 (= kk - 2) and kb (= kk - 1)
+                    // ring slots of planes kb - 1 (= kk - 2) and kb (= kk - 1);
+                    // both colours evaluate the stencil (its operands are in
+                    // place either way), the first colour keeps its ring value
                     const T *Rm = ring[rr == 2 ? 0 : rr + 1], *R0 = ring[rr == 0 ? 2 : rr - 1], *Rp = R;
-                    T zn;
-                    if (((oi + oj + kb) & 1) == c2) {
-                        const T sm = Sm[SW_OF + os] + Sm[SW_OX + os] * R0[op - 1] + Sm[SW_OX + os + 1] * R0[op + 1] +
-                                     Sm[SW_OY + os] * R0[op - SW_X] + Sm[SW_OY + os + SW_R] * R0[op + SW_X] +
-                                     Sm[SW_OC + os] * Rm[op] + S0[SW_OC + os] * Rp[op];
-                        zn = sm * Sm[SW_OD + os];
-                    } else {
-                        zn = R0[op];
-                    }
-                    *zo = zn;
+                    const T sm = Sm[SW_OF + os] + Sm[SW_OX + os] * R0[op - 1] + Sm[SW_OX + os + 1] * R0[op + 1] +
+                                 Sm[SW_OY + os] * R0[op - SW_X] + Sm[SW_OY + os + SW_R] * R0[op + SW_X] +
+                                 Sm[SW_OC + os] * Rm[op] + S0[SW_OC + os] * Rp[op];
+                    *zo = (((oi + oj + kb) & 1) == c2) ? sm * Sm[SW_OD + os] : R0[op];
                 }
                 zo += isxy;
             }
