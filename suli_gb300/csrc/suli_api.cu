@@ -246,6 +246,61 @@ __global__ void k_unpack_field(const double *__restrict__ src, T *__restrict__ b
     }
 }
 
+// the same into the FP32 box and, when master is not null, its FP64 master
+// from one read of the source (the source may be pinned host memory read
+// over the chip-to-chip link)
+template <typename T>
+__global__ void k_unpack_field2(const double *__restrict__ src, T *__restrict__ box, double *__restrict__ master,
+                                long long n, int e0, int e1, int lo0, int lo1, int lo2, long long pitch, long long height)
+{
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % e0);
+        const long long r = t / e0;
+        const int j = (int)(r % e1);
+        const int k = (int)(r / e1);
+        const long long q = (lo0 + i) + pitch * ((lo1 + j) + height * (long long)(lo2 + k));
+        const double v = src[t];
+        box[q] = T(v);
+        if (master) master[q] = v;
+    }
+}
+
+// one field transfer of a list (mixed form, page-locked host side): mode 0
+// host FP64 -> FP32 box (and FP64 master), 1 FP64 master -> host, 2 FP32 box
+// -> host
+template <typename T> struct XferDesc {
+    double *host;
+    T *box;
+    double *master;
+    int n, e0, e1, lo0, lo1, lo2, mode;
+    long long pitch, height;
+};
+
+// every transfer of a list in one launch: blockIdx.y the transfer,
+// blockIdx.x strides its elements
+template <typename T>
+__global__ void __launch_bounds__(256) k_xfer_list(const XferDesc<T> *__restrict__ ds)
+{
+    const XferDesc<T> d = ds[blockIdx.y];
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < d.n; t += gridDim.x * blockDim.x) {
+        const int i = t % d.e0;
+        const int r = t / d.e0;
+        const int j = r % d.e1;
+        const int k = r / d.e1;
+        const long long q = (d.lo0 + i) + d.pitch * ((d.lo1 + j) + d.height * (long long)(d.lo2 + k));
+        if (d.mode == 0) {
+            const double v = d.host[t];
+            d.box[q] = T(v);
+            if (d.master) d.master[q] = v;
+        } else if (d.mode == 1) {
+            d.host[t] = d.master[q];
+        } else {
+            d.host[t] = (double)d.box[q];
+        }
+    }
+}
+
 template <typename T>
 __global__ void k_pack_field(const T *__restrict__ box, double *__restrict__ dst, long long n, int e0, int e1,
                              int lo0, int lo1, int lo2, long long pitch, long long height)
@@ -269,6 +324,8 @@ struct Impl : ImplBase {
     unsigned *dcnt = nullptr, *dactdone = nullptr;
     int *dact = nullptr;
     double *dstage = nullptr;      // mixed form: FP64 staging of field transfers
+    void *dxfer = nullptr, *hxfer = nullptr;   // transfer-list descriptors (device, pinned host)
+    size_t xfer_cap = 0;
     size_t stage_elems = 0;
     // One preconditioned CG iteration (about 75 kernels: product, update,
     // V-cycle, r.z, direction) captured per active-table slot and replayed:
@@ -637,6 +694,8 @@ struct Impl : ImplBase {
         cudaFree(dact);
         cudaFree(dactdone);
         cudaFree(dstage);
+        cudaFree(dxfer);
+        if (hxfer) cudaFreeHost(hxfer);
         for (auto &gx : pcg_graph)
             if (gx) cudaGraphExecDestroy(gx);
         cudaFree(drk);
@@ -1208,7 +1267,55 @@ struct Impl : ImplBase {
         if (n < 0 || (n > 0 && (!cases || !fields || !hosts))) return fail(SULI_BAD_ARG, "bad transfer list");
         if (up) op_valid = false;
         std::vector<int> reset;
+        // mixed form: the transfers of FP32 fields whose host side is page-
+        // locked go in one launch (k_xfer_list), the rest one by one
+        std::vector<char> done(n, 0);
+        if (sizeof(T) == 4 && n > 0) {
+            std::vector<XferDesc<T>> ds;
+            for (int q = 0; q < n; ++q) {
+                if (!hosts[q] || cases[q] < 0 || cases[q] >= ncases || is_int_field(fields[q])) continue;
+                double *hv = device_view(hosts[q]);
+                void *dev = dev_ptr(cases[q], fields[q]);
+                int lo[3], hi[3];
+                if (!hv || !dev || suli_field_shape(&P[cases[q]], fields[q], lo, hi) != SULI_OK) continue;
+                const Geo &g = hc[cases[q]].g;
+                const long long e0 = hi[0] - lo[0] + 1, e1 = hi[1] - lo[1] + 1, e2 = hi[2] - lo[2] + 1;
+                if (e0 * e1 * e2 >= (1LL << 31)) continue;
+                XferDesc<T> d;
+                d.host = hv;
+                d.box = (T *)dev;
+                d.master = master_ptr(cases[q], fields[q]);
+                d.n = (int)(e0 * e1 * e2);
+                d.e0 = (int)e0; d.e1 = (int)e1;
+                d.lo0 = lo[0]; d.lo1 = lo[1]; d.lo2 = lo[2];
+                d.mode = up ? 0 : (d.master ? 1 : 2);
+                d.pitch = is_plane_field(fields[q]) ? (long long)(g.ny + 3) : (long long)g.sx;
+                d.height = is_plane_field(fields[q]) ? (long long)(g.nz + 3) : (long long)(g.ny + 3);
+                ds.push_back(d);
+                done[q] = 1;
+                if (up && fields[q] == SULI_F_PRD1) reset.push_back(cases[q]);
+            }
+            if (!ds.empty()) {
+                const size_t bytes = sizeof(XferDesc<T>) * ds.size();
+                if (bytes > xfer_cap) {
+                    cudaFree(dxfer);
+                    cudaFreeHost(hxfer);
+                    dxfer = nullptr; hxfer = nullptr; xfer_cap = 0;
+                    CK(cudaMalloc(&dxfer, bytes));
+                    CK(cudaMallocHost(&hxfer, bytes));
+                    xfer_cap = bytes;
+                }
+                std::memcpy(hxfer, ds.data(), bytes);
+                CK(cudaMemcpyAsync(dxfer, hxfer, bytes, cudaMemcpyHostToDevice, st));
+                for (size_t q0 = 0; q0 < ds.size(); q0 += 65535) {
+                    const unsigned ny = (unsigned)std::min<size_t>(65535, ds.size() - q0);
+                    k_xfer_list<T><<<dim3(64, ny), 256, 0, st>>>((const XferDesc<T> *)dxfer + q0);
+                }
+                CKL();
+            }
+        }
         for (int q = 0; q < n; ++q) {
+            if (done[q]) continue;
             if (!hosts[q]) return fail(SULI_BAD_ARG, "null host pointer");
             bool p64reset = false;
             int rc = enqueue_copy(cases[q], fields[q], hosts[q], up, p64reset);
@@ -1224,6 +1331,20 @@ struct Impl : ImplBase {
             if (rc) return rc;
         }
         return SULI_OK;
+    }
+
+    // the device's address of page-locked host memory (allocated or
+    // registered through CUDA), or null for any other pointer (pageable
+    // memory goes through the staging buffer)
+    static double *device_view(void *host)
+    {
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+        return static_cast<double *>(a.devicePointer);
     }
 
     // queue one transfer on the library's stream (no synchronisation)
@@ -1245,9 +1366,28 @@ struct Impl : ImplBase {
         if (!isint && sizeof(T) != sizeof(double)) {
             // FP64 host block <-> FP32 box, converted on the GPU; velocities
             // also go to / come from their FP64 masters
-            if (n > stage_elems) return fail(SULI_BAD_ARG, "field larger than the transfer staging buffer");
             const int nb = (int)std::min<size_t>((n + 255) / 256, 4096);
             double *master = master_ptr(icase, f);
+            // page-locked host memory the device can address: the conversion
+            // kernel reads or writes it directly (no staging copy, so the
+            // transfers of a list overlap on the link instead of queueing
+            // behind one staging buffer)
+            if (double *hv = device_view(host)) {
+                if (up) {
+                    k_unpack_field2<T><<<nb, 256, 0, st>>>(hv, (T *)dev, master, (long long)n, (int)e0, (int)e1, lo[0],
+                                                           lo[1], lo[2], (long long)dpitch_el, (long long)dheight);
+                    p64reset = (f == SULI_F_PRD1);
+                } else if (master) {
+                    k_pack_field<double><<<nb, 256, 0, st>>>(master, hv, (long long)n, (int)e0, (int)e1, lo[0], lo[1],
+                                                             lo[2], (long long)dpitch_el, (long long)dheight);
+                } else {
+                    k_pack_field<T><<<nb, 256, 0, st>>>((const T *)dev, hv, (long long)n, (int)e0, (int)e1, lo[0], lo[1],
+                                                        lo[2], (long long)dpitch_el, (long long)dheight);
+                }
+                CKL();
+                return SULI_OK;
+            }
+            if (n > stage_elems) return fail(SULI_BAD_ARG, "field larger than the transfer staging buffer");
             if (up) {
                 CK(cudaMemcpyAsync(dstage, host, n * sizeof(double), cudaMemcpyHostToDevice, st));
                 k_unpack_field<T><<<nb, 256, 0, st>>>(dstage, (T *)dev, (long long)n, (int)e0, (int)e1, lo[0], lo[1],

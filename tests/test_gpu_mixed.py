@@ -445,6 +445,54 @@ def test_batched_transfers_match_single(gpu_lib, precision):
     g.close()
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_pinned_transfers_match_pageable(gpu_lib, precision):
+    """Transfers from and to page-locked host buffers (the mixed form's
+    conversion kernels then read and write them in place, no staging copy)
+    move the same bits as from pageable numpy arrays, one by one and as a
+    list, in both forms."""
+    torch = pytest.importorskip("torch")
+    from suli_gb300.solver import field_shape
+
+    def pinned(shape, dtype):
+        tdt = torch.int32 if dtype == np.int32 else torch.float64
+        t = torch.zeros(tuple(reversed(shape)), dtype=tdt, pin_memory=True)
+        return t, t.numpy().T          # a Fortran-order view of pinned memory
+
+    dims, hcol, amp = cases.ensemble_dims(3, seed=9, lo=12, hi=20)
+    cs = [cases.ensemble_case(i, dims, hcol, amp, precision=precision) for i in range(3)]
+    g = gpu_lib.SuliGPU([c.params for c in cs])
+    g.start([c.fields for c in cs])
+    g.step(1)
+    names = ("U", "V", "W", "LS", "PRD1", "ID_IBM")
+    keep = []
+    items = []
+    for i in range(3):
+        for n in names:
+            ref = g.download(n, i)
+            t, view = pinned(field_shape(cs[i].params, n), ref.dtype)
+            keep.append(t)
+            items.append((n, i, view))
+            g.download_many([(n, i, view)])
+            assert np.array_equal(view, ref), (n, i)
+    # new values uploaded from pinned buffers as one list, read back pageable
+    rng = np.random.default_rng(4)
+    ups = []
+    for n, i, view in items:
+        if n == "ID_IBM":
+            continue
+        view[...] = view + rng.standard_normal(view.shape)
+        ups.append((n, i, view))
+    g.upload_many(ups)
+    for n, i, view in ups:
+        b = g.download(n, i)
+        if precision == 0 or n in ("U", "V", "W", "LS"):
+            assert np.array_equal(b, view), (n, i)
+        else:
+            assert np.array_equal(b, view.astype(np.float32).astype(np.float64)), (n, i)
+    g.close()
+
+
 @pytest.mark.parametrize("mk", ["periodic_odd", "uneven_batch", "k_channel"])
 def test_block_coarse_levels_match_launches(gpu_lib, monkeypatch, mk):
     """The coarse end of the V-cycle in one thread block per case (default:
