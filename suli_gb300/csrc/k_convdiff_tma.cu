@@ -218,7 +218,7 @@ __host__ __device__ __forceinline__ long long cd_shell_count(int nx, int ny, int
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_convdiff_shell(const CaseDev<T> *__restrict__ cs, int ncases, int fuse,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_convdiff_shell(const CaseDev<T> *__restrict__ cs, int ncases, int fuse,
                                                         long long total)
 {
     const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
