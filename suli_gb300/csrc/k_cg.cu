@@ -836,19 +836,6 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_fold(const CaseDev<T> *__restri
     c.e64[q] = c.e64[q] + (double)c.e[q];
 }
 
-// e64 = prd1 sqrt(D) on the interior (start of the solve)
-template <typename T>
-__global__ void __launch_bounds__(NTHREADS) k_cg_e64_init(const CaseDev<T> *__restrict__ cs, int ncases)
-{
-    const CaseDev<T> &c = cs[find_case(cs, ncases)];
-    int i, j, k;
-    tile_ijk(c, i, j, k);
-    const Geo &g = c.g;
-    if (i > g.nx || j > g.ny || k > g.nz) return;
-    long long q = g.at(i, j, k);
-    c.e64[q] = (double)c.prd1[q] * sqrt((double)c.dpr[q]);
-}
-
 // ---- launchers ----------------------------------------------------------------
 template <typename T> void launch_cg_setup(const Batch<T> &b, cudaStream_t s)
 {

@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(NTHREADS) k_reinit_stage(const CaseDev<T> *__r
     const T *src;
     T *dst;
     stage_bufs(c, base, stage, src, dst);
-    double band = 0.0, cnt = 0.0;
+    T band = T(0), cnt = T(0);     // stage 3: the band's change and cell count
     if (in) {
         long long q = g.at(i, j, k);
         T ta, td, tb, te, tc, tf;
@@ -310,14 +310,25 @@ __global__ void __launch_bounds__(NTHREADS) k_reinit_stage(const CaseDev<T> *__r
         }
         if (stage == 3) {
             if (fabs(nv64) <= 2. * c.alpha1 * c.dx1) {
-                band = nv64 - lv64;
-                cnt = 1.0;
+                band = T(nv64 - lv64);
+                cnt = T(1);
             }
         }
     }
     if (stage != 3) return;
-    double vals[2] = {band, cnt}, tot[2];
-    if (last_block_reduce<T, 2>(c, vals, tot) && tid_lin() == 0) {
+    double tot[2];
+    bool last;
+    if constexpr (sizeof(T) == 4) {
+        // mixed form: FP32 warp sums of the band's changes (the stopping
+        // test's mean change) and counts (exact)
+        const float vals[2] = {band, cnt};
+        const double one[2] = {1.0, 1.0};
+        last = last_block_reduce_f32<T, 2>(c, vals, one, tot);
+    } else {
+        const double vals[2] = {band, cnt};
+        last = last_block_reduce<T, 2>(c, vals, tot);
+    }
+    if (last && tid_lin() == 0) {
         double il = (double)iter;
         double active;
         double replay = c.sc[S_RINREPLAY];
@@ -342,6 +353,7 @@ __global__ void __launch_bounds__(NTHREADS) k_heaviside_vol(const CaseDev<T> *__
     tile_ijk(c, i, j, k);
     const Geo &g = c.g;
     double vol = 0.0;
+    float hf = 0.f;     // mixed form: the cell's H for an FP32 warp sum
     if (i <= g.nx && j <= g.ny && k <= g.nz) {
         long long q = g.at(i, j, k);
         T l = c.ls[q];
@@ -389,11 +401,23 @@ __global__ void __launch_bounds__(NTHREADS) k_heaviside_vol(const CaseDev<T> *__
             c.hsy[q] = sy;
             c.hsz[q] = sz;
         }
-        vol = (1. - (1. - hv)) * c.dx * c.dy * (c.dzk ? c.dzk[k] : c.dz);   // SuLi-ICdz/14_level_set.f90:176,222
+        if constexpr (sizeof(T) == 4) hf = (float)hv;
+        else vol = (1. - (1. - hv)) * c.dx * c.dy * (c.dzk ? c.dzk[k] : c.dz);   // SuLi-ICdz/14_level_set.f90:176,222
     }
     if (set_ini < 0) return;     // properties only (heaviside after the level-set IBM)
-    double vals[1] = {vol}, tot[1];
-    if (last_block_reduce<T, 1>(c, vals, tot) && tid_lin() == 0) {
+    double tot[1];
+    bool last;
+    if constexpr (sizeof(T) == 4) {
+        // mixed form: H summed in FP32 along each warp (an x-row of the tile:
+        // one cell volume), times the cell volume once per warp
+        const float vals[1] = {hf};
+        const double cv[1] = {c.dx * c.dy * (c.dzk ? c.dzk[min(k, g.nz)] : c.dz)};
+        last = last_block_reduce_f32<T, 1>(c, vals, cv, tot);
+    } else {
+        const double vals[1] = {vol};
+        last = last_block_reduce<T, 1>(c, vals, tot);
+    }
+    if (last && tid_lin() == 0) {
         double vi = tot[0];
         if (set_ini) c.sc[S_VOLINI] = vi;
         c.sc[S_VOLINS] = vi;

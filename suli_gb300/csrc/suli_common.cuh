@@ -256,11 +256,15 @@ __device__ __forceinline__ double warp_sum(double v)
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     return v;
 }
+// maximum of non-negative values (+0.0, never -0.0; +inf for a NaN): their
+// bit patterns order as unsigned integers, so the maximum runs on the integer
+// units instead of GB300's FP64 pipe, exactly
 __device__ __forceinline__ double warp_max(double v)
 {
+    unsigned long long b = (unsigned long long)__double_as_longlong(v);
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
-    return v;
+    for (int o = 16; o > 0; o >>= 1) b = max(b, __shfl_down_sync(0xffffffffu, b, o));
+    return __longlong_as_double((long long)b);
 }
 
 // sum over the block in a fixed order; result valid in thread 0
@@ -291,21 +295,17 @@ __device__ __forceinline__ double block_max(double v, double *sh)
     return v;
 }
 
-// Publish NS per-tile partial values of tile `gtile` (global tile id);
-// returns true in every thread of the block that completes the case's last
-// tile, after which `tot` holds the case totals (sums for slots with maxmask
-// bit clear, maxima otherwise), reduced in tile order so results do not
-// depend on block scheduling.
+// unit_reduce: publish NS per-unit partial values of unit `gunit` (global
+// unit id); returns true in every thread of the block that completes the
+// case's last unit, after which `tot` holds the case totals (sums for slots
+// with maxmask bit clear, maxima of non-negative values otherwise), reduced
+// in unit order so results do not depend on block scheduling.
+// unit_publish is its second half, from the block's values in thread 0 (bv).
 template <typename T, int NS>
-__device__ bool unit_reduce(const CaseDev<T> &c, int gunit, int ubegin, int nunits, const double (&vals)[NS],
-                            double (&tot)[NS], unsigned maxmask = 0u)
+__device__ bool unit_publish(const CaseDev<T> &c, int gunit, int ubegin, int nunits, const double (&bv)[NS],
+                             double (&tot)[NS], unsigned maxmask, double *sh)
 {
-    __shared__ double sh[32];
     __shared__ bool amlast;
-    double bv[NS];
-#pragma unroll
-    for (int s = 0; s < NS; ++s)
-        bv[s] = ((maxmask >> s) & 1u) ? block_max(vals[s], sh) : block_sum(vals[s], sh);
     int t = tid_lin();
     if (t == 0) {
 #pragma unroll
@@ -331,6 +331,50 @@ __device__ bool unit_reduce(const CaseDev<T> &c, int gunit, int ubegin, int nuni
     if (t == 0) *c.counter = 0u;
     return true;
 }
+template <typename T, int NS>
+__device__ bool unit_reduce(const CaseDev<T> &c, int gunit, int ubegin, int nunits, const double (&vals)[NS],
+                            double (&tot)[NS], unsigned maxmask = 0u)
+{
+    __shared__ double sh[32];
+    double bv[NS];
+#pragma unroll
+    for (int s = 0; s < NS; ++s)
+        bv[s] = ((maxmask >> s) & 1u) ? block_max(vals[s], sh) : block_sum(vals[s], sh);
+    return unit_publish<T, NS>(c, gunit, ubegin, nunits, bv, tot, maxmask, sh);
+}
+
+// unit_reduce of sums of FP32 thread values (mixed form): each warp sums its
+// 32 values in FP32 in a fixed shuffle order (a relative 1e-6 at worst, on
+// quantities that feed stopping tests and diagnostics), lane 0 widens the
+// warp's sum, times wscale[s] (a per-warp factor, e.g. a cell volume that
+// is uniform along a warp's x-row), and thread 0 adds the block's warps in
+// FP64: one FP64 operation per warp instead of a five-level FP64 shuffle
+// tree per thread on GB300's FP64 pipe
+template <typename T, int NS>
+__device__ bool unit_reduce_f32(const CaseDev<T> &c, int gunit, int ubegin, int nunits, const float (&vals)[NS],
+                                const double (&wscale)[NS], double (&tot)[NS])
+{
+    __shared__ double sh[NS * (NTHREADS / 32)];
+    const int t = tid_lin();
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+        float v = vals[s];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((t & 31) == 0) sh[s * (NTHREADS / 32) + (t >> 5)] = (double)v * wscale[s];
+    }
+    __syncthreads();
+    double bv[NS];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+        double a = 0.0;
+        if (t == 0)
+            for (int w = 0; w < NTHREADS / 32; ++w) a += sh[s * (NTHREADS / 32) + w];
+        bv[s] = a;
+    }
+    __shared__ double sh2[32];
+    return unit_publish<T, NS>(c, gunit, ubegin, nunits, bv, tot, 0u, sh2);
+}
 
 // one tile per block (the launch grid is the tile grid)
 template <typename T, int NS>
@@ -338,6 +382,12 @@ __device__ __forceinline__ bool last_block_reduce(const CaseDev<T> &c, const dou
                                                   unsigned maxmask = 0u)
 {
     return unit_reduce<T, NS>(c, (int)blockIdx.x, c.tile_begin, c.ntiles, vals, tot, maxmask);
+}
+template <typename T, int NS>
+__device__ __forceinline__ bool last_block_reduce_f32(const CaseDev<T> &c, const float (&vals)[NS],
+                                                      const double (&wscale)[NS], double (&tot)[NS])
+{
+    return unit_reduce_f32<T, NS>(c, (int)blockIdx.x, c.tile_begin, c.ntiles, vals, wscale, tot);
 }
 
 
