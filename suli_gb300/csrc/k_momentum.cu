@@ -264,16 +264,17 @@ __device__ __forceinline__ void tempo_one(const CaseDev<T> &c, int tt, int it, T
 // the same update on the FP64 masters of the mixed form (u = master, u0 =
 // its stage copy; F, f0, f1 stay FP32); the FP32 copies follow the masters
 template <typename T>
-__device__ __forceinline__ void tempo_one_m(const CaseDev<T> &c, int tt, int it, double dt, long long q, T *u,
+__device__ __forceinline__ void tempo_one_m(const CaseDev<T> &c, int tt, int it, const T (&dtv)[4], long long q, T *u,
                                             double *um, const T *F, T *u0, double *u0m, T *f0, T *f1)
 {
     // the increment of the scheme from the FP32 tendencies in FP32 (dt F is
     // small against u: its FP32 rounding is far below the master's), added
     // to the FP64 master: one widening, one FP64 add and one rounding per
-    // component on GB300's FP64 pipe
+    // component on GB300's FP64 pipe; dtv = dt, dt/6, dt/2, dt/12 rounded
+    // to FP32 (formed once per block)
     const int tte = c.t_tempo;
     const T Fv = F[q];
-    const T dtf = T(dt);
+    const T dtf = dtv[0];
     double x = um[q];
     if ((tte == 0) || ((tte == 3) || ((tte == 4) && (it == 1)))) {
         x = x + (double)(dtf * Fv);
@@ -288,14 +289,14 @@ __device__ __forceinline__ void tempo_one_m(const CaseDev<T> &c, int tt, int it,
             f1[q] = Fv;
             x = u0m[q] + (double)(dtf * (T(2) * Fv - f0[q]));
         } else if (tt == 3) {
-            x = u0m[q] + (double)(T(dt / 6.) * (f0[q] + T(4) * f1[q] + Fv));
+            x = u0m[q] + (double)(dtv[1] * (f0[q] + T(4) * f1[q] + Fv));
         }
     } else if (((tte == 3) && (it != 1)) || ((tte == 4) && (it == 2))) {
-        x = x + (double)(T(dt * 0.5) * (T(3) * Fv - f0[q]));
+        x = x + (double)(dtv[2] * (T(3) * Fv - f0[q]));
         f0[q] = Fv;
         if (tte == 4) f1[q] = f0[q];
     } else if ((tte == 4) && (it >= 3)) {
-        x = x + (double)(T(dt / 12.) * (T(23) * Fv - T(16) * f0[q] + T(5) * f1[q]));
+        x = x + (double)(dtv[3] * (T(23) * Fv - T(16) * f0[q] + T(5) * f1[q]));
         f1[q] = f0[q];
         f0[q] = Fv;
     }
@@ -308,6 +309,16 @@ __global__ void __launch_bounds__(NTHREADS) k_tempo(const CaseDev<T> *__restrict
 {
     if (it < 0) it = (int)cs[0].sc[S_ITSTEP];
     const CaseDev<T> &c = cs[find_case(cs, ncases)];
+    // mixed form: the scheme's FP32 step factors, formed once per block (a
+    // per-thread FP64 divide by 6 or 12 is a long sequence on GB300's FP64 pipe)
+    __shared__ T s_dt[4];
+    if (c.u64 != nullptr) {
+        if (tid_lin() == 0) {
+            const double dt = c.sc[S_DT];
+            s_dt[0] = T(dt); s_dt[1] = T(dt / 6.); s_dt[2] = T(dt * 0.5); s_dt[3] = T(dt / 12.);
+        }
+        __syncthreads();
+    }
     int i, j, k;
     tile_ijk(c, i, j, k);
     const Geo &g = c.g;
@@ -319,10 +330,10 @@ __global__ void __launch_bounds__(NTHREADS) k_tempo(const CaseDev<T> *__restrict
         if (i <= nx && j <= ny && k <= nz + 1) c.Fw[q] = c.Fw[q] + c.pz[q];
     }
     if (c.u64 != nullptr) {
-        const double dt = c.sc[S_DT];
-        if (i <= nx + 1 && j <= ny && k <= nz) tempo_one_m<T>(c, tt, it, dt, q, c.u, c.u64, c.Fu, c.u0, c.u064, c.fu0, c.fu1);
-        if (i <= nx && j <= ny + 1 && k <= nz) tempo_one_m<T>(c, tt, it, dt, q, c.v, c.v64, c.Fv, c.v0, c.v064, c.fv0, c.fv1);
-        if (i <= nx && j <= ny && k <= nz + 1) tempo_one_m<T>(c, tt, it, dt, q, c.w, c.w64, c.Fw, c.w0, c.w064, c.fw0, c.fw1);
+        const T dtv[4] = {s_dt[0], s_dt[1], s_dt[2], s_dt[3]};
+        if (i <= nx + 1 && j <= ny && k <= nz) tempo_one_m<T>(c, tt, it, dtv, q, c.u, c.u64, c.Fu, c.u0, c.u064, c.fu0, c.fu1);
+        if (i <= nx && j <= ny + 1 && k <= nz) tempo_one_m<T>(c, tt, it, dtv, q, c.v, c.v64, c.Fv, c.v0, c.v064, c.fv0, c.fv1);
+        if (i <= nx && j <= ny && k <= nz + 1) tempo_one_m<T>(c, tt, it, dtv, q, c.w, c.w64, c.Fw, c.w0, c.w064, c.fw0, c.fw1);
         return;
     }
     T dt = T(c.sc[S_DT]);
