@@ -38,6 +38,7 @@ time (weak scaling: the per-GPU work is fixed as N grows).
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import math
 import os
@@ -222,19 +223,27 @@ def _nvtx(torch):
 def timed_steps(g, k, torch):
     """Time k steps with CUDA events on the library's stream (synchronized on
     both sides), inside an NVTX range "timed_steps" (so a profiler can keep
-    to the timed launches: ncu --nvtx --nvtx-include "timed_steps/")."""
+    to the timed launches: ncu --nvtx --nvtx-include "timed_steps/").  The
+    interpreter's cyclic garbage collector runs before, not during, the
+    timed steps (each step is a host call: a collection of the bench's
+    earlier arrays inside the region would idle the GPU)."""
     s = torch.cuda.ExternalStream(g.stream_handle())
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     g.synchronize()
-    nvtx = _nvtx(torch)
-    nvtx[0]("timed_steps")
-    e0.record(s)
-    g.step(k)
-    e1.record(s)
-    nvtx[1]()
-    g.synchronize()
-    e1.synchronize()
+    gc.collect()
+    gc.disable()
+    try:
+        nvtx = _nvtx(torch)
+        nvtx[0]("timed_steps")
+        e0.record(s)
+        g.step(k)
+        e1.record(s)
+        nvtx[1]()
+        g.synchronize()
+        e1.synchronize()
+    finally:
+        gc.enable()
     return e0.elapsed_time(e1)
 
 
@@ -553,11 +562,16 @@ def e2e_run(args, cs, torch, parts=2):
     threads = [threading.Thread(target=drive, args=(q, g, items)) for q, (g, items) in enumerate(zip(gs, lists))]
     for th in threads:
         th.start()
-    start.wait()
-    t0 = time.perf_counter()
-    for th in threads:
-        th.join()
-    dt = time.perf_counter() - t0
+    gc.collect()        # the cyclic collector runs before the timed steps, not in them
+    gc.disable()
+    try:
+        start.wait()
+        t0 = time.perf_counter()
+        for th in threads:
+            th.join()
+        dt = time.perf_counter() - t0
+    finally:
+        gc.enable()
     for g in gs:
         g.close()
     if errors:

@@ -50,6 +50,15 @@ __device__ __forceinline__ T icf(int f, int n, bool periodic, F get)
     if (f == 1) return (get(2) + get(1)) * T(0.5);
     return (get(n) + get(n - 1)) * T(0.5);
 }
+// the two cell values icf averages at face f
+template <typename T, typename F>
+__device__ __forceinline__ void icf_pair(int f, int n, bool periodic, F get, T &a, T &b)
+{
+    if (f >= 2 && f <= n) { a = get(f); b = get(f - 1); }
+    else if (periodic) { a = get(1); b = get(n); }
+    else if (f == 1) { a = get(2); b = get(1); }
+    else { a = get(n); b = get(n - 1); }
+}
 
 template <typename T>
 __global__ void __launch_bounds__(NTHREADS) k_cg_setup1(const CaseDev<T> *__restrict__ cs, int ncases)
@@ -146,6 +155,12 @@ template <typename T>
 __global__ void __launch_bounds__(NTHREADS) k_cg_op1m(const CaseDev<T> *__restrict__ cs, int ncases)
 {
     const CaseDev<T> &c = cs[find_case(cs, ncases)];
+    // the two phases' reciprocal densities, once per block by the same
+    // Newton sequence as a face's (a face between two cells of one phase
+    // has that phase's density exactly: the mean of two equal values)
+    __shared__ double s_ir[2];
+    if (tid_lin() == 0) { s_ir[0] = rcp_nr64(c.rho_f1); s_ir[1] = rcp_nr64(c.rho_f2); }
+    __syncthreads();
     int i, j, k;
     tile_ijk(c, i, j, k);
     const Geo &g = c.g;
@@ -154,16 +169,40 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_op1m(const CaseDev<T> *__restri
     const bool px = (c.ccx0 == 0);
     const double *rho = c.rho64;
     const long long q = g.at(i, j, k);
+    const long long b1 = __double_as_longlong(c.rho_f1), b2 = __double_as_longlong(c.rho_f2);
     // per face: the projection's unit factor 1 / (h rho_face), by reciprocal
-    // (no FP64 divide), kept for posdin; the operator's coefficient is it / h
-    auto face = [&](double *pf, double *sp, long long qf, double ih, double rf) {
-        if (c.t_press == 2) rf = c.rho_f1;   // the IPA's operator (9_grad.f90:111-115)
-        const double f = ih * rcp_nr64(rf);
+    // (no FP64 divide), kept for posdin; the operator's coefficient is it / h.
+    // Inside a phase (both cells' densities bit-equal to rho_f1 or rho_f2,
+    // compared as integers) the face takes the phase's reciprocal: the same
+    // bits without the face's FP64 mean and Newton steps on GB300's FP64 pipe
+    auto face = [&](double *pf, double *sp, long long qf, double ih, double ra, double rb) {
+        const long long ba = __double_as_longlong(ra), bb = __double_as_longlong(rb);
+        double ir;
+        if (c.t_press == 2) ir = s_ir[0];    // the IPA's operator (9_grad.f90:111-115): rho_f1
+        else if (ba == bb && ba == b1) ir = s_ir[0];
+        else if (ba == bb && ba == b2) ir = s_ir[1];
+        else ir = rcp_nr64((ra + rb) * 0.5);
+        const double f = ih * ir;
         pf[qf] = f;
         sp[qf] = f * ih;
     };
-    face(c.pfx64, c.spi64, q, c.idx, icf<double>(i, nx, px, [&](int m) { return AT(rho, m, j, k); }));
-    face(c.pfy64, c.spj64, q, c.idy, icf<double>(j, ny, false, [&](int m) { return AT(rho, i, m, k); }));
+    auto facex = [&](long long qf, int fi) {
+        double ra, rb;
+        icf_pair<double>(fi, nx, px, [&](int m) { return AT(rho, m, j, k); }, ra, rb);
+        face(c.pfx64, c.spi64, qf, c.idx, ra, rb);
+    };
+    auto facey = [&](long long qf, int fj) {
+        double ra, rb;
+        icf_pair<double>(fj, ny, false, [&](int m) { return AT(rho, i, m, k); }, ra, rb);
+        face(c.pfy64, c.spj64, qf, c.idy, ra, rb);
+    };
+    auto facez = [&](long long qf, int fk) {
+        double ra, rb;
+        icf_pair<double>(fk, nz, false, [&](int m) { return AT(rho, i, j, m); }, ra, rb);
+        face(c.pfz64, c.spk64, qf, c.idz, ra, rb);
+    };
+    facex(q, i);
+    facey(q, j);
     if (c.dzk) {
         // SuLi-ICdz: conductance 1 / (dz(k)^2 rho_face) (9_grad.f90:141), the
         // projection's factor 1 / (dzz(k) rho_face) (10_pos.f90:41), the face
@@ -178,11 +217,11 @@ __global__ void __launch_bounds__(NTHREADS) k_cg_op1m(const CaseDev<T> *__restri
         zface(q, k);
         if (k == nz) zface(q + g.sxy, nz + 1);
     } else {
-        face(c.pfz64, c.spk64, q, c.idz, icf<double>(k, nz, false, [&](int m) { return AT(rho, i, j, m); }));
+        facez(q, k);
     }
-    if (i == nx) face(c.pfx64, c.spi64, q + 1, c.idx, icf<double>(nx + 1, nx, px, [&](int m) { return AT(rho, m, j, k); }));
-    if (j == ny) face(c.pfy64, c.spj64, q + g.sx, c.idy, icf<double>(ny + 1, ny, false, [&](int m) { return AT(rho, i, m, k); }));
-    if (k == nz && !c.dzk) face(c.pfz64, c.spk64, q + g.sxy, c.idz, icf<double>(nz + 1, nz, false, [&](int m) { return AT(rho, i, j, m); }));
+    if (i == nx) facex(q + 1, nx + 1);
+    if (j == ny) facey(q + g.sx, ny + 1);
+    if (k == nz && !c.dzk) facez(q + g.sxy, nz + 1);
 }
 
 template <typename T>

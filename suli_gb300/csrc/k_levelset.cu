@@ -200,32 +200,12 @@ __device__ __forceinline__ void stage_bufs64(const CaseDev<T> &c, int stage, con
     else { src = c.lsc64; dst = c.ls64; }
 }
 
-// One TVD-RK3 stage on an FP64 master (mixed form): a u0 + b u_s + g dt L
-// with a + b = 1 (a = 1, 3/4, 1/3) as u_s + a (u0 - u_s), plus the stage's
-// increment g dt L formed in FP32 (small against the level set: its FP32
-// rounding is far below the master's).  Stage 1 reads u_s = u0 and needs
-// only the increment: one widening and one FP64 add.
-__device__ __forceinline__ double rk_stage64(const double *__restrict__ rk, int stage, const double *__restrict__ u0,
-                                             const double *__restrict__ us, long long q, float inc)
-{
-    const double s = us[q];
-    if (stage == 1) return s + (double)inc;
-    return fma(rk[stage - 1], u0[q] - s, s) + (double)inc;
-}
-
 // conv_weno + intt_ls (14_level_set.f90:277-334), one TVD-RK3 stage
 template <typename T>
 __global__ void __launch_bounds__(NTHREADS) k_ls_adv_stage(const CaseDev<T> *__restrict__ cs, int ncases, int stage,
                                                            const double *__restrict__ rk)
 {
     const CaseDev<T> &c = cs[find_case(cs, ncases)];
-    // mixed form: the stage's g dt in FP32, formed once per block (no
-    // per-thread FP64 product and conversion on GB300's FP64 pipe)
-    __shared__ float s_gdt;
-    if (sizeof(T) == 4 && c.ls64 != nullptr) {
-        if (tid_lin() == 0) s_gdt = (float)(rk[6 + stage - 1] * c.sc[S_DTADV]);
-        __syncthreads();
-    }
     int i, j, k;
     tile_ijk(c, i, j, k);
     const Geo &g = c.g;
@@ -247,7 +227,8 @@ __global__ void __launch_bounds__(NTHREADS) k_ls_adv_stage(const CaseDev<T> *__r
         const double *s64;
         double *d64;
         stage_bufs64(c, stage, s64, d64);
-        const double nv = rk_stage64(rk, stage, c.ls64, s64, q, s_gdt * (float)sy7);
+        const double nv = rk[stage - 1] * c.ls64[q] + rk[3 + stage - 1] * s64[q] +
+                          rk[6 + stage - 1] * c.sc[S_DTADV] * (double)sy7;
         d64[q] = nv;
         dst[q] = T(nv);
         return;
@@ -291,19 +272,7 @@ __global__ void __launch_bounds__(NTHREADS) k_reinit_stage(const CaseDev<T> *__r
                                                            int iter, const double *__restrict__ rk, int target)
 {
     const CaseDev<T> &c = cs[find_case(cs, ncases)];
-    if (c.sc[S_RINACTIVE] == 0.0) return;      // loop of this case has ended (the whole block)
-    // mixed form: the stage's g dt1 in FP32 and the band half-width, formed
-    // once per block
-    __shared__ float s_gdt;
-    __shared__ double s_band;
-    const bool m64 = sizeof(T) == 4 && target == 0 && c.ls64 != nullptr;
-    if (m64) {
-        if (tid_lin() == 0) {
-            s_gdt = (float)(rk[6 + stage - 1] * c.dt1);
-            s_band = 2. * c.alpha1 * c.dx1;
-        }
-        __syncthreads();
-    }
+    if (c.sc[S_RINACTIVE] == 0.0) return;      // loop of this case has ended
     int i, j, k;
     tile_ijk(c, i, j, k);
     const Geo &g = c.g;
@@ -322,13 +291,13 @@ __global__ void __launch_bounds__(NTHREADS) k_reinit_stage(const CaseDev<T> *__r
         T mod = godunov<T>(lv, ta, tb, tc, td, te, tf);
         T sy7 = c.funcs[q] * (T(1.) - mod);
         double nv64, lv64;
-        if (m64) {
+        if (target == 0 && c.ls64 != nullptr) {
             // mixed form: the stage combination on the FP64 masters
             const double *s64;
             double *d64;
             stage_bufs64(c, stage, s64, d64);
             lv64 = s64[q];
-            nv64 = rk_stage64(rk, stage, c.ls64, s64, q, s_gdt * (float)sy7);
+            nv64 = rk[stage - 1] * c.ls64[q] + rk[3 + stage - 1] * lv64 + rk[6 + stage - 1] * c.dt1 * (double)sy7;
             d64[q] = nv64;
             dst[q] = T(nv64);
         } else {
@@ -340,7 +309,7 @@ __global__ void __launch_bounds__(NTHREADS) k_reinit_stage(const CaseDev<T> *__r
             lv64 = (double)lv;
         }
         if (stage == 3) {
-            if (fabs(nv64) <= (m64 ? s_band : 2. * c.alpha1 * c.dx1)) {
+            if (fabs(nv64) <= 2. * c.alpha1 * c.dx1) {
                 band = T(nv64 - lv64);
                 cnt = T(1);
             }
