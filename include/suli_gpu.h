@@ -235,7 +235,12 @@ int suli_download_field(suli_handle *h, int icase, int field, void *host);
  * queued on the handle's stream and the call synchronises once, at its end
  * (the per-field calls synchronise each).  The buffers must stay valid until
  * the call returns.  For a host that moves a batch's state every step (the
- * reference keeps everything in host memory, so it has no counterpart). */
+ * reference keeps everything in host memory, so it has no counterpart).
+ * Page-locked host buffers (cudaHostAlloc, cudaHostRegister) are the fast
+ * form: the mixed form's conversion kernel then reads or writes them in
+ * place (no staging copy) and one launch covers every field of the list;
+ * pageable buffers go through a device staging buffer one field at a time.
+ * Both give the same bits. */
 int suli_upload_fields(suli_handle *h, int n, const int32_t *cases, const int32_t *fields,
                        const void *const *host);
 int suli_download_fields(suli_handle *h, int n, const int32_t *cases, const int32_t *fields, void *const *host);
