@@ -57,7 +57,7 @@ FALLBACK_HBM_GBS = 6800.0
 METRIC = "cell-steps/s, mixed vs FP64 on one GB300 at \u22641e-6 rel L2; CG HBM GB/s"
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
@@ -89,7 +89,7 @@ def parse():
                     help="skip the field-output and restart measurement")
     ap.add_argument("--accuracy-steps", type=int, default=200,
                     help="steps of the dam-break mixed-vs-FP64 accuracy run (0: skip)")
-    return ap.parse_args()
+    return ap.parse_args(argv)
 
 
 # ---------------------------------------------------------------------------
