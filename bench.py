@@ -130,7 +130,7 @@ def ensemble_share(n, rank, world, precision, lo=32, hi=96):
 
 
 def config_of(args, name, world):
-    """The config object both arms print (the driver compares them)."""
+    """The config object both arms print (the two arms' lines compare over it)."""
     return {"workload": name, "cases_per_gpu": args.ncases if args.workload == "ensemble" else 1,
             "l2": "inputs larger than L2 (working set of GBs per GPU)"}
 

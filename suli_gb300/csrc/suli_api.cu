@@ -1019,11 +1019,11 @@ struct Impl : ImplBase {
     // Tensor maps of the TMA-staged convdiff: per case u, v, w, rho, mu, xmu,
     // ymu, zmu, each its padded box (sx x (ny+3) x (nz+3) elements, x
     // unit-stride) read in boxes of 40 x 12 x 1; out-of-box elements load as
-    // zeros.  Without the driver's encoder (or with SULI_CONVDIFF=0) the
+    // zeros.  Without the CUDA driver's encoder (or with SULI_CONVDIFF=0) the
     // gather kernel runs instead.
     CUtensorMap *dtmaps = nullptr;
     int *dtilecase = nullptr;
-    // the driver's tensor-map encoder (null when the driver has none)
+    // the CUDA driver's tensor-map encoder (null when the CUDA driver has none)
     static PFN_cuTensorMapEncodeTiled_v12000 tensor_encoder()
     {
         void *fn = nullptr;
