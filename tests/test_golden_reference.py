@@ -1,0 +1,59 @@
+"""The oracle against golden vectors of the reference itself.
+
+tests/golden/*.npz hold the state of small cases after each of two full
+time steps of SuLi-IC's own Fortran routines (1_principal.f90:69-111),
+executed in this container by tests/golden/f90sub.py (a runner for the
+Fortran 90 subset the hot-path files use; there is no Fortran compiler on
+either machine) through tests/golden/make_golden.py, which also sets each
+case up the way the reference's program starts a run.  Here the oracle
+runs the same cases from the same start and must reproduce every field and
+the volume integral: on this toolchain bit for bit; the bound below is a
+few units in the last place of each field's largest value.  (The GPU path
+is held to the oracle by the GPU parity tests.)"""
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden")
+
+
+def _cases():
+    import sys
+    sys.path.insert(0, GOLDEN)
+    import make_golden
+    return make_golden, {name: (case, n) for name, case, n in make_golden.cases()}
+
+
+MG, CASES = _cases()
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_oracle_reproduces_the_reference(name):
+    import pyoracle
+    from helpers import oracle_for
+    path = os.path.join(GOLDEN, name + ".npz")
+    assert os.path.exists(path), "fixture missing: run tests/golden/make_golden.py"
+    g = np.load(path)
+    case, nsteps = CASES[name]
+    assert int(g["steps"]) == nsteps
+    pyoracle.Oracle.set_threads(1)
+    o = oracle_for(case)
+    fields = list(MG.FIELDS) + list(MG.model_fields(case.params))
+    for s in range(nsteps + 1):
+        if s:
+            o.step()
+        tag = "s%d" % s
+        for f in fields:
+            ref = g["%s_%s" % (tag, f)]
+            got = o.field(f)
+            assert got.shape == ref.shape, (tag, f, got.shape, ref.shape)
+            assert np.isfinite(ref).all(), (tag, f, "non-finite reference field")
+            scale = float(np.abs(ref).max()) or 1.0
+            err = float(np.abs(got - ref).max())
+            assert err <= 4e-16 * scale, (tag, f, err, scale)
+        if s:
+            vi = float(g["%s_vol_ins" % tag])
+            assert abs(o.scalar("VOL_INS") - vi) <= 4e-16 * abs(vi), (tag, o.scalar("VOL_INS"), vi)
+    assert abs(o.scalar("VOL_INI") - float(g["s0_vol_ini"])) <= 4e-16 * abs(float(g["s0_vol_ini"]))
