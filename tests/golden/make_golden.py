@@ -12,7 +12,7 @@ coef_tempo, then contorno(1), (2), (3).  Each step is the body of the time
 loop (1_principal.f90:69-111).  After every step the fixture keeps the
 fields and scalars the oracle is compared on.
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root:  python tests/golden/make_golden.py [case ...]
 (reads the reference's sources from REFERENCE_DIR or /root/reference).
 """
 from __future__ import annotations
@@ -30,7 +30,7 @@ sys.path.insert(0, ROOT)
 
 import f90sub  # noqa: E402
 
-REF = os.path.join(os.environ.get("REFERENCE_DIR", "/root/reference"), "SuLi-IC")
+REFROOT = os.environ.get("REFERENCE_DIR", "/root/reference")
 FILES = ["0_modules.f90", "2_iniciais.f90", "3_contorno.f90", "5_viscosidade.f90", "6_convdiff.f90",
          "7_advectivo.f90", "8_derivadas.f90", "9_grad.f90", "10_pos.f90", "11_diversos.f90",
          "14_level_set.f90", "15_ibm.f90", "13_mms.f90"]
@@ -51,6 +51,9 @@ def model_fields(p):
         f.update({"PRD0": "prd0", "PX": "px", "PY": "py", "PZ": "pz"})
     if p.t_tens == 1:
         f.update({"KURV": "kurv", "HSX": "hsx", "HSY": "hsy", "HSZ": "hsz"})
+    if p.ibm_t == 2:
+        f.update({"OBS_LSX": "obs_lsx", "OBS_LSY": "obs_lsy", "OBS_LSZ": "obs_lsz", "OBS_LSS": "obs_lss",
+                  "ID_IBMX": "id_ibmx", "ID_IBMY": "id_ibmy", "ID_IBMZ": "id_ibmz", "ID_IBM": "id_ibm"})
     return f
 
 # suli_params fields that are module variables of the reference under the same name
@@ -60,8 +63,10 @@ PARAMS = ["nx", "ny", "nz", "dx", "dy", "dz", "t_tempo", "der", "adv_type", "ibm
           "uinicial", "iturb", "omp_t", "gx", "gz"]
 
 
-def load_reference():
-    return f90sub.load([os.path.join(REF, f) for f in FILES])
+def load_reference(tree="SuLi-IC"):
+    """The hot-path files of one of the reference's programs (SuLi-IC, or
+    SuLi-ICdz with its variable z spacing), translated."""
+    return f90sub.load([os.path.join(REFROOT, tree, f) for f in FILES])
 
 
 def call(prog, name, *args):
@@ -72,18 +77,33 @@ def setup(prog, case):
     """The reference's start of a run for `case` (see the module docstring)."""
     M = prog.M
     p = case.params
+    dzvar = p.dz_t == 1
     for k in PARAMS:
+        if dzvar and k == "dz":
+            continue                # SuLi-ICdz: dz(k) comes from dz_dist
         cur = getattr(M, k)
         setattr(M, k, int(getattr(p, k)) if isinstance(cur, int) else np.float64(getattr(p, k)))
     M.numb_threads = 1
     M.dt0 = np.float64(p.dt)
     # parametros(): the derived quantities, as the reference forms them
     M.dt = M.dt0
-    M.lx, M.ly, M.lz = M.dx * M.nx, M.dy * M.ny, M.dz * M.nz
     M.nx1, M.ny1, M.nz1 = M.nx + 1, M.ny + 1, M.nz + 1
     M.ts = 10 ** 6
-    M.delta = f90sub._max(M.dx, M.dy, M.dz)
-    M.deltai = f90sub._rpow(M.dx * M.dy * M.dz, np.float64(1.0) / np.float64(3.0))
+    third = np.float64(1.0) / np.float64(3.0)
+    if dzvar:
+        # SuLi-ICdz/2_iniciais.f90:104-124
+        M.dzmin, M.dzmax, M.dz_t = np.float64(p.dzmin), np.float64(p.dzmax), 1
+        M.nxx, M.nyy, M.nzz = M.nx1 * 2, M.ny1 * 2, M.nz1 * 2
+        call(prog, "init_disc")
+        call(prog, "dz_dist")
+        M.lx, M.ly = M.dx * M.nx, M.dy * M.ny
+        M.lz = f90sub._fsum(M.dz.d[1:M.nz + 1])
+        M.delta = f90sub._max(M.dx, M.dy, M.dza)
+        M.deltai.d[...] = f90sub._rpow(M.dx * M.dy * M.dz.d, third)
+    else:
+        M.lx, M.ly, M.lz = M.dx * M.nx, M.dy * M.ny, M.dz * M.nz
+        M.delta = f90sub._max(M.dx, M.dy, M.dz)
+        M.deltai = f90sub._rpow(M.dx * M.dy * M.dz, third)
     M.tipo = 0           # no generated level set: the case's own is used
     if p.m_turb >= 2:
         # visco's characteristic length is max(prof, ampl) of the initial
@@ -111,11 +131,33 @@ def setup(prog, case):
             getattr(M, arr).d[...] = case.fields[name]
     if M.m_turb >= 2:
         call(prog, "contorno_les")
-    call(prog, "obstaculo")
-    M.bxx1.d[...] = M.uinicial
-    M.bxx0.d[...] = M.uinicial
-    M.bxy0.d[...] = 0.0
-    M.bxz0.d[...] = 0.0
+    if M.ibm_t == 2:
+        # the reference's obstacles are not cylinders: the case's obstacle
+        # level sets go in where obstaculo() samples its sub-grid, then the
+        # rest of obstaculo()'s ibm_t = 2 branch (3_contorno.f90:991-1003)
+        for name in ("OBS_LS", "OBS_LSX", "OBS_LSY", "OBS_LSZ", "OBS_LSS"):
+            getattr(M, name.lower()).d[...] = case.fields[name]
+        nx, ny, nz, nx1, ny1, nz1 = M.nx, M.ny, M.nz, M.nx1, M.ny1, M.nz1
+        call(prog, "reinic_weno", M.obs_ls, nx1, ny1, nz1)
+        call(prog, "reinic_weno", M.obs_lsx, nx1, ny, nz)
+        call(prog, "reinic_weno", M.obs_lsy, nx, ny1, nz)
+        call(prog, "reinic_weno", M.obs_lsz, nx, ny, nz1)
+        call(prog, "reinic_weno", M.obs_lss, nx, ny, nz)
+        call(prog, "ibm_posicoes", M.id_ibmx, M.obs_lsx, nx1, ny, nz)
+        call(prog, "ibm_posicoes", M.id_ibmy, M.obs_lsy, nx, ny1, nz)
+        call(prog, "ibm_posicoes", M.id_ibmz, M.obs_lsz, nx, ny, nz1)
+        call(prog, "ibm_posicoes", M.id_ibm, M.obs_lss, nx, ny, nz)
+        mod_ls = f90sub.FArr.alloc([(1, nx), (1, ny), (1, nz)], "r")
+        call(prog, "mod_ls1", M.obs_lss, mod_ls, M.norm_xx, M.norm_yy, M.norm_zz, nx, ny, nz)
+    else:
+        call(prog, "obstaculo")
+    if M.wave_t > 0:
+        call(prog, "waves_coef")
+    else:
+        M.bxx1.d[...] = M.uinicial
+        M.bxx0.d[...] = M.uinicial
+        M.bxy0.d[...] = 0.0
+        M.bxz0.d[...] = 0.0
     for a in ("tf_p", "tf_u", "tf_v", "tf_w"):
         getattr(M, a).d[...] = 0.0
     M.it = 0
@@ -123,6 +165,8 @@ def setup(prog, case):
     call(prog, "coef_tempo")
     for n in (1, 2, 3):
         call(prog, "contorno", n)
+    if M.mms_t > 0:
+        call(prog, "mms")
 
 
 def step(prog):
@@ -130,6 +174,8 @@ def step(prog):
     M = prog.M
     M.it = M.it + 1
     M.t = M.t + M.dt
+    if M.mms_t == 1 and M.it == 1:
+        call(prog, "termo_fonte1")
     call(prog, "level_set")
     call(prog, "contorno", 3)
     if M.t_press == 2 and M.mms_t == 0:
@@ -151,18 +197,82 @@ def step(prog):
             call(prog, "contorno", 1)
     if M.t_press == 2 and M.mms_t == 0:
         call(prog, "graddin")
+    if M.mms_t > 0:
+        call(prog, "mms")
+
+
+STATIC = ("OBS_LSX", "OBS_LSY", "OBS_LSZ", "OBS_LSS", "ID_IBMX", "ID_IBMY", "ID_IBMZ", "ID_IBM")
 
 
 def snapshot(prog, tag, p):
     M = prog.M
     out = {}
     for name, arr in list(FIELDS.items()) + list(model_fields(p).items()):
+        if name in STATIC and tag != "s0":
+            continue            # the obstacle does not change after the start
         a = getattr(M, arr)
         out["%s_%s" % (tag, name)] = np.array(a.d)
         out["lb_%s" % name] = np.array(a.l)
     for s in ("vol_ini", "vol_ins", "t", "dt"):
         out["%s_%s" % (tag, s)] = np.float64(getattr(M, s))
     return out
+
+
+def sphere_tank(n=20):
+    """A submerged sphere through the image-point IBM (ibm_t = 2) in a closed
+    1 m cube, water below z = 0.8 m moving at 0.1 m/s, Smagorinsky LES.  The
+    reference's own obstacles (obstaculo(), obst_t 1..3) and the product's
+    cylinder all reach a wall, where the image stencil of ibm_images
+    (15_ibm.f90:240-270) reads past its arrays (x(ii+1), id_ibm(.., kk+1)) --
+    memory the Fortran does not define; an interior sphere keeps every image
+    stencil inside them.  Obstacle level sets are sampled on obstaculo()'s
+    half-cell sub-grid (x = (ii-1) dx/2, 3_contorno.f90:829-841) at the
+    staggered points it takes them from (:905-989)."""
+    from suli_gb300 import cases as C
+    from suli_gb300._abi import default_params
+    h = 1.0 / n
+    p = default_params(nx=n, ny=n, nz=n, dx=h, dy=h, dz=h, dt=5e-4, ccx0=1, ccxf=1, ccy0=1, ccyf=1,
+                       ccz0=2, cczf=1, gz=9.80665, m_turb=1, csmag=0.1, uinicial=0.1, ibm_t=2, obst_t=4)
+    z = (np.arange(1, n + 1) - 0.5) * h
+    ls = np.empty((n, n, n), order="F")
+    ls[...] = 0.8 - z[None, None, :]
+    f = C._base_fields(p, ls)
+    xc, yc, zc, rad = 0.5, 0.5, 0.4, 0.15
+
+    def field(ni, nj, nk, fi, fj, fk):
+        i = np.arange(1, ni + 1)[:, None, None]
+        j = np.arange(1, nj + 1)[None, :, None]
+        k = np.arange(1, nk + 1)[None, None, :]
+        x = (fi(i) - 1.0) * h * 0.5
+        y = (fj(j) - 1.0) * h * 0.5
+        zz = (fk(k) - 1.0) * h * 0.5
+        out = np.empty((ni, nj, nk), order="F")
+        out[...] = rad - np.sqrt((x - xc) * (x - xc) + (y - yc) * (y - yc) + (zz - zc) * (zz - zc))
+        return out
+
+    odd, even = (lambda a: 2 * a - 1), (lambda a: 2 * a)
+    f.update({"OBS_LSX": field(n + 1, n, n, odd, even, even), "OBS_LSY": field(n, n + 1, n, even, odd, even),
+              "OBS_LSZ": field(n, n, n + 1, even, even, odd), "OBS_LSS": field(n, n, n, even, even, even),
+              "OBS_LS": field(n + 1, n + 1, n + 1, odd, odd, odd)})
+    return C.Case("sphere_ibm_les_%d" % n, p, f, steps=2, obstacle={"kind": "fields"})
+
+
+def oracle_setup(case):
+    """The oracle started as tests/helpers.oracle_for does, the obstacle
+    level sets of a "fields" obstacle taken as uploaded (reinitialised and
+    marked by the oracle's obstaculo() tail)."""
+    import pyoracle
+    if not (case.obstacle and case.obstacle.get("kind") == "fields"):
+        from helpers import oracle_for
+        return oracle_for(case)
+    o = pyoracle.Oracle(case.params)
+    for k, v in case.fields.items():
+        o.set_field(k, v)
+    o.heaviside_init()
+    o.ibm_setup()
+    for n in (1, 2, 3):
+        o.contorno(n)
+    return o
 
 
 def cases():
@@ -185,7 +295,17 @@ def cases():
     smag = C.k_channel(16, 4, 8, m_turb=2)
     smag.params.m_turb = 1
     del smag.fields["KA"]
-    return [("dam_break_12x6x6", ref_defaults(C.dam_break(12, 6, 6)), 2),
+    schemes = []
+    for tt, nm in ((0, "euler"), (1, "rk2"), (3, "ab2"), (4, "ab3")):
+        c = ref_defaults(C.dam_break(12, 6, 6))
+        c.params.t_tempo = tt
+        schemes.append(("dam_break_%s_12x6x6" % nm, c, 3))
+    return [("dam_break_12x6x6", ref_defaults(C.dam_break(12, 6, 6)), 2)] + schemes + [
+            ("sphere_ibm_les_20", ref_defaults(sphere_tank(20)), 1),
+            ("dam_break_dz_12x6x8", ref_defaults(C.dam_break_dz(12, 6, 8)), 2),
+            ("wave_flume_stokes1_16x4x8", ref_defaults(C.wave_flume(16, 4, 8, wave_t=1)), 1),
+            ("wave_flume_stokes2_16x4x8", ref_defaults(C.wave_flume(16, 4, 8, wave_t=2)), 1),
+            ("wave_flume_stokes5_16x4x8", ref_defaults(C.wave_flume(16, 4, 8, wave_t=5)), 1),
             ("wave_tank_les_16x4x8", ref_defaults(C.wave_tank(16, 4, 8, dt=5e-4)), 2),
             ("channel_smagorinsky_16x4x8", ref_defaults(smag), 2),
             ("channel_keq_les_16x4x8", ref_defaults(kles), 2),
@@ -200,8 +320,11 @@ def main():
     t0 = time.time()
     prog = load_reference()
     print("translated %d subroutines in %.1f s" % (len(prog.units), time.time() - t0), flush=True)
+    only = set(sys.argv[1:])            # optional: the case names to (re)generate
     for name, case, nsteps in cases():
-        prog = load_reference()         # fresh module state per case
+        if only and name not in only:
+            continue
+        prog = load_reference("SuLi-ICdz" if case.params.dz_t == 1 else "SuLi-IC")   # fresh state per case
         setup(prog, case)
         data = snapshot(prog, "s0", case.params)
         for s in range(1, nsteps + 1):
