@@ -5,8 +5,9 @@ __graft_entry__.build()).  Only tests/, __graft_entry__.smoke() and the
 cpu-baseline / --impl reference legs of bench.py import this module; the
 suli_gb300 package never does.
 
-Parity: unpinned against outputs of the reference itself (see
-oracle/suli_oracle.h); pinned by analytic known-answer tests.
+Parity: pinned against outputs of the reference itself (golden vectors of
+its own Fortran routines, tests/golden/; bit for bit) and by analytic
+known-answer tests (see oracle/suli_oracle.h).
 """
 from __future__ import annotations
 

@@ -7,9 +7,11 @@
  * compiled run (gcc -O3 -ffp-contract=off) reproduces the reference
  * arithmetic.  Citations are file:line into SuLi-IC/ of lacia-udesc/SuLi.
  *
- * Parity: unpinned against outputs of the reference itself (no tests or
- * golden vectors exist upstream and no Fortran compiler is available);
- * pinned by analytic known-answer tests instead (see suli_oracle.h).
+ * Parity: pinned against outputs of the reference itself -- golden vectors
+ * of SuLi-IC's (and SuLi-ICdz's) own Fortran routines, executed by the
+ * Fortran-subset runner of tests/golden/ (no Fortran compiler exists on
+ * either machine), which this file reproduces bit for bit over whole time
+ * steps -- and by analytic known-answer tests (see suli_oracle.h).
  *
  * OpenMP is used exactly where the reference uses it: the CG of 9_grad.f90
  * (parallel loops; reductions only with omp_t = 1) and the interp*_cf

@@ -7,13 +7,20 @@
  * --impl reference arm.  The product (suli_gb300, libsuli_gpu.so) never links,
  * loads or calls it.
  *
- * Parity status: the reference has no tests, golden vectors or fixtures, and
- * no Fortran compiler exists in this build environment, so the oracle cannot
- * be pinned against outputs of the reference itself ("parity unpinned"
- * against reference outputs).  It is instead pinned by analytic known-answer
- * tests derived from the published algorithms (WENO5 exactness on
- * polynomials, manufactured-solution convergence, divergence-free
- * projection, still water at rest, conservation), see tests/test_oracle_*.py.
+ * Parity status: pinned against outputs of the reference itself.  The
+ * reference ships no tests, golden vectors or fixtures, and no Fortran
+ * compiler exists in this build environment; tests/golden/f90sub.py runs the
+ * Fortran 90 subset of the reference's hot-path files by translating it to
+ * Python (IEEE binary64, the reference's evaluation order, glibc's libm), and
+ * tests/golden/make_golden.py records 18 small cases after whole time steps
+ * of the reference's own routines (dam break with all five time schemes,
+ * Smagorinsky and k-equation LES/DES, the IPA, surface tension, both
+ * sponges, the image-point IBM, Stokes I/II/V inflow with free outflow,
+ * SuLi-ICdz's variable z spacing).  tests/test_golden_reference.py holds this
+ * oracle to those fixtures: every field bit for bit.  Analytic known-answer
+ * tests (WENO5 exactness on polynomials, manufactured-solution convergence,
+ * divergence-free projection, still water at rest, conservation) add to it,
+ * see tests/test_oracle_*.py.
  *
  * Arrays use the reference's layout: column-major, i fastest, with the same
  * lower bounds as the Fortran allocations (0_modules.f90).
