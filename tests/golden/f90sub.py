@@ -785,8 +785,16 @@ class Program:
     # ---- code generation
     def build(self):
         src = ["# generated from Fortran sources", "class _M: pass", "M = _M()"]
+        self.untranslated = {}
         for name, u in list(self.units.items()) + list(self.functions.items()):
-            src.append(self._gen_unit(u))
+            try:
+                src.append(self._gen_unit(u))
+            except (SyntaxError, NameError) as e:
+                # outside the subset (character handling, formats, ...): an
+                # error if the routine is ever called
+                self.untranslated[name] = str(e)
+                pre = "F_" if u.kind == "function" else "S_"
+                src.append("def %s%s(*_a):\n    raise RuntimeError(%r)" % (pre, name, "%s: %s" % (name, e)))
         code = "\n".join(src)
         ns = dict(RUNTIME)
         exec(compile(code, "<f90sub>", "exec"), ns)
@@ -891,7 +899,7 @@ class Program:
         for b in body + stmts:
             L.append("    " + b)
         L.append("    " + ret)
-        return "\n".join(L)
+        return "\n".join(_fix_dedents(L))
 
     # statements -> python lines (with relative indentation)
     def _gen_block(self, sc, body, _depth):
@@ -1096,15 +1104,14 @@ class Program:
             if dv.dims is not None:
                 # array dummy: the caller's array, or (element actual) the
                 # storage from that element on
-                if av is None or av.dims is None or (mm and mm.group(2) is None and False):
+                if av is None or av.dims is None:
                     # an array expression: a temporary (copy-in only)
                     n = self.expr(sc, a)
                     if not n.arr:
                         raise SyntaxError("array dummy %s of %s gets %r" % (dv.name, name, a))
                     tmp = "_t%d" % q
-                    pre.append("%s = FArr(np.array(%s, order='F'), [1] * np.ndim(%s))" % (tmp, n.code, tmp + "_v"))
-                    pre[-1] = "%s_v = %s; %s = FArr(np.array(%s_v, order='F'), [1] * np.ndim(%s_v))" % (
-                        tmp, n.code, tmp, tmp, tmp)
+                    pre.append("%s_v = %s" % (tmp, n.code))
+                    pre.append("%s = FArr(np.array(%s_v, order='F'), [1] * np.ndim(%s_v))" % (tmp, tmp, tmp))
                     argcodes.append(tmp)
                     continue
                 if mm.group(2) is None:
@@ -1148,16 +1155,6 @@ def _fix_dedents(code_lines):
             out.append(ln)
     return out
 
-
-# patch the dedent marker handling into unit generation
-_orig_gen_unit = Program._gen_unit
-
-
-def _gen_unit_fixed(self, u):
-    return "\n".join(_fix_dedents(_orig_gen_unit(self, u).split("\n")))
-
-
-Program._gen_unit = _gen_unit_fixed
 
 
 def load(paths):

@@ -33,12 +33,12 @@ import f90sub  # noqa: E402
 REFROOT = os.environ.get("REFERENCE_DIR", "/root/reference")
 FILES = ["0_modules.f90", "2_iniciais.f90", "3_contorno.f90", "5_viscosidade.f90", "6_convdiff.f90",
          "7_advectivo.f90", "8_derivadas.f90", "9_grad.f90", "10_pos.f90", "11_diversos.f90",
-         "14_level_set.f90", "15_ibm.f90", "13_mms.f90"]
+         "14_level_set.f90", "15_ibm.f90", "13_mms.f90", "4_plot.f90"]
 
 # the fields kept per step: fixture name -> reference module array (plus
 # the model's own fields, model_fields())
 FIELDS = {"U": "u", "V": "v", "W": "w", "PRD1": "prd1", "LS": "ls", "HS": "hs", "RHO": "rho",
-          "LS_MU": "ls_mu", "MU": "mu", "XMU": "xmu", "YMU": "ymu", "ZMU": "zmu"}
+          "LS_MU": "ls_mu", "MU": "mu", "XMU": "xmu", "YMU": "ymu", "ZMU": "zmu", "DIV": "div"}
 # case fields a run starts from, beyond the level set and the velocity
 START = {"PRD1": "prd1", "PRD0": "prd0", "KA": "ka"}
 
@@ -199,6 +199,8 @@ def step(prog):
         call(prog, "graddin")
     if M.mms_t > 0:
         call(prog, "mms")
+    # PLOT's mass-conservation check (4_plot.f90:370-392): the divergence field
+    call(prog, "conmassa")
 
 
 STATIC = ("OBS_LSX", "OBS_LSY", "OBS_LSZ", "OBS_LSS", "ID_IBMX", "ID_IBMY", "ID_IBMZ", "ID_IBM")

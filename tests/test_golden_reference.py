@@ -43,6 +43,7 @@ def test_oracle_reproduces_the_reference(name):
     for s in range(nsteps + 1):
         if s:
             o.step()
+            o.conmassa()        # the divergence field of PLOT's CONMASSA, as the reference run after each step
         tag = "s%d" % s
         for f in fields:
             key = "%s_%s" % (tag, f)
