@@ -318,6 +318,64 @@ def cases():
             ("sponge2_16x4x8", ref_defaults(C.sponge_tank(16, 4, 8, esp_type=2)), 2)]
 
 
+# routine by routine from a seeded random state: every routine of the RK
+# stage on velocities of both signs everywhere (all upwind branches, every
+# boundary plane); (routine, args, fields compared after it)
+SEQUENCE = [("contorno", (1,), ("U", "V", "W", "PRD1")),
+            ("visco", (), ("MU", "XMU", "YMU", "ZMU")),
+            ("convdiff", (), ("FU", "FV", "FW")),
+            ("complementos", (), ("FU", "FV", "FW")),
+            ("tempo", (), ("U", "V", "W")),
+            ("contorno", (2,), ("U", "V", "W")),
+            ("posdin", (), ("U", "V", "W"))]
+ARR = {"U": "u", "V": "v", "W": "w", "PRD1": "prd1", "MU": "mu", "XMU": "xmu", "YMU": "ymu", "ZMU": "zmu",
+       "FU": "fu", "FV": "fv", "FW": "fw"}
+
+
+def random_state(case, seed):
+    """Seeded random velocities (both signs, ghosts included) and pressure in
+    the case's own array shapes."""
+    rng = np.random.default_rng(seed)
+    out = {}
+    for name in ("U", "V", "W", "PRD1"):
+        a = case.fields[name] if name in case.fields else None
+        shape = a.shape if a is not None else None
+        if shape is None:
+            from suli_gb300 import cases as C
+            shape = C._zeros(case.params, name).shape
+        scale = 0.3 if name != "PRD1" else 50.0
+        out[name] = np.asfortranarray(scale * rng.standard_normal(shape))
+    return out
+
+
+def routine_cases():
+    from suli_gb300 import cases as C
+    smag = C.k_channel(16, 4, 8, m_turb=2)
+    smag.params.m_turb = 1
+    del smag.fields["KA"]
+    return [("routines_channel_les_16x4x8", smag, 11),
+            ("routines_dam_break_12x6x6", C.dam_break(12, 6, 6), 12),
+            ("routines_wave_flume_16x4x8", C.wave_flume(16, 4, 8, wave_t=1), 13)]
+
+
+def run_routines(prog, case, seed):
+    setup(prog, case)
+    M = prog.M
+    rs = random_state(case, seed)
+    data = {"in_%s" % k: v for k, v in rs.items()}
+    for k, v in rs.items():
+        getattr(M, ARR[k]).d[...] = v
+    M.it = 1
+    M.t = M.t + M.dt
+    M.tt = 1
+    M.dt = M.a_dt.d[0]
+    for q, (name, args, fields) in enumerate(SEQUENCE):
+        call(prog, name, *args)
+        for f in fields:
+            data["r%d_%s" % (q, f)] = np.array(getattr(M, ARR[f]).d)
+    return data
+
+
 def main():
     t0 = time.time()
     prog = load_reference()
@@ -335,6 +393,14 @@ def main():
             data.update(snapshot(prog, "s%d" % s, case.params))
             print("%s step %d: %.1f s" % (name, s, time.time() - t1), flush=True)
         data["steps"] = np.int64(nsteps)
+        path = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(path, **data)
+        print("wrote", path, os.path.getsize(path), "bytes", flush=True)
+    for name, case, seed in routine_cases():
+        if only and name not in only:
+            continue
+        prog = load_reference()
+        data = run_routines(prog, case, seed)
         path = os.path.join(HERE, name + ".npz")
         np.savez_compressed(path, **data)
         print("wrote", path, os.path.getsize(path), "bytes", flush=True)

@@ -60,3 +60,34 @@ def test_oracle_reproduces_the_reference(name):
             vi = float(g["%s_vol_ins" % tag])
             assert abs(o.scalar("VOL_INS") - vi) <= 4e-16 * abs(vi), (tag, o.scalar("VOL_INS"), vi)
     assert abs(o.scalar("VOL_INI") - float(g["s0_vol_ini"])) <= 4e-16 * abs(float(g["s0_vol_ini"]))
+
+
+ROUTINES = {name: (case, seed) for name, case, seed in MG.routine_cases()}
+
+
+@pytest.mark.parametrize("name", sorted(ROUTINES))
+def test_oracle_routines_reproduce_the_reference(name):
+    """One RK stage routine by routine (contorno(1), visco, convdiff,
+    complementos, tempo, contorno(2), posdin) from a seeded random state with
+    velocities of both signs everywhere: the oracle's fields after each
+    routine against the reference's."""
+    import pyoracle
+    path = os.path.join(GOLDEN, name + ".npz")
+    assert os.path.exists(path), "fixture missing: run tests/golden/make_golden.py"
+    g = np.load(path)
+    case, _ = ROUTINES[name]
+    pyoracle.Oracle.set_threads(1)
+    o = MG.oracle_setup(case)
+    for f in ("U", "V", "W", "PRD1"):
+        o.set_field(f, g["in_%s" % f])
+    o.set_stage(1)
+    for q, (routine, args, fields) in enumerate(MG.SEQUENCE):
+        getattr(o, routine)(*args)
+        for f in fields:
+            ref = g["r%d_%s" % (q, f)]
+            got = o.field(f)
+            assert got.shape == ref.shape, (routine, f, got.shape, ref.shape)
+            assert np.isfinite(ref).all(), (routine, f)
+            scale = float(np.abs(ref).max()) or 1.0
+            err = float(np.abs(got - ref).max())
+            assert err <= 4e-16 * scale, (routine, f, err, scale)
