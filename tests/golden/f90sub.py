@@ -202,6 +202,35 @@ def _sqrt(x):
     return np.sqrt(x) if isinstance(x, np.ndarray) else np.sqrt(np.float64(x))
 
 
+def _real4(x):
+    if isinstance(x, np.ndarray):
+        return x.astype(np.float32)
+    return np.float32(x)
+
+
+# unformatted sequential files, kept in memory: unit -> list of records
+FILES = {}
+
+
+def _fopen(unit):
+    FILES[int(unit)] = []
+
+
+def _fclose(unit):
+    pass
+
+
+def _fwrite(unit, items):
+    data = b""
+    for x in items:
+        a = np.asarray(x)
+        if a.dtype.kind == "i":
+            a = a.astype(np.int32)     # default INTEGER is 4 bytes
+        data += a.ravel(order="F").tobytes()
+    n = len(data).to_bytes(4, "little", signed=True)
+    FILES.setdefault(int(unit), []).append(n + data + n)
+
+
 def _random_number(*_a):
     raise RuntimeError("random_number is outside the subset (no reference RNG stream to match)")
 
@@ -216,7 +245,8 @@ RUNTIME = {
     "_sinh": _m1(math.sinh, np.sinh), "_cosh": _m1(math.cosh, np.cosh), "_tanh": _m1(math.tanh, np.tanh),
     "_atan2": lambda a, b: np.float64(math.atan2(float(a), float(b))),
     "_floor": lambda x: int(math.floor(float(x))), "_ceiling": lambda x: int(math.ceil(float(x))),
-    "_random_number": _random_number,
+    "_random_number": _random_number, "_real4": _real4, "_fopen": _fopen, "_fclose": _fclose, "_fwrite": _fwrite,
+    "FILES": FILES,
 }
 
 PYRESERVED = {"np", "math", "M", "FArr", "FStop", "print", "exec", "eval", "range", "int", "float", "abs", "max", "min", "len", "type", "object", "sum"}
@@ -496,6 +526,10 @@ class ExprParser:
             a = self.args()
             nodes = [x[1] if x[0] == "expr" else x[2] for x in a]
             arr = any(n.arr for n in nodes)
+            if name == "real" and len(nodes) == 2:
+                if nodes[1].lit != 4:
+                    raise SyntaxError("real(x, kind) with kind %r" % nodes[1].lit)
+                return Node("_real4(%s)" % nodes[0].code, "r", arr)
             if name in ("sum", "maxval", "minval"):
                 t = nodes[0].t
                 return Node("%s(%s)" % (fn, nodes[0].code), t, False)
@@ -974,7 +1008,26 @@ class Program:
             return ["raise FStop(%r)" % s], 0
         if s == "continue":
             return ["pass"], 0
-        if re.match(r"^(write|print|open|close|read|flush|format|rewind|backspace)\b", s):
+        m = re.match(r"^write\s*\(\s*([a-z_][a-z0-9_]*|\d+)\s*\)\s*(.*)$", s)
+        if m:
+            # an unformatted record: the items' bytes, gfortran's 4-byte
+            # length markers around them (formatted writes are dropped below)
+            unit = self.expr(sc, m.group(1)).code
+            items = [self.expr(sc, x).code for x in _split_top(m.group(2))] if m.group(2).strip() else []
+            return ["_fwrite(%s, [%s])" % (unit, ", ".join(items))], 0
+        m = re.match(r"^(open|close)\s*\((.*)\)$", s)
+        if m:
+            spec = _split_top(m.group(2))
+            unit = None
+            for x in spec:
+                if x.startswith("unit"):
+                    unit = x.split("=", 1)[1].strip()
+            if unit is None and spec and "=" not in spec[0]:
+                unit = spec[0]
+            if unit is None:
+                return ["pass"], 0
+            return ["_f%s(%s)" % (m.group(1), self.expr(sc, unit).code)], 0
+        if re.match(r"^(write|print|read|flush|format|rewind|backspace)\b", s):
             return ["pass"], 0
         if s.startswith("call "):
             return self._gen_call(sc, s[5:].strip()), 0
@@ -1040,6 +1093,10 @@ class Program:
         return None, None
 
     def _gen_assign(self, sc, lhs, rhs):
+        mt = re.match(r"^([a-z_][a-z0-9_]*)", lhs)
+        vt = sc.lookup(mt.group(1)) if mt else None
+        if vt is not None and vt.t == "c":
+            return "pass"           # character data (file names): not needed
         r = self.expr(sc, rhs)
         m = re.match(r"^([a-z_][a-z0-9_]*)\s*(\((.*)\))?$", lhs)
         if not m:

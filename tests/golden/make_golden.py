@@ -376,6 +376,28 @@ def run_routines(prog, case, seed):
     return data
 
 
+# cases whose final state is also written by PRTSCR (4_plot.f90:501-620)
+PRTSCR_CASES = ("dam_break_12x6x6", "sphere_ibm_les_20", "channel_keq_les_16x4x8")
+
+
+def prtscr_records(prog):
+    """The field records PRTSCR writes for t_plot = 0 and 1 (each an
+    unformatted sequential record: length, data, length), as bytes."""
+    M = prog.M
+    out = {}
+    saved = M.t_plot
+    M.dt_frame = np.float64(0.0)        # every call writes a frame
+    for tp in (0, 1):
+        M.t_plot = tp
+        f90sub.FILES.clear()
+        call(prog, "prtscr")
+        (unit, recs), = f90sub.FILES.items()
+        assert len(recs) == 1, recs
+        out["prtscr%d" % tp] = np.frombuffer(recs[0], dtype=np.uint8).copy()
+    M.t_plot = saved
+    return out
+
+
 def main():
     t0 = time.time()
     prog = load_reference()
@@ -393,6 +415,8 @@ def main():
             data.update(snapshot(prog, "s%d" % s, case.params))
             print("%s step %d: %.1f s" % (name, s, time.time() - t1), flush=True)
         data["steps"] = np.int64(nsteps)
+        if name in PRTSCR_CASES:
+            data.update(prtscr_records(prog))
         path = os.path.join(HERE, name + ".npz")
         np.savez_compressed(path, **data)
         print("wrote", path, os.path.getsize(path), "bytes", flush=True)
