@@ -39,7 +39,7 @@ def _pair(nx, ny, nz, inviscid):
 
 
 def test_uniform_limit_matches_the_uniform_oracle():
-    pyoracle.Oracle.set_threads(4)
+    pyoracle.Oracle.set_threads(1)     # serial reductions: the same bits every run
     a, b = _pair(24, 12, 12, inviscid=True)
     for _ in range(3):
         a.step()
@@ -54,7 +54,7 @@ def test_uniform_limit_matches_the_uniform_oracle():
 
 
 def test_stretched_grid_differs_and_conserves_volume():
-    pyoracle.Oracle.set_threads(4)
+    pyoracle.Oracle.set_threads(1)     # serial reductions: the same bits every run
     c = cases.dam_break_dz(24, 12, 12)
     o = oracle_for(c)
     v0 = o.scalar("VOL_INI")
@@ -67,7 +67,7 @@ def test_uniform_limit_viscous_difference_is_the_face_quirk():
     """With viscosity the two oracles part by the undivided top / last-face
     viscous flux of SuLi-ICdz (measured 1.6e-7 in velocity after a step of
     the 24 x 12 x 12 dam break): small, but far above round-off."""
-    pyoracle.Oracle.set_threads(4)
+    pyoracle.Oracle.set_threads(1)     # serial reductions: the same bits every run
     a, b = _pair(24, 12, 12, inviscid=False)
     a.step()
     d = a.diag()
