@@ -693,8 +693,10 @@ def reference_arm(args, rank, world):
                     "d2h_bytes_per_step": 0},
             "cpu_baseline": {k: res[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "note": "the reference Fortran cannot be built (no Fortran compiler on either machine): its "
-                    "line-faithful C restatement runs instead; a step is one time step of one case of "
-                    "the workload, so ms_per_step is per case-step"}
+                    "line-faithful C restatement runs instead (bit-identical to the reference's own "
+                    "routines on the golden cases of tests/golden/), compiled -O3 with OpenMP where the "
+                    "reference has it; a step is one time step of one case of the workload, so "
+                    "ms_per_step is per case-step"}
     print(json.dumps(line))
 
 
