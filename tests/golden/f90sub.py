@@ -70,6 +70,42 @@ def _as_view(actual, bounds, offset=0):
     return FArr(flat[offset:offset + n].reshape(ext, order="F"), [b[0] for b in bounds])
 
 
+class FBounds(IndexError):
+    pass
+
+
+def _ix(arr, name, idx):
+    out = []
+    for q, i in enumerate(idx):
+        z = int(i) - arr.l[q]
+        if z < 0 or z >= arr.d.shape[q]:
+            raise FBounds("%s%r outside its bounds (lower %r, extents %r)" % (name, tuple(int(x) for x in idx),
+                                                                             arr.l, arr.d.shape))
+        out.append(z)
+    return tuple(out)
+
+
+def _ix1(arr, name, q, i):
+    z = int(i) - arr.l[q]
+    if z < 0 or z >= arr.d.shape[q]:
+        raise FBounds("%s: subscript %d = %d outside %d..%d" % (name, q + 1, int(i), arr.l[q],
+                                                                arr.l[q] + arr.d.shape[q] - 1))
+    return z
+
+
+def _sl(arr, name, q, lo, hi, st):
+    a = arr.l[q] if lo is None else int(lo)
+    b = arr.l[q] + arr.d.shape[q] - 1 if hi is None else int(hi)
+    step = 1 if st is None else int(st)
+    if (b - a) * step >= 0:             # a non-empty section: both ends inside
+        for v in (a, b):
+            if v < arr.l[q] or v > arr.l[q] + arr.d.shape[q] - 1:
+                raise FBounds("%s: section %d:%d of dimension %d outside %d..%d" % (
+                    name, a, b, q + 1, arr.l[q], arr.l[q] + arr.d.shape[q] - 1))
+    stop = b - arr.l[q] + (1 if step > 0 else -1)
+    return slice(a - arr.l[q], stop if stop >= 0 else None, step)
+
+
 def _elem_offset(arr, idx):
     off, mul = 0, 1
     for q, i in enumerate(idx):
@@ -245,7 +281,7 @@ RUNTIME = {
     "_sinh": _m1(math.sinh, np.sinh), "_cosh": _m1(math.cosh, np.cosh), "_tanh": _m1(math.tanh, np.tanh),
     "_atan2": lambda a, b: np.float64(math.atan2(float(a), float(b))),
     "_floor": lambda x: int(math.floor(float(x))), "_ceiling": lambda x: int(math.ceil(float(x))),
-    "_random_number": _random_number, "_real4": _real4, "_fopen": _fopen, "_fclose": _fclose, "_fwrite": _fwrite,
+    "_random_number": _random_number, "_ix": _ix, "_ix1": _ix1, "_sl": _sl, "FBounds": FBounds, "_real4": _real4, "_fopen": _fopen, "_fclose": _fclose, "_fwrite": _fwrite,
     "FILES": FILES,
 }
 
@@ -691,21 +727,24 @@ class Scope:
         return Node(py, v.t)
 
     def array_ref(self, name, var, subs):
+        """An element or section reference, bounds-checked: a subscript
+        outside the declared bounds reads or writes memory the Fortran does
+        not define, which no golden vector may depend on (FBounds)."""
         py = self.pyname(name)
-        idx, arr = [], False
+        if all(s[0] == "expr" for s in subs):
+            return Node("%s.d[_ix(%s, %r, (%s,))]" % (py, py, name, ", ".join(s[1].code for s in subs)), var.t)
+        idx = []
         for q, s in enumerate(subs):
             if s[0] == "expr":
-                idx.append("(%s)-%s.l[%d]" % (s[1].code, py, q))
+                idx.append("_ix1(%s, %r, %d, %s)" % (py, name, q, s[1].code))
             elif s[0] == "slice":
                 _, lo, hi, st = s
-                a = "(%s)-%s.l[%d]" % (lo.code, py, q) if lo is not None else ""
-                b = "(%s)-%s.l[%d]+1" % (hi.code, py, q) if hi is not None else ""
-                c = ":" + st.code if st is not None else ""
-                idx.append("%s:%s%s" % (a, b, c))
-                arr = True
+                idx.append("_sl(%s, %r, %d, %s, %s, %s)" % (py, name, q, lo.code if lo is not None else "None",
+                                                            hi.code if hi is not None else "None",
+                                                            st.code if st is not None else "None"))
             else:
                 raise SyntaxError("keyword subscript")
-        return Node("%s.d[%s]" % (py, ", ".join(idx)), var.t, arr)
+        return Node("%s.d[%s]" % (py, ", ".join(idx)), var.t, True)
 
 
 # ---------------------------------------------------------------------------

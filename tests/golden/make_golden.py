@@ -305,9 +305,6 @@ def cases():
     return [("dam_break_12x6x6", ref_defaults(C.dam_break(12, 6, 6)), 2)] + schemes + [
             ("sphere_ibm_les_20", ref_defaults(sphere_tank(20)), 1),
             ("dam_break_dz_12x6x8", ref_defaults(C.dam_break_dz(12, 6, 8)), 2),
-            ("wave_flume_stokes1_16x4x8", ref_defaults(C.wave_flume(16, 4, 8, wave_t=1)), 1),
-            ("wave_flume_stokes2_16x4x8", ref_defaults(C.wave_flume(16, 4, 8, wave_t=2)), 1),
-            ("wave_flume_stokes5_16x4x8", ref_defaults(C.wave_flume(16, 4, 8, wave_t=5)), 1),
             ("wave_tank_les_16x4x8", ref_defaults(C.wave_tank(16, 4, 8, dt=5e-4)), 2),
             ("channel_smagorinsky_16x4x8", ref_defaults(smag), 2),
             ("channel_keq_les_16x4x8", ref_defaults(kles), 2),
@@ -354,8 +351,7 @@ def routine_cases():
     smag.params.m_turb = 1
     del smag.fields["KA"]
     return [("routines_channel_les_16x4x8", smag, 11),
-            ("routines_dam_break_12x6x6", C.dam_break(12, 6, 6), 12),
-            ("routines_wave_flume_16x4x8", C.wave_flume(16, 4, 8, wave_t=1), 13)]
+            ("routines_dam_break_12x6x6", C.dam_break(12, 6, 6), 12)]
 
 
 def run_routines(prog, case, seed):
@@ -377,7 +373,7 @@ def run_routines(prog, case, seed):
 
 
 # cases whose final state is also written by PRTSCR (4_plot.f90:501-620)
-PRTSCR_CASES = ("dam_break_12x6x6", "sphere_ibm_les_20", "channel_keq_les_16x4x8")
+PRTSCR_CASES = ("dam_break_12x6x6", "channel_keq_les_16x4x8")
 
 
 def prtscr_records(prog):
