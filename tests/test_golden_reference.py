@@ -112,3 +112,21 @@ def test_oracle_routines_reproduce_the_reference(name):
             scale = float(np.abs(ref).max()) or 1.0
             err = float(np.abs(got - ref).max())
             assert err <= 4e-16 * scale, (routine, f, err, scale)
+
+
+def test_fixture_regenerates_from_the_reference_sources():
+    """Provenance: where the reference's sources are present (the build
+    container, not the GPU machine), the generator reproduces a committed fixture
+    exactly from them."""
+    if not os.path.isdir(os.path.join(MG.REFROOT, "SuLi-IC")):
+        pytest.skip("reference sources not present")
+    name = "dam_break_12x6x6"
+    case, nsteps = CASES[name]
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    prog = MG.load_reference()
+    MG.setup(prog, case)
+    for s in range(1, nsteps + 1):
+        MG.step(prog)
+        snap = MG.snapshot(prog, "s%d" % s, case.params)
+        for k, v in snap.items():
+            assert np.array_equal(np.asarray(v), g[k]), k
