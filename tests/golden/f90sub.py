@@ -12,8 +12,13 @@ toward zero, x**2 is x*x (GCC folds pow(x, 2.0) that way), other powers and
 the transcendental functions call the C library through Python's math
 module (glibc, as gfortran does).  Arguments pass by reference: arrays as
 views of the caller's storage (explicit-shape dummies by sequence
-association), scalars by copy-in/copy-out.  OpenMP directives are comments
-(the serial semantics); I/O statements are ignored.
+association), sections and expressions through temporaries, scalars by
+copy-in/copy-out.  OpenMP directives are comments (the serial semantics).
+Unformatted WRITEs are kept in memory as gfortran's records (FILES);
+formatted I/O and character data are dropped.  Every subscript is checked
+against its declared bounds (FBounds): an access outside them touches
+memory the Fortran does not define, so no result may rest on it.  Routines
+outside the subset become call-time errors.
 
 This is test infrastructure: it reads the reference's sources where they
 lie and is never part of the product.
