@@ -12,13 +12,14 @@
  * compiler exists in this build environment; tests/golden/f90sub.py runs the
  * Fortran 90 subset of the reference's hot-path files by translating it to
  * Python (IEEE binary64, the reference's evaluation order, glibc's libm), and
- * tests/golden/make_golden.py records 15 small cases after whole time steps
+ * tests/golden/make_golden.py records 18 small cases after whole time steps
  * of the reference's own routines (dam break with all five time schemes,
  * Smagorinsky and k-equation LES/DES, the IPA, surface tension, both
- * sponges, the image-point IBM, SuLi-ICdz's variable z spacing), two RK
- * stages routine by routine from random states, and PRTSCR's field records;
- * every subscript is bounds-checked, so no vector rests on memory the
- * Fortran leaves undefined.  tests/test_golden_reference.py holds this
+ * sponges, the image-point IBM, SuLi-ICdz's variable z spacing, Stokes
+ * I/II/V waves through the inflow), three RK stages routine by routine from
+ * random states, and PRTSCR's field records; every subscript is
+ * bounds-checked, so no vector rests on memory the Fortran leaves undefined
+ * (the inflow fill's one read below its array takes face 1, as here).  tests/test_golden_reference.py holds this
  * oracle to those fixtures: every field bit for bit.  Analytic known-answer
  * tests (WENO5 exactness on polynomials, manufactured-solution convergence,
  * divergence-free projection, still water at rest, conservation) add to it,

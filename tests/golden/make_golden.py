@@ -73,10 +73,21 @@ def call(prog, name, *args):
     return f90sub.call(prog, name, *args)
 
 
+def oob_policy(p):
+    """The one undefined read a case may carry, replaced by the oracle's
+    documented choice: with a prescribed inflow (ccx0 = 3) contorno fills the
+    plane i = 0 from ls_x(0, j, k), below the face array that starts at 1
+    (3_contorno.f90:315); face 1 is taken, as the oracle and the GPU do."""
+    f90sub.OOB_READS.clear()
+    if p.ccx0 == 3:
+        f90sub.OOB_READS["ls_x"] = lambda idx: (1,) + idx[1:] if idx[0] == 0 else idx
+
+
 def setup(prog, case):
     """The reference's start of a run for `case` (see the module docstring)."""
     M = prog.M
     p = case.params
+    oob_policy(p)
     dzvar = p.dz_t == 1
     for k in PARAMS:
         if dzvar and k == "dz":
@@ -305,6 +316,9 @@ def cases():
     return [("dam_break_12x6x6", ref_defaults(C.dam_break(12, 6, 6)), 2)] + schemes + [
             ("sphere_ibm_les_20", ref_defaults(sphere_tank(20)), 1),
             ("dam_break_dz_12x6x8", ref_defaults(C.dam_break_dz(12, 6, 8)), 2),
+            ("wave_flume_stokes1_16x4x8", ref_defaults(C.wave_flume(16, 4, 8, wave_t=1)), 1),
+            ("wave_flume_stokes2_16x4x8", ref_defaults(C.wave_flume(16, 4, 8, wave_t=2)), 1),
+            ("wave_flume_stokes5_16x4x8", ref_defaults(C.wave_flume(16, 4, 8, wave_t=5)), 1),
             ("wave_tank_les_16x4x8", ref_defaults(C.wave_tank(16, 4, 8, dt=5e-4)), 2),
             ("channel_smagorinsky_16x4x8", ref_defaults(smag), 2),
             ("channel_keq_les_16x4x8", ref_defaults(kles), 2),
@@ -351,7 +365,8 @@ def routine_cases():
     smag.params.m_turb = 1
     del smag.fields["KA"]
     return [("routines_channel_les_16x4x8", smag, 11),
-            ("routines_dam_break_12x6x6", C.dam_break(12, 6, 6), 12)]
+            ("routines_dam_break_12x6x6", C.dam_break(12, 6, 6), 12),
+            ("routines_wave_flume_16x4x8", C.wave_flume(16, 4, 8, wave_t=1), 13)]
 
 
 def run_routines(prog, case, seed):
