@@ -9,8 +9,13 @@ read from 00_suli3d.prm, with the reference's own derived quantities),
 init_variables1..7, the body of iniciais() (2_iniciais.f90:126-271) with the
 case's initial velocity and level set in place of the generated ones,
 coef_tempo, then contorno(1), (2), (3).  Each step is the body of the time
-loop (1_principal.f90:69-111).  After every step the fixture keeps the
-fields and scalars the oracle is compared on.
+loop (1_principal.f90:69-111), followed by PLOT's CONMASSA.  After every
+step the fixture keeps the fields and scalars the oracle is compared on;
+some cases add PRTSCR's field records, and three more run one RK stage
+routine by routine from a seeded random state.  Every subscript is
+bounds-checked by the runner; the one undefined read a case may carry (the
+inflow fill's ls_x(0, j, k)) is resolved as the oracle resolves it
+(oob_policy).  SuLi-ICdz cases run on SuLi-ICdz's own sources.
 
 Run from the repository root:  python tests/golden/make_golden.py [case ...]
 (reads the reference's sources from REFERENCE_DIR or /root/reference).
