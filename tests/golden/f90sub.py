@@ -981,7 +981,7 @@ class Program:
         scal = [a for a in u.args if u.vars[a].dims is None]
         ret = "return (%s)" % "".join("%s, " % a for a in scal) if u.kind == "subroutine" else "return %s" % u.name
         self._ret = ret
-        stmts = self._gen_block(sc, u.body, 0)
+        stmts = self._gen_block(sc, u.body)
         stmts = [x.replace("S_%s[" % u.name, "S_%s_saved[" % u.name) for x in stmts]
         for b in body + stmts:
             L.append("    " + b)
@@ -989,13 +989,12 @@ class Program:
         return "\n".join(_fix_dedents(L))
 
     # statements -> python lines (with relative indentation)
-    def _gen_block(self, sc, body, _depth):
+    def _gen_block(self, sc, body):
         out = []
         ind = 0
-        loopvars = []
         for no, s in body:
             try:
-                lines, dind = self._gen_stmt(sc, s, loopvars)
+                lines, dind = self._gen_stmt(sc, s)
             except Exception as e:
                 raise SyntaxError("%s:%d: %r: %s" % (sc.unit.name, no, s, e)) from e
             for ln in lines:
@@ -1007,7 +1006,7 @@ class Program:
             raise SyntaxError("%s: %d blocks left open" % (sc.unit.name, ind))
         return out
 
-    def _gen_stmt(self, sc, s, loopvars):
+    def _gen_stmt(self, sc, s):
         s = re.sub(r"^\d+\s+", "", s)           # statement label
         # block structure
         m = re.match(r"^(\w+\s*:\s*)?do\s+while\s*\((.*)\)$", s)
@@ -1026,7 +1025,6 @@ class Program:
             else:
                 rng = "range(%s, (%s) + (1 if (%s) > 0 else -1), %s)" % (a.code, b.code, st.code, st.code)
             if "." in py or "[" in py:
-                loopvars.append(py)
                 return ["for _lv in %s:" % rng, "    %s = _lv" % py], 1
             return ["for %s in %s:" % (py, rng)], 1
         if re.match(r"^end\s*do$", s):
@@ -1047,7 +1045,7 @@ class Program:
             cond, rest = self._split_logical_if(s)
             if cond is not None:
                 c = self.expr(sc, cond)
-                lines, d = self._gen_stmt(sc, rest, loopvars)
+                lines, d = self._gen_stmt(sc, rest)
                 if d != 0:
                     raise SyntaxError("block statement in a logical IF")
                 return ["if %s:" % c.code] + ["    " + x for x in lines], 0
